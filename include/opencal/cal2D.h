@@ -1,0 +1,189 @@
+/*
+ * cal2D.h -- 2D cellular automaton: model definition, substates, elementary
+ * processes, the global transition and the cell accessors.
+ *
+ * Drop-in for OpenCAL-OMP/include/cal2D.h (the C function-pointer API of
+ * OpenCAL): every function below keeps the reference's name, argument order
+ * and meaning; each cites the declaration it replaces.  The work runs on the
+ * GPU:
+ *   - substates live in device memory, SoA, one buffer per layer; the
+ *     `current`/`next` fields of the substate structs are host mirrors kept
+ *     coherent by the library (see calCommon.h);
+ *   - elementary processes are __device__ functions written with
+ *     CAL_ELEMENTARY_PROCESS_2D (cal2DDevice.cuh) in a .cu file; their host
+ *     name is what calAddElementaryProcess2D takes, exactly as in OpenCAL;
+ *   - calGet/calGetX/calSet/... work both inside device processes (one GPU
+ *     thread per cell) and in host code (init, steering, finalize).
+ *
+ * Semantics kept from the reference (OpenCAL-OMP/source/cal2D.c):
+ *   - after every elementary process the substates are updated: the active
+ *     cell list is rebuilt (row-major) and next is copied to current for
+ *     every registered substate -- on the active cells only when the list is
+ *     non-empty (cal2D.c:738-776);
+ *   - with active cells on but an empty list, processes visit every cell
+ *     (cal2D.c:723-733 tests A.cells, which is NULL when the list is empty);
+ *   - hexagonal neighbourhoods shift the neighbour index by 7 on odd
+ *     columns (or odd rows for the alternative layout).
+ * One deliberate difference: with CAL_SPACE_FLAT a neighbour outside the grid
+ * reads as 0 and adding it as an active cell is ignored (the reference reads
+ * and writes outside its buffers there, cal2D.c:866-867).
+ */
+#ifndef cal2D_h
+#define cal2D_h
+
+#include "calCommon.h"
+
+/* cal2D.h:31-37 */
+enum CALNeighborhood2D {
+    CAL_CUSTOM_NEIGHBORHOOD_2D,
+    CAL_VON_NEUMANN_NEIGHBORHOOD_2D,
+    CAL_MOORE_NEIGHBORHOOD_2D,
+    CAL_HEXAGONAL_NEIGHBORHOOD_2D,
+    CAL_HEXAGONAL_NEIGHBORHOOD_ALT_2D
+};
+
+#define CAL_HEXAGONAL_SHIFT 7 /* cal2D.h:39 */
+
+/* Limits of this implementation (checked; exceeding one records
+ * CAL_ERROR_LIMIT). */
+#define CAL_MAX_SUBSTATES 32          /* per type, double- and single-layer together */
+#define CAL_MAX_NEIGHBORS 64          /* entries of the neighbourhood table */
+#define CAL_MAX_ELEMENTARY_PROCESSES 32
+
+/* cal2D.h:44-50.  flags/cells are host mirrors refreshed by calSync2D. */
+struct CALActiveCells2D {
+    CALbyte* flags;
+    int* size_next;
+    struct CALCell2D* cells;
+    int size_current;
+    int num_threads;
+};
+
+struct CALModel2D;
+/* cal2D.h:56 */
+typedef void (*CALCallbackFunc2D)(struct CALModel2D* ca2D, int i, int j);
+
+struct CALGpuModel2D; /* library-private device state */
+
+/* cal2D.h:61-86: same public fields in the same order; `gpu` is appended. */
+struct CALModel2D {
+    int rows;
+    int columns;
+    enum CALSpaceBoundaryCondition T;
+    enum CALUnsafeState is_safe;
+    enum CALOptimization OPTIMIZATION;
+    struct CALActiveCells2D A;
+    struct CALCell2D* X;
+    int sizeof_X;
+    enum CALNeighborhood2D X_id;
+    struct CALSubstate2Db** pQb_array;
+    struct CALSubstate2Di** pQi_array;
+    struct CALSubstate2Dr** pQr_array;
+    int sizeof_pQb_array;
+    int sizeof_pQi_array;
+    int sizeof_pQr_array;
+    CALCallbackFunc2D* elementary_processes;
+    int num_of_elementary_processes;
+    struct CALGpuModel2D* gpu;
+};
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- the reference API --------------------------------------------- */
+
+struct CALModel2D* calCADef2D(int rows, int columns, enum CALNeighborhood2D CAL_NEIGHBORHOOD_2D,
+                              enum CALSpaceBoundaryCondition CAL_TOROIDALITY,
+                              enum CALOptimization CAL_OPTIMIZATION);           /* cal2D.h:104 */
+void calSetUnsafe2D(struct CALModel2D* ca2D);                                  /* cal2D.h:113 */
+void calAddActiveCell2D(struct CALModel2D* ca2D, int i, int j);                /* cal2D.h:118 */
+void calAddActiveCellX2D(struct CALModel2D* ca2D, int i, int j, int n);        /* cal2D.h:127 */
+void calRemoveActiveCell2D(struct CALModel2D* ca2D, int i, int j);             /* cal2D.h:136 */
+void calUpdateActiveCells2D(struct CALModel2D* ca2D);                          /* cal2D.h:145 */
+struct CALCell2D* calAddNeighbor2D(struct CALModel2D* ca2D, int i, int j);     /* cal2D.h:152 */
+struct CALSubstate2Db* calAddSubstate2Db(struct CALModel2D* ca2D);             /* cal2D.h:161 */
+struct CALSubstate2Di* calAddSubstate2Di(struct CALModel2D* ca2D);             /* cal2D.h:166 */
+struct CALSubstate2Dr* calAddSubstate2Dr(struct CALModel2D* ca2D);             /* cal2D.h:171 */
+struct CALSubstate2Db* calAddSingleLayerSubstate2Db(struct CALModel2D* ca2D);  /* cal2D.h:180 */
+struct CALSubstate2Di* calAddSingleLayerSubstate2Di(struct CALModel2D* ca2D);  /* cal2D.h:187 */
+struct CALSubstate2Dr* calAddSingleLayerSubstate2Dr(struct CALModel2D* ca2D);  /* cal2D.h:194 */
+/* cal2D.h:202.  `elementary_process` must be the host name of a process
+ * defined with CAL_ELEMENTARY_PROCESS_2D; a plain host function is rejected
+ * (NULL, CAL_ERROR_NOT_A_DEVICE_PROCESS) -- there is no CPU fallback. */
+CALCallbackFunc2D* calAddElementaryProcess2D(struct CALModel2D* ca2D, CALCallbackFunc2D elementary_process);
+void calInitSubstate2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, CALbyte value);     /* cal2D.h:210 */
+void calInitSubstate2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, CALint value);      /* cal2D.h:217 */
+void calInitSubstate2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, CALreal value);     /* cal2D.h:224 */
+void calInitSubstateNext2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, CALbyte value); /* cal2D.h:233 */
+void calInitSubstateNext2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, CALint value);  /* cal2D.h:240 */
+void calInitSubstateNext2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, CALreal value); /* cal2D.h:247 */
+void calUpdateSubstate2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q);                  /* cal2D.h:256 */
+void calUpdateSubstate2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q);                  /* cal2D.h:263 */
+void calUpdateSubstate2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q);                  /* cal2D.h:269 */
+void calApplyElementaryProcess2D(struct CALModel2D* ca2D, CALCallbackFunc2D elementary_process); /* cal2D.h:277 */
+void calGlobalTransitionFunction2D(struct CALModel2D* ca2D);                                   /* cal2D.h:287 */
+void calUpdate2D(struct CALModel2D* ca2D);                                                     /* cal2D.h:296 */
+void calInit2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, int i, int j, CALbyte value); /* cal2D.h:303 */
+void calInit2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, int i, int j, CALint value);  /* cal2D.h:312 */
+void calInit2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, int i, int j, CALreal value); /* cal2D.h:321 */
+CALbyte calGet2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, int i, int j);            /* cal2D.h:332 */
+CALint calGet2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, int i, int j);             /* cal2D.h:340 */
+CALreal calGet2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, int i, int j);            /* cal2D.h:348 */
+CALbyte calGetX2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, int i, int j, int n);    /* cal2D.h:358 */
+CALint calGetX2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, int i, int j, int n);     /* cal2D.h:367 */
+CALreal calGetX2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, int i, int j, int n);    /* cal2D.h:376 */
+void calSet2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, int i, int j, CALbyte value); /* cal2D.h:387 */
+void calSet2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, int i, int j, CALint value);  /* cal2D.h:396 */
+void calSet2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, int i, int j, CALreal value); /* cal2D.h:405 */
+void calSetCurrent2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, int i, int j, CALbyte value); /* cal2D.h:417 */
+void calSetCurrent2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, int i, int j, CALint value);  /* cal2D.h:427 */
+void calSetCurrent2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, int i, int j, CALreal value); /* cal2D.h:437 */
+void calFinalize2D(struct CALModel2D* ca2D);                                                   /* cal2D.h:448 */
+
+/* ---- opencal-gb300 additions --------------------------------------- */
+
+/* Bring every host mirror up to date with the device: substate layers,
+ * A.flags, A.cells, A.size_current.  Synchronises the model's stream. */
+void calSync2D(struct CALModel2D* ca2D);
+/* Declare that host code wrote the mirrors directly (Q->current[...] = ...):
+ * the next device operation uploads them. */
+void calMarkHostDirty2D(struct CALModel2D* ca2D);
+/* Wait for all device work queued on the model. */
+void calFinish2D(struct CALModel2D* ca2D);
+/* The CUDA stream (cudaStream_t) the model's work is queued on. */
+void* calGetStream2D(struct CALModel2D* ca2D);
+/* Device buffers of a substate layer (0 = current, 1 = next), for custom
+ * kernels; a kernel that writes a layer must call calMarkDeviceWritten2D. */
+void* calGetDeviceBuffer2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, int layer);
+void* calGetDeviceBuffer2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, int layer);
+void* calGetDeviceBuffer2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, int layer);
+void calMarkDeviceWritten2D(struct CALModel2D* ca2D);
+/* current <-> next as a pointer exchange (no copy).  Only valid after a
+ * kernel has written EVERY cell of next; next then holds stale data, which
+ * the library repairs before any partial write reaches it. */
+void calSwapSubstate2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q);
+void calSwapSubstate2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q);
+void calSwapSubstate2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q);
+/* Device pointers of the active-cell state: flags (rows*columns bytes), the
+ * compacted list and its length (an int in device memory). */
+void calGetDeviceActiveCells2D(struct CALModel2D* ca2D, CALbyte** flags, struct CALCell2D** cells, int** count);
+/* Number of active cells, read from the device (synchronises). */
+int calGetActiveCellCount2D(struct CALModel2D* ca2D);
+
+/* Registration of device elementary processes (used by
+ * CAL_ELEMENTARY_PROCESS_2D; not called directly). */
+struct CALDevModel2D;
+typedef int (*CALLaunchFunc2D)(const struct CALDevModel2D* m, int grid_x, int grid_y, void* stream);
+int calRegisterElementaryProcess2D(CALCallbackFunc2D host_name, CALLaunchFunc2D launch, const char* name);
+void calHostCallOfDeviceProcess2D(const char* name);
+
+#ifdef __cplusplus
+}
+#endif
+
+#if defined(__CUDACC__)
+#include "cal2DDevice.cuh"
+#endif
+
+#endif

@@ -1,0 +1,267 @@
+/*
+ * cal2DDevice.cuh -- device side of the 2D API (included by cal2D.h when the
+ * translation unit is compiled by nvcc).
+ *
+ * Writing an elementary process for the GPU:
+ *
+ *     #include <opencal/cal2D.h>
+ *     __managed__ struct { struct CALSubstate2Dr *z, *h; } Q;   // handles
+ *     __managed__ struct { CALreal eps; } P;                     // parameters
+ *
+ *     CAL_ELEMENTARY_PROCESS_2D(flows)(struct CALModel2D* ca, int i, int j)
+ *     {
+ *         if (calGet2Dr(ca, Q.h, i, j) <= P.eps) return;
+ *         ... calGetX2Dr(ca, Q.z, i, j, n) ... calSet2Dr(ca, Q.h, i, j, v);
+ *     }
+ *     ...
+ *     calAddElementaryProcess2D(model, flows);   // host, same call as OpenCAL
+ *
+ * The body is the reference's per-cell callback; it runs as one GPU thread
+ * per cell (or per active cell).  Globals it reads (substate handles,
+ * parameters) must be visible from the device: declare them __managed__.
+ *
+ * How the accessors find a substate: every model allocates the handles of
+ * one type from a single 32-byte-stride pool, so a handle's slot is
+ * (handle - pool) >> 5.  The launch descriptor (a __grid_constant__ kernel
+ * parameter, i.e. constant-cache resident) maps slots to device buffers.
+ * Nothing is looked up in memory per access besides the cell itself.
+ */
+#ifndef cal2DDevice_cuh
+#define cal2DDevice_cuh
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CAL_TYPE_B 0
+#define CAL_TYPE_I 1
+#define CAL_TYPE_R 2
+#define CAL_HANDLE_SHIFT 5 /* log2(sizeof(struct CALSubstate2Dr)) */
+#define CAL_EP_THREADS 256
+
+/* Launch descriptor of one elementary-process kernel. */
+struct CALDevModel2D {
+    struct CALModel2D model; /* public fields for user code: rows, columns, sizeof_X, X (device copy) */
+    unsigned long long pool[3]; /* host address of the handle pool of each type */
+    void* cur[3][CAL_MAX_SUBSTATES];
+    void* nxt[3][CAL_MAX_SUBSTATES];
+    unsigned int* dirty;         /* [3] bitmasks: substates whose next layer was written */
+    CALbyte* flags;              /* active-cell flags, NULL without the optimisation */
+    struct CALCell2D* cells;     /* compacted active list */
+    int* count;                  /* its length */
+    int rows, cols;
+    int toroidal;
+    int hex;      /* 0: none; 1: shift on odd columns; 2: shift on odd rows */
+    int use_list; /* iterate the active list when it is non-empty */
+    int nx;
+    int xi[CAL_MAX_NEIGHBORS];
+    int xj[CAL_MAX_NEIGHBORS];
+};
+
+#if defined(__CUDACC__)
+
+/* per-block record of which substates a process wrote (plain byte stores:
+ * every writer stores 1, so concurrent writers cannot lose an update) */
+static __shared__ unsigned char cal_written2D[3 * CAL_MAX_SUBSTATES];
+
+static __device__ __forceinline__ const struct CALDevModel2D* cal_dm2D(const struct CALModel2D* ca)
+{
+    return reinterpret_cast<const struct CALDevModel2D*>(ca);
+}
+
+static __device__ __forceinline__ int cal_slot2D(const struct CALDevModel2D* m, int t, const void* q)
+{
+    return (int)(((unsigned long long)(uintptr_t)q - m->pool[t]) >> CAL_HANDLE_SHIFT);
+}
+
+static __device__ __forceinline__ long long cal_lin2D(const struct CALDevModel2D* m, int i, int j)
+{
+    return (long long)i * m->cols + j;
+}
+
+/* neighbour n of (i, j): cal2D.c:859-870 semantics, FLAT = absent outside */
+static __device__ __forceinline__ bool cal_nbr2D(const struct CALDevModel2D* m, int i, int j, int n, int& ni, int& nj)
+{
+    if ((m->hex == 1 && (j & 1)) || (m->hex == 2 && (i & 1)))
+        n += CAL_HEXAGONAL_SHIFT;
+    ni = i + m->xi[n];
+    nj = j + m->xj[n];
+    if (m->toroidal) {
+        ni = ni < 0 ? ni + m->rows : (ni >= m->rows ? ni - m->rows : ni);
+        nj = nj < 0 ? nj + m->cols : (nj >= m->cols ? nj - m->cols : nj);
+        return true;
+    }
+    return (unsigned)ni < (unsigned)m->rows && (unsigned)nj < (unsigned)m->cols;
+}
+
+template <typename T>
+static __device__ __forceinline__ T cal_get2D(const struct CALModel2D* ca, int t, const void* q, int i, int j)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    return static_cast<const T*>(m->cur[t][cal_slot2D(m, t, q)])[cal_lin2D(m, i, j)];
+}
+
+template <typename T>
+static __device__ __forceinline__ T cal_getx2D(const struct CALModel2D* ca, int t, const void* q, int i, int j, int n)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    int a, b;
+    if (!cal_nbr2D(m, i, j, n, a, b))
+        return (T)0;
+    return static_cast<const T*>(m->cur[t][cal_slot2D(m, t, q)])[cal_lin2D(m, a, b)];
+}
+
+template <typename T>
+static __device__ __forceinline__ void cal_set2D(const struct CALModel2D* ca, int t, const void* q, int i, int j, T v)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    int s = cal_slot2D(m, t, q);
+    static_cast<T*>(m->nxt[t][s])[cal_lin2D(m, i, j)] = v;
+    cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
+}
+
+template <typename T>
+static __device__ __forceinline__ void cal_setcur2D(const struct CALModel2D* ca, int t, const void* q, int i, int j, T v)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    static_cast<T*>(m->cur[t][cal_slot2D(m, t, q)])[cal_lin2D(m, i, j)] = v;
+}
+
+template <typename T>
+static __device__ __forceinline__ void cal_init2D(const struct CALModel2D* ca, int t, const void* q, int i, int j, T v)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    int s = cal_slot2D(m, t, q);
+    long long c = cal_lin2D(m, i, j);
+    static_cast<T*>(m->cur[t][s])[c] = v;
+    if (m->nxt[t][s]) {
+        static_cast<T*>(m->nxt[t][s])[c] = v;
+        cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
+    }
+}
+
+static __device__ __forceinline__ void cal_addactive2D(const struct CALModel2D* ca, int i, int j)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    if ((unsigned)i < (unsigned)m->rows && (unsigned)j < (unsigned)m->cols)
+        m->flags[cal_lin2D(m, i, j)] = 1;
+}
+
+static __device__ __forceinline__ void cal_addactivex2D(const struct CALModel2D* ca, int i, int j, int n)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    int a, b;
+    if (cal_nbr2D(m, i, j, n, a, b))
+        m->flags[cal_lin2D(m, a, b)] = 1;
+}
+
+static __device__ __forceinline__ void cal_removeactive2D(const struct CALModel2D* ca, int i, int j)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    m->flags[cal_lin2D(m, i, j)] = 0;
+}
+
+/* One elementary process over every cell, or over the active list when the
+ * optimisation is on and the list is non-empty (cal2D.c:717-734).  The grid
+ * is sized by the host to a few waves of the GPU; both loops are grid-stride.
+ * At the end each block publishes which substates it wrote. */
+template <void (*EP)(struct CALModel2D*, int, int)>
+__global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_constant__ struct CALDevModel2D m)
+{
+    for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x)
+        cal_written2D[t] = 0;
+    __syncthreads();
+    struct CALModel2D* ca = const_cast<struct CALModel2D*>(&m.model);
+    const int listed = m.use_list ? *m.count : 0;
+    if (listed > 0) {
+        const int stride = gridDim.x * gridDim.y * blockDim.x;
+        for (int n = (blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; n < listed; n += stride) {
+            const struct CALCell2D c = m.cells[n];
+            EP(ca, c.i, c.j);
+        }
+    } else {
+        for (int i = blockIdx.y; i < m.rows; i += gridDim.y)
+            for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m.cols; j += gridDim.x * blockDim.x)
+                EP(ca, i, j);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x)
+        if (cal_written2D[t])
+            atomicOr(&m.dirty[t / CAL_MAX_SUBSTATES], 1u << (t % CAL_MAX_SUBSTATES));
+}
+
+template <void (*EP)(struct CALModel2D*, int, int)>
+static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* stream)
+{
+    cal_ep2D_kernel<EP><<<dim3(gx, gy), CAL_EP_THREADS, 0, (cudaStream_t)stream>>>(*m);
+    return (int)cudaGetLastError();
+}
+
+/* Defines the device elementary process NAME and its host-side name, which
+ * is what calAddElementaryProcess2D / calApplyElementaryProcess2D take.
+ * Usage: CAL_ELEMENTARY_PROCESS_2D(NAME)(struct CALModel2D* ca, int i, int j) { body } */
+#define CAL_ELEMENTARY_PROCESS_2D(NAME)                                                                 \
+    static __device__ __forceinline__ void NAME##_cal_device_(struct CALModel2D*, int, int);          \
+    extern "C" void NAME(struct CALModel2D* ca2D_, int i_, int j_)                                      \
+    {                                                                                                   \
+        (void)ca2D_; (void)i_; (void)j_;                                                                \
+        calHostCallOfDeviceProcess2D(#NAME);                                                            \
+    }                                                                                                   \
+    static const int NAME##_cal_registered_ =                                                           \
+        calRegisterElementaryProcess2D(NAME, cal_launch_ep2D<NAME##_cal_device_>, #NAME);               \
+    static __device__ __forceinline__ void NAME##_cal_device_
+
+#ifndef CAL_BUILDING_LIBRARY
+/* Accessors callable from both host code and device processes.  In device
+ * code they touch the cell in device memory; in host code they call the
+ * library's exported C functions of the same name. */
+#ifdef __CUDA_ARCH__
+#define CAL_HD_BODY(dev, host) return dev
+#else
+#define CAL_HD_BODY(dev, host) return host
+#endif
+
+#define CAL_HD_ACCESSORS_2D(S, T, TC)                                                                       \
+    static __host__ __device__ __forceinline__ T cal_hd_get2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* q, int i, int j) \
+    { CAL_HD_BODY((cal_get2D<T>(ca, TC, q, i, j)), (calGet2D##S(ca, q, i, j))); }                           \
+    static __host__ __device__ __forceinline__ T cal_hd_getx2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* q, int i, int j, int n) \
+    { CAL_HD_BODY((cal_getx2D<T>(ca, TC, q, i, j, n)), (calGetX2D##S(ca, q, i, j, n))); }                   \
+    static __host__ __device__ __forceinline__ void cal_hd_set2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* q, int i, int j, T v) \
+    { CAL_HD_BODY((cal_set2D<T>(ca, TC, q, i, j, v)), (calSet2D##S(ca, q, i, j, v))); }                     \
+    static __host__ __device__ __forceinline__ void cal_hd_setcur2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* q, int i, int j, T v) \
+    { CAL_HD_BODY((cal_setcur2D<T>(ca, TC, q, i, j, v)), (calSetCurrent2D##S(ca, q, i, j, v))); }           \
+    static __host__ __device__ __forceinline__ void cal_hd_init2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* q, int i, int j, T v) \
+    { CAL_HD_BODY((cal_init2D<T>(ca, TC, q, i, j, v)), (calInit2D##S(ca, q, i, j, v))); }
+
+CAL_HD_ACCESSORS_2D(b, CALbyte, CAL_TYPE_B)
+CAL_HD_ACCESSORS_2D(i, CALint, CAL_TYPE_I)
+CAL_HD_ACCESSORS_2D(r, CALreal, CAL_TYPE_R)
+
+static __host__ __device__ __forceinline__ void cal_hd_addactive2D(struct CALModel2D* ca, int i, int j)
+{ CAL_HD_BODY(cal_addactive2D(ca, i, j), calAddActiveCell2D(ca, i, j)); }
+static __host__ __device__ __forceinline__ void cal_hd_addactivex2D(struct CALModel2D* ca, int i, int j, int n)
+{ CAL_HD_BODY(cal_addactivex2D(ca, i, j, n), calAddActiveCellX2D(ca, i, j, n)); }
+static __host__ __device__ __forceinline__ void cal_hd_removeactive2D(struct CALModel2D* ca, int i, int j)
+{ CAL_HD_BODY(cal_removeactive2D(ca, i, j), calRemoveActiveCell2D(ca, i, j)); }
+
+#define calGet2Db cal_hd_get2Db
+#define calGet2Di cal_hd_get2Di
+#define calGet2Dr cal_hd_get2Dr
+#define calGetX2Db cal_hd_getx2Db
+#define calGetX2Di cal_hd_getx2Di
+#define calGetX2Dr cal_hd_getx2Dr
+#define calSet2Db cal_hd_set2Db
+#define calSet2Di cal_hd_set2Di
+#define calSet2Dr cal_hd_set2Dr
+#define calSetCurrent2Db cal_hd_setcur2Db
+#define calSetCurrent2Di cal_hd_setcur2Di
+#define calSetCurrent2Dr cal_hd_setcur2Dr
+#define calInit2Db cal_hd_init2Db
+#define calInit2Di cal_hd_init2Di
+#define calInit2Dr cal_hd_init2Dr
+#define calAddActiveCell2D cal_hd_addactive2D
+#define calAddActiveCellX2D cal_hd_addactivex2D
+#define calRemoveActiveCell2D cal_hd_removeactive2D
+#endif /* CAL_BUILDING_LIBRARY */
+
+#endif /* __CUDACC__ */
+#endif

@@ -1,0 +1,66 @@
+/*
+ * cal2DRun.h -- simulation run control for 2D models.
+ *
+ * Drop-in for OpenCAL-OMP/include/cal2DRun.h: the same CALRun2D fields and
+ * functions.  Callbacks are host functions, as in the reference; the work
+ * they queue through this library (elementary processes, substate
+ * initialisation, updates) runs asynchronously on the model's CUDA stream,
+ * so a run of N steps is N rounds of kernel launches with no host/device
+ * synchronisation unless a callback reads device data through the host
+ * accessors.
+ *
+ * Graph mode (calRunSetGraph2D): the first step is recorded as a CUDA graph
+ * and later steps replay it.  Only valid when the callbacks queue the same
+ * device work every step (e.g. SCIDDICA-T's steering); the stop condition is
+ * still evaluated on the host after every step.
+ */
+#ifndef cal2DRun_h
+#define cal2DRun_h
+
+#include "cal2D.h"
+
+struct CALGpuRun2D;
+
+/* cal2DRun.h:21-33 (+ gpu) */
+struct CALRun2D {
+    struct CALModel2D* ca2D;
+    int step;
+    int initial_step;
+    int final_step;
+    enum CALUpdateMode UPDATE_MODE;
+    void (*init)(struct CALModel2D*);
+    void (*globalTransition)(struct CALModel2D*);
+    void (*steering)(struct CALModel2D*);
+    CALbyte (*stopCondition)(struct CALModel2D*);
+    void (*finalize)(struct CALModel2D*);
+    struct CALGpuRun2D* gpu;
+};
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct CALRun2D* calRunDef2D(struct CALModel2D* ca2D, int initial_step, int final_step,
+                             enum CALUpdateMode UPDATE_MODE);                                       /* cal2DRun.h:42 */
+void calRunAddInitFunc2D(struct CALRun2D* simulation, void (*init)(struct CALModel2D*));             /* cal2DRun.h:52 */
+void calRunAddGlobalTransitionFunc2D(struct CALRun2D* simulation, void (*globalTransition)(struct CALModel2D*)); /* :59 */
+void calRunAddSteeringFunc2D(struct CALRun2D* simulation, void (*steering)(struct CALModel2D*));     /* cal2DRun.h:65 */
+void calRunAddStopConditionFunc2D(struct CALRun2D* simulation, CALbyte (*stopCondition)(struct CALModel2D*)); /* :71 */
+void calRunAddFinalizeFunc2D(struct CALRun2D* simulation, void (*finalize)(struct CALModel2D*));     /* cal2DRun.h:77 */
+void calRunInitSimulation2D(struct CALRun2D* simulation);                                            /* cal2DRun.h:83 */
+CALbyte calRunCAStep2D(struct CALRun2D* simulation);                                                 /* cal2DRun.h:90 */
+void calRunFinalizeSimulation2D(struct CALRun2D* simulation);                                        /* cal2DRun.h:95 */
+void calRun2D(struct CALRun2D* simulation);                                                          /* cal2DRun.h:101 */
+void calRunFinalize2D(struct CALRun2D* cal2DRun);                                                    /* cal2DRun.h:108 */
+
+/* ---- opencal-gb300 additions --------------------------------------- */
+/* Record the step as a CUDA graph on first use and replay it afterwards. */
+void calRunSetGraph2D(struct CALRun2D* simulation, CALbyte enable);
+/* Number of steps whose device work was replayed from the recorded graph. */
+long calRunGraphReplays2D(struct CALRun2D* simulation);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

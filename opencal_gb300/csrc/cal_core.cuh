@@ -1,0 +1,122 @@
+/*
+ * cal_core.cuh -- library-private engine shared by the 2D and 3D C APIs.
+ *
+ * One CalGrid per model holds:
+ *   - the substates: per slot two device layers (SoA, cudaMalloc, 256-byte
+ *     aligned) and two pinned host mirrors, with per-layer coherence flags;
+ *   - the active-cell state on the device: byte flags, the compacted list of
+ *     cells in the reference's order plus the same list as linear indices,
+ *     and its length (an int in device memory, never read back per step);
+ *   - the CUDA stream every operation of the model is queued on.
+ *
+ * Update semantics (OpenCAL-OMP/source/cal2D.c:758-776): rebuild the active
+ * list, then copy next -> current for every registered substate, at the
+ * active cells when the list is non-empty, else everywhere.  Without active
+ * cells a substate that no process wrote since the last update already has
+ * next == current everywhere, so its copy is skipped (device-side written
+ * bits).  With active cells every registered substate is copied, because a
+ * cell can re-enter the list with next != current.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "opencal/calCommon.h"
+
+#define CAL_MAX_SUBSTATES_CORE 32
+#define CAL_NTYPES 3
+
+namespace cal {
+
+/* ---- error recording --------------------------------------------------- */
+void set_error(CALError code, const std::string& msg);
+bool cuda_ok(cudaError_t e, const char* what);
+
+struct Layer {
+    void* dev = nullptr;   /* device buffer */
+    bool host_valid = true;
+    bool dev_valid = true;
+};
+
+struct Sub {
+    bool used = false;
+    bool single = false;     /* single-layer: no next, not registered, not updated */
+    int type = 0;            /* 0 byte, 1 int, 2 real */
+    size_t elem = 1;
+    Layer layer[2];          /* logical layers: 0 = current, 1 = next */
+    void* host[2] = {nullptr, nullptr};
+    bool next_stale = false; /* after a pointer swap next holds old data */
+    bool forced_dirty = false;
+};
+
+typedef int (*LaunchFn)(const void* desc, int gx, int gy, void* stream);
+
+struct CalGrid {
+    int dim = 2;
+    int rows = 0, cols = 0, slices = 1;
+    long long ncells = 0;
+    int toroidal = 0;
+    int active = 0; /* CAL_OPT_ACTIVE_CELLS */
+    cudaStream_t stream = nullptr;
+
+    Sub sub[CAL_NTYPES][CAL_MAX_SUBSTATES_CORE];
+    void* pool[CAL_NTYPES] = {nullptr, nullptr, nullptr}; /* host handle pools */
+    int nslot[CAL_NTYPES] = {0, 0, 0};
+
+    /* active cells (device) */
+    unsigned char* d_flags = nullptr;
+    int* d_cells = nullptr;  /* dim ints per cell, reference order */
+    int* d_lin = nullptr;    /* linear index per listed cell */
+    int* d_count = nullptr;
+    int* d_block_counts = nullptr;
+    int n_blocks = 0;
+    bool flags_host_valid = true, flags_dev_valid = true;
+    unsigned char* h_flags = nullptr; /* host mirror (pinned) */
+
+    unsigned* d_dirty = nullptr; /* [3] written-substate bits */
+    int transfers = 0;           /* host<->device coherence copies made so far */
+    int capturing = 0;
+
+    /* lifecycle */
+    bool init(int dim, int rows, int cols, int slices, int toroidal, int active);
+    void destroy();
+
+    /* substates */
+    int add_sub(int type, bool single, void** cur_mirror, void** next_mirror);
+    Sub& s(int type, int slot) { return sub[type][slot]; }
+
+    /* coherence */
+    bool to_device_all();                      /* every layer of every substate + flags */
+    bool to_host(int type, int slot, int layer);
+    bool flags_to_host();
+    void host_wrote(int type, int slot, int layer);
+    void device_wrote_all();                   /* after a user process */
+    bool repair_stale(int type, int slot);      /* next <- current after a swap */
+    bool repair_all_stale();
+
+    /* device operations */
+    bool fill(int type, int slot, int layer, const void* value, bool at_active);
+    bool copy_next_to_current(const std::vector<std::pair<int, int>>& which, bool use_dirty, bool at_active);
+    bool update_all();                         /* calUpdate: compaction + copies */
+    bool compact();                            /* calUpdateActiveCells */
+    bool clear_dirty();
+    bool swap(int type, int slot);
+    bool sync();
+    long long lin(int i, int j, int k) const
+    {
+        return dim == 2 ? (long long)i * cols + j : (long long)k * rows * cols + (long long)i * cols + j;
+    }
+    void launch_grid(int* gx, int* gy) const;
+};
+
+/* compaction of byte flags into the reference-ordered active list */
+cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int cols, int slices, int* cells, int* lin,
+                          int* count, int* block_counts, int n_blocks, cudaStream_t stream);
+int compact_blocks_needed(long long ncells);
+
+} // namespace cal

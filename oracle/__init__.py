@@ -1,0 +1,145 @@
+"""ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this package: it is the checker, never the thing
+measured or shipped.
+
+Three interchangeable back ends expose the same entry points:
+  * ``serial``  -- oracle/build/liboracle.so: the C restatement (the checker)
+  * ``omp``     -- oracle/build/liboracle_omp.so: the same code with OpenMP
+  * ``ref``     -- oracle/_ref/libref.so: the reference library itself,
+                   compiled from its own sources by oracle/ref/Makefile; exists
+                   only where the reference tree is present
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_TREE = os.environ.get("OPENCAL_REFERENCE", "/root/reference")
+
+_LIBS: dict[str, C.CDLL] = {}
+
+NB_CUSTOM, NB_VN, NB_MOORE, NB_HEX, NB_HEX_ALT = 0, 1, 2, 3, 4
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+_i32 = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_pl = C.POINTER(C.c_long)
+
+
+def build(ref: bool = False) -> None:
+    """Compile the oracle (and, when asked and available, the reference)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref and os.path.isdir(os.path.join(REF_TREE, "OpenCAL-OMP", "source")):
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={REF_TREE}"], check=True)
+
+
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libref.so"))
+
+
+def _bind(lib: C.CDLL, prefix: str) -> C.CDLL:
+    f = getattr(lib, prefix + "sciddicaT")
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                  _dp, _dp, _dp, _dp, _pl, C.c_void_p]
+    f.restype = C.c_int
+    f = getattr(lib, prefix + "life2d")
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _u8, _u8]
+    f.restype = C.c_int
+    f = getattr(lib, prefix + "nbprobe2d")
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]
+    f.restype = C.c_int
+    f = getattr(lib, prefix + "acprobe")
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                  _dp, _dp, _pl, C.c_void_p]
+    f.restype = C.c_int
+    f = getattr(lib, prefix + "life3d")
+    f.argtypes = [C.c_int] * 10 + [_u8, _u8]
+    f.restype = C.c_int
+    return lib
+
+
+def lib(kind: str = "serial") -> C.CDLL:
+    if kind not in _LIBS:
+        if kind == "ref":
+            path = os.path.join(HERE, "_ref", "libref.so")
+        else:
+            path = os.path.join(HERE, "build", "liboracle.so" if kind == "serial" else "liboracle_omp.so")
+        if not os.path.exists(path):
+            build(ref=(kind == "ref"))
+        _LIBS[kind] = _bind(C.CDLL(path), "ref_" if kind == "ref" else "orc_")
+    return _LIBS[kind]
+
+
+def _fn(kind: str, name: str):
+    return getattr(lib(kind), ("ref_" if kind == "ref" else "orc_") + name)
+
+
+def sciddicaT(z0, h0, steps, *, toroidal=False, ac=False, p_r=0.5, p_eps=0.001, kind="serial",
+              want_cells=True):
+    """Run SCIDDICA-T; returns (z, h, cells) with cells an (n, 2) int32 array of (i, j)."""
+    z0 = np.ascontiguousarray(z0, dtype=np.float64)
+    h0 = np.ascontiguousarray(h0, dtype=np.float64)
+    rows, cols = z0.shape
+    z = np.empty_like(z0)
+    h = np.empty_like(h0)
+    n = C.c_long(0)
+    cells = np.zeros((rows * cols if (ac and want_cells) else 1, 2), dtype=np.int32)
+    rc = _fn(kind, "sciddicaT")(rows, cols, int(toroidal), int(ac), int(steps), p_r, p_eps,
+                                z0, h0, z, h, C.byref(n),
+                                cells.ctypes.data if (ac and want_cells) else None)
+    if rc:
+        raise RuntimeError(f"oracle sciddicaT failed ({rc})")
+    return z, h, (cells[: n.value].copy() if (ac and want_cells) else np.zeros((0, 2), np.int32))
+
+
+def life2d(s0, steps, *, toroidal=True, as_int=False, kind="serial"):
+    s0 = np.ascontiguousarray(s0, dtype=np.uint8)
+    out = np.empty_like(s0)
+    rows, cols = s0.shape
+    if _fn(kind, "life2d")(rows, cols, int(toroidal), int(as_int), int(steps), s0, out):
+        raise RuntimeError("oracle life2d failed")
+    return out
+
+
+def nbprobe2d(v0, steps, *, nbhd=NB_HEX, toroidal=True, kind="serial"):
+    v0 = np.ascontiguousarray(v0, dtype=np.float64)
+    out = np.empty_like(v0)
+    rows, cols = v0.shape
+    if _fn(kind, "nbprobe2d")(rows, cols, int(nbhd), int(toroidal), int(steps), v0, out):
+        raise RuntimeError("oracle nbprobe2d failed")
+    return out
+
+
+def acprobe(v0, steps, *, nbhd=NB_MOORE, toroidal=True, thr=0.5, kind="serial"):
+    """2D: v0 shape (rows, cols); 3D: v0 shape (slices, rows, cols).  Returns (v, cells)."""
+    v0 = np.ascontiguousarray(v0, dtype=np.float64)
+    dim = v0.ndim
+    if dim == 2:
+        rows, cols = v0.shape
+        slices = 1
+    else:
+        slices, rows, cols = v0.shape
+    out = np.empty_like(v0)
+    n = C.c_long(0)
+    cells = np.zeros((v0.size, dim), dtype=np.int32)
+    if _fn(kind, "acprobe")(dim, rows, cols, slices, int(nbhd), int(toroidal), int(steps), thr,
+                            v0, out, C.byref(n), cells.ctypes.data):
+        raise RuntimeError("oracle acprobe failed (active-cell count mismatch)")
+    return out, cells[: n.value].copy()
+
+
+def life3d(s0, steps, *, nbhd=NB_MOORE - 0, toroidal=True, rule=(5, 7, 6, 6), kind="serial"):
+    """s0 shape (slices, rows, cols) uint8 in OpenCAL's slice-major layout."""
+    s0 = np.ascontiguousarray(s0, dtype=np.uint8)
+    slices, rows, cols = s0.shape
+    out = np.empty_like(s0)
+    # 3D neighbourhood enum: 1 = von Neumann, 2 = Moore (OpenCAL-OMP/include/cal3D.h)
+    if _fn(kind, "life3d")(rows, cols, slices, int(nbhd), int(toroidal), int(steps), *rule, s0, out):
+        raise RuntimeError("oracle life3d failed")
+    return out

@@ -1,0 +1,111 @@
+"""The oracle (CPU restatement, oracle/) pinned against the reference.
+
+* the reference's shipped SCIDDICA-T golden (610x496, toroidal, 4000 steps):
+  the oracle's %.9f text must hash to the golden file's sha256, byte for byte;
+* the shipped active-cells golden (printed with %f) and the reference's own
+  rerun of that example (tests/golden/make_golden.py);
+* fixtures generated by running the reference library itself on seeded
+  synthetic cases: every neighbourhood, both boundaries, active cells on and
+  off, 2D and 3D -- bit-exact, active lists included;
+* when the reference tree is present (not on the GPU machine), extra seeds are
+  checked against the live reference build.
+"""
+import hashlib
+import io
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def _manifest():
+    with open(os.path.join(GOLDEN, "manifest.json")) as f:
+        return json.load(f)
+
+
+def format_pct9(h):
+    """calSaveSubstate2Dr's text format (OpenCAL-OMP/source/cal2DBufferIO.c:142)."""
+    out = io.StringIO()
+    for row in h:
+        out.write("".join("%.9f  " % v for v in row))
+        out.write("\n")
+    return out.getvalue().encode()
+
+
+def bits_equal(a, b):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    return a.shape == b.shape and a.dtype == b.dtype and a.tobytes() == b.tobytes()
+
+
+@pytest.mark.slow
+def test_oracle_reproduces_shipped_plain_golden(oracle_lib):
+    g = np.load(os.path.join(GOLDEN, "sciddicaT_610x496.npz"))
+    meta = _manifest()["sciddicaT_610x496"]
+    _, h, _ = oracle_lib.sciddicaT(g["z"], g["h0"], meta["steps"], toroidal=True, ac=False,
+                                   p_r=meta["p_r"], p_eps=meta["p_eps"], kind="omp")
+    assert hashlib.sha256(format_pct9(h)).hexdigest() == meta["plain_text_sha256"]
+
+
+@pytest.mark.slow
+def test_oracle_reproduces_shipped_ac_golden(oracle_lib):
+    g = np.load(os.path.join(GOLDEN, "sciddicaT_610x496.npz"))
+    meta = _manifest()["sciddicaT_610x496"]
+    _, h, cells = oracle_lib.sciddicaT(g["z"], g["h0"], meta["steps"], toroidal=True, ac=True,
+                                       p_r=meta["p_r"], p_eps=meta["p_eps"])
+    printed = np.array([[float("%.9f" % v) for v in row] for row in h])
+    assert np.array_equal(printed, g["h_ac_ref_run"])   # the reference rerun here, %.9f
+    assert np.abs(h - g["h_ac"]).max() <= 5e-7            # the shipped %f golden
+    assert len(cells) > 0 and np.all(h[cells[:, 0], cells[:, 1]] > meta["p_eps"])
+
+
+def _cases():
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden  # noqa: E402  (the generator defines the case list and inputs)
+    return make_golden
+
+
+@pytest.mark.parametrize("idx", range(len(_manifest()["synthetic_cases"])))
+def test_oracle_matches_reference_fixtures(oracle_lib, idx):
+    mg = _cases()
+    meta = _manifest()["synthetic_cases"][idx]
+    fx = np.load(os.path.join(GOLDEN, "synthetic_cases.npz"))
+    out = mg.run_case(meta["kind"], meta["kw"], "serial")
+    for key in meta["keys"]:
+        assert bits_equal(out[key], fx[f"c{idx}_{key}"]), (meta, key)
+
+
+def test_oracle_serial_equals_openmp(oracle_lib):
+    from opencal_gb300 import workloads as W
+    z, h = W.sciddicaT_inputs(192, 160, seed=21)
+    for ac in (0, 1):
+        a = oracle_lib.sciddicaT(z, h, 40, toroidal=False, ac=ac, kind="serial")
+        b = oracle_lib.sciddicaT(z, h, 40, toroidal=False, ac=ac, kind="omp")
+        assert bits_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("OPENCAL_REFERENCE", "/root/reference"),
+                                                   "OpenCAL-OMP")), reason="reference tree absent")
+@pytest.mark.parametrize("seed", [31, 32])
+def test_oracle_vs_live_reference(oracle_lib, seed):
+    import oracle
+    from opencal_gb300 import workloads as W
+    oracle.build(ref=True)
+    z, h = W.sciddicaT_inputs(200, 176, seed=seed)
+    for tor in (0, 1):
+        for ac in (0, 1):
+            a = oracle.sciddicaT(z, h, 35, toroidal=tor, ac=ac)
+            b = oracle.sciddicaT(z, h, 35, toroidal=tor, ac=ac, kind="ref")
+            inner = a[1].copy()
+            inner[2:-2, 2:-2] = 0
+            if not tor:
+                assert not inner.any(), "flat case reached the edge band"
+            assert bits_equal(a[1], b[1]) and bits_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+    v = W.random_field((30, 26), seed=seed)
+    for nb in (1, 2, 3, 4):
+        assert bits_equal(oracle.nbprobe2d(v, 4, nbhd=nb), oracle.nbprobe2d(v, 4, nbhd=nb, kind="ref"))
