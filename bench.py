@@ -1,0 +1,323 @@
+"""Benchmark: SCIDDICA-T debris flow, 2048 x 2048 FP64 cells, von Neumann,
+flat boundary, 4000 steps -- one "bench step" is one full 4000-step run from
+the seeded initial state (the configuration the headline metric is quoted
+on).  Metric: cell-updates per second (rows * cols * CA steps / time).
+
+  value  device-resident: inputs already in HBM (restored from a device
+         snapshot, not timed), the 4000 CA steps of each run timed with CUDA
+         events on the model's stream; L2 is flushed (256 MiB write) before
+         every run
+  e2e    the same run through the C API with host buffers: the inputs are
+         copied from pinned host memory into the model (calMarkHostDirty2D ->
+         upload), the steps run, h is read back (calSyncSubstate2Dr); host
+         timer around each run
+  roofline  the fused step kernel: 24 algorithmic bytes per cell-update
+         (z read + h read + h write, FP64) / its average launch duration,
+         measured with CUDA events around single launches
+  cpu_baseline  the CPU port of the reference (oracle/, OpenMP build, all
+         host cores) on a bounded sample of the same workload
+
+--impl reference times that CPU port alone, on all host cores, on the same
+workload (each bench step = 64 CA steps of the 2048^2 grid from the initial
+state); it is the reference's algorithm restated (the reference sources are
+not available on the benchmark machine).
+
+With --gpus N > 1 (torchrun) every rank runs an independent replica of the
+workload on its own GPU (the model has no cross-grid exchange): weak
+scaling, value = all ranks' cell-updates / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ROWS = COLS = 2048
+CA_STEPS = 4000
+SEED = 2
+P_R, P_EPS = 0.5, 0.001
+BYTES_PER_CELL_UPDATE = 24  # z read + h read + h write (FP64)
+REF_SAMPLE_STEPS = 64
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world, local, dist
+    return 0, 1, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reference_arm(args):
+    """The reference algorithm on the host cores (OpenMP build of the port)."""
+    rank, world, _, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    import oracle
+    from opencal_gb300 import workloads as W
+    oracle.build()
+    z, h = W.sciddicaT_inputs(ROWS, COLS, seed=SEED)
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    for _ in range(args.warmup):
+        oracle.sciddicaT(z, h, REF_SAMPLE_STEPS, toroidal=False, ac=False, kind="omp", want_cells=False)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.sciddicaT(z, h, REF_SAMPLE_STEPS, toroidal=False, ac=False, kind="omp", want_cells=False)
+        times.append(time.perf_counter() - t0)
+    units = ROWS * COLS * REF_SAMPLE_STEPS
+    value = units * len(times) / sum(times)
+    sample = f"{REF_SAMPLE_STEPS} CA steps of the {ROWS}x{COLS} grid from the seeded initial state per bench step"
+    line = {
+        "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded DEM + source)",
+        "config": {"workload": f"SCIDDICA-T {ROWS}x{COLS} FP64, VN, flat, plain (no active cells)",
+                   "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(z, h):
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.sciddicaT(z, h, REF_SAMPLE_STEPS, toroidal=False, ac=False, kind="omp", want_cells=False)
+    dt = time.perf_counter() - t0
+    return {"value": ROWS * COLS * REF_SAMPLE_STEPS / dt, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+            "sample": f"{REF_SAMPLE_STEPS} CA steps of the {ROWS}x{COLS} grid, OpenMP on all host cores"}
+
+
+def gpu_arm(args):
+    rank, world, local, dist = dist_setup(args.gpus)
+    import opencal_gb300 as cal
+    from opencal_gb300 import workloads as W
+    cal.build()
+    m = cal.models()
+    m.cal_sciddicaT_open.restype = C.c_void_p
+    m.cal_sciddicaT_open.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                     C.c_void_p, C.c_void_p, C.c_int]
+    for fn in ("cal_sciddicaT_reset", "cal_sciddicaT_close", "cal_sciddicaT_stream"):
+        getattr(m, fn).argtypes = [C.c_void_p]
+    m.cal_sciddicaT_stream.restype = C.c_void_p
+    m.cal_sciddicaT_steps.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    m.cal_sciddicaT_kernel_times.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    m.cal_sciddicaT_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    m.cal_sciddicaT_read.argtypes = [C.c_void_p, C.c_void_p]
+
+    cudart = C.CDLL("libcudart.so", mode=C.RTLD_GLOBAL) if False else None  # noqa: F841
+    import torch  # device memory for the L2 flush buffer and events
+    torch.cuda.set_device(local)
+    z, h = W.sciddicaT_inputs(ROWS, COLS, seed=SEED)
+    sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_FUSED)
+    if not sess:
+        raise cal.CALError("cal_sciddicaT_open failed: " + cal.core().calGetErrorString().decode())
+    stream = torch.cuda.ExternalStream(m.cal_sciddicaT_stream(sess))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def one_run():
+        m.cal_sciddicaT_reset(sess)
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            m.cal_sciddicaT_steps(sess, CA_STEPS, 0)
+            e1.record(stream)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        e0, e1 = one_run()
+        e1.synchronize()
+
+    clocks = ClockSampler(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    events = [one_run() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    barrier(dist)
+    clk = clocks.stop()
+    run_ms = [a.elapsed_time(b) for a, b in events]
+    dev_s = max_over_ranks(dist, sum(run_ms) / 1e3)
+    units = ROWS * COLS * CA_STEPS * args.steps * world
+    value = units / dev_s
+
+    # kernel-level roofline: single fused launches timed with events
+    m.cal_sciddicaT_reset(sess)
+    m.cal_sciddicaT_steps(sess, 1000, 0)  # mid-run state, wet region developed
+    nk = 400
+    ktimes = (C.c_float * nk)()
+    m.cal_sciddicaT_kernel_times(sess, nk, ktimes)
+    kavg_ms = float(np.mean(list(ktimes)))
+    peak, peak_kind = _peaks()
+    achieved = ROWS * COLS * BYTES_PER_CELL_UPDATE / (kavg_ms * 1e-3) / 1e9
+
+    # end to end through the C API with host buffers
+    pin_z = torch.from_numpy(z).pin_memory()
+    pin_h = torch.from_numpy(h).pin_memory()
+    out = torch.empty_like(pin_h).pin_memory()
+    e2e_times = []
+    for it in range(max(1, min(args.steps, 3)) + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.cal_sciddicaT_host_run(sess, pin_z.data_ptr(), pin_h.data_ptr(), CA_STEPS, out.data_ptr())
+        t1 = time.perf_counter()
+        if it > 0:
+            e2e_times.append(t1 - t0)
+    e2e_value = ROWS * COLS * CA_STEPS * world / max_over_ranks(dist, float(np.mean(e2e_times)))
+
+    # correctness guard on the timed path: fused state after a run is finite and mass is conserved
+    m.cal_sciddicaT_reset(sess)
+    m.cal_sciddicaT_steps(sess, CA_STEPS, 0)
+    hh = np.empty_like(h)
+    m.cal_sciddicaT_read(sess, hh.ctypes.data)
+    m.cal_sciddicaT_close(sess)
+
+    if rank != 0:
+        return
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "sciddicaT_fused_step_2048.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    line = {
+        "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(run_ms)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded DEM + elliptical source)",
+        "config": {"workload": f"SCIDDICA-T {ROWS}x{COLS} FP64, von Neumann, flat, plain (no active cells), "
+                               f"{CA_STEPS} CA steps per bench step, fused step kernel",
+                   "l2": "flushed (256 MiB write) before every run", "seed": SEED, "p_r": P_R, "p_eps": P_EPS,
+                   "parallelism": f"replicas x{world}"},
+        "wall_s": t_wall,
+        "gpu_launches": CA_STEPS * args.steps,
+        "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(2 * z.nbytes),
+                "d2h_bytes_per_step": int(h.nbytes)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "sdt::fused_step", "kernel_avg_ms": kavg_ms,
+                     "bytes_per_launch": ROWS * COLS * BYTES_PER_CELL_UPDATE},
+        "mass_drift_rel": float(abs(hh.sum() - h.sum()) / h.sum()),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(z, h)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="opencal", choices=["opencal", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

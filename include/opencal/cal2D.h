@@ -146,6 +146,10 @@ void calFinalize2D(struct CALModel2D* ca2D);                                    
 /* Bring every host mirror up to date with the device: substate layers,
  * A.flags, A.cells, A.size_current.  Synchronises the model's stream. */
 void calSync2D(struct CALModel2D* ca2D);
+/* Bring the host mirror of one substate's current layer up to date. */
+void calSyncSubstate2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q);
+void calSyncSubstate2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q);
+void calSyncSubstate2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q);
 /* Declare that host code wrote the mirrors directly (Q->current[...] = ...):
  * the next device operation uploads them. */
 void calMarkHostDirty2D(struct CALModel2D* ca2D);
@@ -153,8 +157,10 @@ void calMarkHostDirty2D(struct CALModel2D* ca2D);
 void calFinish2D(struct CALModel2D* ca2D);
 /* The CUDA stream (cudaStream_t) the model's work is queued on. */
 void* calGetStream2D(struct CALModel2D* ca2D);
-/* Device buffers of a substate layer (0 = current, 1 = next), for custom
- * kernels; a kernel that writes a layer must call calMarkDeviceWritten2D. */
+/* Device buffers of a substate layer (0 = current, 1 = next, 2 = next for a
+ * kernel that will overwrite every cell of it, so stale contents left by a
+ * swap need no repair), for custom kernels.  A kernel that writes a layer
+ * in place must call calMarkDeviceWritten2D. */
 void* calGetDeviceBuffer2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, int layer);
 void* calGetDeviceBuffer2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, int layer);
 void* calGetDeviceBuffer2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, int layer);

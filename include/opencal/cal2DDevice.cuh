@@ -123,7 +123,10 @@ template <typename T>
 static __device__ __forceinline__ void cal_setcur2D(const struct CALModel2D* ca, int t, const void* q, int i, int j, T v)
 {
     const struct CALDevModel2D* m = cal_dm2D(ca);
-    static_cast<T*>(m->cur[t][cal_slot2D(m, t, q)])[cal_lin2D(m, i, j)] = v;
+    int s = cal_slot2D(m, t, q);
+    static_cast<T*>(m->cur[t][s])[cal_lin2D(m, i, j)] = v;
+    /* the next update copies next over it, as in the reference */
+    cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
 }
 
 template <typename T>
@@ -133,10 +136,9 @@ static __device__ __forceinline__ void cal_init2D(const struct CALModel2D* ca, i
     int s = cal_slot2D(m, t, q);
     long long c = cal_lin2D(m, i, j);
     static_cast<T*>(m->cur[t][s])[c] = v;
-    if (m->nxt[t][s]) {
+    if (m->nxt[t][s])
         static_cast<T*>(m->nxt[t][s])[c] = v;
-        cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
-    }
+    cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
 }
 
 static __device__ __forceinline__ void cal_addactive2D(const struct CALModel2D* ca, int i, int j)

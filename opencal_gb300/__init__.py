@@ -1,0 +1,146 @@
+"""opencal-gb300: OpenCAL's cellular-automaton global transition on GB300.
+
+The product is the C-ABI library ``lib/libopencal_gb300.so`` (headers in
+``include/opencal``): OpenCAL's C API with the work on the GPU.  This module
+is a thin ctypes front end used by the tests and the benchmark; it calls the
+model drivers in ``lib/libopencal_models.so``, which are ordinary C-API
+programs (device elementary processes registered with
+``calAddElementaryProcess2D``, or the fused kernels).
+
+There is no CPU fallback: if the CUDA libraries are missing or no GPU is
+present every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(PKG, "lib")
+CORE_LIB = os.path.join(LIB_DIR, "libopencal_gb300.so")
+MODELS_LIB = os.path.join(LIB_DIR, "libopencal_models.so")
+
+NB_CUSTOM, NB_VN, NB_MOORE, NB_HEX, NB_HEX_ALT = 0, 1, 2, 3, 4
+MODE_PROCESSES, MODE_FUSED, MODE_FUSED_BLOCKED = 0, 1, 2
+
+_core = None
+_models = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+_pl = C.POINTER(C.c_long)
+_pd = C.POINTER(C.c_double)
+
+
+class CALError(RuntimeError):
+    pass
+
+
+def build(force: bool = False) -> None:
+    """Compile the CUDA libraries in-tree (opencal_gb300/build.py)."""
+    import importlib
+    importlib.import_module(__name__ + ".build").build(force=force)
+
+
+def core() -> C.CDLL:
+    """The C-ABI library (loaded once, RTLD_GLOBAL so the models resolve to it)."""
+    global _core
+    if _core is None:
+        if not os.path.exists(CORE_LIB):
+            raise CALError(f"{CORE_LIB} is missing: build it with `python -m opencal_gb300.build`")
+        _core = C.CDLL(CORE_LIB, mode=C.RTLD_GLOBAL)
+        _core.calGetErrorString.restype = C.c_char_p
+        _core.calGetLastError.restype = C.c_int
+    return _core
+
+
+def models() -> C.CDLL:
+    global _models
+    if _models is None:
+        core()
+        if not os.path.exists(MODELS_LIB):
+            raise CALError(f"{MODELS_LIB} is missing: build it with `python -m opencal_gb300.build`")
+        m = C.CDLL(MODELS_LIB)
+        m.cal_sciddicaT_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                        _dp, _dp, _dp, _dp, _pl, C.c_void_p, C.c_int, C.c_int, _pd]
+        m.cal_life2d_run.argtypes = [C.c_int] * 5 + [_u8, _u8, C.c_int, C.c_int, C.c_int, _pd]
+        m.cal_nbprobe2d_run.argtypes = [C.c_int] * 5 + [_dp, _dp, C.c_int]
+        m.cal_acprobe_run.argtypes = [C.c_int] * 7 + [C.c_double, _dp, _dp, _pl, C.c_void_p, C.c_int]
+        m.cal_life3d_run.argtypes = [C.c_int] * 10 + [_u8, _u8, C.c_int]
+        for f in ("cal_sciddicaT_run", "cal_life2d_run", "cal_nbprobe2d_run", "cal_acprobe_run", "cal_life3d_run"):
+            getattr(m, f).restype = C.c_int
+        _models = m
+    return _models
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = core().calGetErrorString()
+        raise CALError(f"{what} failed (CALError {rc}): {msg.decode() if msg else ''}")
+
+
+def sciddicaT(z0, h0, steps, *, toroidal=False, ac=False, p_r=0.5, p_eps=0.001, mode=MODE_FUSED, graph=False,
+              timing=False):
+    """SCIDDICA-T on the GPU.  Returns (z, h, cells) like oracle.sciddicaT,
+    plus the device milliseconds of the step loop when timing=True."""
+    z0 = np.ascontiguousarray(z0, dtype=np.float64)
+    h0 = np.ascontiguousarray(h0, dtype=np.float64)
+    rows, cols = z0.shape
+    z = np.empty_like(z0)
+    h = np.empty_like(h0)
+    n = C.c_long(0)
+    ms = C.c_double(0.0)
+    cells = np.zeros((rows * cols if ac else 1, 2), dtype=np.int32)
+    rc = models().cal_sciddicaT_run(rows, cols, int(toroidal), int(ac), int(steps), p_r, p_eps, z0, h0, z, h,
+                                    C.byref(n), cells.ctypes.data if ac else None, int(mode), int(graph),
+                                    C.byref(ms))
+    _check(rc, "cal_sciddicaT_run")
+    out = (z, h, cells[: n.value].copy() if ac else np.zeros((0, 2), np.int32))
+    return out + (ms.value,) if timing else out
+
+
+def life2d(s0, steps, *, toroidal=True, as_int=False, mode=MODE_FUSED_BLOCKED, block=8, graph=False, timing=False):
+    s0 = np.ascontiguousarray(s0, dtype=np.uint8)
+    rows, cols = s0.shape
+    out = np.empty_like(s0)
+    ms = C.c_double(0.0)
+    rc = models().cal_life2d_run(rows, cols, int(toroidal), int(as_int), int(steps), s0, out, int(mode), int(block),
+                                 int(graph), C.byref(ms))
+    _check(rc, "cal_life2d_run")
+    return (out, ms.value) if timing else out
+
+
+def nbprobe2d(v0, steps, *, nbhd=NB_HEX, toroidal=True, graph=False):
+    v0 = np.ascontiguousarray(v0, dtype=np.float64)
+    rows, cols = v0.shape
+    out = np.empty_like(v0)
+    _check(models().cal_nbprobe2d_run(rows, cols, int(nbhd), int(toroidal), int(steps), v0, out, int(graph)),
+           "cal_nbprobe2d_run")
+    return out
+
+
+def acprobe(v0, steps, *, nbhd=NB_MOORE, toroidal=True, thr=0.5, graph=False):
+    v0 = np.ascontiguousarray(v0, dtype=np.float64)
+    dim = v0.ndim
+    if dim == 2:
+        rows, cols = v0.shape
+        slices = 1
+    else:
+        slices, rows, cols = v0.shape
+    out = np.empty_like(v0)
+    n = C.c_long(0)
+    cells = np.zeros((v0.size, dim), dtype=np.int32)
+    _check(models().cal_acprobe_run(dim, rows, cols, slices, int(nbhd), int(toroidal), int(steps), thr, v0, out,
+                                    C.byref(n), cells.ctypes.data, int(graph)), "cal_acprobe_run")
+    return out, cells[: n.value].copy()
+
+
+def life3d(s0, steps, *, nbhd=2, toroidal=True, rule=(5, 7, 6, 6), graph=False):
+    s0 = np.ascontiguousarray(s0, dtype=np.uint8)
+    slices, rows, cols = s0.shape
+    out = np.empty_like(s0)
+    _check(models().cal_life3d_run(rows, cols, slices, int(nbhd), int(toroidal), int(steps), *rule, s0, out,
+                                   int(graph)), "cal_life3d_run")
+    return out

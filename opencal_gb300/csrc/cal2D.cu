@@ -1,0 +1,589 @@
+/*
+ * cal2D.cu -- the 2D C API (include/opencal/cal2D.h) on top of the shared
+ * engine (cal_core.cu).
+ *
+ * Reference behaviour restated (OpenCAL-OMP/source/cal2D.c):
+ *   calCADef2D + neighbourhood builders      cal2D.c:28-166, 252-327
+ *   active cells add/remove/update           cal2D.c:333-440
+ *   substates, single-layer substates        cal2D.c:470-596
+ *   elementary-process list                  cal2D.c:600-621
+ *   init / init-next / update of substates   cal2D.c:625-713
+ *   apply, global transition, update         cal2D.c:717-776
+ *   cell accessors (host side)               cal2D.c:780-930
+ *   finalize                                 cal2D.c:933-961
+ */
+#define CAL_BUILDING_LIBRARY
+#include <stdlib.h>
+#include <string.h>
+
+#include "cal_model_internal.cuh"
+
+using cal::CalGrid;
+
+/* ======================= process registry =============================== */
+/* Filled by static initialisers of the translation units that define
+ * processes, possibly before main(): plain zero-initialised arrays. */
+#define CAL_REGISTRY_MAX 4096
+static CALCallbackFunc2D g_reg_host[CAL_REGISTRY_MAX];
+static CALLaunchFunc2D g_reg_launch[CAL_REGISTRY_MAX];
+static int g_reg_n;
+
+extern "C" int calRegisterElementaryProcess2D(CALCallbackFunc2D host_name, CALLaunchFunc2D launch, const char* name)
+{
+    for (int r = 0; r < g_reg_n; r++)
+        if (g_reg_host[r] == host_name) {
+            g_reg_launch[r] = launch;
+            return 1;
+        }
+    if (g_reg_n >= CAL_REGISTRY_MAX)
+        return 0;
+    g_reg_host[g_reg_n] = host_name;
+    g_reg_launch[g_reg_n] = launch;
+    (void)name;
+    g_reg_n++;
+    return 1;
+}
+
+static CALLaunchFunc2D find_launch(CALCallbackFunc2D f)
+{
+    for (int r = 0; r < g_reg_n; r++)
+        if (g_reg_host[r] == f)
+            return g_reg_launch[r];
+    return nullptr;
+}
+
+extern "C" void calHostCallOfDeviceProcess2D(const char* name)
+{
+    cal::set_error(CAL_ERROR_NOT_A_DEVICE_PROCESS,
+                   std::string("device elementary process '") + name +
+                       "' called as a host function; apply it with calApplyElementaryProcess2D");
+}
+
+/* ======================= helpers ======================================== */
+
+static inline CalGrid& G(struct CALModel2D* ca) { return ca->gpu->g; }
+
+template <typename Q>
+static inline int slot_of(struct CALModel2D* ca, int type, Q* q)
+{
+    return (int)(((char*)q - (char*)G(ca).pool[type]) / 32);
+}
+
+static bool neighbor(const struct CALModel2D* ca, int i, int j, int n, int* oi, int* oj)
+{
+    if ((ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_2D && (j % 2) == 1) ||
+        (ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_ALT_2D && (i % 2) == 1))
+        n += CAL_HEXAGONAL_SHIFT;
+    int a = i + ca->X[n].i, b = j + ca->X[n].j;
+    if (ca->T == CAL_SPACE_TOROIDAL) {
+        a = calGetToroidalX(a, ca->rows);
+        b = calGetToroidalX(b, ca->columns);
+    } else if (a < 0 || a >= ca->rows || b < 0 || b >= ca->columns) {
+        return false;
+    }
+    *oi = a;
+    *oj = b;
+    return true;
+}
+
+static int table_len(const struct CALModel2D* ca);
+
+/* the table only changes through calAddNeighbor2D: upload it when it did */
+static bool upload_X(struct CALModel2D* ca)
+{
+    CALGpuModel2D* gm = ca->gpu;
+    const int len = table_len(ca);
+    if (gm->d_X_len == len || len == 0)
+        return true;
+    if (gm->g.capturing) {
+        cal::set_error(CAL_ERROR_NOT_CAPTURABLE, "neighbourhood changed during graph capture");
+        return false;
+    }
+    if (!cal::cuda_ok(cudaMemcpy(gm->d_X, ca->X, sizeof(struct CALCell2D) * len, cudaMemcpyHostToDevice), "upload X"))
+        return false;
+    gm->d_X_len = len;
+    return true;
+}
+
+static int table_len(const struct CALModel2D* ca)
+{
+    /* hexagonal models keep 14 entries and report 7 (cal2D.c:115, 160) */
+    return (ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_2D || ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_ALT_2D)
+               ? 2 * ca->sizeof_X : ca->sizeof_X;
+}
+
+/* launch descriptor for a process kernel */
+static bool build_desc(struct CALModel2D* ca, CALDevModel2D* d)
+{
+    CalGrid& g = G(ca);
+    memset(d, 0, sizeof(*d));
+    d->model = *ca;
+    d->model.gpu = nullptr;
+    d->model.pQb_array = nullptr;
+    d->model.pQi_array = nullptr;
+    d->model.pQr_array = nullptr;
+    d->model.elementary_processes = nullptr;
+    d->model.A.size_next = nullptr;
+    d->model.A.flags = (CALbyte*)g.d_flags;
+    d->model.A.cells = (struct CALCell2D*)g.d_cells;
+    const int len = table_len(ca);
+    if (len > CAL_MAX_NEIGHBORS) {
+        cal::set_error(CAL_ERROR_LIMIT, "neighbourhood larger than CAL_MAX_NEIGHBORS");
+        return false;
+    }
+    if (!upload_X(ca))
+        return false;
+    d->model.X = ca->gpu->d_X;
+    for (int t = 0; t < CAL_NTYPES; t++) {
+        d->pool[t] = (unsigned long long)(uintptr_t)g.pool[t];
+        for (int s = 0; s < g.nslot[t]; s++) {
+            d->cur[t][s] = g.sub[t][s].layer[0].dev;
+            d->nxt[t][s] = g.sub[t][s].single ? nullptr : g.sub[t][s].layer[1].dev;
+        }
+    }
+    d->dirty = g.d_dirty;
+    d->flags = (CALbyte*)g.d_flags;
+    d->cells = (struct CALCell2D*)g.d_cells;
+    d->count = g.d_count;
+    d->rows = ca->rows;
+    d->cols = ca->columns;
+    d->toroidal = ca->T == CAL_SPACE_TOROIDAL;
+    d->hex = ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_2D ? 1 : (ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_ALT_2D ? 2 : 0);
+    d->use_list = ca->OPTIMIZATION == CAL_OPT_ACTIVE_CELLS;
+    d->nx = ca->sizeof_X;
+    for (int n = 0; n < len; n++) {
+        d->xi[n] = ca->X[n].i;
+        d->xj[n] = ca->X[n].j;
+    }
+    return true;
+}
+
+/* ======================= definition ===================================== */
+
+static void add_default_neighborhood(struct CALModel2D* ca)
+{
+    /* index order of the reference's tables (cal2D.c:28-166) */
+    static const int vn[5][2] = {{0, 0}, {-1, 0}, {0, -1}, {0, 1}, {1, 0}};
+    static const int moore[9][2] = {{0, 0}, {-1, 0}, {0, -1}, {0, 1}, {1, 0}, {-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+    static const int hex[14][2] = {{0, 0}, {-1, 1}, {-1, 0}, {-1, -1}, {0, -1}, {1, 0}, {0, 1},
+                                   {0, 0}, {0, 1}, {-1, 0}, {0, -1}, {1, -1}, {1, 0}, {1, 1}};
+    static const int hexalt[14][2] = {{0, 0}, {-1, 0}, {-1, -1}, {0, -1}, {1, -1}, {1, 0}, {0, 1},
+                                      {0, 0}, {-1, 1}, {-1, 0}, {0, -1}, {1, 0}, {1, 1}, {0, 1}};
+    const int(*t)[2] = nullptr;
+    int cnt = 0;
+    switch (ca->X_id) {
+    case CAL_VON_NEUMANN_NEIGHBORHOOD_2D: t = vn; cnt = 5; break;
+    case CAL_MOORE_NEIGHBORHOOD_2D: t = moore; cnt = 9; break;
+    case CAL_HEXAGONAL_NEIGHBORHOOD_2D: t = hex; cnt = 14; break;
+    case CAL_HEXAGONAL_NEIGHBORHOOD_ALT_2D: t = hexalt; cnt = 14; break;
+    default: return;
+    }
+    for (int n = 0; n < cnt; n++)
+        calAddNeighbor2D(ca, t[n][0], t[n][1]);
+    if (cnt == 14) {
+        ca->sizeof_X = 7;
+        ca->gpu->d_X_len = -1;
+        upload_X(ca);
+    }
+}
+
+extern "C" struct CALModel2D* calCADef2D(int rows, int columns, enum CALNeighborhood2D nb,
+                                         enum CALSpaceBoundaryCondition bc, enum CALOptimization opt)
+{
+    struct CALModel2D* ca = (struct CALModel2D*)calloc(1, sizeof(struct CALModel2D));
+    if (!ca) {
+        cal::set_error(CAL_ERROR_OUT_OF_MEMORY, "calCADef2D");
+        return nullptr;
+    }
+    ca->gpu = new (std::nothrow) CALGpuModel2D();
+    if (!ca->gpu || !ca->gpu->g.init(2, rows, columns, 1, bc == CAL_SPACE_TOROIDAL, opt == CAL_OPT_ACTIVE_CELLS)) {
+        if (ca->gpu) {
+            ca->gpu->g.destroy();
+            delete ca->gpu;
+        }
+        free(ca);
+        return nullptr;
+    }
+    if (!cal::cuda_ok(cudaMalloc(&ca->gpu->d_X, sizeof(struct CALCell2D) * CAL_MAX_NEIGHBORS), "cudaMalloc X")) {
+        ca->gpu->g.destroy();
+        delete ca->gpu;
+        free(ca);
+        return nullptr;
+    }
+    ca->rows = rows;
+    ca->columns = columns;
+    ca->T = bc;
+    ca->is_safe = CAL_UNSAFE_INACTIVE;
+    ca->OPTIMIZATION = opt;
+    ca->A.flags = opt == CAL_OPT_ACTIVE_CELLS ? (CALbyte*)ca->gpu->g.h_flags : nullptr;
+    ca->A.num_threads = 1;
+    ca->A.size_next = (int*)calloc(1, sizeof(int));
+    ca->A.cells = nullptr;
+    ca->A.size_current = 0;
+    ca->X = nullptr;
+    ca->sizeof_X = 0;
+    ca->X_id = nb;
+    add_default_neighborhood(ca);
+    return ca;
+}
+
+extern "C" void calSetUnsafe2D(struct CALModel2D* ca2D)
+{
+    ca2D->is_safe = CAL_UNSAFE_ACTIVE;
+}
+
+extern "C" struct CALCell2D* calAddNeighbor2D(struct CALModel2D* ca, int i, int j)
+{
+    if (table_len(ca) + 1 > CAL_MAX_NEIGHBORS) {
+        cal::set_error(CAL_ERROR_LIMIT, "neighbourhood larger than CAL_MAX_NEIGHBORS");
+        return nullptr;
+    }
+    int len = ca->sizeof_X;
+    struct CALCell2D* X = (struct CALCell2D*)realloc(ca->X, sizeof(struct CALCell2D) * (len + 1));
+    if (!X) {
+        cal::set_error(CAL_ERROR_OUT_OF_MEMORY, "calAddNeighbor2D");
+        return nullptr;
+    }
+    X[len].i = i;
+    X[len].j = j;
+    ca->X = X;
+    ca->sizeof_X = len + 1;
+    ca->gpu->d_X_len = -1;
+    upload_X(ca); /* at definition time, never inside a recorded step */
+    return ca->X;
+}
+
+template <typename QT, int TYPE>
+static QT* add_substate(struct CALModel2D* ca, bool single)
+{
+    CalGrid& g = G(ca);
+    void *cur = nullptr, *next = nullptr;
+    int slot = g.add_sub(TYPE, single, &cur, &next);
+    if (slot < 0)
+        return nullptr;
+    QT* q = (QT*)((char*)g.pool[TYPE] + 32 * slot);
+    q->current = (decltype(q->current))cur;
+    q->next = (decltype(q->next))next;
+    if (!single) {
+        QT*** arr = TYPE == 0 ? (QT***)&ca->pQb_array : (TYPE == 1 ? (QT***)&ca->pQi_array : (QT***)&ca->pQr_array);
+        int* n = TYPE == 0 ? &ca->sizeof_pQb_array : (TYPE == 1 ? &ca->sizeof_pQi_array : &ca->sizeof_pQr_array);
+        QT** na = (QT**)realloc(*arr, sizeof(QT*) * (*n + 1));
+        if (!na) {
+            cal::set_error(CAL_ERROR_OUT_OF_MEMORY, "substate array");
+            return nullptr;
+        }
+        na[*n] = q;
+        *arr = na;
+        (*n)++;
+    }
+    return q;
+}
+
+extern "C" struct CALSubstate2Db* calAddSubstate2Db(struct CALModel2D* ca) { return add_substate<struct CALSubstate2Db, 0>(ca, false); }
+extern "C" struct CALSubstate2Di* calAddSubstate2Di(struct CALModel2D* ca) { return add_substate<struct CALSubstate2Di, 1>(ca, false); }
+extern "C" struct CALSubstate2Dr* calAddSubstate2Dr(struct CALModel2D* ca) { return add_substate<struct CALSubstate2Dr, 2>(ca, false); }
+extern "C" struct CALSubstate2Db* calAddSingleLayerSubstate2Db(struct CALModel2D* ca) { return add_substate<struct CALSubstate2Db, 0>(ca, true); }
+extern "C" struct CALSubstate2Di* calAddSingleLayerSubstate2Di(struct CALModel2D* ca) { return add_substate<struct CALSubstate2Di, 1>(ca, true); }
+extern "C" struct CALSubstate2Dr* calAddSingleLayerSubstate2Dr(struct CALModel2D* ca) { return add_substate<struct CALSubstate2Dr, 2>(ca, true); }
+
+extern "C" CALCallbackFunc2D* calAddElementaryProcess2D(struct CALModel2D* ca, CALCallbackFunc2D ep)
+{
+    CALLaunchFunc2D launch = find_launch(ep);
+    if (!launch) {
+        cal::set_error(CAL_ERROR_NOT_A_DEVICE_PROCESS,
+                       "calAddElementaryProcess2D: not a device process (define it with CAL_ELEMENTARY_PROCESS_2D)");
+        return nullptr;
+    }
+    if (ca->num_of_elementary_processes >= CAL_MAX_ELEMENTARY_PROCESSES) {
+        cal::set_error(CAL_ERROR_LIMIT, "too many elementary processes");
+        return nullptr;
+    }
+    CALCallbackFunc2D* arr = (CALCallbackFunc2D*)realloc(ca->elementary_processes,
+                                                         sizeof(CALCallbackFunc2D) * (ca->num_of_elementary_processes + 1));
+    if (!arr) {
+        cal::set_error(CAL_ERROR_OUT_OF_MEMORY, "calAddElementaryProcess2D");
+        return nullptr;
+    }
+    arr[ca->num_of_elementary_processes] = ep;
+    ca->gpu->launch[ca->num_of_elementary_processes] = launch;
+    ca->elementary_processes = arr;
+    ca->num_of_elementary_processes++;
+    return ca->elementary_processes;
+}
+
+/* ======================= active cells (host side) ======================== */
+
+extern "C" void calAddActiveCell2D(struct CALModel2D* ca, int i, int j)
+{
+    CalGrid& g = G(ca);
+    if (!g.active || i < 0 || i >= ca->rows || j < 0 || j >= ca->columns)
+        return;
+    if (!g.flags_to_host())
+        return;
+    g.h_flags[(long long)i * ca->columns + j] = 1;
+    g.flags_dev_valid = false;
+}
+
+extern "C" void calAddActiveCellX2D(struct CALModel2D* ca, int i, int j, int n)
+{
+    int a, b;
+    if (neighbor(ca, i, j, n, &a, &b))
+        calAddActiveCell2D(ca, a, b);
+}
+
+extern "C" void calRemoveActiveCell2D(struct CALModel2D* ca, int i, int j)
+{
+    CalGrid& g = G(ca);
+    if (!g.active || i < 0 || i >= ca->rows || j < 0 || j >= ca->columns)
+        return;
+    if (!g.flags_to_host())
+        return;
+    g.h_flags[(long long)i * ca->columns + j] = 0;
+    g.flags_dev_valid = false;
+}
+
+extern "C" void calUpdateActiveCells2D(struct CALModel2D* ca)
+{
+    G(ca).compact();
+}
+
+/* ======================= whole-substate operations ====================== */
+
+#define CAL_SUBSTATE_OPS_2D(S, T, TC)                                                                   \
+    extern "C" void calInitSubstate2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, T value)    \
+    {                                                                                                   \
+        int s = slot_of(ca, TC, Q);                                                                     \
+        if (G(ca).fill(TC, s, 0, &value, true))                                                         \
+            G(ca).fill(TC, s, 1, &value, true);                                                         \
+    }                                                                                                   \
+    extern "C" void calInitSubstateNext2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, T value) \
+    {                                                                                                   \
+        G(ca).fill(TC, slot_of(ca, TC, Q), 1, &value, true);                                            \
+    }                                                                                                   \
+    extern "C" void calUpdateSubstate2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q)           \
+    {                                                                                                   \
+        CalGrid& g = G(ca);                                                                             \
+        if (!g.to_device_all())                                                                         \
+            return;                                                                                     \
+        std::vector<std::pair<int, int>> one(1, std::make_pair(TC, slot_of(ca, TC, Q)));                \
+        g.copy_next_to_current(one, false, true);                                                       \
+    }                                                                                                   \
+    extern "C" void* calGetDeviceBuffer2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int layer) \
+    {                                                                                                   \
+        CalGrid& g = G(ca);                                                                             \
+        int s = slot_of(ca, TC, Q);                                                                     \
+        if (!g.to_device_all())                                                                         \
+            return nullptr;                                                                             \
+        if (layer == 1 && !g.repair_stale(TC, s))                                                       \
+            return nullptr;                                                                             \
+        return g.sub[TC][s].layer[layer ? 1 : 0].dev;  /* layer 2: next, to be overwritten whole */     \
+    }                                                                                                   \
+    extern "C" void calSyncSubstate2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q)             \
+    {                                                                                                   \
+        G(ca).to_host(TC, slot_of(ca, TC, Q), 0);                                                       \
+    }                                                                                                   \
+    extern "C" void calSwapSubstate2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q)             \
+    {                                                                                                   \
+        G(ca).swap(TC, slot_of(ca, TC, Q));                                                             \
+    }
+
+CAL_SUBSTATE_OPS_2D(b, CALbyte, 0)
+CAL_SUBSTATE_OPS_2D(i, CALint, 1)
+CAL_SUBSTATE_OPS_2D(r, CALreal, 2)
+
+/* ======================= transition ===================================== */
+
+static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch)
+{
+    CalGrid& g = G(ca);
+    if (!g.repair_all_stale() || !g.to_device_all())
+        return;
+    CALDevModel2D d;
+    if (!build_desc(ca, &d))
+        return;
+    int gx, gy;
+    g.launch_grid(&gx, &gy);
+    int rc = launch(&d, gx, gy, (void*)g.stream);
+    if (rc != 0) {
+        cal::cuda_ok((cudaError_t)rc, "elementary process launch");
+        return;
+    }
+    g.device_wrote_all();
+}
+
+extern "C" void calApplyElementaryProcess2D(struct CALModel2D* ca, CALCallbackFunc2D ep)
+{
+    CALLaunchFunc2D launch = find_launch(ep);
+    if (!launch) {
+        cal::set_error(CAL_ERROR_NOT_A_DEVICE_PROCESS, "calApplyElementaryProcess2D: not a device process");
+        return;
+    }
+    apply_launch(ca, launch);
+}
+
+extern "C" void calUpdate2D(struct CALModel2D* ca)
+{
+    G(ca).update_all();
+}
+
+extern "C" void calGlobalTransitionFunction2D(struct CALModel2D* ca)
+{
+    for (int b = 0; b < ca->num_of_elementary_processes; b++) {
+        apply_launch(ca, ca->gpu->launch[b]);
+        calUpdate2D(ca);
+    }
+}
+
+/* ======================= host cell accessors ============================ */
+
+#define CAL_CELL_OPS_2D(S, T, TC)                                                                          \
+    extern "C" T calGet2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j)              \
+    {                                                                                                      \
+        G(ca).to_host(TC, slot_of(ca, TC, Q), 0);                                                          \
+        return Q->current[(long long)i * ca->columns + j];                                                 \
+    }                                                                                                      \
+    extern "C" T calGetX2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, int n)      \
+    {                                                                                                      \
+        int a, b;                                                                                          \
+        if (!neighbor(ca, i, j, n, &a, &b))                                                                \
+            return (T)0;                                                                                   \
+        return calGet2D##S(ca, Q, a, b);                                                                   \
+    }                                                                                                      \
+    extern "C" void calSet2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, T v)      \
+    {                                                                                                      \
+        int s = slot_of(ca, TC, Q);                                                                        \
+        if (!G(ca).to_host(TC, s, 1))                                                                      \
+            return;                                                                                        \
+        Q->next[(long long)i * ca->columns + j] = v;                                                       \
+        G(ca).host_wrote(TC, s, 1);                                                                        \
+    }                                                                                                      \
+    extern "C" void calSetCurrent2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, T v) \
+    {                                                                                                      \
+        int s = slot_of(ca, TC, Q);                                                                        \
+        if (!G(ca).to_host(TC, s, 0))                                                                      \
+            return;                                                                                        \
+        Q->current[(long long)i * ca->columns + j] = v;                                                    \
+        G(ca).host_wrote(TC, s, 0);                                                                        \
+    }                                                                                                      \
+    extern "C" void calInit2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, T v)     \
+    {                                                                                                      \
+        int s = slot_of(ca, TC, Q);                                                                        \
+        calSetCurrent2D##S(ca, Q, i, j, v);                                                                \
+        if (Q->next && G(ca).to_host(TC, s, 1)) {                                                          \
+            Q->next[(long long)i * ca->columns + j] = v;                                                   \
+            G(ca).host_wrote(TC, s, 1);                                                                    \
+        }                                                                                                  \
+    }
+
+CAL_CELL_OPS_2D(b, CALbyte, 0)
+CAL_CELL_OPS_2D(i, CALint, 1)
+CAL_CELL_OPS_2D(r, CALreal, 2)
+
+/* ======================= additions ===================================== */
+
+extern "C" void calSync2D(struct CALModel2D* ca)
+{
+    CalGrid& g = G(ca);
+    for (int t = 0; t < CAL_NTYPES; t++)
+        for (int s = 0; s < g.nslot[t]; s++) {
+            g.to_host(t, s, 0);
+            if (!g.sub[t][s].single)
+                g.to_host(t, s, 1);
+        }
+    if (!g.active) {
+        g.sync();
+        return;
+    }
+    g.flags_to_host();
+    int n = 0;
+    if (!cal::cuda_ok(cudaMemcpyAsync(&n, g.d_count, sizeof(int), cudaMemcpyDeviceToHost, g.stream), "read count") ||
+        !g.sync())
+        return;
+    free(ca->A.cells);
+    ca->A.cells = nullptr;
+    ca->A.size_current = n;
+    if (n > 0) {
+        int* tmp = (int*)malloc(sizeof(int) * 2 * (size_t)n);
+        ca->A.cells = (struct CALCell2D*)malloc(sizeof(struct CALCell2D) * (size_t)n);
+        if (!tmp || !ca->A.cells) {
+            free(tmp);
+            cal::set_error(CAL_ERROR_OUT_OF_MEMORY, "calSync2D active list");
+            return;
+        }
+        if (cal::cuda_ok(cudaMemcpyAsync(tmp, g.d_cells, sizeof(int) * 2 * (size_t)n, cudaMemcpyDeviceToHost, g.stream),
+                         "read active list") && g.sync())
+            for (int c = 0; c < n; c++) {
+                ca->A.cells[c].i = tmp[2 * c];
+                ca->A.cells[c].j = tmp[2 * c + 1];
+            }
+        free(tmp);
+    }
+}
+
+extern "C" void calMarkHostDirty2D(struct CALModel2D* ca)
+{
+    CalGrid& g = G(ca);
+    for (int t = 0; t < CAL_NTYPES; t++)
+        for (int s = 0; s < g.nslot[t]; s++)
+            for (int l = 0; l < (g.sub[t][s].single ? 1 : 2); l++)
+                if (g.sub[t][s].layer[l].host_valid)
+                    g.host_wrote(t, s, l);
+    if (g.active && g.flags_host_valid)
+        g.flags_dev_valid = false;
+}
+
+extern "C" void calMarkDeviceWritten2D(struct CALModel2D* ca)
+{
+    G(ca).device_wrote_all();
+}
+
+extern "C" void calFinish2D(struct CALModel2D* ca)
+{
+    G(ca).sync();
+}
+
+extern "C" void* calGetStream2D(struct CALModel2D* ca)
+{
+    return (void*)G(ca).stream;
+}
+
+extern "C" void calGetDeviceActiveCells2D(struct CALModel2D* ca, CALbyte** flags, struct CALCell2D** cells, int** count)
+{
+    CalGrid& g = G(ca);
+    g.to_device_all();
+    if (flags)
+        *flags = (CALbyte*)g.d_flags;
+    if (cells)
+        *cells = (struct CALCell2D*)g.d_cells;
+    if (count)
+        *count = g.d_count;
+}
+
+extern "C" int calGetActiveCellCount2D(struct CALModel2D* ca)
+{
+    CalGrid& g = G(ca);
+    int n = 0;
+    if (cal::cuda_ok(cudaMemcpyAsync(&n, g.d_count, sizeof(int), cudaMemcpyDeviceToHost, g.stream), "read count"))
+        g.sync();
+    return n;
+}
+
+extern "C" void calFinalize2D(struct CALModel2D* ca)
+{
+    if (!ca)
+        return;
+    if (ca->gpu) {
+        ca->gpu->g.destroy();
+        if (ca->gpu->d_X)
+            cudaFree(ca->gpu->d_X);
+        delete ca->gpu;
+    }
+    free(ca->A.cells);
+    free(ca->A.size_next);
+    free(ca->X);
+    free(ca->pQb_array);
+    free(ca->pQi_array);
+    free(ca->pQr_array);
+    free(ca->elementary_processes);
+    free(ca);
+}

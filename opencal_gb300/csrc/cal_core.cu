@@ -1,0 +1,695 @@
+/*
+ * cal_core.cu -- engine shared by the 2D and 3D C APIs: device buffers and
+ * host mirrors of the substates, the update (next -> current) kernel, the
+ * substate fill kernel and the active-cell compaction.
+ *
+ * Reference behaviour restated here:
+ *   calUpdate2D            OpenCAL-OMP/source/cal2D.c:758-776
+ *   calUpdateActiveCells2D OpenCAL-OMP/source/cal2D.c:382-440 (row-major list)
+ *   calUpdateActiveCells3D OpenCAL-OMP/source/cal3D.c:313-370 (i, j, k order)
+ *   calCopyBuffer2D* / calCopyActiveCellsBuffer2D*  cal2DBuffer.c:44-160
+ *   calSetBuffer2D* / calSetActiveCellsBuffer2D*    cal2DBuffer.c:223-259
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "cal_core.cuh"
+
+namespace cal {
+
+/* ======================= errors ========================================= */
+
+static thread_local CALError g_err = CAL_SUCCESS;
+static thread_local char g_msg[512] = "";
+
+void set_error(CALError code, const std::string& msg)
+{
+    g_err = code;
+    snprintf(g_msg, sizeof(g_msg), "%s", msg.c_str());
+    static const char* verbose = getenv("OPENCAL_VERBOSE_ERRORS");
+    if (code != CAL_SUCCESS && (verbose == nullptr || verbose[0] != '0'))
+        fprintf(stderr, "opencal-gb300: %s\n", g_msg);
+    const char* ab = getenv("OPENCAL_ABORT_ON_ERROR");
+    if (code != CAL_SUCCESS && ab && ab[0] == '1')
+        abort();
+}
+
+bool cuda_ok(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess)
+        return true;
+    set_error(CAL_ERROR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+/* ======================= kernels ======================================== */
+
+static const int kThreads = 256;
+
+static int grid_for(long long work)
+{
+    long long b = (work + kThreads - 1) / kThreads;
+    const long long cap = 152LL * 8;
+    if (b < 1)
+        b = 1;
+    return (int)(b < cap ? b : cap);
+}
+
+/* every cell, or the listed cells when the list is non-empty */
+template <typename T>
+__global__ void k_fill(T* buf, T v, long long n, const int* lin, const int* count, int at_active)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int listed = at_active ? *count : 0;
+    if (listed > 0) {
+        for (long long c = t; c < listed; c += stride)
+            buf[lin[c]] = v;
+    } else {
+        for (long long c = t; c < n; c += stride)
+            buf[c] = v;
+    }
+}
+
+#define CAL_UPDATE_MAX (CAL_NTYPES * CAL_MAX_SUBSTATES_CORE)
+
+struct UpdateParams {
+    const void* src[CAL_UPDATE_MAX];
+    void* dst[CAL_UPDATE_MAX];
+    unsigned char elem[CAL_UPDATE_MAX];
+    unsigned char type[CAL_UPDATE_MAX];
+    unsigned char slot[CAL_UPDATE_MAX];
+    int n_entries;
+    long long ncells;
+    const unsigned* dirty;
+    unsigned forced[CAL_NTYPES];
+    int use_dirty;
+    int at_active;
+    const int* lin;
+    const int* count;
+};
+
+/* next -> current of the selected substates.  Whole-grid copies move 16-byte
+ * vectors (device buffers are 256-byte aligned); active-cell copies move one
+ * element per listed cell (calCopyActiveCellsBuffer2D*). */
+__global__ void k_update(const __grid_constant__ UpdateParams p)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int listed = p.at_active ? *p.count : 0;
+    for (int e = 0; e < p.n_entries; e++) {
+        if (p.use_dirty && !(((p.dirty[p.type[e]] | p.forced[p.type[e]]) >> p.slot[e]) & 1u))
+            continue;
+        const int es = p.elem[e];
+        if (listed > 0) {
+            for (long long c = t0; c < listed; c += stride) {
+                const long long o = (long long)p.lin[c];
+                if (es == 8)
+                    ((unsigned long long*)p.dst[e])[o] = ((const unsigned long long*)p.src[e])[o];
+                else if (es == 4)
+                    ((unsigned*)p.dst[e])[o] = ((const unsigned*)p.src[e])[o];
+                else
+                    ((unsigned char*)p.dst[e])[o] = ((const unsigned char*)p.src[e])[o];
+            }
+        } else {
+            const long long bytes = p.ncells * es;
+            const long long vecs = bytes >> 4;
+            const uint4* s = (const uint4*)p.src[e];
+            uint4* d = (uint4*)p.dst[e];
+            for (long long c = t0; c < vecs; c += stride)
+                d[c] = s[c];
+            for (long long c = (vecs << 4) + t0; c < bytes; c += stride)
+                ((unsigned char*)p.dst[e])[c] = ((const unsigned char*)p.src[e])[c];
+        }
+    }
+}
+
+/* ---- active-cell compaction -------------------------------------------
+ * Two passes over the flags, in the reference's list order:
+ *   2D: memory order (row-major);
+ *   3D: i, then j, then k, while memory is slice-major (k*rows*cols + ...).
+ * Pass 1 counts set flags per block; pass 2 gives each block its offset
+ * (sum of the counts before it), scans within the block and writes the
+ * cells in order.  Each thread owns a contiguous run of kPerThread
+ * positions, so thread order is list order.  block_counts is scratch
+ * (n_blocks ints); the last block writes the total. */
+static const int kPerThread = 16;
+static const int kChunk = kThreads * kPerThread; /* positions per block */
+
+struct CompactGeom {
+    int dim, rows, cols, slices;
+    long long n;
+};
+
+static __device__ __forceinline__ long long order_to_mem(const CompactGeom& g, long long v)
+{
+    if (g.dim == 2)
+        return v;
+    const long long k = v % g.slices;
+    const long long ij = v / g.slices; /* i*cols + j */
+    return k * (long long)g.rows * g.cols + ij;
+}
+
+static __device__ __forceinline__ int count_run(const unsigned char* flags, const CompactGeom& g, long long start)
+{
+    int c = 0;
+    if (g.dim == 2 && start + kPerThread <= g.n) {
+        const uint4 w = *(const uint4*)(flags + start); /* start is a multiple of 16 */
+        const unsigned ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            /* one bit per non-zero byte */
+            const unsigned x = ws[q];
+            const unsigned nz = ((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x;
+            c += __popc(nz & 0x80808080u);
+        }
+        return c;
+    }
+    for (int q = 0; q < kPerThread; q++) {
+        const long long v = start + q;
+        if (v < g.n && flags[order_to_mem(g, v)])
+            c++;
+    }
+    return c;
+}
+
+__global__ void k_compact_count(const unsigned char* flags, CompactGeom g, int* block_counts)
+{
+    __shared__ int warp_sums[kThreads / 32];
+    const long long start = ((long long)blockIdx.x * kThreads + threadIdx.x) * kPerThread;
+    int c = start < g.n ? count_run(flags, g, start) : 0;
+    for (int o = 16; o > 0; o >>= 1)
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0)
+        warp_sums[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int w = 0; w < kThreads / 32; w++)
+            s += warp_sums[w];
+        block_counts[blockIdx.x] = s;
+    }
+}
+
+__global__ void k_compact_scatter(const unsigned char* flags, CompactGeom g, const int* block_counts,
+                                  int* cells, int* lin, int* count)
+{
+    __shared__ int warp_sums[kThreads / 32];
+    __shared__ int s_offset;
+    /* offset of this block = sum of the counts of the blocks before it */
+    int part = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x)
+        part += block_counts[b];
+    for (int o = 16; o > 0; o >>= 1)
+        part += __shfl_down_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0)
+        warp_sums[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int w = 0; w < kThreads / 32; w++)
+            s += warp_sums[w];
+        s_offset = s;
+    }
+    __syncthreads();
+
+    const long long start = ((long long)blockIdx.x * kThreads + threadIdx.x) * kPerThread;
+    const int mine = start < g.n ? count_run(flags, g, start) : 0;
+    /* exclusive scan of `mine` across the block */
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o)
+            incl += y;
+    }
+    __syncthreads();
+    if (lane == 31)
+        warp_sums[warp] = incl;
+    __syncthreads();
+    int warp_base = 0;
+    for (int w = 0; w < warp; w++)
+        warp_base += warp_sums[w];
+    int pos = s_offset + warp_base + incl - mine;
+    if (mine > 0) {
+        for (int q = 0; q < kPerThread; q++) {
+            const long long v = start + q;
+            if (v >= g.n)
+                break;
+            const long long mem = order_to_mem(g, v);
+            if (flags[mem]) {
+                int i, j, k = 0;
+                if (g.dim == 2) {
+                    i = (int)(v / g.cols);
+                    j = (int)(v % g.cols);
+                    cells[2 * pos] = i;
+                    cells[2 * pos + 1] = j;
+                } else {
+                    k = (int)(v % g.slices);
+                    const long long ij = v / g.slices;
+                    i = (int)(ij / g.cols);
+                    j = (int)(ij % g.cols);
+                    cells[3 * pos] = i;
+                    cells[3 * pos + 1] = j;
+                    cells[3 * pos + 2] = k;
+                }
+                lin[pos] = (int)mem;
+                pos++;
+            }
+        }
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1)
+        *count = pos; /* the last thread ends at the running total */
+}
+
+int compact_blocks_needed(long long ncells)
+{
+    return (int)((ncells + kChunk - 1) / kChunk);
+}
+
+cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int cols, int slices, int* cells, int* lin,
+                          int* count, int* block_counts, int n_blocks, cudaStream_t stream)
+{
+    CompactGeom g;
+    g.dim = dim;
+    g.rows = rows;
+    g.cols = cols;
+    g.slices = dim == 3 ? slices : 1;
+    g.n = (long long)rows * cols * g.slices;
+    if (n_blocks < compact_blocks_needed(g.n))
+        return cudaErrorInvalidValue;
+    const int nb = compact_blocks_needed(g.n);
+    k_compact_count<<<nb, kThreads, 0, stream>>>(flags, g, block_counts);
+    k_compact_scatter<<<nb, kThreads, 0, stream>>>(flags, g, block_counts, cells, lin, count);
+    return cudaGetLastError();
+}
+
+/* ======================= CalGrid ======================================== */
+
+static size_t type_size(int t)
+{
+    return t == 0 ? sizeof(CALbyte) : (t == 1 ? sizeof(CALint) : sizeof(CALreal));
+}
+
+bool CalGrid::init(int dim_, int rows_, int cols_, int slices_, int toroidal_, int active_)
+{
+    dim = dim_;
+    rows = rows_;
+    cols = cols_;
+    slices = dim == 3 ? slices_ : 1;
+    toroidal = toroidal_;
+    active = active_;
+    ncells = (long long)rows * cols * slices;
+    if (rows <= 0 || cols <= 0 || slices <= 0 || ncells > 0x7fffffffLL) {
+        set_error(CAL_ERROR_INVALID_ARGUMENT, "grid dimensions must be positive and hold < 2^31 cells");
+        return false;
+    }
+    if (!cuda_ok(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate"))
+        return false;
+    for (int t = 0; t < CAL_NTYPES; t++) {
+        /* handle pool: one 32-byte record per slot, addresses stable */
+        pool[t] = calloc(CAL_MAX_SUBSTATES_CORE, 32);
+        if (!pool[t]) {
+            set_error(CAL_ERROR_OUT_OF_MEMORY, "handle pool");
+            return false;
+        }
+    }
+    if (!cuda_ok(cudaMalloc(&d_dirty, 4 * sizeof(unsigned)), "cudaMalloc dirty") ||
+        !cuda_ok(cudaMemsetAsync(d_dirty, 0, 4 * sizeof(unsigned), stream), "memset dirty"))
+        return false;
+    if (!cuda_ok(cudaMalloc(&d_count, sizeof(int)), "cudaMalloc count") ||
+        !cuda_ok(cudaMemsetAsync(d_count, 0, sizeof(int), stream), "memset count"))
+        return false;
+    if (active) {
+        n_blocks = compact_blocks_needed(ncells);
+        if (!cuda_ok(cudaMalloc(&d_flags, (size_t)ncells), "cudaMalloc flags") ||
+            !cuda_ok(cudaMalloc(&d_cells, (size_t)ncells * dim * sizeof(int)), "cudaMalloc cells") ||
+            !cuda_ok(cudaMalloc(&d_lin, (size_t)ncells * sizeof(int)), "cudaMalloc lin") ||
+            !cuda_ok(cudaMalloc(&d_block_counts, (size_t)n_blocks * sizeof(int)), "cudaMalloc scratch") ||
+            !cuda_ok(cudaMemsetAsync(d_flags, 0, (size_t)ncells, stream), "memset flags"))
+            return false;
+        if (!cuda_ok(cudaMallocHost(&h_flags, (size_t)ncells), "cudaMallocHost flags"))
+            return false;
+        memset(h_flags, 0, (size_t)ncells);
+    }
+    return true;
+}
+
+void CalGrid::destroy()
+{
+    if (stream)
+        cudaStreamSynchronize(stream);
+    for (int t = 0; t < CAL_NTYPES; t++) {
+        for (int s = 0; s < nslot[t]; s++) {
+            Sub& q = sub[t][s];
+            for (int l = 0; l < 2; l++) {
+                if (q.layer[l].dev)
+                    cudaFree(q.layer[l].dev);
+                if (q.host[l])
+                    cudaFreeHost(q.host[l]);
+            }
+        }
+        free(pool[t]);
+        pool[t] = nullptr;
+    }
+    cudaFree(d_flags);
+    cudaFree(d_cells);
+    cudaFree(d_lin);
+    cudaFree(d_count);
+    cudaFree(d_block_counts);
+    cudaFree(d_dirty);
+    if (h_flags)
+        cudaFreeHost(h_flags);
+    if (stream)
+        cudaStreamDestroy(stream);
+    stream = nullptr;
+}
+
+int CalGrid::add_sub(int type, bool single, void** cur_mirror, void** next_mirror)
+{
+    if (nslot[type] >= CAL_MAX_SUBSTATES_CORE) {
+        set_error(CAL_ERROR_LIMIT, "too many substates of one type (limit 32)");
+        return -1;
+    }
+    const int slot = nslot[type];
+    Sub& q = sub[type][slot];
+    q.used = true;
+    q.single = single;
+    q.type = type;
+    q.elem = type_size(type);
+    const size_t bytes = (size_t)ncells * q.elem;
+    const int layers = single ? 1 : 2;
+    for (int l = 0; l < layers; l++) {
+        if (!cuda_ok(cudaMalloc(&q.layer[l].dev, bytes), "cudaMalloc substate"))
+            return -1;
+        if (!cuda_ok(cudaMemsetAsync(q.layer[l].dev, 0, bytes, stream), "memset substate"))
+            return -1;
+        if (!cuda_ok(cudaMallocHost(&q.host[l], bytes), "cudaMallocHost substate mirror"))
+            return -1;
+        memset(q.host[l], 0, bytes);
+        q.layer[l].host_valid = true;
+        q.layer[l].dev_valid = true;
+    }
+    *cur_mirror = q.host[0];
+    *next_mirror = single ? nullptr : q.host[1];
+    nslot[type]++;
+    return slot;
+}
+
+/* ---- coherence ---------------------------------------------------------- */
+
+bool CalGrid::to_device_all()
+{
+    for (int t = 0; t < CAL_NTYPES; t++)
+        for (int s = 0; s < nslot[t]; s++) {
+            Sub& q = sub[t][s];
+            for (int l = 0; l < (q.single ? 1 : 2); l++) {
+                if (q.layer[l].dev_valid)
+                    continue;
+                if (capturing) {
+                    set_error(CAL_ERROR_NOT_CAPTURABLE, "host data must be uploaded during graph capture");
+                    return false;
+                }
+                if (!cuda_ok(cudaMemcpyAsync(q.layer[l].dev, q.host[l], (size_t)ncells * q.elem,
+                                             cudaMemcpyHostToDevice, stream), "upload substate"))
+                    return false;
+                q.layer[l].dev_valid = true;
+                transfers++;
+            }
+        }
+    if (active && !flags_dev_valid) {
+        if (capturing) {
+            set_error(CAL_ERROR_NOT_CAPTURABLE, "active flags must be uploaded during graph capture");
+            return false;
+        }
+        if (!cuda_ok(cudaMemcpyAsync(d_flags, h_flags, (size_t)ncells, cudaMemcpyHostToDevice, stream),
+                     "upload flags"))
+            return false;
+        flags_dev_valid = true;
+        transfers++;
+    }
+    return true;
+}
+
+bool CalGrid::to_host(int type, int slot, int layer)
+{
+    Sub& q = sub[type][slot];
+    if (q.layer[layer].host_valid)
+        return true;
+    if (capturing) {
+        set_error(CAL_ERROR_NOT_CAPTURABLE, "host read of device data during graph capture");
+        return false;
+    }
+    if (layer == 1 && q.next_stale && !repair_stale(type, slot))
+        return false;
+    if (!cuda_ok(cudaMemcpyAsync(q.host[layer], q.layer[layer].dev, (size_t)ncells * q.elem,
+                                 cudaMemcpyDeviceToHost, stream), "download substate") ||
+        !cuda_ok(cudaStreamSynchronize(stream), "sync"))
+        return false;
+    q.layer[layer].host_valid = true;
+    transfers++;
+    return true;
+}
+
+bool CalGrid::flags_to_host()
+{
+    if (!active || flags_host_valid)
+        return true;
+    if (capturing) {
+        set_error(CAL_ERROR_NOT_CAPTURABLE, "host read of active flags during graph capture");
+        return false;
+    }
+    if (!cuda_ok(cudaMemcpyAsync(h_flags, d_flags, (size_t)ncells, cudaMemcpyDeviceToHost, stream), "download flags") ||
+        !cuda_ok(cudaStreamSynchronize(stream), "sync"))
+        return false;
+    flags_host_valid = true;
+    transfers++;
+    return true;
+}
+
+void CalGrid::host_wrote(int type, int slot, int layer)
+{
+    Sub& q = sub[type][slot];
+    q.layer[layer].dev_valid = false;
+    q.forced_dirty = true;
+}
+
+void CalGrid::device_wrote_all()
+{
+    written_since_update = true;
+    for (int t = 0; t < CAL_NTYPES; t++)
+        for (int s = 0; s < nslot[t]; s++) {
+            sub[t][s].layer[0].host_valid = false;
+            sub[t][s].layer[1].host_valid = false;
+        }
+    if (active)
+        flags_host_valid = false;
+}
+
+bool CalGrid::repair_stale(int type, int slot)
+{
+    Sub& q = sub[type][slot];
+    if (!q.next_stale)
+        return true;
+    if (!cuda_ok(cudaMemcpyAsync(q.layer[1].dev, q.layer[0].dev, (size_t)ncells * q.elem, cudaMemcpyDeviceToDevice,
+                                 stream), "repair next layer"))
+        return false;
+    q.next_stale = false;
+    q.layer[1].host_valid = false;
+    q.layer[1].dev_valid = true;
+    return true;
+}
+
+bool CalGrid::repair_all_stale()
+{
+    for (int t = 0; t < CAL_NTYPES; t++)
+        for (int s = 0; s < nslot[t]; s++)
+            if (!repair_stale(t, s))
+                return false;
+    return true;
+}
+
+/* ---- device operations ----------------------------------------------- */
+
+bool CalGrid::fill(int type, int slot, int layer, const void* value, bool at_active)
+{
+    Sub& q = sub[type][slot];
+    if (!q.used || (layer == 1 && q.single))
+        return true;
+    if (layer == 1 && !repair_stale(type, slot))
+        return false;
+    if (!to_device_all())
+        return false;
+    const int use = (at_active && active) ? 1 : 0;
+    const int g = grid_for(ncells);
+    void* buf = q.layer[layer].dev;
+    switch (type) {
+    case 0: k_fill<CALbyte><<<g, kThreads, 0, stream>>>((CALbyte*)buf, *(const CALbyte*)value, ncells, d_lin, d_count, use); break;
+    case 1: k_fill<CALint><<<g, kThreads, 0, stream>>>((CALint*)buf, *(const CALint*)value, ncells, d_lin, d_count, use); break;
+    default: k_fill<CALreal><<<g, kThreads, 0, stream>>>((CALreal*)buf, *(const CALreal*)value, ncells, d_lin, d_count, use); break;
+    }
+    if (!cuda_ok(cudaGetLastError(), "fill kernel"))
+        return false;
+    q.layer[layer].host_valid = false;
+    q.forced_dirty = true;
+    return true;
+}
+
+bool CalGrid::copy_next_to_current(const std::vector<std::pair<int, int>>& which, bool use_dirty, bool at_active)
+{
+    UpdateParams p;
+    memset(&p, 0, sizeof(p));
+    for (size_t w = 0; w < which.size(); w++) {
+        Sub& q = sub[which[w].first][which[w].second];
+        if (!q.used || q.single || q.next_stale)
+            continue;
+        const int e = p.n_entries++;
+        p.src[e] = q.layer[1].dev;
+        p.dst[e] = q.layer[0].dev;
+        p.elem[e] = (unsigned char)q.elem;
+        p.type[e] = (unsigned char)which[w].first;
+        p.slot[e] = (unsigned char)which[w].second;
+        if (q.forced_dirty)
+            p.forced[which[w].first] |= 1u << which[w].second;
+    }
+    if (p.n_entries == 0)
+        return true;
+    p.ncells = ncells;
+    p.dirty = d_dirty;
+    p.use_dirty = use_dirty ? 1 : 0;
+    p.at_active = (at_active && active) ? 1 : 0;
+    p.lin = d_lin;
+    p.count = d_count;
+    const long long work = p.at_active ? ncells : (ncells * 8) / 16;
+    k_update<<<grid_for(work), kThreads, 0, stream>>>(p);
+    if (!cuda_ok(cudaGetLastError(), "update kernel"))
+        return false;
+    for (size_t w = 0; w < which.size(); w++) {
+        Sub& q = sub[which[w].first][which[w].second];
+        if (!q.used || q.single || q.next_stale)
+            continue;
+        q.layer[0].host_valid = false;
+        q.forced_dirty = false;
+    }
+    return true;
+}
+
+bool CalGrid::compact()
+{
+    if (!active)
+        return true;
+    if (!to_device_all())
+        return false;
+    return cuda_ok(compact_flags(d_flags, dim, rows, cols, slices, d_cells, d_lin, d_count, d_block_counts,
+                                 n_blocks, stream),
+                   "active-cell compaction");
+}
+
+bool CalGrid::clear_dirty()
+{
+    return cuda_ok(cudaMemsetAsync(d_dirty, 0, 4 * sizeof(unsigned), stream), "clear written bits");
+}
+
+bool CalGrid::update_all()
+{
+    if (!to_device_all())
+        return false;
+    if (active && !compact())
+        return false;
+    std::vector<std::pair<int, int>> all;
+    for (int t = 0; t < CAL_NTYPES; t++)
+        for (int s = 0; s < nslot[t]; s++)
+            if (!sub[t][s].single)
+                all.push_back(std::make_pair(t, s));
+    /* without active cells, untouched substates are skipped (next == current
+     * everywhere); with them, every registered substate is copied */
+    if (!active && !written_since_update) {
+        bool forced = false;
+        for (size_t w = 0; w < all.size(); w++)
+            forced = forced || sub[all[w].first][all[w].second].forced_dirty;
+        if (!forced)
+            return true; /* nothing was written since the last update */
+    }
+    if (!copy_next_to_current(all, !active, true))
+        return false;
+    written_since_update = false;
+    return clear_dirty();
+}
+
+bool CalGrid::swap(int type, int slot)
+{
+    Sub& q = sub[type][slot];
+    if (!q.used || q.single)
+        return true;
+    Layer tmp = q.layer[0];
+    q.layer[0] = q.layer[1];
+    q.layer[1] = tmp;
+    q.layer[0].host_valid = false;
+    q.layer[1].host_valid = false;
+    q.next_stale = true;
+    swaps++;
+    return true;
+}
+
+bool CalGrid::sync()
+{
+    return cuda_ok(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+}
+
+void CalGrid::save(GridState* st) const
+{
+    memcpy(st->sub, sub, sizeof(sub));
+    st->flags_host_valid = flags_host_valid;
+    st->flags_dev_valid = flags_dev_valid;
+    st->transfers = transfers;
+    st->swaps = swaps;
+}
+
+void CalGrid::restore(const GridState* st)
+{
+    memcpy(sub, st->sub, sizeof(sub));
+    flags_host_valid = st->flags_host_valid;
+    flags_dev_valid = st->flags_dev_valid;
+    transfers = st->transfers;
+    swaps = st->swaps;
+}
+
+void CalGrid::launch_grid(int* gx, int* gy) const
+{
+    int x = (cols + 255) / 256;
+    if (x > 16)
+        x = 16;
+    const long long lines = (long long)rows * slices;
+    long long y = (152LL * 8 * 2) / x;
+    if (y > lines)
+        y = lines;
+    if (y > 65535)
+        y = 65535;
+    if (y < 1)
+        y = 1;
+    *gx = x;
+    *gy = (int)y;
+}
+
+} // namespace cal
+
+/* ======================= error API ====================================== */
+
+extern "C" enum CALError calGetLastError(void)
+{
+    return cal::g_err;
+}
+
+extern "C" const char* calGetErrorString(void)
+{
+    return cal::g_err == CAL_SUCCESS ? "no error" : cal::g_msg;
+}
+
+extern "C" void calClearError(void)
+{
+    cal::g_err = CAL_SUCCESS;
+    cal::g_msg[0] = 0;
+}

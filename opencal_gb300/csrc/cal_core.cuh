@@ -54,7 +54,14 @@ struct Sub {
     bool forced_dirty = false;
 };
 
-typedef int (*LaunchFn)(const void* desc, int gx, int gy, void* stream);
+/* host-side bookkeeping that a step may change; restored when a graph
+ * recording of the step is abandoned */
+struct GridState {
+    Sub sub[CAL_NTYPES][CAL_MAX_SUBSTATES_CORE];
+    bool flags_host_valid, flags_dev_valid;
+    int transfers;
+    long swaps;
+};
 
 struct CalGrid {
     int dim = 2;
@@ -80,7 +87,9 @@ struct CalGrid {
 
     unsigned* d_dirty = nullptr; /* [3] written-substate bits */
     int transfers = 0;           /* host<->device coherence copies made so far */
+    long swaps = 0;              /* pointer swaps made so far */
     int capturing = 0;
+    bool written_since_update = true; /* a process kernel may have set written bits */
 
     /* lifecycle */
     bool init(int dim, int rows, int cols, int slices, int toroidal, int active);
@@ -112,6 +121,8 @@ struct CalGrid {
         return dim == 2 ? (long long)i * cols + j : (long long)k * rows * cols + (long long)i * cols + j;
     }
     void launch_grid(int* gx, int* gy) const;
+    void save(GridState* st) const;
+    void restore(const GridState* st);
 };
 
 /* compaction of byte flags into the reference-ordered active list */

@@ -1,0 +1,23 @@
+/*
+ * cal_model_internal.cuh -- library-private device state hung off the public
+ * CALModel2D / CALModel3D structs (their `gpu` field).
+ */
+#pragma once
+
+#include "cal_core.cuh"
+#include "opencal/cal2D.h"
+#include "opencal/cal3D.h"
+
+struct CALGpuModel2D {
+    cal::CalGrid g;
+    struct CALCell2D* d_X = nullptr; /* device copy of the neighbourhood table */
+    int d_X_len = 0;                 /* entries uploaded; -1 forces an upload */
+    CALLaunchFunc2D launch[CAL_MAX_ELEMENTARY_PROCESSES];
+};
+
+struct CALGpuModel3D {
+    cal::CalGrid g;
+    struct CALCell3D* d_X = nullptr;
+    int d_X_len = 0;
+    CALLaunchFunc3D launch[CAL_MAX_ELEMENTARY_PROCESSES];
+};

@@ -1,0 +1,267 @@
+/*
+ * probes.cu -- small rules that exercise the engine's semantics, written as
+ * device elementary processes through the public API.  Each entry point has
+ * the same contract as the oracle's function of the same suffix
+ * (oracle/oracle_models.c), so the parity tests compare them directly.
+ *
+ *   nbprobe2d  v' = v/4 + sum_n v_n * n/64 on any 2D neighbourhood (exercises
+ *              the neighbour tables, including the hexagonal odd-column /
+ *              odd-row shift of OpenCAL-OMP/source/cal2D.c:859-870)
+ *   acprobe    three processes with SCIDDICA-T's active-cell structure,
+ *              2D or 3D (add on outflow, update, remove, steering on next)
+ *   life3d     OpenCAL/examples/cal_life3D-glut/source/life3D.cpp:70-83
+ */
+#include <string.h>
+
+#include "opencal/cal2D.h"
+#include "opencal/cal2DRun.h"
+#include "opencal/cal3D.h"
+#include "opencal/cal3DRun.h"
+
+static int finish2d(struct CALModel2D* ca, struct CALRun2D* run)
+{
+    int err = calGetLastError();
+    calRunFinalize2D(run);
+    calFinalize2D(ca);
+    return err;
+}
+
+static int finish3d(struct CALModel3D* ca, struct CALRun3D* run)
+{
+    int err = calGetLastError();
+    calRunFinalize3D(run);
+    calFinalize3D(ca);
+    return err;
+}
+
+/* ======================= neighbourhood probe ============================ */
+
+__managed__ struct CALSubstate2Dr* nbQ;
+
+CAL_ELEMENTARY_PROCESS_2D(nbprobe_rule)(struct CALModel2D* ca, int i, int j)
+{
+    double acc = calGet2Dr(ca, nbQ, i, j) * 0.25;
+    for (int n = 1; n < ca->sizeof_X; n++)
+        acc += calGetX2Dr(ca, nbQ, i, j, n) * ((double)n * 0.015625);
+    calSet2Dr(ca, nbQ, i, j, acc);
+}
+
+extern "C" int cal_nbprobe2d_run(int rows, int cols, int nbhd, int toroidal, int steps, const double* v0,
+                                 double* v_out, int graph)
+{
+    calClearError();
+    struct CALModel2D* ca = calCADef2D(rows, cols, (enum CALNeighborhood2D)nbhd,
+                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    if (!ca)
+        return calGetLastError();
+    struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
+    calAddElementaryProcess2D(ca, nbprobe_rule);
+    nbQ = calAddSubstate2Dr(ca);
+    const size_t bytes = sizeof(double) * (size_t)rows * cols;
+    memcpy(nbQ->current, v0, bytes);
+    memcpy(nbQ->next, v0, bytes);
+    calMarkHostDirty2D(ca);
+    calRunSetGraph2D(run, graph ? CAL_TRUE : CAL_FALSE);
+    if (steps > 0)
+        calRun2D(run);
+    calSync2D(ca);
+    memcpy(v_out, nbQ->current, bytes);
+    return finish2d(ca, run);
+}
+
+/* ======================= active-cell probe ============================== */
+
+struct acp2_t {
+    struct CALSubstate2Dr *v, *w;
+};
+struct acp3_t {
+    struct CALSubstate3Dr *v, *w;
+};
+__managed__ struct acp2_t A2;
+__managed__ struct acp3_t A3;
+__managed__ double acp_thr;
+
+CAL_ELEMENTARY_PROCESS_2D(acp2_ep1)(struct CALModel2D* ca, int i, int j)
+{
+    double c = calGet2Dr(ca, A2.v, i, j);
+    if (c <= acp_thr)
+        return;
+    for (int n = 1; n < ca->sizeof_X; n++)
+        if (calGetX2Dr(ca, A2.v, i, j, n) < c)
+            calAddActiveCellX2D(ca, i, j, n);
+    calSet2Dr(ca, A2.w, i, j, c * 0.125);
+}
+
+CAL_ELEMENTARY_PROCESS_2D(acp2_ep2)(struct CALModel2D* ca, int i, int j)
+{
+    double acc = calGet2Dr(ca, A2.v, i, j);
+    for (int n = 1; n < ca->sizeof_X; n++)
+        acc += calGetX2Dr(ca, A2.w, i, j, n) - calGet2Dr(ca, A2.w, i, j);
+    calSet2Dr(ca, A2.v, i, j, acc);
+}
+
+CAL_ELEMENTARY_PROCESS_2D(acp2_ep3)(struct CALModel2D* ca, int i, int j)
+{
+    if (calGet2Dr(ca, A2.v, i, j) <= acp_thr)
+        calRemoveActiveCell2D(ca, i, j);
+}
+
+static void acp2_init(struct CALModel2D* ca)
+{
+    calInitSubstate2Dr(ca, A2.w, 0);
+    for (int i = 0; i < ca->rows; i++)
+        for (int j = 0; j < ca->columns; j++)
+            if (calGet2Dr(ca, A2.v, i, j) > acp_thr)
+                calAddActiveCell2D(ca, i, j);
+}
+
+static void acp2_steer(struct CALModel2D* ca) { calInitSubstateNext2Dr(ca, A2.w, 0); }
+
+CAL_ELEMENTARY_PROCESS_3D(acp3_ep1)(struct CALModel3D* ca, int i, int j, int k)
+{
+    double c = calGet3Dr(ca, A3.v, i, j, k);
+    if (c <= acp_thr)
+        return;
+    for (int n = 1; n < ca->sizeof_X; n++)
+        if (calGetX3Dr(ca, A3.v, i, j, k, n) < c)
+            calAddActiveCellX3D(ca, i, j, k, n);
+    calSet3Dr(ca, A3.w, i, j, k, c * 0.125);
+}
+
+CAL_ELEMENTARY_PROCESS_3D(acp3_ep2)(struct CALModel3D* ca, int i, int j, int k)
+{
+    double acc = calGet3Dr(ca, A3.v, i, j, k);
+    for (int n = 1; n < ca->sizeof_X; n++)
+        acc += calGetX3Dr(ca, A3.w, i, j, k, n) - calGet3Dr(ca, A3.w, i, j, k);
+    calSet3Dr(ca, A3.v, i, j, k, acc);
+}
+
+CAL_ELEMENTARY_PROCESS_3D(acp3_ep3)(struct CALModel3D* ca, int i, int j, int k)
+{
+    if (calGet3Dr(ca, A3.v, i, j, k) <= acp_thr)
+        calRemoveActiveCell3D(ca, i, j, k);
+}
+
+static void acp3_init(struct CALModel3D* ca)
+{
+    calInitSubstate3Dr(ca, A3.w, 0);
+    for (int i = 0; i < ca->rows; i++)
+        for (int j = 0; j < ca->columns; j++)
+            for (int k = 0; k < ca->slices; k++)
+                if (calGet3Dr(ca, A3.v, i, j, k) > acp_thr)
+                    calAddActiveCell3D(ca, i, j, k);
+}
+
+static void acp3_steer(struct CALModel3D* ca) { calInitSubstateNext3Dr(ca, A3.w, 0); }
+
+extern "C" int cal_acprobe_run(int dim, int rows, int cols, int slices, int nbhd, int toroidal, int steps,
+                               double thr, const double* v0, double* v_out, long* n_active, int* cells_out, int graph)
+{
+    calClearError();
+    acp_thr = thr;
+    if (dim == 2) {
+        struct CALModel2D* ca = calCADef2D(rows, cols, (enum CALNeighborhood2D)nbhd,
+                                           toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_OPT_ACTIVE_CELLS);
+        if (!ca)
+            return calGetLastError();
+        struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
+        calAddElementaryProcess2D(ca, acp2_ep1);
+        calAddElementaryProcess2D(ca, acp2_ep2);
+        calAddElementaryProcess2D(ca, acp2_ep3);
+        A2.v = calAddSubstate2Dr(ca);
+        A2.w = calAddSubstate2Dr(ca);
+        const size_t bytes = sizeof(double) * (size_t)rows * cols;
+        memcpy(A2.v->current, v0, bytes);
+        memcpy(A2.v->next, v0, bytes);
+        calMarkHostDirty2D(ca);
+        calRunAddInitFunc2D(run, acp2_init);
+        calRunAddSteeringFunc2D(run, acp2_steer);
+        calRunSetGraph2D(run, graph ? CAL_TRUE : CAL_FALSE);
+        if (steps > 0)
+            calRun2D(run);
+        else
+            calRunInitSimulation2D(run);
+        calSync2D(ca);
+        memcpy(v_out, A2.v->current, bytes);
+        if (n_active)
+            *n_active = ca->A.size_current;
+        if (cells_out && ca->A.size_current > 0)
+            memcpy(cells_out, ca->A.cells, sizeof(int) * 2 * (size_t)ca->A.size_current);
+        return finish2d(ca, run);
+    }
+    struct CALModel3D* ca = calCADef3D(rows, cols, slices, (enum CALNeighborhood3D)nbhd,
+                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_OPT_ACTIVE_CELLS);
+    if (!ca)
+        return calGetLastError();
+    struct CALRun3D* run = calRunDef3D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
+    calAddElementaryProcess3D(ca, acp3_ep1);
+    calAddElementaryProcess3D(ca, acp3_ep2);
+    calAddElementaryProcess3D(ca, acp3_ep3);
+    A3.v = calAddSubstate3Dr(ca);
+    A3.w = calAddSubstate3Dr(ca);
+    const size_t bytes = sizeof(double) * (size_t)rows * cols * slices;
+    memcpy(A3.v->current, v0, bytes);
+    memcpy(A3.v->next, v0, bytes);
+    calMarkHostDirty3D(ca);
+    calRunAddInitFunc3D(run, acp3_init);
+    calRunAddSteeringFunc3D(run, acp3_steer);
+    calRunSetGraph3D(run, graph ? CAL_TRUE : CAL_FALSE);
+    if (steps > 0)
+        calRun3D(run);
+    else
+        calRunInitSimulation3D(run);
+    calSync3D(ca);
+    memcpy(v_out, A3.v->current, bytes);
+    if (n_active)
+        *n_active = ca->A.size_current;
+    if (cells_out && ca->A.size_current > 0)
+        memcpy(cells_out, ca->A.cells, sizeof(int) * 3 * (size_t)ca->A.size_current);
+    return finish3d(ca, run);
+}
+
+/* ======================= Life 3D ======================================== */
+
+__managed__ struct CALSubstate3Db* L3;
+__managed__ int L3rule[4];
+
+CAL_ELEMENTARY_PROCESS_3D(life3d_rule)(struct CALModel3D* ca, int i, int j, int k)
+{
+    int sum = 0, n;
+    CALbyte alive = calGet3Db(ca, L3, i, j, k);
+    CALbyte nextState = alive;
+    for (n = 0; n < ca->sizeof_X; n++)
+        sum += calGetX3Db(ca, L3, i, j, k, n);
+    if (alive && (sum < L3rule[0] || sum > L3rule[1]))
+        nextState = 0;
+    else if (!alive && (sum >= L3rule[2] && sum <= L3rule[3]))
+        nextState = 1;
+    calSet3Db(ca, L3, i, j, k, nextState);
+}
+
+extern "C" int cal_life3d_run(int rows, int cols, int slices, int nbhd, int toroidal, int steps, int r1, int r2,
+                              int r3, int r4, const unsigned char* s0, unsigned char* s_out, int graph)
+{
+    calClearError();
+    struct CALModel3D* ca = calCADef3D(rows, cols, slices, (enum CALNeighborhood3D)nbhd,
+                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    if (!ca)
+        return calGetLastError();
+    struct CALRun3D* run = calRunDef3D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
+    L3rule[0] = r1;
+    L3rule[1] = r2;
+    L3rule[2] = r3;
+    L3rule[3] = r4;
+    calAddElementaryProcess3D(ca, life3d_rule);
+    L3 = calAddSubstate3Db(ca);
+    const long long n = (long long)rows * cols * slices;
+    for (long long c = 0; c < n; c++)
+        L3->current[c] = L3->next[c] = (CALbyte)s0[c];
+    calMarkHostDirty3D(ca);
+    calRunSetGraph3D(run, graph ? CAL_TRUE : CAL_FALSE);
+    if (steps > 0)
+        calRun3D(run);
+    calSync3D(ca);
+    for (long long c = 0; c < n; c++)
+        s_out[c] = (unsigned char)L3->current[c];
+    return finish3d(ca, run);
+}
