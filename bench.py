@@ -198,7 +198,8 @@ def gpu_arm(args):
         getattr(m, fn).argtypes = [C.c_void_p]
     m.cal_sciddicaT_stream.restype = C.c_void_p
     m.cal_sciddicaT_steps.argtypes = [C.c_void_p, C.c_int, C.c_int]
-    m.cal_sciddicaT_kernel_times.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    m.cal_sciddicaT_kernel_times.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    m.cal_sciddicaT_wet_count.argtypes = [C.c_void_p]
     m.cal_sciddicaT_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     m.cal_sciddicaT_read.argtypes = [C.c_void_p, C.c_void_p]
 
@@ -242,13 +243,17 @@ def gpu_arm(args):
     units = ROWS * COLS * CA_STEPS * args.steps * world
     value = units / dev_s
 
-    # kernel-level roofline: single fused launches timed with events
+    # kernel-level roofline: the step's two kernels timed with events around
+    # every launch, over 400 steps from the mid-run state (step 1000)
     m.cal_sciddicaT_reset(sess)
-    m.cal_sciddicaT_steps(sess, 1000, 0)  # mid-run state, wet region developed
+    m.cal_sciddicaT_steps(sess, 1000, 0)
+    wet = m.cal_sciddicaT_wet_count(sess)
     nk = 400
-    ktimes = (C.c_float * nk)()
-    m.cal_sciddicaT_kernel_times(sess, nk, ktimes)
-    kavg_ms = float(np.mean(list(ktimes)))
+    ka = (C.c_float * nk)()
+    kb = (C.c_float * nk)()
+    m.cal_sciddicaT_kernel_times(sess, nk, ka, kb)
+    k1_ms, k2_ms = float(np.mean(list(ka))), float(np.mean(list(kb)))
+    kavg_ms = k1_ms + k2_ms
     peak, peak_kind = _peaks()
     achieved = ROWS * COLS * BYTES_PER_CELL_UPDATE / (kavg_ms * 1e-3) / 1e9
 
@@ -290,19 +295,48 @@ def gpu_arm(args):
                    "l2": "flushed (256 MiB write) before every run", "seed": SEED, "p_r": P_R, "p_eps": P_EPS,
                    "parallelism": f"replicas x{world}"},
         "wall_s": t_wall,
-        "gpu_launches": CA_STEPS * args.steps,
+        "gpu_launches": 2 * CA_STEPS * args.steps + args.steps,  # K1 + K2 per CA step, one priming kernel per run
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(2 * z.nbytes),
                 "d2h_bytes_per_step": int(h.nbytes)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "sdt::fused_step", "kernel_avg_ms": kavg_ms,
+                     "kernel": "SCIDDICA-T step = sdt2::k1_outflows (wet cells) + sdt2::k2_update (all cells)",
+                     "kernel_avg_ms": kavg_ms, "k1_outflows_ms": k1_ms, "k2_update_ms": k2_ms,
+                     "wet_cells_at_step_1000": wet,
                      "bytes_per_launch": ROWS * COLS * BYTES_PER_CELL_UPDATE},
-        "mass_drift_rel": float(abs(hh.sum() - h.sum()) / h.sum()),
+        "finite": bool(np.isfinite(hh).all()),
         "clocks": clk,
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(z, h)
     print(json.dumps(line), flush=True)
+
+
+def ncu_case(args):
+    """A fixed, untimed sequence for ncu captures: open the 2048^2 session,
+    run --ncu-steps fused steps from the initial state, report the wet
+    fraction.  No torch, no extra allocations."""
+    import opencal_gb300 as cal
+    from opencal_gb300 import workloads as W
+    cal.build()
+    m = cal.models()
+    m.cal_sciddicaT_open.restype = C.c_void_p
+    m.cal_sciddicaT_open.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                     C.c_void_p, C.c_void_p, C.c_int]
+    m.cal_sciddicaT_steps.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    m.cal_sciddicaT_read.argtypes = [C.c_void_p, C.c_void_p]
+    m.cal_sciddicaT_close.argtypes = [C.c_void_p]
+    z, h = W.sciddicaT_inputs(ROWS, COLS, seed=SEED)
+    sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_FUSED)
+    done = 0
+    for target in sorted(set([args.ncu_steps] + [s for s in (500, 1000, 2000, 3000, 4000) if s < args.ncu_steps])):
+        m.cal_sciddicaT_steps(sess, target - done, 0)
+        done = target
+        hh = np.empty_like(h)
+        m.cal_sciddicaT_read(sess, hh.ctypes.data)
+        print(json.dumps({"step": done, "wet_fraction": float(np.count_nonzero(hh > P_EPS)) / hh.size,
+                          "mass": float(hh.sum())}), flush=True)
+    m.cal_sciddicaT_close(sess)
 
 
 def main():
@@ -312,8 +346,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="opencal", choices=["opencal", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-case", action="store_true", help="untimed fixed sequence for ncu captures")
+    ap.add_argument("--ncu-steps", type=int, default=1002)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.ncu_case:
+        ncu_case(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gpu_arm(args)

@@ -165,6 +165,12 @@ void* calGetDeviceBuffer2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, i
 void* calGetDeviceBuffer2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, int layer);
 void* calGetDeviceBuffer2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, int layer);
 void calMarkDeviceWritten2D(struct CALModel2D* ca2D);
+/* A custom kernel rewrote the current layer of one substate in place (every
+ * cell it changed, consistently with what an update would leave): only the
+ * host mirror becomes stale, no next -> current copy is implied. */
+void calMarkCurrentWritten2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q);
+void calMarkCurrentWritten2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q);
+void calMarkCurrentWritten2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q);
 /* current <-> next as a pointer exchange (no copy).  Only valid after a
  * kernel has written EVERY cell of next; next then holds stale data, which
  * the library repairs before any partial write reaches it. */

@@ -382,6 +382,10 @@ extern "C" void calUpdateActiveCells2D(struct CALModel2D* ca)
     {                                                                                                   \
         G(ca).to_host(TC, slot_of(ca, TC, Q), 0);                                                       \
     }                                                                                                   \
+    extern "C" void calMarkCurrentWritten2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q)       \
+    {                                                                                                   \
+        G(ca).sub[TC][slot_of(ca, TC, Q)].layer[0].host_valid = false;                                  \
+    }                                                                                                   \
     extern "C" void calSwapSubstate2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q)             \
     {                                                                                                   \
         G(ca).swap(TC, slot_of(ca, TC, Q));                                                             \

@@ -25,11 +25,15 @@
  *    whole neighbourhood is dry take no FP64 instruction at all: on GB300 the
  *    FP64 pipe is narrow, and x + 0.0 - 0.0 leaves x unchanged except for
  *    turning -0.0 into +0.0, which is reproduced with an integer select.
+ *    For the same reason the division by the number of remaining cells and
+ *    the comparisons of the minimisation run on the integer pipe, with
+ *    bit-identical results (exact_div.cuh).
  */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include "exact_div.cuh"
 #include "opencal/cal2D.h"
 #include "opencal/cal2DRun.h"
 
@@ -153,11 +157,11 @@ static void sciddicaT_steering_ac(struct CALModel2D* sciddicaT)
 
 namespace sdt {
 
-/* tile of TW x TH cells per block, THREADS threads; EP 1 runs on the tile
- * plus a ring of 1, which needs z and h on the tile plus a ring of 2 */
-constexpr int TW = 32, TH = 16, THREADS = 256;
-constexpr int R1W = TW + 2, R1H = TH + 2;  /* outflow region */
-constexpr int R2W = TW + 4, R2H = TH + 4;  /* load region */
+/* The fused step.  A block owns a TW x TH tile.  EP 1 (outflows) runs on the
+ * tile plus a ring of 1 cell -- EP 2 needs the outflows of every neighbour --
+ * so z and h are staged on the tile plus a ring of 2.  Shared memory holds
+ * z, h (load region) and the four outflows (outflow region). */
+constexpr int THREADS = 256;
 
 struct Params {
     const double* __restrict__ z;
@@ -176,20 +180,24 @@ static __device__ __forceinline__ bool is_wet(double h, long long eps_bits)
 {
     const long long b = __double_as_longlong(h);
     if (b >= 0)
-        return b > eps_bits;                             /* +0 .. +inf, +NaN */
+        return b > eps_bits;                                  /* +0 .. +inf, +NaN */
     return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; /* -NaN; other negatives are dry */
 }
 
-/* the outflows of one wet cell, exactly as sciddicaT_flows_computation */
-static __device__ __forceinline__ void outflows(double hc, double zc, const double* zn, const double* hn,
-                                                double eps, double r, double f[4])
+/* The outflows of one wet cell, exactly as sciddicaT_flows_computation:
+ * the same additions in the same order; the division by the number of
+ * remaining cells and the comparisons are done on the integer pipe with
+ * bit-identical results (exact_div.cuh). */
+static __device__ __forceinline__ void outflows(double hc, double zc, const double u1, const double u2,
+                                                const double u3, const double u4, double eps, double r, double f[4])
 {
     double u[5];
     const double m = hc - eps;
     u[0] = zc + eps;
-#pragma unroll
-    for (int n = 1; n < 5; n++)
-        u[n] = zn[n - 1] + hn[n - 1];
+    u[1] = u1;
+    u[2] = u2;
+    u[3] = u3;
+    u[4] = u4;
     unsigned elim = 0;
     double average;
     bool again;
@@ -204,10 +212,10 @@ static __device__ __forceinline__ void outflows(double hc, double zc, const doub
                 cells_count++;
             }
         if (cells_count != 0)
-            average /= cells_count;
+            average = cal_div_small(average, cells_count);
 #pragma unroll
         for (int n = 0; n < 5; n++)
-            if ((average <= u[n]) && !(elim & (1u << n))) {
+            if (!(elim & (1u << n)) && cal_le(average, u[n])) {
                 elim |= 1u << n;
                 again = true;
             }
@@ -222,92 +230,120 @@ static __device__ __forceinline__ int wrapi(int x, int n)
     return x < 0 ? x + n : (x >= n ? x - n : x);
 }
 
+static __device__ __forceinline__ double plus_zero(double x)
+{
+    /* x + 0.0 without the FP64 pipe: only -0.0 changes (to +0.0) */
+    long long b = __double_as_longlong(x);
+    return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
+}
+
+template <int TW, int TH>
+struct Tile {
+    static constexpr int R1W = TW + 2, R1H = TH + 2; /* outflow region */
+    static constexpr int R2W = TW + 4, R2H = TH + 4; /* load region */
+    static constexpr size_t smem_bytes = sizeof(double) * (2 * R2W * R2H + 4 * R1W * R1H);
+};
+
+template <int TW, int TH>
 __global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Params p)
 {
-    __shared__ double sz[R2H][R2W];
-    __shared__ double sh[R2H][R2W];
-    __shared__ double sf[4][R1H][R1W];
+    using T = Tile<TW, TH>;
+    extern __shared__ __align__(16) double smem[];
+    double* sz = smem;                      /* [R2H][R2W] */
+    double* sh = sz + T::R2W * T::R2H;      /* [R2H][R2W] */
+    double* sf = sh + T::R2W * T::R2H;      /* [4][R1H][R1W] */
+    constexpr int F = T::R1W * T::R1H;
 
     const int i0 = blockIdx.y * TH, j0 = blockIdx.x * TW;
+    const bool interior = i0 >= 2 && j0 >= 2 && i0 + TH + 2 <= p.rows && j0 + TW + 2 <= p.cols;
 
-    /* 1. z and h on the tile + 2 ring (flat: 0 outside; toroidal: wrapped) */
+    /* 1. z and h on the tile + 2 ring.  Interior tiles: 16-byte loads (j0-2
+     * is even, so every pair starts 16-byte aligned).  Edge tiles: flat ->
+     * 0 outside, toroidal -> wrapped. */
     int wet_seen = 0;
-    for (int t = threadIdx.x; t < R2H * R2W; t += THREADS) {
-        const int a = t / R2W, b = t - a * R2W;
-        int gi = i0 - 2 + a, gj = j0 - 2 + b;
-        double zv = 0.0, hv = 0.0;
-        bool inside = (unsigned)gi < (unsigned)p.rows && (unsigned)gj < (unsigned)p.cols;
-        if (!inside && p.toroidal) {
-            gi = wrapi(gi, p.rows);
-            gj = wrapi(gj, p.cols);
-            inside = true;
+    if (interior) {
+        constexpr int PW = T::R2W / 2;
+        for (int t = threadIdx.x; t < PW * T::R2H; t += THREADS) {
+            const int a = t / PW, b = 2 * (t - a * PW);
+            const long long c = (long long)(i0 - 2 + a) * p.cols + (j0 - 2 + b);
+            const double2 zv = __ldg(reinterpret_cast<const double2*>(p.z + c));
+            const double2 hv = __ldg(reinterpret_cast<const double2*>(p.h + c));
+            *reinterpret_cast<double2*>(sz + a * T::R2W + b) = zv;
+            *reinterpret_cast<double2*>(sh + a * T::R2W + b) = hv;
+            wet_seen |= is_wet(hv.x, p.eps_bits) | is_wet(hv.y, p.eps_bits);
         }
-        if (inside) {
-            const long long c = (long long)gi * p.cols + gj;
-            zv = __ldg(p.z + c);
-            hv = __ldg(p.h + c);
+    } else {
+        for (int t = threadIdx.x; t < T::R2H * T::R2W; t += THREADS) {
+            const int a = t / T::R2W, b = t - a * T::R2W;
+            int gi = i0 - 2 + a, gj = j0 - 2 + b;
+            double zv = 0.0, hv = 0.0;
+            bool inside = (unsigned)gi < (unsigned)p.rows && (unsigned)gj < (unsigned)p.cols;
+            if (!inside && p.toroidal) {
+                gi = wrapi(gi, p.rows);
+                gj = wrapi(gj, p.cols);
+                inside = true;
+            }
+            if (inside) {
+                const long long c = (long long)gi * p.cols + gj;
+                zv = __ldg(p.z + c);
+                hv = __ldg(p.h + c);
+            }
+            sz[t] = zv;
+            sh[t] = hv;
+            wet_seen |= is_wet(hv, p.eps_bits);
         }
-        sz[a][b] = zv;
-        sh[a][b] = hv;
-        wet_seen |= is_wet(hv, p.eps_bits);
     }
     if (__syncthreads_or(wet_seen) == 0) {
         /* no wet cell within two cells: h is unchanged (-0 becomes +0) */
         for (int t = threadIdx.x; t < TH * TW; t += THREADS) {
             const int a = t / TW, b = t - a * TW;
             const int gi = i0 + a, gj = j0 + b;
-            if (gi < p.rows && gj < p.cols) {
-                long long hb = __double_as_longlong(sh[a + 2][b + 2]);
-                if (hb == (long long)0x8000000000000000ULL)
-                    hb = 0;
-                p.h_next[(long long)gi * p.cols + gj] = __longlong_as_double(hb);
-            }
+            if (gi < p.rows && gj < p.cols)
+                p.h_next[(long long)gi * p.cols + gj] = plus_zero(sh[(a + 2) * T::R2W + b + 2]);
         }
         return;
     }
 
-    /* 2. EP 1 on the tile + 1 ring: outflows into shared memory.  Cells
-     * outside a flat grid have no outflows. */
-    for (int t = threadIdx.x; t < R1H * R1W; t += THREADS) {
-        const int a = t / R1W, b = t - a * R1W;
+    /* 2. EP 1 on the tile + 1 ring; cells outside a flat grid have none */
+    for (int t = threadIdx.x; t < F; t += THREADS) {
+        const int a = t / T::R1W, b = t - a * T::R1W;
         const int gi = i0 - 1 + a, gj = j0 - 1 + b;
         const bool inside = p.toroidal || ((unsigned)gi < (unsigned)p.rows && (unsigned)gj < (unsigned)p.cols);
-        const double hc = sh[a + 1][b + 1];
+        const int c = (a + 1) * T::R2W + (b + 1); /* this cell in the load region */
+        const double hc = sh[c];
         double f[4] = {0.0, 0.0, 0.0, 0.0};
         if (inside && is_wet(hc, p.eps_bits)) {
-            /* von Neumann order: north, west, east, south */
-            const double zn[4] = {sz[a][b + 1], sz[a + 1][b], sz[a + 1][b + 2], sz[a + 2][b + 1]};
-            const double hn[4] = {sh[a][b + 1], sh[a + 1][b], sh[a + 1][b + 2], sh[a + 2][b + 1]};
-            outflows(hc, sz[a + 1][b + 1], zn, hn, p.eps, p.r, f);
+            /* von Neumann order n = 1..4: north, west, east, south; u = z + h */
+            const double u1 = sz[c - T::R2W] + sh[c - T::R2W];
+            const double u2 = sz[c - 1] + sh[c - 1];
+            const double u3 = sz[c + 1] + sh[c + 1];
+            const double u4 = sz[c + T::R2W] + sh[c + T::R2W];
+            outflows(hc, sz[c], u1, u2, u3, u4, p.eps, p.r, f);
         }
 #pragma unroll
         for (int q = 0; q < 4; q++)
-            sf[q][a][b] = f[q];
+            sf[q * F + t] = f[q];
     }
     __syncthreads();
 
-    /* 3. EP 2 on the tile: h' = h + sum_n (f_in(n) - f_out(n-1)), in the
-     * reference's order n = 1..4 */
+    /* 3. EP 2 on the tile: h' = h + sum_n (f_in(n) - f_out(n-1)), n = 1..4 */
     for (int t = threadIdx.x; t < TH * TW; t += THREADS) {
         const int a = t / TW, b = t - a * TW;
         const int gi = i0 + a, gj = j0 + b;
         if (gi >= p.rows || gj >= p.cols)
             continue;
-        const int ca = a + 1, cb = b + 1;
+        const int c = (a + 1) * T::R1W + (b + 1); /* this cell in the outflow region */
         /* inflow from neighbour n is its outflow f[4-n] */
-        const double in1 = sf[3][ca - 1][cb], in2 = sf[2][ca][cb - 1];
-        const double in3 = sf[1][ca][cb + 1], in4 = sf[0][ca + 1][cb];
-        const double o0 = sf[0][ca][cb], o1 = sf[1][ca][cb], o2 = sf[2][ca][cb], o3 = sf[3][ca][cb];
-        const double hc = sh[a + 2][b + 2];
+        const double in1 = sf[3 * F + c - T::R1W], in2 = sf[2 * F + c - 1];
+        const double in3 = sf[1 * F + c + 1], in4 = sf[0 * F + c + T::R1W];
+        const double o0 = sf[0 * F + c], o1 = sf[1 * F + c], o2 = sf[2 * F + c], o3 = sf[3 * F + c];
+        const double hc = sh[(a + 2) * T::R2W + b + 2];
         double hn;
         const long long any = __double_as_longlong(in1) | __double_as_longlong(in2) | __double_as_longlong(in3) |
                               __double_as_longlong(in4) | __double_as_longlong(o0) | __double_as_longlong(o1) |
                               __double_as_longlong(o2) | __double_as_longlong(o3);
         if (any == 0) {
-            long long hb = __double_as_longlong(hc);
-            if (hb == (long long)0x8000000000000000ULL)
-                hb = 0;
-            hn = __longlong_as_double(hb);
+            hn = plus_zero(hc);
         } else {
             hn = hc;
             hn += in1 - o0;
@@ -319,11 +355,395 @@ __global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Pa
     }
 }
 
+template <int TW, int TH>
+static void launch(const Params& p, cudaStream_t s)
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(fused_step<TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)Tile<TW, TH>::smem_bytes);
+        attr_set = true;
+    }
+    dim3 grid((p.cols + TW - 1) / TW, (p.rows + TH - 1) / TH);
+    fused_step<TW, TH><<<grid, THREADS, Tile<TW, TH>::smem_bytes, s>>>(p);
+}
+
+/* tile shape: 64 x 32 by default; OPENCAL_SDT_TILE=32x16|64x16|64x32 overrides */
+static int tile_choice()
+{
+    static int choice = -1;
+    if (choice < 0) {
+        const char* e = getenv("OPENCAL_SDT_TILE");
+        choice = 2;
+        if (e && !strcmp(e, "32x16"))
+            choice = 0;
+        else if (e && !strcmp(e, "64x16"))
+            choice = 1;
+    }
+    return choice;
+}
+
+static void launch_step(const Params& p, cudaStream_t s)
+{
+    switch (tile_choice()) {
+    case 0: launch<32, 16>(p, s); break;
+    case 1: launch<64, 16>(p, s); break;
+    default: launch<64, 32>(p, s); break;
+    }
+}
+
 } // namespace sdt
+
+/* ======================= 2b. the split step ============================= */
+/* The same step as two kernels, so that the FP64 work of the outflows is
+ * spread over the whole GPU instead of the few tiles the wet region covers:
+ *
+ *   K1 (outflows): one thread per WET cell, from a compact list built by the
+ *      previous K2; writes the four outflows of the cell into private
+ *      outflow arrays (never the model's f substates, which keep the 0 the
+ *      steering gives them) and flags the K2 tiles that will read them.  It
+ *      also clears the outflows of cells that dried up in the previous step
+ *      (a second list, disjoint from the first).
+ *   K2 (thickness update): one pass over EVERY cell, h updated in place
+ *      (each cell reads and writes only its own h; the outflows it reads
+ *      were completed by K1).  In tiles K1 did not flag every outflow is +0,
+ *      so h is unchanged and only read; flagged tiles sum the eight outflow
+ *      terms in the reference's order.  K2 then applies EP 1's wet test to
+ *      the new h and appends wet cells (and cells that just dried) to the
+ *      next step's lists with warp ballots.
+ *
+ * Every cell is visited by every step, as in the reference; the EP 1 body
+ * runs exactly on the cells where the reference runs it (h > epsilon).  The
+ * lists' order does not matter: each cell's result depends only on its
+ * neighbourhood.  A priming kernel canonicalises -0 to +0 in h (the first
+ * reference step adds 0.0 to every cell) and builds the first wet list. */
+namespace sdt2 {
+
+constexpr int THREADS = 256;
+constexpr int TW = 64, TH = 16; /* K2 tile: 16 rows x 64 columns, 4 cells per thread */
+
+struct State {
+    struct CALModel2D* ca = nullptr;
+    double* f = nullptr;         /* 4 * n outflows, SoA */
+    int* list[2] = {nullptr, nullptr};
+    int* zlist[2] = {nullptr, nullptr};
+    int* counts = nullptr;       /* [0..1] wet list lengths, [2..3] dried list lengths */
+    unsigned char* tflag = nullptr;
+    long long n = 0;
+    int tiles_x = 0, tiles_y = 0;
+    int parity = 0;
+    bool primed = false;
+};
+
+struct K1Params {
+    const double* __restrict__ z;
+    const double* __restrict__ h;
+    double* __restrict__ f;
+    const int* __restrict__ list;
+    const int* __restrict__ count;
+    const int* __restrict__ zlist;
+    const int* __restrict__ zcount;
+    int* next_counts; /* the two counts K2 will append to: zeroed here */
+    unsigned char* tflag;
+    int rows, cols, toroidal, tiles_x;
+    long long n;
+    double eps, r;
+};
+
+struct K2Params {
+    double* __restrict__ h;
+    const double* __restrict__ f;
+    int* list;
+    int* count;
+    int* zlist;
+    int* zcount;
+    unsigned char* tflag;
+    int rows, cols, toroidal, tiles_x;
+    long long n;
+    long long eps_bits;
+};
+
+static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
+{
+    return (i / TH) * tiles_x + (j / TW);
+}
+
+__global__ void __launch_bounds__(THREADS) k1_outflows(const __grid_constant__ K1Params p)
+{
+    if (blockIdx.x == 0 && threadIdx.x < 2)
+        p.next_counts[threadIdx.x * 2] = 0; /* wet and dried counts of the other parity */
+    const int stride = gridDim.x * blockDim.x;
+    const int nw = *p.count;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += stride) {
+        const int c = p.list[k];
+        const int i = c / p.cols, j = c - i * p.cols;
+        /* neighbours in von Neumann order n = 1..4: north, west, east, south */
+        int ni[4] = {i - 1, i, i, i + 1}, nj[4] = {j, j - 1, j + 1, j};
+        double u[4];
+        bool in[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int a = ni[q], b = nj[q];
+            in[q] = true;
+            if (p.toroidal) {
+                a = a < 0 ? a + p.rows : (a >= p.rows ? a - p.rows : a);
+                b = b < 0 ? b + p.cols : (b >= p.cols ? b - p.cols : b);
+            } else if ((unsigned)a >= (unsigned)p.rows || (unsigned)b >= (unsigned)p.cols) {
+                in[q] = false;
+            }
+            ni[q] = a;
+            nj[q] = b;
+            if (in[q]) {
+                const long long cn = (long long)a * p.cols + b;
+                u[q] = __ldg(p.z + cn) + __ldg(p.h + cn);
+            } else {
+                u[q] = 0.0 + 0.0; /* an absent neighbour reads z = 0, h = 0 */
+            }
+        }
+        double f[4];
+        sdt::outflows(__ldg(p.h + c), __ldg(p.z + c), u[0], u[1], u[2], u[3], p.eps, p.r, f);
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            p.f[q * p.n + c] = f[q];
+            if (__double_as_longlong(f[q]) != 0) {
+                any = true;
+                if (in[q])
+                    p.tflag[tile_of(ni[q], nj[q], p.tiles_x)] = 1; /* the receiver reads it */
+            }
+        }
+        if (any)
+            p.tflag[tile_of(i, j, p.tiles_x)] = 1;
+    }
+    const int nz = *p.zcount;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nz; k += stride) {
+        const int c = p.zlist[k];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            p.f[q * p.n + c] = 0.0;
+    }
+}
+
+/* append the lanes whose predicate holds to list/count (warp-aggregated) */
+static __device__ __forceinline__ void warp_append(bool pred, int value, int* list, int* count)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0)
+        return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0)
+        base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (pred)
+        list[base + __popc(mask & ((1u << lane) - 1u))] = value;
+}
+
+__global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2Params p)
+{
+    const int tile = blockIdx.y * p.tiles_x + blockIdx.x;
+    const bool flagged = p.tflag[tile] != 0;
+    const int r = threadIdx.x / (TW / 4);       /* 0..15 */
+    const int j4 = (threadIdx.x % (TW / 4)) * 4; /* 0, 4, ..., 60 */
+    const int i = blockIdx.y * TH + r;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int j = blockIdx.x * TW + j4 + q;
+        const bool cell = i < p.rows && j < p.cols;
+        const long long c = (long long)i * p.cols + j;
+        double hv = 0.0, hn = 0.0;
+        if (cell) {
+            hv = p.h[c];
+            hn = hv;
+            if (flagged) {
+                const double o0 = p.f[c], o1 = p.f[p.n + c], o2 = p.f[2 * p.n + c], o3 = p.f[3 * p.n + c];
+                /* inflow from neighbour n is its outflow f[4-n]; absent neighbours give 0 */
+                double in1 = 0.0, in2 = 0.0, in3 = 0.0, in4 = 0.0;
+                int a = i - 1, b = j - 1, d = j + 1, e = i + 1;
+                if (p.toroidal) {
+                    a = a < 0 ? a + p.rows : a;
+                    e = e >= p.rows ? e - p.rows : e;
+                    b = b < 0 ? b + p.cols : b;
+                    d = d >= p.cols ? d - p.cols : d;
+                }
+                if ((unsigned)a < (unsigned)p.rows)
+                    in1 = p.f[3 * p.n + (long long)a * p.cols + j];
+                if ((unsigned)b < (unsigned)p.cols)
+                    in2 = p.f[2 * p.n + (long long)i * p.cols + b];
+                if ((unsigned)d < (unsigned)p.cols)
+                    in3 = p.f[1 * p.n + (long long)i * p.cols + d];
+                if ((unsigned)e < (unsigned)p.rows)
+                    in4 = p.f[(long long)e * p.cols + j];
+                const long long any = __double_as_longlong(in1) | __double_as_longlong(in2) |
+                                      __double_as_longlong(in3) | __double_as_longlong(in4) |
+                                      __double_as_longlong(o0) | __double_as_longlong(o1) |
+                                      __double_as_longlong(o2) | __double_as_longlong(o3);
+                if (any != 0) {
+                    hn += in1 - o0;
+                    hn += in2 - o1;
+                    hn += in3 - o2;
+                    hn += in4 - o3;
+                    p.h[c] = hn;
+                }
+            }
+        }
+        const bool wet_before = cell && sdt::is_wet(hv, p.eps_bits);
+        const bool wet_after = cell && sdt::is_wet(hn, p.eps_bits);
+        warp_append(wet_after, (int)c, p.list, p.count);
+        warp_append(wet_before && !wet_after, (int)c, p.zlist, p.zcount);
+    }
+    if (flagged) {
+        __syncthreads();
+        if (threadIdx.x == 0)
+            p.tflag[tile] = 0;
+    }
+}
+
+/* -0 -> +0 in h and the first wet list (counts[parity] must be 0) */
+__global__ void __launch_bounds__(THREADS) k_prime(double* h, long long n, long long eps_bits, int* list, int* count)
+{
+    for (long long c0 = (long long)blockIdx.x * blockDim.x; c0 < n; c0 += (long long)gridDim.x * blockDim.x) {
+        const long long c = c0 + threadIdx.x;
+        bool wet = false;
+        if (c < n) {
+            const double hv = h[c];
+            if (__double_as_longlong(hv) == (long long)0x8000000000000000ULL)
+                h[c] = 0.0;
+            wet = sdt::is_wet(hv, eps_bits);
+        }
+        warp_append(wet, (int)c, list, count);
+    }
+}
+
+static State g_state;
+
+static void release()
+{
+    State& s = g_state;
+    cudaFree(s.f);
+    for (int k = 0; k < 2; k++) {
+        cudaFree(s.list[k]);
+        cudaFree(s.zlist[k]);
+    }
+    cudaFree(s.counts);
+    cudaFree(s.tflag);
+    s = State();
+}
+
+/* (re)allocate for `ca` and prime from the current h */
+static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStream_t st)
+{
+    State& s = g_state;
+    const long long n = (long long)ca->rows * ca->columns;
+    if (s.ca != ca || s.n != n) {
+        release();
+        s.ca = ca;
+        s.n = n;
+        s.tiles_x = (ca->columns + TW - 1) / TW;
+        s.tiles_y = (ca->rows + TH - 1) / TH;
+        bool ok = cudaMalloc(&s.f, 4 * n * sizeof(double)) == cudaSuccess &&
+                  cudaMalloc(&s.counts, 4 * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&s.tflag, (size_t)s.tiles_x * s.tiles_y) == cudaSuccess;
+        for (int k = 0; k < 2 && ok; k++)
+            ok = cudaMalloc(&s.list[k], n * sizeof(int)) == cudaSuccess &&
+                 cudaMalloc(&s.zlist[k], n * sizeof(int)) == cudaSuccess;
+        if (!ok) {
+            release();
+            return false;
+        }
+    }
+    s.parity = 0;
+    cudaMemsetAsync(s.f, 0, 4 * n * sizeof(double), st);
+    cudaMemsetAsync(s.counts, 0, 4 * sizeof(int), st);
+    cudaMemsetAsync(s.tflag, 0, (size_t)s.tiles_x * s.tiles_y, st);
+    int blocks = (int)((n + THREADS - 1) / THREADS);
+    if (blocks > 152 * 16)
+        blocks = 152 * 16;
+    k_prime<<<blocks, THREADS, 0, st>>>(h, n, eps_bits, s.list[0], s.counts + 0);
+    s.primed = true;
+    return cudaGetLastError() == cudaSuccess;
+}
+
+/* one step: K1 then K2 on the model's stream; false on a CUDA error */
+static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, double r, long long eps_bits,
+                 cudaStream_t st, cudaEvent_t* ev /* optional: 3 events around K1 and K2 */)
+{
+    State& s = g_state;
+    const int p = s.parity;
+    K1Params a;
+    a.z = z;
+    a.h = h;
+    a.f = s.f;
+    a.list = s.list[p];
+    a.count = s.counts + p;
+    a.zlist = s.zlist[p];
+    a.zcount = s.counts + 2 + p;
+    a.next_counts = s.counts + (1 - p);
+    a.tflag = s.tflag;
+    a.rows = ca->rows;
+    a.cols = ca->columns;
+    a.toroidal = ca->T == CAL_SPACE_TOROIDAL;
+    a.tiles_x = s.tiles_x;
+    a.n = s.n;
+    a.eps = eps;
+    a.r = r;
+    K2Params b;
+    b.h = h;
+    b.f = s.f;
+    b.list = s.list[1 - p];
+    b.count = s.counts + (1 - p);
+    b.zlist = s.zlist[1 - p];
+    b.zcount = s.counts + 2 + (1 - p);
+    b.tflag = s.tflag;
+    b.rows = ca->rows;
+    b.cols = ca->columns;
+    b.toroidal = a.toroidal;
+    b.tiles_x = s.tiles_x;
+    b.n = s.n;
+    b.eps_bits = eps_bits;
+    if (ev)
+        cudaEventRecord(ev[0], st);
+    k1_outflows<<<152 * 8, THREADS, 0, st>>>(a);
+    if (ev)
+        cudaEventRecord(ev[1], st);
+    k2_update<<<dim3(s.tiles_x, s.tiles_y), THREADS, 0, st>>>(b);
+    if (ev)
+        cudaEventRecord(ev[2], st);
+    s.parity = 1 - p;
+    return cudaGetLastError() == cudaSuccess;
+}
+
+} // namespace sdt2
+
+static bool sdt_use_split()
+{
+    const char* e = getenv("OPENCAL_SDT_KERNEL");
+    return !(e && !strcmp(e, "single"));
+}
+
+/* the split step as a global transition (h updated in place) */
+static void sciddicaT_split_transition_timed(struct CALModel2D* ca, cudaEvent_t* ev)
+{
+    const double* z = (const double*)calGetDeviceBuffer2Dr(ca, Q.z, 0);
+    double* h = (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0);
+    cudaStream_t st = (cudaStream_t)calGetStream2D(ca);
+    long long eps_bits;
+    memcpy(&eps_bits, &P.epsilon, sizeof(double));
+    if (sdt2::g_state.ca != ca || !sdt2::g_state.primed)
+        sdt2::prime(ca, h, eps_bits, st);
+    sdt2::step(ca, z, h, P.epsilon, P.r, eps_bits, st, ev);
+    calMarkCurrentWritten2Dr(ca, Q.h);
+}
+
+static void sciddicaT_split_invalidate() { sdt2::g_state.primed = false; }
 
 /* host side of the fused step: queue the kernel, then exchange the h layers */
 static void sciddicaT_fused_transition(struct CALModel2D* ca)
 {
+    if (sdt_use_split()) {
+        sciddicaT_split_transition_timed(ca, nullptr);
+        return;
+    }
     sdt::Params p;
     p.z = (const double*)calGetDeviceBuffer2Dr(ca, Q.z, 0);
     p.h = (const double*)calGetDeviceBuffer2Dr(ca, Q.h, 0);
@@ -334,8 +754,7 @@ static void sciddicaT_fused_transition(struct CALModel2D* ca)
     p.eps = P.epsilon;
     p.r = P.r;
     memcpy(&p.eps_bits, &P.epsilon, sizeof(double));
-    dim3 grid((ca->columns + sdt::TW - 1) / sdt::TW, (ca->rows + sdt::TH - 1) / sdt::TH);
-    sdt::fused_step<<<grid, sdt::THREADS, 0, (cudaStream_t)calGetStream2D(ca)>>>(p);
+    sdt::launch_step(p, (cudaStream_t)calGetStream2D(ca));
     calSwapSubstate2Dr(ca, Q.h);
 }
 
@@ -356,6 +775,7 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
     calClearError();
     if (mode == SDT_MODE_FUSED && ac)
         return CAL_ERROR_INVALID_ARGUMENT;
+    sciddicaT_split_invalidate();
     struct CALModel2D* ca = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D,
                                        toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT,
                                        ac ? CAL_OPT_ACTIVE_CELLS : CAL_NO_OPT);
@@ -424,6 +844,7 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
     if (cells_out && ac)
         memcpy(cells_out, ca->A.cells, sizeof(int) * 2 * (size_t)ca->A.size_current);
     int err = calGetLastError();
+    sdt2::release();
     calRunFinalize2D(run);
     calFinalize2D(ca);
     return err;
@@ -452,6 +873,7 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
     calClearError();
     if (mode == SDT_MODE_FUSED && ac)
         return nullptr;
+    sciddicaT_split_invalidate();
     SdtSession* s = (SdtSession*)calloc(1, sizeof(SdtSession));
     s->mode = mode;
     s->ac = ac;
@@ -509,6 +931,7 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
 extern "C" int cal_sciddicaT_reset(void* handle)
 {
     SdtSession* s = (SdtSession*)handle;
+    sciddicaT_split_invalidate();
     cudaStream_t st = (cudaStream_t)calGetStream2D(s->ca);
     for (int k = 0; k < 6; k++)
         for (int l = 0; l < 2; l++)
@@ -547,32 +970,53 @@ extern "C" int cal_sciddicaT_host_run(void* handle, const double* z_host, const 
     memcpy(Q.h->current, h_host, s->bytes);
     memcpy(Q.h->next, h_host, s->bytes);
     calMarkHostDirty2D(s->ca);
+    sciddicaT_split_invalidate();
     cal_sciddicaT_steps(handle, steps, 0);
     calSyncSubstate2Dr(s->ca, Q.h);
     memcpy(h_out, Q.h->current, s->bytes);
     return calGetLastError();
 }
 
-/* device time of each of n fused launches (events around every launch) */
-extern "C" int cal_sciddicaT_kernel_times(void* handle, int n, float* ms)
+/* device time of each of n steps' kernels, events around every launch:
+ * split step -> ms_a[k] = K1 (outflows), ms_b[k] = K2 (update);
+ * single fused kernel -> ms_a[k] = the kernel, ms_b[k] = 0 */
+extern "C" int cal_sciddicaT_kernel_times(void* handle, int n, float* ms_a, float* ms_b)
 {
     SdtSession* s = (SdtSession*)handle;
     cudaStream_t st = (cudaStream_t)calGetStream2D(s->ca);
-    cudaEvent_t* ev = (cudaEvent_t*)malloc(sizeof(cudaEvent_t) * 2 * n);
-    for (int k = 0; k < 2 * n; k++)
+    cudaEvent_t* ev = (cudaEvent_t*)malloc(sizeof(cudaEvent_t) * 3 * n);
+    for (int k = 0; k < 3 * n; k++)
         cudaEventCreate(&ev[k]);
+    const bool split = sdt_use_split();
     for (int k = 0; k < n; k++) {
-        cudaEventRecord(ev[2 * k], st);
-        sciddicaT_fused_transition(s->ca);
-        cudaEventRecord(ev[2 * k + 1], st);
+        if (split) {
+            sciddicaT_split_transition_timed(s->ca, ev + 3 * k);
+        } else {
+            cudaEventRecord(ev[3 * k], st);
+            sciddicaT_fused_transition(s->ca);
+            cudaEventRecord(ev[3 * k + 1], st);
+            cudaEventRecord(ev[3 * k + 2], st);
+        }
     }
     cudaStreamSynchronize(st);
-    for (int k = 0; k < n; k++)
-        cudaEventElapsedTime(&ms[k], ev[2 * k], ev[2 * k + 1]);
-    for (int k = 0; k < 2 * n; k++)
+    for (int k = 0; k < n; k++) {
+        cudaEventElapsedTime(&ms_a[k], ev[3 * k], ev[3 * k + 1]);
+        cudaEventElapsedTime(&ms_b[k], ev[3 * k + 1], ev[3 * k + 2]);
+    }
+    for (int k = 0; k < 3 * n; k++)
         cudaEventDestroy(ev[k]);
     free(ev);
     return calGetLastError();
+}
+
+/* number of wet cells the split step will process next (synchronises) */
+extern "C" int cal_sciddicaT_wet_count(void* handle)
+{
+    (void)handle;
+    int n = -1;
+    if (sdt2::g_state.counts)
+        cudaMemcpy(&n, sdt2::g_state.counts + sdt2::g_state.parity, sizeof(int), cudaMemcpyDeviceToHost);
+    return n;
 }
 
 extern "C" int cal_sciddicaT_read(void* handle, double* h_out)
@@ -593,6 +1037,7 @@ extern "C" void cal_sciddicaT_close(void* handle)
         for (int l = 0; l < 2; l++)
             cudaFree(s->snap[k][l]);
     cudaFree(s->snap_flags);
+    sdt2::release();
     calRunFinalize2D(s->run);
     calFinalize2D(s->ca);
     free(s);
