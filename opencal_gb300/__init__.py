@@ -39,9 +39,9 @@ class CALError(RuntimeError):
 
 
 def build(force: bool = False) -> None:
-    """Compile the CUDA libraries in-tree (opencal_gb300/build.py)."""
+    """Compile the CUDA libraries in-tree (opencal_gb300/nvbuild.py)."""
     import importlib
-    importlib.import_module(__name__ + ".build").build(force=force)
+    importlib.import_module(__name__ + ".nvbuild").build(force=force)
 
 
 def core() -> C.CDLL:
@@ -49,7 +49,7 @@ def core() -> C.CDLL:
     global _core
     if _core is None:
         if not os.path.exists(CORE_LIB):
-            raise CALError(f"{CORE_LIB} is missing: build it with `python -m opencal_gb300.build`")
+            raise CALError(f"{CORE_LIB} is missing: build it with `python -m opencal_gb300.nvbuild`")
         _core = C.CDLL(CORE_LIB, mode=C.RTLD_GLOBAL)
         _core.calGetErrorString.restype = C.c_char_p
         _core.calGetLastError.restype = C.c_int
@@ -61,7 +61,7 @@ def models() -> C.CDLL:
     if _models is None:
         core()
         if not os.path.exists(MODELS_LIB):
-            raise CALError(f"{MODELS_LIB} is missing: build it with `python -m opencal_gb300.build`")
+            raise CALError(f"{MODELS_LIB} is missing: build it with `python -m opencal_gb300.nvbuild`")
         m = C.CDLL(MODELS_LIB)
         m.cal_sciddicaT_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                         _dp, _dp, _dp, _dp, _pl, C.c_void_p, C.c_int, C.c_int, _pd]

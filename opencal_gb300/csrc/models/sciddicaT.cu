@@ -427,23 +427,27 @@ struct State {
     double* f = nullptr;         /* 4 * n outflows, SoA */
     int* list[2] = {nullptr, nullptr};
     int* zlist[2] = {nullptr, nullptr};
-    int* counts = nullptr;       /* [0..1] wet list lengths, [2..3] dried list lengths */
+    int* counts = nullptr;       /* [0..1] wet list lengths, [2..3] dried list lengths,
+                                    [4] list parity, [5] K2 block ticket */
     unsigned char* tflag = nullptr;
     long long n = 0;
     int tiles_x = 0, tiles_y = 0;
-    int parity = 0;
     bool primed = false;
 };
 
+/* The lists alternate between two buffers; which one a step reads is the
+ * parity word counts[4], flipped by the last K2 block of the step.  Keeping
+ * it in device memory makes every step's launches identical, so a step can
+ * be recorded once as a CUDA graph and replayed. */
 struct K1Params {
     const double* __restrict__ z;
     const double* __restrict__ h;
     double* __restrict__ f;
-    const int* __restrict__ list;
-    const int* __restrict__ count;
-    const int* __restrict__ zlist;
-    const int* __restrict__ zcount;
-    int* next_counts; /* the two counts K2 will append to: zeroed here */
+    int* list0;
+    int* list1;
+    int* zlist0;
+    int* zlist1;
+    int* counts;
     unsigned char* tflag;
     int rows, cols, toroidal, tiles_x;
     long long n;
@@ -453,10 +457,11 @@ struct K1Params {
 struct K2Params {
     double* __restrict__ h;
     const double* __restrict__ f;
-    int* list;
-    int* count;
-    int* zlist;
-    int* zcount;
+    int* list0;
+    int* list1;
+    int* zlist0;
+    int* zlist1;
+    int* counts;
     unsigned char* tflag;
     int rows, cols, toroidal, tiles_x;
     long long n;
@@ -470,12 +475,15 @@ static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
 
 __global__ void __launch_bounds__(THREADS) k1_outflows(const __grid_constant__ K1Params p)
 {
+    const int par = p.counts[4];
+    const int* list = par ? p.list1 : p.list0;
+    const int* zlist = par ? p.zlist1 : p.zlist0;
     if (blockIdx.x == 0 && threadIdx.x < 2)
-        p.next_counts[threadIdx.x * 2] = 0; /* wet and dried counts of the other parity */
+        p.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists K2 will append to */
     const int stride = gridDim.x * blockDim.x;
-    const int nw = *p.count;
+    const int nw = p.counts[par];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += stride) {
-        const int c = p.list[k];
+        const int c = list[k];
         const int i = c / p.cols, j = c - i * p.cols;
         /* neighbours in von Neumann order n = 1..4: north, west, east, south */
         int ni[4] = {i - 1, i, i, i + 1}, nj[4] = {j, j - 1, j + 1, j};
@@ -515,9 +523,9 @@ __global__ void __launch_bounds__(THREADS) k1_outflows(const __grid_constant__ K
         if (any)
             p.tflag[tile_of(i, j, p.tiles_x)] = 1;
     }
-    const int nz = *p.zcount;
+    const int nz = p.counts[2 + par];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nz; k += stride) {
-        const int c = p.zlist[k];
+        const int c = zlist[k];
 #pragma unroll
         for (int q = 0; q < 4; q++)
             p.f[q * p.n + c] = 0.0;
@@ -541,6 +549,11 @@ static __device__ __forceinline__ void warp_append(bool pred, int value, int* li
 
 __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2Params p)
 {
+    const int par = p.counts[4];
+    int* list = par ? p.list0 : p.list1; /* next step's lists */
+    int* zlist = par ? p.zlist0 : p.zlist1;
+    int* count = p.counts + (1 - par);
+    int* zcount = p.counts + 2 + (1 - par);
     const int tile = blockIdx.y * p.tiles_x + blockIdx.x;
     const bool flagged = p.tflag[tile] != 0;
     const int r = threadIdx.x / (TW / 4);       /* 0..15 */
@@ -589,13 +602,21 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
         }
         const bool wet_before = cell && sdt::is_wet(hv, p.eps_bits);
         const bool wet_after = cell && sdt::is_wet(hn, p.eps_bits);
-        warp_append(wet_after, (int)c, p.list, p.count);
-        warp_append(wet_before && !wet_after, (int)c, p.zlist, p.zcount);
+        warp_append(wet_after, (int)c, list, count);
+        warp_append(wet_before && !wet_after, (int)c, zlist, zcount);
     }
-    if (flagged) {
-        __syncthreads();
-        if (threadIdx.x == 0)
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (flagged)
             p.tflag[tile] = 0;
+        /* every block read the parity at its start; the last one to finish
+         * flips it for the next step (no block waits for another) */
+        __threadfence();
+        const unsigned nblocks = gridDim.x * gridDim.y;
+        if (atomicAdd(reinterpret_cast<unsigned*>(p.counts + 5), 1u) == nblocks - 1) {
+            p.counts[4] = 1 - par;
+            p.counts[5] = 0;
+        }
     }
 }
 
@@ -642,7 +663,7 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         s.tiles_x = (ca->columns + TW - 1) / TW;
         s.tiles_y = (ca->rows + TH - 1) / TH;
         bool ok = cudaMalloc(&s.f, 4 * n * sizeof(double)) == cudaSuccess &&
-                  cudaMalloc(&s.counts, 4 * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&s.counts, 8 * sizeof(int)) == cudaSuccess &&
                   cudaMalloc(&s.tflag, (size_t)s.tiles_x * s.tiles_y) == cudaSuccess;
         for (int k = 0; k < 2 && ok; k++)
             ok = cudaMalloc(&s.list[k], n * sizeof(int)) == cudaSuccess &&
@@ -652,9 +673,8 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
             return false;
         }
     }
-    s.parity = 0;
     cudaMemsetAsync(s.f, 0, 4 * n * sizeof(double), st);
-    cudaMemsetAsync(s.counts, 0, 4 * sizeof(int), st);
+    cudaMemsetAsync(s.counts, 0, 8 * sizeof(int), st); /* parity 0, ticket 0 */
     cudaMemsetAsync(s.tflag, 0, (size_t)s.tiles_x * s.tiles_y, st);
     int blocks = (int)((n + THREADS - 1) / THREADS);
     if (blocks > 152 * 16)
@@ -669,16 +689,15 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
                  cudaStream_t st, cudaEvent_t* ev /* optional: 3 events around K1 and K2 */)
 {
     State& s = g_state;
-    const int p = s.parity;
     K1Params a;
     a.z = z;
     a.h = h;
     a.f = s.f;
-    a.list = s.list[p];
-    a.count = s.counts + p;
-    a.zlist = s.zlist[p];
-    a.zcount = s.counts + 2 + p;
-    a.next_counts = s.counts + (1 - p);
+    a.list0 = s.list[0];
+    a.list1 = s.list[1];
+    a.zlist0 = s.zlist[0];
+    a.zlist1 = s.zlist[1];
+    a.counts = s.counts;
     a.tflag = s.tflag;
     a.rows = ca->rows;
     a.cols = ca->columns;
@@ -690,10 +709,11 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     K2Params b;
     b.h = h;
     b.f = s.f;
-    b.list = s.list[1 - p];
-    b.count = s.counts + (1 - p);
-    b.zlist = s.zlist[1 - p];
-    b.zcount = s.counts + 2 + (1 - p);
+    b.list0 = s.list[0];
+    b.list1 = s.list[1];
+    b.zlist0 = s.zlist[0];
+    b.zlist1 = s.zlist[1];
+    b.counts = s.counts;
     b.tflag = s.tflag;
     b.rows = ca->rows;
     b.cols = ca->columns;
@@ -709,7 +729,6 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     k2_update<<<dim3(s.tiles_x, s.tiles_y), THREADS, 0, st>>>(b);
     if (ev)
         cudaEventRecord(ev[2], st);
-    s.parity = 1 - p;
     return cudaGetLastError() == cudaSuccess;
 }
 
@@ -736,6 +755,17 @@ static void sciddicaT_split_transition_timed(struct CALModel2D* ca, cudaEvent_t*
 }
 
 static void sciddicaT_split_invalidate() { sdt2::g_state.primed = false; }
+
+/* prime now (eagerly) if the next split step would: keeps the priming out of
+ * a step that is being recorded as a graph */
+static void sciddicaT_split_prepare(struct CALModel2D* ca)
+{
+    if (!sdt_use_split() || (sdt2::g_state.ca == ca && sdt2::g_state.primed))
+        return;
+    long long eps_bits;
+    memcpy(&eps_bits, &P.epsilon, sizeof(double));
+    sdt2::prime(ca, (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0), eps_bits, (cudaStream_t)calGetStream2D(ca));
+}
 
 /* host side of the fused step: queue the kernel, then exchange the h layers */
 static void sciddicaT_fused_transition(struct CALModel2D* ca)
@@ -821,6 +851,8 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     calRunInitSimulation2D(run);
+    if (mode == SDT_MODE_FUSED)
+        sciddicaT_split_prepare(ca);
     cudaEventRecord(e0, s);
     for (run->step = run->initial_step; run->step <= run->final_step; run->step++)
         if (!calRunCAStep2D(run))
@@ -951,6 +983,8 @@ extern "C" int cal_sciddicaT_reset(void* handle)
 extern "C" int cal_sciddicaT_steps(void* handle, int steps, int graph)
 {
     SdtSession* s = (SdtSession*)handle;
+    if (s->mode == SDT_MODE_FUSED)
+        sciddicaT_split_prepare(s->ca);
     calRunSetGraph2D(s->run, graph ? CAL_TRUE : CAL_FALSE);
     for (int k = 0; k < steps; k++)
         calRunCAStep2D(s->run);
@@ -1013,10 +1047,10 @@ extern "C" int cal_sciddicaT_kernel_times(void* handle, int n, float* ms_a, floa
 extern "C" int cal_sciddicaT_wet_count(void* handle)
 {
     (void)handle;
-    int n = -1;
+    int c[6] = {-1, -1, -1, -1, 0, 0};
     if (sdt2::g_state.counts)
-        cudaMemcpy(&n, sdt2::g_state.counts + sdt2::g_state.parity, sizeof(int), cudaMemcpyDeviceToHost);
-    return n;
+        cudaMemcpy(c, sdt2::g_state.counts, sizeof(c), cudaMemcpyDeviceToHost);
+    return c[c[4] & 1];
 }
 
 extern "C" int cal_sciddicaT_read(void* handle, double* h_out)

@@ -8,7 +8,7 @@
 Compiles translation units in parallel and skips those whose object is newer
 than the source and every header.  No cmake.
 
-    python -m opencal_gb300.build [--force] [--verbose]
+    python -m opencal_gb300.nvbuild [--force] [--verbose]
 """
 from __future__ import annotations
 
@@ -32,7 +32,7 @@ COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-cuda
 # model kernels restate reference arithmetic operation by operation: no FMA contraction
 MODEL_FLAGS = ["--fmad=false"]
 
-CORE_SOURCES = ["cal_core.cu", "cal2D.cu", "cal3D.cu", "cal2DRun.cu", "cal3DRun.cu", "calIO.cu"]
+CORE_SOURCES = ["cal_core.cu", "cal2D.cu", "cal3D.cu", "cal2DRun.cu", "cal3DRun.cu", "calIO.cu", "cal_noalloc.cu"]
 MODEL_SOURCES = ["models/sciddicaT.cu", "models/life.cu", "models/probes.cu"]
 
 

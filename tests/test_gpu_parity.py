@@ -77,11 +77,11 @@ def test_sciddicaT_processes_bit_exact(cal, orc, rows, cols, seed, steps, tor, a
     assert_same(got[2], ref[2], "active cells")
 
 
-@pytest.mark.parametrize("ac", [0, 1])
-def test_sciddicaT_graph_replay_bit_exact(cal, orc, ac):
+@pytest.mark.parametrize("ac,mode", [(0, 0), (1, 0), (0, 1)])
+def test_sciddicaT_graph_replay_bit_exact(cal, orc, ac, mode):
     z, h = W.sciddicaT_inputs(180, 150, seed=17)
     ref = orc.sciddicaT(z, h, 50, toroidal=False, ac=ac)
-    got = cal.sciddicaT(z, h, 50, toroidal=False, ac=ac, mode=cal.MODE_PROCESSES, graph=True)
+    got = cal.sciddicaT(z, h, 50, toroidal=False, ac=ac, mode=mode, graph=True)
     assert_same(got[1], ref[1], "h")
     assert_same(got[2], ref[2], "active cells")
 
