@@ -204,6 +204,10 @@ int calCompactActiveCellsNoAlloc2D(const CALbyte* flags, int rows, int columns, 
 struct CALDevModel2D;
 typedef int (*CALLaunchFunc2D)(const struct CALDevModel2D* m, int grid_x, int grid_y, void* stream);
 int calRegisterElementaryProcess2D(CALCallbackFunc2D host_name, CALLaunchFunc2D launch, const char* name);
+typedef CALbyte (*CALStopFunc2D)(struct CALModel2D* ca2D);
+typedef int (*CALStopLaunchFunc2D)(const struct CALDevModel2D* m, unsigned long long handle, int use_handle,
+                                   int final_step, int* flag, void* stream);
+int calRegisterDeviceStopCondition2D(CALStopFunc2D host_name, CALStopLaunchFunc2D launch, const char* name);
 void calHostCallOfDeviceProcess2D(const char* name);
 
 #ifdef __cplusplus

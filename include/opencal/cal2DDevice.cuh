@@ -45,6 +45,7 @@ struct CALDevModel2D {
     void* cur[3][CAL_MAX_SUBSTATES];
     void* nxt[3][CAL_MAX_SUBSTATES];
     unsigned int* dirty;         /* [3] bitmasks: substates whose next layer was written */
+    int* step;                   /* current step of a device-driven run (calRunDevice2D) */
     CALbyte* flags;              /* active-cell flags, NULL without the optimisation */
     struct CALCell2D* cells;     /* compacted active list */
     int* count;                  /* its length */
@@ -162,6 +163,21 @@ static __device__ __forceinline__ void cal_removeactive2D(const struct CALModel2
     m->flags[cal_lin2D(m, i, j)] = 0;
 }
 
+/* the step number a device-driven run is executing (calRunDevice2D); the
+ * device counterpart of reading CALRun2D::step in a stop condition */
+static __device__ __forceinline__ int calRunGetStep2D(const struct CALModel2D* ca)
+{
+    return *cal_dm2D(ca)->step;
+}
+
+/* number of active cells after the last update (device counterpart of
+ * A.size_current) */
+static __device__ __forceinline__ int calGetActiveCellCountDevice2D(const struct CALModel2D* ca)
+{
+    const struct CALDevModel2D* m = cal_dm2D(ca);
+    return m->count ? *m->count : 0;
+}
+
 /* One elementary process over every cell, or over the active list when the
  * optimisation is on and the list is non-empty (cal2D.c:717-734).  The grid
  * is sized by the host to a few waves of the GPU; both loops are grid-stride.
@@ -197,6 +213,52 @@ static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* 
     cal_ep2D_kernel<EP><<<dim3(gx, gy), CAL_EP_THREADS, 0, (cudaStream_t)stream>>>(*m);
     return (int)cudaGetLastError();
 }
+
+/* Device stop condition of a device-driven run: one thread evaluates STOP
+ * after each step.  The run continues while STOP is false and, with a
+ * final step, while the step number has not passed it (cal2DRun.c:125-139);
+ * the decision drives the graph's conditional WHILE node.  `flag` receives
+ * the decision too, for the step-by-step fallback. */
+template <CALbyte (*STOP)(struct CALModel2D*)>
+__global__ void cal_stop2D_kernel(const __grid_constant__ struct CALDevModel2D m, cudaGraphConditionalHandle h,
+                                  int use_handle, int final_step, int* flag)
+{
+    struct CALModel2D* ca = const_cast<struct CALModel2D*>(&m.model);
+    const bool stop = STOP(ca) != 0;
+    int again = 0;
+    if (!stop) {
+        const int next = *m.step + 1;
+        *m.step = next;
+        again = (final_step == CAL_RUN_LOOP || next <= final_step) ? 1 : 0;
+    }
+    *flag = again;
+    if (use_handle)
+        cudaGraphSetConditional(h, (unsigned)again);
+}
+
+template <CALbyte (*STOP)(struct CALModel2D*)>
+static int cal_launch_stop2D(const struct CALDevModel2D* m, unsigned long long handle, int use_handle, int final_step,
+                             int* flag, void* stream)
+{
+    cal_stop2D_kernel<STOP><<<1, 1, 0, (cudaStream_t)stream>>>(*m, (cudaGraphConditionalHandle)handle, use_handle,
+                                                                final_step, flag);
+    return (int)cudaGetLastError();
+}
+
+/* Defines a device stop condition NAME, registered for
+ * calRunAddDeviceStopConditionFunc2D.  Usage:
+ *   CAL_DEVICE_STOP_CONDITION_2D(NAME)(struct CALModel2D* ca) { return ...; } */
+#define CAL_DEVICE_STOP_CONDITION_2D(NAME)                                                              \
+    static __device__ __forceinline__ CALbyte NAME##_cal_device_(struct CALModel2D*);                 \
+    extern "C" CALbyte NAME(struct CALModel2D* ca2D_)                                                   \
+    {                                                                                                   \
+        (void)ca2D_;                                                                                    \
+        calHostCallOfDeviceProcess2D(#NAME);                                                            \
+        return CAL_FALSE;                                                                               \
+    }                                                                                                   \
+    static const int NAME##_cal_registered_ =                                                           \
+        calRegisterDeviceStopCondition2D(NAME, cal_launch_stop2D<NAME##_cal_device_>, #NAME);           \
+    static __device__ __forceinline__ CALbyte NAME##_cal_device_
 
 /* Defines the device elementary process NAME and its host-side name, which
  * is what calAddElementaryProcess2D / calApplyElementaryProcess2D take.

@@ -58,6 +58,25 @@ void calRunFinalize2D(struct CALRun2D* cal2DRun);                               
 void calRunSetGraph2D(struct CALRun2D* simulation, CALbyte enable);
 /* Number of steps whose device work was replayed from the recorded graph. */
 long calRunGraphReplays2D(struct CALRun2D* simulation);
+/* A stop condition evaluated on the GPU after every step (a function defined
+ * with CAL_DEVICE_STOP_CONDITION_2D; on the device it reads the step with
+ * calRunGetStep2D).  Used by calRunDevice2D. */
+void calRunAddDeviceStopConditionFunc2D(struct CALRun2D* simulation, CALbyte (*stopCondition)(struct CALModel2D*));
+/* calRun2D with the step loop on the GPU: init, then ONE graph launch whose
+ * conditional WHILE node repeats [step; device stop condition] until the
+ * stop condition holds or the final step is done, then finalize.  Needs the
+ * step's device work to be recordable (see calRunSetGraph2D) and no host
+ * stop condition; otherwise it runs the steps one by one, still deciding
+ * with the device stop condition.  On return CALRun2D::step is the step the
+ * loop ended on, as after calRun2D. */
+void calRunDevice2D(struct CALRun2D* simulation);
+/* The device-driven loop alone (no init/finalize) over steps first..last
+ * (last = CAL_RUN_LOOP: until the device stop condition); returns the step
+ * it ended on (also stored in CALRun2D::step). */
+int calRunDeviceSteps2D(struct CALRun2D* simulation, int first_step, int last_step);
+/* 1 if the last calRunDevice2D ran as a single device loop, 0 if it fell
+ * back to one launch sequence per step. */
+int calRunDeviceLoopUsed2D(struct CALRun2D* simulation);
 
 #ifdef __cplusplus
 }

@@ -122,6 +122,10 @@ int calGetActiveCellCount3D(struct CALModel3D* ca3D);
 struct CALDevModel3D;
 typedef int (*CALLaunchFunc3D)(const struct CALDevModel3D* m, int grid_x, int grid_y, void* stream);
 int calRegisterElementaryProcess3D(CALCallbackFunc3D host_name, CALLaunchFunc3D launch, const char* name);
+typedef CALbyte (*CALStopFunc3D)(struct CALModel3D* ca3D);
+typedef int (*CALStopLaunchFunc3D)(const struct CALDevModel3D* m, unsigned long long handle, int use_handle,
+                                   int final_step, int* flag, void* stream);
+int calRegisterDeviceStopCondition3D(CALStopFunc3D host_name, CALStopLaunchFunc3D launch, const char* name);
 void calHostCallOfDeviceProcess3D(const char* name);
 
 #ifdef __cplusplus

@@ -25,6 +25,7 @@ struct CALDevModel3D {
     void* cur[3][CAL_MAX_SUBSTATES];
     void* nxt[3][CAL_MAX_SUBSTATES];
     unsigned int* dirty;
+    int* step; /* current step of a device-driven run (calRunDevice3D) */
     CALbyte* flags;
     struct CALCell3D* cells;
     int* count;
@@ -138,6 +139,56 @@ static __device__ __forceinline__ void cal_removeactive3D(const struct CALModel3
     const struct CALDevModel3D* m = cal_dm3D(ca);
     m->flags[cal_lin3D(m, i, j, k)] = 0;
 }
+
+static __device__ __forceinline__ int calRunGetStep3D(const struct CALModel3D* ca)
+{
+    return *cal_dm3D(ca)->step;
+}
+
+static __device__ __forceinline__ int calGetActiveCellCountDevice3D(const struct CALModel3D* ca)
+{
+    const struct CALDevModel3D* m = cal_dm3D(ca);
+    return m->count ? *m->count : 0;
+}
+
+/* device stop condition kernel of a device-driven 3D run (see cal2DDevice.cuh) */
+template <CALbyte (*STOP)(struct CALModel3D*)>
+__global__ void cal_stop3D_kernel(const __grid_constant__ struct CALDevModel3D m, cudaGraphConditionalHandle h,
+                                  int use_handle, int final_step, int* flag)
+{
+    struct CALModel3D* ca = const_cast<struct CALModel3D*>(&m.model);
+    const bool stop = STOP(ca) != 0;
+    int again = 0;
+    if (!stop) {
+        const int next = *m.step + 1;
+        *m.step = next;
+        again = (final_step == CAL_RUN_LOOP || next <= final_step) ? 1 : 0;
+    }
+    *flag = again;
+    if (use_handle)
+        cudaGraphSetConditional(h, (unsigned)again);
+}
+
+template <CALbyte (*STOP)(struct CALModel3D*)>
+static int cal_launch_stop3D(const struct CALDevModel3D* m, unsigned long long handle, int use_handle, int final_step,
+                             int* flag, void* stream)
+{
+    cal_stop3D_kernel<STOP><<<1, 1, 0, (cudaStream_t)stream>>>(*m, (cudaGraphConditionalHandle)handle, use_handle,
+                                                                final_step, flag);
+    return (int)cudaGetLastError();
+}
+
+#define CAL_DEVICE_STOP_CONDITION_3D(NAME)                                                              \
+    static __device__ __forceinline__ CALbyte NAME##_cal_device_(struct CALModel3D*);                 \
+    extern "C" CALbyte NAME(struct CALModel3D* ca3D_)                                                   \
+    {                                                                                                   \
+        (void)ca3D_;                                                                                    \
+        calHostCallOfDeviceProcess3D(#NAME);                                                            \
+        return CAL_FALSE;                                                                               \
+    }                                                                                                   \
+    static const int NAME##_cal_registered_ =                                                           \
+        calRegisterDeviceStopCondition3D(NAME, cal_launch_stop3D<NAME##_cal_device_>, #NAME);           \
+    static __device__ __forceinline__ CALbyte NAME##_cal_device_
 
 /* one elementary process over every cell (lines of j for each (k, i)) or
  * over the active list when it is non-empty (cal3D.c:658-674) */

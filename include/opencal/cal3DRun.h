@@ -58,6 +58,25 @@ void calRunFinalize3D(struct CALRun3D* cal3DRun);                               
 void calRunSetGraph3D(struct CALRun3D* simulation, CALbyte enable);
 /* Number of steps whose device work was replayed from the recorded graph. */
 long calRunGraphReplays3D(struct CALRun3D* simulation);
+/* A stop condition evaluated on the GPU after every step (a function defined
+ * with CAL_DEVICE_STOP_CONDITION_3D; on the device it reads the step with
+ * calRunGetStep3D).  Used by calRunDevice3D. */
+void calRunAddDeviceStopConditionFunc3D(struct CALRun3D* simulation, CALbyte (*stopCondition)(struct CALModel3D*));
+/* calRun3D with the step loop on the GPU: init, then ONE graph launch whose
+ * conditional WHILE node repeats [step; device stop condition] until the
+ * stop condition holds or the final step is done, then finalize.  Needs the
+ * step's device work to be recordable (see calRunSetGraph3D) and no host
+ * stop condition; otherwise it runs the steps one by one, still deciding
+ * with the device stop condition.  On return CALRun3D::step is the step the
+ * loop ended on, as after calRun3D. */
+void calRunDevice3D(struct CALRun3D* simulation);
+/* The device-driven loop alone (no init/finalize) over steps first..last
+ * (last = CAL_RUN_LOOP: until the device stop condition); returns the step
+ * it ended on (also stored in CALRun3D::step). */
+int calRunDeviceSteps3D(struct CALRun3D* simulation, int first_step, int last_step);
+/* 1 if the last calRunDevice3D ran as a single device loop, 0 if it fell
+ * back to one launch sequence per step. */
+int calRunDeviceLoopUsed3D(struct CALRun3D* simulation);
 
 #ifdef __cplusplus
 }

@@ -142,6 +142,7 @@ static bool build_desc(struct CALModel2D* ca, CALDevModel2D* d)
         }
     }
     d->dirty = g.d_dirty;
+    d->step = g.d_step;
     d->flags = (CALbyte*)g.d_flags;
     d->cells = (struct CALCell2D*)g.d_cells;
     d->count = g.d_count;
@@ -156,6 +157,12 @@ static bool build_desc(struct CALModel2D* ca, CALDevModel2D* d)
         d->xj[n] = ca->X[n].j;
     }
     return true;
+}
+
+/* launch descriptor for library-internal kernels (run loop) */
+bool cal_internal_desc2D(struct CALModel2D* ca, CALDevModel2D* d)
+{
+    return build_desc(ca, d);
 }
 
 /* ======================= definition ===================================== */

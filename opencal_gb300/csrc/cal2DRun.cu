@@ -26,7 +26,38 @@ struct CALGpuRun2D {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long replays = 0;
+    CALStopLaunchFunc2D dev_stop = nullptr; /* device stop condition */
+    int* d_flag = nullptr;                  /* its decision, for the step-by-step fallback */
+    int device_loop_used = 0;
 };
+
+bool cal_internal_desc2D(struct CALModel2D* ca, CALDevModel2D* d);
+
+/* ======================= device stop conditions ========================= */
+
+#define CAL_STOP_REGISTRY_MAX 1024
+static CALStopFunc2D g_stop_host[CAL_STOP_REGISTRY_MAX];
+static CALStopLaunchFunc2D g_stop_launch[CAL_STOP_REGISTRY_MAX];
+static int g_stop_n;
+
+extern "C" int calRegisterDeviceStopCondition2D(CALStopFunc2D host_name, CALStopLaunchFunc2D launch, const char* name)
+{
+    (void)name;
+    for (int r = 0; r < g_stop_n; r++)
+        if (g_stop_host[r] == host_name) {
+            g_stop_launch[r] = launch;
+            return 1;
+        }
+    if (g_stop_n >= CAL_STOP_REGISTRY_MAX)
+        return 0;
+    g_stop_host[g_stop_n] = host_name;
+    g_stop_launch[g_stop_n] = launch;
+    g_stop_n++;
+    return 1;
+}
+
+/* the condition of a run without a device stop condition: only the final step ends it */
+static __device__ CALbyte cal_never_stop(struct CALModel2D*) { return CAL_FALSE; }
 
 static inline cal::CalGrid& G(struct CALModel2D* ca) { return ca->gpu->g; }
 
@@ -178,9 +209,158 @@ extern "C" void calRunFinalize2D(struct CALRun2D* sim)
             cudaGraphExecDestroy(sim->gpu->exec);
         if (sim->gpu->graph)
             cudaGraphDestroy(sim->gpu->graph);
+        if (sim->gpu->d_flag)
+            cudaFree(sim->gpu->d_flag);
         delete sim->gpu;
     }
     free(sim);
+}
+
+extern "C" void calRunAddDeviceStopConditionFunc2D(struct CALRun2D* sim, CALbyte (*stop)(struct CALModel2D*))
+{
+    for (int r = 0; r < g_stop_n; r++)
+        if (g_stop_host[r] == stop) {
+            sim->gpu->dev_stop = g_stop_launch[r];
+            return;
+        }
+    cal::set_error(CAL_ERROR_NOT_A_DEVICE_PROCESS,
+                   "calRunAddDeviceStopConditionFunc2D: not a device stop condition (CAL_DEVICE_STOP_CONDITION_2D)");
+}
+
+/* record [step; stop] as the body of a conditional WHILE node and run it;
+ * false (with nothing executed) when the step cannot be recorded */
+static bool device_loop(struct CALRun2D* sim, CALStopLaunchFunc2D stop, int have_steps)
+{
+    CALGpuRun2D* gr = sim->gpu;
+    cal::CalGrid& g = G(sim->ca2D);
+    if (!g.repair_all_stale() || !g.to_device_all())
+        return false;
+    CALDevModel2D d;
+    if (!cal_internal_desc2D(sim->ca2D, &d))
+        return false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphConditionalHandle handle;
+    if (!cal::cuda_ok(cudaGraphCreate(&graph, 0), "cudaGraphCreate"))
+        return false;
+    if (!cal::cuda_ok(cudaGraphConditionalHandleCreate(&handle, graph, have_steps ? 1u : 0u,
+                                                       cudaGraphCondAssignDefault), "conditional handle")) {
+        cudaGraphDestroy(graph);
+        return false;
+    }
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (!cal::cuda_ok(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp), "conditional node")) {
+        cudaGraphDestroy(graph);
+        return false;
+    }
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cal::GridState* before = new cal::GridState;
+    g.save(before);
+    const int transfers0 = g.transfers;
+    const long swaps0 = g.swaps;
+    calClearError();
+    bool clean = cal::cuda_ok(cudaStreamBeginCaptureToGraph(g.stream, body, nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal), "capture body");
+    if (clean) {
+        g.capturing = 1;
+        step_work(sim);
+        const int rc = stop(&d, (unsigned long long)handle, 1, sim->final_step, gr->d_flag, (void*)g.stream);
+        g.capturing = 0;
+        cudaGraph_t out = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(g.stream, &out);
+        clean = rc == 0 && e == cudaSuccess && calGetLastError() == CAL_SUCCESS && g.transfers == transfers0 &&
+                g.swaps == swaps0;
+    }
+    cudaGraphExec_t exec = nullptr;
+    if (clean)
+        clean = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    if (!clean) {
+        (void)cudaGetLastError();
+        g.restore(before);
+        delete before;
+        cudaGraphDestroy(graph);
+        calClearError();
+        return false;
+    }
+    delete before;
+    const bool ok = cal::cuda_ok(cudaGraphLaunch(exec, g.stream), "device loop launch");
+    g.device_wrote_all();
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    return ok;
+}
+
+/* steps first..last (last == CAL_RUN_LOOP: until the stop condition) with
+ * the loop on the device when possible; returns the step the loop ended on */
+static int run_device_steps(struct CALRun2D* sim, int first, int last)
+{
+    CALGpuRun2D* gr = sim->gpu;
+    cal::CalGrid& g = G(sim->ca2D);
+    if (!gr->d_flag && !cal::cuda_ok(cudaMalloc(&gr->d_flag, sizeof(int)), "cudaMalloc stop flag"))
+        return first;
+    CALStopLaunchFunc2D stop = gr->dev_stop ? gr->dev_stop : cal_launch_stop2D<cal_never_stop>;
+    const int have_steps = last == CAL_RUN_LOOP || first <= last;
+    int step = first;
+    gr->device_loop_used = 0;
+    if (!have_steps)
+        return step;
+    cal::cuda_ok(cudaMemcpyAsync(g.d_step, &step, sizeof(int), cudaMemcpyHostToDevice, g.stream), "set step");
+    g.sync();
+    const int saved_final = sim->final_step;
+    sim->final_step = last;
+    if (!sim->stopCondition && device_loop(sim, stop, have_steps)) {
+        gr->device_loop_used = 1;
+    } else {
+        /* one step at a time; the device condition still decides */
+        for (;;) {
+            step_work(sim);
+            CALDevModel2D d;
+            if (!cal_internal_desc2D(sim->ca2D, &d))
+                break;
+            if (stop(&d, 0ULL, 0, last, gr->d_flag, (void*)g.stream) != 0)
+                break;
+            int again = 0;
+            if (!cal::cuda_ok(cudaMemcpyAsync(&again, gr->d_flag, sizeof(int), cudaMemcpyDeviceToHost, g.stream),
+                              "read stop flag") || !g.sync())
+                break;
+            if (sim->stopCondition) {
+                cal::cuda_ok(cudaMemcpyAsync(&sim->step, g.d_step, sizeof(int), cudaMemcpyDeviceToHost, g.stream),
+                             "read step");
+                g.sync();
+                if (sim->stopCondition(sim->ca2D))
+                    break;
+            }
+            if (!again)
+                break;
+        }
+    }
+    sim->final_step = saved_final;
+    cal::cuda_ok(cudaMemcpyAsync(&step, g.d_step, sizeof(int), cudaMemcpyDeviceToHost, g.stream), "read step");
+    g.sync();
+    return step;
+}
+
+extern "C" void calRunDevice2D(struct CALRun2D* sim)
+{
+    calRunInitSimulation2D(sim);
+    sim->step = run_device_steps(sim, sim->initial_step, sim->final_step);
+    calRunFinalizeSimulation2D(sim);
+    G(sim->ca2D).sync();
+}
+
+extern "C" int calRunDeviceSteps2D(struct CALRun2D* sim, int first_step, int last_step)
+{
+    sim->step = run_device_steps(sim, first_step, last_step);
+    return sim->step;
+}
+
+extern "C" int calRunDeviceLoopUsed2D(struct CALRun2D* sim)
+{
+    return (sim && sim->gpu) ? sim->gpu->device_loop_used : 0;
 }
 
 extern "C" void calRunSetGraph2D(struct CALRun2D* sim, CALbyte enable)

@@ -120,6 +120,7 @@ static bool build_desc(struct CALModel3D* ca, CALDevModel3D* d)
         }
     }
     d->dirty = g.d_dirty;
+    d->step = g.d_step;
     d->flags = (CALbyte*)g.d_flags;
     d->cells = (struct CALCell3D*)g.d_cells;
     d->count = g.d_count;
@@ -135,6 +136,11 @@ static bool build_desc(struct CALModel3D* ca, CALDevModel3D* d)
         d->xk[n] = ca->X[n].k;
     }
     return true;
+}
+
+bool cal_internal_desc3D(struct CALModel3D* ca, CALDevModel3D* d)
+{
+    return build_desc(ca, d);
 }
 
 extern "C" struct CALCell3D* calAddNeighbor3D(struct CALModel3D* ca, int i, int j, int k)

@@ -320,6 +320,9 @@ bool CalGrid::init(int dim_, int rows_, int cols_, int slices_, int toroidal_, i
     if (!cuda_ok(cudaMalloc(&d_dirty, 4 * sizeof(unsigned)), "cudaMalloc dirty") ||
         !cuda_ok(cudaMemsetAsync(d_dirty, 0, 4 * sizeof(unsigned), stream), "memset dirty"))
         return false;
+    if (!cuda_ok(cudaMalloc(&d_step, 2 * sizeof(int)), "cudaMalloc step") ||
+        !cuda_ok(cudaMemsetAsync(d_step, 0, 2 * sizeof(int), stream), "memset step"))
+        return false;
     if (!cuda_ok(cudaMalloc(&d_count, sizeof(int)), "cudaMalloc count") ||
         !cuda_ok(cudaMemsetAsync(d_count, 0, sizeof(int), stream), "memset count"))
         return false;
@@ -361,6 +364,7 @@ void CalGrid::destroy()
     cudaFree(d_count);
     cudaFree(d_block_counts);
     cudaFree(d_dirty);
+    cudaFree(d_step);
     if (h_flags)
         cudaFreeHost(h_flags);
     if (stream)

@@ -86,6 +86,7 @@ struct CalGrid {
     unsigned char* h_flags = nullptr; /* host mirror (pinned) */
 
     unsigned* d_dirty = nullptr; /* [3] written-substate bits */
+    int* d_step = nullptr;       /* step counter of a device-driven run */
     int transfers = 0;           /* host<->device coherence copies made so far */
     long swaps = 0;              /* pointer swaps made so far */
     int capturing = 0;

@@ -50,6 +50,7 @@ struct sciddicaTParameters {
     CALParameterr epsilon;
     CALParameterr r;
     int active;
+    int steps; /* run length used by the device stop condition */
 };
 
 __managed__ struct sciddicaTSubstates Q;
@@ -118,6 +119,13 @@ CAL_ELEMENTARY_PROCESS_2D(sciddicaT_remove_inactive_cells)(struct CALModel2D* sc
 {
     if (calGet2Dr(sciddicaT, Q.h, i, j) <= P.epsilon)
         calRemoveActiveCell2D(sciddicaT, i, j);
+}
+
+/* the active-cells example's stop condition (cal_sciddicaT-activecells-glut/
+ * source/sciddicaT.c:149-154: step >= STEPS), evaluated on the GPU */
+CAL_DEVICE_STOP_CONDITION_2D(sciddicaT_device_stop)(struct CALModel2D* sciddicaT)
+{
+    return calRunGetStep2D(sciddicaT) >= P.steps ? CAL_TRUE : CAL_FALSE;
 }
 
 /* host callbacks (sciddicaT.c:104-140) */
@@ -473,7 +481,9 @@ static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
     return (i / TH) * tiles_x + (j / TW);
 }
 
-__global__ void __launch_bounds__(THREADS) k1_outflows(const __grid_constant__ K1Params p)
+constexpr int K1_THREADS = 64; /* small blocks: the wet list spreads over every SM */
+
+__global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant__ K1Params p)
 {
     const int par = p.counts[4];
     const int* list = par ? p.list1 : p.list0;
@@ -547,6 +557,52 @@ static __device__ __forceinline__ void warp_append(bool pred, int value, int* li
         list[base + __popc(mask & ((1u << lane) - 1u))] = value;
 }
 
+/* Block-wide append of up to 4 items per thread to two lists, one atomicAdd
+ * per list per block.  want[q] / dried[q]: item q goes to list / zlist. */
+static __device__ __forceinline__ void block_append4(const bool want[4], const bool dried[4], const int value[4],
+                                                     int* list, int* count, int* zlist, int* zcount)
+{
+    __shared__ int s_warp[2][THREADS / 32];
+    __shared__ int s_base[2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    unsigned mw[4], md[4];
+    int nw = 0, nd = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        mw[q] = __ballot_sync(0xffffffffu, want[q]);
+        md[q] = __ballot_sync(0xffffffffu, dried[q]);
+        nw += __popc(mw[q]);
+        nd += __popc(md[q]);
+    }
+    if (lane == 0) {
+        s_warp[0][warp] = nw;
+        s_warp[1][warp] = nd;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        int tot = 0;
+        for (int w = 0; w < THREADS / 32; w++)
+            tot += s_warp[threadIdx.x][w];
+        s_base[threadIdx.x] = tot ? atomicAdd(threadIdx.x == 0 ? count : zcount, tot) : 0;
+    }
+    __syncthreads();
+    int bw = s_base[0], bd = s_base[1];
+    for (int w = 0; w < warp; w++) {
+        bw += s_warp[0][w];
+        bd += s_warp[1][w];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (want[q])
+            list[bw + __popc(mw[q] & below)] = value[q];
+        if (dried[q])
+            zlist[bd + __popc(md[q] & below)] = value[q];
+        bw += __popc(mw[q]);
+        bd += __popc(md[q]);
+    }
+}
+
 __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2Params p)
 {
     const int par = p.counts[4];
@@ -559,53 +615,77 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
     const int r = threadIdx.x / (TW / 4);       /* 0..15 */
     const int j4 = (threadIdx.x % (TW / 4)) * 4; /* 0, 4, ..., 60 */
     const int i = blockIdx.y * TH + r;
+    const int jb = blockIdx.x * TW + j4;
+    const long long c0 = (long long)i * p.cols + jb;
+    double hv[4] = {0.0, 0.0, 0.0, 0.0};
+    bool cell[4];
+    const bool full = i < p.rows && jb + 3 < p.cols && (p.cols & 1) == 0;
+    if (full) {
+        /* c0 is a multiple of 2 (jb and cols even): two 16-byte loads */
+        const double2 a = *reinterpret_cast<const double2*>(p.h + c0);
+        const double2 b = *reinterpret_cast<const double2*>(p.h + c0 + 2);
+        hv[0] = a.x;
+        hv[1] = a.y;
+        hv[2] = b.x;
+        hv[3] = b.y;
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            cell[q] = true;
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            cell[q] = i < p.rows && jb + q < p.cols;
+            if (cell[q])
+                hv[q] = p.h[c0 + q];
+        }
+    }
+    double hn[4];
+    bool want[4], dried[4];
+    int value[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        const int j = blockIdx.x * TW + j4 + q;
-        const bool cell = i < p.rows && j < p.cols;
-        const long long c = (long long)i * p.cols + j;
-        double hv = 0.0, hn = 0.0;
-        if (cell) {
-            hv = p.h[c];
-            hn = hv;
-            if (flagged) {
-                const double o0 = p.f[c], o1 = p.f[p.n + c], o2 = p.f[2 * p.n + c], o3 = p.f[3 * p.n + c];
-                /* inflow from neighbour n is its outflow f[4-n]; absent neighbours give 0 */
-                double in1 = 0.0, in2 = 0.0, in3 = 0.0, in4 = 0.0;
-                int a = i - 1, b = j - 1, d = j + 1, e = i + 1;
-                if (p.toroidal) {
-                    a = a < 0 ? a + p.rows : a;
-                    e = e >= p.rows ? e - p.rows : e;
-                    b = b < 0 ? b + p.cols : b;
-                    d = d >= p.cols ? d - p.cols : d;
-                }
-                if ((unsigned)a < (unsigned)p.rows)
-                    in1 = p.f[3 * p.n + (long long)a * p.cols + j];
-                if ((unsigned)b < (unsigned)p.cols)
-                    in2 = p.f[2 * p.n + (long long)i * p.cols + b];
-                if ((unsigned)d < (unsigned)p.cols)
-                    in3 = p.f[1 * p.n + (long long)i * p.cols + d];
-                if ((unsigned)e < (unsigned)p.rows)
-                    in4 = p.f[(long long)e * p.cols + j];
-                const long long any = __double_as_longlong(in1) | __double_as_longlong(in2) |
-                                      __double_as_longlong(in3) | __double_as_longlong(in4) |
-                                      __double_as_longlong(o0) | __double_as_longlong(o1) |
-                                      __double_as_longlong(o2) | __double_as_longlong(o3);
-                if (any != 0) {
-                    hn += in1 - o0;
-                    hn += in2 - o1;
-                    hn += in3 - o2;
-                    hn += in4 - o3;
-                    p.h[c] = hn;
-                }
+        const int j = jb + q;
+        const long long c = c0 + q;
+        hn[q] = hv[q];
+        if (flagged && cell[q]) {
+            const double o0 = p.f[c], o1 = p.f[p.n + c], o2 = p.f[2 * p.n + c], o3 = p.f[3 * p.n + c];
+            /* inflow from neighbour n is its outflow f[4-n]; absent neighbours give 0 */
+            double in1 = 0.0, in2 = 0.0, in3 = 0.0, in4 = 0.0;
+            int a = i - 1, b = j - 1, d = j + 1, e = i + 1;
+            if (p.toroidal) {
+                a = a < 0 ? a + p.rows : a;
+                e = e >= p.rows ? e - p.rows : e;
+                b = b < 0 ? b + p.cols : b;
+                d = d >= p.cols ? d - p.cols : d;
+            }
+            if ((unsigned)a < (unsigned)p.rows)
+                in1 = p.f[3 * p.n + (long long)a * p.cols + j];
+            if ((unsigned)b < (unsigned)p.cols)
+                in2 = p.f[2 * p.n + (long long)i * p.cols + b];
+            if ((unsigned)d < (unsigned)p.cols)
+                in3 = p.f[1 * p.n + (long long)i * p.cols + d];
+            if ((unsigned)e < (unsigned)p.rows)
+                in4 = p.f[(long long)e * p.cols + j];
+            const long long any = __double_as_longlong(in1) | __double_as_longlong(in2) |
+                                  __double_as_longlong(in3) | __double_as_longlong(in4) |
+                                  __double_as_longlong(o0) | __double_as_longlong(o1) |
+                                  __double_as_longlong(o2) | __double_as_longlong(o3);
+            if (any != 0) {
+                double x = hv[q];
+                x += in1 - o0;
+                x += in2 - o1;
+                x += in3 - o2;
+                x += in4 - o3;
+                hn[q] = x;
+                p.h[c] = x;
             }
         }
-        const bool wet_before = cell && sdt::is_wet(hv, p.eps_bits);
-        const bool wet_after = cell && sdt::is_wet(hn, p.eps_bits);
-        warp_append(wet_after, (int)c, list, count);
-        warp_append(wet_before && !wet_after, (int)c, zlist, zcount);
+        const bool wb = cell[q] && sdt::is_wet(hv[q], p.eps_bits);
+        want[q] = cell[q] && sdt::is_wet(hn[q], p.eps_bits);
+        dried[q] = wb && !want[q];
+        value[q] = (int)c;
     }
-    __syncthreads();
+    block_append4(want, dried, value, list, count, zlist, zcount);
     if (threadIdx.x == 0) {
         if (flagged)
             p.tflag[tile] = 0;
@@ -723,7 +803,7 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     b.eps_bits = eps_bits;
     if (ev)
         cudaEventRecord(ev[0], st);
-    k1_outflows<<<152 * 8, THREADS, 0, st>>>(a);
+    k1_outflows<<<152 * 32, K1_THREADS, 0, st>>>(a);
     if (ev)
         cudaEventRecord(ev[1], st);
     k2_update<<<dim3(s.tiles_x, s.tiles_y), THREADS, 0, st>>>(b);
@@ -788,9 +868,23 @@ static void sciddicaT_fused_transition(struct CALModel2D* ca)
     calSwapSubstate2Dr(ca, Q.h);
 }
 
+/* init of the fused/split program: the reference init, then the split
+ * step's priming, so that no recorded step ever contains the priming */
+static void sciddicaT_simulation_init_fused(struct CALModel2D* sciddicaT)
+{
+    sciddicaT_simulation_init(sciddicaT);
+    sciddicaT_split_invalidate();
+    sciddicaT_split_prepare(sciddicaT);
+}
+
 /* ======================= driver entry points ============================ */
 
 enum { SDT_MODE_PROCESSES = 0, SDT_MODE_FUSED = 1 };
+
+/* how many device-loop runs had to fall back to a launch sequence per step */
+static int g_fallbacks = 0;
+static void cal_note_fallback() { g_fallbacks++; }
+extern "C" int cal_sciddicaT_device_loop_fallbacks(void) { return g_fallbacks; }
 
 /* Runs SCIDDICA-T for `steps` steps on (z0, h0) and returns the final z, h
  * and active list -- the same contract as the oracle's orc_sciddicaT.
@@ -838,7 +932,7 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
     memcpy(Q.h->next, h0, bytes);
     calMarkHostDirty2D(ca);
 
-    calRunAddInitFunc2D(run, sciddicaT_simulation_init);
+    calRunAddInitFunc2D(run, mode == SDT_MODE_FUSED ? sciddicaT_simulation_init_fused : sciddicaT_simulation_init);
     if (mode == SDT_MODE_FUSED)
         calRunAddGlobalTransitionFunc2D(run, sciddicaT_fused_transition);
     else
@@ -851,12 +945,21 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     calRunInitSimulation2D(run);
-    if (mode == SDT_MODE_FUSED)
-        sciddicaT_split_prepare(ca);
     cudaEventRecord(e0, s);
-    for (run->step = run->initial_step; run->step <= run->final_step; run->step++)
-        if (!calRunCAStep2D(run))
-            break;
+    if (graph == 2) {
+        /* the whole step loop as one device-driven graph launch, bounded by
+         * the final step */
+        calRunDeviceSteps2D(run, run->initial_step, run->final_step);
+    } else if (graph == 3) {
+        /* the same, as an open loop ended by the device stop condition */
+        P.steps = steps;
+        calRunAddDeviceStopConditionFunc2D(run, sciddicaT_device_stop);
+        calRunDeviceSteps2D(run, run->initial_step, CAL_RUN_LOOP);
+    } else {
+        for (run->step = run->initial_step; run->step <= run->final_step; run->step++)
+            if (!calRunCAStep2D(run))
+                break;
+    }
     cudaEventRecord(e1, s);
     calRunFinalizeSimulation2D(run);
     calSync2D(ca);
@@ -866,6 +969,8 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
         *ms = t;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (graph >= 2 && !calRunDeviceLoopUsed2D(run) && calGetLastError() == CAL_SUCCESS)
+        cal_note_fallback();
 
     if (z_out)
         memcpy(z_out, Q.z->current, bytes);
@@ -938,7 +1043,7 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
     memcpy(Q.h->current, h0, s->bytes);
     memcpy(Q.h->next, h0, s->bytes);
     calMarkHostDirty2D(s->ca);
-    calRunAddInitFunc2D(s->run, sciddicaT_simulation_init);
+    calRunAddInitFunc2D(s->run, mode == SDT_MODE_FUSED ? sciddicaT_simulation_init_fused : sciddicaT_simulation_init);
     calRunInitSimulation2D(s->run);
     cudaStream_t st = (cudaStream_t)calGetStream2D(s->ca);
     for (int k = 0; k < 6; k++)
@@ -985,6 +1090,11 @@ extern "C" int cal_sciddicaT_steps(void* handle, int steps, int graph)
     SdtSession* s = (SdtSession*)handle;
     if (s->mode == SDT_MODE_FUSED)
         sciddicaT_split_prepare(s->ca);
+    if (graph == 2) {
+        /* one device-driven graph launch for all the steps */
+        calRunDeviceSteps2D(s->run, 1, steps);
+        return calGetLastError();
+    }
     calRunSetGraph2D(s->run, graph ? CAL_TRUE : CAL_FALSE);
     for (int k = 0; k < steps; k++)
         calRunCAStep2D(s->run);

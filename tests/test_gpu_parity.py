@@ -86,6 +86,21 @@ def test_sciddicaT_graph_replay_bit_exact(cal, orc, ac, mode):
     assert_same(got[2], ref[2], "active cells")
 
 
+@pytest.mark.parametrize("mode,ac,loop", [(1, 0, 2), (1, 0, 3), (0, 0, 2), (0, 1, 3)])
+def test_sciddicaT_device_loop_bit_exact(cal, orc, mode, ac, loop):
+    """calRunDeviceSteps2D: the whole run as one graph launch with a
+    conditional WHILE node (loop 2: bounded by the final step; loop 3: open
+    loop ended by a device stop condition)."""
+    import ctypes as C
+    z, h = W.sciddicaT_inputs(170, 160, seed=19)
+    ref = orc.sciddicaT(z, h, 45, toroidal=True, ac=ac)
+    before = cal.models().cal_sciddicaT_device_loop_fallbacks()
+    got = cal.sciddicaT(z, h, 45, toroidal=True, ac=ac, mode=mode, graph=loop)
+    assert_same(got[1], ref[1], "h")
+    assert_same(got[2], ref[2], "active cells")
+    assert cal.models().cal_sciddicaT_device_loop_fallbacks() == before, "device loop fell back"
+
+
 def _fmt9(h):
     return "".join("".join("%.9f  " % v for v in row) + "\n" for row in h).encode()
 
