@@ -228,6 +228,8 @@ static QT* add_substate(struct CALModel3D* ca, bool single)
     QT* q = (QT*)((char*)g.pool[TYPE] + 32 * slot);
     q->current = (decltype(q->current))cur;
     q->next = (decltype(q->next))next;
+    q->cal_reserved_[0] = &g; /* lets handle-only calls (getValue*AtIndex) find the grid */
+    q->cal_reserved_[1] = (void*)(intptr_t)slot;
     if (!single) {
         QT*** arr = TYPE == 0 ? (QT***)&ca->pQb_array : (TYPE == 1 ? (QT***)&ca->pQi_array : (QT***)&ca->pQr_array);
         int* n = TYPE == 0 ? &ca->sizeof_pQb_array : (TYPE == 1 ? &ca->sizeof_pQi_array : &ca->sizeof_pQr_array);

@@ -365,6 +365,8 @@ void CalGrid::destroy()
     cudaFree(d_block_counts);
     cudaFree(d_dirty);
     cudaFree(d_step);
+    cudaFree(d_reduce_partial);
+    cudaFree(d_reduce_result);
     if (h_flags)
         cudaFreeHost(h_flags);
     if (stream)

@@ -87,6 +87,8 @@ struct CalGrid {
 
     unsigned* d_dirty = nullptr; /* [3] written-substate bits */
     int* d_step = nullptr;       /* step counter of a device-driven run */
+    void* d_reduce_partial = nullptr; /* reduction scratch (per-block partials) */
+    void* d_reduce_result = nullptr;  /* reduction result read back by the host */
     int transfers = 0;           /* host<->device coherence copies made so far */
     long swaps = 0;              /* pointer swaps made so far */
     int capturing = 0;

@@ -324,3 +324,36 @@ extern "C" long cal_test_exact_div(const double* x_host, const int* c_host, cons
     cudaFree(li);
     return bad;
 }
+
+/* ======================= reductions ===================================== */
+#include "opencal/cal2DReduction.h"
+
+/* Reduce `data` (rows x cols of type 0 byte / 1 int / 2 real) with `op`
+ * through the C API; *out receives the result as a double. */
+extern "C" int cal_reduce2d_run(int type, int rows, int cols, const void* data, int op, double* out)
+{
+    calClearError();
+    struct CALModel2D* ca = calCADef2D(rows, cols, CAL_MOORE_NEIGHBORHOOD_2D, CAL_SPACE_TOROIDAL, CAL_NO_OPT);
+    if (!ca)
+        return calGetLastError();
+    const long long n = (long long)rows * cols;
+    if (type == 0) {
+        struct CALSubstate2Db* q = calAddSubstate2Db(ca);
+        memcpy(q->current, data, n);
+        calMarkHostDirty2D(ca);
+        *out = (double)calReductionOperation2Db(ca, q, (enum REDUCTION_OPERATION)op);
+    } else if (type == 1) {
+        struct CALSubstate2Di* q = calAddSubstate2Di(ca);
+        memcpy(q->current, data, n * sizeof(int));
+        calMarkHostDirty2D(ca);
+        *out = (double)calReductionOperation2Di(ca, q, (enum REDUCTION_OPERATION)op);
+    } else {
+        struct CALSubstate2Dr* q = calAddSubstate2Dr(ca);
+        memcpy(q->current, data, n * sizeof(double));
+        calMarkHostDirty2D(ca);
+        *out = calReductionOperation2Dr(ca, q, (enum REDUCTION_OPERATION)op);
+    }
+    int err = calGetLastError();
+    calFinalize2D(ca);
+    return err;
+}

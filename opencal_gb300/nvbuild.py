@@ -32,7 +32,7 @@ COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-cuda
 # model kernels restate reference arithmetic operation by operation: no FMA contraction
 MODEL_FLAGS = ["--fmad=false"]
 
-CORE_SOURCES = ["cal_core.cu", "cal2D.cu", "cal3D.cu", "cal2DRun.cu", "cal3DRun.cu", "calIO.cu", "cal_noalloc.cu"]
+CORE_SOURCES = ["cal_core.cu", "cal2D.cu", "cal3D.cu", "cal2DRun.cu", "cal3DRun.cu", "calIO.cu", "calReduction.cu", "cal_noalloc.cu"]
 MODEL_SOURCES = ["models/sciddicaT.cu", "models/life.cu", "models/probes.cu"]
 
 

@@ -6,7 +6,8 @@ import re
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADERS = ["calCommon.h", "cal2D.h", "cal2DRun.h", "cal2DIO.h", "cal3D.h", "cal3DRun.h", "cal3DIO.h"]
+HEADERS = ["calCommon.h", "cal2D.h", "cal2DRun.h", "cal2DIO.h", "cal2DReduction.h", "cal3D.h", "cal3DRun.h",
+           "cal3DIO.h", "cal3DReduction.h"]
 
 
 def declared_functions():
