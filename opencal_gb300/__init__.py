@@ -75,6 +75,14 @@ def models() -> C.CDLL:
     return _models
 
 
+def __getattr__(name):
+    # opencal_gb300.adjoint imports torch: load it on first use only
+    if name == "adjoint":
+        import importlib
+        return importlib.import_module(__name__ + ".adjoint")
+    raise AttributeError(name)
+
+
 def _check(rc: int, what: str) -> None:
     if rc != 0:
         msg = core().calGetErrorString()

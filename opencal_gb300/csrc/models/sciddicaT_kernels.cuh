@@ -1,0 +1,252 @@
+/*
+ * sciddicaT_kernels.cuh -- device code of the SCIDDICA-T step shared by the
+ * forward paths (sciddicaT.cu) and the adjoint (sciddicaT_adjoint.cu): the
+ * wet test, the outflow computation (the reference's minimisation of
+ * differences, operation by operation) and the single fused step kernel.
+ * Reference: OpenCAL-OMP/examples/calomp_sciddicaT/source/sciddicaT.c:36-100.
+ */
+#pragma once
+
+#include <stdlib.h>
+#include <string.h>
+
+#include "exact_div.cuh"
+
+namespace sdt {
+
+/* The fused step.  A block owns a TW x TH tile.  EP 1 (outflows) runs on the
+ * tile plus a ring of 1 cell -- EP 2 needs the outflows of every neighbour --
+ * so z and h are staged on the tile plus a ring of 2.  Shared memory holds
+ * z, h (load region) and the four outflows (outflow region). */
+constexpr int THREADS = 256;
+
+struct Params {
+    const double* __restrict__ z;
+    const double* __restrict__ h;
+    double* __restrict__ h_next;
+    int rows, cols;
+    int toroidal;
+    double eps, r;
+    long long eps_bits;
+};
+
+/* h > eps as the reference evaluates `!(h <= eps)`, on the bit pattern:
+ * for a non-negative double the IEEE encoding orders like the value; NaN
+ * compares false with <= and therefore counts as wet */
+static __device__ __forceinline__ bool is_wet(double h, long long eps_bits)
+{
+    const long long b = __double_as_longlong(h);
+    if (b >= 0)
+        return b > eps_bits;                                  /* +0 .. +inf, +NaN */
+    return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; /* -NaN; other negatives are dry */
+}
+
+/* The outflows of one wet cell, exactly as sciddicaT_flows_computation:
+ * the same additions in the same order; the division by the number of
+ * remaining cells and the comparisons are done on the integer pipe with
+ * bit-identical results (exact_div.cuh). */
+static __device__ __forceinline__ void outflows(double hc, double zc, const double u1, const double u2,
+                                                const double u3, const double u4, double eps, double r, double f[4])
+{
+    double u[5];
+    const double m = hc - eps;
+    u[0] = zc + eps;
+    u[1] = u1;
+    u[2] = u2;
+    u[3] = u3;
+    u[4] = u4;
+    unsigned elim = 0;
+    double average;
+    bool again;
+    do {
+        again = false;
+        average = m;
+        int cells_count = 0;
+#pragma unroll
+        for (int n = 0; n < 5; n++)
+            if (!(elim & (1u << n))) {
+                average += u[n];
+                cells_count++;
+            }
+        if (cells_count != 0)
+            average = cal_div_small(average, cells_count);
+#pragma unroll
+        for (int n = 0; n < 5; n++)
+            if (!(elim & (1u << n)) && cal_le(average, u[n])) {
+                elim |= 1u << n;
+                again = true;
+            }
+    } while (again);
+#pragma unroll
+    for (int n = 1; n < 5; n++)
+        f[n - 1] = (elim & (1u << n)) ? 0.0 : (average - u[n]) * r;
+}
+
+static __device__ __forceinline__ int wrapi(int x, int n)
+{
+    return x < 0 ? x + n : (x >= n ? x - n : x);
+}
+
+static __device__ __forceinline__ double plus_zero(double x)
+{
+    /* x + 0.0 without the FP64 pipe: only -0.0 changes (to +0.0) */
+    long long b = __double_as_longlong(x);
+    return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
+}
+
+template <int TW, int TH>
+struct Tile {
+    static constexpr int R1W = TW + 2, R1H = TH + 2; /* outflow region */
+    static constexpr int R2W = TW + 4, R2H = TH + 4; /* load region */
+    static constexpr size_t smem_bytes = sizeof(double) * (2 * R2W * R2H + 4 * R1W * R1H);
+};
+
+template <int TW, int TH>
+__global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Params p)
+{
+    using T = Tile<TW, TH>;
+    extern __shared__ __align__(16) double smem[];
+    double* sz = smem;                      /* [R2H][R2W] */
+    double* sh = sz + T::R2W * T::R2H;      /* [R2H][R2W] */
+    double* sf = sh + T::R2W * T::R2H;      /* [4][R1H][R1W] */
+    constexpr int F = T::R1W * T::R1H;
+
+    const int i0 = blockIdx.y * TH, j0 = blockIdx.x * TW;
+    const bool interior = i0 >= 2 && j0 >= 2 && i0 + TH + 2 <= p.rows && j0 + TW + 2 <= p.cols;
+
+    /* 1. z and h on the tile + 2 ring.  Interior tiles: 16-byte loads (j0-2
+     * is even, so every pair starts 16-byte aligned).  Edge tiles: flat ->
+     * 0 outside, toroidal -> wrapped. */
+    int wet_seen = 0;
+    if (interior) {
+        constexpr int PW = T::R2W / 2;
+        for (int t = threadIdx.x; t < PW * T::R2H; t += THREADS) {
+            const int a = t / PW, b = 2 * (t - a * PW);
+            const long long c = (long long)(i0 - 2 + a) * p.cols + (j0 - 2 + b);
+            const double2 zv = __ldg(reinterpret_cast<const double2*>(p.z + c));
+            const double2 hv = __ldg(reinterpret_cast<const double2*>(p.h + c));
+            *reinterpret_cast<double2*>(sz + a * T::R2W + b) = zv;
+            *reinterpret_cast<double2*>(sh + a * T::R2W + b) = hv;
+            wet_seen |= is_wet(hv.x, p.eps_bits) | is_wet(hv.y, p.eps_bits);
+        }
+    } else {
+        for (int t = threadIdx.x; t < T::R2H * T::R2W; t += THREADS) {
+            const int a = t / T::R2W, b = t - a * T::R2W;
+            int gi = i0 - 2 + a, gj = j0 - 2 + b;
+            double zv = 0.0, hv = 0.0;
+            bool inside = (unsigned)gi < (unsigned)p.rows && (unsigned)gj < (unsigned)p.cols;
+            if (!inside && p.toroidal) {
+                gi = wrapi(gi, p.rows);
+                gj = wrapi(gj, p.cols);
+                inside = true;
+            }
+            if (inside) {
+                const long long c = (long long)gi * p.cols + gj;
+                zv = __ldg(p.z + c);
+                hv = __ldg(p.h + c);
+            }
+            sz[t] = zv;
+            sh[t] = hv;
+            wet_seen |= is_wet(hv, p.eps_bits);
+        }
+    }
+    if (__syncthreads_or(wet_seen) == 0) {
+        /* no wet cell within two cells: h is unchanged (-0 becomes +0) */
+        for (int t = threadIdx.x; t < TH * TW; t += THREADS) {
+            const int a = t / TW, b = t - a * TW;
+            const int gi = i0 + a, gj = j0 + b;
+            if (gi < p.rows && gj < p.cols)
+                p.h_next[(long long)gi * p.cols + gj] = plus_zero(sh[(a + 2) * T::R2W + b + 2]);
+        }
+        return;
+    }
+
+    /* 2. EP 1 on the tile + 1 ring; cells outside a flat grid have none */
+    for (int t = threadIdx.x; t < F; t += THREADS) {
+        const int a = t / T::R1W, b = t - a * T::R1W;
+        const int gi = i0 - 1 + a, gj = j0 - 1 + b;
+        const bool inside = p.toroidal || ((unsigned)gi < (unsigned)p.rows && (unsigned)gj < (unsigned)p.cols);
+        const int c = (a + 1) * T::R2W + (b + 1); /* this cell in the load region */
+        const double hc = sh[c];
+        double f[4] = {0.0, 0.0, 0.0, 0.0};
+        if (inside && is_wet(hc, p.eps_bits)) {
+            /* von Neumann order n = 1..4: north, west, east, south; u = z + h */
+            const double u1 = sz[c - T::R2W] + sh[c - T::R2W];
+            const double u2 = sz[c - 1] + sh[c - 1];
+            const double u3 = sz[c + 1] + sh[c + 1];
+            const double u4 = sz[c + T::R2W] + sh[c + T::R2W];
+            outflows(hc, sz[c], u1, u2, u3, u4, p.eps, p.r, f);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            sf[q * F + t] = f[q];
+    }
+    __syncthreads();
+
+    /* 3. EP 2 on the tile: h' = h + sum_n (f_in(n) - f_out(n-1)), n = 1..4 */
+    for (int t = threadIdx.x; t < TH * TW; t += THREADS) {
+        const int a = t / TW, b = t - a * TW;
+        const int gi = i0 + a, gj = j0 + b;
+        if (gi >= p.rows || gj >= p.cols)
+            continue;
+        const int c = (a + 1) * T::R1W + (b + 1); /* this cell in the outflow region */
+        /* inflow from neighbour n is its outflow f[4-n] */
+        const double in1 = sf[3 * F + c - T::R1W], in2 = sf[2 * F + c - 1];
+        const double in3 = sf[1 * F + c + 1], in4 = sf[0 * F + c + T::R1W];
+        const double o0 = sf[0 * F + c], o1 = sf[1 * F + c], o2 = sf[2 * F + c], o3 = sf[3 * F + c];
+        const double hc = sh[(a + 2) * T::R2W + b + 2];
+        double hn;
+        const long long any = __double_as_longlong(in1) | __double_as_longlong(in2) | __double_as_longlong(in3) |
+                              __double_as_longlong(in4) | __double_as_longlong(o0) | __double_as_longlong(o1) |
+                              __double_as_longlong(o2) | __double_as_longlong(o3);
+        if (any == 0) {
+            hn = plus_zero(hc);
+        } else {
+            hn = hc;
+            hn += in1 - o0;
+            hn += in2 - o1;
+            hn += in3 - o2;
+            hn += in4 - o3;
+        }
+        p.h_next[(long long)gi * p.cols + gj] = hn;
+    }
+}
+
+template <int TW, int TH>
+static void launch(const Params& p, cudaStream_t s)
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(fused_step<TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)Tile<TW, TH>::smem_bytes);
+        attr_set = true;
+    }
+    dim3 grid((p.cols + TW - 1) / TW, (p.rows + TH - 1) / TH);
+    fused_step<TW, TH><<<grid, THREADS, Tile<TW, TH>::smem_bytes, s>>>(p);
+}
+
+/* tile shape: 64 x 32 by default; OPENCAL_SDT_TILE=32x16|64x16|64x32 overrides */
+static int tile_choice()
+{
+    static int choice = -1;
+    if (choice < 0) {
+        const char* e = getenv("OPENCAL_SDT_TILE");
+        choice = 2;
+        if (e && !strcmp(e, "32x16"))
+            choice = 0;
+        else if (e && !strcmp(e, "64x16"))
+            choice = 1;
+    }
+    return choice;
+}
+
+static void launch_step(const Params& p, cudaStream_t s)
+{
+    switch (tile_choice()) {
+    case 0: launch<32, 16>(p, s); break;
+    case 1: launch<64, 16>(p, s); break;
+    default: launch<64, 32>(p, s); break;
+    }
+}
+
+} // namespace sdt
