@@ -49,6 +49,9 @@ SEED = 2
 P_R, P_EPS = 0.5, 0.001
 BYTES_PER_CELL_UPDATE = 24  # z read + h read + h write (FP64)
 REF_SAMPLE_STEPS = 64
+# how the 4000 steps are issued: a launch sequence per step, a recorded step
+# replayed as a CUDA graph, or one device-driven graph launch for the loop
+LOOPS = {"eager": 0, "graph": 1, "device": 2}
 
 
 def _peaks():
@@ -220,7 +223,7 @@ def gpu_arm(args):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            m.cal_sciddicaT_steps(sess, CA_STEPS, 0)
+            m.cal_sciddicaT_steps(sess, CA_STEPS, LOOPS[args.loop])
             e1.record(stream)
         return e0, e1
 
@@ -291,7 +294,8 @@ def gpu_arm(args):
         "ms_per_step": float(np.mean(run_ms)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded DEM + elliptical source)",
         "config": {"workload": f"SCIDDICA-T {ROWS}x{COLS} FP64, von Neumann, flat, plain (no active cells), "
-                               f"{CA_STEPS} CA steps per bench step, fused step kernel",
+                               f"{CA_STEPS} CA steps per bench step, split step (outflows of wet cells, "
+                               f"update of flagged tiles), step loop: {args.loop}",
                    "l2": "flushed (256 MiB write) before every run", "seed": SEED, "p_r": P_R, "p_eps": P_EPS,
                    "parallelism": f"replicas x{world}"},
         "wall_s": t_wall,
@@ -346,6 +350,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="opencal", choices=["opencal", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--loop", default="eager", choices=sorted(LOOPS))
     ap.add_argument("--ncu-case", action="store_true", help="untimed fixed sequence for ncu captures")
     ap.add_argument("--ncu-steps", type=int, default=1002)
     args = ap.parse_args()

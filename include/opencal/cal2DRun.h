@@ -54,7 +54,9 @@ void calRun2D(struct CALRun2D* simulation);                                     
 void calRunFinalize2D(struct CALRun2D* cal2DRun);                                                    /* cal2DRun.h:108 */
 
 /* ---- opencal-gb300 additions --------------------------------------- */
-/* Record the step as a CUDA graph on first use and replay it afterwards. */
+/* Record the step as a CUDA graph on first use and replay it afterwards.
+ * Disabling drops a recorded step, so that a step whose launches change
+ * (new parameters baked into its kernels) is recorded again when re-enabled. */
 void calRunSetGraph2D(struct CALRun2D* simulation, CALbyte enable);
 /* Number of steps whose device work was replayed from the recorded graph. */
 long calRunGraphReplays2D(struct CALRun2D* simulation);

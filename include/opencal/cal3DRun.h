@@ -54,7 +54,9 @@ void calRun3D(struct CALRun3D* simulation);                                     
 void calRunFinalize3D(struct CALRun3D* cal3DRun);                                                    /* cal3DRun.h:103 */
 
 /* ---- opencal-gb300 additions --------------------------------------- */
-/* Record the step as a CUDA graph on first use and replay it afterwards. */
+/* Record the step as a CUDA graph on first use and replay it afterwards.
+ * Disabling drops a recorded step, so that a step whose launches change
+ * (new parameters baked into its kernels) is recorded again when re-enabled. */
 void calRunSetGraph3D(struct CALRun3D* simulation, CALbyte enable);
 /* Number of steps whose device work was replayed from the recorded graph. */
 long calRunGraphReplays3D(struct CALRun3D* simulation);

@@ -1,0 +1,95 @@
+/*
+ * calModels.h -- entry points of libopencal_models.so: the reference's
+ * example programs built on the C API (cal2D.h / cal3D.h) as callable
+ * drivers, plus the calibration machinery of SCIDDICA-T.
+ *
+ * The reference ships these programs as executables with a main()
+ * (OpenCAL-OMP/examples/calomp_sciddicaT/source/sciddicaT.c,
+ * OpenCAL-OMP/examples/calomp_life/source/life.c, ...); none of the functions
+ * below has a counterpart in the reference's library.  They exist so that
+ * tests, the benchmark and calibration code can run those programs on given
+ * inputs and read the results back.  Arrays are host memory unless a comment
+ * says device; every function returns 0 (CAL_SUCCESS) or an error code
+ * unless it returns a handle (NULL on failure).
+ */
+#ifndef calModels_h
+#define calModels_h
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- SCIDDICA-T (OpenCAL-OMP/examples/calomp_sciddicaT/source/sciddicaT.c) ---- */
+
+/* mode: 0 = the reference program (device elementary processes registered
+ * with calAddElementaryProcess2D, steering, calRun2D); 1 = the same program
+ * with the split step as its global transition (plain only).  graph: 0 =
+ * launch sequence per step, 1 = recorded step replayed, 2 = device-driven
+ * loop bounded by the final step, 3 = device loop ended by a device stop
+ * condition.  n_active / cells_out: the active cells after the run (ac). */
+int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int steps, double p_r, double p_eps, const double* z0,
+                      const double* h0, double* z_out, double* h_out, long* n_active, int* cells_out, int mode,
+                      int graph, double* ms);
+/* how many device-loop runs fell back to a launch sequence per step */
+int cal_sciddicaT_device_loop_fallbacks(void);
+
+/* A session: the program created once, reset to its initial state and rerun.
+ * The program's substates are globals, as in the reference's example: one
+ * session is open at a time. */
+void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, double p_r, double p_eps, const double* z0,
+                         const double* h0, int mode);
+int cal_sciddicaT_reset(void* session);
+int cal_sciddicaT_steps(void* session, int steps, int graph);
+int cal_sciddicaT_set_params(void* session, double p_r, double p_eps);
+void* cal_sciddicaT_stream(void* session); /* cudaStream_t of the model */
+int cal_sciddicaT_host_run(void* session, const double* z_host, const double* h_host, int steps, double* h_out);
+int cal_sciddicaT_kernel_times(void* session, int n, float* ms_outflows, float* ms_update);
+int cal_sciddicaT_wet_count(void* session);
+int cal_sciddicaT_read(void* session, double* h_out);
+void cal_sciddicaT_close(void* session);
+
+/* ---- SCIDDICA-T adjoint (one grid; device arrays) ---- */
+void* cal_sdt_adj_create(int rows, int cols, int steps, int toroidal);
+void cal_sdt_adj_destroy(void* work);
+int cal_sdt_adj_forward(void* work, const double* z_dem, const double* h0, double p_r, double p_eps, double* hT,
+                        void* stream);
+int cal_sdt_adj_backward(void* work, const double* dL_dhT, double* dL_dh0, double* dL_dpr, double* dL_dpeps,
+                         void* stream);
+
+/* ---- SCIDDICA-T ensembles (many grids, one launch per step) ----
+ * dims: 2B ints (rows, cols); params: 2B doubles (p_r, p_eps); z_dem, h0:
+ * the instances' values back to back (unpadded, row-major).  Device arrays
+ * of the ensemble use the padded layout given by cal_sdt_batch_cells. */
+void* cal_sdt_batch_create(int B, const int* dims, const double* params, const double* z_dem, const double* h0,
+                           int steps);
+void cal_sdt_batch_destroy(void* ensemble);
+long long cal_sdt_batch_cells(void* ensemble, long long* offsets /* B + 1, or NULL */);
+void* cal_sdt_batch_stream(void* ensemble);
+int cal_sdt_batch_shape(void* ensemble);
+int cal_sdt_batch_set_shape(void* ensemble, int shape /* 0: 32x16, 1: 64x16, 2: 64x32 */);
+int cal_sdt_batch_autotune(void* ensemble, int probe_steps, float* ms /* 3 */);
+int cal_sdt_batch_set_params(void* ensemble, const double* params);
+int cal_sdt_batch_forward(void* ensemble, double* hT /* device, or NULL */);
+int cal_sdt_batch_active_tiles(void* ensemble, int* counts /* steps + 1 */);
+int cal_sdt_batch_loss_grad(void* ensemble, const double* target /* device */, double* loss /* B */,
+                            double* grad /* 2B */, double* dL_dh0 /* device, or NULL */);
+
+/* ---- Game of Life (OpenCAL-OMP/examples/calomp_life) and the 3D rule ---- */
+int cal_life2d_run(int rows, int cols, int toroidal, int as_int, int steps, const unsigned char* s0,
+                   unsigned char* s_out, int mode, int block, int graph, double* ms);
+int cal_life3d_run(int rows, int cols, int slices, int nbhd, int toroidal, int steps, int r1, int r2, int r3, int r4,
+                   const unsigned char* s0, unsigned char* s_out, int graph);
+
+/* ---- engine probes used by the parity tests ---- */
+int cal_nbprobe2d_run(int rows, int cols, int nbhd, int toroidal, int steps, const double* v0, double* v_out,
+                      int graph);
+int cal_acprobe_run(int dim, int rows, int cols, int slices, int nbhd, int toroidal, int steps, double thr,
+                    const double* v0, double* v_out, long* n_active, int* cells_out, int graph);
+int cal_reduce2d_run(int type, int rows, int cols, const void* data, int op, double* out);
+long cal_test_exact_div(const double* x, const int* c, const double* y, long long n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -365,8 +365,17 @@ extern "C" int calRunDeviceLoopUsed2D(struct CALRun2D* sim)
 
 extern "C" void calRunSetGraph2D(struct CALRun2D* sim, CALbyte enable)
 {
-    if (sim && sim->gpu)
-        sim->gpu->graph_enabled = enable != 0;
+    if (!sim || !sim->gpu)
+        return;
+    if (!enable && sim->gpu->exec) {
+        /* a recorded step is dropped: the next enabled step records anew */
+        cudaGraphExecDestroy(sim->gpu->exec);
+        sim->gpu->exec = nullptr;
+        if (sim->gpu->graph)
+            cudaGraphDestroy(sim->gpu->graph);
+        sim->gpu->graph = nullptr;
+    }
+    sim->gpu->graph_enabled = enable != 0;
 }
 
 extern "C" long calRunGraphReplays2D(struct CALRun2D* sim)

@@ -175,17 +175,21 @@ static void sciddicaT_steering_ac(struct CALModel2D* sciddicaT)
  *      steering gives them) and flags the K2 tiles that will read them.  It
  *      also clears the outflows of cells that dried up in the previous step
  *      (a second list, disjoint from the first).
- *   K2 (thickness update): one pass over EVERY cell, h updated in place
- *      (each cell reads and writes only its own h; the outflows it reads
- *      were completed by K1).  In tiles K1 did not flag every outflow is +0,
- *      so h is unchanged and only read; flagged tiles sum the eight outflow
- *      terms in the reference's order.  K2 then applies EP 1's wet test to
- *      the new h and appends wet cells (and cells that just dried) to the
- *      next step's lists with warp ballots.
+ *   K2 (thickness update): only the tiles K1 flagged.  K1 appends every
+ *      tile it flags to a tile work-list once per step (the flag is an epoch
+ *      stamp, so it never needs clearing); K2 is a fixed grid of blocks that
+ *      take work items from that list and update their tile's h in place
+ *      (each cell reads and writes only its own h; the outflows it reads were
+ *      completed by K1), then apply EP 1's wet test to the new h and append
+ *      wet cells (and cells that just dried) to the next step's lists.  In
+ *      every other tile all outflows in and out are +0, so h is unchanged
+ *      bit for bit: K2's remaining work items carry the wet cells of the
+ *      current list that lie in unflagged tiles over to the next list.
  *
- * Every cell is visited by every step, as in the reference; the EP 1 body
- * runs exactly on the cells where the reference runs it (h > epsilon).  The
- * lists' order does not matter: each cell's result depends only on its
+ * The result is the reference's: EP 1's body runs exactly on the cells
+ * where the reference runs it (h > epsilon), and a cell EP 2 does not visit
+ * here is one where the reference's EP 2 adds eight zero terms.  The lists'
+ * order does not matter: each cell's result depends only on its
  * neighbourhood.  A priming kernel canonicalises -0 to +0 in h (the first
  * reference step adds 0.0 to every cell) and builds the first wet list. */
 namespace sdt2 {
@@ -199,17 +203,20 @@ struct State {
     int* list[2] = {nullptr, nullptr};
     int* zlist[2] = {nullptr, nullptr};
     int* counts = nullptr;       /* [0..1] wet list lengths, [2..3] dried list lengths,
-                                    [4] list parity, [5] K2 block ticket */
-    unsigned char* tflag = nullptr;
+                                    [4] list parity, [5] K2 block ticket, [6] step epoch,
+                                    [7] flagged tiles */
+    int* tflag = nullptr;        /* per K2 tile: epoch of the step that flagged it */
+    int* tlist = nullptr;        /* flagged tiles of the current step */
     long long n = 0;
     int tiles_x = 0, tiles_y = 0;
     bool primed = false;
 };
 
 /* The lists alternate between two buffers; which one a step reads is the
- * parity word counts[4], flipped by the last K2 block of the step.  Keeping
- * it in device memory makes every step's launches identical, so a step can
- * be recorded once as a CUDA graph and replayed. */
+ * parity word counts[4], flipped by the last K2 block of the step, which
+ * also advances the epoch counts[6] and empties the tile list counts[7].
+ * Keeping them in device memory makes every step's launches identical, so a
+ * step can be recorded once as a CUDA graph and replayed. */
 struct K1Params {
     const double* __restrict__ z;
     const double* __restrict__ h;
@@ -219,7 +226,8 @@ struct K1Params {
     int* zlist0;
     int* zlist1;
     int* counts;
-    unsigned char* tflag;
+    int* tflag;
+    int* tlist;
     int rows, cols, toroidal, tiles_x;
     long long n;
     double eps, r;
@@ -233,7 +241,8 @@ struct K2Params {
     int* zlist0;
     int* zlist1;
     int* counts;
-    unsigned char* tflag;
+    const int* tflag;
+    const int* tlist;
     int rows, cols, toroidal, tiles_x;
     long long n;
     long long eps_bits;
@@ -245,10 +254,19 @@ static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
 }
 
 constexpr int K1_THREADS = 64; /* small blocks: the wet list spreads over every SM */
+constexpr int K2_BLOCKS = 152 * 4;
+
+/* flag tile t for this step's K2 and append it to the work-list once */
+static __device__ __forceinline__ void flag_tile(int* tflag, int* tlist, int* tcount, int t, int epoch)
+{
+    if (tflag[t] != epoch && atomicExch(tflag + t, epoch) != epoch)
+        tlist[atomicAdd(tcount, 1)] = t;
+}
 
 __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant__ K1Params p)
 {
     const int par = p.counts[4];
+    const int epoch = p.counts[6];
     const int* list = par ? p.list1 : p.list0;
     const int* zlist = par ? p.zlist1 : p.zlist0;
     if (blockIdx.x == 0 && threadIdx.x < 2)
@@ -289,12 +307,12 @@ __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant_
             p.f[q * p.n + c] = f[q];
             if (__double_as_longlong(f[q]) != 0) {
                 any = true;
-                if (in[q])
-                    p.tflag[tile_of(ni[q], nj[q], p.tiles_x)] = 1; /* the receiver reads it */
+                if (in[q]) /* the receiver reads it */
+                    flag_tile(p.tflag, p.tlist, p.counts + 7, tile_of(ni[q], nj[q], p.tiles_x), epoch);
             }
         }
         if (any)
-            p.tflag[tile_of(i, j, p.tiles_x)] = 1;
+            flag_tile(p.tflag, p.tlist, p.counts + 7, tile_of(i, j, p.tiles_x), epoch);
     }
     const int nz = p.counts[2 + par];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nz; k += stride) {
@@ -366,19 +384,15 @@ static __device__ __forceinline__ void block_append4(const bool want[4], const b
     }
 }
 
-__global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2Params p)
+/* one flagged tile: h += inflows - outflows in place, then the wet test */
+static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int* list, int* count, int* zlist,
+                                               int* zcount)
 {
-    const int par = p.counts[4];
-    int* list = par ? p.list0 : p.list1; /* next step's lists */
-    int* zlist = par ? p.zlist0 : p.zlist1;
-    int* count = p.counts + (1 - par);
-    int* zcount = p.counts + 2 + (1 - par);
-    const int tile = blockIdx.y * p.tiles_x + blockIdx.x;
-    const bool flagged = p.tflag[tile] != 0;
+    const int ty = tile / p.tiles_x, tx = tile - ty * p.tiles_x;
     const int r = threadIdx.x / (TW / 4);       /* 0..15 */
     const int j4 = (threadIdx.x % (TW / 4)) * 4; /* 0, 4, ..., 60 */
-    const int i = blockIdx.y * TH + r;
-    const int jb = blockIdx.x * TW + j4;
+    const int i = ty * TH + r;
+    const int jb = tx * TW + j4;
     const long long c0 = (long long)i * p.cols + jb;
     double hv[4] = {0.0, 0.0, 0.0, 0.0};
     bool cell[4];
@@ -402,15 +416,14 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
                 hv[q] = p.h[c0 + q];
         }
     }
-    double hn[4];
     bool want[4], dried[4];
     int value[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int j = jb + q;
         const long long c = c0 + q;
-        hn[q] = hv[q];
-        if (flagged && cell[q]) {
+        double hn = hv[q];
+        if (cell[q]) {
             const double o0 = p.f[c], o1 = p.f[p.n + c], o2 = p.f[2 * p.n + c], o3 = p.f[3 * p.n + c];
             /* inflow from neighbour n is its outflow f[4-n]; absent neighbours give 0 */
             double in1 = 0.0, in2 = 0.0, in3 = 0.0, in4 = 0.0;
@@ -439,26 +452,59 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
                 x += in2 - o1;
                 x += in3 - o2;
                 x += in4 - o3;
-                hn[q] = x;
+                hn = x;
                 p.h[c] = x;
             }
         }
         const bool wb = cell[q] && sdt::is_wet(hv[q], p.eps_bits);
-        want[q] = cell[q] && sdt::is_wet(hn[q], p.eps_bits);
+        want[q] = cell[q] && sdt::is_wet(hn, p.eps_bits);
         dried[q] = wb && !want[q];
         value[q] = (int)c;
     }
     block_append4(want, dried, value, list, count, zlist, zcount);
+}
+
+/* K2: a fixed grid working through the flagged tiles, then through the
+ * current wet list in chunks of THREADS entries (carrying over the wet
+ * cells of unflagged tiles, whose h did not change) */
+__global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2Params p)
+{
+    const int par = p.counts[4];
+    const int epoch = p.counts[6];
+    const int ntiles = p.counts[7];
+    const int nwet = p.counts[par];
+    const int* cur = par ? p.list1 : p.list0;
+    int* list = par ? p.list0 : p.list1; /* next step's lists */
+    int* zlist = par ? p.zlist0 : p.zlist1;
+    int* count = p.counts + (1 - par);
+    int* zcount = p.counts + 2 + (1 - par);
+    const int items = ntiles + (nwet + THREADS - 1) / THREADS;
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        if (item < ntiles) {
+            k2_tile(p, p.tlist[item], list, count, zlist, zcount);
+            __syncthreads(); /* block_append4's shared words are reused */
+        } else {
+            const int k = (item - ntiles) * THREADS + threadIdx.x;
+            bool carry = false;
+            int c = 0;
+            if (k < nwet) {
+                c = cur[k];
+                const int i = c / p.cols, j = c - i * p.cols;
+                carry = p.tflag[tile_of(i, j, p.tiles_x)] != epoch;
+            }
+            warp_append(carry, c, list, count);
+        }
+    }
     if (threadIdx.x == 0) {
-        if (flagged)
-            p.tflag[tile] = 0;
-        /* every block read the parity at its start; the last one to finish
-         * flips it for the next step (no block waits for another) */
+        /* every block read parity, epoch and counts at its start; the last
+         * one to finish advances them for the next step (no block waits for
+         * another) */
         __threadfence();
-        const unsigned nblocks = gridDim.x * gridDim.y;
-        if (atomicAdd(reinterpret_cast<unsigned*>(p.counts + 5), 1u) == nblocks - 1) {
+        if (atomicAdd(reinterpret_cast<unsigned*>(p.counts + 5), 1u) == gridDim.x - 1) {
             p.counts[4] = 1 - par;
             p.counts[5] = 0;
+            p.counts[6] = epoch + 1;
+            p.counts[7] = 0;
         }
     }
 }
@@ -466,6 +512,8 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
 /* -0 -> +0 in h and the first wet list (counts[parity] must be 0) */
 __global__ void __launch_bounds__(THREADS) k_prime(double* h, long long n, long long eps_bits, int* list, int* count)
 {
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        count[6] = 1; /* first epoch (tile stamps start at 0) */
     for (long long c0 = (long long)blockIdx.x * blockDim.x; c0 < n; c0 += (long long)gridDim.x * blockDim.x) {
         const long long c = c0 + threadIdx.x;
         bool wet = false;
@@ -491,6 +539,7 @@ static void release()
     }
     cudaFree(s.counts);
     cudaFree(s.tflag);
+    cudaFree(s.tlist);
     s = State();
 }
 
@@ -507,7 +556,8 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         s.tiles_y = (ca->rows + TH - 1) / TH;
         bool ok = cudaMalloc(&s.f, 4 * n * sizeof(double)) == cudaSuccess &&
                   cudaMalloc(&s.counts, 8 * sizeof(int)) == cudaSuccess &&
-                  cudaMalloc(&s.tflag, (size_t)s.tiles_x * s.tiles_y) == cudaSuccess;
+                  cudaMalloc(&s.tflag, sizeof(int) * s.tiles_x * s.tiles_y) == cudaSuccess &&
+                  cudaMalloc(&s.tlist, sizeof(int) * s.tiles_x * s.tiles_y) == cudaSuccess;
         for (int k = 0; k < 2 && ok; k++)
             ok = cudaMalloc(&s.list[k], n * sizeof(int)) == cudaSuccess &&
                  cudaMalloc(&s.zlist[k], n * sizeof(int)) == cudaSuccess;
@@ -517,8 +567,8 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         }
     }
     cudaMemsetAsync(s.f, 0, 4 * n * sizeof(double), st);
-    cudaMemsetAsync(s.counts, 0, 8 * sizeof(int), st); /* parity 0, ticket 0 */
-    cudaMemsetAsync(s.tflag, 0, (size_t)s.tiles_x * s.tiles_y, st);
+    cudaMemsetAsync(s.counts, 0, 8 * sizeof(int), st); /* parity 0, ticket 0, no flagged tile */
+    cudaMemsetAsync(s.tflag, 0, sizeof(int) * s.tiles_x * s.tiles_y, st);
     int blocks = (int)((n + THREADS - 1) / THREADS);
     if (blocks > 152 * 16)
         blocks = 152 * 16;
@@ -542,6 +592,7 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     a.zlist1 = s.zlist[1];
     a.counts = s.counts;
     a.tflag = s.tflag;
+    a.tlist = s.tlist;
     a.rows = ca->rows;
     a.cols = ca->columns;
     a.toroidal = ca->T == CAL_SPACE_TOROIDAL;
@@ -558,6 +609,7 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     b.zlist1 = s.zlist[1];
     b.counts = s.counts;
     b.tflag = s.tflag;
+    b.tlist = s.tlist;
     b.rows = ca->rows;
     b.cols = ca->columns;
     b.toroidal = a.toroidal;
@@ -569,7 +621,7 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     k1_outflows<<<152 * 32, K1_THREADS, 0, st>>>(a);
     if (ev)
         cudaEventRecord(ev[1], st);
-    k2_update<<<dim3(s.tiles_x, s.tiles_y), THREADS, 0, st>>>(b);
+    k2_update<<<K2_BLOCKS, THREADS, 0, st>>>(b);
     if (ev)
         cudaEventRecord(ev[2], st);
     return cudaGetLastError() == cudaSuccess;
@@ -864,6 +916,17 @@ extern "C" int cal_sciddicaT_steps(void* handle, int steps, int graph)
     return calGetLastError();
 }
 
+/* new p_r, p_epsilon for the following runs of the session (a recorded
+ * step, which bakes them into its launches, is dropped) */
+extern "C" int cal_sciddicaT_set_params(void* handle, double p_r, double p_eps)
+{
+    SdtSession* s = (SdtSession*)handle;
+    P.r = p_r;
+    P.epsilon = p_eps;
+    calRunSetGraph2D(s->run, CAL_FALSE);
+    return calGetLastError();
+}
+
 extern "C" void* cal_sciddicaT_stream(void* handle) { return calGetStream2D(((SdtSession*)handle)->ca); }
 
 /* host-buffer round trip through the API: load z and h into the host
@@ -919,10 +982,13 @@ extern "C" int cal_sciddicaT_kernel_times(void* handle, int n, float* ms_a, floa
 /* number of wet cells the split step will process next (synchronises) */
 extern "C" int cal_sciddicaT_wet_count(void* handle)
 {
-    (void)handle;
+    SdtSession* s = (SdtSession*)handle;
     int c[6] = {-1, -1, -1, -1, 0, 0};
-    if (sdt2::g_state.counts)
+    if (sdt2::g_state.counts) {
+        /* the model's stream does not synchronise with the legacy stream */
+        cudaStreamSynchronize((cudaStream_t)calGetStream2D(s->ca));
         cudaMemcpy(c, sdt2::g_state.counts, sizeof(c), cudaMemcpyDeviceToHost);
+    }
     return c[c[4] & 1];
 }
 

@@ -1,0 +1,813 @@
+/*
+ * sciddicaT_batch.cu -- an ensemble of independent SCIDDICA-T instances
+ * (calibration ensembles, scenarios) advanced together, forward and adjoint.
+ * Every instance is the plain program of OpenCAL/examples/cal_sciddicaT
+ * (flat boundary, von Neumann, EP 1 outflows + EP 2 width update,
+ * OpenCAL-OMP/examples/calomp_sciddicaT/source/sciddicaT.c), each with its
+ * own grid size, DEM, source, p_r and p_epsilon.
+ *
+ * Layout.  The fields of all instances are packed back to back, one
+ * allocation per field; instance b occupies [off_b, off_b + rows_b*cols_b)
+ * with off_b a multiple of 32 cells (256 bytes), so every instance's rows
+ * start 16-byte aligned when its column count is even.  A device table holds
+ * per-instance dimensions and parameters.  Each instance is cut into
+ * TW x TH tiles; the tiles of all instances are numbered in one range.
+ *
+ * Forward.  One launch per step over a packed tile WORK-LIST L_t spanning
+ * every instance: a fixed grid of blocks takes tiles from the list, looks up
+ * the tile's instance and origin, and runs the fused step on it (the device
+ * function of the single-model fused kernel, so every instance stays
+ * bit-identical to a run of its own).  h ping-pongs between two buffers.  A
+ * tile can only change in a step if it holds a wet cell or borders one, so
+ * L_t = dilate(W_{t-1}) u dilate(W_t), with W_t the tiles holding a wet cell
+ * of h_t and dilate() the 3 x 3 tile neighbourhood: a tile that processed
+ * step t marks its neighbourhood for step t+1 when it held a wet cell before
+ * or after the step (an epoch stamp per tile keeps each tile once per list).
+ * Invariant: the input buffer of step t holds h_t everywhere, because a tile
+ * left out of L_t was unchanged by steps t-1 and t, so both buffers hold its
+ * value.  Dry tiles far from the flow cost nothing.
+ *
+ * Adjoint.  sqrt(T) checkpointing: h is stored every K = ceil(sqrt(T))
+ * steps.  The backward recomputes one segment from its checkpoint with the
+ * stored work-lists and, doing so, TAPES each processed tile's input
+ * values; reversing the segment, it restores the taped tiles of step t into
+ * the state (turning h_{t+1} into h_t in place: the other tiles did not
+ * change) and runs the adjoint kernels on the tiles of L_t only (lambda
+ * changes only within one cell of a wet cell).  The adjoint of one step is
+ * the single-model one (sciddicaT_adjoint.cu): elimination sets recomputed
+ * bit-identically from h_t and frozen; lambda is updated in place; per-
+ * instance dL/dp_r and dL/dp_eps are block-reduced per tile and added with
+ * one atomic per tile (so their summation order is not fixed).
+ *
+ * Tile shape is chosen by a small autotuner (cal_sdt_batch_autotune): each
+ * candidate shape times a forward probe with CUDA events and the fastest is
+ * kept for the ensemble.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "sciddicaT_kernels.cuh"
+
+namespace sdtb {
+
+constexpr int T = 256;
+constexpr int MAX_INST = 4096;
+constexpr long long ALIGN = 32; /* cells */
+
+struct Inst {
+    int rows, cols;
+    long long off;
+    double r, eps;
+    long long eps_bits;
+    int tiles_x, tiles_y, tile0, pad;
+};
+
+struct Shape {
+    int tw, th;
+};
+static const Shape kShapes[3] = {{32, 16}, {64, 16}, {64, 32}};
+
+struct Batch {
+    int B = 0, steps = 0, K = 0, nseg = 0, shape = 1;
+    long long N = 0; /* padded cells */
+    int ntiles = 0;
+    std::vector<Inst> inst;
+    std::vector<long long> offs; /* B + 1 (offs[B] = N) */
+    Inst* d_inst = nullptr;
+    long long* d_offs = nullptr;
+    int* d_tile_inst = nullptr;
+    int* stamps = nullptr;
+    int* lists = nullptr;  /* (steps + 1) x ntiles */
+    int* counts = nullptr; /* steps + 1 */
+    std::vector<int> h_counts;
+    double *z_dem = nullptr, *z = nullptr, *h0 = nullptr;
+    double* hbuf[2] = {nullptr, nullptr};
+    double* ckpt = nullptr; /* nseg x N */
+    double* tape = nullptr;
+    size_t tape_cap = 0;    /* doubles */
+    double *lam = nullptr, *lamz = nullptr, *g = nullptr, *gz = nullptr, *w = nullptr;
+    double* grad = nullptr; /* 2B: dL/dr[0..B), dL/deps[B..2B) */
+    double* loss = nullptr; /* B */
+    cudaStream_t st = nullptr;
+};
+
+static int tile_cells(const Batch& bt) { return kShapes[bt.shape].tw * kShapes[bt.shape].th; }
+
+/* re-tile every instance for the current shape */
+static bool tiles_for(Batch& bt)
+{
+    const int tw = kShapes[bt.shape].tw, th = kShapes[bt.shape].th;
+    std::vector<int> tinst;
+    for (int b = 0; b < bt.B; b++) {
+        Inst& I = bt.inst[b];
+        I.tiles_x = (I.cols + tw - 1) / tw;
+        I.tiles_y = (I.rows + th - 1) / th;
+        I.tile0 = (int)tinst.size();
+        tinst.insert(tinst.end(), (size_t)I.tiles_x * I.tiles_y, b);
+    }
+    bt.ntiles = (int)tinst.size();
+    cudaStreamSynchronize(bt.st);
+    cudaFree(bt.d_tile_inst);
+    cudaFree(bt.stamps);
+    cudaFree(bt.lists);
+    bt.d_tile_inst = nullptr;
+    bt.stamps = nullptr;
+    bt.lists = nullptr;
+    bool ok = cudaMalloc(&bt.d_tile_inst, sizeof(int) * tinst.size()) == cudaSuccess &&
+              cudaMalloc(&bt.stamps, sizeof(int) * tinst.size()) == cudaSuccess &&
+              cudaMalloc(&bt.lists, sizeof(int) * (size_t)bt.ntiles * (bt.steps + 1)) == cudaSuccess;
+    if (!ok)
+        return false;
+    cudaMemcpy(bt.d_tile_inst, tinst.data(), sizeof(int) * tinst.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(bt.d_inst, bt.inst.data(), sizeof(Inst) * bt.B, cudaMemcpyHostToDevice);
+    return true;
+}
+
+static __device__ __forceinline__ sdt::Params params_of(const Inst& I, const double* z, const double* h, double* hn)
+{
+    sdt::Params p;
+    p.z = z + I.off;
+    p.h = h + I.off;
+    p.h_next = hn + I.off;
+    p.rows = I.rows;
+    p.cols = I.cols;
+    p.toroidal = 0;
+    p.eps = I.eps;
+    p.r = I.r;
+    p.eps_bits = I.eps_bits;
+    return p;
+}
+
+/* instance of packed cell c (offsets in shared memory); false on padding */
+static __device__ __forceinline__ bool locate(const long long* s_offs, const Inst* inst, int B, long long c, int* b)
+{
+    int lo = 0, hi = B - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_offs[mid] <= c)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    *b = lo;
+    return c - s_offs[lo] < (long long)inst[lo].rows * inst[lo].cols;
+}
+
+/* put tile t into list `list`/`count` for the step whose stamp is `stamp` */
+static __device__ __forceinline__ void mark(int* stamps, int* list, int* count, int t, int stamp)
+{
+    if (stamps[t] != stamp && atomicExch(stamps + t, stamp) != stamp)
+        list[atomicAdd(count, 1)] = t;
+}
+
+/* One ensemble step over the work-list (list, *count): h -> hn.  With a
+ * next list the following step's list is built; with a tape the processed
+ * tiles' input values are saved (tile k of the list at tape + k * TW * TH). */
+template <int TW, int TH>
+__global__ void __launch_bounds__(sdt::THREADS) k_step(const Inst* __restrict__ inst, const int* __restrict__ tile_inst,
+                                                       const double* __restrict__ z, const double* __restrict__ h,
+                                                       double* __restrict__ hn, const int* __restrict__ list,
+                                                       const int* __restrict__ count, int* list_next, int* count_next,
+                                                       int* stamps, int stamp, double* __restrict__ tape)
+{
+    extern __shared__ __align__(16) double smem[];
+    using TL = sdt::Tile<TW, TH>;
+    const int n = *count;
+    for (int k = blockIdx.x; k < n; k += gridDim.x) {
+        const int t = list[k];
+        const Inst I = inst[tile_inst[t]];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        const sdt::Params p = params_of(I, z, h, hn);
+        const int wet = sdt::fused_tile<TW, TH, true>(p, ty * TH, tx * TW, smem);
+        if (tape) {
+            /* the tile's input h is still in shared memory (load region, +2 ring) */
+            const double* sh = smem + TL::R2W * TL::R2H;
+            double* dst = tape + (size_t)k * (TW * TH);
+            for (int c = threadIdx.x; c < TW * TH; c += sdt::THREADS) {
+                const int a = c / TW, b = c - a * TW;
+                dst[c] = sh[(a + 2) * TL::R2W + b + 2];
+            }
+        }
+        if (list_next && wet && threadIdx.x < 9) {
+            const int y = ty + (int)threadIdx.x / 3 - 1, x = tx + (int)threadIdx.x % 3 - 1;
+            if ((unsigned)y < (unsigned)I.tiles_y && (unsigned)x < (unsigned)I.tiles_x)
+                mark(stamps, list_next, count_next, I.tile0 + y * I.tiles_x + x, stamp);
+        }
+        __syncthreads(); /* shared memory is reused by the next tile */
+    }
+}
+
+/* the taped tiles of one step back into the state: h_{t+1} -> h_t */
+template <int TW, int TH>
+__global__ void __launch_bounds__(sdt::THREADS) k_restore(const Inst* __restrict__ inst,
+                                                          const int* __restrict__ tile_inst,
+                                                          const int* __restrict__ list, const int* __restrict__ count,
+                                                          const double* __restrict__ tape, double* __restrict__ h)
+{
+    const int n = *count;
+    for (int k = blockIdx.x; k < n; k += gridDim.x) {
+        const int t = list[k];
+        const Inst I = inst[tile_inst[t]];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        const double* src = tape + (size_t)k * (TW * TH);
+        for (int c = threadIdx.x; c < TW * TH; c += sdt::THREADS) {
+            const int a = c / TW, b = c - a * TW;
+            const int i = ty * TH + a, j = tx * TW + b;
+            if (i < I.rows && j < I.cols)
+                h[I.off + (long long)i * I.cols + j] = src[c];
+        }
+    }
+}
+
+/* z after the initialisation (z_dem - h0 where h0 > 0), both h buffers = h0
+ * with -0 made +0 (the first reference step adds 0.0 to every cell), and
+ * list L_0 = the 3 x 3 tiles around every tile holding a wet cell */
+__global__ void k_init(const Inst* __restrict__ inst, const long long* __restrict__ offs, int B, long long N, int tw,
+                       int th, const double* __restrict__ z_dem, const double* __restrict__ h0, double* __restrict__ z,
+                       double* __restrict__ h_a, double* __restrict__ h_b, int* stamps, int* list0, int* count0)
+{
+    extern __shared__ long long s_offs[];
+    for (int k = threadIdx.x; k <= B; k += blockDim.x)
+        s_offs[k] = offs[k];
+    __syncthreads();
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N; c += (long long)gridDim.x * blockDim.x) {
+        int b;
+        if (!locate(s_offs, inst, B, c, &b)) {
+            z[c] = 0.0;
+            h_a[c] = 0.0;
+            h_b[c] = 0.0;
+            continue;
+        }
+        const Inst I = inst[b];
+        const double hv = h0[c];
+        z[c] = hv > 0.0 ? z_dem[c] - hv : z_dem[c];
+        const double hc = sdt::plus_zero(hv);
+        h_a[c] = hc;
+        h_b[c] = hc;
+        if (sdt::is_wet(hc, I.eps_bits)) {
+            const long long lc = c - I.off;
+            const int i = (int)(lc / I.cols), j = (int)(lc - (long long)i * I.cols);
+            const int ty = i / th, tx = j / tw;
+            for (int q = 0; q < 9; q++) {
+                const int y = ty + q / 3 - 1, x = tx + q % 3 - 1;
+                if ((unsigned)y < (unsigned)I.tiles_y && (unsigned)x < (unsigned)I.tiles_x)
+                    mark(stamps, list0, count0, I.tile0 + y * I.tiles_x + x, 1);
+            }
+        }
+    }
+}
+
+/* dL/dh_T = 2 (h_T - target), lambda_z = 0, and the per-instance loss */
+__global__ void k_loss(const Inst* __restrict__ inst, const long long* __restrict__ offs, int B, long long N,
+                       const double* __restrict__ hT, const double* __restrict__ tgt, double* __restrict__ lam,
+                       double* __restrict__ lamz, double* __restrict__ loss)
+{
+    extern __shared__ long long s_offs[];
+    for (int k = threadIdx.x; k <= B; k += blockDim.x)
+        s_offs[k] = offs[k];
+    __syncthreads();
+    for (long long c0 = blockIdx.x * (long long)blockDim.x; c0 < N; c0 += (long long)gridDim.x * blockDim.x) {
+        const long long c = c0 + threadIdx.x;
+        double d2 = 0.0;
+        int b = 0;
+        bool valid = false;
+        if (c < N) {
+            valid = locate(s_offs, inst, B, c, &b);
+            const double d = valid ? hT[c] - tgt[c] : 0.0;
+            lam[c] = 2.0 * d;
+            lamz[c] = 0.0;
+            d2 = d * d;
+        }
+        const int b0 = __shfl_sync(0xffffffffu, b, 0);
+        if (__all_sync(0xffffffffu, b == b0 || !valid)) {
+            for (int o = 16; o > 0; o >>= 1)
+                d2 += __shfl_down_sync(0xffffffffu, d2, o);
+            if ((threadIdx.x & 31) == 0)
+                atomicAdd(loss + b0, d2);
+        } else if (valid) {
+            atomicAdd(loss + b, d2);
+        }
+    }
+}
+
+/* neighbour n = 1..4 (north, west, east, south) of (i, j) in instance I; false outside (flat) */
+static __device__ __forceinline__ bool nbr(const Inst& I, int i, int j, int n, long long* c)
+{
+    const int a = i + (n == 1 ? -1 : (n == 4 ? 1 : 0));
+    const int b = j + (n == 2 ? -1 : (n == 3 ? 1 : 0));
+    if ((unsigned)a >= (unsigned)I.rows || (unsigned)b >= (unsigned)I.cols)
+        return false;
+    *c = I.off + (long long)a * I.cols + b;
+    return true;
+}
+
+/* block sum, result in thread 0; every thread calls it */
+static __device__ __forceinline__ double block_sum(double v, double* s_red)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0)
+        s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < T / 32; q++)
+            s += s_red[q];
+    __syncthreads();
+    return s;
+}
+
+/* adjoint coefficients g, gz, w of every cell of the listed tiles (the
+ * single-model k_coeffs), and the tiles' contributions to dL/dr, dL/deps */
+template <int TW, int TH>
+__global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, const int* __restrict__ tile_inst,
+                                              const int* __restrict__ list, const int* __restrict__ count, long long N,
+                                              const double* __restrict__ z, const double* __restrict__ h,
+                                              const double* __restrict__ lam, double* __restrict__ g,
+                                              double* __restrict__ gz, double* __restrict__ w,
+                                              double* __restrict__ grad, int B)
+{
+    __shared__ double s_red[T / 32];
+    const int n = *count;
+    for (int k = blockIdx.x; k < n; k += gridDim.x) {
+        const int t = list[k];
+        const int bi = tile_inst[t];
+        const Inst I = inst[bi];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        double pr = 0.0, pe = 0.0;
+        for (int q0 = threadIdx.x; q0 < TW * TH; q0 += T) {
+            const int i = ty * TH + q0 / TW, j = tx * TW + q0 % TW;
+            if (i >= I.rows || j >= I.cols)
+                continue;
+            const long long c = I.off + (long long)i * I.cols + j;
+            const double hc = h[c];
+            double gc = 0.0, gzc = 0.0, wc[4] = {0.0, 0.0, 0.0, 0.0};
+            if (sdt::is_wet(hc, I.eps_bits)) {
+                double u[5], lnb[4];
+                u[0] = z[c] + I.eps;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    long long cn = 0;
+                    const bool in = nbr(I, i, j, q + 1, &cn);
+                    u[q + 1] = in ? z[cn] + h[cn] : 0.0 + 0.0;
+                    lnb[q] = in ? lam[cn] : 0.0;
+                }
+                const double m = hc - I.eps;
+                unsigned elim = 0;
+                double avg;
+                bool again;
+                do {
+                    again = false;
+                    avg = m;
+                    int cnt = 0;
+#pragma unroll
+                    for (int q = 0; q < 5; q++)
+                        if (!(elim & (1u << q))) {
+                            avg += u[q];
+                            cnt++;
+                        }
+                    if (cnt != 0)
+                        avg = cal_div_small(avg, cnt);
+#pragma unroll
+                    for (int q = 0; q < 5; q++)
+                        if (!(elim & (1u << q)) && cal_le(avg, u[q])) {
+                            elim |= 1u << q;
+                            again = true;
+                        }
+                } while (again);
+                const unsigned a_set = (~elim) & 31u;
+                const int kk = __popc(a_set);
+                if (kk > 0) {
+                    const double lc = lam[c];
+                    double S = 0.0, lf[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        lf[q] = 0.0;
+                        if (a_set & (1u << (q + 1))) {
+                            lf[q] = lnb[q] - lc;
+                            S += lf[q];
+                            pr += lf[q] * (avg - u[q + 1]);
+                        }
+                    }
+                    gc = (I.r / kk) * S;
+                    gzc = (a_set & 1u) ? gc : 0.0;
+                    pe += S * I.r * ((a_set & 1u) ? 0.0 : -1.0) / kk;
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (a_set & (1u << (q + 1)))
+                            wc[q] = gc - I.r * lf[q];
+                }
+            }
+            g[c] = gc;
+            gz[c] = gzc;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                w[q * N + c] = wc[q];
+        }
+        const double sr = block_sum(pr, s_red);
+        const double se = block_sum(pe, s_red);
+        if (threadIdx.x == 0) {
+            if (sr != 0.0)
+                atomicAdd(grad + bi, sr);
+            if (se != 0.0)
+                atomicAdd(grad + B + bi, se);
+        }
+    }
+}
+
+/* lambda_t = lambda_{t+1} + g + the wet neighbours' w (in place), and
+ * lambda_z; coefficients are read only at wet cells, where this step's
+ * k_coeffs wrote them (a wet cell's tile is always in the list) */
+template <int TW, int TH>
+__global__ void __launch_bounds__(T) k_gather(const Inst* __restrict__ inst, const int* __restrict__ tile_inst,
+                                              const int* __restrict__ list, const int* __restrict__ count, long long N,
+                                              const double* __restrict__ h, const double* __restrict__ g,
+                                              const double* __restrict__ gz, const double* __restrict__ w,
+                                              double* __restrict__ lam, double* __restrict__ lamz)
+{
+    const int n = *count;
+    for (int k = blockIdx.x; k < n; k += gridDim.x) {
+        const int t = list[k];
+        const Inst I = inst[tile_inst[t]];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        for (int q0 = threadIdx.x; q0 < TW * TH; q0 += T) {
+            const int i = ty * TH + q0 / TW, j = tx * TW + q0 % TW;
+            if (i >= I.rows || j >= I.cols)
+                continue;
+            const long long c = I.off + (long long)i * I.cols + j;
+            double from_nb = 0.0;
+            long long cn = 0;
+            /* x is neighbour opp(d) of its neighbour d: north<->south, west<->east */
+            if (nbr(I, i, j, 1, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+                from_nb += w[3 * N + cn];
+            if (nbr(I, i, j, 2, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+                from_nb += w[2 * N + cn];
+            if (nbr(I, i, j, 3, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+                from_nb += w[1 * N + cn];
+            if (nbr(I, i, j, 4, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+                from_nb += w[cn];
+            double gc = 0.0, gzc = 0.0;
+            if (sdt::is_wet(h[c], I.eps_bits)) {
+                gc = g[c];
+                gzc = gz[c];
+            }
+            lam[c] = lam[c] + gc + from_nb;
+            lamz[c] += gzc + from_nb;
+        }
+    }
+}
+
+__global__ void k_final_grad(const double* __restrict__ h0, const double* __restrict__ lam,
+                             const double* __restrict__ lamz, double* __restrict__ g_h0, long long n)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        g_h0[c] = lam[c] - (h0[c] > 0.0 ? lamz[c] : 0.0);
+}
+
+static int dense_grid(long long n)
+{
+    long long b = (n + T - 1) / T;
+    return (int)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
+}
+
+/* a resident grid for the step kernel: SMs x blocks per SM */
+template <int TW, int TH>
+static int step_grid()
+{
+    static int blocks = 0;
+    if (!blocks) {
+        const int smem = (int)sdt::Tile<TW, TH>::smem_bytes;
+        cudaFuncSetAttribute(k_step<TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step<TW, TH>, sdt::THREADS, smem);
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    return blocks;
+}
+
+/* step t: list L_t -> (mark ? L_{t+1}) */
+template <int TW, int TH>
+static void launch_step(Batch& bt, int t, const double* h, double* hn, bool mark, double* tape)
+{
+    const size_t nt = (size_t)bt.ntiles;
+    k_step<TW, TH><<<step_grid<TW, TH>(), sdt::THREADS, sdt::Tile<TW, TH>::smem_bytes, bt.st>>>(
+        bt.d_inst, bt.d_tile_inst, bt.z, h, hn, bt.lists + nt * t, bt.counts + t,
+        mark ? bt.lists + nt * (t + 1) : nullptr, bt.counts + t + 1, bt.stamps, t + 2, tape);
+}
+
+template <int TW, int TH>
+static void launch_restore(Batch& bt, int t, const double* tape, double* h)
+{
+    k_restore<TW, TH><<<152 * 8, sdt::THREADS, 0, bt.st>>>(bt.d_inst, bt.d_tile_inst, bt.lists + (size_t)bt.ntiles * t,
+                                                            bt.counts + t, tape, h);
+}
+
+template <int TW, int TH>
+static void launch_adjoint(Batch& bt, int t, const double* h)
+{
+    const int* list = bt.lists + (size_t)bt.ntiles * t;
+    k_coeffs<TW, TH><<<152 * 8, T, 0, bt.st>>>(bt.d_inst, bt.d_tile_inst, list, bt.counts + t, bt.N, bt.z, h, bt.lam,
+                                                bt.g, bt.gz, bt.w, bt.grad, bt.B);
+    k_gather<TW, TH><<<152 * 8, T, 0, bt.st>>>(bt.d_inst, bt.d_tile_inst, list, bt.counts + t, bt.N, h, bt.g, bt.gz,
+                                                bt.w, bt.lam, bt.lamz);
+}
+
+#define SDTB_DISPATCH(batch, fn, ...)                          \
+    switch ((batch).shape) {                                   \
+    case 0: fn<32, 16>(__VA_ARGS__); break;                    \
+    case 1: fn<64, 16>(__VA_ARGS__); break;                    \
+    default: fn<64, 32>(__VA_ARGS__); break;                   \
+    }
+
+/* forward over `steps` steps from h0; checkpoints every K steps when keep */
+static void forward(Batch& bt, int steps, bool keep)
+{
+    const size_t nb = (size_t)bt.N * sizeof(double);
+    const int tw = kShapes[bt.shape].tw, th = kShapes[bt.shape].th;
+    cudaMemsetAsync(bt.stamps, 0, sizeof(int) * bt.ntiles, bt.st);
+    cudaMemsetAsync(bt.counts, 0, sizeof(int) * (bt.steps + 1), bt.st);
+    k_init<<<dense_grid(bt.N), T, sizeof(long long) * (bt.B + 1), bt.st>>>(bt.d_inst, bt.d_offs, bt.B, bt.N, tw, th,
+                                                                           bt.z_dem, bt.h0, bt.z, bt.hbuf[0],
+                                                                           bt.hbuf[1], bt.stamps, bt.lists, bt.counts);
+    for (int t = 0; t < steps; t++) {
+        if (keep && t % bt.K == 0)
+            cudaMemcpyAsync(bt.ckpt + (size_t)(t / bt.K) * bt.N, bt.hbuf[t & 1], nb, cudaMemcpyDeviceToDevice, bt.st);
+        SDTB_DISPATCH(bt, launch_step, bt, t, bt.hbuf[t & 1], bt.hbuf[(t + 1) & 1], true, nullptr);
+    }
+}
+
+static void destroy(Batch* bt)
+{
+    if (bt->st)
+        cudaStreamSynchronize(bt->st);
+    void* ptrs[] = {bt->d_inst, bt->d_offs, bt->d_tile_inst, bt->stamps, bt->lists, bt->counts, bt->z_dem,
+                    bt->z,      bt->h0,     bt->hbuf[0],      bt->hbuf[1], bt->ckpt, bt->tape,   bt->lam,
+                    bt->lamz,   bt->g,      bt->gz,           bt->w,      bt->grad,  bt->loss};
+    for (void* p : ptrs)
+        cudaFree(p);
+    if (bt->st)
+        cudaStreamDestroy(bt->st);
+    delete bt;
+}
+
+} // namespace sdtb
+
+using sdtb::Batch;
+
+/* Create an ensemble of B instances.  dims[2b], dims[2b+1] = rows, cols;
+ * params[2b], params[2b+1] = p_r, p_eps; z_dem, h0: host arrays holding the
+ * instances' rows*cols values back to back (row-major, unpadded); `steps`
+ * per rollout.  NULL on a bad argument or when device memory runs out. */
+extern "C" void* cal_sdt_batch_create(int B, const int* dims, const double* params, const double* z_dem_host,
+                                      const double* h0_host, int steps)
+{
+    if (B <= 0 || B > sdtb::MAX_INST || steps < 0 || !dims || !params || !z_dem_host || !h0_host)
+        return nullptr;
+    Batch* bt = new Batch();
+    bt->B = B;
+    bt->steps = steps;
+    bt->K = (int)ceil(sqrt((double)(steps > 0 ? steps : 1)));
+    bt->nseg = steps > 0 ? (steps + bt->K - 1) / bt->K : 1;
+    bt->offs.assign(B + 1, 0);
+    for (int b = 0; b < B; b++) {
+        sdtb::Inst I;
+        memset(&I, 0, sizeof(I));
+        I.rows = dims[2 * b];
+        I.cols = dims[2 * b + 1];
+        if (I.rows <= 0 || I.cols <= 0) {
+            delete bt;
+            return nullptr;
+        }
+        I.off = bt->offs[b];
+        I.r = params[2 * b];
+        I.eps = params[2 * b + 1];
+        memcpy(&I.eps_bits, &I.eps, sizeof(double));
+        bt->inst.push_back(I);
+        const long long n = (long long)I.rows * I.cols;
+        bt->offs[b + 1] = bt->offs[b] + (n + sdtb::ALIGN - 1) / sdtb::ALIGN * sdtb::ALIGN;
+    }
+    bt->N = bt->offs[B];
+    const size_t nb = (size_t)bt->N * sizeof(double);
+    bool ok = cudaStreamCreateWithFlags(&bt->st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc(&bt->d_inst, sizeof(sdtb::Inst) * B) == cudaSuccess &&
+              cudaMalloc(&bt->d_offs, sizeof(long long) * (B + 1)) == cudaSuccess &&
+              cudaMalloc(&bt->counts, sizeof(int) * (steps + 1)) == cudaSuccess &&
+              cudaMalloc(&bt->z_dem, nb) == cudaSuccess && cudaMalloc(&bt->z, nb) == cudaSuccess &&
+              cudaMalloc(&bt->h0, nb) == cudaSuccess && cudaMalloc(&bt->hbuf[0], nb) == cudaSuccess &&
+              cudaMalloc(&bt->hbuf[1], nb) == cudaSuccess && cudaMalloc(&bt->ckpt, nb * bt->nseg) == cudaSuccess &&
+              cudaMalloc(&bt->lam, nb) == cudaSuccess && cudaMalloc(&bt->lamz, nb) == cudaSuccess &&
+              cudaMalloc(&bt->g, nb) == cudaSuccess && cudaMalloc(&bt->gz, nb) == cudaSuccess &&
+              cudaMalloc(&bt->w, 4 * nb) == cudaSuccess &&
+              cudaMalloc(&bt->grad, 2 * B * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&bt->loss, B * sizeof(double)) == cudaSuccess;
+    if (ok) {
+        cudaMemcpy(bt->d_offs, bt->offs.data(), sizeof(long long) * (B + 1), cudaMemcpyHostToDevice);
+        cudaMemset(bt->z_dem, 0, nb);
+        cudaMemset(bt->h0, 0, nb);
+        size_t src = 0;
+        for (int b = 0; b < B; b++) {
+            const size_t n = (size_t)bt->inst[b].rows * bt->inst[b].cols;
+            cudaMemcpy(bt->z_dem + bt->offs[b], z_dem_host + src, n * sizeof(double), cudaMemcpyHostToDevice);
+            cudaMemcpy(bt->h0 + bt->offs[b], h0_host + src, n * sizeof(double), cudaMemcpyHostToDevice);
+            src += n;
+        }
+        ok = sdtb::tiles_for(*bt) && cudaGetLastError() == cudaSuccess;
+    }
+    if (!ok) {
+        fprintf(stderr, "opencal-gb300: cal_sdt_batch_create: out of device memory\n");
+        sdtb::destroy(bt);
+        return nullptr;
+    }
+    return bt;
+}
+
+extern "C" void cal_sdt_batch_destroy(void* handle)
+{
+    if (handle)
+        sdtb::destroy((Batch*)handle);
+}
+
+/* padded cell count and the B + 1 instance offsets of the device layout */
+extern "C" long long cal_sdt_batch_cells(void* handle, long long* offsets)
+{
+    Batch* bt = (Batch*)handle;
+    if (offsets)
+        memcpy(offsets, bt->offs.data(), sizeof(long long) * (bt->B + 1));
+    return bt->N;
+}
+
+extern "C" void* cal_sdt_batch_stream(void* handle) { return ((Batch*)handle)->st; }
+extern "C" int cal_sdt_batch_shape(void* handle) { return ((Batch*)handle)->shape; }
+
+/* replace the per-instance parameters (host array of 2B doubles: p_r, p_eps) */
+extern "C" int cal_sdt_batch_set_params(void* handle, const double* params)
+{
+    Batch* bt = (Batch*)handle;
+    for (int b = 0; b < bt->B; b++) {
+        bt->inst[b].r = params[2 * b];
+        bt->inst[b].eps = params[2 * b + 1];
+        memcpy(&bt->inst[b].eps_bits, &bt->inst[b].eps, sizeof(double));
+    }
+    cudaStreamSynchronize(bt->st);
+    return (int)cudaMemcpy(bt->d_inst, bt->inst.data(), sizeof(sdtb::Inst) * bt->B, cudaMemcpyHostToDevice);
+}
+
+/* Forward rollout of every instance (`steps` steps); h_T copied into hT (a
+ * device array in the padded layout, or NULL).  Asynchronous on the
+ * ensemble's stream. */
+extern "C" int cal_sdt_batch_forward(void* handle, double* hT)
+{
+    Batch* bt = (Batch*)handle;
+    sdtb::forward(*bt, bt->steps, false);
+    if (hT)
+        cudaMemcpyAsync(hT, bt->hbuf[bt->steps & 1], (size_t)bt->N * sizeof(double), cudaMemcpyDeviceToDevice, bt->st);
+    return (int)cudaGetLastError();
+}
+
+/* Tiles processed by each step of the last rollout (steps + 1 counts: the
+ * list built for step t, t in [0, steps]).  Synchronises. */
+extern "C" int cal_sdt_batch_active_tiles(void* handle, int* out)
+{
+    Batch* bt = (Batch*)handle;
+    cudaStreamSynchronize(bt->st);
+    return (int)cudaMemcpy(out, bt->counts, sizeof(int) * (bt->steps + 1), cudaMemcpyDeviceToHost);
+}
+
+/* Loss L_b = sum over instance b of (h_T - target)^2 and its gradients:
+ * forward with checkpoints, then the adjoint.  target: device array in the
+ * padded layout.  loss_out[B], grad_out[2B] (dL/dp_r, dL/dp_eps of each
+ * instance, interleaved): host arrays; g_h0: device array for dL/dh0 (padded
+ * layout), or NULL.  Synchronises. */
+extern "C" int cal_sdt_batch_loss_grad(void* handle, const double* target, double* loss_out, double* grad_out,
+                                       double* g_h0)
+{
+    Batch* bt = (Batch*)handle;
+    const size_t nb = (size_t)bt->N * sizeof(double);
+    const int tc = sdtb::tile_cells(*bt);
+    cudaStream_t st = bt->st;
+    sdtb::forward(*bt, bt->steps, true);
+    bt->h_counts.resize(bt->steps + 1);
+    cudaMemcpyAsync(bt->h_counts.data(), bt->counts, sizeof(int) * (bt->steps + 1), cudaMemcpyDeviceToHost, st);
+    cudaMemsetAsync(bt->loss, 0, bt->B * sizeof(double), st);
+    cudaMemsetAsync(bt->grad, 0, 2 * bt->B * sizeof(double), st);
+    sdtb::k_loss<<<sdtb::dense_grid(bt->N), sdtb::T, sizeof(long long) * (bt->B + 1), st>>>(
+        bt->d_inst, bt->d_offs, bt->B, bt->N, bt->hbuf[bt->steps & 1], target, bt->lam, bt->lamz, bt->loss);
+    if (cudaStreamSynchronize(st) != cudaSuccess)
+        return (int)cudaGetLastError();
+    /* the tape holds one segment: its layout follows the work-list sizes */
+    std::vector<size_t> tape_off(bt->steps + 1, 0);
+    size_t need = 0;
+    for (int s = 0; s < bt->nseg; s++) {
+        const int t0 = s * bt->K, t1 = std::min(t0 + bt->K, bt->steps);
+        size_t acc = 0;
+        for (int t = t0; t < t1; t++) {
+            tape_off[t] = acc;
+            acc += (size_t)bt->h_counts[t] * tc;
+        }
+        need = std::max(need, acc);
+    }
+    if (need > bt->tape_cap) {
+        cudaFree(bt->tape);
+        bt->tape = nullptr;
+        bt->tape_cap = 0;
+        if (cudaMalloc(&bt->tape, need * sizeof(double)) != cudaSuccess) {
+            fprintf(stderr, "opencal-gb300: cal_sdt_batch_loss_grad: out of device memory for the tape\n");
+            return (int)cudaErrorMemoryAllocation;
+        }
+        bt->tape_cap = need;
+    }
+    for (int s = bt->nseg - 1; s >= 0; s--) {
+        const int t0 = s * bt->K, t1 = std::min(t0 + bt->K, bt->steps);
+        if (t1 <= t0)
+            continue;
+        cudaMemcpyAsync(bt->hbuf[0], bt->ckpt + (size_t)s * bt->N, nb, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(bt->hbuf[1], bt->ckpt + (size_t)s * bt->N, nb, cudaMemcpyDeviceToDevice, st);
+        for (int t = t0; t < t1; t++)
+            SDTB_DISPATCH(*bt, sdtb::launch_step, *bt, t, bt->hbuf[(t - t0) & 1], bt->hbuf[(t - t0 + 1) & 1], false,
+                          bt->tape + tape_off[t]);
+        double* X = bt->hbuf[(t1 - t0) & 1]; /* h_{t1} everywhere */
+        for (int t = t1 - 1; t >= t0; t--) {
+            SDTB_DISPATCH(*bt, sdtb::launch_restore, *bt, t, bt->tape + tape_off[t], X);
+            SDTB_DISPATCH(*bt, sdtb::launch_adjoint, *bt, t, X);
+        }
+    }
+    if (g_h0)
+        sdtb::k_final_grad<<<sdtb::dense_grid(bt->N), sdtb::T, 0, st>>>(bt->h0, bt->lam, bt->lamz, g_h0, bt->N);
+    std::vector<double> tmp(2 * bt->B);
+    cudaMemcpyAsync(tmp.data(), bt->grad, 2 * bt->B * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (loss_out)
+        cudaMemcpyAsync(loss_out, bt->loss, bt->B * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (grad_out)
+        for (int b = 0; b < bt->B; b++) {
+            grad_out[2 * b] = tmp[b];
+            grad_out[2 * b + 1] = tmp[bt->B + b];
+        }
+    return (int)cudaGetLastError();
+}
+
+/* Pick the fastest tile shape for this ensemble: a forward of `probe_steps`
+ * steps per candidate (0: 32x16, 1: 64x16, 2: 64x32), timed with CUDA
+ * events after one untimed probe.  Writes the milliseconds to ms[3] and
+ * returns the chosen shape, or -1 on a CUDA error. */
+extern "C" int cal_sdt_batch_autotune(void* handle, int probe_steps, float* ms)
+{
+    Batch* bt = (Batch*)handle;
+    if (probe_steps > bt->steps)
+        probe_steps = bt->steps;
+    int best = bt->shape;
+    float best_ms = 1e30f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int s = 0; s < 3; s++) {
+        bt->shape = s;
+        if (!sdtb::tiles_for(*bt)) {
+            best = -1;
+            break;
+        }
+        sdtb::forward(*bt, probe_steps, false);
+        cudaEventRecord(e0, bt->st);
+        sdtb::forward(*bt, probe_steps, false);
+        cudaEventRecord(e1, bt->st);
+        cudaEventSynchronize(e1);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (ms)
+            ms[s] = t;
+        if (t < best_ms) {
+            best_ms = t;
+            best = s;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best < 0)
+        return -1;
+    bt->shape = best;
+    if (!sdtb::tiles_for(*bt))
+        return -1;
+    return cudaGetLastError() == cudaSuccess ? best : -1;
+}
+
+/* set the tile shape (0: 32x16, 1: 64x16, 2: 64x32); 0 on success */
+extern "C" int cal_sdt_batch_set_shape(void* handle, int shape)
+{
+    Batch* bt = (Batch*)handle;
+    if (shape < 0 || shape > 2)
+        return 1;
+    bt->shape = shape;
+    return sdtb::tiles_for(*bt) ? 0 : 2;
+}

@@ -101,23 +101,28 @@ struct Tile {
     static constexpr size_t smem_bytes = sizeof(double) * (2 * R2W * R2H + 4 * R1W * R1H);
 };
 
-template <int TW, int TH>
-__global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Params p)
+/* one TW x TH tile of one step; i0, j0 = tile origin; smem sized
+ * Tile<TW, TH>::smem_bytes; every thread of the block calls it.  With TRACK
+ * the block-uniform result has bit 0 set when a cell of the tile was wet
+ * before the step and bit 1 when one is wet after it (0 without TRACK). */
+template <int TW, int TH, bool TRACK = false>
+__device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, double* smem)
 {
     using T = Tile<TW, TH>;
-    extern __shared__ __align__(16) double smem[];
     double* sz = smem;                      /* [R2H][R2W] */
     double* sh = sz + T::R2W * T::R2H;      /* [R2H][R2W] */
     double* sf = sh + T::R2W * T::R2H;      /* [4][R1H][R1W] */
     constexpr int F = T::R1W * T::R1H;
 
-    const int i0 = blockIdx.y * TH, j0 = blockIdx.x * TW;
-    const bool interior = i0 >= 2 && j0 >= 2 && i0 + TH + 2 <= p.rows && j0 + TW + 2 <= p.cols;
+    /* 16-byte loads need an even row length and 16-byte aligned fields */
+    const bool interior = i0 >= 2 && j0 >= 2 && i0 + TH + 2 <= p.rows && j0 + TW + 2 <= p.cols && (p.cols & 1) == 0 &&
+                          ((reinterpret_cast<unsigned long long>(p.z) | reinterpret_cast<unsigned long long>(p.h)) &
+                           15) == 0;
 
     /* 1. z and h on the tile + 2 ring.  Interior tiles: 16-byte loads (j0-2
      * is even, so every pair starts 16-byte aligned).  Edge tiles: flat ->
      * 0 outside, toroidal -> wrapped. */
-    int wet_seen = 0;
+    int wet_seen = 0, wet_in = 0, wet_out = 0;
     if (interior) {
         constexpr int PW = T::R2W / 2;
         for (int t = threadIdx.x; t < PW * T::R2H; t += THREADS) {
@@ -127,7 +132,10 @@ __global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Pa
             const double2 hv = __ldg(reinterpret_cast<const double2*>(p.h + c));
             *reinterpret_cast<double2*>(sz + a * T::R2W + b) = zv;
             *reinterpret_cast<double2*>(sh + a * T::R2W + b) = hv;
-            wet_seen |= is_wet(hv.x, p.eps_bits) | is_wet(hv.y, p.eps_bits);
+            const int w = is_wet(hv.x, p.eps_bits) | is_wet(hv.y, p.eps_bits);
+            wet_seen |= w;
+            if (TRACK && a >= 2 && a < TH + 2 && b >= 2 && b < TW + 2)
+                wet_in |= w;
         }
     } else {
         for (int t = threadIdx.x; t < T::R2H * T::R2W; t += THREADS) {
@@ -147,7 +155,10 @@ __global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Pa
             }
             sz[t] = zv;
             sh[t] = hv;
-            wet_seen |= is_wet(hv, p.eps_bits);
+            const int w = is_wet(hv, p.eps_bits);
+            wet_seen |= w;
+            if (TRACK && a >= 2 && a < TH + 2 && b >= 2 && b < TW + 2 && i0 - 2 + a < p.rows && j0 - 2 + b < p.cols)
+                wet_in |= w;
         }
     }
     if (__syncthreads_or(wet_seen) == 0) {
@@ -158,7 +169,7 @@ __global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Pa
             if (gi < p.rows && gj < p.cols)
                 p.h_next[(long long)gi * p.cols + gj] = plus_zero(sh[(a + 2) * T::R2W + b + 2]);
         }
-        return;
+        return 0;
     }
 
     /* 2. EP 1 on the tile + 1 ring; cells outside a flat grid have none */
@@ -209,7 +220,19 @@ __global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Pa
             hn += in4 - o3;
         }
         p.h_next[(long long)gi * p.cols + gj] = hn;
+        if (TRACK)
+            wet_out |= is_wet(hn, p.eps_bits);
     }
+    if (TRACK)
+        return __syncthreads_or(wet_in | (wet_out << 1));
+    return 0;
+}
+
+template <int TW, int TH>
+__global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Params p)
+{
+    extern __shared__ __align__(16) double smem[];
+    fused_tile<TW, TH>(p, blockIdx.y * TH, blockIdx.x * TW, smem);
 }
 
 template <int TW, int TH>

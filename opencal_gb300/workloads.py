@@ -124,3 +124,31 @@ def sparse_blobs(shape, seed: int, n_blobs: int = 3, radius: float = 3.0, peak: 
         r2 = sum((g - ci) ** 2 for g, ci in zip(grids, c)) / (radius * radius)
         v = v + np.where(r2 < 1.0, peak * (1.0 - r2), 0.0)
     return quantise(v)
+
+
+def ensemble_spec(n: int, seed: int = 4, size_range=(128, 1024), p_r_range=(0.3, 0.7),
+                  p_eps_range=(5e-4, 5e-3)):
+    """Dimensions and parameters of a calibration ensemble of ``n`` SCIDDICA-T
+    instances: rows and cols independently uniform in ``size_range``
+    (inclusive), p_r and p_eps uniform in their ranges; instance i's DEM and
+    source come from ``sciddicaT_inputs(rows, cols, seed=1000 + i)``.
+    Returns (dims [(rows, cols)], params [(p_r, p_eps)])."""
+    rng = SplitMix64(seed)
+    lo, hi = size_range
+    dims, params = [], []
+    for _ in range(n):
+        rows = lo + int(rng.next_u64() % (hi - lo + 1))
+        cols = lo + int(rng.next_u64() % (hi - lo + 1))
+        dims.append((rows, cols))
+        params.append((rng.uniform(*p_r_range), rng.uniform(*p_eps_range)))
+    return dims, params
+
+
+def ensemble_inputs(dims, first_seed: int = 1000):
+    """(z list, h list) for the instances of an ensemble."""
+    zs, hs = [], []
+    for i, (rows, cols) in enumerate(dims):
+        z, h = sciddicaT_inputs(rows, cols, seed=first_seed + i)
+        zs.append(z)
+        hs.append(h)
+    return zs, hs
