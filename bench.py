@@ -283,11 +283,12 @@ def gpu_arm(args):
 
     if rank != 0:
         return
+    # DRAM bytes of one step (K1 + K2) from the committed ncu capture
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "sciddicaT_fused_step_2048.json")
+    tpath = os.path.join(ROOT, "profiles", "sciddicaT_split_step_2048.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            traffic = json.load(f).get("dram_bytes_per_step")
     line = {
         "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -304,22 +305,126 @@ def gpu_arm(args):
                 "d2h_bytes_per_step": int(h.nbytes)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "SCIDDICA-T step = sdt2::k1_outflows (wet cells) + sdt2::k2_update (all cells)",
+                     "kernel": "SCIDDICA-T step = sdt2::k1_outflows (wet cells) + sdt2::k2_update (flagged tiles)",
+                     "basis": "achieved = 24 B x rows x cols per step (dense algorithmic bytes) / (K1 + K2 mean "
+                              "event time); traffic = ncu DRAM bytes of K1 + K2 at the same step (fields stay "
+                              "in L2)",
                      "kernel_avg_ms": kavg_ms, "k1_outflows_ms": k1_ms, "k2_update_ms": k2_ms,
                      "wet_cells_at_step_1000": wet,
-                     "bytes_per_launch": ROWS * COLS * BYTES_PER_CELL_UPDATE},
+                     "bytes_per_step": ROWS * COLS * BYTES_PER_CELL_UPDATE},
         "finite": bool(np.isfinite(hh).all()),
         "clocks": clk,
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(z, h)
+    if not args.no_calibration:
+        line["calibration"] = calibration_section(args)
     print(json.dumps(line), flush=True)
+
+
+ENS_INSTANCES = 256
+ENS_STEPS = 1000
+ENS_SEED = 4
+
+
+def calibration_section(args):
+    """Batched calibration: 256 SCIDDICA-T instances, rows and cols uniform in
+    128..1024, each with its own seeded DEM and source (seed 1000 + i) and its
+    own p_r in [0.3, 0.7], p_eps in [5e-4, 5e-3]; 1000 steps each.  Targets
+    are forward runs at the true parameters; the calibration starts from
+    p_r * 1.08, p_eps * 0.92.
+
+    batched: one calibration iteration = one ensemble forward + adjoint
+      (all instances' losses and gradients), timed on the host around the
+      synchronous call, after one untimed iteration;
+    plain: the same iteration with the plain GPU drop-in per instance and
+      central finite differences (five 1000-step runs per instance),
+      timed over all 256 instances (one session open at a time; opening
+      and closing the sessions is not timed)."""
+    import torch
+
+    from opencal_gb300 import ensemble as E
+    from opencal_gb300 import workloads as W
+    dims, ptrue = W.ensemble_spec(ENS_INSTANCES, seed=ENS_SEED)
+    zs, hs = W.ensemble_inputs(dims)
+    ens = E.Ensemble(dims, ptrue, zs, hs, ENS_STEPS)
+    shape, tune_ms = ens.autotune(100)
+    tgt = ens.forward()
+    tg_host = ens.unpack(tgt)
+    active = ens.active_tiles()
+    p0 = [(p[0] * 1.08, p[1] * 0.92) for p in ptrue]
+    ens.set_params(p0)
+    ens.loss_grad(tgt)  # untimed
+    t_b = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        loss, grad = ens.loss_grad(tgt)
+        t_b.append(time.perf_counter() - t0)
+    batched_s = float(np.median(t_b))
+
+    fd_s = 0.0
+    rel = []
+    for b in range(ENS_INSTANCES):
+        sess = E.FDSession(zs[b], hs[b], p0[b][0], p0[b][1], ENS_STEPS, tg_host[b])
+        t0 = time.perf_counter()
+        f0, g = sess.fd_grad(*p0[b])
+        fd_s += time.perf_counter() - t0
+        sess.close()
+        den = np.maximum(np.abs(grad[b]), 1e-300)
+        rel.append(np.abs(g - grad[b]) / den)
+    rel = np.asarray(rel)
+
+    cal = E.calibrate(ens, tgt, p0, iters=args.calib_iters, p_true=ptrue, tol=1e-3)
+    ens.close()
+    del tgt
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"{ENS_INSTANCES} SCIDDICA-T FP64 instances, rows/cols uniform 128..1024 "
+                    f"({sum(r * c for r, c in dims)} cells), own DEM/source/p_r/p_eps, {ENS_STEPS} steps, "
+                    "loss = sum (h_T - target)^2",
+        "metric": "calibration_iters_per_s", "unit": "iterations/s",
+        "batched_iter_s": batched_s, "batched_iters_per_s": 1.0 / batched_s,
+        "plain_fd_iter_s": fd_s, "plain_fd_iters_per_s": 1.0 / fd_s,
+        "speedup": fd_s / batched_s,
+        "tile_shape": shape, "autotune_ms": tune_ms,
+        "active_tiles_per_step_mean": float(active.mean()),
+        "fd_vs_adjoint_rel_diff_median": [float(np.median(rel[:, 0])), float(np.median(rel[:, 1]))],
+        "calibration": {"start": "p_r * 1.08, p_eps * 0.92", "iterations": cal["iterations"],
+                        "recovered_1e-3_by_iteration": cal["recovered"],
+                        "p_r_within_1e-3": float(np.mean(cal["rel_err"][:, 0] < 1e-3)),
+                        "p_eps_within_1e-3": float(np.mean(cal["rel_err"][:, 1] < 1e-3)),
+                        "median_rel_err": [float(np.median(cal["rel_err"][:, 0])),
+                                           float(np.median(cal["rel_err"][:, 1]))]},
+        # forward: init + one step kernel per step, loss kernel; backward per
+        # step: recomputed step, tape restore, coefficients, gather
+        "gpu_launches_per_batched_iter": 5 * ENS_STEPS + 2,
+    }
+
+
+def ncu_case_ensemble(args):
+    """A fixed, untimed ensemble sequence for ncu captures: the first 32
+    instances of the calibration ensemble, one forward of --ncu-steps steps
+    and one loss + gradient evaluation against it."""
+    from opencal_gb300 import ensemble as E
+    from opencal_gb300 import workloads as W
+    dims, ptrue = W.ensemble_spec(ENS_INSTANCES, seed=ENS_SEED)
+    dims, ptrue = dims[:32], ptrue[:32]
+    zs, hs = W.ensemble_inputs(dims)
+    ens = E.Ensemble(dims, ptrue, zs, hs, args.ncu_steps)
+    ens.set_shape("32x16")
+    tgt = ens.forward()
+    ens.set_params([(p[0] * 1.08, p[1] * 0.92) for p in ptrue])
+    loss, grad = ens.loss_grad(tgt)
+    print(json.dumps({"cells": ens.cells, "active_tiles_mean": float(ens.active_tiles().mean()),
+                      "loss_median": float(np.median(loss))}), flush=True)
 
 
 def ncu_case(args):
     """A fixed, untimed sequence for ncu captures: open the 2048^2 session,
     run --ncu-steps fused steps from the initial state, report the wet
     fraction.  No torch, no extra allocations."""
+    if args.ncu_case == "ensemble":
+        return ncu_case_ensemble(args)
     import opencal_gb300 as cal
     from opencal_gb300 import workloads as W
     cal.build()
@@ -351,7 +456,10 @@ def main():
     ap.add_argument("--impl", default="opencal", choices=["opencal", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--loop", default="eager", choices=sorted(LOOPS))
-    ap.add_argument("--ncu-case", action="store_true", help="untimed fixed sequence for ncu captures")
+    ap.add_argument("--no-calibration", action="store_true", help="skip the batched-calibration section")
+    ap.add_argument("--calib-iters", type=int, default=12)
+    ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble"],
+                    help="untimed fixed sequence for ncu captures")
     ap.add_argument("--ncu-steps", type=int, default=1002)
     args = ap.parse_args()
     if args.ncu_case:

@@ -324,8 +324,10 @@ static __device__ __forceinline__ double block_sum(double v, double* s_red)
     return s;
 }
 
-/* adjoint coefficients g, gz, w of every cell of the listed tiles (the
- * single-model k_coeffs), and the tiles' contributions to dL/dr, dL/deps */
+/* adjoint coefficients g, gz, w of the wet cells of the listed tiles (the
+ * single-model k_coeffs; k_gather reads them at wet cells only), and the
+ * tiles' contributions to dL/dr, dL/deps.  The wet cells of a tile are
+ * compacted first so that warps run the FP64 elimination densely. */
 template <int TW, int TH>
 __global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, const int* __restrict__ tile_inst,
                                               const int* __restrict__ list, const int* __restrict__ count, long long N,
@@ -335,6 +337,8 @@ __global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, con
                                               double* __restrict__ grad, int B)
 {
     __shared__ double s_red[T / 32];
+    __shared__ unsigned short s_wet[TW * TH];
+    __shared__ int s_n;
     const int n = *count;
     for (int k = blockIdx.x; k < n; k += gridDim.x) {
         const int t = list[k];
@@ -342,75 +346,84 @@ __global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, con
         const Inst I = inst[bi];
         const int lt = t - I.tile0;
         const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        if (threadIdx.x == 0)
+            s_n = 0;
+        __syncthreads();
+        for (int q0 = 0; q0 < TW * TH; q0 += T) {
+            const int q = q0 + threadIdx.x;
+            const int i = ty * TH + q / TW, j = tx * TW + q % TW;
+            const bool wet = q < TW * TH && i < I.rows && j < I.cols &&
+                             sdt::is_wet(h[I.off + (long long)i * I.cols + j], I.eps_bits);
+            sdt::warp_append_shared(wet, q, s_wet, &s_n);
+        }
+        __syncthreads();
+        const int nw = s_n;
         double pr = 0.0, pe = 0.0;
-        for (int q0 = threadIdx.x; q0 < TW * TH; q0 += T) {
-            const int i = ty * TH + q0 / TW, j = tx * TW + q0 % TW;
-            if (i >= I.rows || j >= I.cols)
-                continue;
+        for (int e = threadIdx.x; e < nw; e += T) {
+            const int q = s_wet[e];
+            const int i = ty * TH + q / TW, j = tx * TW + q % TW;
             const long long c = I.off + (long long)i * I.cols + j;
             const double hc = h[c];
             double gc = 0.0, gzc = 0.0, wc[4] = {0.0, 0.0, 0.0, 0.0};
-            if (sdt::is_wet(hc, I.eps_bits)) {
-                double u[5], lnb[4];
-                u[0] = z[c] + I.eps;
+            double u[5], lnb[4];
+            u[0] = z[c] + I.eps;
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    long long cn = 0;
-                    const bool in = nbr(I, i, j, q + 1, &cn);
-                    u[q + 1] = in ? z[cn] + h[cn] : 0.0 + 0.0;
-                    lnb[q] = in ? lam[cn] : 0.0;
-                }
-                const double m = hc - I.eps;
-                unsigned elim = 0;
-                double avg;
-                bool again;
-                do {
-                    again = false;
-                    avg = m;
-                    int cnt = 0;
+            for (int d = 0; d < 4; d++) {
+                long long cn = 0;
+                const bool in = nbr(I, i, j, d + 1, &cn);
+                u[d + 1] = in ? z[cn] + h[cn] : 0.0 + 0.0;
+                lnb[d] = in ? lam[cn] : 0.0;
+            }
+            const double m = hc - I.eps;
+            unsigned elim = 0;
+            double avg;
+            bool again;
+            do {
+                again = false;
+                avg = m;
+                int cnt = 0;
 #pragma unroll
-                    for (int q = 0; q < 5; q++)
-                        if (!(elim & (1u << q))) {
-                            avg += u[q];
-                            cnt++;
-                        }
-                    if (cnt != 0)
-                        avg = cal_div_small(avg, cnt);
-#pragma unroll
-                    for (int q = 0; q < 5; q++)
-                        if (!(elim & (1u << q)) && cal_le(avg, u[q])) {
-                            elim |= 1u << q;
-                            again = true;
-                        }
-                } while (again);
-                const unsigned a_set = (~elim) & 31u;
-                const int kk = __popc(a_set);
-                if (kk > 0) {
-                    const double lc = lam[c];
-                    double S = 0.0, lf[4];
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        lf[q] = 0.0;
-                        if (a_set & (1u << (q + 1))) {
-                            lf[q] = lnb[q] - lc;
-                            S += lf[q];
-                            pr += lf[q] * (avg - u[q + 1]);
-                        }
+                for (int d = 0; d < 5; d++)
+                    if (!(elim & (1u << d))) {
+                        avg += u[d];
+                        cnt++;
                     }
-                    gc = (I.r / kk) * S;
-                    gzc = (a_set & 1u) ? gc : 0.0;
-                    pe += S * I.r * ((a_set & 1u) ? 0.0 : -1.0) / kk;
+                if (cnt != 0)
+                    avg = cal_div_small(avg, cnt);
 #pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        if (a_set & (1u << (q + 1)))
-                            wc[q] = gc - I.r * lf[q];
+                for (int d = 0; d < 5; d++)
+                    if (!(elim & (1u << d)) && cal_le(avg, u[d])) {
+                        elim |= 1u << d;
+                        again = true;
+                    }
+            } while (again);
+            const unsigned a_set = (~elim) & 31u;
+            const int kk = __popc(a_set);
+            if (kk > 0) {
+                const double lc = lam[c];
+                double S = 0.0, lf[4];
+#pragma unroll
+                for (int d = 0; d < 4; d++) {
+                    lf[d] = 0.0;
+                    if (a_set & (1u << (d + 1))) {
+                        lf[d] = lnb[d] - lc;
+                        S += lf[d];
+                        pr += lf[d] * (avg - u[d + 1]);
+                    }
                 }
+                gc = (I.r / kk) * S;
+                gzc = (a_set & 1u) ? gc : 0.0;
+                pe += S * I.r * ((a_set & 1u) ? 0.0 : -1.0) / kk;
+#pragma unroll
+                for (int d = 0; d < 4; d++)
+                    if (a_set & (1u << (d + 1)))
+                        wc[d] = gc - I.r * lf[d];
             }
             g[c] = gc;
             gz[c] = gzc;
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                w[q * N + c] = wc[q];
+            for (int d = 0; d < 4; d++)
+                w[d * N + c] = wc[d];
         }
         const double sr = block_sum(pr, s_red);
         const double se = block_sum(pe, s_red);

@@ -98,8 +98,28 @@ template <int TW, int TH>
 struct Tile {
     static constexpr int R1W = TW + 2, R1H = TH + 2; /* outflow region */
     static constexpr int R2W = TW + 4, R2H = TH + 4; /* load region */
-    static constexpr size_t smem_bytes = sizeof(double) * (2 * R2W * R2H + 4 * R1W * R1H);
+    /* z, h (load region), four outflows (outflow region), then the compacted
+     * list of wet cells of the outflow region (16-bit indices) and its count */
+    static constexpr size_t list_offset = sizeof(double) * (2 * R2W * R2H + 4 * R1W * R1H);
+    static constexpr size_t smem_bytes =
+        list_offset + ((sizeof(unsigned short) * ((R1W * R1H + 1) & ~1) + sizeof(int) + 15) / 16) * 16;
 };
+
+/* append the lanes whose predicate holds to a shared-memory list (one
+ * shared atomic per warp) */
+static __device__ __forceinline__ void warp_append_shared(bool pred, int value, unsigned short* list, int* count)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0)
+        return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0)
+        base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (pred)
+        list[base + __popc(mask & ((1u << lane) - 1u))] = (unsigned short)value;
+}
 
 /* one TW x TH tile of one step; i0, j0 = tile origin; smem sized
  * Tile<TW, TH>::smem_bytes; every thread of the block calls it.  With TRACK
@@ -161,6 +181,9 @@ __device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, doubl
                 wet_in |= w;
         }
     }
+    if (threadIdx.x == 0)
+        *reinterpret_cast<int*>(reinterpret_cast<unsigned short*>(reinterpret_cast<char*>(smem) + T::list_offset) +
+                                ((T::R1W * T::R1H + 1) & ~1)) = 0;
     if (__syncthreads_or(wet_seen) == 0) {
         /* no wet cell within two cells: h is unchanged (-0 becomes +0) */
         for (int t = threadIdx.x; t < TH * TW; t += THREADS) {
@@ -172,22 +195,39 @@ __device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, doubl
         return 0;
     }
 
-    /* 2. EP 1 on the tile + 1 ring; cells outside a flat grid have none */
-    for (int t = threadIdx.x; t < F; t += THREADS) {
-        const int a = t / T::R1W, b = t - a * T::R1W;
-        const int gi = i0 - 1 + a, gj = j0 - 1 + b;
-        const bool inside = p.toroidal || ((unsigned)gi < (unsigned)p.rows && (unsigned)gj < (unsigned)p.cols);
-        const int c = (a + 1) * T::R2W + (b + 1); /* this cell in the load region */
-        const double hc = sh[c];
-        double f[4] = {0.0, 0.0, 0.0, 0.0};
-        if (inside && is_wet(hc, p.eps_bits)) {
-            /* von Neumann order n = 1..4: north, west, east, south; u = z + h */
-            const double u1 = sz[c - T::R2W] + sh[c - T::R2W];
-            const double u2 = sz[c - 1] + sh[c - 1];
-            const double u3 = sz[c + 1] + sh[c + 1];
-            const double u4 = sz[c + T::R2W] + sh[c + T::R2W];
-            outflows(hc, sz[c], u1, u2, u3, u4, p.eps, p.r, f);
+    /* 2. EP 1 on the tile + 1 ring; cells outside a flat grid have none.
+     * 2a: outflows start at +0 and the wet cells are compacted into a list,
+     * 2b: one thread per listed cell, so that the FP64 work of a warp is not
+     * spread over the dry lanes of a partly wet tile. */
+    unsigned short* s_list = reinterpret_cast<unsigned short*>(reinterpret_cast<char*>(smem) + T::list_offset);
+    int* s_count = reinterpret_cast<int*>(s_list + ((F + 1) & ~1));
+    for (int t0 = 0; t0 < F; t0 += THREADS) {
+        const int t = t0 + threadIdx.x;
+        bool wet = false;
+        if (t < F) {
+            const int a = t / T::R1W, b = t - a * T::R1W;
+            const int gi = i0 - 1 + a, gj = j0 - 1 + b;
+            const bool inside = p.toroidal || ((unsigned)gi < (unsigned)p.rows && (unsigned)gj < (unsigned)p.cols);
+            wet = inside && is_wet(sh[(a + 1) * T::R2W + (b + 1)], p.eps_bits);
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                sf[q * F + t] = 0.0;
         }
+        warp_append_shared(wet, t, s_list, s_count);
+    }
+    __syncthreads();
+    const int nwet = *s_count;
+    for (int k = threadIdx.x; k < nwet; k += THREADS) {
+        const int t = s_list[k];
+        const int a = t / T::R1W, b = t - a * T::R1W;
+        const int c = (a + 1) * T::R2W + (b + 1); /* this cell in the load region */
+        /* von Neumann order n = 1..4: north, west, east, south; u = z + h */
+        const double u1 = sz[c - T::R2W] + sh[c - T::R2W];
+        const double u2 = sz[c - 1] + sh[c - 1];
+        const double u3 = sz[c + 1] + sh[c + 1];
+        const double u4 = sz[c + T::R2W] + sh[c + T::R2W];
+        double f[4];
+        outflows(sh[c], sz[c], u1, u2, u3, u4, p.eps, p.r, f);
 #pragma unroll
         for (int q = 0; q < 4; q++)
             sf[q * F + t] = f[q];

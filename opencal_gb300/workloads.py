@@ -152,3 +152,66 @@ def ensemble_inputs(dims, first_seed: int = 1000):
         zs.append(z)
         hs.append(h)
     return zs, hs
+
+
+# SCIARA-fv2 parameters of the reference's 2006 configuration file, in the
+# file's order (Pclock, PTsol, PTvent, Pr(Tsol), Pr(Tvent), Phc(Tsol),
+# Phc(Tvent), Pcool, Prho, Pepsilon, Psigma, Pcv), plus the cell size Pc.
+SCIARA_PARAMS = (60.0, 1143.0, 1360.0, 0.075, 0.90, 60.0, 0.4, 9.0, 2600.0, 0.90, 5.68e-08, 1150.0, 10.0)
+
+
+def _value_noise(rows: int, cols: int, seed: int, octaves: int = 5, base: int = 64) -> np.ndarray:
+    """Sum of bilinearly interpolated random lattices, one per octave (lattice
+    spacing halving, amplitude halving), scaled to [-1, 1]."""
+    rng_seed = seed
+    out = np.zeros((rows, cols))
+    amp = 1.0
+    step = float(base)
+    total = 0.0
+    for _ in range(octaves):
+        gr = int(rows / step) + 2
+        gc = int(cols / step) + 2
+        lat = uniform_array(rng_seed, (gr, gc)) * 2.0 - 1.0
+        rng_seed += 1
+        y = np.arange(rows, dtype=np.float64)[:, None] / step
+        x = np.arange(cols, dtype=np.float64)[None, :] / step
+        y0 = np.floor(y).astype(np.int64)
+        x0 = np.floor(x).astype(np.int64)
+        fy = y - y0
+        fx = x - x0
+        v = (lat[y0, x0] * (1 - fy) * (1 - fx) + lat[y0 + 1, x0] * fy * (1 - fx) +
+             lat[y0, x0 + 1] * (1 - fy) * fx + lat[y0 + 1, x0 + 1] * fy * fx)
+        out = out + amp * v
+        total += amp
+        amp *= 0.5
+        step = max(step / 2.0, 1.0)
+    return out / total
+
+
+def sciara_inputs(rows: int, cols: int, seed: int = 5, cell: float = 10.0, nvents: int | None = None,
+                  phases: int = 6, rate_range=(10.0, 50.0), slope: float = 3000.0 / 20480.0):
+    """A synthetic volcano for SCIARA-fv2: a cone (height falling linearly
+    from the centre with the given slope, 3000 m over 20.48 km on a 4096^2
+    grid of 10 m cells, clipped at 0) plus fractal value noise of +-5 m,
+    quantised to 2^-10 m; 1-3 vents (seeded) near the summit; emission rates
+    uniform in rate_range m^3/s for each of ``phases`` phases.
+    Returns (z, vents [(x, y)], rates [nvents][phases])."""
+    rng = SplitMix64(seed)
+    ci, cj = (rows - 1) / 2.0, (cols - 1) / 2.0
+    ii = np.arange(rows, dtype=np.float64)[:, None]
+    jj = np.arange(cols, dtype=np.float64)[None, :]
+    d = np.sqrt((ii - ci) ** 2 + (jj - cj) ** 2) * cell
+    height = slope * min(rows, cols) / 2.0 * cell
+    z = np.maximum(height - slope * d, 0.0) + 5.0 * _value_noise(rows, cols, seed * 7 + 1)
+    z = quantise(np.maximum(z, 0.0))
+    if nvents is None:
+        nvents = 1 + int(rng.next_u64() % 3)
+    spread = max(1.0, min(rows, cols) / 16.0)
+    vents = []
+    while len(vents) < nvents:
+        vi = int(round(ci + rng.uniform(-spread, spread)))
+        vj = int(round(cj + rng.uniform(-spread, spread)))
+        if (vj, vi) not in vents:
+            vents.append((vj, vi))
+    rates = [[rng.uniform(*rate_range) for _ in range(phases)] for _ in range(nvents)]
+    return np.ascontiguousarray(z), vents, rates

@@ -143,3 +143,37 @@ def life3d(s0, steps, *, nbhd=NB_MOORE - 0, toroidal=True, rule=(5, 7, 6, 6), ki
     if _fn(kind, "life3d")(rows, cols, slices, int(nbhd), int(toroidal), int(steps), *rule, s0, out):
         raise RuntimeError("oracle life3d failed")
     return out
+
+
+def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt0=None, st0=None,
+           kind="serial", want_cells=True):
+    """Run SCIARA-fv2 (oracle_sciara.c).  vents: [(x, y)], rates: [nvents][nphases]
+    m^3/s, emission_time: seconds per phase, steps: maximum steps (0 = until
+    the emission ends).  Returns dict(z, slt, st, msl, steps, cells)."""
+    from opencal_gb300.workloads import SCIARA_PARAMS
+    z0 = np.ascontiguousarray(z0, dtype=np.float64)
+    rows, cols = z0.shape
+    p = np.ascontiguousarray(params if params is not None else SCIARA_PARAMS, dtype=np.float64)
+    v = np.ascontiguousarray(np.asarray(vents, dtype=np.int32).reshape(-1))
+    r = np.ascontiguousarray(np.asarray(rates, dtype=np.float64).reshape(-1))
+    nphases = len(rates[0]) if len(rates) else 0
+    outs = {k: np.empty_like(z0) for k in ("z", "slt", "st", "msl")}
+    done = C.c_int(0)
+    n = C.c_long(0)
+    cells = np.zeros((rows * cols if (ac and want_cells) else 1, 2), dtype=np.int32)
+    f = _fn(kind, "sciara")
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_uint, C.c_int, C.c_void_p,
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                  C.POINTER(C.c_int), C.POINTER(C.c_long), C.c_void_p]
+    slt0 = None if slt0 is None else np.ascontiguousarray(slt0, dtype=np.float64)
+    st0 = None if st0 is None else np.ascontiguousarray(st0, dtype=np.float64)
+    rc = f(rows, cols, int(ac), int(steps), p.ctypes.data, len(vents), v.ctypes.data, int(emission_time), nphases,
+           r.ctypes.data, z0.ctypes.data, None if slt0 is None else slt0.ctypes.data,
+           None if st0 is None else st0.ctypes.data, outs["z"].ctypes.data, outs["slt"].ctypes.data,
+           outs["st"].ctypes.data, outs["msl"].ctypes.data, C.byref(done), C.byref(n),
+           cells.ctypes.data if (ac and want_cells) else None)
+    if rc:
+        raise RuntimeError(f"oracle sciara failed ({rc})")
+    outs["steps"] = done.value
+    outs["cells"] = cells[: n.value].copy() if (ac and want_cells) else np.zeros((0, 2), np.int32)
+    return outs
