@@ -74,6 +74,16 @@ int cal_sdt_batch_active_tiles(void* ensemble, int* counts /* steps + 1 */);
 int cal_sdt_batch_loss_grad(void* ensemble, const double* target /* device */, double* loss /* B */,
                             double* grad /* 2B */, double* dL_dh0 /* device, or NULL */);
 
+/* ---- SCIARA-fv2 (OpenCAL-OMP/examples/calomp_sciara-fv2/source/Sciara.cpp) ----
+ * params: Pclock, PTsol, PTvent, Pr(Tsol), Pr(Tvent), Phc(Tsol), Phc(Tvent),
+ * Pcool, Prho, Pepsilon, Psigma, Pcv (the .cfg order), Pc (cell size).
+ * vent_xy: (x = column, y = row) pairs in the reference's vent order; rates:
+ * nvents x nphases m^3/s; max_steps 0 runs until the emission ends. */
+int cal_sciara_run(int rows, int cols, int ac, int max_steps, const double* params, int nvents, const int* vent_xy,
+                   unsigned emission_time, int nphases, const double* rates, const double* z0, const double* slt0,
+                   const double* st0, double* z_out, double* slt_out, double* st_out, double* msl_out,
+                   int* steps_done, long* n_active, int* cells_out, int graph, double* ms);
+
 /* ---- Game of Life (OpenCAL-OMP/examples/calomp_life) and the 3D rule ---- */
 int cal_life2d_run(int rows, int cols, int toroidal, int as_int, int steps, const unsigned char* s0,
                    unsigned char* s_out, int mode, int block, int graph, double* ms);

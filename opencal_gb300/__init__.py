@@ -152,3 +152,42 @@ def life3d(s0, steps, *, nbhd=2, toroidal=True, rule=(5, 7, 6, 6), graph=False):
     _check(models().cal_life3d_run(rows, cols, slices, int(nbhd), int(toroidal), int(steps), *rule, s0, out,
                                    int(graph)), "cal_life3d_run")
     return out
+
+
+def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt0=None, st0=None, graph=False,
+           timing=False):
+    """SCIARA-fv2 on the GPU (csrc/models/sciara.cu): the reference program's
+    elementary processes as device processes behind the C API.  Same
+    arguments and result as oracle.sciara (dict z, slt, st, msl, steps,
+    cells), plus the device milliseconds of the step loop with timing=True."""
+    from .workloads import SCIARA_PARAMS
+    z0 = np.ascontiguousarray(z0, dtype=np.float64)
+    rows, cols = z0.shape
+    p = np.ascontiguousarray(params if params is not None else SCIARA_PARAMS, dtype=np.float64)
+    v = np.ascontiguousarray(np.asarray(vents, dtype=np.int32).reshape(-1))
+    r = np.ascontiguousarray(np.asarray(rates, dtype=np.float64).reshape(-1))
+    nphases = len(rates[0]) if len(rates) else 0
+    outs = {k: np.empty_like(z0) for k in ("z", "slt", "st", "msl")}
+    done = C.c_int(0)
+    n = C.c_long(0)
+    ms = C.c_double(0.0)
+    cells = np.zeros((rows * cols if ac else 1, 2), dtype=np.int32)
+    m = models()
+    f = m.cal_sciara_run
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_uint, C.c_int, C.c_void_p,
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                  C.POINTER(C.c_int), C.POINTER(C.c_long), C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+    slt0 = None if slt0 is None else np.ascontiguousarray(slt0, dtype=np.float64)
+    st0 = None if st0 is None else np.ascontiguousarray(st0, dtype=np.float64)
+    rc = f(rows, cols, int(ac), int(steps), p.ctypes.data, len(vents), v.ctypes.data, int(emission_time), nphases,
+           r.ctypes.data, z0.ctypes.data, None if slt0 is None else slt0.ctypes.data,
+           None if st0 is None else st0.ctypes.data, outs["z"].ctypes.data, outs["slt"].ctypes.data,
+           outs["st"].ctypes.data, outs["msl"].ctypes.data, C.byref(done), C.byref(n),
+           cells.ctypes.data if ac else None, int(bool(graph)), C.byref(ms))
+    _check(rc, "cal_sciara_run")
+    outs["steps"] = done.value
+    outs["cells"] = cells[: n.value].copy() if ac else np.zeros((0, 2), np.int32)
+    if timing:
+        outs["ms"] = ms.value
+    return outs

@@ -109,3 +109,30 @@ def test_oracle_vs_live_reference(oracle_lib, seed):
     v = W.random_field((30, 26), seed=seed)
     for nb in (1, 2, 3, 4):
         assert bits_equal(oracle.nbprobe2d(v, 4, nbhd=nb), oracle.nbprobe2d(v, 4, nbhd=nb, kind="ref"))
+
+
+def _sciara_cases():
+    fx = np.load(os.path.join(GOLDEN, "sciara_cases.npz"))
+    n = len([k for k in fx.files if k.endswith("_dims")])
+    return fx, n
+
+
+@pytest.mark.parametrize("idx", range(6))
+def test_oracle_sciara_matches_reference_fixtures(oracle_lib, idx):
+    """oracle_sciara.c against the reference's own SCIARA-fv2 program
+    (compiled from its sources, run on the same synthetic inputs): Sz, Slt,
+    St and Msl bit for bit.  The transcendental functions are the C
+    library's on both sides (same machine class as the fixtures: x86-64
+    glibc)."""
+    fx, n = _sciara_cases()
+    assert idx < n
+    p = f"c{idx}_"
+    rows, cols, seed, et, steps, ac = (int(v) for v in fx[p + "dims"])
+    vents = [tuple(v) for v in fx[p + "vents"]]
+    rates = fx[p + "rates"].tolist()
+    out = oracle_lib.sciara(fx[p + "z0"], vents, rates, et, steps, ac=bool(ac))
+    for k in ("z", "slt", "st", "msl"):
+        assert out[k].tobytes() == fx[p + k].tobytes(), k
+    assert out["steps"] == int(fx[p + "steps"][0])
+    if ac:
+        assert len(out["cells"]) == int(fx[p + "active"][0])
