@@ -51,7 +51,24 @@ BYTES_PER_CELL_UPDATE = 24  # z read + h read + h write (FP64)
 REF_SAMPLE_STEPS = 64
 # how the 4000 steps are issued: a launch sequence per step, a recorded step
 # replayed as a CUDA graph, or one device-driven graph launch for the loop
-LOOPS = {"eager": 0, "graph": 1, "device": 2}
+# or every step in one cooperative launch of the persistent split-step kernel
+LOOPS = {"eager": 0, "graph": 1, "device": 2, "persistent": 4}
+# The plain step: the split step (K1 + K2 per step) unless
+# OPENCAL_SDT_KERNEL selects the sparse fused step (one launch per step) or
+# the dense single kernel.  Kernels of ours per CA step and per run: the device loop
+# adds its step-count check per step, the persistent loop (split step only)
+# is one kernel per run; every run starts with the priming kernel.
+STEP_KERNEL = os.environ.get("OPENCAL_SDT_KERNEL", "split")
+
+
+def launches_per_step(loop):
+    if loop == "persistent":
+        return 0
+    base = 2 if STEP_KERNEL == "split" else 1
+    return base + (1 if loop == "device" else 0)
+
+
+LAUNCHES_PER_RUN = {"eager": 1, "graph": 1, "device": 1, "persistent": 2}
 
 
 def _peaks():
@@ -203,7 +220,8 @@ def gpu_arm(args):
     m.cal_sciddicaT_steps.argtypes = [C.c_void_p, C.c_int, C.c_int]
     m.cal_sciddicaT_kernel_times.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     m.cal_sciddicaT_wet_count.argtypes = [C.c_void_p]
-    m.cal_sciddicaT_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    m.cal_sciddicaT_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    m.cal_sciddicaT_persist_failed.argtypes = [C.c_void_p]
     m.cal_sciddicaT_read.argtypes = [C.c_void_p, C.c_void_p]
 
     cudart = C.CDLL("libcudart.so", mode=C.RTLD_GLOBAL) if False else None  # noqa: F841
@@ -250,13 +268,26 @@ def gpu_arm(args):
     # every launch, over 400 steps from the mid-run state (step 1000)
     m.cal_sciddicaT_reset(sess)
     m.cal_sciddicaT_steps(sess, 1000, 0)
-    wet = m.cal_sciddicaT_wet_count(sess)
+    h1000 = np.empty_like(h)
+    m.cal_sciddicaT_read(sess, h1000.ctypes.data)
+    wet = int(np.count_nonzero(h1000 > P_EPS))
     nk = 400
     ka = (C.c_float * nk)()
     kb = (C.c_float * nk)()
     m.cal_sciddicaT_kernel_times(sess, nk, ka, kb)
     k1_ms, k2_ms = float(np.mean(list(ka))), float(np.mean(list(kb)))
     kavg_ms = k1_ms + k2_ms
+    kernel_desc = "SCIDDICA-T step = sdt2::k1_outflows (wet cells) + sdt2::k2_update (flagged tiles)"
+    if STEP_KERNEL == "sparse":
+        kernel_desc = ("SCIDDICA-T sparse fused step sdt3::k_sparse_step (one launch per step over the flagged "
+                       "32x16 tiles, h layers used alternately)")
+    elif STEP_KERNEL == "single":
+        kernel_desc = "SCIDDICA-T dense fused step sdt::fused_step (every tile every step)"
+    if args.loop == "persistent":
+        # one launch runs all 4000 steps: its per-step time is the run's
+        kavg_ms = float(np.mean(run_ms)) / CA_STEPS
+        kernel_desc = ("SCIDDICA-T split step, all 4000 steps in one cooperative launch of sdt2::k_persist "
+                       "(K1 and K2 phases separated by grid barriers)")
     peak, peak_kind = _peaks()
     achieved = ROWS * COLS * BYTES_PER_CELL_UPDATE / (kavg_ms * 1e-3) / 1e9
 
@@ -268,24 +299,33 @@ def gpu_arm(args):
     for it in range(max(1, min(args.steps, 3)) + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        m.cal_sciddicaT_host_run(sess, pin_z.data_ptr(), pin_h.data_ptr(), CA_STEPS, out.data_ptr())
+        m.cal_sciddicaT_host_run(sess, pin_z.data_ptr(), pin_h.data_ptr(), CA_STEPS, LOOPS[args.loop],
+                                 out.data_ptr())
         t1 = time.perf_counter()
         if it > 0:
             e2e_times.append(t1 - t0)
     e2e_value = ROWS * COLS * CA_STEPS * world / max_over_ranks(dist, float(np.mean(e2e_times)))
 
-    # correctness guard on the timed path: fused state after a run is finite and mass is conserved
+    # correctness guard on the timed path: a run in the timed mode is finite,
+    # no grid barrier gave up, and it equals, bit for bit, the end-to-end run
+    # and a run with one launch sequence per step
     m.cal_sciddicaT_reset(sess)
-    m.cal_sciddicaT_steps(sess, CA_STEPS, 0)
+    m.cal_sciddicaT_steps(sess, CA_STEPS, LOOPS[args.loop])
+    barrier_failed = m.cal_sciddicaT_persist_failed(sess) if args.loop == "persistent" else 0
     hh = np.empty_like(h)
     m.cal_sciddicaT_read(sess, hh.ctypes.data)
+    m.cal_sciddicaT_reset(sess)
+    m.cal_sciddicaT_steps(sess, CA_STEPS, 0)
+    he = np.empty_like(h)
+    m.cal_sciddicaT_read(sess, he.ctypes.data)
     m.cal_sciddicaT_close(sess)
+    consistent = bool(hh.tobytes() == he.tobytes() == out.numpy().tobytes()) and not barrier_failed
 
     if rank != 0:
         return
     # DRAM bytes of one step (K1 + K2) from the committed ncu capture
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "sciddicaT_split_step_2048.json")
+    tpath = os.path.join(ROOT, "profiles", f"sciddicaT_{STEP_KERNEL}_step_2048.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             traffic = json.load(f).get("dram_bytes_per_step")
@@ -295,24 +335,24 @@ def gpu_arm(args):
         "ms_per_step": float(np.mean(run_ms)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded DEM + elliptical source)",
         "config": {"workload": f"SCIDDICA-T {ROWS}x{COLS} FP64, von Neumann, flat, plain (no active cells), "
-                               f"{CA_STEPS} CA steps per bench step, split step (outflows of wet cells, "
-                               f"update of flagged tiles), step loop: {args.loop}",
+                               f"{CA_STEPS} CA steps per bench step, {STEP_KERNEL} step, step loop: {args.loop}",
                    "l2": "flushed (256 MiB write) before every run", "seed": SEED, "p_r": P_R, "p_eps": P_EPS,
                    "parallelism": f"replicas x{world}"},
         "wall_s": t_wall,
-        "gpu_launches": 2 * CA_STEPS * args.steps + args.steps,  # K1 + K2 per CA step, one priming kernel per run
+        "gpu_launches": (launches_per_step(args.loop) * CA_STEPS + LAUNCHES_PER_RUN[args.loop]) * args.steps,
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": int(2 * z.nbytes),
                 "d2h_bytes_per_step": int(h.nbytes)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "SCIDDICA-T step = sdt2::k1_outflows (wet cells) + sdt2::k2_update (flagged tiles)",
-                     "basis": "achieved = 24 B x rows x cols per step (dense algorithmic bytes) / (K1 + K2 mean "
-                              "event time); traffic = ncu DRAM bytes of K1 + K2 at the same step (fields stay "
-                              "in L2)",
-                     "kernel_avg_ms": kavg_ms, "k1_outflows_ms": k1_ms, "k2_update_ms": k2_ms,
+                     "kernel": kernel_desc,
+                     "basis": "achieved = 24 B x rows x cols per step (dense algorithmic bytes) / mean event "
+                              "time of one step's kernels; traffic = ncu DRAM bytes of one step at step ~1000 "
+                              "(fields stay in L2)",
+                     "kernel_avg_ms": kavg_ms,
                      "wet_cells_at_step_1000": wet,
                      "bytes_per_step": ROWS * COLS * BYTES_PER_CELL_UPDATE},
         "finite": bool(np.isfinite(hh).all()),
+        "consistent": consistent,
         "clocks": clk,
     }
     if not args.no_cpu_baseline:
@@ -439,7 +479,7 @@ def ncu_case(args):
     sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_FUSED)
     done = 0
     for target in sorted(set([args.ncu_steps] + [s for s in (500, 1000, 2000, 3000, 4000) if s < args.ncu_steps])):
-        m.cal_sciddicaT_steps(sess, target - done, 0)
+        m.cal_sciddicaT_steps(sess, target - done, LOOPS[args.loop])
         done = target
         hh = np.empty_like(h)
         m.cal_sciddicaT_read(sess, hh.ctypes.data)

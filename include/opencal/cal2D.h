@@ -150,8 +150,11 @@ void calSync2D(struct CALModel2D* ca2D);
 void calSyncSubstate2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q);
 void calSyncSubstate2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q);
 void calSyncSubstate2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q);
-/* Declare that host code wrote the mirrors directly (Q->current[...] = ...):
- * the next device operation uploads them. */
+/* Declare that host code wrote the mirrors directly (Q->current[...] = ...,
+ * Q->next[...] = ...): every layer's host mirror becomes the authoritative
+ * copy and the next device operation uploads it.  After device work the
+ * mirrors are stale: call calSync2D before writing only part of them (a
+ * program that overwrites them entirely need not). */
 void calMarkHostDirty2D(struct CALModel2D* ca2D);
 /* Wait for all device work queued on the model. */
 void calFinish2D(struct CALModel2D* ca2D);

@@ -39,10 +39,15 @@ int cal_sciddicaT_device_loop_fallbacks(void);
 void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, double p_r, double p_eps, const double* z0,
                          const double* h0, int mode);
 int cal_sciddicaT_reset(void* session);
+/* graph: as for cal_sciddicaT_run, plus 4 = every step in one cooperative
+ * launch of the persistent split-step kernel (mode 1, plain) */
 int cal_sciddicaT_steps(void* session, int steps, int graph);
+/* 1 when a grid barrier of the last persistent run gave up (synchronises) */
+int cal_sciddicaT_persist_failed(void* session);
 int cal_sciddicaT_set_params(void* session, double p_r, double p_eps);
 void* cal_sciddicaT_stream(void* session); /* cudaStream_t of the model */
-int cal_sciddicaT_host_run(void* session, const double* z_host, const double* h_host, int steps, double* h_out);
+int cal_sciddicaT_host_run(void* session, const double* z_host, const double* h_host, int steps, int graph,
+                           double* h_out);
 int cal_sciddicaT_kernel_times(void* session, int n, float* ms_outflows, float* ms_update);
 int cal_sciddicaT_wet_count(void* session);
 int cal_sciddicaT_read(void* session, double* h_out);

@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include "cal_model_internal.cuh"
+#include "opencal/cal2DUnsafe.h"
 
 using cal::CalGrid;
 
@@ -535,12 +536,17 @@ extern "C" void calSync2D(struct CALModel2D* ca)
 
 extern "C" void calMarkHostDirty2D(struct CALModel2D* ca)
 {
+    /* every layer's host mirror becomes the authoritative copy (the caller
+     * either overwrote it entirely or made it current first with calSync) */
     CalGrid& g = G(ca);
     for (int t = 0; t < CAL_NTYPES; t++)
         for (int s = 0; s < g.nslot[t]; s++)
-            for (int l = 0; l < (g.sub[t][s].single ? 1 : 2); l++)
-                if (g.sub[t][s].layer[l].host_valid)
-                    g.host_wrote(t, s, l);
+            for (int l = 0; l < (g.sub[t][s].single ? 1 : 2); l++) {
+                g.host_wrote(t, s, l);
+                g.sub[t][s].layer[l].host_valid = true;
+                if (l == 1)
+                    g.sub[t][s].next_stale = false;
+            }
     if (g.active && g.flags_host_valid)
         g.flags_dev_valid = false;
 }
@@ -600,3 +606,59 @@ extern "C" void calFinalize2D(struct CALModel2D* ca)
     free(ca->elementary_processes);
     free(ca);
 }
+
+/* ======================= unsafe operations (cal2DUnsafe.h) ============== */
+/* OpenCAL-OMP/source/cal2DUnsafe.c:17-275, on the host mirrors */
+
+#define CAL_UNSAFE_OPS_2D(S, T, TC)                                                                          \
+    extern "C" T calGetNext2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j)            \
+    {                                                                                                        \
+        if (!G(ca).to_host(TC, slot_of(ca, TC, Q), 1))                                                       \
+            return (T)0;                                                                                     \
+        return Q->next[(long long)i * ca->columns + j];                                                      \
+    }                                                                                                        \
+    extern "C" T calGetNextX2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, int n)    \
+    {                                                                                                        \
+        int a, b;                                                                                            \
+        if (!neighbor(ca, i, j, n, &a, &b))                                                                  \
+            return (T)0;                                                                                     \
+        return calGetNext2D##S(ca, Q, a, b);                                                                 \
+    }                                                                                                        \
+    extern "C" void calSetX2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, int n, T v) \
+    {                                                                                                        \
+        int a, b;                                                                                            \
+        if (neighbor(ca, i, j, n, &a, &b))                                                                   \
+            calSet2D##S(ca, Q, a, b, v);                                                                     \
+    }                                                                                                        \
+    extern "C" void calSetCurrentX2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, int n, \
+                                        T v)                                                                 \
+    {                                                                                                        \
+        int a, b;                                                                                            \
+        if (neighbor(ca, i, j, n, &a, &b))                                                                   \
+            calSetCurrent2D##S(ca, Q, a, b, v);                                                              \
+    }                                                                                                        \
+    extern "C" void calInitX2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, int n, T v) \
+    {                                                                                                        \
+        int a, b;                                                                                            \
+        if (neighbor(ca, i, j, n, &a, &b))                                                                   \
+            calInit2D##S(ca, Q, a, b, v);                                                                    \
+    }                                                                                                        \
+    extern "C" void calAddNext2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, T v)    \
+    {                                                                                                        \
+        const int s = slot_of(ca, TC, Q);                                                                    \
+        if (!G(ca).to_host(TC, s, 1))                                                                        \
+            return;                                                                                          \
+        T* p = &Q->next[(long long)i * ca->columns + j];                                                     \
+        *p = (T)(*p + v);                                                                                    \
+        G(ca).host_wrote(TC, s, 1);                                                                          \
+    }                                                                                                        \
+    extern "C" void calAddNextX2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, int i, int j, int n, T v) \
+    {                                                                                                        \
+        int a, b;                                                                                            \
+        if (neighbor(ca, i, j, n, &a, &b))                                                                   \
+            calAddNext2D##S(ca, Q, a, b, v);                                                                 \
+    }
+
+CAL_UNSAFE_OPS_2D(b, CALbyte, 0)
+CAL_UNSAFE_OPS_2D(i, CALint, 1)
+CAL_UNSAFE_OPS_2D(r, CALreal, 2)

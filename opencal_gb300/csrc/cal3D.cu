@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include "cal_model_internal.cuh"
+#include "opencal/cal3DUnsafe.h"
 
 using cal::CalGrid;
 
@@ -449,12 +450,17 @@ extern "C" void calSync3D(struct CALModel3D* ca)
 
 extern "C" void calMarkHostDirty3D(struct CALModel3D* ca)
 {
+    /* every layer's host mirror becomes the authoritative copy (the caller
+     * either overwrote it entirely or made it current first with calSync) */
     CalGrid& g = G(ca);
     for (int t = 0; t < CAL_NTYPES; t++)
         for (int s = 0; s < g.nslot[t]; s++)
-            for (int l = 0; l < (g.sub[t][s].single ? 1 : 2); l++)
-                if (g.sub[t][s].layer[l].host_valid)
-                    g.host_wrote(t, s, l);
+            for (int l = 0; l < (g.sub[t][s].single ? 1 : 2); l++) {
+                g.host_wrote(t, s, l);
+                g.sub[t][s].layer[l].host_valid = true;
+                if (l == 1)
+                    g.sub[t][s].next_stale = false;
+            }
     if (g.active && g.flags_host_valid)
         g.flags_dev_valid = false;
 }
@@ -490,3 +496,62 @@ extern "C" void calFinalize3D(struct CALModel3D* ca)
     free(ca->elementary_processes);
     free(ca);
 }
+
+/* ======================= unsafe operations (cal3DUnsafe.h) ============== */
+/* OpenCAL-OMP/source/cal3DUnsafe.c:18-245, on the host mirrors */
+
+#define CAL_UNSAFE_OPS_3D(S, T, TC)                                                                          \
+    extern "C" T calGetNext3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q, int i, int j, int k)     \
+    {                                                                                                        \
+        if (!G(ca).to_host(TC, slot_of(ca, TC, Q), 1))                                                       \
+            return (T)0;                                                                                     \
+        return Q->next[G(ca).lin(i, j, k)];                                                                  \
+    }                                                                                                        \
+    extern "C" T calGetNextX3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q, int i, int j, int k, int n) \
+    {                                                                                                        \
+        int a, b, c;                                                                                         \
+        if (!neighbor(ca, i, j, k, n, &a, &b, &c))                                                           \
+            return (T)0;                                                                                     \
+        return calGetNext3D##S(ca, Q, a, b, c);                                                              \
+    }                                                                                                        \
+    extern "C" void calSetX3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q, int i, int j, int k, int n, \
+                                 T v)                                                                        \
+    {                                                                                                        \
+        int a, b, c;                                                                                         \
+        if (neighbor(ca, i, j, k, n, &a, &b, &c))                                                            \
+            calSet3D##S(ca, Q, a, b, c, v);                                                                  \
+    }                                                                                                        \
+    extern "C" void calSetCurrentX3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q, int i, int j, int k, \
+                                        int n, T v)                                                          \
+    {                                                                                                        \
+        int a, b, c;                                                                                         \
+        if (neighbor(ca, i, j, k, n, &a, &b, &c))                                                            \
+            calSetCurrent3D##S(ca, Q, a, b, c, v);                                                           \
+    }                                                                                                        \
+    extern "C" void calInitX3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q, int i, int j, int k, int n, \
+                                  T v)                                                                       \
+    {                                                                                                        \
+        int a, b, c;                                                                                         \
+        if (neighbor(ca, i, j, k, n, &a, &b, &c))                                                            \
+            calInit3D##S(ca, Q, a, b, c, v);                                                                 \
+    }                                                                                                        \
+    extern "C" void calAddNext3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q, int i, int j, int k, T v) \
+    {                                                                                                        \
+        const int s = slot_of(ca, TC, Q);                                                                    \
+        if (!G(ca).to_host(TC, s, 1))                                                                        \
+            return;                                                                                          \
+        T* p = &Q->next[G(ca).lin(i, j, k)];                                                                 \
+        *p = (T)(*p + v);                                                                                    \
+        G(ca).host_wrote(TC, s, 1);                                                                          \
+    }                                                                                                        \
+    extern "C" void calAddNextX3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q, int i, int j, int k, int n, \
+                                     T v)                                                                    \
+    {                                                                                                        \
+        int a, b, c;                                                                                         \
+        if (neighbor(ca, i, j, k, n, &a, &b, &c))                                                            \
+            calAddNext3D##S(ca, Q, a, b, c, v);                                                              \
+    }
+
+CAL_UNSAFE_OPS_3D(b, CALbyte, 0)
+CAL_UNSAFE_OPS_3D(i, CALint, 1)
+CAL_UNSAFE_OPS_3D(r, CALreal, 2)

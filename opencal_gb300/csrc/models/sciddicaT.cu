@@ -256,25 +256,40 @@ static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
 constexpr int K1_THREADS = 64; /* small blocks: the wet list spreads over every SM */
 constexpr int K2_BLOCKS = 152 * 4;
 
+/* Loads of data that other blocks write while the kernel runs: in the
+ * persistent kernel (CO = true) they go to L2 (ld.global.cg) so that no
+ * stale L1 line from an earlier step is read; the per-step kernels use the
+ * ordinary paths. */
+template <bool CO, typename T>
+static __device__ __forceinline__ T ldm(const T* p)
+{
+    return CO ? __ldcg(p) : *p;
+}
+template <bool CO>
+static __device__ __forceinline__ double ldh(const double* p)
+{
+    return CO ? __ldcg(p) : __ldg(p);
+}
+
 /* flag tile t for this step's K2 and append it to the work-list once */
+template <bool CO>
 static __device__ __forceinline__ void flag_tile(int* tflag, int* tlist, int* tcount, int t, int epoch)
 {
-    if (tflag[t] != epoch && atomicExch(tflag + t, epoch) != epoch)
+    if (ldm<CO>(tflag + t) != epoch && atomicExch(tflag + t, epoch) != epoch)
         tlist[atomicAdd(tcount, 1)] = t;
 }
 
-__global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant__ K1Params p)
+/* K1's work: the outflows of every listed wet cell (threads tid, tid +
+ * nthreads, ...) and the clearing of the dried cells' outflows */
+template <bool CO>
+static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int epoch, int* tcount, int tid,
+                                               int nthreads)
 {
-    const int par = p.counts[4];
-    const int epoch = p.counts[6];
     const int* list = par ? p.list1 : p.list0;
     const int* zlist = par ? p.zlist1 : p.zlist0;
-    if (blockIdx.x == 0 && threadIdx.x < 2)
-        p.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists K2 will append to */
-    const int stride = gridDim.x * blockDim.x;
-    const int nw = p.counts[par];
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nw; k += stride) {
-        const int c = list[k];
+    const int nw = ldm<CO>(p.counts + par);
+    for (int k = tid; k < nw; k += nthreads) {
+        const int c = ldm<CO>(list + k);
         const int i = c / p.cols, j = c - i * p.cols;
         /* neighbours in von Neumann order n = 1..4: north, west, east, south */
         int ni[4] = {i - 1, i, i, i + 1}, nj[4] = {j, j - 1, j + 1, j};
@@ -294,13 +309,13 @@ __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant_
             nj[q] = b;
             if (in[q]) {
                 const long long cn = (long long)a * p.cols + b;
-                u[q] = __ldg(p.z + cn) + __ldg(p.h + cn);
+                u[q] = __ldg(p.z + cn) + ldh<CO>(p.h + cn);
             } else {
                 u[q] = 0.0 + 0.0; /* an absent neighbour reads z = 0, h = 0 */
             }
         }
         double f[4];
-        sdt::outflows(__ldg(p.h + c), __ldg(p.z + c), u[0], u[1], u[2], u[3], p.eps, p.r, f);
+        sdt::outflows(ldh<CO>(p.h + c), __ldg(p.z + c), u[0], u[1], u[2], u[3], p.eps, p.r, f);
         bool any = false;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
@@ -308,19 +323,28 @@ __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant_
             if (__double_as_longlong(f[q]) != 0) {
                 any = true;
                 if (in[q]) /* the receiver reads it */
-                    flag_tile(p.tflag, p.tlist, p.counts + 7, tile_of(ni[q], nj[q], p.tiles_x), epoch);
+                    flag_tile<CO>(p.tflag, p.tlist, tcount, tile_of(ni[q], nj[q], p.tiles_x), epoch);
             }
         }
         if (any)
-            flag_tile(p.tflag, p.tlist, p.counts + 7, tile_of(i, j, p.tiles_x), epoch);
+            flag_tile<CO>(p.tflag, p.tlist, tcount, tile_of(i, j, p.tiles_x), epoch);
     }
-    const int nz = p.counts[2 + par];
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nz; k += stride) {
-        const int c = zlist[k];
+    const int nz = ldm<CO>(p.counts + 2 + par);
+    for (int k = tid; k < nz; k += nthreads) {
+        const int c = ldm<CO>(zlist + k);
 #pragma unroll
         for (int q = 0; q < 4; q++)
             p.f[q * p.n + c] = 0.0;
     }
+}
+
+__global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant__ K1Params p)
+{
+    const int par = p.counts[4];
+    const int epoch = p.counts[6];
+    if (blockIdx.x == 0 && threadIdx.x < 2)
+        p.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists K2 will append to */
+    k1_work<false>(p, par, epoch, p.counts + 7, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 /* append the lanes whose predicate holds to list/count (warp-aggregated) */
@@ -385,6 +409,7 @@ static __device__ __forceinline__ void block_append4(const bool want[4], const b
 }
 
 /* one flagged tile: h += inflows - outflows in place, then the wet test */
+template <bool CO>
 static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int* list, int* count, int* zlist,
                                                int* zcount)
 {
@@ -399,8 +424,8 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
     const bool full = i < p.rows && jb + 3 < p.cols && (p.cols & 1) == 0;
     if (full) {
         /* c0 is a multiple of 2 (jb and cols even): two 16-byte loads */
-        const double2 a = *reinterpret_cast<const double2*>(p.h + c0);
-        const double2 b = *reinterpret_cast<const double2*>(p.h + c0 + 2);
+        const double2 a = ldm<CO>(reinterpret_cast<const double2*>(p.h + c0));
+        const double2 b = ldm<CO>(reinterpret_cast<const double2*>(p.h + c0 + 2));
         hv[0] = a.x;
         hv[1] = a.y;
         hv[2] = b.x;
@@ -413,7 +438,7 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
         for (int q = 0; q < 4; q++) {
             cell[q] = i < p.rows && jb + q < p.cols;
             if (cell[q])
-                hv[q] = p.h[c0 + q];
+                hv[q] = ldm<CO>(p.h + c0 + q);
         }
     }
     bool want[4], dried[4];
@@ -424,7 +449,8 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
         const long long c = c0 + q;
         double hn = hv[q];
         if (cell[q]) {
-            const double o0 = p.f[c], o1 = p.f[p.n + c], o2 = p.f[2 * p.n + c], o3 = p.f[3 * p.n + c];
+            const double o0 = ldm<CO>(p.f + c), o1 = ldm<CO>(p.f + p.n + c), o2 = ldm<CO>(p.f + 2 * p.n + c),
+                         o3 = ldm<CO>(p.f + 3 * p.n + c);
             /* inflow from neighbour n is its outflow f[4-n]; absent neighbours give 0 */
             double in1 = 0.0, in2 = 0.0, in3 = 0.0, in4 = 0.0;
             int a = i - 1, b = j - 1, d = j + 1, e = i + 1;
@@ -435,13 +461,13 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
                 d = d >= p.cols ? d - p.cols : d;
             }
             if ((unsigned)a < (unsigned)p.rows)
-                in1 = p.f[3 * p.n + (long long)a * p.cols + j];
+                in1 = ldm<CO>(p.f + 3 * p.n + (long long)a * p.cols + j);
             if ((unsigned)b < (unsigned)p.cols)
-                in2 = p.f[2 * p.n + (long long)i * p.cols + b];
+                in2 = ldm<CO>(p.f + 2 * p.n + (long long)i * p.cols + b);
             if ((unsigned)d < (unsigned)p.cols)
-                in3 = p.f[1 * p.n + (long long)i * p.cols + d];
+                in3 = ldm<CO>(p.f + 1 * p.n + (long long)i * p.cols + d);
             if ((unsigned)e < (unsigned)p.rows)
-                in4 = p.f[(long long)e * p.cols + j];
+                in4 = ldm<CO>(p.f + (long long)e * p.cols + j);
             const long long any = __double_as_longlong(in1) | __double_as_longlong(in2) |
                                   __double_as_longlong(in3) | __double_as_longlong(in4) |
                                   __double_as_longlong(o0) | __double_as_longlong(o1) |
@@ -464,37 +490,42 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
     block_append4(want, dried, value, list, count, zlist, zcount);
 }
 
-/* K2: a fixed grid working through the flagged tiles, then through the
- * current wet list in chunks of THREADS entries (carrying over the wet
+/* K2's work for blocks block, block + nblocks, ...: the flagged tiles, then
+ * the current wet list in chunks of THREADS entries (carrying over the wet
  * cells of unflagged tiles, whose h did not change) */
-__global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2Params p)
+template <bool CO>
+static __device__ __forceinline__ void k2_work(const K2Params& p, int par, int epoch, int ntiles, int nwet, int block,
+                                               int nblocks)
 {
-    const int par = p.counts[4];
-    const int epoch = p.counts[6];
-    const int ntiles = p.counts[7];
-    const int nwet = p.counts[par];
     const int* cur = par ? p.list1 : p.list0;
     int* list = par ? p.list0 : p.list1; /* next step's lists */
     int* zlist = par ? p.zlist0 : p.zlist1;
     int* count = p.counts + (1 - par);
     int* zcount = p.counts + 2 + (1 - par);
     const int items = ntiles + (nwet + THREADS - 1) / THREADS;
-    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    for (int item = block; item < items; item += nblocks) {
         if (item < ntiles) {
-            k2_tile(p, p.tlist[item], list, count, zlist, zcount);
+            k2_tile<CO>(p, ldm<CO>(p.tlist + item), list, count, zlist, zcount);
             __syncthreads(); /* block_append4's shared words are reused */
         } else {
             const int k = (item - ntiles) * THREADS + threadIdx.x;
             bool carry = false;
             int c = 0;
             if (k < nwet) {
-                c = cur[k];
+                c = ldm<CO>(cur + k);
                 const int i = c / p.cols, j = c - i * p.cols;
-                carry = p.tflag[tile_of(i, j, p.tiles_x)] != epoch;
+                carry = ldm<CO>(p.tflag + tile_of(i, j, p.tiles_x)) != epoch;
             }
             warp_append(carry, c, list, count);
         }
     }
+}
+
+__global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2Params p)
+{
+    const int par = p.counts[4];
+    const int epoch = p.counts[6];
+    k2_work<false>(p, par, epoch, p.counts[7], p.counts[par], blockIdx.x, gridDim.x);
     if (threadIdx.x == 0) {
         /* every block read parity, epoch and counts at its start; the last
          * one to finish advances them for the next step (no block waits for
@@ -506,6 +537,78 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
             p.counts[6] = epoch + 1;
             p.counts[7] = 0;
         }
+    }
+}
+
+/* ---- persistent form: every step of a run in one cooperative launch ----
+ * The two phases of each step (K1's and K2's work) are separated by a grid
+ * barrier.  counts[7 + (s & 1)] counts the flagged tiles of step s (one
+ * step's count is cleared while the other is in use); counts[12..13] are the
+ * barrier's arrival count and generation, counts[14] the error flag. */
+constexpr unsigned BARRIER_SPIN_LIMIT = 1u << 22;
+
+/* Grid barrier for a cooperative launch (all blocks resident).  Every wait
+ * is bounded: after BARRIER_SPIN_LIMIT polls the error flag is set and the
+ * block goes on; callers stop working once the flag is set.  Returns false
+ * when it is. */
+static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblocks)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned* arrived = reinterpret_cast<unsigned*>(counts + 12);
+        unsigned* generation = reinterpret_cast<unsigned*>(counts + 13);
+        const unsigned g = __ldcg(generation);
+        __threadfence();
+        if (atomicAdd(arrived, 1u) == nblocks - 1) {
+            atomicExch(arrived, 0u);
+            __threadfence();
+            atomicAdd(generation, 1u);
+        } else {
+            unsigned polls = 0;
+            while (__ldcg(generation) == g) {
+                if (++polls > BARRIER_SPIN_LIMIT) {
+                    atomicExch(counts + 14, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return __ldcg(counts + 14) == 0;
+}
+
+__global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ K1Params a,
+                                                     const __grid_constant__ K2Params b, int nsteps)
+{
+    int par = __ldcg(a.counts + 4);
+    int epoch = __ldcg(a.counts + 6);
+    const unsigned nb = gridDim.x;
+    for (int s = 0; s < nsteps; s++) {
+        int* tcount = a.counts + 7 + (s & 1);
+        if (blockIdx.x == 0 && threadIdx.x < 3) {
+            if (threadIdx.x < 2)
+                a.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists phase B appends to */
+            else
+                a.counts[7 + ((s + 1) & 1)] = 0; /* next step's tile count (read last in step s - 1) */
+        }
+        k1_work<true>(a, par, epoch, tcount, blockIdx.x * THREADS + threadIdx.x, nb * THREADS);
+        if (!grid_barrier(a.counts, nb))
+            return;
+        k2_work<true>(b, par, epoch, __ldcg(tcount), __ldcg(a.counts + par), blockIdx.x, nb);
+        if (!grid_barrier(a.counts, nb))
+            return;
+        par = 1 - par;
+        epoch++;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        /* the state the per-step kernels expect */
+        a.counts[4] = par;
+        a.counts[5] = 0;
+        a.counts[6] = epoch;
+        a.counts[7] = 0;
+        a.counts[8] = 0;
     }
 }
 
@@ -555,7 +658,7 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         s.tiles_x = (ca->columns + TW - 1) / TW;
         s.tiles_y = (ca->rows + TH - 1) / TH;
         bool ok = cudaMalloc(&s.f, 4 * n * sizeof(double)) == cudaSuccess &&
-                  cudaMalloc(&s.counts, 8 * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&s.counts, 16 * sizeof(int)) == cudaSuccess &&
                   cudaMalloc(&s.tflag, sizeof(int) * s.tiles_x * s.tiles_y) == cudaSuccess &&
                   cudaMalloc(&s.tlist, sizeof(int) * s.tiles_x * s.tiles_y) == cudaSuccess;
         for (int k = 0; k < 2 && ok; k++)
@@ -567,7 +670,7 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         }
     }
     cudaMemsetAsync(s.f, 0, 4 * n * sizeof(double), st);
-    cudaMemsetAsync(s.counts, 0, 8 * sizeof(int), st); /* parity 0, ticket 0, no flagged tile */
+    cudaMemsetAsync(s.counts, 0, 16 * sizeof(int), st); /* parity 0, ticket 0, no flagged tile */
     cudaMemsetAsync(s.tflag, 0, sizeof(int) * s.tiles_x * s.tiles_y, st);
     int blocks = (int)((n + THREADS - 1) / THREADS);
     if (blocks > 152 * 16)
@@ -627,13 +730,365 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     return cudaGetLastError() == cudaSuccess;
 }
 
+/* `nsteps` steps in one cooperative launch of k_persist (one resident grid:
+ * SMs x resident blocks per SM); false when the launch is refused or a
+ * CUDA error is pending.  A barrier that gave up sets counts[14], which
+ * persist_failed() reports. */
+static bool persist(struct CALModel2D* ca, const double* z, double* h, double eps, double r, long long eps_bits,
+                    int nsteps, cudaStream_t st)
+{
+    State& s = g_state;
+    static int grid = 0;
+    if (!grid) {
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persist, THREADS, 0);
+        grid = sms * per_sm;
+        if (grid <= 0)
+            return false;
+    }
+    K1Params a;
+    K2Params b;
+    a.z = z;
+    a.h = h;
+    a.f = s.f;
+    a.list0 = b.list0 = s.list[0];
+    a.list1 = b.list1 = s.list[1];
+    a.zlist0 = b.zlist0 = s.zlist[0];
+    a.zlist1 = b.zlist1 = s.zlist[1];
+    a.counts = b.counts = s.counts;
+    a.tflag = s.tflag;
+    b.tflag = s.tflag;
+    a.tlist = s.tlist;
+    b.tlist = s.tlist;
+    a.rows = b.rows = ca->rows;
+    a.cols = b.cols = ca->columns;
+    a.toroidal = b.toroidal = ca->T == CAL_SPACE_TOROIDAL;
+    a.tiles_x = b.tiles_x = s.tiles_x;
+    a.n = b.n = s.n;
+    a.eps = eps;
+    a.r = r;
+    b.h = h;
+    b.f = s.f;
+    b.eps_bits = eps_bits;
+    cudaMemsetAsync(s.counts + 12, 0, 3 * sizeof(int), st); /* barrier words and error flag */
+    void* args[] = {&a, &b, &nsteps};
+    return cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(THREADS), args, 0, st) ==
+           cudaSuccess;
+}
+
+/* did the last persistent run give up at a barrier?  (synchronises) */
+static int persist_failed(cudaStream_t st)
+{
+    int flag = 0;
+    if (!g_state.counts)
+        return 0;
+    cudaStreamSynchronize(st);
+    cudaMemcpy(&flag, g_state.counts + 14, sizeof(int), cudaMemcpyDeviceToHost);
+    return flag;
+}
+
 } // namespace sdt2
 
-static bool sdt_use_split()
+/* ======================= 2c. the sparse fused step ======================
+ * One launch per step.  A tile (32 x 16 cells) can only change in a step if
+ * it holds a wet cell or borders one, so the step works on the tiles of
+ * L_t = dilate(W_{t-1}) u dilate(W_t), W_t the tiles holding a wet cell of
+ * h_t and dilate() the 3 x 3 tile neighbourhood (wrapping on a toroidal
+ * grid).  Each listed tile runs the fused step of the single-kernel path
+ * (sdt::fused_tile: z, h staged with a 2-cell ring in shared memory, the
+ * wet cells of tile + ring compacted, EP 1 on them, EP 2 on the tile) from
+ * one h buffer into the other, and marks its neighbourhood for step t+1
+ * when it held a wet cell before or after the step.  Membership is a flag
+ * per tile, double-buffered by step parity: step t reads and clears one
+ * buffer (each tile's flag belongs to one block: tile t to block t mod
+ * grid), marks go to the other.  The h buffers are the substate's two
+ * layers, used alternately; the parity word says which one holds the state.
+ * Invariant: the input buffer of step t holds h_t everywhere, because a tile
+ * left out of L_t was not changed by steps t-1 and t, so both buffers hold
+ * its value.  Resolving (before the host reads h) swaps the layer pointers
+ * when the state sits in the second buffer: a pointer exchange, no copy.
+ * Every launch of the step is identical (parity and ticket in device
+ * memory), so a recorded step replays. */
+namespace sdt3 {
+
+constexpr int TW = 32, TH = 16;
+constexpr int THREADS = sdt::THREADS;
+
+struct Params {
+    const double* __restrict__ z;
+    double* h0;
+    double* h1;
+    int* flags0;
+    int* flags1;
+    int* ctrl; /* [0] parity: which buffer holds the state, [1] block ticket */
+    int rows, cols, toroidal, tiles_x, tiles_y, ntiles;
+    double eps, r;
+    long long eps_bits;
+};
+
+struct State {
+    struct CALModel2D* ca = nullptr;
+    double* h[2] = {nullptr, nullptr};
+    int* flags[2] = {nullptr, nullptr};
+    int* ctrl = nullptr;
+    int tiles_x = 0, tiles_y = 0;
+    long long n = 0;
+    bool primed = false;
+};
+static State g_state;
+
+__global__ void __launch_bounds__(THREADS, 4) k_sparse_step(const __grid_constant__ Params p)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ int s_tiles[THREADS];
+    __shared__ int s_count;
+    const int par = p.ctrl[0];
+    const double* hin = par ? p.h1 : p.h0;
+    double* hout = par ? p.h0 : p.h1;
+    int* cur = par ? p.flags1 : p.flags0;
+    int* nxt = par ? p.flags0 : p.flags1;
+    sdt::Params fp;
+    fp.z = p.z;
+    fp.h = hin;
+    fp.h_next = hout;
+    fp.rows = p.rows;
+    fp.cols = p.cols;
+    fp.toroidal = p.toroidal;
+    fp.eps = p.eps;
+    fp.r = p.r;
+    fp.eps_bits = p.eps_bits;
+    /* this block's tiles: blockIdx.x + k * gridDim.x, THREADS candidates at a time */
+    for (int base = 0; base * (int)gridDim.x < p.ntiles; base += THREADS) {
+        if (threadIdx.x == 0)
+            s_count = 0;
+        __syncthreads();
+        const int t = blockIdx.x + (base + (int)threadIdx.x) * (int)gridDim.x;
+        bool mine = false;
+        if (t < p.ntiles && cur[t]) {
+            cur[t] = 0; /* read and cleared by its owner only */
+            mine = true;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, mine);
+        if (m) {
+            int b = 0;
+            if ((threadIdx.x & 31) == 0)
+                b = atomicAdd(&s_count, __popc(m));
+            b = __shfl_sync(0xffffffffu, b, 0);
+            if (mine)
+                s_tiles[b + __popc(m & ((1u << (threadIdx.x & 31)) - 1u))] = t;
+        }
+        __syncthreads();
+        const int nt = s_count;
+        for (int k = 0; k < nt; k++) {
+            const int tile = s_tiles[k];
+            const int ty = tile / p.tiles_x, tx = tile - ty * p.tiles_x;
+            const int wet = sdt::fused_tile<TW, TH, true>(fp, ty * TH, tx * TW, smem);
+            if (wet && threadIdx.x < 9) {
+                int y = ty + (int)threadIdx.x / 3 - 1, x = tx + (int)threadIdx.x % 3 - 1;
+                bool ok = true;
+                if (p.toroidal) {
+                    y = y < 0 ? y + p.tiles_y : (y >= p.tiles_y ? y - p.tiles_y : y);
+                    x = x < 0 ? x + p.tiles_x : (x >= p.tiles_x ? x - p.tiles_x : x);
+                } else {
+                    ok = (unsigned)y < (unsigned)p.tiles_y && (unsigned)x < (unsigned)p.tiles_x;
+                }
+                if (ok)
+                    nxt[y * p.tiles_x + x] = 1;
+            }
+            __syncthreads(); /* shared memory is reused by the next tile */
+        }
+    }
+    if (threadIdx.x == 0) {
+        /* every block read the parity at its start; the last one to finish
+         * flips it (no block waits for another) */
+        __threadfence();
+        if (atomicAdd(reinterpret_cast<unsigned*>(p.ctrl + 1), 1u) == gridDim.x - 1) {
+            p.ctrl[0] = 1 - par;
+            p.ctrl[1] = 0;
+        }
+    }
+}
+
+/* both buffers = h with -0 made +0 (the first reference step adds 0.0 to
+ * every cell); flags0 = the 3 x 3 tiles around every tile with a wet cell */
+__global__ void k_prime(double* h0, double* h1, long long n, int cols, int tiles_x, int tiles_y, int toroidal,
+                        long long eps_bits, int* flags0)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const double v = sdt::plus_zero(h0[c]);
+        h0[c] = v;
+        h1[c] = v;
+        if (sdt::is_wet(v, eps_bits)) {
+            const int i = (int)(c / cols), j = (int)(c - (long long)(c / cols) * cols);
+            const int ty = i / TH, tx = j / TW;
+            for (int q = 0; q < 9; q++) {
+                int y = ty + q / 3 - 1, x = tx + q % 3 - 1;
+                if (toroidal) {
+                    y = y < 0 ? y + tiles_y : (y >= tiles_y ? y - tiles_y : y);
+                    x = x < 0 ? x + tiles_x : (x >= tiles_x ? x - tiles_x : x);
+                } else if ((unsigned)y >= (unsigned)tiles_y || (unsigned)x >= (unsigned)tiles_x) {
+                    continue;
+                }
+                flags0[y * tiles_x + x] = 1;
+            }
+        }
+    }
+}
+
+static void release()
+{
+    State& s = g_state;
+    cudaFree(s.flags[0]);
+    cudaFree(s.flags[1]);
+    cudaFree(s.ctrl);
+    s = State();
+}
+
+static int step_grid()
+{
+    static int blocks = 0;
+    if (!blocks) {
+        const int smem = (int)sdt::Tile<TW, TH>::smem_bytes;
+        cudaFuncSetAttribute(k_sparse_step, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int per_sm = 1, dev = 0, sms = 152;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sparse_step, THREADS, smem);
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    return blocks;
+}
+
+/* (re)prime from the substate's current layer; its next layer becomes the
+ * second buffer */
+static bool prime(struct CALModel2D* ca, double* cur, double* nxt, long long eps_bits, cudaStream_t st)
+{
+    State& s = g_state;
+    const long long n = (long long)ca->rows * ca->columns;
+    if (s.ca != ca || s.n != n) {
+        release();
+        s.ca = ca;
+        s.n = n;
+        s.tiles_x = (ca->columns + TW - 1) / TW;
+        s.tiles_y = (ca->rows + TH - 1) / TH;
+        const size_t fb = sizeof(int) * (size_t)s.tiles_x * s.tiles_y;
+        if (cudaMalloc(&s.flags[0], fb) != cudaSuccess || cudaMalloc(&s.flags[1], fb) != cudaSuccess ||
+            cudaMalloc(&s.ctrl, 4 * sizeof(int)) != cudaSuccess) {
+            release();
+            return false;
+        }
+    }
+    s.h[0] = cur;
+    s.h[1] = nxt;
+    const size_t fb = sizeof(int) * (size_t)s.tiles_x * s.tiles_y;
+    cudaMemsetAsync(s.flags[0], 0, fb, st);
+    cudaMemsetAsync(s.flags[1], 0, fb, st);
+    cudaMemsetAsync(s.ctrl, 0, 4 * sizeof(int), st);
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16)
+        blocks = 152 * 16;
+    k_prime<<<blocks, 256, 0, st>>>(cur, nxt, n, ca->columns, s.tiles_x, s.tiles_y, ca->T == CAL_SPACE_TOROIDAL,
+                                    eps_bits, s.flags[0]);
+    s.primed = true;
+    return cudaGetLastError() == cudaSuccess;
+}
+
+static bool step(struct CALModel2D* ca, const double* z, double eps, double r, long long eps_bits, cudaStream_t st)
+{
+    State& s = g_state;
+    Params p;
+    p.z = z;
+    p.h0 = s.h[0];
+    p.h1 = s.h[1];
+    p.flags0 = s.flags[0];
+    p.flags1 = s.flags[1];
+    p.ctrl = s.ctrl;
+    p.rows = ca->rows;
+    p.cols = ca->columns;
+    p.toroidal = ca->T == CAL_SPACE_TOROIDAL;
+    p.tiles_x = s.tiles_x;
+    p.tiles_y = s.tiles_y;
+    p.ntiles = s.tiles_x * s.tiles_y;
+    p.eps = eps;
+    p.r = r;
+    p.eps_bits = eps_bits;
+    k_sparse_step<<<step_grid(), THREADS, sdt::Tile<TW, TH>::smem_bytes, st>>>(p);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+} // namespace sdt3
+
+enum SdtKernel { SDT_SPARSE = 0, SDT_SPLIT = 1, SDT_SINGLE = 2 };
+
+/* the plain-mode step: the split step (outflows of the wet cells spread
+ * over the whole GPU, then the update) unless OPENCAL_SDT_KERNEL=sparse |
+ * single selects the sparse fused step (one launch per step; its FP64 work
+ * stays on the SMs that own the flow's tiles) or the dense single kernel */
+static SdtKernel sdt_kernel()
 {
     const char* e = getenv("OPENCAL_SDT_KERNEL");
-    return !(e && !strcmp(e, "single"));
+    if (e && !strcmp(e, "sparse"))
+        return SDT_SPARSE;
+    if (e && !strcmp(e, "single"))
+        return SDT_SINGLE;
+    return SDT_SPLIT;
 }
+
+static bool sdt_use_split() { return sdt_kernel() == SDT_SPLIT; }
+
+/* before the host or another process touches h: if the sparse step left the
+ * state in the substate's next layer, exchange the layer pointers (and the
+ * step's buffer roles) so that current holds it.  Synchronises. */
+static void sciddicaT_sparse_resolve(struct CALModel2D* ca)
+{
+    sdt3::State& s = sdt3::g_state;
+    if (!s.primed || s.ca != ca)
+        return;
+    cudaStream_t st = (cudaStream_t)calGetStream2D(ca);
+    int par = 0;
+    cudaStreamSynchronize(st);
+    cudaMemcpy(&par, s.ctrl, sizeof(int), cudaMemcpyDeviceToHost);
+    if (par) {
+        calSwapSubstate2Dr(ca, Q.h);
+        double* t = s.h[0];
+        s.h[0] = s.h[1];
+        s.h[1] = t;
+        int* f = s.flags[0];
+        s.flags[0] = s.flags[1];
+        s.flags[1] = f;
+        const int zero = 0;
+        cudaMemcpy(s.ctrl, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    }
+}
+
+static void sciddicaT_sparse_invalidate() { sdt3::g_state.primed = false; }
+
+static void sciddicaT_sparse_prepare(struct CALModel2D* ca)
+{
+    if (sdt_kernel() != SDT_SPARSE || (sdt3::g_state.ca == ca && sdt3::g_state.primed))
+        return;
+    long long eps_bits;
+    memcpy(&eps_bits, &P.epsilon, sizeof(double));
+    double* cur = (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0);
+    double* nxt = (double*)calGetDeviceBuffer2Dr(ca, Q.h, 2);
+    sdt3::prime(ca, cur, nxt, eps_bits, (cudaStream_t)calGetStream2D(ca));
+}
+
+static void sciddicaT_sparse_transition(struct CALModel2D* ca)
+{
+    long long eps_bits;
+    memcpy(&eps_bits, &P.epsilon, sizeof(double));
+    if (sdt3::g_state.ca != ca || !sdt3::g_state.primed)
+        sciddicaT_sparse_prepare(ca);
+    const double* z = (const double*)calGetDeviceBuffer2Dr(ca, Q.z, 0);
+    (void)calGetDeviceBuffer2Dr(ca, Q.h, 2); /* both layers change: host copies stale */
+    calMarkCurrentWritten2Dr(ca, Q.h);
+    sdt3::step(ca, z, P.epsilon, P.r, eps_bits, (cudaStream_t)calGetStream2D(ca));
+}
+
+static void sciddicaT_split_prepare_now(struct CALModel2D* ca);
 
 /* the split step as a global transition (h updated in place) */
 static void sciddicaT_split_transition_timed(struct CALModel2D* ca, cudaEvent_t* ev)
@@ -643,28 +1098,59 @@ static void sciddicaT_split_transition_timed(struct CALModel2D* ca, cudaEvent_t*
     cudaStream_t st = (cudaStream_t)calGetStream2D(ca);
     long long eps_bits;
     memcpy(&eps_bits, &P.epsilon, sizeof(double));
-    if (sdt2::g_state.ca != ca || !sdt2::g_state.primed)
-        sdt2::prime(ca, h, eps_bits, st);
+    if (sdt2::g_state.ca != ca || !sdt2::g_state.primed || sdt3::g_state.primed) {
+        sciddicaT_split_prepare_now(ca);
+        h = (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0);
+    }
     sdt2::step(ca, z, h, P.epsilon, P.r, eps_bits, st, ev);
     calMarkCurrentWritten2Dr(ca, Q.h);
 }
 
-static void sciddicaT_split_invalidate() { sdt2::g_state.primed = false; }
-
-/* prime now (eagerly) if the next split step would: keeps the priming out of
- * a step that is being recorded as a graph */
-static void sciddicaT_split_prepare(struct CALModel2D* ca)
+/* the split and sparse steps keep device state derived from h; anything
+ * that changes h behind their back makes them re-prime */
+static void sciddicaT_step_invalidate()
 {
-    if (!sdt_use_split() || (sdt2::g_state.ca == ca && sdt2::g_state.primed))
+    sdt2::g_state.primed = false;
+    sdt3::g_state.primed = false;
+}
+
+/* prime the split step now (eagerly), handing h over from the sparse step
+ * if that ran last */
+static void sciddicaT_split_prepare_now(struct CALModel2D* ca)
+{
+    if (sdt3::g_state.primed && sdt3::g_state.ca == ca) {
+        sciddicaT_sparse_resolve(ca);
+        sciddicaT_sparse_invalidate();
+        sdt2::g_state.primed = false;
+    }
+    if (sdt2::g_state.ca == ca && sdt2::g_state.primed)
         return;
     long long eps_bits;
     memcpy(&eps_bits, &P.epsilon, sizeof(double));
     sdt2::prime(ca, (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0), eps_bits, (cudaStream_t)calGetStream2D(ca));
 }
 
+/* prime the selected plain-mode step now if its next step would: keeps the
+ * priming out of a step that is being recorded as a graph */
+static void sciddicaT_step_prepare(struct CALModel2D* ca)
+{
+    const SdtKernel k = sdt_kernel();
+    if (k == SDT_SPLIT) {
+        sciddicaT_split_prepare_now(ca);
+    } else if (k == SDT_SPARSE) {
+        if (sdt2::g_state.primed && sdt2::g_state.ca == ca) /* h is current after split steps */
+            sdt2::g_state.primed = false;
+        sciddicaT_sparse_prepare(ca);
+    }
+}
+
 /* host side of the fused step: queue the kernel, then exchange the h layers */
 static void sciddicaT_fused_transition(struct CALModel2D* ca)
 {
+    if (sdt_kernel() == SDT_SPARSE) {
+        sciddicaT_sparse_transition(ca);
+        return;
+    }
     if (sdt_use_split()) {
         sciddicaT_split_transition_timed(ca, nullptr);
         return;
@@ -688,8 +1174,8 @@ static void sciddicaT_fused_transition(struct CALModel2D* ca)
 static void sciddicaT_simulation_init_fused(struct CALModel2D* sciddicaT)
 {
     sciddicaT_simulation_init(sciddicaT);
-    sciddicaT_split_invalidate();
-    sciddicaT_split_prepare(sciddicaT);
+    sciddicaT_step_invalidate();
+    sciddicaT_step_prepare(sciddicaT);
 }
 
 /* ======================= driver entry points ============================ */
@@ -714,7 +1200,7 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
     calClearError();
     if (mode == SDT_MODE_FUSED && ac)
         return CAL_ERROR_INVALID_ARGUMENT;
-    sciddicaT_split_invalidate();
+    sciddicaT_step_invalidate();
     struct CALModel2D* ca = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D,
                                        toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT,
                                        ac ? CAL_OPT_ACTIVE_CELLS : CAL_NO_OPT);
@@ -776,6 +1262,7 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
                 break;
     }
     cudaEventRecord(e1, s);
+    sciddicaT_sparse_resolve(ca);
     calRunFinalizeSimulation2D(run);
     calSync2D(ca);
     float t = 0.f;
@@ -825,7 +1312,7 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
     calClearError();
     if (mode == SDT_MODE_FUSED && ac)
         return nullptr;
-    sciddicaT_split_invalidate();
+    sciddicaT_step_invalidate();
     SdtSession* s = (SdtSession*)calloc(1, sizeof(SdtSession));
     s->mode = mode;
     s->ac = ac;
@@ -883,7 +1370,7 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
 extern "C" int cal_sciddicaT_reset(void* handle)
 {
     SdtSession* s = (SdtSession*)handle;
-    sciddicaT_split_invalidate();
+    sciddicaT_step_invalidate();
     cudaStream_t st = (cudaStream_t)calGetStream2D(s->ca);
     for (int k = 0; k < 6; k++)
         for (int l = 0; l < 2; l++)
@@ -903,8 +1390,22 @@ extern "C" int cal_sciddicaT_reset(void* handle)
 extern "C" int cal_sciddicaT_steps(void* handle, int steps, int graph)
 {
     SdtSession* s = (SdtSession*)handle;
+    if (graph == 4) {
+        /* every step in one cooperative launch (split step, plain mode) */
+        if (s->mode != SDT_MODE_FUSED)
+            return CAL_ERROR_INVALID_ARGUMENT;
+        sciddicaT_split_prepare_now(s->ca);
+        long long eps_bits;
+        memcpy(&eps_bits, &P.epsilon, sizeof(double));
+        const double* z = (const double*)calGetDeviceBuffer2Dr(s->ca, Q.z, 0);
+        double* h = (double*)calGetDeviceBuffer2Dr(s->ca, Q.h, 0);
+        if (!sdt2::persist(s->ca, z, h, P.epsilon, P.r, eps_bits, steps, (cudaStream_t)calGetStream2D(s->ca)))
+            return CAL_ERROR_CUDA;
+        calMarkCurrentWritten2Dr(s->ca, Q.h);
+        return calGetLastError();
+    }
     if (s->mode == SDT_MODE_FUSED)
-        sciddicaT_split_prepare(s->ca);
+        sciddicaT_step_prepare(s->ca);
     if (graph == 2) {
         /* one device-driven graph launch for all the steps */
         calRunDeviceSteps2D(s->run, 1, steps);
@@ -929,9 +1430,17 @@ extern "C" int cal_sciddicaT_set_params(void* handle, double p_r, double p_eps)
 
 extern "C" void* cal_sciddicaT_stream(void* handle) { return calGetStream2D(((SdtSession*)handle)->ca); }
 
+/* 1 when a barrier of the last persistent run gave up (the run stopped
+ * early and the state is not that of the requested step); synchronises */
+extern "C" int cal_sciddicaT_persist_failed(void* handle)
+{
+    return sdt2::persist_failed((cudaStream_t)calGetStream2D(((SdtSession*)handle)->ca));
+}
+
 /* host-buffer round trip through the API: load z and h into the host
- * mirrors (uploaded by the next device operation), run, read h back */
-extern "C" int cal_sciddicaT_host_run(void* handle, const double* z_host, const double* h_host, int steps,
+ * mirrors (uploaded by the next device operation), run the program's init
+ * and `steps` steps (graph: as for cal_sciddicaT_steps), read h back */
+extern "C" int cal_sciddicaT_host_run(void* handle, const double* z_host, const double* h_host, int steps, int graph,
                                       double* h_out)
 {
     SdtSession* s = (SdtSession*)handle;
@@ -940,8 +1449,10 @@ extern "C" int cal_sciddicaT_host_run(void* handle, const double* z_host, const 
     memcpy(Q.h->current, h_host, s->bytes);
     memcpy(Q.h->next, h_host, s->bytes);
     calMarkHostDirty2D(s->ca);
-    sciddicaT_split_invalidate();
-    cal_sciddicaT_steps(handle, steps, 0);
+    sciddicaT_step_invalidate();
+    calRunInitSimulation2D(s->run); /* the program's init: z -= h at the source, f = 0 */
+    cal_sciddicaT_steps(handle, steps, graph);
+    sciddicaT_sparse_resolve(s->ca);
     calSyncSubstate2Dr(s->ca, Q.h);
     memcpy(h_out, Q.h->current, s->bytes);
     return calGetLastError();
@@ -995,6 +1506,7 @@ extern "C" int cal_sciddicaT_wet_count(void* handle)
 extern "C" int cal_sciddicaT_read(void* handle, double* h_out)
 {
     SdtSession* s = (SdtSession*)handle;
+    sciddicaT_sparse_resolve(s->ca);
     calSyncSubstate2Dr(s->ca, Q.h);
     memcpy(h_out, Q.h->current, s->bytes);
     return calGetLastError();

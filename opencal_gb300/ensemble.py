@@ -62,6 +62,8 @@ def _lib():
         m.cal_sciddicaT_close.argtypes = [C.c_void_p]
         m.cal_sciddicaT_stream.restype = C.c_void_p
         m.cal_sciddicaT_stream.argtypes = [C.c_void_p]
+        m.cal_sciddicaT_persist_failed.argtypes = [C.c_void_p]
+        m.cal_sciddicaT_host_run.argtypes = [C.c_void_p, _pd, _pd, C.c_int, C.c_int, _pd]
         _bound = True
     return m
 

@@ -6,7 +6,8 @@ import re
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADERS = ["calCommon.h", "cal2D.h", "cal2DRun.h", "cal2DIO.h", "cal2DReduction.h", "cal3D.h", "cal3DRun.h",
+HEADERS = ["calCommon.h", "cal2D.h", "cal2DRun.h", "cal2DIO.h", "cal2DReduction.h", "cal2DUnsafe.h", "cal3D.h",
+           "cal3DRun.h", "cal3DUnsafe.h",
            "cal3DIO.h", "cal3DReduction.h"]
 
 
@@ -15,6 +16,7 @@ def declared_functions(headers=HEADERS):
     for h in headers:
         text = open(os.path.join(ROOT, "include", "opencal", h)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = text.split("#if defined(__CUDACC__)")[0]  # device-side helpers are not exports
         for m in re.finditer(r"^[A-Za-z][\w\s\*]*?\b(cal\w+)\s*\(", text, flags=re.M):
             if not m.group(0).lstrip().startswith(("typedef", "#")):
                 names.add(m.group(1))

@@ -221,3 +221,80 @@ def test_sciddicaT_2048_properties(cal):
     assert not edge.any()
     m0, m1 = h.sum(), a[1].sum()
     assert abs(m1 - m0) <= 1e-12 * m0
+
+
+@pytest.mark.parametrize("rows,cols,tor", [(256, 256, 0), (203, 177, 0), (160, 144, 1)])
+def test_persistent_split_step_bit_exact(cal, orc, rows, cols, tor):
+    """All steps in one cooperative launch (grid barriers between the two
+    phases of each step) == the oracle, alone and interleaved with per-step
+    launches of the same session."""
+    import ctypes as C
+
+    from opencal_gb300 import ensemble as E
+    lib = E._lib()
+    z, h = W.sciddicaT_inputs(rows, cols, seed=17)
+    ref = orc.sciddicaT(z, h, 150, toroidal=tor, ac=False)[1]
+    ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    sess = lib.cal_sciddicaT_open(rows, cols, int(tor), 0, 0.5, 0.001, ptr(z), ptr(h), cal.MODE_FUSED)
+    assert sess
+    try:
+        out = np.empty_like(h)
+        assert lib.cal_sciddicaT_steps(sess, 150, 4) == 0
+        assert lib.cal_sciddicaT_persist_failed(sess) == 0
+        assert lib.cal_sciddicaT_read(sess, ptr(out)) == 0
+        assert_same(out, ref, "h persistent")
+        lib.cal_sciddicaT_reset(sess)
+        for n, mode in ((40, 0), (60, 4), (20, 1), (30, 4)):
+            assert lib.cal_sciddicaT_steps(sess, n, mode) == 0
+        assert lib.cal_sciddicaT_persist_failed(sess) == 0
+        assert lib.cal_sciddicaT_read(sess, ptr(out)) == 0
+        assert_same(out, ref, "h interleaved")
+    finally:
+        lib.cal_sciddicaT_close(sess)
+
+
+def test_host_round_trip_after_device_work(cal, orc):
+    """Host arrays written in full after device work, marked with
+    calMarkHostDirty2D, win over the stale device copies: a session that
+    already ran reloads its inputs from the host, reruns the program's init
+    and steps, and matches the oracle (the bench's end-to-end path)."""
+    import ctypes as C
+
+    from opencal_gb300 import ensemble as E
+    lib = E._lib()
+    z, h = W.sciddicaT_inputs(256, 256, seed=2)
+    ref = orc.sciddicaT(z, h, 60, toroidal=False, ac=False)[1]
+    ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    sess = lib.cal_sciddicaT_open(256, 256, 0, 0, 0.5, 0.001, ptr(z), ptr(h), cal.MODE_FUSED)
+    assert sess
+    try:
+        assert lib.cal_sciddicaT_steps(sess, 100, 0) == 0  # device work first
+        for graph in (0, 1, 4):
+            out = np.empty_like(h)
+            assert lib.cal_sciddicaT_host_run(sess, ptr(z), ptr(h), 60, graph, ptr(out)) == 0
+            assert_same(out, ref, f"h after host round trip, graph {graph}")
+    finally:
+        lib.cal_sciddicaT_close(sess)
+
+
+@pytest.mark.parametrize("kernel", ["sparse", "single"])
+@pytest.mark.parametrize("rows,cols,seed,steps,tor", SDT_CASES[:3])
+def test_sciddicaT_other_step_kernels_bit_exact(cal, orc, monkeypatch, kernel, rows, cols, seed, steps, tor):
+    """the sparse fused step and the dense single kernel, selected with
+    OPENCAL_SDT_KERNEL, against the oracle (the default is the split step)"""
+    monkeypatch.setenv("OPENCAL_SDT_KERNEL", kernel)
+    z, h = W.sciddicaT_inputs(rows, cols, seed=seed)
+    ref = orc.sciddicaT(z, h, steps, toroidal=tor, ac=False)
+    got = cal.sciddicaT(z, h, steps, toroidal=tor, ac=False, mode=cal.MODE_FUSED)
+    assert_same(got[1], ref[1], f"h ({kernel})")
+
+
+@pytest.mark.parametrize("graph", [0, 1, 2])
+def test_sparse_step_graph_and_device_loop(cal, orc, monkeypatch, graph):
+    """the sparse step replayed as a recorded step and inside the device-driven
+    loop: identical to the oracle (parity and ticket live in device memory)"""
+    monkeypatch.setenv("OPENCAL_SDT_KERNEL", "sparse")
+    z, h = W.sciddicaT_inputs(200, 248, seed=21)
+    ref = orc.sciddicaT(z, h, 77, toroidal=False, ac=False)
+    got = cal.sciddicaT(z, h, 77, toroidal=False, ac=False, mode=cal.MODE_FUSED, graph=graph)
+    assert_same(got[1], ref[1], f"h graph={graph}")

@@ -21,7 +21,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # relative tolerance per cell on thickness, temperature, altitude and
 # solidified thickness after the whole run (cells above 1e-9 of the field's
 # maximum); the transcendental functions differ in the last bit
-RTOL = 1e-11
+RTOL = 1e-10
 
 
 @pytest.fixture(scope="module")
