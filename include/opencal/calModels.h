@@ -101,6 +101,13 @@ int cal_nbprobe2d_run(int rows, int cols, int nbhd, int toroidal, int steps, con
 int cal_acprobe_run(int dim, int rows, int cols, int slices, int nbhd, int toroidal, int steps, double thr,
                     const double* v0, double* v_out, long* n_active, int* cells_out, int graph);
 int cal_reduce2d_run(int type, int rows, int cols, const void* data, int op, double* out);
+int cal_unsafe2d_run(int rows, int cols, int nbhd, int toroidal, int steps, const int* v0, const signed char* b0,
+                     const double* w0, int* v_out, signed char* b_out, double* w_out, double* u_out, double* x_out,
+                     int graph);
+/* SCIDDICA-T in the reference's unsafe form
+ * (OpenCAL/examples/cal_sciddicaT-unsafe/source/sciddicaT.c) */
+int cal_sciddicaT_unsafe_run(int rows, int cols, int toroidal, int steps, double p_r, double p_eps, const double* z0,
+                             const double* h0, double* z_out, double* h_out, int graph);
 long cal_test_exact_div(const double* x, const int* c, const double* y, long long n);
 
 #ifdef __cplusplus

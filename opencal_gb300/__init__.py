@@ -191,3 +191,35 @@ def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt
     if timing:
         outs["ms"] = ms.value
     return outs
+
+
+def unsafe2d(v0, b0, w0, steps, *, nbhd=NB_MOORE, toroidal=True, graph=False):
+    """The unsafe-operation probe on the GPU (csrc/models/probes.cu); same
+    contract as oracle.unsafe2d."""
+    v0 = np.ascontiguousarray(v0, dtype=np.int32)
+    b0 = np.ascontiguousarray(b0, dtype=np.int8)
+    w0 = np.ascontiguousarray(w0, dtype=np.float64)
+    rows, cols = v0.shape
+    v, b, w = np.empty_like(v0), np.empty_like(b0), np.empty_like(w0)
+    u, x = np.empty_like(w0), np.empty_like(w0)
+    f = models().cal_unsafe2d_run
+    f.restype = C.c_int
+    f.argtypes = [C.c_int] * 5 + [C.c_void_p] * 8 + [C.c_int]
+    _check(f(rows, cols, int(nbhd), int(toroidal), int(steps), v0.ctypes.data, b0.ctypes.data, w0.ctypes.data,
+             v.ctypes.data, b.ctypes.data, w.ctypes.data, u.ctypes.data, x.ctypes.data, int(bool(graph))),
+           "cal_unsafe2d_run")
+    return v, b, w, u, x
+
+
+def sciddicaT_unsafe(z0, h0, steps, *, toroidal=True, p_r=0.5, p_eps=0.001, graph=False):
+    """SCIDDICA-T in the reference's unsafe form on the GPU; returns (z, h)."""
+    z0 = np.ascontiguousarray(z0, dtype=np.float64)
+    h0 = np.ascontiguousarray(h0, dtype=np.float64)
+    rows, cols = z0.shape
+    z, h = np.empty_like(z0), np.empty_like(h0)
+    f = models().cal_sciddicaT_unsafe_run
+    f.restype = C.c_int
+    f.argtypes = [C.c_int] * 4 + [C.c_double, C.c_double] + [C.c_void_p] * 4 + [C.c_int]
+    _check(f(rows, cols, int(toroidal), int(steps), p_r, p_eps, z0.ctypes.data, h0.ctypes.data, z.ctypes.data,
+             h.ctypes.data, int(bool(graph))), "cal_sciddicaT_unsafe_run")
+    return z, h

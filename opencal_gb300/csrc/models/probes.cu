@@ -10,11 +10,19 @@
  *   acprobe    three processes with SCIDDICA-T's active-cell structure,
  *              2D or 3D (add on outflow, update, remove, steering on next)
  *   life3d     OpenCAL/examples/cal_life3D-glut/source/life3D.cpp:70-83
+ *   unsafe2d   every unsafe operation (cal2DUnsafe.h): integer spreads with
+ *              calAddNext / calAddNextX, and single-writer neighbour stores
+ *              with calSetX / calGetNextX / calSetCurrentX / calInitX
+ *   sciddicaT_unsafe  OpenCAL/examples/cal_sciddicaT-unsafe/source/
+ *              sciddicaT.c:35-107: outflows moved at once into next(h) of
+ *              the cell and the receiver (calAddNext / calAddNextX on the
+ *              GPU: the reference's get-then-set under a lock)
  */
 #include <string.h>
 
 #include "opencal/cal2D.h"
 #include "opencal/cal2DRun.h"
+#include "opencal/cal2DUnsafe.h"
 #include "opencal/cal3D.h"
 #include "opencal/cal3DRun.h"
 
@@ -356,4 +364,165 @@ extern "C" int cal_reduce2d_run(int type, int rows, int cols, const void* data, 
     int err = calGetLastError();
     calFinalize2D(ca);
     return err;
+}
+
+/* ======================= unsafe-operation probe ========================= */
+
+struct UnsafeQ {
+    struct CALSubstate2Di* v;
+    struct CALSubstate2Db* b;
+    struct CALSubstate2Dr* w;
+    struct CALSubstate2Dr* u;
+    struct CALSubstate2Dr* x;
+};
+__managed__ struct UnsafeQ UQ;
+
+CAL_ELEMENTARY_PROCESS_2D(unsafe_ep1)(struct CALModel2D* ca, int i, int j)
+{
+    if (calGet2Di(ca, UQ.v, i, j) > 0) {
+        for (int n = 1; n < ca->sizeof_X; n++)
+            calAddNextX2Di(ca, UQ.v, i, j, n, 1);
+        calAddNext2Di(ca, UQ.v, i, j, -(ca->sizeof_X - 1));
+    }
+    if (calGet2Db(ca, UQ.b, i, j) > 0) {
+        calAddNextX2Db(ca, UQ.b, i, j, 1 + (i + j) % (ca->sizeof_X - 1), 1);
+        calAddNext2Db(ca, UQ.b, i, j, -1);
+    }
+}
+
+CAL_ELEMENTARY_PROCESS_2D(unsafe_ep2)(struct CALModel2D* ca, int i, int j)
+{
+    const double w = calGet2Dr(ca, UQ.w, i, j);
+    calSetX2Dr(ca, UQ.w, i, j, 1, w * 0.5 + calGetNextX2Dr(ca, UQ.w, i, j, 1) * 0.25);
+    calSetCurrentX2Dr(ca, UQ.u, i, j, 2, w);
+    calInitX2Dr(ca, UQ.x, i, j, 3, w + 1.0);
+}
+
+extern "C" int cal_unsafe2d_run(int rows, int cols, int nbhd, int toroidal, int steps, const int* v0,
+                                const signed char* b0, const double* w0, int* v_out, signed char* b_out,
+                                double* w_out, double* u_out, double* x_out, int graph)
+{
+    calClearError();
+    struct CALModel2D* ca = calCADef2D(rows, cols, (enum CALNeighborhood2D)nbhd,
+                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    if (!ca)
+        return calGetLastError();
+    calSetUnsafe2D(ca);
+    struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
+    calAddElementaryProcess2D(ca, unsafe_ep1);
+    if (nbhd == CAL_VON_NEUMANN_NEIGHBORHOOD_2D || nbhd == CAL_MOORE_NEIGHBORHOOD_2D)
+        calAddElementaryProcess2D(ca, unsafe_ep2);
+    UQ.v = calAddSubstate2Di(ca);
+    UQ.b = calAddSubstate2Db(ca);
+    UQ.w = calAddSubstate2Dr(ca);
+    UQ.u = calAddSingleLayerSubstate2Dr(ca);
+    UQ.x = calAddSubstate2Dr(ca);
+    const size_t n = (size_t)rows * cols;
+    memcpy(UQ.v->current, v0, n * sizeof(int));
+    memcpy(UQ.v->next, v0, n * sizeof(int));
+    memcpy(UQ.b->current, b0, n);
+    memcpy(UQ.b->next, b0, n);
+    memcpy(UQ.w->current, w0, n * sizeof(double));
+    memcpy(UQ.w->next, w0, n * sizeof(double));
+    memset(UQ.u->current, 0, n * sizeof(double));
+    memset(UQ.x->current, 0, n * sizeof(double));
+    memset(UQ.x->next, 0, n * sizeof(double));
+    calMarkHostDirty2D(ca);
+    calRunSetGraph2D(run, graph ? CAL_TRUE : CAL_FALSE);
+    if (steps > 0)
+        calRun2D(run);
+    calSync2D(ca);
+    memcpy(v_out, UQ.v->current, n * sizeof(int));
+    memcpy(b_out, UQ.b->current, n);
+    memcpy(w_out, UQ.w->current, n * sizeof(double));
+    memcpy(u_out, UQ.u->current, n * sizeof(double));
+    memcpy(x_out, UQ.x->current, n * sizeof(double));
+    return finish2d(ca, run);
+}
+
+/* ======================= SCIDDICA-T, unsafe form ======================== */
+
+struct SdtuQ {
+    struct CALSubstate2Dr* z;
+    struct CALSubstate2Dr* h;
+    double r, eps;
+};
+__managed__ struct SdtuQ SU;
+
+CAL_ELEMENTARY_PROCESS_2D(sciddicaT_unsafe_transition)(struct CALModel2D* ca, int i, int j)
+{
+    bool out[5] = {false, false, false, false, false};
+    double u[5];
+    const double m = calGet2Dr(ca, SU.h, i, j) - SU.eps;
+    u[0] = calGet2Dr(ca, SU.z, i, j) + SU.eps;
+    for (int n = 1; n < ca->sizeof_X; n++)
+        u[n] = calGetX2Dr(ca, SU.z, i, j, n) + calGetX2Dr(ca, SU.h, i, j, n);
+    double avg;
+    bool again;
+    do {
+        again = false;
+        avg = m;
+        int count = 0;
+        for (int n = 0; n < ca->sizeof_X; n++)
+            if (!out[n]) {
+                avg += u[n];
+                count++;
+            }
+        if (count != 0)
+            avg /= count;
+        for (int n = 0; n < ca->sizeof_X; n++)
+            if (avg <= u[n] && !out[n]) {
+                out[n] = true;
+                again = true;
+            }
+    } while (again);
+    for (int n = 1; n < ca->sizeof_X; n++)
+        if (!out[n]) {
+            const double f = (avg - u[n]) * SU.r;
+            calAddNext2Dr(ca, SU.h, i, j, -f);
+            calAddNextX2Dr(ca, SU.h, i, j, n, f);
+        }
+}
+
+static void sciddicaT_unsafe_init(struct CALModel2D* ca)
+{
+    for (int i = 0; i < ca->rows; i++)
+        for (int j = 0; j < ca->columns; j++) {
+            const double h = calGet2Dr(ca, SU.h, i, j);
+            if (h > 0.0)
+                calSetCurrent2Dr(ca, SU.z, i, j, calGet2Dr(ca, SU.z, i, j) - h);
+        }
+}
+
+extern "C" int cal_sciddicaT_unsafe_run(int rows, int cols, int toroidal, int steps, double p_r, double p_eps,
+                                        const double* z0, const double* h0, double* z_out, double* h_out, int graph)
+{
+    calClearError();
+    struct CALModel2D* ca = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D,
+                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    if (!ca)
+        return calGetLastError();
+    calSetUnsafe2D(ca);
+    struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
+    calAddElementaryProcess2D(ca, sciddicaT_unsafe_transition);
+    SU.z = calAddSubstate2Dr(ca);
+    SU.h = calAddSubstate2Dr(ca);
+    SU.r = p_r;
+    SU.eps = p_eps;
+    const size_t bytes = sizeof(double) * (size_t)rows * cols;
+    memcpy(SU.z->current, z0, bytes);
+    memcpy(SU.z->next, z0, bytes);
+    memcpy(SU.h->current, h0, bytes);
+    memcpy(SU.h->next, h0, bytes);
+    calMarkHostDirty2D(ca);
+    calRunAddInitFunc2D(run, sciddicaT_unsafe_init);
+    calRunSetGraph2D(run, graph ? CAL_TRUE : CAL_FALSE);
+    if (steps > 0)
+        calRun2D(run);
+    else
+        calRunInitSimulation2D(run);
+    calSync2D(ca);
+    memcpy(z_out, SU.z->current, bytes);
+    memcpy(h_out, SU.h->current, bytes);
+    return finish2d(ca, run);
 }

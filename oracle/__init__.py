@@ -177,3 +177,33 @@ def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt
     outs["steps"] = done.value
     outs["cells"] = cells[: n.value].copy() if (ac and want_cells) else np.zeros((0, 2), np.int32)
     return outs
+
+
+def unsafe2d(v0, b0, w0, steps, *, nbhd=NB_MOORE, toroidal=True, kind="serial"):
+    """The unsafe-operation probe (oracle_models.c): returns v, b, w, u, x."""
+    v0 = np.ascontiguousarray(v0, dtype=np.int32)
+    b0 = np.ascontiguousarray(b0, dtype=np.int8)
+    w0 = np.ascontiguousarray(w0, dtype=np.float64)
+    rows, cols = v0.shape
+    v, b, w = np.empty_like(v0), np.empty_like(b0), np.empty_like(w0)
+    u, x = np.empty_like(w0), np.empty_like(w0)
+    f = _fn(kind, "unsafe2d")
+    f.argtypes = [C.c_int] * 5 + [C.c_void_p] * 8
+    if f(rows, cols, int(nbhd), int(toroidal), int(steps), v0.ctypes.data, b0.ctypes.data, w0.ctypes.data,
+         v.ctypes.data, b.ctypes.data, w.ctypes.data, u.ctypes.data, x.ctypes.data):
+        raise RuntimeError("oracle unsafe2d failed")
+    return v, b, w, u, x
+
+
+def sciddicaT_unsafe(z0, h0, steps, *, toroidal=True, p_r=0.5, p_eps=0.001, kind="serial"):
+    """SCIDDICA-T in the reference's unsafe form; returns (z, h)."""
+    z0 = np.ascontiguousarray(z0, dtype=np.float64)
+    h0 = np.ascontiguousarray(h0, dtype=np.float64)
+    rows, cols = z0.shape
+    z, h = np.empty_like(z0), np.empty_like(h0)
+    f = _fn(kind, "sciddicaT_unsafe")
+    f.argtypes = [C.c_int] * 4 + [C.c_double, C.c_double] + [C.c_void_p] * 4
+    if f(rows, cols, int(toroidal), int(steps), p_r, p_eps, z0.ctypes.data, h0.ctypes.data, z.ctypes.data,
+         h.ctypes.data):
+        raise RuntimeError("oracle sciddicaT_unsafe failed")
+    return z, h

@@ -492,3 +492,52 @@ void orc_run_all(orc_run* r)
             break;
     orc_run_finalize(r);
 }
+
+/* unsafe operations, OpenCAL-OMP/source/cal2DUnsafe.c:17-275 and
+ * cal3DUnsafe.c:18-245 (serial: the per-cell locks are no-ops) */
+double orc_get_next(const orc_ca* m, const orc_sub* q, int i, int j, int k)
+{
+    return load_elem(q->nxt, q->type, orc_index(m, i, j, k));
+}
+
+double orc_getx_next(const orc_ca* m, const orc_sub* q, int i, int j, int k, int n)
+{
+    int a, b, c;
+    if (!orc_neighbor(m, i, j, k, n, &a, &b, &c))
+        return 0.0;
+    return load_elem(q->nxt, q->type, orc_index(m, a, b, c));
+}
+
+void orc_setx(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v)
+{
+    int a, b, c;
+    if (orc_neighbor(m, i, j, k, n, &a, &b, &c))
+        orc_set(m, q, a, b, c, v);
+}
+
+void orc_setx_cur(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v)
+{
+    int a, b, c;
+    if (orc_neighbor(m, i, j, k, n, &a, &b, &c))
+        orc_set_cur(m, q, a, b, c, v);
+}
+
+void orc_initx(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v)
+{
+    int a, b, c;
+    if (orc_neighbor(m, i, j, k, n, &a, &b, &c))
+        orc_init_cell(m, q, a, b, c, v);
+}
+
+void orc_add_next(orc_ca* m, orc_sub* q, int i, int j, int k, double v)
+{
+    const long c = orc_index(m, i, j, k);
+    store_elem(q->nxt, q->type, c, load_elem(q->nxt, q->type, c) + v);
+}
+
+void orc_add_nextx(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v)
+{
+    int a, b, c;
+    if (orc_neighbor(m, i, j, k, n, &a, &b, &c))
+        orc_add_next(m, q, a, b, c, v);
+}

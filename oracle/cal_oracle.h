@@ -104,6 +104,15 @@ void orc_set(orc_ca* m, orc_sub* q, int i, int j, int k, double v);
 void orc_set_cur(orc_ca* m, orc_sub* q, int i, int j, int k, double v);
 void orc_init_cell(orc_ca* m, orc_sub* q, int i, int j, int k, double v);
 
+/* unsafe operations (cal2DUnsafe.h / cal3DUnsafe.h) */
+double orc_get_next(const orc_ca* m, const orc_sub* q, int i, int j, int k);
+double orc_getx_next(const orc_ca* m, const orc_sub* q, int i, int j, int k, int n);
+void orc_setx(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v);
+void orc_setx_cur(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v);
+void orc_initx(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v);
+void orc_add_next(orc_ca* m, orc_sub* q, int i, int j, int k, double v);
+void orc_add_nextx(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v);
+
 /* whole-substate operations */
 void orc_init_sub(orc_ca* m, orc_sub* q, double v);      /* calInitSubstate2D* */
 void orc_init_sub_next(orc_ca* m, orc_sub* q, double v); /* calInitSubstateNext2D* */

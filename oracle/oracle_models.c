@@ -407,3 +407,170 @@ int orc_life3d(int rows, int cols, int slices, int nbhd, int toroidal, int steps
     orc_free(m);
     return 0;
 }
+
+/* ======================= unsafe-operation probe ========================= */
+/* A rule of this project exercising every unsafe operation:
+ *   EP 1: a cell with v > 0 adds 1 to v at each neighbour and removes as
+ *         much from itself (calAddNextX2Di / calAddNext2Di); a cell with
+ *         b > 0 moves one unit of b to its neighbour 1 + (i + j) % (nx - 1)
+ *         (calAddNextX2Db / calAddNext2Db).  Integer sums: order-free.
+ *   EP 2 (von Neumann / Moore): each cell writes, as the only writer of the
+ *         target: w.next of its neighbour 1 = 0.5 w + 0.25 w.next there
+ *         (calSetX2Dr, calGetNextX2Dr); u.current (single layer) of its
+ *         neighbour 2 = w (calSetCurrentX2Dr); both layers of x at its
+ *         neighbour 3 = w + 1 (calInitX2Dr).
+ * Implicit update after each process. */
+static struct {
+    orc_sub *v, *b, *w, *u, *x;
+    int ep2;
+} U;
+
+static void unsafe_ep1(orc_ca* m, int i, int j)
+{
+    int n;
+    if (orc_get(m, U.v, i, j, 0) > 0) {
+        for (n = 1; n < m->nx; n++)
+            orc_add_nextx(m, U.v, i, j, 0, n, 1);
+        orc_add_next(m, U.v, i, j, 0, -(m->nx - 1));
+    }
+    if (orc_get(m, U.b, i, j, 0) > 0) {
+        orc_add_nextx(m, U.b, i, j, 0, 1 + (i + j) % (m->nx - 1), 1);
+        orc_add_next(m, U.b, i, j, 0, -1);
+    }
+}
+
+static void unsafe_ep2(orc_ca* m, int i, int j)
+{
+    const double w = orc_get(m, U.w, i, j, 0);
+    orc_setx(m, U.w, i, j, 0, 1, w * 0.5 + orc_getx_next(m, U.w, i, j, 0, 1) * 0.25);
+    orc_setx_cur(m, U.u, i, j, 0, 2, w);
+    orc_initx(m, U.x, i, j, 0, 3, w + 1.0);
+}
+
+int orc_unsafe2d(int rows, int cols, int nbhd, int toroidal, int steps, const int* v0, const signed char* b0,
+                 const double* w0, int* v_out, signed char* b_out, double* w_out, double* u_out, double* x_out)
+{
+    orc_run run;
+    int err;
+    orc_ca* m = orc_def2d(rows, cols, nbhd, toroidal, 0);
+    if (!m)
+        return 1;
+    memset(&U, 0, sizeof(U));
+    U.ep2 = nbhd == ORC_NB_VN || nbhd == ORC_NB_MOORE;
+    orc_add_ep2(m, unsafe_ep1);
+    if (U.ep2)
+        orc_add_ep2(m, unsafe_ep2);
+    U.v = orc_add_sub(m, ORC_I);
+    U.b = orc_add_sub(m, ORC_B);
+    U.w = orc_add_sub(m, ORC_R);
+    U.u = orc_add_single(m, ORC_R);
+    U.x = orc_add_sub(m, ORC_R);
+    orc_load(m, U.v, v0);
+    orc_load(m, U.b, b0);
+    orc_load(m, U.w, w0);
+    orc_init_sub(m, U.u, 0.0);
+    orc_init_sub(m, U.x, 0.0);
+    memset(&run, 0, sizeof(run));
+    run.m = m;
+    run.initial = 1;
+    run.final_ = steps;
+    run.implicit = 1;
+    if (steps > 0)
+        orc_run_all(&run);
+    orc_store(m, U.v, v_out);
+    orc_store(m, U.b, b_out);
+    orc_store(m, U.w, w_out);
+    orc_store(m, U.u, u_out);
+    orc_store(m, U.x, x_out);
+    err = m->error;
+    orc_free(m);
+    return err;
+}
+
+/* ======================= SCIDDICA-T, unsafe form ======================== */
+/* OpenCAL/examples/cal_sciddicaT-unsafe/source/sciddicaT.c:35-107 (plain):
+ * one process computes the outflows and moves them at once,
+ * next(h) -= f at the cell, next(h) += f at the receiver, through
+ * calGetNext / calSet / calGetNextX / calSetX. */
+static struct {
+    orc_sub *z, *h;
+    double r, eps;
+} SU;
+
+static void sdtu_transition(orc_ca* m, int i, int j)
+{
+    unsigned char out[5] = {0, 0, 0, 0, 0};
+    double u[5], mass, avg, f;
+    int n, again, count;
+    mass = orc_get(m, SU.h, i, j, 0) - SU.eps;
+    u[0] = orc_get(m, SU.z, i, j, 0) + SU.eps;
+    for (n = 1; n < m->nx; n++)
+        u[n] = orc_getx(m, SU.z, i, j, 0, n) + orc_getx(m, SU.h, i, j, 0, n);
+    do {
+        again = 0;
+        avg = mass;
+        count = 0;
+        for (n = 0; n < m->nx; n++)
+            if (!out[n]) {
+                avg += u[n];
+                count++;
+            }
+        if (count != 0)
+            avg /= count;
+        for (n = 0; n < m->nx; n++)
+            if (avg <= u[n] && !out[n]) {
+                out[n] = 1;
+                again = 1;
+            }
+    } while (again);
+    for (n = 1; n < m->nx; n++)
+        if (!out[n]) {
+            f = (avg - u[n]) * SU.r;
+            orc_set(m, SU.h, i, j, 0, orc_get_next(m, SU.h, i, j, 0) - f);
+            orc_setx(m, SU.h, i, j, 0, n, orc_getx_next(m, SU.h, i, j, 0, n) + f);
+        }
+}
+
+static void sdtu_init(orc_ca* m)
+{
+    int i, j;
+    for (i = 0; i < m->rows; i++)
+        for (j = 0; j < m->cols; j++) {
+            const double h = orc_get(m, SU.h, i, j, 0);
+            if (h > 0.0)
+                orc_set_cur(m, SU.z, i, j, 0, orc_get(m, SU.z, i, j, 0) - h);
+        }
+}
+
+int orc_sciddicaT_unsafe(int rows, int cols, int toroidal, int steps, double p_r, double p_eps, const double* z0,
+                         const double* h0, double* z_out, double* h_out)
+{
+    orc_run run;
+    int err;
+    orc_ca* m = orc_def2d(rows, cols, ORC_NB_VN, toroidal, 0);
+    if (!m)
+        return 1;
+    memset(&SU, 0, sizeof(SU));
+    SU.r = p_r;
+    SU.eps = p_eps;
+    orc_add_ep2(m, sdtu_transition);
+    SU.z = orc_add_sub(m, ORC_R);
+    SU.h = orc_add_sub(m, ORC_R);
+    orc_load(m, SU.z, z0);
+    orc_load(m, SU.h, h0);
+    memset(&run, 0, sizeof(run));
+    run.m = m;
+    run.initial = 1;
+    run.final_ = steps;
+    run.implicit = 1;
+    run.init = sdtu_init;
+    if (steps > 0)
+        orc_run_all(&run);
+    else
+        orc_run_init(&run);
+    orc_store(m, SU.z, z_out);
+    orc_store(m, SU.h, h_out);
+    err = m->error;
+    orc_free(m);
+    return err;
+}

@@ -12,6 +12,7 @@
 #include <cal2D.h>
 #include <cal2DBuffer.h>
 #include <cal2DRun.h>
+#include <cal2DUnsafe.h>
 #include <cal3D.h>
 #include <cal3DBuffer.h>
 #include <cal3DRun.h>
@@ -467,5 +468,156 @@ int ref_life3d(int rows, int cols, int slices, int nbhd, int toroidal, int steps
         s_out[c] = (unsigned char)L3->current[c];
     calRunFinalize3D(run);
     finalize3d(m);
+    return 0;
+}
+
+/* ======================= unsafe-operation probe ======================= */
+
+static struct {
+    struct CALSubstate2Di* v;
+    struct CALSubstate2Db* b;
+    struct CALSubstate2Dr *w, *u, *x;
+} UR;
+
+static void ur_ep1(struct CALModel2D* m, int i, int j)
+{
+    int n;
+    if (calGet2Di(m, UR.v, i, j) > 0) {
+        for (n = 1; n < m->sizeof_X; n++)
+            calAddNextX2Di(m, UR.v, i, j, n, 1);
+        calAddNext2Di(m, UR.v, i, j, -(m->sizeof_X - 1));
+    }
+    if (calGet2Db(m, UR.b, i, j) > 0) {
+        calAddNextX2Db(m, UR.b, i, j, 1 + (i + j) % (m->sizeof_X - 1), 1);
+        calAddNext2Db(m, UR.b, i, j, -1);
+    }
+}
+
+static void ur_ep2(struct CALModel2D* m, int i, int j)
+{
+    const double w = calGet2Dr(m, UR.w, i, j);
+    calSetX2Dr(m, UR.w, i, j, 1, w * 0.5 + calGetNextX2Dr(m, UR.w, i, j, 1) * 0.25);
+    calSetCurrentX2Dr(m, UR.u, i, j, 2, w);
+    calInitX2Dr(m, UR.x, i, j, 3, w + 1.0);
+}
+
+int ref_unsafe2d(int rows, int cols, int nbhd, int toroidal, int steps, const int* v0, const signed char* b0,
+                 const double* w0, int* v_out, signed char* b_out, double* w_out, double* u_out, double* x_out)
+{
+    struct CALModel2D* m = calCADef2D(rows, cols, (enum CALNeighborhood2D)nbhd,
+                                      toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    struct CALRun2D* run = calRunDef2D(m, 1, steps, CAL_UPDATE_IMPLICIT);
+    const size_t n = (size_t)rows * cols;
+    calSetUnsafe2D(m);
+    calAddElementaryProcess2D(m, ur_ep1);
+    if (nbhd == CAL_VON_NEUMANN_NEIGHBORHOOD_2D || nbhd == CAL_MOORE_NEIGHBORHOOD_2D)
+        calAddElementaryProcess2D(m, ur_ep2);
+    UR.v = calAddSubstate2Di(m);
+    UR.b = calAddSubstate2Db(m);
+    UR.w = calAddSubstate2Dr(m);
+    UR.u = calAddSingleLayerSubstate2Dr(m);
+    UR.x = calAddSubstate2Dr(m);
+    memcpy(UR.v->current, v0, n * sizeof(int));
+    memcpy(UR.v->next, v0, n * sizeof(int));
+    memcpy(UR.b->current, b0, n);
+    memcpy(UR.b->next, b0, n);
+    memcpy(UR.w->current, w0, n * sizeof(double));
+    memcpy(UR.w->next, w0, n * sizeof(double));
+    memset(UR.u->current, 0, n * sizeof(double));
+    memset(UR.x->current, 0, n * sizeof(double));
+    memset(UR.x->next, 0, n * sizeof(double));
+    if (steps > 0)
+        calRun2D(run);
+    memcpy(v_out, UR.v->current, n * sizeof(int));
+    memcpy(b_out, UR.b->current, n);
+    memcpy(w_out, UR.w->current, n * sizeof(double));
+    memcpy(u_out, UR.u->current, n * sizeof(double));
+    memcpy(x_out, UR.x->current, n * sizeof(double));
+    calRunFinalize2D(run);
+    finalize2d(m);
+    return 0;
+}
+
+/* ======================= SCIDDICA-T, unsafe form ====================== */
+/* the transition of OpenCAL/examples/cal_sciddicaT-unsafe/source/sciddicaT.c,
+ * written against the reference's API as there */
+
+static struct {
+    struct CALSubstate2Dr *z, *h;
+    double r, eps;
+} SUR;
+
+static void sur_transition(struct CALModel2D* m, int i, int j)
+{
+    CALbyte out[5] = {CAL_FALSE, CAL_FALSE, CAL_FALSE, CAL_FALSE, CAL_FALSE};
+    CALbyte again;
+    CALint count, n;
+    CALreal avg, mass, u[5], f;
+    mass = calGet2Dr(m, SUR.h, i, j) - SUR.eps;
+    u[0] = calGet2Dr(m, SUR.z, i, j) + SUR.eps;
+    for (n = 1; n < m->sizeof_X; n++)
+        u[n] = calGetX2Dr(m, SUR.z, i, j, n) + calGetX2Dr(m, SUR.h, i, j, n);
+    do {
+        again = CAL_FALSE;
+        avg = mass;
+        count = 0;
+        for (n = 0; n < m->sizeof_X; n++)
+            if (!out[n]) {
+                avg += u[n];
+                count++;
+            }
+        if (count != 0)
+            avg /= count;
+        for (n = 0; n < m->sizeof_X; n++)
+            if ((avg <= u[n]) && (!out[n])) {
+                out[n] = CAL_TRUE;
+                again = CAL_TRUE;
+            }
+    } while (again);
+    for (n = 1; n < m->sizeof_X; n++)
+        if (!out[n]) {
+            f = (avg - u[n]) * SUR.r;
+            calSet2Dr(m, SUR.h, i, j, calGetNext2Dr(m, SUR.h, i, j) - f);
+            calSetX2Dr(m, SUR.h, i, j, n, calGetNextX2Dr(m, SUR.h, i, j, n) + f);
+        }
+}
+
+static void sur_init(struct CALModel2D* m)
+{
+    int i, j;
+    for (i = 0; i < m->rows; i++)
+        for (j = 0; j < m->columns; j++) {
+            const CALreal h = calGet2Dr(m, SUR.h, i, j);
+            if (h > 0.0)
+                calSetCurrent2Dr(m, SUR.z, i, j, calGet2Dr(m, SUR.z, i, j) - h);
+        }
+}
+
+int ref_sciddicaT_unsafe(int rows, int cols, int toroidal, int steps, double p_r, double p_eps, const double* z0,
+                         const double* h0, double* z_out, double* h_out)
+{
+    struct CALModel2D* m = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D,
+                                      toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    struct CALRun2D* run = calRunDef2D(m, 1, steps, CAL_UPDATE_IMPLICIT);
+    const size_t bytes = sizeof(double) * (size_t)rows * cols;
+    calSetUnsafe2D(m);
+    calAddElementaryProcess2D(m, sur_transition);
+    SUR.z = calAddSubstate2Dr(m);
+    SUR.h = calAddSubstate2Dr(m);
+    SUR.r = p_r;
+    SUR.eps = p_eps;
+    memcpy(SUR.z->current, z0, bytes);
+    memcpy(SUR.z->next, z0, bytes);
+    memcpy(SUR.h->current, h0, bytes);
+    memcpy(SUR.h->next, h0, bytes);
+    calRunAddInitFunc2D(run, sur_init);
+    if (steps > 0)
+        calRun2D(run);
+    else
+        calRunInitSimulation2D(run);
+    memcpy(z_out, SUR.z->current, bytes);
+    memcpy(h_out, SUR.h->current, bytes);
+    calRunFinalize2D(run);
+    finalize2d(m);
     return 0;
 }

@@ -136,3 +136,20 @@ def test_oracle_sciara_matches_reference_fixtures(oracle_lib, idx):
     assert out["steps"] == int(fx[p + "steps"][0])
     if ac:
         assert len(out["cells"]) == int(fx[p + "active"][0])
+
+
+@pytest.mark.parametrize("nb", [1, 2, 3, 4])
+def test_oracle_unsafe_probe_matches_reference_fixtures(oracle_lib, nb):
+    """the unsafe-operation probe (calAddNext*, calSetX*, calGetNextX*,
+    calSetCurrentX*, calInitX*) against the reference library's run"""
+    fx = np.load(os.path.join(GOLDEN, "unsafe_cases.npz"))
+    p = f"probe{nb}_"
+    got = oracle_lib.unsafe2d(fx[p + "v0"], fx[p + "b0"], fx[p + "w0"], 12, nbhd=nb, toroidal=True)
+    for name, a in zip(("v", "b", "w", "u", "x"), got):
+        assert a.tobytes() == fx[p + name].tobytes(), name
+
+
+def test_oracle_sciddicaT_unsafe_matches_reference_fixture(oracle_lib):
+    fx = np.load(os.path.join(GOLDEN, "unsafe_cases.npz"))
+    z, h = oracle_lib.sciddicaT_unsafe(fx["sdtu_z0"], fx["sdtu_h0"], 50, toroidal=True)
+    assert z.tobytes() == fx["sdtu_z"].tobytes() and h.tobytes() == fx["sdtu_h"].tobytes()
