@@ -89,6 +89,20 @@ int cal_sciara_run(int rows, int cols, int ac, int max_steps, const double* para
                    const double* st0, double* z_out, double* slt_out, double* st_out, double* msl_out,
                    int* steps_done, long* n_active, int* cells_out, int graph, double* ms);
 
+/* SCIARA-fv2 scenarios by the split step (vents, flows of the lava cells,
+ * update of the flagged tiles); one scenario or many in the same launches.
+ * dims: 2B ints; z0 / slt0 / st0: the scenarios' grids back to back (slt0,
+ * st0 may be NULL); vents: scenario index and (x, y) per vent, in each
+ * scenario's vent order; rates: nvents x nphases.  list_fraction: capacity
+ * of the lava list as a fraction of all cells. */
+void* cal_sciara_batch_create(int B, const int* dims, const double* z0, const double* slt0, const double* st0,
+                              const double* params, int nvents, const int* vent_inst, const int* vent_xy,
+                              unsigned emission_time, int nphases, const double* rates, double list_fraction);
+void cal_sciara_batch_destroy(void* batch);
+int cal_sciara_batch_run(void* batch, int max_steps, int* steps_done, float* ms);
+int cal_sciara_batch_read(void* batch, double* z, double* slt, double* st, double* msl);
+int cal_sciara_batch_lava_cells(void* batch);
+
 /* ---- Game of Life (OpenCAL-OMP/examples/calomp_life) and the 3D rule ---- */
 int cal_life2d_run(int rows, int cols, int toroidal, int as_int, int steps, const unsigned char* s0,
                    unsigned char* s_out, int mode, int block, int graph, double* ms);

@@ -223,3 +223,59 @@ def sciddicaT_unsafe(z0, h0, steps, *, toroidal=True, p_r=0.5, p_eps=0.001, grap
     _check(f(rows, cols, int(toroidal), int(steps), p_r, p_eps, z0.ctypes.data, h0.ctypes.data, z.ctypes.data,
              h.ctypes.data, int(bool(graph))), "cal_sciddicaT_unsafe_run")
     return z, h
+
+
+def sciara_batch(scenarios, steps=0, *, params=None, list_fraction=0.0, timing=False):
+    """SCIARA-fv2 scenarios advanced together by the split step
+    (csrc/models/sciara_batch.cu).  scenarios: [(z0, vents, rates)] sharing
+    the emission schedule (emission_time given as scenarios' common
+    `emission_time` in each tuple's 4th element).  Returns a list of dicts
+    (z, slt, st, msl) plus the steps run (and the device milliseconds with
+    timing=True)."""
+    from .workloads import SCIARA_PARAMS
+    B = len(scenarios)
+    ets = {int(s[3]) for s in scenarios}
+    nph = {len(s[2][0]) for s in scenarios}
+    if len(ets) != 1 or len(nph) != 1:
+        raise ValueError("scenarios must share the emission schedule (emission_time, number of phases)")
+    et, nphases = ets.pop(), nph.pop()
+    dims = np.ascontiguousarray(np.array([np.shape(s[0]) for s in scenarios], dtype=np.int32).reshape(-1))
+    z = np.ascontiguousarray(np.concatenate([np.asarray(s[0], np.float64).ravel() for s in scenarios]))
+    vinst, vxy, rates = [], [], []
+    for b, s in enumerate(scenarios):
+        for v, r in zip(s[1], s[2]):
+            vinst.append(b)
+            vxy.extend(v)
+            rates.extend(r)
+    vinst = np.ascontiguousarray(np.array(vinst, dtype=np.int32))
+    vxy = np.ascontiguousarray(np.array(vxy, dtype=np.int32))
+    rates = np.ascontiguousarray(np.array(rates, dtype=np.float64))
+    p = np.ascontiguousarray(params if params is not None else SCIARA_PARAMS, dtype=np.float64)
+    m = models()
+    m.cal_sciara_batch_create.restype = C.c_void_p
+    m.cal_sciara_batch_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_int, C.c_void_p, C.c_void_p, C.c_uint, C.c_int, C.c_void_p,
+                                          C.c_double]
+    m.cal_sciara_batch_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+    m.cal_sciara_batch_read.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+    m.cal_sciara_batch_destroy.argtypes = [C.c_void_p]
+    h = m.cal_sciara_batch_create(B, dims.ctypes.data, z.ctypes.data, None, None, p.ctypes.data, len(vinst),
+                                  vinst.ctypes.data, vxy.ctypes.data, et, nphases, rates.ctypes.data,
+                                  float(list_fraction))
+    if not h:
+        raise CALError("cal_sciara_batch_create failed (bad argument or out of device memory)")
+    try:
+        done = C.c_int(0)
+        ms = C.c_float(0.0)
+        _check(m.cal_sciara_batch_run(h, int(steps), C.byref(done), C.byref(ms)), "cal_sciara_batch_run")
+        outs = {k: np.empty_like(z) for k in ("z", "slt", "st", "msl")}
+        _check(m.cal_sciara_batch_read(h, outs["z"].ctypes.data, outs["slt"].ctypes.data, outs["st"].ctypes.data,
+                                       outs["msl"].ctypes.data), "cal_sciara_batch_read")
+    finally:
+        m.cal_sciara_batch_destroy(h)
+    res, pos = [], 0
+    for s in scenarios:
+        r, c = np.shape(s[0])
+        res.append({k: outs[k][pos:pos + r * c].reshape(r, c).copy() for k in outs})
+        pos += r * c
+    return (res, done.value, ms.value) if timing else (res, done.value)

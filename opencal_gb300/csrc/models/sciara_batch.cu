@@ -1,0 +1,716 @@
+/*
+ * sciara_batch.cu -- SCIARA-fv2 scenarios (one grid or many, each with its
+ * own morphology, vents and emission rates) advanced by a split step:
+ *
+ *   K0 (vents): updateVentsEmission (OpenCAL-OMP/examples/calomp_sciara-fv2/
+ *      source/Sciara.cpp:3-16): thickness += rate / Pac * Pclock at each
+ *      emitting vent (the last vent listed for a cell wins, as the EP's
+ *      get-current-then-set does), temperature = PTvent; a vent cell that
+ *      had no lava joins the lava list.
+ *   K1 (flows): empiricalFlows + outflowsMin (Sciara.cpp:18-105) for every
+ *      cell of the lava list (Slt > 0), one thread each, spread over the
+ *      whole GPU -- the pow / atan / cos and the minimisation are the step's
+ *      FP64 work.  The eight outflows of list entry k, and each outflow
+ *      times the cell's temperature (the product width_update forms at the
+ *      receiver, same operands), go to compact slot k; a per-cell (epoch,
+ *      slot) map makes them addressable by cell.  The tiles of the cell and
+ *      of every receiver are flagged (epoch stamps) and listed once.
+ *   K2 (update): width_update, updateTemperature and the steering's border
+ *      reset (Sciara.cpp:106-169, 185-193) on every cell of the flagged
+ *      tiles, in place: each cell reads only its own state and the compact
+ *      outflows; it joins the next lava list if it still holds lava.
+ *      Every lava cell's tile is flagged, so cooling and solidification
+ *      reach all of them; a cell outside the flagged tiles has no lava and
+ *      no inflow and is unchanged.
+ *
+ * Arithmetic is the reference's, operation by operation (--fmad=false);
+ * pow, atan, cos are CUDA's, as in the device-process program
+ * (sciara.cu), which this step reproduces bit for bit.  All scenarios share
+ * the physical parameters and the emission schedule's length, so they run
+ * the same number of steps (the reference stops when the elapsed time
+ * reaches the emission's end).
+ *
+ * Layout: scenarios packed back to back (offsets padded to 32 cells); per
+ * cell Sz, Slt, St, Msl (FP64), Mb (byte), the (epoch, slot) map (8 B) and
+ * two list entries (8 B): ~49 B per cell; outflows only per lava cell
+ * (128 B per list slot, capacity chosen at creation).
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+namespace sci2 {
+
+constexpr int T = 256;
+constexpr int K1T = 64;
+constexpr int TW = 32, TH = 16; /* K2 tile; 2 cells per thread */
+constexpr int K2_BLOCKS = 152 * 4;
+constexpr int MAX_INST = 1024;
+
+struct Phys {
+    double Pclock, Pc, Pac, PTsol, PTvent, a, b, c, d, Pcool, Prho, Pepsilon, Psigma, Pcv, rad2;
+};
+
+struct Inst {
+    int rows, cols;
+    long long off;
+    int tiles_x, tiles_y, tile0, pad;
+};
+
+/* counts[]: [0..1] lava list lengths, [4] list parity, [5] K2 ticket,
+ * [6] epoch, [7] flagged tiles, [8] overflow flag */
+struct Dev {
+    const Inst* inst;
+    const long long* offs;
+    int B;
+    double* Sz;
+    double* Slt;
+    double* St;
+    double* Msl;
+    const unsigned char* Mb;
+    double* fc;   /* 16 doubles per list slot: f[8], f * St[8] */
+    int2* map;    /* per cell: (epoch, slot) */
+    int* list0;
+    int* list1;
+    int* counts;
+    int* tflag;
+    int* tlist;
+    long long ncells;
+    int capacity;
+    int nvents;
+    const int* vent_cell;  /* packed cell index of each vent */
+    const int* vent_first; /* B + 1: vents of instance b are [vent_first[b], vent_first[b + 1]) */
+    const double* rates;   /* nvents x nphases */
+    int nphases;
+    unsigned emission_time;
+    Phys ph;
+};
+
+static __device__ __forceinline__ int locate(const long long* s_offs, int B, long long c)
+{
+    int lo = 0, hi = B - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_offs[mid] <= c)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+/* Moore neighbour k = 0..8 (OpenCAL order: centre, N, W, E, S, NW, SW, SE, NE) */
+__device__ __constant__ int kMi[9] = {0, -1, 0, 0, 1, -1, 1, 1, -1};
+__device__ __constant__ int kMj[9] = {0, 0, -1, 1, 0, -1, -1, 1, 1};
+
+static __device__ __forceinline__ bool nbr(const Inst& I, int i, int j, int k, long long* c)
+{
+    const int a = i + kMi[k], b = j + kMj[k];
+    if ((unsigned)a >= (unsigned)I.rows || (unsigned)b >= (unsigned)I.cols)
+        return false; /* flat boundary */
+    *c = I.off + (long long)a * I.cols + b;
+    return true;
+}
+
+static __device__ __forceinline__ void append(int* list, int* count, int capacity, int* overflow, int value)
+{
+    const int pos = atomicAdd(count, 1);
+    if (pos < capacity)
+        list[pos] = value;
+    else
+        atomicExch(overflow, 1);
+}
+
+static __device__ __forceinline__ void flag_tile(const Dev& d, int t, int epoch)
+{
+    if (d.tflag[t] != epoch && atomicExch(d.tflag + t, epoch) != epoch)
+        d.tlist[atomicAdd(d.counts + 7, 1)] = t;
+}
+
+/* K0: vent emission, one thread per scenario; empties the next lava list */
+__global__ void k_vents(const __grid_constant__ Dev d, double elapsed)
+{
+    const int par = d.counts[4];
+    int* list = par ? d.list1 : d.list0;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        d.counts[1 - par] = 0;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.B)
+        return;
+    const unsigned phase = (unsigned)(elapsed / d.emission_time);
+    const int v0 = d.vent_first[b], v1 = d.vent_first[b + 1];
+    for (int v = v0; v < v1; v++) {
+        const int c = d.vent_cell[v];
+        /* the process reads the current thickness: every vent of a cell adds
+         * to the value before this step's emission */
+        double orig = d.Slt[c];
+        for (int w = v0; w < v; w++)
+            if (d.vent_cell[w] == c) {
+                orig = -1.0; /* handled with the first vent of this cell */
+                break;
+            }
+        if (orig < 0.0)
+            continue;
+        bool emitted_any = false;
+        for (int w = v; w < v1; w++) {
+            if (d.vent_cell[w] != c)
+                continue;
+            const double emitted = phase >= (unsigned)d.nphases ? 0.0
+                                                                : d.rates[(size_t)w * d.nphases + phase] / d.ph.Pac * d.ph.Pclock;
+            if (emitted > 0) {
+                d.Slt[c] = orig + emitted;
+                d.St[c] = d.ph.PTvent;
+                emitted_any = true;
+            }
+        }
+        if (emitted_any && !(orig > 0))
+            append(list, d.counts + par, d.capacity, d.counts + 8, c);
+    }
+}
+
+static __device__ __forceinline__ double power_law(double k1, double k2, double t) { return pow(10.0, k1 + k2 * t); }
+
+/* K1: outflows of every lava cell into compact slots; tiles flagged */
+__global__ void __launch_bounds__(K1T) k_flows(const __grid_constant__ Dev d)
+{
+    __shared__ long long s_offs[MAX_INST + 1];
+    for (int k = threadIdx.x; k <= d.B; k += blockDim.x)
+        s_offs[k] = d.offs[k];
+    __syncthreads();
+    const int par = d.counts[4];
+    const int epoch = d.counts[6];
+    const int* list = par ? d.list1 : d.list0;
+    const int n = min(d.counts[par], d.capacity);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int c = list[k];
+        const Inst I = d.inst[locate(s_offs, d.B, c)];
+        const long long lc = c - I.off;
+        const int i = (int)(lc / I.cols), j = (int)(lc - (long long)i * I.cols);
+        double f[9], z[9], h[9], H[9], theta[9];
+        bool in_set[9];
+        const double t = d.St[c];
+        const double w = d.ph.Pc;
+        const double Pr = power_law(d.ph.a, d.ph.b, t);
+        const double hc = power_law(d.ph.c, d.ph.d, t);
+        const double sz0 = d.Sz[c];
+        bool inside[9];
+        long long cn[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            inside[q] = nbr(I, i, j, q, &cn[q]);
+            h[q] = inside[q] ? d.Slt[cn[q]] : 0.0;
+            const double sz = inside[q] ? d.Sz[cn[q]] : 0.0;
+            H[q] = f[q] = theta[q] = 0;
+            z[q] = q < 5 ? sz : sz0 - (sz0 - sz) / d.ph.rad2;
+        }
+        H[0] = z[0];
+        in_set[0] = true;
+#pragma unroll
+        for (int q = 1; q < 9; q++)
+            if (z[0] + h[0] > z[q] + h[q]) {
+                H[q] = z[q] + h[q];
+                theta[q] = atan(((z[0] + h[0]) - (z[q] + h[q])) / w);
+                in_set[q] = true;
+            } else {
+                in_set[q] = false;
+            }
+        bool loop;
+        double avg;
+        do {
+            loop = false;
+            avg = h[0];
+            int counter = 0;
+#pragma unroll
+            for (int q = 0; q < 9; q++)
+                if (in_set[q]) {
+                    avg += H[q];
+                    counter++;
+                }
+            if (counter != 0)
+                avg = avg / (double)counter;
+#pragma unroll
+            for (int q = 0; q < 9; q++)
+                if (in_set[q] && avg <= H[q]) {
+                    in_set[q] = false;
+                    loop = true;
+                }
+        } while (loop);
+        double* slot = d.fc + (size_t)k * 16;
+        bool any = false;
+#pragma unroll
+        for (int q = 1; q < 9; q++) {
+            double fq = 0.0;
+            if (in_set[q] && h[0] > hc * cos(theta[q]))
+                fq = Pr * (avg - H[q]);
+            /* empiricalFlows stores only positive outflows; the rest stay 0 */
+            if (!(fq > 0))
+                fq = 0.0;
+            slot[q - 1] = fq;
+            slot[8 + q - 1] = fq * t;
+            if (fq > 0 && inside[q]) {
+                any = true;
+                const long long rc = cn[q] - I.off;
+                const int ri = (int)(rc / I.cols), rj = (int)(rc - (long long)ri * I.cols);
+                flag_tile(d, I.tile0 + (ri / TH) * I.tiles_x + rj / TW, epoch);
+            }
+        }
+        (void)any;
+        d.map[c] = make_int2(epoch, k);
+        flag_tile(d, I.tile0 + (i / TH) * I.tiles_x + j / TW, epoch); /* cooling reaches every lava cell */
+    }
+}
+
+/* width_update, updateTemperature and the border reset of one cell, in place */
+static __device__ __forceinline__ bool update_cell(const Dev& d, const Inst& I, int i, int j, int epoch)
+{
+    const int opp[8] = {3, 2, 1, 0, 6, 7, 4, 5};
+    const long long x = I.off + (long long)i * I.cols + j;
+    const double initial_h = d.Slt[x];
+    const double initial_t = d.St[x];
+    const int2 me = d.map[x];
+    const double* mine = me.x == epoch ? d.fc + (size_t)me.y * 16 : nullptr;
+    double ht = 0, in_sum = 0, out_sum = 0;
+#pragma unroll
+    for (int n = 1; n < 9; n++) {
+        long long cn;
+        double in_flow = 0.0, in_ft = 0.0;
+        if (nbr(I, i, j, n, &cn)) {
+            const int2 m = d.map[cn];
+            if (m.x == epoch) {
+                const double* s = d.fc + (size_t)m.y * 16;
+                in_flow = s[opp[n - 1]];
+                in_ft = s[8 + opp[n - 1]];
+            }
+        }
+        const double out_flow = mine ? mine[n - 1] : 0.0;
+        ht += in_ft; /* inFlow * neigh_t, formed at the source with the same operands */
+        in_sum += in_flow;
+        out_sum += out_flow;
+    }
+    double h_next = initial_h;
+    double t_next = initial_t;
+    h_next += in_sum - out_sum;
+    if (in_sum > 0 || out_sum > 0) {
+        const double residual = initial_h - out_sum;
+        t_next = (residual * initial_t + ht) / (residual + in_sum);
+    }
+    double sh = h_next, st = t_next;
+    const bool border = d.Mb[x] != 0;
+    if (sh > 0 && !border) {
+        const double sz = d.Sz[x];
+        if (sh != 0) {
+            const double nT = st;
+            const double aus = 1.0 + (3 * pow(nT, 3.0) * d.ph.Pepsilon * d.ph.Psigma * d.ph.Pclock * d.ph.Pcool) /
+                                         (d.ph.Prho * d.ph.Pcv * sh * d.ph.Pac);
+            st = nT / pow(aus, 1.0 / 3.0);
+        }
+        if (st <= d.ph.PTsol && sh > 0) {
+            d.Sz[x] = sz + sh;
+            d.Msl[x] = d.Msl[x] + sh;
+            sh = 0;
+            st = d.ph.PTsol;
+        }
+    }
+    if (border) {
+        sh = 0;
+        st = 0;
+    }
+    d.Slt[x] = sh;
+    d.St[x] = st;
+    return sh > 0;
+}
+
+/* K2: every cell of the flagged tiles; the next lava list */
+__global__ void __launch_bounds__(T) k_update(const __grid_constant__ Dev d)
+{
+    const int par = d.counts[4];
+    const int epoch = d.counts[6];
+    const int ntiles = d.counts[7];
+    int* next = par ? d.list0 : d.list1;
+    int* ncount = d.counts + (1 - par);
+    for (int item = blockIdx.x; item < ntiles; item += gridDim.x) {
+        const int t = d.tlist[item];
+        /* the tile's instance: largest b with tile0 <= t */
+        int lo = 0, hi = d.B - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (d.inst[mid].tile0 <= t)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const Inst I = d.inst[lo];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        for (int q = threadIdx.x; q < TW * TH; q += T) {
+            const int i = ty * TH + q / TW, j = tx * TW + q % TW;
+            bool lava = false;
+            long long x = 0;
+            if (i < I.rows && j < I.cols) {
+                lava = update_cell(d, I, i, j, epoch);
+                x = I.off + (long long)i * I.cols + j;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, lava);
+            if (m) {
+                const int lane = threadIdx.x & 31;
+                int base = 0;
+                if (lane == 0)
+                    base = atomicAdd(ncount, __popc(m));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (lava) {
+                    const int pos = base + __popc(m & ((1u << lane) - 1u));
+                    if (pos < d.capacity)
+                        next[pos] = (int)x;
+                    else
+                        atomicExch(d.counts + 8, 1);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(reinterpret_cast<unsigned*>(d.counts + 5), 1u) == gridDim.x - 1) {
+            d.counts[4] = 1 - par;
+            d.counts[5] = 0;
+            d.counts[6] = epoch + 1;
+            d.counts[7] = 0;
+        }
+    }
+}
+
+/* MakeBorder (Sciara.cpp:206-250) on the device, the border reset of the
+ * initial state, and the first lava list */
+__global__ void k_prime(const __grid_constant__ Dev d)
+{
+    __shared__ long long s_offs[MAX_INST + 1];
+    for (int k = threadIdx.x; k <= d.B; k += blockDim.x)
+        s_offs[k] = d.offs[k];
+    __syncthreads();
+    unsigned char* Mb = const_cast<unsigned char*>(d.Mb);
+    for (long long c0 = (long long)blockIdx.x * blockDim.x; c0 < d.ncells; c0 += (long long)gridDim.x * blockDim.x) {
+        const long long c = c0 + threadIdx.x;
+        bool lava = false;
+        if (c < d.ncells) {
+            const Inst I = d.inst[locate(s_offs, d.B, c)];
+            const long long lc = c - I.off;
+            if (lc < (long long)I.rows * I.cols) {
+                const int i = (int)(lc / I.cols), j = (int)(lc - (long long)i * I.cols);
+                bool border = false;
+                if (d.Sz[c] >= 0) {
+                    if (i == 0 || i == I.rows - 1 || j == 0 || j == I.cols - 1) {
+                        border = true;
+                    } else {
+                        for (int k = 1; k < 9 && !border; k++) {
+                            long long cn;
+                            if (nbr(I, i, j, k, &cn) && d.Sz[cn] < 0)
+                                border = true;
+                        }
+                    }
+                }
+                Mb[c] = border ? 1 : 0;
+                if (border) {
+                    d.Slt[c] = 0;
+                    d.St[c] = 0;
+                }
+                lava = !border && d.Slt[c] > 0;
+            } else {
+                Mb[c] = 0;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, lava);
+        if (m) {
+            const int lane = threadIdx.x & 31;
+            int base = 0;
+            if (lane == 0)
+                base = atomicAdd(d.counts + 0, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (lava) {
+                const int pos = base + __popc(m & ((1u << lane) - 1u));
+                if (pos < d.capacity)
+                    d.list0[pos] = (int)c;
+                else
+                    atomicExch(d.counts + 8, 1);
+            }
+        }
+    }
+}
+
+struct Batch {
+    int B = 0, nvents = 0, nphases = 0;
+    unsigned emission_time = 0;
+    long long N = 0;
+    int ntiles = 0, capacity = 0;
+    std::vector<Inst> inst;
+    std::vector<long long> offs;
+    Dev d;
+    double effusion_duration = 0;
+    cudaStream_t st = nullptr;
+    void* allocs[32] = {};
+    int nalloc = 0;
+    bool primed = false;
+};
+
+template <typename T>
+static bool dalloc(Batch& bt, T** p, size_t bytes)
+{
+    if (bt.nalloc >= (int)(sizeof(bt.allocs) / sizeof(bt.allocs[0])) || cudaMalloc(p, bytes) != cudaSuccess)
+        return false;
+    bt.allocs[bt.nalloc++] = *p;
+    return true;
+}
+
+static void destroy(Batch* bt)
+{
+    if (bt->st)
+        cudaStreamSynchronize(bt->st);
+    for (int k = 0; k < bt->nalloc; k++)
+        cudaFree(bt->allocs[k]);
+    if (bt->st)
+        cudaStreamDestroy(bt->st);
+    delete bt;
+}
+
+} // namespace sci2
+
+using sci2::Batch;
+
+/* Create B SCIARA-fv2 scenarios.  dims: 2B ints (rows, cols); z0, slt0, st0:
+ * the scenarios' morphology, initial thickness and temperature back to back
+ * (unpadded, row-major; slt0 / st0 may be NULL for zero); params: the 13
+ * physical parameters (Pclock, PTsol, PTvent, Pr(Tsol), Pr(Tvent),
+ * Phc(Tsol), Phc(Tvent), Pcool, Prho, Pepsilon, Psigma, Pcv, Pc); vents:
+ * vent_inst[v] = scenario, vent_xy[2v..2v+1] = (x, y), in each scenario's
+ * vent order; rates: nvents x nphases m^3/s, each phase emission_time
+ * seconds.  list_fraction: lava-list capacity as a fraction of all cells,
+ * or <= 0 for the default (all cells up to 16M cells, an eighth beyond); a
+ * run that needs more reports CAL_ERROR_OUT_OF_MEMORY. */
+extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z0, const double* slt0,
+                                         const double* st0, const double* params, int nvents, const int* vent_inst,
+                                         const int* vent_xy, unsigned emission_time, int nphases, const double* rates,
+                                         double list_fraction)
+{
+    if (B <= 0 || B > sci2::MAX_INST || nvents < 0 || nphases < 0 || emission_time == 0)
+        return nullptr;
+    Batch* bt = new Batch();
+    bt->B = B;
+    bt->nvents = nvents;
+    bt->nphases = nphases;
+    bt->emission_time = emission_time;
+    bt->offs.assign(B + 1, 0);
+    int tiles = 0;
+    for (int b = 0; b < B; b++) {
+        sci2::Inst I;
+        memset(&I, 0, sizeof(I));
+        I.rows = dims[2 * b];
+        I.cols = dims[2 * b + 1];
+        if (I.rows < 3 || I.cols < 3) {
+            delete bt;
+            return nullptr;
+        }
+        I.off = bt->offs[b];
+        I.tiles_x = (I.cols + sci2::TW - 1) / sci2::TW;
+        I.tiles_y = (I.rows + sci2::TH - 1) / sci2::TH;
+        I.tile0 = tiles;
+        tiles += I.tiles_x * I.tiles_y;
+        bt->inst.push_back(I);
+        const long long n = (long long)I.rows * I.cols;
+        bt->offs[b + 1] = bt->offs[b] + (n + 31) / 32 * 32;
+    }
+    bt->N = bt->offs[B];
+    bt->ntiles = tiles;
+    /* default (list_fraction <= 0): every cell up to 16M cells, an eighth
+     * beyond (lava covers a small part of a large volcano) */
+    if (list_fraction <= 0)
+        list_fraction = bt->N <= (16LL << 20) ? 1.0 : 0.125;
+    const double frac = list_fraction > 1.0 ? 1.0 : list_fraction;
+    bt->capacity = (int)std::min<long long>(bt->N, std::max<long long>(1024, (long long)(frac * bt->N)));
+    /* vents: packed cell indices, grouped by scenario in the given order */
+    std::vector<int> vcell(nvents), vfirst(B + 1, 0);
+    std::vector<double> vrates((size_t)nvents * nphases);
+    {
+        std::vector<int> order(nvents);
+        for (int v = 0; v < nvents; v++)
+            order[v] = v;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return vent_inst[a] < vent_inst[b]; });
+        for (int k = 0; k < nvents; k++) {
+            const int v = order[k];
+            const int b = vent_inst[v];
+            const int x = vent_xy[2 * v], y = vent_xy[2 * v + 1];
+            if (b < 0 || b >= B || x < 0 || y < 0 || x >= bt->inst[b].cols || y >= bt->inst[b].rows) {
+                delete bt;
+                return nullptr;
+            }
+            vcell[k] = (int)(bt->inst[b].off + (long long)y * bt->inst[b].cols + x);
+            vfirst[b + 1]++;
+            for (int p = 0; p < nphases; p++)
+                vrates[(size_t)k * nphases + p] = rates[(size_t)v * nphases + p];
+        }
+        for (int b = 0; b < B; b++)
+            vfirst[b + 1] += vfirst[b];
+    }
+    sci2::Dev& d = bt->d;
+    memset(&d, 0, sizeof(d));
+    d.B = B;
+    d.ncells = bt->N;
+    d.capacity = bt->capacity;
+    d.nvents = nvents;
+    d.nphases = nphases;
+    d.emission_time = emission_time;
+    d.ph.Pclock = params[0];
+    d.ph.PTsol = params[1];
+    d.ph.PTvent = params[2];
+    const double Pr_Tsol = params[3], Pr_Tvent = params[4], Phc_Tsol = params[5], Phc_Tvent = params[6];
+    d.ph.Pcool = params[7];
+    d.ph.Prho = params[8];
+    d.ph.Pepsilon = params[9];
+    d.ph.Psigma = params[10];
+    d.ph.Pcv = params[11];
+    d.ph.Pc = params[12];
+    d.ph.Pac = d.ph.Pc * d.ph.Pc;
+    d.ph.rad2 = sqrt(2.0);
+    /* evaluatePowerLawParams (Sciara.cpp:199-204), C library log10 */
+    d.ph.b = (log10(Pr_Tvent) - log10(Pr_Tsol)) / (d.ph.PTvent - d.ph.PTsol);
+    d.ph.a = log10(Pr_Tsol) - d.ph.b * (d.ph.PTsol);
+    d.ph.d = (log10(Phc_Tvent) - log10(Phc_Tsol)) / (d.ph.PTvent - d.ph.PTsol);
+    d.ph.c = log10(Phc_Tsol) - d.ph.d * (d.ph.PTsol);
+    bt->effusion_duration = (double)emission_time * nphases;
+
+    const size_t nb = (size_t)bt->N * sizeof(double);
+    bool ok = cudaStreamCreateWithFlags(&bt->st, cudaStreamNonBlocking) == cudaSuccess &&
+              sci2::dalloc(*bt, (sci2::Inst**)&d.inst, sizeof(sci2::Inst) * B) &&
+              sci2::dalloc(*bt, (long long**)&d.offs, sizeof(long long) * (B + 1)) &&
+              sci2::dalloc(*bt, &d.Sz, nb) && sci2::dalloc(*bt, &d.Slt, nb) && sci2::dalloc(*bt, &d.St, nb) &&
+              sci2::dalloc(*bt, &d.Msl, nb) && sci2::dalloc(*bt, (unsigned char**)&d.Mb, (size_t)bt->N) &&
+              sci2::dalloc(*bt, &d.map, sizeof(int2) * (size_t)bt->N) &&
+              sci2::dalloc(*bt, &d.list0, sizeof(int) * (size_t)bt->capacity) &&
+              sci2::dalloc(*bt, &d.list1, sizeof(int) * (size_t)bt->capacity) &&
+              sci2::dalloc(*bt, &d.fc, sizeof(double) * 16 * (size_t)bt->capacity) &&
+              sci2::dalloc(*bt, &d.counts, 16 * sizeof(int)) &&
+              sci2::dalloc(*bt, &d.tflag, sizeof(int) * (size_t)tiles) &&
+              sci2::dalloc(*bt, &d.tlist, sizeof(int) * (size_t)tiles) &&
+              sci2::dalloc(*bt, (int**)&d.vent_cell, sizeof(int) * std::max(1, nvents)) &&
+              sci2::dalloc(*bt, (int**)&d.vent_first, sizeof(int) * (B + 1)) &&
+              sci2::dalloc(*bt, (double**)&d.rates, sizeof(double) * std::max<size_t>(1, vrates.size()));
+    if (!ok) {
+        fprintf(stderr, "opencal-gb300: cal_sciara_batch_create: out of device memory\n");
+        sci2::destroy(bt);
+        return nullptr;
+    }
+    cudaMemcpy((void*)d.inst, bt->inst.data(), sizeof(sci2::Inst) * B, cudaMemcpyHostToDevice);
+    cudaMemcpy((void*)d.offs, bt->offs.data(), sizeof(long long) * (B + 1), cudaMemcpyHostToDevice);
+    if (nvents) {
+        cudaMemcpy((void*)d.vent_cell, vcell.data(), sizeof(int) * nvents, cudaMemcpyHostToDevice);
+        cudaMemcpy((void*)d.rates, vrates.data(), sizeof(double) * vrates.size(), cudaMemcpyHostToDevice);
+    }
+    cudaMemcpy((void*)d.vent_first, vfirst.data(), sizeof(int) * (B + 1), cudaMemcpyHostToDevice);
+    cudaMemset(d.Sz, 0, nb);
+    cudaMemset(d.Slt, 0, nb);
+    cudaMemset(d.St, 0, nb);
+    cudaMemset(d.Msl, 0, nb);
+    size_t src = 0;
+    for (int b = 0; b < B; b++) {
+        const size_t n = (size_t)bt->inst[b].rows * bt->inst[b].cols;
+        const long long o = bt->offs[b];
+        cudaMemcpy(d.Sz + o, z0 + src, n * sizeof(double), cudaMemcpyHostToDevice);
+        if (slt0)
+            cudaMemcpy(d.Slt + o, slt0 + src, n * sizeof(double), cudaMemcpyHostToDevice);
+        if (st0)
+            cudaMemcpy(d.St + o, st0 + src, n * sizeof(double), cudaMemcpyHostToDevice);
+        src += n;
+    }
+    if (cudaGetLastError() != cudaSuccess) {
+        sci2::destroy(bt);
+        return nullptr;
+    }
+    return bt;
+}
+
+extern "C" void cal_sciara_batch_destroy(void* handle)
+{
+    if (handle)
+        sci2::destroy((Batch*)handle);
+}
+
+/* Run every scenario from its initial state until the emission ends (or
+ * max_steps > 0 steps); the state stays on the device for
+ * cal_sciara_batch_read.  steps_done: steps run; ms: device time of the step
+ * loop.  0, or a CALError code (CAL_ERROR_OUT_OF_MEMORY = list overflow). */
+extern "C" int cal_sciara_batch_run(void* handle, int max_steps, int* steps_done, float* ms)
+{
+    Batch* bt = (Batch*)handle;
+    sci2::Dev& d = bt->d;
+    cudaStream_t st = bt->st;
+    cudaMemsetAsync(d.counts, 0, 16 * sizeof(int), st);
+    cudaMemsetAsync(d.map, 0, sizeof(int2) * (size_t)bt->N, st);
+    cudaMemsetAsync(d.tflag, 0, sizeof(int) * (size_t)bt->ntiles, st);
+    const int one = 1;
+    cudaMemcpyAsync(d.counts + 6, &one, sizeof(int), cudaMemcpyHostToDevice, st);
+    int blocks = (int)std::min<long long>((bt->N + sci2::T - 1) / sci2::T, 152 * 16);
+    sci2::k_prime<<<blocks, sci2::T, 0, st>>>(d);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    double elapsed = 0.0;
+    int done = 0;
+    /* the run loop of calRun2D with the stop condition of Sciara.cpp:177-183 */
+    for (int step = 1; max_steps <= 0 || step <= max_steps; step++) {
+        sci2::k_vents<<<(bt->B + 63) / 64, 64, 0, st>>>(d, elapsed);
+        sci2::k_flows<<<152 * 32, sci2::K1T, 0, st>>>(d);
+        sci2::k_update<<<sci2::K2_BLOCKS, sci2::T, 0, st>>>(d);
+        done++;
+        elapsed += d.ph.Pclock;
+        if (elapsed >= bt->effusion_duration)
+            break;
+    }
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms)
+        *ms = t;
+    if (steps_done)
+        *steps_done = done;
+    int overflow = 0;
+    cudaMemcpy(&overflow, d.counts + 8, sizeof(int), cudaMemcpyDeviceToHost);
+    if (cudaGetLastError() != cudaSuccess)
+        return 3; /* CAL_ERROR_CUDA */
+    return overflow ? 2 /* CAL_ERROR_OUT_OF_MEMORY */ : 0;
+}
+
+/* the scenarios' final Sz, Slt, St, Msl, back to back and unpadded (any may be NULL) */
+extern "C" int cal_sciara_batch_read(void* handle, double* z, double* slt, double* st, double* msl)
+{
+    Batch* bt = (Batch*)handle;
+    cudaStreamSynchronize(bt->st);
+    double* outs[4] = {z, slt, st, msl};
+    const double* src[4] = {bt->d.Sz, bt->d.Slt, bt->d.St, bt->d.Msl};
+    for (int q = 0; q < 4; q++) {
+        if (!outs[q])
+            continue;
+        size_t pos = 0;
+        for (int b = 0; b < bt->B; b++) {
+            const size_t n = (size_t)bt->inst[b].rows * bt->inst[b].cols;
+            cudaMemcpy(outs[q] + pos, src[q] + bt->offs[b], n * sizeof(double), cudaMemcpyDeviceToHost);
+            pos += n;
+        }
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : 3;
+}
+
+/* lava cells of the last step (all scenarios) */
+extern "C" int cal_sciara_batch_lava_cells(void* handle)
+{
+    Batch* bt = (Batch*)handle;
+    int c[5] = {0, 0, 0, 0, 0};
+    cudaStreamSynchronize(bt->st);
+    cudaMemcpy(c, bt->d.counts, sizeof(c), cudaMemcpyDeviceToHost);
+    return c[c[4] & 1];
+}

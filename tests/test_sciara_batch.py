@@ -1,0 +1,72 @@
+"""SCIARA-fv2 split step (csrc/models/sciara_batch.cu): one scenario
+reproduces the device-process program (csrc/models/sciara.cu, the
+reference's elementary processes behind the C API) bit for bit -- both use
+CUDA's pow / atan / cos with the reference's operation order -- and a batch
+of scenarios with uneven grids reproduces each scenario run alone.  Against
+the oracle (the C library's transcendental functions) the tolerance of
+test_sciara.py applies.  A lava list too small for the flow is reported as
+an error, not overrun."""
+import numpy as np
+import pytest
+
+from opencal_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10  # as tests/test_sciara.py: pow / atan / cos of CUDA vs the C library
+
+
+@pytest.fixture(scope="module")
+def cal():
+    import opencal_gb300 as cal
+    cal.build()
+    return cal
+
+
+def _scenario(rows, cols, seed, et):
+    z, vents, rates = W.sciara_inputs(rows, cols, seed=seed)
+    return (z, vents, rates, et)
+
+
+def _same(a, b, what):
+    for k in ("z", "slt", "st", "msl"):
+        assert a[k].tobytes() == b[k].tobytes(), f"{what}: {k} max diff {np.abs(a[k] - b[k]).max()}"
+
+
+@pytest.mark.parametrize("rows,cols,seed", [(64, 80, 5), (96, 128, 6), (77, 101, 7)])
+def test_split_step_equals_device_processes(cal, rows, cols, seed):
+    sc = _scenario(rows, cols, seed, 600)
+    ref = cal.sciara(sc[0], sc[1], sc[2], 600, 0, ac=False)
+    (got,), steps = cal.sciara_batch([sc])
+    assert steps == ref["steps"]
+    _same(got, ref, f"{rows}x{cols}")
+
+
+def test_batch_equals_scenarios_alone(cal):
+    scs = [_scenario(64, 80, 11, 900), _scenario(120, 90, 12, 900), _scenario(97, 130, 13, 900)]
+    got, steps = cal.sciara_batch(scs)
+    for k, sc in enumerate(scs):
+        ref = cal.sciara(sc[0], sc[1], sc[2], 900, 0, ac=True)
+        assert steps == ref["steps"]
+        _same(got[k], ref, f"scenario {k}")
+
+
+def test_batch_close_to_oracle(cal):
+    import oracle
+    oracle.build()
+    sc = _scenario(96, 112, 21, 1200)
+    ref = oracle.sciara(sc[0], sc[1], sc[2], 1200, 0, ac=False)
+    (got,), steps = cal.sciara_batch([sc])
+    assert steps == ref["steps"]
+    for k in ("slt", "st", "z", "msl"):
+        r, g = ref[k], got[k]
+        scale = max(np.abs(r).max(), 1e-300)
+        mask = (np.abs(r) > 1e-9 * scale) | (np.abs(g) > 1e-9 * scale)
+        rel = np.abs(g - r)[mask] / np.maximum(np.abs(r)[mask], 1e-300)
+        assert (rel.max() if rel.size else 0.0) <= RTOL, k
+
+
+def test_list_overflow_is_an_error(cal):
+    sc = _scenario(160, 160, 31, 3600)
+    with pytest.raises(cal.CALError):
+        cal.sciara_batch([sc], 200, list_fraction=1e-9)
