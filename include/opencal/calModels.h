@@ -101,6 +101,12 @@ void* cal_sciara_batch_create(int B, const int* dims, const double* z0, const do
 void cal_sciara_batch_destroy(void* batch);
 int cal_sciara_batch_run(void* batch, int max_steps, int* steps_done, float* ms);
 int cal_sciara_batch_read(void* batch, double* z, double* slt, double* st, double* msl);
+/* L_b = sum (Slt_T - target)^2 per scenario and dL/drate of every vent and
+ * phase (caller's vent order), by the adjoint with the forward's decisions
+ * (elimination sets, shear test, solidification, border) frozen; undo tape
+ * of tape_slots tiles (0: default) */
+int cal_sciara_batch_loss_grad(void* batch, const double* target, int max_steps, double* loss, double* grad,
+                               int* steps_done, long long tape_slots, float* ms);
 int cal_sciara_batch_lava_cells(void* batch);
 
 /* ---- Game of Life (OpenCAL-OMP/examples/calomp_life) and the 3D rule ---- */

@@ -225,13 +225,7 @@ def sciddicaT_unsafe(z0, h0, steps, *, toroidal=True, p_r=0.5, p_eps=0.001, grap
     return z, h
 
 
-def sciara_batch(scenarios, steps=0, *, params=None, list_fraction=0.0, timing=False):
-    """SCIARA-fv2 scenarios advanced together by the split step
-    (csrc/models/sciara_batch.cu).  scenarios: [(z0, vents, rates)] sharing
-    the emission schedule (emission_time given as scenarios' common
-    `emission_time` in each tuple's 4th element).  Returns a list of dicts
-    (z, slt, st, msl) plus the steps run (and the device milliseconds with
-    timing=True)."""
+def _sciara_batch_handle(scenarios, params, list_fraction):
     from .workloads import SCIARA_PARAMS
     B = len(scenarios)
     ets = {int(s[3]) for s in scenarios}
@@ -259,11 +253,32 @@ def sciara_batch(scenarios, steps=0, *, params=None, list_fraction=0.0, timing=F
     m.cal_sciara_batch_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     m.cal_sciara_batch_read.argtypes = [C.c_void_p] + [C.c_void_p] * 4
     m.cal_sciara_batch_destroy.argtypes = [C.c_void_p]
+    m.cal_sciara_batch_loss_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                             C.POINTER(C.c_int), C.c_longlong, C.POINTER(C.c_float)]
     h = m.cal_sciara_batch_create(B, dims.ctypes.data, z.ctypes.data, None, None, p.ctypes.data, len(vinst),
                                   vinst.ctypes.data, vxy.ctypes.data, et, nphases, rates.ctypes.data,
                                   float(list_fraction))
     if not h:
         raise CALError("cal_sciara_batch_create failed (bad argument or out of device memory)")
+    return m, h, z, len(vinst), nphases
+
+
+def _sciara_unpack(scenarios, flat):
+    res, pos = [], 0
+    for s in scenarios:
+        r, c = np.shape(s[0])
+        res.append(flat[pos:pos + r * c].reshape(r, c).copy())
+        pos += r * c
+    return res
+
+
+def sciara_batch(scenarios, steps=0, *, params=None, list_fraction=0.0, timing=False):
+    """SCIARA-fv2 scenarios advanced together by the split step
+    (csrc/models/sciara_batch.cu).  scenarios: [(z0, vents, rates,
+    emission_time)], sharing the emission schedule.  Returns a list of dicts
+    (z, slt, st, msl) and the steps run (and the device milliseconds with
+    timing=True)."""
+    m, h, z, _, _ = _sciara_batch_handle(scenarios, params, list_fraction)
     try:
         done = C.c_int(0)
         ms = C.c_float(0.0)
@@ -273,9 +288,32 @@ def sciara_batch(scenarios, steps=0, *, params=None, list_fraction=0.0, timing=F
                                        outs["msl"].ctypes.data), "cal_sciara_batch_read")
     finally:
         m.cal_sciara_batch_destroy(h)
-    res, pos = [], 0
-    for s in scenarios:
-        r, c = np.shape(s[0])
-        res.append({k: outs[k][pos:pos + r * c].reshape(r, c).copy() for k in outs})
-        pos += r * c
+    per = {k: _sciara_unpack(scenarios, v) for k, v in outs.items()}
+    res = [{k: per[k][b] for k in per} for b in range(len(scenarios))]
     return (res, done.value, ms.value) if timing else (res, done.value)
+
+
+def sciara_loss_grad(scenarios, targets, steps=0, *, params=None, list_fraction=0.0, tape_slots=0, timing=False):
+    """L_b = sum (Slt_T - target_b)^2 for every scenario and dL/drate for
+    every vent and phase (csrc/models/sciara_batch.cu, adjoint with the
+    forward's decisions frozen).  Returns (loss[B], [grad_b (nvents_b x
+    nphases)]) (and the device milliseconds with timing=True)."""
+    m, h, z, nv, nphases = _sciara_batch_handle(scenarios, params, list_fraction)
+    try:
+        tgt = np.ascontiguousarray(np.concatenate([np.asarray(t, np.float64).ravel() for t in targets]))
+        assert tgt.size == z.size
+        loss = np.zeros(len(scenarios))
+        grad = np.zeros(max(1, nv * nphases))
+        done = C.c_int(0)
+        ms = C.c_float(0.0)
+        _check(m.cal_sciara_batch_loss_grad(h, tgt.ctypes.data, int(steps), loss.ctypes.data, grad.ctypes.data,
+                                            C.byref(done), int(tape_slots), C.byref(ms)),
+               "cal_sciara_batch_loss_grad")
+    finally:
+        m.cal_sciara_batch_destroy(h)
+    grads, pos = [], 0
+    for s in scenarios:
+        k = len(s[1])
+        grads.append(grad[pos * nphases:(pos + k) * nphases].reshape(k, nphases).copy())
+        pos += k
+    return (loss, grads, ms.value) if timing else (loss, grads)

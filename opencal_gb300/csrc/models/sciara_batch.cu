@@ -31,9 +31,10 @@
  * reaches the emission's end).
  *
  * Layout: scenarios packed back to back (offsets padded to 32 cells); per
- * cell Sz, Slt, St, Msl (FP64), Mb (byte), the (epoch, slot) map (8 B) and
- * two list entries (8 B): ~49 B per cell; outflows only per lava cell
- * (128 B per list slot, capacity chosen at creation).
+ * cell Sz, Slt, St, Msl (FP64), Mb (byte), the (epoch, slot) map (8 B),
+ * two list entries (8 B) and a copy of the initial Sz, Slt, St (every run
+ * starts from it): ~73 B per cell; outflows only per lava cell (128 B per
+ * list slot, capacity chosen at creation).
  */
 #include <math.h>
 #include <stdio.h>
@@ -131,8 +132,11 @@ static __device__ __forceinline__ void flag_tile(const Dev& d, int t, int epoch)
         d.tlist[atomicAdd(d.counts + 7, 1)] = t;
 }
 
-/* K0: vent emission, one thread per scenario; empties the next lava list */
-__global__ void k_vents(const __grid_constant__ Dev d, double elapsed)
+/* K0: vent emission, one thread per scenario; empties the next lava list.
+ * With a vent tape (one record of 3 doubles per vent and step) the first
+ * vent of each cell records the cell's thickness and temperature before the
+ * emission and which vent's emission took effect. */
+__global__ void k_vents(const __grid_constant__ Dev d, double elapsed, double* vtape)
 {
     const int par = d.counts[4];
     int* list = par ? d.list1 : d.list0;
@@ -147,15 +151,20 @@ __global__ void k_vents(const __grid_constant__ Dev d, double elapsed)
         const int c = d.vent_cell[v];
         /* the process reads the current thickness: every vent of a cell adds
          * to the value before this step's emission */
-        double orig = d.Slt[c];
+        bool first = true;
         for (int w = v0; w < v; w++)
             if (d.vent_cell[w] == c) {
-                orig = -1.0; /* handled with the first vent of this cell */
+                first = false; /* handled with the first vent of this cell */
                 break;
             }
-        if (orig < 0.0)
+        if (!first) {
+            if (vtape)
+                vtape[3 * v + 2] = -2.0;
             continue;
-        bool emitted_any = false;
+        }
+        const double orig = d.Slt[c];
+        const double orig_t = d.St[c];
+        int eff = -1;
         for (int w = v; w < v1; w++) {
             if (d.vent_cell[w] != c)
                 continue;
@@ -164,15 +173,105 @@ __global__ void k_vents(const __grid_constant__ Dev d, double elapsed)
             if (emitted > 0) {
                 d.Slt[c] = orig + emitted;
                 d.St[c] = d.ph.PTvent;
-                emitted_any = true;
+                eff = w;
             }
         }
-        if (emitted_any && !(orig > 0))
+        if (vtape) {
+            vtape[3 * v] = orig;
+            vtape[3 * v + 1] = orig_t;
+            vtape[3 * v + 2] = (double)eff;
+        }
+        if (eff >= 0 && !(orig > 0))
             append(list, d.counts + par, d.capacity, d.counts + 8, c);
     }
 }
 
 static __device__ __forceinline__ double power_law(double k1, double k2, double t) { return pow(10.0, k1 + k2 * t); }
+
+/* outflowsMin (Sciara.cpp:23-90) at lava cell c, with what its adjoint needs */
+struct Flow {
+    double h[9], z[9], H[9], f[9];
+    double avg, Pr, t;
+    long long cn[9];
+    unsigned inside, S, F; /* in-grid neighbours, final set, positive outflows */
+    int nS;
+};
+
+static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I, long long c, int i, int j, Flow& F)
+{
+    double theta[9];
+    bool in_set[9];
+    const double t = d.St[c];
+    const double w = d.ph.Pc;
+    F.t = t;
+    F.Pr = power_law(d.ph.a, d.ph.b, t);
+    const double hc = power_law(d.ph.c, d.ph.d, t);
+    const double sz0 = d.Sz[c];
+    F.inside = 0;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+        const bool in = nbr(I, i, j, q, &F.cn[q]);
+        F.inside |= (in ? 1u : 0u) << q;
+        F.h[q] = in ? d.Slt[F.cn[q]] : 0.0;
+        const double sz = in ? d.Sz[F.cn[q]] : 0.0;
+        F.H[q] = F.f[q] = theta[q] = 0;
+        F.z[q] = q < 5 ? sz : sz0 - (sz0 - sz) / d.ph.rad2;
+    }
+    F.H[0] = F.z[0];
+    in_set[0] = true;
+#pragma unroll
+    for (int q = 1; q < 9; q++)
+        if (F.z[0] + F.h[0] > F.z[q] + F.h[q]) {
+            F.H[q] = F.z[q] + F.h[q];
+            theta[q] = atan(((F.z[0] + F.h[0]) - (F.z[q] + F.h[q])) / w);
+            in_set[q] = true;
+        } else {
+            in_set[q] = false;
+        }
+    bool loop;
+    double avg;
+    int counter;
+    do {
+        loop = false;
+        avg = F.h[0];
+        counter = 0;
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+            if (in_set[q]) {
+                avg += F.H[q];
+                counter++;
+            }
+        if (counter != 0)
+            avg = avg / (double)counter;
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+            if (in_set[q] && avg <= F.H[q]) {
+                in_set[q] = false;
+                loop = true;
+            }
+    } while (loop);
+    /* the last average was formed over the set before the final (empty)
+     * round of eliminations: that set is the final one */
+    F.avg = avg;
+    F.nS = counter;
+    F.S = 0;
+    F.F = 0;
+#pragma unroll
+    for (int q = 0; q < 9; q++)
+        F.S |= (in_set[q] ? 1u : 0u) << q;
+#pragma unroll
+    for (int q = 1; q < 9; q++) {
+        double fq = 0.0;
+        if (in_set[q] && F.h[0] > hc * cos(theta[q]))
+            fq = F.Pr * (avg - F.H[q]);
+        /* empiricalFlows stores only positive outflows; the rest stay 0 */
+        if (!(fq > 0))
+            fq = 0.0;
+        F.f[q] = fq;
+        if (fq > 0)
+            F.F |= 1u << q;
+    }
+}
 
 /* K1: outflows of every lava cell into compact slots; tiles flagged */
 __global__ void __launch_bounds__(K1T) k_flows(const __grid_constant__ Dev d)
@@ -190,87 +289,39 @@ __global__ void __launch_bounds__(K1T) k_flows(const __grid_constant__ Dev d)
         const Inst I = d.inst[locate(s_offs, d.B, c)];
         const long long lc = c - I.off;
         const int i = (int)(lc / I.cols), j = (int)(lc - (long long)i * I.cols);
-        double f[9], z[9], h[9], H[9], theta[9];
-        bool in_set[9];
-        const double t = d.St[c];
-        const double w = d.ph.Pc;
-        const double Pr = power_law(d.ph.a, d.ph.b, t);
-        const double hc = power_law(d.ph.c, d.ph.d, t);
-        const double sz0 = d.Sz[c];
-        bool inside[9];
-        long long cn[9];
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            inside[q] = nbr(I, i, j, q, &cn[q]);
-            h[q] = inside[q] ? d.Slt[cn[q]] : 0.0;
-            const double sz = inside[q] ? d.Sz[cn[q]] : 0.0;
-            H[q] = f[q] = theta[q] = 0;
-            z[q] = q < 5 ? sz : sz0 - (sz0 - sz) / d.ph.rad2;
-        }
-        H[0] = z[0];
-        in_set[0] = true;
-#pragma unroll
-        for (int q = 1; q < 9; q++)
-            if (z[0] + h[0] > z[q] + h[q]) {
-                H[q] = z[q] + h[q];
-                theta[q] = atan(((z[0] + h[0]) - (z[q] + h[q])) / w);
-                in_set[q] = true;
-            } else {
-                in_set[q] = false;
-            }
-        bool loop;
-        double avg;
-        do {
-            loop = false;
-            avg = h[0];
-            int counter = 0;
-#pragma unroll
-            for (int q = 0; q < 9; q++)
-                if (in_set[q]) {
-                    avg += H[q];
-                    counter++;
-                }
-            if (counter != 0)
-                avg = avg / (double)counter;
-#pragma unroll
-            for (int q = 0; q < 9; q++)
-                if (in_set[q] && avg <= H[q]) {
-                    in_set[q] = false;
-                    loop = true;
-                }
-        } while (loop);
+        Flow F;
+        compute_flows(d, I, c, i, j, F);
         double* slot = d.fc + (size_t)k * 16;
-        bool any = false;
 #pragma unroll
         for (int q = 1; q < 9; q++) {
-            double fq = 0.0;
-            if (in_set[q] && h[0] > hc * cos(theta[q]))
-                fq = Pr * (avg - H[q]);
-            /* empiricalFlows stores only positive outflows; the rest stay 0 */
-            if (!(fq > 0))
-                fq = 0.0;
-            slot[q - 1] = fq;
-            slot[8 + q - 1] = fq * t;
-            if (fq > 0 && inside[q]) {
-                any = true;
-                const long long rc = cn[q] - I.off;
+            slot[q - 1] = F.f[q];
+            slot[8 + q - 1] = F.f[q] * F.t;
+            if ((F.F >> q) & (F.inside >> q) & 1u) {
+                const long long rc = F.cn[q] - I.off;
                 const int ri = (int)(rc / I.cols), rj = (int)(rc - (long long)ri * I.cols);
                 flag_tile(d, I.tile0 + (ri / TH) * I.tiles_x + rj / TW, epoch);
             }
         }
-        (void)any;
         d.map[c] = make_int2(epoch, k);
         flag_tile(d, I.tile0 + (i / TH) * I.tiles_x + j / TW, epoch); /* cooling reaches every lava cell */
     }
 }
 
-/* width_update, updateTemperature and the border reset of one cell, in place */
-static __device__ __forceinline__ bool update_cell(const Dev& d, const Inst& I, int i, int j, int epoch)
+/* width_update and updateTemperature at one cell (Sciara.cpp:106-169):
+ * the forward quantities, with the outflows found through the (epoch, slot)
+ * map */
+struct CellFwd {
+    double h, t, sz, in_sum, out_sum, ht, residual, D, hn, tn, aus, st;
+    bool flowcond, border, lava, solid;
+};
+
+static __device__ __forceinline__ void compute_cell(const Dev& d, const Inst& I, int i, int j, long long x, int epoch,
+                                                    CellFwd& Cf)
 {
     const int opp[8] = {3, 2, 1, 0, 6, 7, 4, 5};
-    const long long x = I.off + (long long)i * I.cols + j;
-    const double initial_h = d.Slt[x];
-    const double initial_t = d.St[x];
+    Cf.h = d.Slt[x];
+    Cf.t = d.St[x];
+    Cf.sz = d.Sz[x];
     const int2 me = d.map[x];
     const double* mine = me.x == epoch ? d.fc + (size_t)me.y * 16 : nullptr;
     double ht = 0, in_sum = 0, out_sum = 0;
@@ -291,31 +342,53 @@ static __device__ __forceinline__ bool update_cell(const Dev& d, const Inst& I, 
         in_sum += in_flow;
         out_sum += out_flow;
     }
-    double h_next = initial_h;
-    double t_next = initial_t;
+    Cf.ht = ht;
+    Cf.in_sum = in_sum;
+    Cf.out_sum = out_sum;
+    double h_next = Cf.h;
+    double t_next = Cf.t;
     h_next += in_sum - out_sum;
-    if (in_sum > 0 || out_sum > 0) {
-        const double residual = initial_h - out_sum;
-        t_next = (residual * initial_t + ht) / (residual + in_sum);
+    Cf.flowcond = in_sum > 0 || out_sum > 0;
+    Cf.residual = 0.0;
+    Cf.D = 1.0;
+    if (Cf.flowcond) {
+        Cf.residual = Cf.h - out_sum;
+        Cf.D = Cf.residual + in_sum;
+        t_next = (Cf.residual * Cf.t + ht) / Cf.D;
     }
-    double sh = h_next, st = t_next;
-    const bool border = d.Mb[x] != 0;
-    if (sh > 0 && !border) {
-        const double sz = d.Sz[x];
-        if (sh != 0) {
-            const double nT = st;
-            const double aus = 1.0 + (3 * pow(nT, 3.0) * d.ph.Pepsilon * d.ph.Psigma * d.ph.Pclock * d.ph.Pcool) /
-                                         (d.ph.Prho * d.ph.Pcv * sh * d.ph.Pac);
-            st = nT / pow(aus, 1.0 / 3.0);
-        }
-        if (st <= d.ph.PTsol && sh > 0) {
-            d.Sz[x] = sz + sh;
+    Cf.hn = h_next;
+    Cf.tn = t_next;
+    Cf.border = d.Mb[x] != 0;
+    Cf.lava = h_next > 0 && !Cf.border;
+    Cf.solid = false;
+    Cf.aus = 1.0;
+    Cf.st = t_next;
+    if (Cf.lava) {
+        const double nT = t_next;
+        Cf.aus = 1.0 + (3 * pow(nT, 3.0) * d.ph.Pepsilon * d.ph.Psigma * d.ph.Pclock * d.ph.Pcool) /
+                           (d.ph.Prho * d.ph.Pcv * h_next * d.ph.Pac);
+        Cf.st = nT / pow(Cf.aus, 1.0 / 3.0);
+        Cf.solid = Cf.st <= d.ph.PTsol;
+    }
+}
+
+/* the step at one cell, in place (the border reset of the steering last) */
+static __device__ __forceinline__ bool update_cell(const Dev& d, const Inst& I, int i, int j, int epoch)
+{
+    const long long x = I.off + (long long)i * I.cols + j;
+    CellFwd Cf;
+    compute_cell(d, I, i, j, x, epoch, Cf);
+    double sh = Cf.hn, st = Cf.tn;
+    if (Cf.lava) {
+        st = Cf.st;
+        if (Cf.solid) {
+            d.Sz[x] = Cf.sz + sh;
             d.Msl[x] = d.Msl[x] + sh;
             sh = 0;
             st = d.ph.PTsol;
         }
     }
-    if (border) {
+    if (Cf.border) {
         sh = 0;
         st = 0;
     }
@@ -324,12 +397,25 @@ static __device__ __forceinline__ bool update_cell(const Dev& d, const Inst& I, 
     return sh > 0;
 }
 
-/* K2: every cell of the flagged tiles; the next lava list */
-__global__ void __launch_bounds__(T) k_update(const __grid_constant__ Dev d)
+/* undo tape of a run whose gradient is wanted: per flagged tile and step,
+ * the tile's (Slt, St, Sz) before the update; per step and vent cell, its
+ * thickness and temperature before the emission and the vent that emitted */
+struct Tape {
+    int* tile;        /* per slot: tile */
+    double* state;    /* per slot: 3 x TW*TH */
+    int* step_base;   /* per step: first slot */
+    int* step_count;  /* per step: slots */
+    double* vent;     /* per step and vent: orig Slt, orig St, emitting vent (-1: none, -2: not the cell's first) */
+    long long cap;    /* slots */
+};
+
+/* K2: every cell of the flagged tiles; the next lava list; the tape */
+__global__ void __launch_bounds__(T) k_update(const __grid_constant__ Dev d, const __grid_constant__ Tape tp, int step)
 {
     const int par = d.counts[4];
     const int epoch = d.counts[6];
     const int ntiles = d.counts[7];
+    const int base = d.counts[9];
     int* next = par ? d.list0 : d.list1;
     int* ncount = d.counts + (1 - par);
     for (int item = blockIdx.x; item < ntiles; item += gridDim.x) {
@@ -346,23 +432,35 @@ __global__ void __launch_bounds__(T) k_update(const __grid_constant__ Dev d)
         const Inst I = d.inst[lo];
         const int lt = t - I.tile0;
         const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        const long long slot = (long long)base + item;
+        const bool taping = tp.state && slot < tp.cap;
+        if (tp.state && !taping && threadIdx.x == 0)
+            atomicExch(d.counts + 10, 1);
+        if (taping && threadIdx.x == 0)
+            tp.tile[slot] = t;
         for (int q = threadIdx.x; q < TW * TH; q += T) {
             const int i = ty * TH + q / TW, j = tx * TW + q % TW;
             bool lava = false;
             long long x = 0;
             if (i < I.rows && j < I.cols) {
-                lava = update_cell(d, I, i, j, epoch);
                 x = I.off + (long long)i * I.cols + j;
+                if (taping) {
+                    double* s = tp.state + (size_t)slot * 3 * TW * TH;
+                    s[q] = d.Slt[x];
+                    s[TW * TH + q] = d.St[x];
+                    s[2 * TW * TH + q] = d.Sz[x];
+                }
+                lava = update_cell(d, I, i, j, epoch);
             }
             const unsigned m = __ballot_sync(0xffffffffu, lava);
             if (m) {
                 const int lane = threadIdx.x & 31;
-                int base = 0;
+                int b = 0;
                 if (lane == 0)
-                    base = atomicAdd(ncount, __popc(m));
-                base = __shfl_sync(0xffffffffu, base, 0);
+                    b = atomicAdd(ncount, __popc(m));
+                b = __shfl_sync(0xffffffffu, b, 0);
                 if (lava) {
-                    const int pos = base + __popc(m & ((1u << lane) - 1u));
+                    const int pos = b + __popc(m & ((1u << lane) - 1u));
                     if (pos < d.capacity)
                         next[pos] = (int)x;
                     else
@@ -375,11 +473,291 @@ __global__ void __launch_bounds__(T) k_update(const __grid_constant__ Dev d)
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(reinterpret_cast<unsigned*>(d.counts + 5), 1u) == gridDim.x - 1) {
+            if (tp.state) {
+                tp.step_base[step] = base;
+                tp.step_count[step] = ntiles;
+                d.counts[9] = base + ntiles;
+            }
             d.counts[4] = 1 - par;
             d.counts[5] = 0;
             d.counts[6] = epoch + 1;
             d.counts[7] = 0;
         }
+    }
+}
+
+/* ---- adjoint of the final-thickness misfit --------------------------------
+ * L = sum over every scenario's cells of (Slt_T - target)^2; gradient with
+ * respect to every vent's emission rate of every phase.  The forward's
+ * discrete decisions are frozen: the minimisation's elimination sets and the
+ * shear-resistance test, whether a cell has any flow, whether it holds lava,
+ * whether it solidifies, the border mask.  Reverse mode, step by step from
+ * the last: restore the step's taped tiles (the state after its emission),
+ * recompute its outflows, then
+ *   B2 (per cell of the step's tiles): mixing and cooling backward, in
+ *      place on the cell's own adjoints; keeps, per cell, dL/dh' (A_h),
+ *      dL/dt' / D (A_t) and t' for the outflow adjoints;
+ *   B1 (per lava cell): the adjoint of each outflow gathered from the two
+ *      cells it connects, then the minimisation backward, scattered (FP64
+ *      atomics) to the thickness, altitude and temperature adjoints of the
+ *      nine cells it read;
+ *   B0 (per scenario): the emission backward -- dL/drate += dL/dSlt(vent) *
+ *      Pclock / Pac for the vent whose emission took effect, the temperature
+ *      adjoint of the vent cell reset (the emission overwrote it) -- and the
+ *      vent cells restored to their state before the emission. */
+struct Adj {
+    double* lh;   /* dense: dL/dSlt */
+    double* lt;   /* dense: dL/dSt */
+    double* lz;   /* dense: dL/dSz */
+    double* fcb;  /* per compact cell: recomputed outflows (16 doubles) */
+    double* Ah;   /* per compact cell */
+    double* At;
+    double* tp;
+    double* grad; /* nvents x nphases, internal vent order */
+};
+
+static __device__ __forceinline__ int tile_instance(const Dev& d, int t)
+{
+    int lo = 0, hi = d.B - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (d.inst[mid].tile0 <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(T) k_brestore(const __grid_constant__ Dev d, const __grid_constant__ Tape tp, int base,
+                                                int count)
+{
+    for (int item = blockIdx.x; item < count; item += gridDim.x) {
+        const long long slot = (long long)base + item;
+        const int t = tp.tile[slot];
+        const Inst I = d.inst[tile_instance(d, t)];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        const double* s = tp.state + (size_t)slot * 3 * TW * TH;
+        for (int q = threadIdx.x; q < TW * TH; q += T) {
+            const int i = ty * TH + q / TW, j = tx * TW + q % TW;
+            if (i < I.rows && j < I.cols) {
+                const long long x = I.off + (long long)i * I.cols + j;
+                d.Slt[x] = s[q];
+                d.St[x] = s[TW * TH + q];
+                d.Sz[x] = s[2 * TW * TH + q];
+            }
+        }
+    }
+}
+
+/* the step's outflows again, from the restored state, into compact cells */
+__global__ void __launch_bounds__(T) k_bflows(const __grid_constant__ Dev db, const __grid_constant__ Tape tp,
+                                              int base, int count, int epoch_b)
+{
+    for (int item = blockIdx.x; item < count; item += gridDim.x) {
+        const int t = tp.tile[(long long)base + item];
+        const Inst I = db.inst[tile_instance(db, t)];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        for (int q = threadIdx.x; q < TW * TH; q += T) {
+            const int i = ty * TH + q / TW, j = tx * TW + q % TW;
+            if (i >= I.rows || j >= I.cols)
+                continue;
+            const long long x = I.off + (long long)i * I.cols + j;
+            const int idx = item * TW * TH + q;
+            double* slot = db.fc + (size_t)idx * 16;
+            db.map[x] = make_int2(epoch_b, idx);
+            if (db.Slt[x] > 0) {
+                Flow F;
+                compute_flows(db, I, x, i, j, F);
+#pragma unroll
+                for (int k = 1; k < 9; k++) {
+                    slot[k - 1] = F.f[k];
+                    slot[8 + k - 1] = F.f[k] * F.t;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                    slot[k] = 0.0;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(T) k_bcells(const __grid_constant__ Dev db, const __grid_constant__ Tape tp,
+                                              const __grid_constant__ Adj a, int base, int count, int epoch_b)
+{
+    for (int item = blockIdx.x; item < count; item += gridDim.x) {
+        const int t = tp.tile[(long long)base + item];
+        const Inst I = db.inst[tile_instance(db, t)];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        for (int q = threadIdx.x; q < TW * TH; q += T) {
+            const int i = ty * TH + q / TW, j = tx * TW + q % TW;
+            if (i >= I.rows || j >= I.cols)
+                continue;
+            const long long x = I.off + (long long)i * I.cols + j;
+            const int idx = item * TW * TH + q;
+            CellFwd Cf;
+            compute_cell(db, I, i, j, x, epoch_b, Cf);
+            const double lh = a.lh[x], lt_ = a.lt[x];
+            double Lh = lh, Lt = lt_; /* adjoints of h', t' */
+            if (Cf.border) {
+                Lh = 0.0;
+                Lt = 0.0;
+            } else if (Cf.lava) {
+                if (Cf.solid) {
+                    Lh = a.lz[x]; /* Sz += h' */
+                    Lt = 0.0;
+                } else {
+                    /* st = nT / aus^(1/3), aus = 1 + 3 K nT^3 / (C h') */
+                    const double K = db.ph.Pepsilon * db.ph.Psigma * db.ph.Pclock * db.ph.Pcool;
+                    const double Cc = db.ph.Prho * db.ph.Pcv * db.ph.Pac;
+                    const double nT = Cf.tn, hn = Cf.hn;
+                    const double dst_daus = -Cf.st / (3.0 * Cf.aus);
+                    const double daus_dT = 9.0 * K * nT * nT / (Cc * hn);
+                    const double daus_dh = -3.0 * K * nT * nT * nT / (Cc * hn * hn);
+                    const double dst_dT = Cf.st / nT + dst_daus * daus_dT;
+                    Lh = lh + lt_ * (dst_daus * daus_dh);
+                    Lt = lt_ * dst_dT;
+                }
+            }
+            double new_lh = Lh, new_lt = Lt, At = 0.0;
+            if (Cf.flowcond) {
+                new_lh = Lh + Lt * (Cf.t - Cf.tn) / Cf.D;
+                new_lt = Lt * Cf.residual / Cf.D;
+                At = Lt / Cf.D;
+            }
+            a.lh[x] = new_lh;
+            a.lt[x] = new_lt;
+            a.Ah[idx] = Lh;
+            a.At[idx] = At;
+            a.tp[idx] = Cf.tn;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(T) k_bflowadj(const __grid_constant__ Dev db, const __grid_constant__ Tape tp,
+                                                const __grid_constant__ Adj a, int base, int count, int epoch_b)
+{
+    for (int item = blockIdx.x; item < count; item += gridDim.x) {
+        const int t = tp.tile[(long long)base + item];
+        const Inst I = db.inst[tile_instance(db, t)];
+        const int lt = t - I.tile0;
+        const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+        for (int q0 = threadIdx.x; q0 < TW * TH; q0 += T) {
+            const int i = ty * TH + q0 / TW, j = tx * TW + q0 % TW;
+            if (i >= I.rows || j >= I.cols)
+                continue;
+            const long long x = I.off + (long long)i * I.cols + j;
+            if (!(db.Slt[x] > 0))
+                continue;
+            Flow F;
+            compute_flows(db, I, x, i, j, F);
+            if (!F.F)
+                continue;
+            const int idx = item * TW * TH + q0;
+            const double Ahc = a.Ah[idx], Atc = a.At[idx], tpc = a.tp[idx];
+            double lf[9];
+            double lt_add = 0.0;
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                lf[k] = 0.0;
+#pragma unroll
+            for (int k = 1; k < 9; k++) {
+                if (!((F.F >> k) & 1u))
+                    continue;
+                double v = -Ahc + Atc * (tpc - F.t); /* this cell's outflow */
+                if ((F.inside >> k) & 1u) {
+                    const int2 m = db.map[F.cn[k]];
+                    if (m.x == epoch_b) { /* the receiver's inflow (its tile is in the list) */
+                        const double Ahr = a.Ah[m.y], Atr = a.At[m.y], tpr = a.tp[m.y];
+                        v += Ahr + Atr * (F.t - tpr);
+                        lt_add += Atr * F.f[k]; /* the receiver's heat term f * t */
+                    }
+                }
+                lf[k] = v;
+            }
+            /* f[k] = Pr(t) (avg - H[k]), avg = (h0 + sum_S H) / |S| */
+            const double dPr = F.Pr * db.ph.b * 2.302585092994045684;
+            double G = 0.0, lH[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                lH[k] = 0.0;
+#pragma unroll
+            for (int k = 1; k < 9; k++)
+                if ((F.F >> k) & 1u) {
+                    G += lf[k] * F.Pr;
+                    lH[k] -= lf[k] * F.Pr;
+                    lt_add += lf[k] * dPr * (F.avg - F.H[k]);
+                }
+            const double g = G / (double)F.nS;
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                if ((F.S >> k) & 1u)
+                    lH[k] += g;
+            atomicAdd(a.lh + x, g); /* avg's h[0] */
+            atomicAdd(a.lt + x, lt_add);
+            const double inv = 1.0 / db.ph.rad2;
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                if (lH[k] == 0.0)
+                    continue;
+                const bool in = (F.inside >> k) & 1u;
+                /* H[k] = z[k] + h[k] for k >= 1, H[0] = z[0] */
+                if (k >= 1 && in)
+                    atomicAdd(a.lh + F.cn[k], lH[k]);
+                if (k < 5) {
+                    if (in)
+                        atomicAdd(a.lz + F.cn[k], lH[k]);
+                } else {
+                    /* z[k] = sz0 - (sz0 - sz_k) / rad2 */
+                    if (in)
+                        atomicAdd(a.lz + F.cn[k], lH[k] * inv);
+                    atomicAdd(a.lz + x, lH[k] * (1.0 - inv));
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_bvents(const __grid_constant__ Dev d, const __grid_constant__ Adj a, const double* vtape, int phase)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.B)
+        return;
+    for (int v = d.vent_first[b]; v < d.vent_first[b + 1]; v++) {
+        const double* rec = vtape + 3 * v;
+        const int eff = (int)rec[2];
+        if (eff < 0)
+            continue; /* not the cell's first vent, or no emission */
+        const int c = d.vent_cell[v];
+        if (phase < d.nphases)
+            a.grad[(size_t)eff * d.nphases + phase] += a.lh[c] * d.ph.Pclock / d.ph.Pac;
+        a.lt[c] = 0.0;
+        d.Slt[c] = rec[0];
+        d.St[c] = rec[1];
+    }
+}
+
+/* dL/dSlt_T = 2 (Slt_T - target), the other adjoints 0; per-scenario loss */
+__global__ void k_bloss(const __grid_constant__ Dev d, const __grid_constant__ Adj a, const double* tgt, double* loss)
+{
+    __shared__ long long s_offs[MAX_INST + 1];
+    for (int k = threadIdx.x; k <= d.B; k += blockDim.x)
+        s_offs[k] = d.offs[k];
+    __syncthreads();
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < d.ncells; c += (long long)gridDim.x * blockDim.x) {
+        const int b = locate(s_offs, d.B, c);
+        const Inst I = d.inst[b];
+        const bool valid = c - I.off < (long long)I.rows * I.cols;
+        const double diff = valid ? d.Slt[c] - tgt[c] : 0.0;
+        a.lh[c] = 2.0 * diff;
+        a.lt[c] = 0.0;
+        a.lz[c] = 0.0;
+        if (valid && diff != 0.0)
+            atomicAdd(loss + b, diff * diff);
     }
 }
 
@@ -449,6 +827,8 @@ struct Batch {
     std::vector<long long> offs;
     Dev d;
     double effusion_duration = 0;
+    std::vector<int> vent_order; /* internal vent k -> the caller's vent index */
+    double *Sz0 = nullptr, *Slt0 = nullptr, *St0 = nullptr; /* the initial state, for every run */
     cudaStream_t st = nullptr;
     void* allocs[32] = {};
     int nalloc = 0;
@@ -537,6 +917,7 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
         for (int v = 0; v < nvents; v++)
             order[v] = v;
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return vent_inst[a] < vent_inst[b]; });
+        bt->vent_order = order;
         for (int k = 0; k < nvents; k++) {
             const int v = order[k];
             const int b = vent_inst[v];
@@ -595,7 +976,8 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
               sci2::dalloc(*bt, &d.tlist, sizeof(int) * (size_t)tiles) &&
               sci2::dalloc(*bt, (int**)&d.vent_cell, sizeof(int) * std::max(1, nvents)) &&
               sci2::dalloc(*bt, (int**)&d.vent_first, sizeof(int) * (B + 1)) &&
-              sci2::dalloc(*bt, (double**)&d.rates, sizeof(double) * std::max<size_t>(1, vrates.size()));
+              sci2::dalloc(*bt, (double**)&d.rates, sizeof(double) * std::max<size_t>(1, vrates.size())) &&
+              sci2::dalloc(*bt, &bt->Sz0, nb) && sci2::dalloc(*bt, &bt->Slt0, nb) && sci2::dalloc(*bt, &bt->St0, nb);
     if (!ok) {
         fprintf(stderr, "opencal-gb300: cal_sciara_batch_create: out of device memory\n");
         sci2::destroy(bt);
@@ -623,6 +1005,9 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
             cudaMemcpy(d.St + o, st0 + src, n * sizeof(double), cudaMemcpyHostToDevice);
         src += n;
     }
+    cudaMemcpy(bt->Sz0, d.Sz, nb, cudaMemcpyDeviceToDevice);
+    cudaMemcpy(bt->Slt0, d.Slt, nb, cudaMemcpyDeviceToDevice);
+    cudaMemcpy(bt->St0, d.St, nb, cudaMemcpyDeviceToDevice);
     if (cudaGetLastError() != cudaSuccess) {
         sci2::destroy(bt);
         return nullptr;
@@ -636,33 +1021,44 @@ extern "C" void cal_sciara_batch_destroy(void* handle)
         sci2::destroy((Batch*)handle);
 }
 
-/* Run every scenario from its initial state until the emission ends (or
- * max_steps > 0 steps); the state stays on the device for
- * cal_sciara_batch_read.  steps_done: steps run; ms: device time of the step
- * loop.  0, or a CALError code (CAL_ERROR_OUT_OF_MEMORY = list overflow). */
-extern "C" int cal_sciara_batch_run(void* handle, int max_steps, int* steps_done, float* ms)
+namespace sci2 {
+
+/* the run from the initial state: calRun2D's loop with the stop condition
+ * of Sciara.cpp:177-183 (elapsed time >= emission's end).  With a tape the
+ * undo records of every step are kept (vtape: steps x nvents x 3). */
+static int forward(Batch* bt, int max_steps, const Tape* tape, double* vtape, std::vector<double>* elapsed_of,
+                   int* steps_done, float* ms)
 {
-    Batch* bt = (Batch*)handle;
-    sci2::Dev& d = bt->d;
+    Dev& d = bt->d;
     cudaStream_t st = bt->st;
+    const size_t nb = (size_t)bt->N * sizeof(double);
+    cudaMemcpyAsync(d.Sz, bt->Sz0, nb, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(d.Slt, bt->Slt0, nb, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(d.St, bt->St0, nb, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(d.Msl, 0, nb, st);
     cudaMemsetAsync(d.counts, 0, 16 * sizeof(int), st);
     cudaMemsetAsync(d.map, 0, sizeof(int2) * (size_t)bt->N, st);
     cudaMemsetAsync(d.tflag, 0, sizeof(int) * (size_t)bt->ntiles, st);
     const int one = 1;
     cudaMemcpyAsync(d.counts + 6, &one, sizeof(int), cudaMemcpyHostToDevice, st);
-    int blocks = (int)std::min<long long>((bt->N + sci2::T - 1) / sci2::T, 152 * 16);
-    sci2::k_prime<<<blocks, sci2::T, 0, st>>>(d);
+    int blocks = (int)std::min<long long>((bt->N + T - 1) / T, 152 * 16);
+    k_prime<<<blocks, T, 0, st>>>(d);
+    Tape tp;
+    memset(&tp, 0, sizeof(tp));
+    if (tape)
+        tp = *tape;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
     double elapsed = 0.0;
     int done = 0;
-    /* the run loop of calRun2D with the stop condition of Sciara.cpp:177-183 */
     for (int step = 1; max_steps <= 0 || step <= max_steps; step++) {
-        sci2::k_vents<<<(bt->B + 63) / 64, 64, 0, st>>>(d, elapsed);
-        sci2::k_flows<<<152 * 32, sci2::K1T, 0, st>>>(d);
-        sci2::k_update<<<sci2::K2_BLOCKS, sci2::T, 0, st>>>(d);
+        if (elapsed_of)
+            elapsed_of->push_back(elapsed);
+        k_vents<<<(bt->B + 63) / 64, 64, 0, st>>>(d, elapsed, vtape ? vtape + (size_t)done * 3 * bt->nvents : nullptr);
+        k_flows<<<152 * 32, K1T, 0, st>>>(d);
+        k_update<<<K2_BLOCKS, T, 0, st>>>(d, tp, done);
         done++;
         elapsed += d.ph.Pclock;
         if (elapsed >= bt->effusion_duration)
@@ -678,11 +1074,164 @@ extern "C" int cal_sciara_batch_run(void* handle, int max_steps, int* steps_done
         *ms = t;
     if (steps_done)
         *steps_done = done;
-    int overflow = 0;
-    cudaMemcpy(&overflow, d.counts + 8, sizeof(int), cudaMemcpyDeviceToHost);
+    int flags[3] = {0, 0, 0};
+    cudaMemcpy(flags, d.counts + 8, sizeof(flags), cudaMemcpyDeviceToHost);
     if (cudaGetLastError() != cudaSuccess)
         return 3; /* CAL_ERROR_CUDA */
-    return overflow ? 2 /* CAL_ERROR_OUT_OF_MEMORY */ : 0;
+    return (flags[0] || flags[2]) ? 2 /* CAL_ERROR_OUT_OF_MEMORY: lava list or tape too small */ : 0;
+}
+
+/* steps a run takes (the stop condition's accumulation of the clock) */
+static int run_length(const Batch* bt, int max_steps)
+{
+    double elapsed = 0.0;
+    int done = 0;
+    for (int step = 1; max_steps <= 0 || step <= max_steps; step++) {
+        done++;
+        elapsed += bt->d.ph.Pclock;
+        if (elapsed >= bt->effusion_duration)
+            break;
+    }
+    return done;
+}
+
+} // namespace sci2
+
+/* Run every scenario from its initial state (as created) until the emission ends (or
+ * max_steps > 0 steps); the state stays on the device for
+ * cal_sciara_batch_read.  steps_done: steps run; ms: device time of the step
+ * loop.  0, or a CALError code (CAL_ERROR_OUT_OF_MEMORY = list overflow). */
+extern "C" int cal_sciara_batch_run(void* handle, int max_steps, int* steps_done, float* ms)
+{
+    return sci2::forward((Batch*)handle, max_steps, nullptr, nullptr, nullptr, steps_done, ms);
+}
+
+/* Loss L_b = sum over scenario b of (Slt_T - target)^2 and its gradient
+ * with respect to every emission rate, by the adjoint with the forward's
+ * decisions frozen.  target: host array, the scenarios' grids back to back
+ * (unpadded); loss_out[B]; grad_out[nvents x nphases] in the caller's vent
+ * order.  tape_slots: undo-tape capacity in tiles summed over the steps
+ * (0: twice the scenarios' tiles + 4096).  The state after the call is the
+ * run's final one for Slt, St, Sz (Msl is not restored).  0 or a CALError
+ * code; ms: device time of forward + adjoint. */
+extern "C" int cal_sciara_batch_loss_grad(void* handle, const double* target, int max_steps, double* loss_out,
+                                          double* grad_out, int* steps_done, long long tape_slots, float* ms)
+{
+    Batch* bt = (Batch*)handle;
+    sci2::Dev& d = bt->d;
+    cudaStream_t st = bt->st;
+    const int steps = sci2::run_length(bt, max_steps);
+    const long long cap = tape_slots > 0 ? tape_slots : 2LL * bt->ntiles + 4096;
+    const size_t tile_cells = (size_t)sci2::TW * sci2::TH;
+    sci2::Tape tp;
+    memset(&tp, 0, sizeof(tp));
+    tp.cap = cap;
+    double* vtape = nullptr;
+    double* tgt = nullptr;
+    double* dloss = nullptr;
+    sci2::Adj a;
+    memset(&a, 0, sizeof(a));
+    std::vector<void*> mem;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (cudaMalloc(p, bytes) != cudaSuccess)
+            return false;
+        mem.push_back(*p);
+        return true;
+    };
+    const size_t nb = (size_t)bt->N * sizeof(double);
+    bool ok = alloc((void**)&tp.tile, sizeof(int) * cap) && alloc((void**)&tp.state, sizeof(double) * 3 * tile_cells * cap) &&
+              alloc((void**)&tp.step_base, sizeof(int) * (steps + 1)) &&
+              alloc((void**)&tp.step_count, sizeof(int) * (steps + 1)) &&
+              alloc((void**)&vtape, sizeof(double) * 3 * std::max(1, bt->nvents) * (size_t)steps) &&
+              alloc((void**)&tgt, nb) && alloc((void**)&dloss, sizeof(double) * bt->B) &&
+              alloc((void**)&a.lh, nb) && alloc((void**)&a.lt, nb) && alloc((void**)&a.lz, nb) &&
+              alloc((void**)&a.grad, sizeof(double) * std::max(1, bt->nvents * bt->nphases));
+    auto release = [&]() {
+        cudaStreamSynchronize(st);
+        for (void* p : mem)
+            cudaFree(p);
+    };
+    if (!ok) {
+        release();
+        return 2; /* CAL_ERROR_OUT_OF_MEMORY */
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    std::vector<double> elapsed_of;
+    int done = 0;
+    int rc = sci2::forward(bt, max_steps, &tp, vtape, &elapsed_of, &done, nullptr);
+    if (rc) {
+        release();
+        return rc;
+    }
+    /* target in the padded layout */
+    cudaMemsetAsync(tgt, 0, nb, st);
+    size_t src = 0;
+    for (int b = 0; b < bt->B; b++) {
+        const size_t n = (size_t)bt->inst[b].rows * bt->inst[b].cols;
+        cudaMemcpyAsync(tgt + bt->offs[b], target + src, n * sizeof(double), cudaMemcpyHostToDevice, st);
+        src += n;
+    }
+    cudaMemsetAsync(dloss, 0, sizeof(double) * bt->B, st);
+    cudaMemsetAsync(a.grad, 0, sizeof(double) * std::max(1, bt->nvents * bt->nphases), st);
+    const int blocks = (int)std::min<long long>((bt->N + sci2::T - 1) / sci2::T, 152 * 16);
+    sci2::k_bloss<<<blocks, sci2::T, 0, st>>>(d, a, tgt, dloss);
+    /* backward scratch: the largest step's tiles */
+    std::vector<int> base(done), count(done);
+    cudaMemcpyAsync(base.data(), tp.step_base, sizeof(int) * done, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(count.data(), tp.step_count, sizeof(int) * done, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    int maxc = 1;
+    for (int t = 0; t < done; t++)
+        maxc = std::max(maxc, count[t]);
+    const size_t nc = (size_t)maxc * tile_cells;
+    ok = alloc((void**)&a.fcb, sizeof(double) * 16 * nc) && alloc((void**)&a.Ah, sizeof(double) * nc) &&
+         alloc((void**)&a.At, sizeof(double) * nc) && alloc((void**)&a.tp, sizeof(double) * nc);
+    if (!ok) {
+        release();
+        return 2;
+    }
+    sci2::Dev db = d;
+    db.fc = a.fcb;
+    for (int t = done - 1; t >= 0; t--) {
+        const int epoch_b = -(t + 1);
+        const int g = std::max(1, std::min(count[t], sci2::K2_BLOCKS));
+        if (count[t] > 0) {
+            sci2::k_brestore<<<g, sci2::T, 0, st>>>(d, tp, base[t], count[t]);
+            sci2::k_bflows<<<g, sci2::T, 0, st>>>(db, tp, base[t], count[t], epoch_b);
+            sci2::k_bcells<<<g, sci2::T, 0, st>>>(db, tp, a, base[t], count[t], epoch_b);
+            sci2::k_bflowadj<<<g, sci2::T, 0, st>>>(db, tp, a, base[t], count[t], epoch_b);
+        }
+        const int phase = (int)(unsigned)(elapsed_of[t] / bt->emission_time);
+        sci2::k_bvents<<<(bt->B + 63) / 64, 64, 0, st>>>(d, a, vtape + (size_t)t * 3 * bt->nvents, phase);
+    }
+    cudaEventRecord(e1, st);
+    std::vector<double> grad((size_t)std::max(1, bt->nvents * bt->nphases));
+    cudaMemcpyAsync(grad.data(), a.grad, sizeof(double) * grad.size(), cudaMemcpyDeviceToHost, st);
+    if (loss_out)
+        cudaMemcpyAsync(loss_out, dloss, sizeof(double) * bt->B, cudaMemcpyDeviceToHost, st);
+    cudaEventSynchronize(e1);
+    float t_ms = 0.f;
+    cudaEventElapsedTime(&t_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms)
+        *ms = t_ms;
+    if (steps_done)
+        *steps_done = done;
+    if (grad_out)
+        for (int k = 0; k < bt->nvents; k++)
+            for (int p = 0; p < bt->nphases; p++)
+                grad_out[(size_t)bt->vent_order[k] * bt->nphases + p] = grad[(size_t)k * bt->nphases + p];
+    rc = cudaGetLastError() == cudaSuccess ? 0 : 3;
+    release();
+    /* the tape undid the run: run again so that reads see the final state,
+     * as after cal_sciara_batch_run */
+    if (!rc)
+        rc = sci2::forward(bt, max_steps, nullptr, nullptr, nullptr, nullptr, nullptr);
+    return rc;
 }
 
 /* the scenarios' final Sz, Slt, St, Msl, back to back and unpadded (any may be NULL) */

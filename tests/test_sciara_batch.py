@@ -70,3 +70,50 @@ def test_list_overflow_is_an_error(cal):
     sc = _scenario(160, 160, 31, 3600)
     with pytest.raises(cal.CALError):
         cal.sciara_batch([sc], 200, list_fraction=1e-9)
+
+
+def _loss(cal, sc, target):
+    (out,), _ = cal.sciara_batch([sc])
+    d = out["slt"] - target
+    return float((d * d).sum())
+
+
+def test_emission_rate_gradient_matches_finite_differences(cal):
+    """dL/drate of the adjoint (decisions frozen) against central finite
+    differences of the forward, at a point where no decision flips within
+    the step (relative step 1e-7)"""
+    z, vents, rates = W.sciara_inputs(56, 64, seed=41, nvents=2, phases=3)
+    et = 300
+    true = [[r * 0.9 for r in rr] for rr in rates]
+    (tgt_run,), _ = cal.sciara_batch([(z, vents, true, et)])
+    target = tgt_run["slt"]
+    sc = (z, vents, rates, et)
+    loss, (g,) = cal.sciara_loss_grad([sc], [target])
+    assert loss[0] == pytest.approx(_loss(cal, sc, target), rel=1e-12)
+    checked = 0
+    for v in range(len(vents)):
+        for p in range(3):
+            d = rates[v][p] * 1e-7
+            up = [list(rr) for rr in rates]
+            dn = [list(rr) for rr in rates]
+            up[v][p] += d
+            dn[v][p] -= d
+            fd = (_loss(cal, (z, vents, up, et), target) - _loss(cal, (z, vents, dn, et), target)) / (2 * d)
+            assert g[v, p] == pytest.approx(fd, rel=2e-4, abs=1e-9 * max(1.0, abs(fd))), (v, p)
+            checked += 1
+    assert checked == 6 and np.abs(g).max() > 0
+
+
+def test_gradient_batch_equals_scenarios_alone(cal):
+    scs, tgts = [], []
+    for k, (r, c) in enumerate([(48, 60), (64, 52)]):
+        z, vents, rates = W.sciara_inputs(r, c, seed=50 + k, phases=3)
+        sc = (z, vents, rates, 300)
+        (t,), _ = cal.sciara_batch([(z, vents, [[x * 1.1 for x in rr] for rr in rates], 300)])
+        scs.append(sc)
+        tgts.append(t["slt"])
+    loss, grads = cal.sciara_loss_grad(scs, tgts)
+    for k in range(2):
+        l1, (g1,) = cal.sciara_loss_grad([scs[k]], [tgts[k]])
+        assert loss[k] == pytest.approx(l1[0], rel=1e-13)
+        np.testing.assert_allclose(grads[k], g1, rtol=1e-10, atol=1e-14)
