@@ -225,51 +225,129 @@ def sciddicaT_unsafe(z0, h0, steps, *, toroidal=True, p_r=0.5, p_eps=0.001, grap
     return z, h
 
 
-def _sciara_batch_handle(scenarios, params, list_fraction):
-    from .workloads import SCIARA_PARAMS
-    B = len(scenarios)
-    ets = {int(s[3]) for s in scenarios}
-    nph = {len(s[2][0]) for s in scenarios}
-    if len(ets) != 1 or len(nph) != 1:
-        raise ValueError("scenarios must share the emission schedule (emission_time, number of phases)")
-    et, nphases = ets.pop(), nph.pop()
-    dims = np.ascontiguousarray(np.array([np.shape(s[0]) for s in scenarios], dtype=np.int32).reshape(-1))
-    z = np.ascontiguousarray(np.concatenate([np.asarray(s[0], np.float64).ravel() for s in scenarios]))
-    vinst, vxy, rates = [], [], []
-    for b, s in enumerate(scenarios):
-        for v, r in zip(s[1], s[2]):
-            vinst.append(b)
-            vxy.extend(v)
-            rates.extend(r)
-    vinst = np.ascontiguousarray(np.array(vinst, dtype=np.int32))
-    vxy = np.ascontiguousarray(np.array(vxy, dtype=np.int32))
-    rates = np.ascontiguousarray(np.array(rates, dtype=np.float64))
-    p = np.ascontiguousarray(params if params is not None else SCIARA_PARAMS, dtype=np.float64)
-    m = models()
-    m.cal_sciara_batch_create.restype = C.c_void_p
-    m.cal_sciara_batch_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                          C.c_int, C.c_void_p, C.c_void_p, C.c_uint, C.c_int, C.c_void_p,
-                                          C.c_double]
-    m.cal_sciara_batch_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
-    m.cal_sciara_batch_read.argtypes = [C.c_void_p] + [C.c_void_p] * 4
-    m.cal_sciara_batch_destroy.argtypes = [C.c_void_p]
-    m.cal_sciara_batch_loss_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
-                                             C.POINTER(C.c_int), C.c_longlong, C.POINTER(C.c_float)]
-    h = m.cal_sciara_batch_create(B, dims.ctypes.data, z.ctypes.data, None, None, p.ctypes.data, len(vinst),
-                                  vinst.ctypes.data, vxy.ctypes.data, et, nphases, rates.ctypes.data,
-                                  float(list_fraction))
-    if not h:
-        raise CALError("cal_sciara_batch_create failed (bad argument or out of device memory)")
-    return m, h, z, len(vinst), nphases
+class SciaraBatch:
+    """SCIARA-fv2 scenarios on the device, advanced together by the split step
+    (csrc/models/sciara_batch.cu): created once, then run (always from the
+    initial state), read back and differentiated as often as wanted.
+    scenarios: [(z0, vents [(x, y)], rates [nvents][nphases], emission_time)]
+    sharing the emission schedule.  close() (or ``with``) frees the device
+    memory."""
 
+    def __init__(self, scenarios, *, params=None, list_fraction=0.0):
+        from .workloads import SCIARA_PARAMS
+        self.shapes = [tuple(np.shape(s[0])) for s in scenarios]
+        self.vents_per = [len(s[1]) for s in scenarios]
+        ets = {int(s[3]) for s in scenarios}
+        nph = {len(s[2][0]) for s in scenarios}
+        if len(ets) != 1 or len(nph) != 1:
+            raise ValueError("scenarios must share the emission schedule (emission_time, number of phases)")
+        et, self.nphases = ets.pop(), nph.pop()
+        self.cells = int(sum(r * c for r, c in self.shapes))
+        dims = np.ascontiguousarray(np.array(self.shapes, dtype=np.int32).reshape(-1))
+        z = np.empty(self.cells)
+        pos = 0
+        for s in scenarios:
+            n = int(np.size(s[0]))
+            z[pos:pos + n] = np.asarray(s[0], np.float64).ravel()
+            pos += n
+        vinst, vxy, rates = [], [], []
+        for b, s in enumerate(scenarios):
+            for v, r in zip(s[1], s[2]):
+                vinst.append(b)
+                vxy.extend(v)
+                rates.extend(r)
+        self.nvents = len(vinst)
+        vinst = np.ascontiguousarray(np.array(vinst, dtype=np.int32))
+        vxy = np.ascontiguousarray(np.array(vxy, dtype=np.int32))
+        rates = np.ascontiguousarray(np.array(rates, dtype=np.float64))
+        p = np.ascontiguousarray(params if params is not None else SCIARA_PARAMS, dtype=np.float64)
+        m = models()
+        m.cal_sciara_batch_create.restype = C.c_void_p
+        m.cal_sciara_batch_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_int, C.c_void_p, C.c_void_p, C.c_uint, C.c_int, C.c_void_p,
+                                              C.c_double]
+        m.cal_sciara_batch_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+        m.cal_sciara_batch_read.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+        m.cal_sciara_batch_destroy.argtypes = [C.c_void_p]
+        m.cal_sciara_batch_lava_cells.argtypes = [C.c_void_p]
+        m.cal_sciara_batch_loss_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                                 C.POINTER(C.c_int), C.c_longlong, C.POINTER(C.c_float)]
+        self._m = m
+        self._h = m.cal_sciara_batch_create(len(scenarios), dims.ctypes.data, z.ctypes.data, None, None,
+                                            p.ctypes.data, self.nvents, vinst.ctypes.data, vxy.ctypes.data, et,
+                                            self.nphases, rates.ctypes.data, float(list_fraction))
+        if not self._h:
+            raise CALError("cal_sciara_batch_create failed (bad argument or out of device memory)")
 
-def _sciara_unpack(scenarios, flat):
-    res, pos = [], 0
-    for s in scenarios:
-        r, c = np.shape(s[0])
-        res.append(flat[pos:pos + r * c].reshape(r, c).copy())
-        pos += r * c
-    return res
+    def run(self, steps=0):
+        """Run every scenario from its initial state (steps 0: until the
+        emission ends).  Returns (steps run, device milliseconds)."""
+        done, ms = C.c_int(0), C.c_float(0.0)
+        _check(self._m.cal_sciara_batch_run(self._h, int(steps), C.byref(done), C.byref(ms)),
+               "cal_sciara_batch_run")
+        return done.value, ms.value
+
+    def read(self, *names):
+        """The final grids named ("z", "slt", "st", "msl"), each a list of
+        per-scenario arrays; default all four as a list of dicts."""
+        want = names or ("z", "slt", "st", "msl")
+        outs = {k: np.empty(self.cells) for k in want}
+        ptr = [outs[k].ctypes.data if k in outs else None for k in ("z", "slt", "st", "msl")]
+        _check(self._m.cal_sciara_batch_read(self._h, *ptr), "cal_sciara_batch_read")
+        per = {k: self._unpack(v) for k, v in outs.items()}
+        if names:
+            return per[names[0]] if len(names) == 1 else [per[k] for k in names]
+        return [{k: per[k][b] for k in per} for b in range(len(self.shapes))]
+
+    def lava_cells(self):
+        return int(self._m.cal_sciara_batch_lava_cells(self._h))
+
+    def loss_grad(self, targets, steps=0, *, tape_slots=0):
+        """L_b = sum (Slt_T - target_b)^2 and dL/drate of every vent and phase
+        (adjoint with the forward's decisions frozen).  targets: per-scenario
+        grids or one flat array.  Returns (loss[B], [grad_b (nvents_b x
+        nphases)], device milliseconds of forward + adjoint)."""
+        if isinstance(targets, np.ndarray) and targets.ndim == 1:
+            tgt = np.ascontiguousarray(targets, dtype=np.float64)
+        else:
+            tgt = np.ascontiguousarray(np.concatenate([np.asarray(t, np.float64).ravel() for t in targets]))
+        if tgt.size != self.cells:
+            raise ValueError("targets do not match the scenarios' grids")
+        loss = np.zeros(len(self.shapes))
+        grad = np.zeros(max(1, self.nvents * self.nphases))
+        done, ms = C.c_int(0), C.c_float(0.0)
+        _check(self._m.cal_sciara_batch_loss_grad(self._h, tgt.ctypes.data, int(steps), loss.ctypes.data,
+                                                  grad.ctypes.data, C.byref(done), int(tape_slots), C.byref(ms)),
+               "cal_sciara_batch_loss_grad")
+        grads, pos = [], 0
+        for k in self.vents_per:
+            grads.append(grad[pos * self.nphases:(pos + k) * self.nphases].reshape(k, self.nphases).copy())
+            pos += k
+        return loss, grads, ms.value
+
+    def _unpack(self, flat):
+        res, pos = [], 0
+        for r, c in self.shapes:
+            res.append(flat[pos:pos + r * c].reshape(r, c))
+            pos += r * c
+        return res
+
+    def close(self):
+        if self._h:
+            self._m.cal_sciara_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def sciara_batch(scenarios, steps=0, *, params=None, list_fraction=0.0, timing=False):
@@ -278,19 +356,10 @@ def sciara_batch(scenarios, steps=0, *, params=None, list_fraction=0.0, timing=F
     emission_time)], sharing the emission schedule.  Returns a list of dicts
     (z, slt, st, msl) and the steps run (and the device milliseconds with
     timing=True)."""
-    m, h, z, _, _ = _sciara_batch_handle(scenarios, params, list_fraction)
-    try:
-        done = C.c_int(0)
-        ms = C.c_float(0.0)
-        _check(m.cal_sciara_batch_run(h, int(steps), C.byref(done), C.byref(ms)), "cal_sciara_batch_run")
-        outs = {k: np.empty_like(z) for k in ("z", "slt", "st", "msl")}
-        _check(m.cal_sciara_batch_read(h, outs["z"].ctypes.data, outs["slt"].ctypes.data, outs["st"].ctypes.data,
-                                       outs["msl"].ctypes.data), "cal_sciara_batch_read")
-    finally:
-        m.cal_sciara_batch_destroy(h)
-    per = {k: _sciara_unpack(scenarios, v) for k, v in outs.items()}
-    res = [{k: per[k][b] for k in per} for b in range(len(scenarios))]
-    return (res, done.value, ms.value) if timing else (res, done.value)
+    with SciaraBatch(scenarios, params=params, list_fraction=list_fraction) as sb:
+        done, ms = sb.run(steps)
+        res = sb.read()
+    return (res, done, ms) if timing else (res, done)
 
 
 def sciara_loss_grad(scenarios, targets, steps=0, *, params=None, list_fraction=0.0, tape_slots=0, timing=False):
@@ -298,22 +367,6 @@ def sciara_loss_grad(scenarios, targets, steps=0, *, params=None, list_fraction=
     every vent and phase (csrc/models/sciara_batch.cu, adjoint with the
     forward's decisions frozen).  Returns (loss[B], [grad_b (nvents_b x
     nphases)]) (and the device milliseconds with timing=True)."""
-    m, h, z, nv, nphases = _sciara_batch_handle(scenarios, params, list_fraction)
-    try:
-        tgt = np.ascontiguousarray(np.concatenate([np.asarray(t, np.float64).ravel() for t in targets]))
-        assert tgt.size == z.size
-        loss = np.zeros(len(scenarios))
-        grad = np.zeros(max(1, nv * nphases))
-        done = C.c_int(0)
-        ms = C.c_float(0.0)
-        _check(m.cal_sciara_batch_loss_grad(h, tgt.ctypes.data, int(steps), loss.ctypes.data, grad.ctypes.data,
-                                            C.byref(done), int(tape_slots), C.byref(ms)),
-               "cal_sciara_batch_loss_grad")
-    finally:
-        m.cal_sciara_batch_destroy(h)
-    grads, pos = [], 0
-    for s in scenarios:
-        k = len(s[1])
-        grads.append(grad[pos * nphases:(pos + k) * nphases].reshape(k, nphases).copy())
-        pos += k
-    return (loss, grads, ms.value) if timing else (loss, grads)
+    with SciaraBatch(scenarios, params=params, list_fraction=list_fraction) as sb:
+        loss, grads, ms = sb.loss_grad(targets, steps, tape_slots=tape_slots)
+    return (loss, grads, ms) if timing else (loss, grads)

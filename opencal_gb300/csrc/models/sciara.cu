@@ -20,10 +20,11 @@
  *     by a one-thread kernel in the steering (so that a recorded step
  *     replays correctly); the host stop condition keeps its own copy,
  *     advanced by the same additions, from the run's step counter.
- * The transcendental functions are CUDA's pow, atan, cos; log10 of the
- * power-law parameters is evaluated once on the host (C library), as in
- * the reference.  Results therefore agree with the reference to rounding
- * (not bit for bit) where pow/atan/cos are involved.
+ * The transcendental parts (power laws, shear test, cooling) use the
+ * equivalent forms of sciara_math.cuh (exp10, no atan / cos, T^3, cbrt);
+ * log10 of the power-law parameters is evaluated once on the host (C
+ * library), as in the reference.  Results therefore agree with the
+ * reference to rounding (not bit for bit) where those are involved.
  */
 #include <math.h>
 #include <stdio.h>
@@ -32,6 +33,8 @@
 
 #include "opencal/cal2D.h"
 #include "opencal/cal2DRun.h"
+
+#include "sciara_math.cuh"
 
 #define SCI_NF 8
 #define SCI_MAX_VENTS 64
@@ -89,16 +92,11 @@ CAL_ELEMENTARY_PROCESS_2D(sciara_vents_emission)(struct CALModel2D* model, int i
     }
 }
 
-static __device__ __forceinline__ double sci_power_law(double k1, double k2, double T)
-{
-    return pow(10.0, k1 + k2 * T);
-}
-
 /* outflowsMin (Sciara.cpp:23-90); f[0..8], f[0] unused */
 static __device__ void sci_outflows_min(struct CALModel2D* model, int i, int j, double* f)
 {
     bool in_set[9];
-    double z[9], h[9], H[9], theta[9];
+    double z[9], h[9], H[9], dz[9];
     const double t = calGet2Dr(model, SQ.St, i, j);
     const double w = SP.Pc;
     const double Pr = sci_power_law(SP.a, SP.b, t);
@@ -106,7 +104,7 @@ static __device__ void sci_outflows_min(struct CALModel2D* model, int i, int j, 
     const double sz0 = calGet2Dr(model, SQ.Sz, i, j);
     for (int k = 0; k < 9; k++) {
         h[k] = calGetX2Dr(model, SQ.Slt, i, j, k);
-        H[k] = f[k] = theta[k] = 0;
+        H[k] = f[k] = dz[k] = 0;
         const double sz = calGetX2Dr(model, SQ.Sz, i, j, k);
         if (k < 5)
             z[k] = sz;
@@ -118,7 +116,7 @@ static __device__ void sci_outflows_min(struct CALModel2D* model, int i, int j, 
     for (int k = 1; k < 9; k++)
         if (z[0] + h[0] > z[k] + h[k]) {
             H[k] = z[k] + h[k];
-            theta[k] = atan(((z[0] + h[0]) - (z[k] + h[k])) / w);
+            dz[k] = (z[0] + h[0]) - (z[k] + h[k]);
             in_set[k] = true;
         } else {
             in_set[k] = false;
@@ -143,7 +141,7 @@ static __device__ void sci_outflows_min(struct CALModel2D* model, int i, int j, 
             }
     } while (loop);
     for (int k = 1; k < 9; k++)
-        if (in_set[k] && h[0] > hc * cos(theta[k]))
+        if (in_set[k] && sci_shear_exceeded(h[0], hc, dz[k], w))
             f[k] = Pr * (avg - H[k]);
 }
 
@@ -196,9 +194,8 @@ CAL_ELEMENTARY_PROCESS_2D(sciara_update_temperature)(struct CALModel2D* model, i
         const double T = st;
         if (h != 0) {
             const double nT = T;
-            const double aus = 1.0 + (3 * pow(nT, 3.0) * SP.Pepsilon * SP.Psigma * SP.Pclock * SP.Pcool) /
-                                         (SP.Prho * SP.Pcv * h * SP.Pac);
-            st = nT / pow(aus, 1.0 / 3.0);
+            double aus;
+            st = sci_cool(nT, h, SP.Pepsilon, SP.Psigma, SP.Pclock, SP.Pcool, SP.Prho, SP.Pcv, SP.Pac, &aus);
             calSet2Dr(model, SQ.St, i, j, st);
         }
         if (st <= SP.PTsol && sh > 0) {

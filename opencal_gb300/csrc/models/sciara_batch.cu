@@ -9,8 +9,8 @@
  *      had no lava joins the lava list.
  *   K1 (flows): empiricalFlows + outflowsMin (Sciara.cpp:18-105) for every
  *      cell of the lava list (Slt > 0), one thread each, spread over the
- *      whole GPU -- the pow / atan / cos and the minimisation are the step's
- *      FP64 work.  The eight outflows of list entry k, and each outflow
+ *      whole GPU -- the power laws, the shear test and the minimisation
+ *      are the step's FP64 work.  The eight outflows of list entry k, and each outflow
  *      times the cell's temperature (the product width_update forms at the
  *      receiver, same operands), go to compact slot k; a per-cell (epoch,
  *      slot) map makes them addressable by cell.  The tiles of the cell and
@@ -23,8 +23,9 @@
  *      reach all of them; a cell outside the flagged tiles has no lava and
  *      no inflow and is unchanged.
  *
- * Arithmetic is the reference's, operation by operation (--fmad=false);
- * pow, atan, cos are CUDA's, as in the device-process program
+ * Arithmetic is the reference's, operation by operation (--fmad=false),
+ * except the transcendental forms of sciara_math.cuh (exp10, the shear test
+ * without atan / cos, T^3 and cbrt), shared with the device-process program
  * (sciara.cu), which this step reproduces bit for bit.  All scenarios share
  * the physical parameters and the emission schedule's length, so they run
  * the same number of steps (the reference stops when the elapsed time
@@ -43,6 +44,8 @@
 
 #include <algorithm>
 #include <vector>
+
+#include "sciara_math.cuh"
 
 namespace sci2 {
 
@@ -63,7 +66,9 @@ struct Inst {
 };
 
 /* counts[]: [0..1] lava list lengths, [4] list parity, [5] K2 ticket,
- * [6] epoch, [7] flagged tiles, [8] overflow flag */
+ * [6] epoch, [7] flagged tiles, [8] lava-list overflow flag, [9] tape
+ * slots used so far (counted on past the capacity), [10] tape overflow
+ * flag */
 struct Dev {
     const Inst* inst;
     const long long* offs;
@@ -186,8 +191,6 @@ __global__ void k_vents(const __grid_constant__ Dev d, double elapsed, double* v
     }
 }
 
-static __device__ __forceinline__ double power_law(double k1, double k2, double t) { return pow(10.0, k1 + k2 * t); }
-
 /* outflowsMin (Sciara.cpp:23-90) at lava cell c, with what its adjoint needs */
 struct Flow {
     double h[9], z[9], H[9], f[9];
@@ -199,13 +202,13 @@ struct Flow {
 
 static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I, long long c, int i, int j, Flow& F)
 {
-    double theta[9];
+    double dz[9];
     bool in_set[9];
     const double t = d.St[c];
     const double w = d.ph.Pc;
     F.t = t;
-    F.Pr = power_law(d.ph.a, d.ph.b, t);
-    const double hc = power_law(d.ph.c, d.ph.d, t);
+    F.Pr = sci_power_law(d.ph.a, d.ph.b, t);
+    const double hc = sci_power_law(d.ph.c, d.ph.d, t);
     const double sz0 = d.Sz[c];
     F.inside = 0;
 #pragma unroll
@@ -214,7 +217,7 @@ static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I
         F.inside |= (in ? 1u : 0u) << q;
         F.h[q] = in ? d.Slt[F.cn[q]] : 0.0;
         const double sz = in ? d.Sz[F.cn[q]] : 0.0;
-        F.H[q] = F.f[q] = theta[q] = 0;
+        F.H[q] = F.f[q] = dz[q] = 0;
         F.z[q] = q < 5 ? sz : sz0 - (sz0 - sz) / d.ph.rad2;
     }
     F.H[0] = F.z[0];
@@ -223,7 +226,7 @@ static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I
     for (int q = 1; q < 9; q++)
         if (F.z[0] + F.h[0] > F.z[q] + F.h[q]) {
             F.H[q] = F.z[q] + F.h[q];
-            theta[q] = atan(((F.z[0] + F.h[0]) - (F.z[q] + F.h[q])) / w);
+            dz[q] = (F.z[0] + F.h[0]) - (F.z[q] + F.h[q]);
             in_set[q] = true;
         } else {
             in_set[q] = false;
@@ -262,7 +265,7 @@ static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I
 #pragma unroll
     for (int q = 1; q < 9; q++) {
         double fq = 0.0;
-        if (in_set[q] && F.h[0] > hc * cos(theta[q]))
+        if (in_set[q] && sci_shear_exceeded(F.h[0], hc, dz[q], w))
             fq = F.Pr * (avg - F.H[q]);
         /* empiricalFlows stores only positive outflows; the rest stay 0 */
         if (!(fq > 0))
@@ -365,9 +368,8 @@ static __device__ __forceinline__ void compute_cell(const Dev& d, const Inst& I,
     Cf.st = t_next;
     if (Cf.lava) {
         const double nT = t_next;
-        Cf.aus = 1.0 + (3 * pow(nT, 3.0) * d.ph.Pepsilon * d.ph.Psigma * d.ph.Pclock * d.ph.Pcool) /
-                           (d.ph.Prho * d.ph.Pcv * h_next * d.ph.Pac);
-        Cf.st = nT / pow(Cf.aus, 1.0 / 3.0);
+        Cf.st = sci_cool(nT, h_next, d.ph.Pepsilon, d.ph.Psigma, d.ph.Pclock, d.ph.Pcool, d.ph.Prho, d.ph.Pcv,
+                         d.ph.Pac, &Cf.aus);
         Cf.solid = Cf.st <= d.ph.PTsol;
     }
 }
@@ -1111,7 +1113,9 @@ extern "C" int cal_sciara_batch_run(void* handle, int max_steps, int* steps_done
  * decisions frozen.  target: host array, the scenarios' grids back to back
  * (unpadded); loss_out[B]; grad_out[nvents x nphases] in the caller's vent
  * order.  tape_slots: undo-tape capacity in tiles summed over the steps
- * (0: twice the scenarios' tiles + 4096).  The state after the call is the
+ * (0: twice the scenarios' tiles + 4096, and when that proves too small,
+ * the forward runs once more with a tape of the size it asked for; a given
+ * tape_slots that is too small is an error).  The state after the call is the
  * run's final one for Slt, St, Sz (Msl is not restored).  0 or a CALError
  * code; ms: device time of forward + adjoint. */
 extern "C" int cal_sciara_batch_loss_grad(void* handle, const double* target, int max_steps, double* loss_out,
@@ -1139,19 +1143,35 @@ extern "C" int cal_sciara_batch_loss_grad(void* handle, const double* target, in
         return true;
     };
     const size_t nb = (size_t)bt->N * sizeof(double);
-    bool ok = alloc((void**)&tp.tile, sizeof(int) * cap) && alloc((void**)&tp.state, sizeof(double) * 3 * tile_cells * cap) &&
-              alloc((void**)&tp.step_base, sizeof(int) * (steps + 1)) &&
+    bool ok = alloc((void**)&tp.step_base, sizeof(int) * (steps + 1)) &&
               alloc((void**)&tp.step_count, sizeof(int) * (steps + 1)) &&
               alloc((void**)&vtape, sizeof(double) * 3 * std::max(1, bt->nvents) * (size_t)steps) &&
               alloc((void**)&tgt, nb) && alloc((void**)&dloss, sizeof(double) * bt->B) &&
               alloc((void**)&a.lh, nb) && alloc((void**)&a.lt, nb) && alloc((void**)&a.lz, nb) &&
               alloc((void**)&a.grad, sizeof(double) * std::max(1, bt->nvents * bt->nphases));
-    auto release = [&]() {
+    auto free_tape = [&]() {
         cudaStreamSynchronize(st);
+        cudaFree(tp.tile);
+        cudaFree(tp.state);
+        tp.tile = nullptr;
+        tp.state = nullptr;
+    };
+    auto alloc_tape = [&](long long slots) {
+        tp.cap = slots;
+        if (cudaMalloc((void**)&tp.tile, sizeof(int) * slots) != cudaSuccess ||
+            cudaMalloc((void**)&tp.state, sizeof(double) * 3 * tile_cells * slots) != cudaSuccess) {
+            cudaGetLastError();
+            free_tape();
+            return false;
+        }
+        return true;
+    };
+    auto release = [&]() {
+        free_tape();
         for (void* p : mem)
             cudaFree(p);
     };
-    if (!ok) {
+    if (!ok || !alloc_tape(cap)) {
         release();
         return 2; /* CAL_ERROR_OUT_OF_MEMORY */
     }
@@ -1162,8 +1182,30 @@ extern "C" int cal_sciara_batch_loss_grad(void* handle, const double* target, in
     std::vector<double> elapsed_of;
     int done = 0;
     int rc = sci2::forward(bt, max_steps, &tp, vtape, &elapsed_of, &done, nullptr);
+    if (rc == 2 && tape_slots <= 0) {
+        /* the default tape was too small but the lava list was not: the
+         * forward counted every slot it wanted, so run it again once with
+         * a tape of exactly that size */
+        int c[3] = {0, 0, 0};
+        cudaMemcpy(c, d.counts + 8, sizeof(c), cudaMemcpyDeviceToHost);
+        if (!c[0] && c[2] && c[1] > cap) {
+            const long long need = c[1];
+            free_tape();
+            if (!alloc_tape(need)) {
+                release();
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return 2;
+            }
+            elapsed_of.clear();
+            cudaEventRecord(e0, st);
+            rc = sci2::forward(bt, max_steps, &tp, vtape, &elapsed_of, &done, nullptr);
+        }
+    }
     if (rc) {
         release();
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
         return rc;
     }
     /* target in the padded layout */

@@ -215,3 +215,28 @@ def sciara_inputs(rows: int, cols: int, seed: int = 5, cell: float = 10.0, nvent
             vents.append((vj, vi))
     rates = [[rng.uniform(*rate_range) for _ in range(phases)] for _ in range(nvents)]
     return np.ascontiguousarray(z), vents, rates
+
+
+def sciara_scenarios(count: int, rows: int, cols: int, seed: int = 5, dems: int = 8, phases: int = 6,
+                     emission_time: int = 3600):
+    """``count`` SCIARA-fv2 scenarios for hazard mapping: ``dems`` synthetic
+    volcanoes (sciara_inputs with seeds seed .. seed + dems - 1), scenario k
+    on volcano k % dems with its own 1-3 vents near the summit and emission
+    rates (SplitMix64 seeded by seed * 1009 + k).  Scenarios on the same
+    volcano share its elevation array (read-only).  Returns [(z, vents,
+    rates, emission_time)]."""
+    zs = [sciara_inputs(rows, cols, seed=seed + d, phases=phases)[0] for d in range(min(dems, count))]
+    ci, cj = (rows - 1) / 2.0, (cols - 1) / 2.0
+    spread = max(1.0, min(rows, cols) / 16.0)
+    out = []
+    for k in range(count):
+        rng = SplitMix64(seed * 1009 + k)
+        nv = 1 + int(rng.next_u64() % 3)
+        vents = []
+        while len(vents) < nv:
+            v = (int(round(cj + rng.uniform(-spread, spread))), int(round(ci + rng.uniform(-spread, spread))))
+            if v not in vents:
+                vents.append(v)
+        rates = [[rng.uniform(10.0, 50.0) for _ in range(phases)] for _ in range(nv)]
+        out.append((zs[k % len(zs)], vents, rates, emission_time))
+    return out

@@ -4,9 +4,11 @@ device processes behind the C API) against the reference's own program
 and against the oracle.
 
 The reference calls the C library's pow, atan and cos; the GPU program
-calls CUDA's, which may differ in the last bit.  So the comparison with the
-reference is to a tolerance, stated below, while everything that does not
-involve those functions is exact: the border mask, the step count at which
+evaluates the same quantities by identities that suit its FP64 pipe
+(csrc/models/sciara_math.cuh: exp10, the shear test without atan / cos, T^3,
+cbrt), which differ from the C library's in the last bits.  So the
+comparison with the reference is to a tolerance, stated below, while
+everything that does not involve those functions is exact: the border mask, the step count at which
 the emission ends, active cells on == active cells off (bit for bit on the
 GPU, as in the reference), and a recorded-step replay == the launch
 sequence."""
@@ -20,7 +22,7 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # relative tolerance per cell on thickness, temperature, altitude and
 # solidified thickness after the whole run (cells above 1e-9 of the field's
-# maximum); the transcendental functions differ in the last bit
+# maximum); the transcendental parts differ in the last bits
 RTOL = 1e-10
 
 

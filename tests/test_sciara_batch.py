@@ -1,7 +1,8 @@
 """SCIARA-fv2 split step (csrc/models/sciara_batch.cu): one scenario
 reproduces the device-process program (csrc/models/sciara.cu, the
 reference's elementary processes behind the C API) bit for bit -- both use
-CUDA's pow / atan / cos with the reference's operation order -- and a batch
+the transcendental forms of csrc/models/sciara_math.cuh and the reference's
+operation order -- and a batch
 of scenarios with uneven grids reproduces each scenario run alone.  Against
 the oracle (the C library's transcendental functions) the tolerance of
 test_sciara.py applies.  A lava list too small for the flow is reported as
@@ -13,7 +14,7 @@ from opencal_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-10  # as tests/test_sciara.py: pow / atan / cos of CUDA vs the C library
+RTOL = 1e-10  # as tests/test_sciara.py: the GPU's transcendental forms vs the C library
 
 
 @pytest.fixture(scope="module")
@@ -70,6 +71,23 @@ def test_list_overflow_is_an_error(cal):
     sc = _scenario(160, 160, 31, 3600)
     with pytest.raises(cal.CALError):
         cal.sciara_batch([sc], 200, list_fraction=1e-9)
+
+
+def test_undo_tape_grows_to_the_run(cal):
+    """Four small grids (6 tiles each) over the whole emission (360 steps)
+    flag more tiles than the default tape holds (2 x 24 + 4096): the call
+    reruns the forward with the size it counted and matches a generous
+    explicit tape; an explicit tape that is too small is an error."""
+    scs = [_scenario(48, 64, 41 + k, 3600) for k in range(4)]
+    targets = [np.zeros((48, 64)) for _ in scs]
+    loss_d, g_d = cal.sciara_loss_grad(scs, targets)
+    loss_e, g_e = cal.sciara_loss_grad(scs, targets, tape_slots=200000)
+    # loss and gradients are sums by double atomics: equal up to their order
+    np.testing.assert_allclose(loss_d, loss_e, rtol=1e-12)
+    for a, b in zip(g_d, g_e):
+        np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-14)
+    with pytest.raises(cal.CALError):
+        cal.sciara_loss_grad(scs, targets, tape_slots=16)
 
 
 def _loss(cal, sc, target):
