@@ -277,56 +277,63 @@ extern "C" int cal_life3d_run(int rows, int cols, int slices, int nbhd, int toro
 /* ======================= exact small-integer division check ============= */
 #include "exact_div.cuh"
 
-__global__ void exact_div_kernel(const double* x, const int* c, const double* y, double* q_exact, double* q_ieee,
-                                 int* le_exact, int* le_ieee, long long n)
+__global__ void exact_div_kernel(const double* x, const int* c, const double* y, double b, double rb, double* q_exact,
+                                 double* q_ieee, double* r_exact, double* r_ieee, int* le_exact, int* le_ieee,
+                                 long long n)
 {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         q_exact[t] = cal_div_small(x[t], c[t]);
         q_ieee[t] = x[t] / (double)c[t];
-        le_exact[t] = cal_le(x[t], y[t]);
-        le_ieee[t] = x[t] <= y[t];
+        r_exact[t] = cal_div_recip(x[t], b, rb);
+        r_ieee[t] = x[t] / b;
+        le_exact[t] = (int)cal_le(x[t], y[t]) | (int)cal_gt(x[t], y[t]) << 1 | (int)cal_pos(x[t]) << 2;
+        le_ieee[t] = (int)(x[t] <= y[t]) | (int)(x[t] > y[t]) << 1 | (int)(x[t] > 0) << 2;
     }
 }
 
+static bool same_bits(double a, double b)
+{
+    return memcmp(&a, &b, sizeof(double)) == 0 || (a != a && b != b);
+}
+
 /* Device-side check of exact_div.cuh against the device's own IEEE
- * division and comparison; returns the number of mismatches. */
+ * division and comparisons: x / c (c in 1..9), x / b by the reciprocal
+ * method (b = sqrt(2), the SCIARA-fv2 diagonal divisor), <=, > and > 0;
+ * returns the number of mismatches (-1: CUDA error, -2: the reciprocal
+ * method's precondition does not hold for b). */
 extern "C" long cal_test_exact_div(const double* x_host, const int* c_host, const double* y_host, long long n)
 {
-    double *x, *y, *qe, *qi;
+    const double b = sqrt(2.0), rb = 1.0 / b;
+    if (!cal_recip_exact_ok(b, rb))
+        return -2;
+    double *x, *y, *buf;
     int *c, *le, *li;
     cudaMalloc(&x, n * sizeof(double));
     cudaMalloc(&y, n * sizeof(double));
-    cudaMalloc(&qe, n * sizeof(double));
-    cudaMalloc(&qi, n * sizeof(double));
+    cudaMalloc(&buf, 4 * n * sizeof(double));
     cudaMalloc(&c, n * sizeof(int));
     cudaMalloc(&le, n * sizeof(int));
     cudaMalloc(&li, n * sizeof(int));
     cudaMemcpy(x, x_host, n * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(y, y_host, n * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(c, c_host, n * sizeof(int), cudaMemcpyHostToDevice);
-    exact_div_kernel<<<1024, 256>>>(x, c, y, qe, qi, le, li, n);
-    double* hqe = (double*)malloc(n * sizeof(double));
-    double* hqi = (double*)malloc(n * sizeof(double));
+    exact_div_kernel<<<1024, 256>>>(x, c, y, b, rb, buf, buf + n, buf + 2 * n, buf + 3 * n, le, li, n);
+    double* hq = (double*)malloc(4 * n * sizeof(double));
     int* hle = (int*)malloc(n * sizeof(int));
     int* hli = (int*)malloc(n * sizeof(int));
-    cudaMemcpy(hqe, qe, n * sizeof(double), cudaMemcpyDeviceToHost);
-    cudaMemcpy(hqi, qi, n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(hq, buf, 4 * n * sizeof(double), cudaMemcpyDeviceToHost);
     cudaMemcpy(hle, le, n * sizeof(int), cudaMemcpyDeviceToHost);
     cudaMemcpy(hli, li, n * sizeof(int), cudaMemcpyDeviceToHost);
     long bad = cudaGetLastError() == cudaSuccess ? 0 : -1;
-    for (long long t = 0; bad >= 0 && t < n; t++) {
-        const bool nan_both = hqe[t] != hqe[t] && hqi[t] != hqi[t];
-        if ((memcmp(&hqe[t], &hqi[t], sizeof(double)) != 0 && !nan_both) || hle[t] != hli[t])
+    for (long long t = 0; bad >= 0 && t < n; t++)
+        if (!same_bits(hq[t], hq[n + t]) || !same_bits(hq[2 * n + t], hq[3 * n + t]) || hle[t] != hli[t])
             bad++;
-    }
-    free(hqe);
-    free(hqi);
+    free(hq);
     free(hle);
     free(hli);
     cudaFree(x);
     cudaFree(y);
-    cudaFree(qe);
-    cudaFree(qi);
+    cudaFree(buf);
     cudaFree(c);
     cudaFree(le);
     cudaFree(li);

@@ -10,18 +10,20 @@
  *   K1 (flows): empiricalFlows + outflowsMin (Sciara.cpp:18-105) for every
  *      cell of the lava list (Slt > 0), one thread each, spread over the
  *      whole GPU -- the power laws, the shear test and the minimisation
- *      are the step's FP64 work.  The eight outflows of list entry k, and each outflow
- *      times the cell's temperature (the product width_update forms at the
- *      receiver, same operands), go to compact slot k; a per-cell (epoch,
- *      slot) map makes them addressable by cell.  The tiles of the cell and
- *      of every receiver are flagged (epoch stamps) and listed once.
+ *      are the step's FP64 work.  The eight outflows of list entry k, and
+ *      each outflow times the cell's temperature (the product width_update
+ *      forms at the receiver, same operands), go to compact slot k; a
+ *      per-cell (epoch, slot) map makes them addressable by cell.  A
+ *      receiver without lava joins the receiver list once (epoch stamp).
  *   K2 (update): width_update, updateTemperature and the steering's border
- *      reset (Sciara.cpp:106-169, 185-193) on every cell of the flagged
- *      tiles, in place: each cell reads only its own state and the compact
- *      outflows; it joins the next lava list if it still holds lava.
- *      Every lava cell's tile is flagged, so cooling and solidification
- *      reach all of them; a cell outside the flagged tiles has no lava and
- *      no inflow and is unchanged.
+ *      reset (Sciara.cpp:106-169, 185-193) at every lava cell and every
+ *      receiver, one thread each over the whole GPU, in place: a cell reads
+ *      only its own state and the compact outflows; it joins the next lava
+ *      list if it still holds lava.  Any other cell has no lava and no
+ *      inflow, so it is unchanged (border cells hold 0 from the start).
+ *   For the adjoint, K1 also flags the 32 x 16 tiles of the lava cells and
+ *   receivers, and a tape kernel between K1 and K2 copies those tiles'
+ *   state before the update.
  *
  * Arithmetic is the reference's, operation by operation (--fmad=false),
  * except the transcendental forms of sciara_math.cuh (exp10, the shear test
@@ -32,10 +34,11 @@
  * reaches the emission's end).
  *
  * Layout: scenarios packed back to back (offsets padded to 32 cells); per
- * cell Sz, Slt, St, Msl (FP64), Mb (byte), the (epoch, slot) map (8 B),
- * two list entries (8 B) and a copy of the initial Sz, Slt, St (every run
- * starts from it): ~73 B per cell; outflows only per lava cell (128 B per
- * list slot, capacity chosen at creation).
+ * cell Sz, Slt, St, Msl (FP64), Mb (byte), the (epoch, slot) map (8 B), the
+ * receiver stamp (4 B) and a copy of the initial Sz, Slt, St (every run
+ * starts from it): 69 B per cell; per list slot (capacity chosen at
+ * creation) two lava-list entries, a receiver entry and the outflows
+ * (140 B).
  */
 #include <math.h>
 #include <stdio.h>
@@ -45,6 +48,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "exact_div.cuh"
 #include "sciara_math.cuh"
 
 namespace sci2 {
@@ -57,6 +61,8 @@ constexpr int MAX_INST = 1024;
 
 struct Phys {
     double Pclock, Pc, Pac, PTsol, PTvent, a, b, c, d, Pcool, Prho, Pepsilon, Psigma, Pcv, rad2;
+    double rrad2, w2; /* RN(1 / rad2), Pc * Pc */
+    int rad2_recip;   /* x / rad2 by cal_div_recip (its precondition holds) */
 };
 
 struct Inst {
@@ -65,10 +71,11 @@ struct Inst {
     int tiles_x, tiles_y, tile0, pad;
 };
 
-/* counts[]: [0..1] lava list lengths, [4] list parity, [5] K2 ticket,
- * [6] epoch, [7] flagged tiles, [8] lava-list overflow flag, [9] tape
+/* counts[]: [0] lava list length, [5] K2 ticket, [6] epoch, [7] tiles
+ * flagged in this step, [8] lava- or receiver-list overflow flag, [9] tape
  * slots used so far (counted on past the capacity), [10] tape overflow
- * flag */
+ * flag, [11] receiver list length, [12] tiles flagged in the previous step,
+ * [13] lava cells after the last update */
 struct Dev {
     const Inst* inst;
     const long long* offs;
@@ -80,8 +87,10 @@ struct Dev {
     const unsigned char* Mb;
     double* fc;   /* 16 doubles per list slot: f[8], f * St[8] */
     int2* map;    /* per cell: (epoch, slot) */
-    int* list0;
-    int* list1;
+    int* recv;    /* per cell: epoch in which it was listed as a receiver */
+    int* rlist;   /* cells without lava that receive a flow this step */
+    int* list;    /* lava cells, tile by tile, row-major within a tile */
+    unsigned* mask; /* per tile 16 words: bit j of word r = cell (r, j) holds lava after K2 */
     int* counts;
     int* tflag;
     int* tlist;
@@ -90,7 +99,7 @@ struct Dev {
     int nvents;
     const int* vent_cell;  /* packed cell index of each vent */
     const int* vent_first; /* B + 1: vents of instance b are [vent_first[b], vent_first[b + 1]) */
-    const double* rates;   /* nvents x nphases */
+    const double* emit;    /* nvents x nphases: rate / Pac * Pclock, the thickness a vent adds per step */
     int nphases;
     unsigned emission_time;
     Phys ph;
@@ -137,57 +146,116 @@ static __device__ __forceinline__ void flag_tile(const Dev& d, int t, int epoch)
         d.tlist[atomicAdd(d.counts + 7, 1)] = t;
 }
 
-/* K0: vent emission, one thread per scenario; empties the next lava list.
- * With a vent tape (one record of 3 doubles per vent and step) the first
- * vent of each cell records the cell's thickness and temperature before the
- * emission and which vent's emission took effect. */
-__global__ void k_vents(const __grid_constant__ Dev d, double elapsed, double* vtape)
+/* K0: the lava list of this step, and the vent emission.
+ * The list is collected from the lava masks K2 left in the tiles flagged by
+ * the previous step (every cell that can hold lava after an update lies in
+ * one), tile by tile and row-major within a tile, so that neighbouring list
+ * entries are neighbouring cells; the masks are cleared on the way.  Half a
+ * warp reads a tile's 16 mask words and reserves the tile's run of list
+ * slots with one atomic.  (The first step uses the list the priming kernel
+ * built.)  Block 0 also emits at the vents, one thread per scenario; a
+ * vent cell that had no lava is appended.  With a vent tape (one record of
+ * 3 doubles per vent and step) the first vent of each cell records the
+ * cell's thickness and temperature before the emission and which vent's
+ * emission took effect. */
+__global__ void __launch_bounds__(T) k_collect(const __grid_constant__ Dev d, unsigned phase, double* vtape,
+                                               int rebuild)
 {
-    const int par = d.counts[4];
-    int* list = par ? d.list1 : d.list0;
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        d.counts[1 - par] = 0;
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= d.B)
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0)
+            d.counts[13] = 0;
+        for (int b = threadIdx.x; b < d.B; b += blockDim.x) {
+            const int v0 = d.vent_first[b], v1 = d.vent_first[b + 1];
+            for (int v = v0; v < v1; v++) {
+                const int c = d.vent_cell[v];
+                /* the process reads the current thickness: every vent of a
+                 * cell adds to the value before this step's emission */
+                bool first = true;
+                for (int w = v0; w < v; w++)
+                    if (d.vent_cell[w] == c) {
+                        first = false; /* handled with the first vent of this cell */
+                        break;
+                    }
+                if (!first) {
+                    if (vtape)
+                        vtape[3 * v + 2] = -2.0;
+                    continue;
+                }
+                const double orig = d.Slt[c];
+                const double orig_t = d.St[c];
+                int eff = -1;
+                for (int w = v; w < v1; w++) {
+                    if (d.vent_cell[w] != c)
+                        continue;
+                    const double emitted = phase >= (unsigned)d.nphases ? 0.0 : d.emit[(size_t)w * d.nphases + phase];
+                    if (emitted > 0) {
+                        d.Slt[c] = orig + emitted;
+                        d.St[c] = d.ph.PTvent;
+                        eff = w;
+                    }
+                }
+                if (vtape) {
+                    vtape[3 * v] = orig;
+                    vtape[3 * v + 1] = orig_t;
+                    vtape[3 * v + 2] = (double)eff;
+                }
+                if (eff >= 0 && !(orig > 0))
+                    append(d.list, d.counts + 0, d.capacity, d.counts + 8, c);
+            }
+        }
+    }
+    if (!rebuild)
         return;
-    const unsigned phase = (unsigned)(elapsed / d.emission_time);
-    const int v0 = d.vent_first[b], v1 = d.vent_first[b + 1];
-    for (int v = v0; v < v1; v++) {
-        const int c = d.vent_cell[v];
-        /* the process reads the current thickness: every vent of a cell adds
-         * to the value before this step's emission */
-        bool first = true;
-        for (int w = v0; w < v; w++)
-            if (d.vent_cell[w] == c) {
-                first = false; /* handled with the first vent of this cell */
-                break;
+    const int ntiles = d.counts[12];
+    const int lane = threadIdx.x & 31, half = lane >> 4, l = lane & 15;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int item0 = 2 * warp; item0 < ntiles; item0 += 2 * nwarps) {
+        const int item = item0 + half;
+        unsigned w = 0;
+        int t = 0;
+        if (item < ntiles) {
+            t = d.tlist[item];
+            w = d.mask[(size_t)t * 16 + l];
+            if (w)
+                d.mask[(size_t)t * 16 + l] = 0;
+        }
+        const int cnt = __popc(w);
+        int inc = cnt; /* inclusive scan over the half warp */
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, o, 16);
+            if (l >= o)
+                inc += v;
+        }
+        int base = 0;
+        if (l == 15 && inc > 0)
+            base = atomicAdd(d.counts + 0, inc);
+        base = __shfl_sync(0xffffffffu, base, 15, 16);
+        if (w) {
+            int lo = 0, hi = d.B - 1; /* the tile's instance: largest b with tile0 <= t */
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (d.inst[mid].tile0 <= t)
+                    lo = mid;
+                else
+                    hi = mid - 1;
             }
-        if (!first) {
-            if (vtape)
-                vtape[3 * v + 2] = -2.0;
-            continue;
-        }
-        const double orig = d.Slt[c];
-        const double orig_t = d.St[c];
-        int eff = -1;
-        for (int w = v; w < v1; w++) {
-            if (d.vent_cell[w] != c)
-                continue;
-            const double emitted = phase >= (unsigned)d.nphases ? 0.0
-                                                                : d.rates[(size_t)w * d.nphases + phase] / d.ph.Pac * d.ph.Pclock;
-            if (emitted > 0) {
-                d.Slt[c] = orig + emitted;
-                d.St[c] = d.ph.PTvent;
-                eff = w;
+            const Inst I = d.inst[lo];
+            const int lt = t - I.tile0;
+            const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
+            const long long row = I.off + (long long)(ty * TH + l) * I.cols + tx * TW;
+            int pos = base + inc - cnt;
+            while (w) {
+                const int bit = __ffs(w) - 1;
+                w &= w - 1;
+                if (pos < d.capacity)
+                    d.list[pos] = (int)(row + bit);
+                else
+                    atomicExch(d.counts + 8, 1);
+                pos++;
             }
         }
-        if (vtape) {
-            vtape[3 * v] = orig;
-            vtape[3 * v + 1] = orig_t;
-            vtape[3 * v + 2] = (double)eff;
-        }
-        if (eff >= 0 && !(orig > 0))
-            append(list, d.counts + par, d.capacity, d.counts + 8, c);
     }
 }
 
@@ -200,16 +268,23 @@ struct Flow {
     int nS;
 };
 
+/* The arithmetic of outflowsMin with every FP64 operation that can leave
+ * the narrow FP64 pipe moved to the integer pipe, each with identical
+ * results (exact_div.cuh): comparisons of non-negative values on the bit
+ * patterns; z0 + h0 > z_k + h_k as the sign of their difference (for finite
+ * values, a - b > 0 exactly when a > b); the average's division by the set
+ * size (1..9) by integer long division; the diagonal altitude's division by
+ * rad2 through its reciprocal with Markstein's correction. */
 static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I, long long c, int i, int j, Flow& F)
 {
     double dz[9];
     bool in_set[9];
     const double t = d.St[c];
-    const double w = d.ph.Pc;
     F.t = t;
     F.Pr = sci_power_law(d.ph.a, d.ph.b, t);
     const double hc = sci_power_law(d.ph.c, d.ph.d, t);
     const double sz0 = d.Sz[c];
+    const bool recip = d.ph.rad2_recip != 0;
     F.inside = 0;
 #pragma unroll
     for (int q = 0; q < 9; q++) {
@@ -218,19 +293,24 @@ static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I
         F.h[q] = in ? d.Slt[F.cn[q]] : 0.0;
         const double sz = in ? d.Sz[F.cn[q]] : 0.0;
         F.H[q] = F.f[q] = dz[q] = 0;
-        F.z[q] = q < 5 ? sz : sz0 - (sz0 - sz) / d.ph.rad2;
+        if (q < 5)
+            F.z[q] = sz;
+        else
+            F.z[q] = sz0 - (recip ? cal_div_recip(sz0 - sz, d.ph.rad2, d.ph.rrad2) : (sz0 - sz) / d.ph.rad2);
     }
     F.H[0] = F.z[0];
     in_set[0] = true;
+    const double zh0 = F.z[0] + F.h[0];
 #pragma unroll
-    for (int q = 1; q < 9; q++)
-        if (F.z[0] + F.h[0] > F.z[q] + F.h[q]) {
-            F.H[q] = F.z[q] + F.h[q];
-            dz[q] = (F.z[0] + F.h[0]) - (F.z[q] + F.h[q]);
-            in_set[q] = true;
-        } else {
-            in_set[q] = false;
+    for (int q = 1; q < 9; q++) {
+        const double Hq = F.z[q] + F.h[q];
+        const double dq = zh0 - Hq;
+        in_set[q] = cal_pos(dq);
+        if (in_set[q]) {
+            F.H[q] = Hq;
+            dz[q] = dq;
         }
+    }
     bool loop;
     double avg;
     int counter;
@@ -245,10 +325,10 @@ static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I
                 counter++;
             }
         if (counter != 0)
-            avg = avg / (double)counter;
+            avg = cal_div_small(avg, counter);
 #pragma unroll
         for (int q = 0; q < 9; q++)
-            if (in_set[q] && avg <= F.H[q]) {
+            if (in_set[q] && cal_le(avg, F.H[q])) {
                 in_set[q] = false;
                 loop = true;
             }
@@ -262,33 +342,39 @@ static __device__ __forceinline__ void compute_flows(const Dev& d, const Inst& I
 #pragma unroll
     for (int q = 0; q < 9; q++)
         F.S |= (in_set[q] ? 1u : 0u) << q;
+    const double h0 = F.h[0];
+    const double h0sq = h0 * h0, rhs = hc * hc * d.ph.w2;
 #pragma unroll
     for (int q = 1; q < 9; q++) {
         double fq = 0.0;
-        if (in_set[q] && sci_shear_exceeded(F.h[0], hc, dz[q], w))
+        /* sci_shear_exceeded(h0, hc, dz, w): h0 > 0 and h0^2 (w^2 + dz^2) > hc^2 w^2 */
+        if (in_set[q] && cal_pos(h0) && cal_gt(h0sq * (d.ph.w2 + dz[q] * dz[q]), rhs))
             fq = F.Pr * (avg - F.H[q]);
         /* empiricalFlows stores only positive outflows; the rest stay 0 */
-        if (!(fq > 0))
+        if (!cal_pos(fq))
             fq = 0.0;
         F.f[q] = fq;
-        if (fq > 0)
+        if (cal_pos(fq))
             F.F |= 1u << q;
     }
 }
 
-/* K1: outflows of every lava cell into compact slots; tiles flagged */
+/* K1: outflows of every lava cell into compact slots.  A receiver without
+ * lava joins the receiver list once (epoch stamp), so that K2 visits
+ * exactly the lava cells and the cells they flow into.  The tiles of the
+ * lava cells and receivers are flagged: they hold every cell that can hold
+ * lava after K2 (K0 of the next step collects the list from them) and every
+ * cell the step changes besides the vents (the tape copies them). */
 __global__ void __launch_bounds__(K1T) k_flows(const __grid_constant__ Dev d)
 {
     __shared__ long long s_offs[MAX_INST + 1];
     for (int k = threadIdx.x; k <= d.B; k += blockDim.x)
         s_offs[k] = d.offs[k];
     __syncthreads();
-    const int par = d.counts[4];
     const int epoch = d.counts[6];
-    const int* list = par ? d.list1 : d.list0;
-    const int n = min(d.counts[par], d.capacity);
+    const int n = min(d.counts[0], d.capacity);
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int c = list[k];
+        const int c = d.list[k];
         const Inst I = d.inst[locate(s_offs, d.B, c)];
         const long long lc = c - I.off;
         const int i = (int)(lc / I.cols), j = (int)(lc - (long long)i * I.cols);
@@ -300,13 +386,17 @@ __global__ void __launch_bounds__(K1T) k_flows(const __grid_constant__ Dev d)
             slot[q - 1] = F.f[q];
             slot[8 + q - 1] = F.f[q] * F.t;
             if ((F.F >> q) & (F.inside >> q) & 1u) {
-                const long long rc = F.cn[q] - I.off;
-                const int ri = (int)(rc / I.cols), rj = (int)(rc - (long long)ri * I.cols);
-                flag_tile(d, I.tile0 + (ri / TH) * I.tiles_x + rj / TW, epoch);
+                const int cn = (int)F.cn[q];
+                if (!cal_pos(F.h[q]) && d.recv[cn] != epoch && atomicExch(d.recv + cn, epoch) != epoch) {
+                    append(d.rlist, d.counts + 11, d.capacity, d.counts + 8, cn);
+                    const long long rc = F.cn[q] - I.off;
+                    const int ri = (int)(rc / I.cols), rj = (int)(rc - (long long)ri * I.cols);
+                    flag_tile(d, I.tile0 + (ri / TH) * I.tiles_x + rj / TW, epoch);
+                }
             }
         }
         d.map[c] = make_int2(epoch, k);
-        flag_tile(d, I.tile0 + (i / TH) * I.tiles_x + j / TW, epoch); /* cooling reaches every lava cell */
+        flag_tile(d, I.tile0 + (i / TH) * I.tiles_x + j / TW, epoch);
     }
 }
 
@@ -411,19 +501,17 @@ struct Tape {
     long long cap;    /* slots */
 };
 
-/* K2: every cell of the flagged tiles; the next lava list; the tape */
-__global__ void __launch_bounds__(T) k_update(const __grid_constant__ Dev d, const __grid_constant__ Tape tp, int step)
+/* With a tape: every cell of the flagged tiles, (Slt, St, Sz) before the
+ * update, into the tape slot of the tile.  The flagged tiles hold every
+ * cell K0 and K2 change in this step besides the vent cells, which the
+ * vent tape records. */
+__global__ void __launch_bounds__(T) k_tape(const __grid_constant__ Dev d, const __grid_constant__ Tape tp)
 {
-    const int par = d.counts[4];
-    const int epoch = d.counts[6];
     const int ntiles = d.counts[7];
     const int base = d.counts[9];
-    int* next = par ? d.list0 : d.list1;
-    int* ncount = d.counts + (1 - par);
     for (int item = blockIdx.x; item < ntiles; item += gridDim.x) {
         const int t = d.tlist[item];
-        /* the tile's instance: largest b with tile0 <= t */
-        int lo = 0, hi = d.B - 1;
+        int lo = 0, hi = d.B - 1; /* the tile's instance: largest b with tile0 <= t */
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (d.inst[mid].tile0 <= t)
@@ -435,55 +523,77 @@ __global__ void __launch_bounds__(T) k_update(const __grid_constant__ Dev d, con
         const int lt = t - I.tile0;
         const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
         const long long slot = (long long)base + item;
-        const bool taping = tp.state && slot < tp.cap;
-        if (tp.state && !taping && threadIdx.x == 0)
-            atomicExch(d.counts + 10, 1);
-        if (taping && threadIdx.x == 0)
+        if (slot >= tp.cap) {
+            if (threadIdx.x == 0)
+                atomicExch(d.counts + 10, 1);
+            continue;
+        }
+        if (threadIdx.x == 0)
             tp.tile[slot] = t;
+        double* s = tp.state + (size_t)slot * 3 * TW * TH;
         for (int q = threadIdx.x; q < TW * TH; q += T) {
             const int i = ty * TH + q / TW, j = tx * TW + q % TW;
-            bool lava = false;
-            long long x = 0;
             if (i < I.rows && j < I.cols) {
-                x = I.off + (long long)i * I.cols + j;
-                if (taping) {
-                    double* s = tp.state + (size_t)slot * 3 * TW * TH;
-                    s[q] = d.Slt[x];
-                    s[TW * TH + q] = d.St[x];
-                    s[2 * TW * TH + q] = d.Sz[x];
-                }
-                lava = update_cell(d, I, i, j, epoch);
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, lava);
-            if (m) {
-                const int lane = threadIdx.x & 31;
-                int b = 0;
-                if (lane == 0)
-                    b = atomicAdd(ncount, __popc(m));
-                b = __shfl_sync(0xffffffffu, b, 0);
-                if (lava) {
-                    const int pos = b + __popc(m & ((1u << lane) - 1u));
-                    if (pos < d.capacity)
-                        next[pos] = (int)x;
-                    else
-                        atomicExch(d.counts + 8, 1);
-                }
+                const long long x = I.off + (long long)i * I.cols + j;
+                s[q] = d.Slt[x];
+                s[TW * TH + q] = d.St[x];
+                s[2 * TW * TH + q] = d.Sz[x];
             }
         }
+    }
+}
+
+/* K2: width_update, updateTemperature and the border reset at every lava
+ * cell and every receiver (the only cells whose state can change: any
+ * other cell has no lava and no inflow, so h + (0 - 0) = h and the
+ * temperature stays; border cells hold 0 from the start); one thread per
+ * cell over the whole GPU; a cell that still holds lava sets its bit in
+ * its tile's mask.  The last block to finish advances the step's
+ * counters. */
+__global__ void __launch_bounds__(K1T) k_update(const __grid_constant__ Dev d, const __grid_constant__ Tape tp,
+                                                int step)
+{
+    __shared__ long long s_offs[MAX_INST + 1];
+    for (int k = threadIdx.x; k <= d.B; k += blockDim.x)
+        s_offs[k] = d.offs[k];
+    __syncthreads();
+    const int epoch = d.counts[6];
+    const int nl = min(d.counts[0], d.capacity);
+    const int n = nl + min(d.counts[11], d.capacity);
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int k0 = blockIdx.x * blockDim.x; k0 < n; k0 += stride) {
+        const int k = k0 + threadIdx.x;
+        bool lava = false;
+        if (k < n) {
+            const int c = k < nl ? d.list[k] : d.rlist[k - nl];
+            const Inst I = d.inst[locate(s_offs, d.B, c)];
+            const long long lc = c - I.off;
+            const int i = (int)(lc / I.cols), j = (int)(lc - (long long)i * I.cols);
+            lava = update_cell(d, I, i, j, epoch);
+            if (lava)
+                atomicOr(d.mask + (size_t)(I.tile0 + (i / TH) * I.tiles_x + j / TW) * 16 + (i % TH), 1u << (j % TW));
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, lava);
+        if (m && lane == 0)
+            atomicAdd(d.counts + 13, __popc(m));
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(reinterpret_cast<unsigned*>(d.counts + 5), 1u) == gridDim.x - 1) {
             if (tp.state) {
+                const int ntiles = d.counts[7], base = d.counts[9];
                 tp.step_base[step] = base;
                 tp.step_count[step] = ntiles;
                 d.counts[9] = base + ntiles;
             }
-            d.counts[4] = 1 - par;
+            d.counts[0] = 0; /* K0 of the next step collects the list from the masks */
             d.counts[5] = 0;
             d.counts[6] = epoch + 1;
+            d.counts[12] = d.counts[7];
             d.counts[7] = 0;
+            d.counts[11] = 0;
         }
     }
 }
@@ -796,6 +906,8 @@ __global__ void k_prime(const __grid_constant__ Dev d)
                 if (border) {
                     d.Slt[c] = 0;
                     d.St[c] = 0;
+                } else if (cal_d2i(d.Slt[c]) == (long long)0x8000000000000000LL) {
+                    d.Slt[c] = 0; /* -0 thickness: the first update would make it +0 */
                 }
                 lava = !border && d.Slt[c] > 0;
             } else {
@@ -812,7 +924,7 @@ __global__ void k_prime(const __grid_constant__ Dev d)
             if (lava) {
                 const int pos = base + __popc(m & ((1u << lane) - 1u));
                 if (pos < d.capacity)
-                    d.list0[pos] = (int)c;
+                    d.list[pos] = (int)c;
                 else
                     atomicExch(d.counts + 8, 1);
             }
@@ -956,6 +1068,9 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
     d.ph.Pc = params[12];
     d.ph.Pac = d.ph.Pc * d.ph.Pc;
     d.ph.rad2 = sqrt(2.0);
+    d.ph.rrad2 = 1.0 / d.ph.rad2;
+    d.ph.rad2_recip = cal_recip_exact_ok(d.ph.rad2, d.ph.rrad2) ? 1 : 0;
+    d.ph.w2 = d.ph.Pc * d.ph.Pc;
     /* evaluatePowerLawParams (Sciara.cpp:199-204), C library log10 */
     d.ph.b = (log10(Pr_Tvent) - log10(Pr_Tsol)) / (d.ph.PTvent - d.ph.PTsol);
     d.ph.a = log10(Pr_Tsol) - d.ph.b * (d.ph.PTsol);
@@ -970,15 +1085,17 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
               sci2::dalloc(*bt, &d.Sz, nb) && sci2::dalloc(*bt, &d.Slt, nb) && sci2::dalloc(*bt, &d.St, nb) &&
               sci2::dalloc(*bt, &d.Msl, nb) && sci2::dalloc(*bt, (unsigned char**)&d.Mb, (size_t)bt->N) &&
               sci2::dalloc(*bt, &d.map, sizeof(int2) * (size_t)bt->N) &&
-              sci2::dalloc(*bt, &d.list0, sizeof(int) * (size_t)bt->capacity) &&
-              sci2::dalloc(*bt, &d.list1, sizeof(int) * (size_t)bt->capacity) &&
+              sci2::dalloc(*bt, &d.recv, sizeof(int) * (size_t)bt->N) &&
+              sci2::dalloc(*bt, &d.rlist, sizeof(int) * (size_t)bt->capacity) &&
+              sci2::dalloc(*bt, &d.list, sizeof(int) * (size_t)bt->capacity) &&
+              sci2::dalloc(*bt, &d.mask, sizeof(unsigned) * 16 * (size_t)tiles) &&
               sci2::dalloc(*bt, &d.fc, sizeof(double) * 16 * (size_t)bt->capacity) &&
               sci2::dalloc(*bt, &d.counts, 16 * sizeof(int)) &&
               sci2::dalloc(*bt, &d.tflag, sizeof(int) * (size_t)tiles) &&
               sci2::dalloc(*bt, &d.tlist, sizeof(int) * (size_t)tiles) &&
               sci2::dalloc(*bt, (int**)&d.vent_cell, sizeof(int) * std::max(1, nvents)) &&
               sci2::dalloc(*bt, (int**)&d.vent_first, sizeof(int) * (B + 1)) &&
-              sci2::dalloc(*bt, (double**)&d.rates, sizeof(double) * std::max<size_t>(1, vrates.size())) &&
+              sci2::dalloc(*bt, (double**)&d.emit, sizeof(double) * std::max<size_t>(1, vrates.size())) &&
               sci2::dalloc(*bt, &bt->Sz0, nb) && sci2::dalloc(*bt, &bt->Slt0, nb) && sci2::dalloc(*bt, &bt->St0, nb);
     if (!ok) {
         fprintf(stderr, "opencal-gb300: cal_sciara_batch_create: out of device memory\n");
@@ -989,7 +1106,14 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
     cudaMemcpy((void*)d.offs, bt->offs.data(), sizeof(long long) * (B + 1), cudaMemcpyHostToDevice);
     if (nvents) {
         cudaMemcpy((void*)d.vent_cell, vcell.data(), sizeof(int) * nvents, cudaMemcpyHostToDevice);
-        cudaMemcpy((void*)d.rates, vrates.data(), sizeof(double) * vrates.size(), cudaMemcpyHostToDevice);
+    {
+        /* updateVentsEmission's emitted thickness, rate / Pac * Pclock, in
+         * the same IEEE operations on the host */
+        std::vector<double> emit(vrates.size());
+        for (size_t k = 0; k < vrates.size(); k++)
+            emit[k] = vrates[k] / d.ph.Pac * d.ph.Pclock;
+        cudaMemcpy((void*)d.emit, emit.data(), sizeof(double) * emit.size(), cudaMemcpyHostToDevice);
+    }
     }
     cudaMemcpy((void*)d.vent_first, vfirst.data(), sizeof(int) * (B + 1), cudaMemcpyHostToDevice);
     cudaMemset(d.Sz, 0, nb);
@@ -1040,6 +1164,8 @@ static int forward(Batch* bt, int max_steps, const Tape* tape, double* vtape, st
     cudaMemsetAsync(d.Msl, 0, nb, st);
     cudaMemsetAsync(d.counts, 0, 16 * sizeof(int), st);
     cudaMemsetAsync(d.map, 0, sizeof(int2) * (size_t)bt->N, st);
+    cudaMemsetAsync(d.recv, 0, sizeof(int) * (size_t)bt->N, st);
+    cudaMemsetAsync(d.mask, 0, sizeof(unsigned) * 16 * (size_t)bt->ntiles, st);
     cudaMemsetAsync(d.tflag, 0, sizeof(int) * (size_t)bt->ntiles, st);
     const int one = 1;
     cudaMemcpyAsync(d.counts + 6, &one, sizeof(int), cudaMemcpyHostToDevice, st);
@@ -1058,9 +1184,14 @@ static int forward(Batch* bt, int max_steps, const Tape* tape, double* vtape, st
     for (int step = 1; max_steps <= 0 || step <= max_steps; step++) {
         if (elapsed_of)
             elapsed_of->push_back(elapsed);
-        k_vents<<<(bt->B + 63) / 64, 64, 0, st>>>(d, elapsed, vtape ? vtape + (size_t)done * 3 * bt->nvents : nullptr);
+        /* the phase as the vent process forms it: (unsigned)(elapsed / emission_time) */
+        const unsigned phase = (unsigned)(elapsed / (double)bt->emission_time);
+        k_collect<<<K2_BLOCKS, T, 0, st>>>(d, phase, vtape ? vtape + (size_t)done * 3 * bt->nvents : nullptr,
+                                           done > 0);
         k_flows<<<152 * 32, K1T, 0, st>>>(d);
-        k_update<<<K2_BLOCKS, T, 0, st>>>(d, tp, done);
+        if (tp.state)
+            k_tape<<<K2_BLOCKS, T, 0, st>>>(d, tp);
+        k_update<<<152 * 32, K1T, 0, st>>>(d, tp, done);
         done++;
         elapsed += d.ph.Pclock;
         if (elapsed >= bt->effusion_duration)
@@ -1300,8 +1431,8 @@ extern "C" int cal_sciara_batch_read(void* handle, double* z, double* slt, doubl
 extern "C" int cal_sciara_batch_lava_cells(void* handle)
 {
     Batch* bt = (Batch*)handle;
-    int c[5] = {0, 0, 0, 0, 0};
+    int c = 0;
     cudaStreamSynchronize(bt->st);
-    cudaMemcpy(c, bt->d.counts, sizeof(c), cudaMemcpyDeviceToHost);
-    return c[c[4] & 1];
+    cudaMemcpy(&c, bt->d.counts + 13, sizeof(int), cudaMemcpyDeviceToHost);
+    return c;
 }

@@ -1,5 +1,6 @@
-// Host-side check of cal_div_small / cal_le against the host's IEEE
-// division and comparison.  Usage: exact_div_check <n_random> <seed>
+// Host-side check of cal_div_small (c = 1..9), cal_div_recip (b = sqrt(2)),
+// cal_le, cal_gt and cal_pos against the host's IEEE division and
+// comparisons.  Usage: exact_div_check <n_random> <seed>
 // Prints the number of mismatches (0 expected).
 #include <cmath>
 #include <cstdint>
@@ -31,11 +32,16 @@ int main(int argc, char** argv)
     long n = argc > 1 ? atol(argv[1]) : 10000000;
     s_state = argc > 2 ? strtoull(argv[2], 0, 10) : 1;
     long bad = 0;
+    const double rb_b = std::sqrt(2.0), rb_y = 1.0 / rb_b;
+    if (!cal_recip_exact_ok(rb_b, rb_y)) {
+        printf("reciprocal precondition fails for sqrt(2)\n");
+        return 1;
+    }
     const double specials[] = {0.0, -0.0, 1.0, -1.0, 3.0, 5.0, 15.0, 1e-310, -1e-310, 2.2250738585072014e-308,
                                1e308, 1.7976931348623157e308, INFINITY, -INFINITY, NAN, 0.1, 1.0 / 3.0,
                                4503599627370496.0, 9007199254740991.0, 1e-300, 6.0e-305};
     for (double x : specials)
-        for (int c = 1; c <= 5; c++)
+        for (int c = 1; c <= 9; c++)
             if (!same(cal_div_small(x, c), x / (double)c)) {
                 if (bad < 10) printf("special x=%a c=%d got %a want %a\n", x, c, cal_div_small(x, c), x / (double)c);
                 bad++;
@@ -50,7 +56,7 @@ int main(int argc, char** argv)
             /* values of the model's range: sums of thicknesses and altitudes */
             x = (double)(r >> 11) * (1.0 / 9007199254740992.0) * 4000.0 - 200.0;
         }
-        int c = 1 + (int)(next_u64() % 5);
+        int c = 1 + (int)(next_u64() % 9);
         if (!same(cal_div_small(x, c), x / (double)c)) {
             if (bad < 10) printf("x=%a c=%d got %a want %a\n", x, c, cal_div_small(x, c), x / (double)c);
             bad++;
@@ -61,8 +67,12 @@ int main(int argc, char** argv)
             memcpy(&y, &r2, 8);
         else
             y = x + (double)((int64_t)(r2 % 7) - 3) * (std::fabs(x) * 1e-16);
-        if (cal_le(x, y) != (x <= y)) {
-            if (bad < 10) printf("le x=%a y=%a\n", x, y);
+        if (cal_le(x, y) != (x <= y) || cal_gt(x, y) != (x > y) || cal_pos(x) != (x > 0)) {
+            if (bad < 10) printf("compare x=%a y=%a\n", x, y);
+            bad++;
+        }
+        if (!same(cal_div_recip(x, rb_b, rb_y), x / rb_b)) {
+            if (bad < 10) printf("recip x=%a got %a want %a\n", x, cal_div_recip(x, rb_b, rb_y), x / rb_b);
             bad++;
         }
     }

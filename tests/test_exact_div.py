@@ -1,6 +1,7 @@
-"""exact_div.cuh: division of a double by 1..5 and <= on the integer pipe
-must return exactly the IEEE results (the fused SCIDDICA-T kernel relies on
-it for bit-exactness)."""
+"""exact_div.cuh: division of a double by 1..9, division by sqrt(2) through
+its reciprocal with Markstein's correction, and <=, >, > 0 on the integer
+pipe must return exactly the IEEE results (the SCIDDICA-T and SCIARA-fv2
+kernels rely on them for bit-exactness)."""
 import ctypes as C
 import os
 import subprocess
@@ -25,7 +26,7 @@ def _inputs(n, seed):
     raw = r[:n].view(np.float64).copy()
     model = (r[n:2 * n] >> np.uint64(11)).astype(np.float64) / 2.0 ** 53 * 4000.0 - 200.0
     x = np.where(np.arange(n) % 2 == 0, raw, model)
-    c = (r[2 * n:] % np.uint64(5)).astype(np.int32) + 1
+    c = (r[2 * n:] % np.uint64(9)).astype(np.int32) + 1
     y = np.where(np.arange(n) % 3 == 0, x * (1 + 1e-16), np.roll(x, 1))
     specials = np.array([0.0, -0.0, 1e-310, -1e-310, np.inf, -np.inf, np.nan, 1e308, 2.2250738585072014e-308, 0.1])
     x[: len(specials)] = specials
