@@ -219,6 +219,12 @@ static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* 
  * final step, while the step number has not passed it (cal2DRun.c:125-139);
  * the decision drives the graph's conditional WHILE node.  `flag` receives
  * the decision too, for the step-by-step fallback. */
+/* the largest step a device-driven run executes: past it the loop ends and
+ * the second word of the step counter is set (the host reports an error) */
+#ifndef CAL_DEVICE_LOOP_MAX_STEP
+#define CAL_DEVICE_LOOP_MAX_STEP (1 << 26)
+#endif
+
 template <CALbyte (*STOP)(struct CALModel2D*)>
 __global__ void cal_stop2D_kernel(const __grid_constant__ struct CALDevModel2D m, cudaGraphConditionalHandle h,
                                   int use_handle, int final_step, int* flag)
@@ -230,6 +236,10 @@ __global__ void cal_stop2D_kernel(const __grid_constant__ struct CALDevModel2D m
         const int next = *m.step + 1;
         *m.step = next;
         again = (final_step == CAL_RUN_LOOP || next <= final_step) ? 1 : 0;
+        if (again && next > CAL_DEVICE_LOOP_MAX_STEP) {
+            again = 0; /* a device-driven run never loops without bound */
+            m.step[1] = 1;
+        }
     }
     *flag = again;
     if (use_handle)

@@ -152,6 +152,12 @@ static __device__ __forceinline__ int calGetActiveCellCountDevice3D(const struct
 }
 
 /* device stop condition kernel of a device-driven 3D run (see cal2DDevice.cuh) */
+/* the largest step a device-driven run executes: past it the loop ends and
+ * the second word of the step counter is set (the host reports an error) */
+#ifndef CAL_DEVICE_LOOP_MAX_STEP
+#define CAL_DEVICE_LOOP_MAX_STEP (1 << 26)
+#endif
+
 template <CALbyte (*STOP)(struct CALModel3D*)>
 __global__ void cal_stop3D_kernel(const __grid_constant__ struct CALDevModel3D m, cudaGraphConditionalHandle h,
                                   int use_handle, int final_step, int* flag)
@@ -163,6 +169,10 @@ __global__ void cal_stop3D_kernel(const __grid_constant__ struct CALDevModel3D m
         const int next = *m.step + 1;
         *m.step = next;
         again = (final_step == CAL_RUN_LOOP || next <= final_step) ? 1 : 0;
+        if (again && next > CAL_DEVICE_LOOP_MAX_STEP) {
+            again = 0; /* a device-driven run never loops without bound */
+            m.step[1] = 1;
+        }
     }
     *flag = again;
     if (use_handle)

@@ -109,6 +109,14 @@ int cal_sciara_batch_loss_grad(void* batch, const double* target, int max_steps,
                                int* steps_done, long long tape_slots, float* ms);
 int cal_sciara_batch_lava_cells(void* batch);
 
+/* ---- mbusu, 3D subsurface flow (OpenCAL/examples/cal_mbusu-glut/source/mbusu.c) ----
+ * steps: 0 = until the stop condition (10 days), > 0 = at most that many, < 0 =
+ * none; mode: 0 = launch sequence per step, 1 = recorded step replayed, 2 =
+ * device-driven loop ended by the device stop condition.  state: 8 x 624000
+ * doubles (teta, moist_cont, psi, k, h, dqdh, convergence, moist_diff, each
+ * slice-major 130 x 160 x 30) or NULL; tail: step reached, delta_t, delta_t_cum. */
+int cal_mbusu_run(int steps, int mode, double* state, double* tail, double* ms);
+
 /* ---- Game of Life (OpenCAL-OMP/examples/calomp_life) and the 3D rule ---- */
 int cal_life2d_run(int rows, int cols, int toroidal, int as_int, int steps, const unsigned char* s0,
                    unsigned char* s_out, int mode, int block, int graph, double* ms);

@@ -225,6 +225,32 @@ def sciddicaT_unsafe(z0, h0, steps, *, toroidal=True, p_r=0.5, p_eps=0.001, grap
     return z, h
 
 
+MBUSU_SHAPE = (130, 160, 30)  # slices, rows, cols
+MBUSU_FIELDS = ("teta", "moist_cont", "psi", "k", "h", "dqdh", "convergence", "moist_diff")
+
+
+def mbusu(steps=0, *, mode=2, timing=False):
+    """The reference's mbusu subsurface-flow program on the GPU through the
+    3D C API (csrc/models/mbusu.cu).  steps: 0 = until its stop condition at
+    10 days, > 0 = at most that many, < 0 = none.  mode: 0 = launches per
+    step, 1 = recorded step replayed, 2 = one device-driven loop.  Returns a
+    dict of the eight substates (slices, rows, cols) plus steps, delta_t,
+    delta_t_cum (and ms with timing=True)."""
+    n = MBUSU_SHAPE[0] * MBUSU_SHAPE[1] * MBUSU_SHAPE[2]
+    state = np.empty(8 * n)
+    tail = np.zeros(3)
+    ms = C.c_double(0.0)
+    m = models()
+    m.cal_mbusu_run.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    _check(m.cal_mbusu_run(int(steps), int(mode), state.ctypes.data, tail.ctypes.data, C.byref(ms)),
+           "cal_mbusu_run")
+    out = {name: state[q * n:(q + 1) * n].reshape(MBUSU_SHAPE).copy() for q, name in enumerate(MBUSU_FIELDS)}
+    out["steps"], out["delta_t"], out["delta_t_cum"] = int(tail[0]), float(tail[1]), float(tail[2])
+    if timing:
+        out["ms"] = ms.value
+    return out
+
+
 class SciaraBatch:
     """SCIARA-fv2 scenarios on the device, advanced together by the split step
     (csrc/models/sciara_batch.cu): created once, then run (always from the

@@ -308,7 +308,8 @@ static int run_device_steps(struct CALRun3D* sim, int first, int last)
     gr->device_loop_used = 0;
     if (!have_steps)
         return step;
-    cal::cuda_ok(cudaMemcpyAsync(g.d_step, &step, sizeof(int), cudaMemcpyHostToDevice, g.stream), "set step");
+    const int words[2] = {step, 0}; /* step, "gave up at the step limit" */
+    cal::cuda_ok(cudaMemcpyAsync(g.d_step, words, sizeof(words), cudaMemcpyHostToDevice, g.stream), "set step");
     g.sync();
     const int saved_final = sim->final_step;
     sim->final_step = last;
@@ -339,9 +340,12 @@ static int run_device_steps(struct CALRun3D* sim, int first, int last)
         }
     }
     sim->final_step = saved_final;
-    cal::cuda_ok(cudaMemcpyAsync(&step, g.d_step, sizeof(int), cudaMemcpyDeviceToHost, g.stream), "read step");
+    int out[2] = {step, 0};
+    cal::cuda_ok(cudaMemcpyAsync(out, g.d_step, sizeof(out), cudaMemcpyDeviceToHost, g.stream), "read step");
     g.sync();
-    return step;
+    if (out[1])
+        cal::set_error(CAL_ERROR_INVALID_ARGUMENT, "device-driven run stopped at the step limit (CAL_DEVICE_LOOP_MAX_STEP)");
+    return out[0];
 }
 
 extern "C" void calRunDevice3D(struct CALRun3D* sim)

@@ -133,9 +133,11 @@ bool reduce_device(cal::CalGrid& g, int type, int slot, int op, T* out)
     }
     if (!g.to_device_all())
         return false;
-    if (!g.d_reduce_partial &&
-        !cal::cuda_ok(cudaMalloc(&g.d_reduce_partial, RBLOCKS * sizeof(double) + 64), "cudaMalloc reduction"))
+    static_assert(RBLOCKS <= 512, "the grid allocates 512 partials");
+    if (!g.d_reduce_partial) {
+        cal::set_error(CAL_ERROR_CUDA, "reduction: no scratch");
         return false;
+    }
     typedef typename Acc<T>::type A;
     const T* x = (const T*)g.sub[type][slot].layer[0].dev;
     long long blocks = (g.ncells + RT - 1) / RT;
@@ -150,8 +152,10 @@ bool reduce_device(cal::CalGrid& g, int type, int slot, int op, T* out)
 template <typename T>
 T reduce_host(cal::CalGrid& g, int type, int slot, int op)
 {
-    if (!g.d_reduce_result && !cal::cuda_ok(cudaMalloc(&g.d_reduce_result, 64), "cudaMalloc reduction result"))
+    if (!g.d_reduce_result) {
+        cal::set_error(CAL_ERROR_CUDA, "reduction: no result word");
         return (T)0;
+    }
     T v = (T)0;
     if (reduce_device<T>(g, type, slot, op, (T*)g.d_reduce_result) &&
         cal::cuda_ok(cudaMemcpyAsync(&v, g.d_reduce_result, sizeof(T), cudaMemcpyDeviceToHost, g.stream),

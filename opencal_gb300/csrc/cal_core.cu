@@ -326,6 +326,12 @@ bool CalGrid::init(int dim_, int rows_, int cols_, int slices_, int toroidal_, i
     if (!cuda_ok(cudaMalloc(&d_count, sizeof(int)), "cudaMalloc count") ||
         !cuda_ok(cudaMemsetAsync(d_count, 0, sizeof(int), stream), "memset count"))
         return false;
+    /* reduction scratch (512 per-block partials of up to 8 bytes, plus the
+     * result word), allocated here so that a reduction queued while a step
+     * is being recorded as a graph never has to allocate */
+    if (!cuda_ok(cudaMalloc(&d_reduce_partial, 512 * sizeof(double) + 64), "cudaMalloc reduction") ||
+        !cuda_ok(cudaMalloc(&d_reduce_result, 64), "cudaMalloc reduction result"))
+        return false;
     if (active) {
         n_blocks = compact_blocks_needed(ncells);
         if (!cuda_ok(cudaMalloc(&d_flags, (size_t)ncells), "cudaMalloc flags") ||

@@ -34,7 +34,7 @@ MODEL_FLAGS = ["--fmad=false"]
 
 CORE_SOURCES = ["cal_core.cu", "cal2D.cu", "cal3D.cu", "cal2DRun.cu", "cal3DRun.cu", "calIO.cu", "calReduction.cu", "cal_noalloc.cu"]
 MODEL_SOURCES = ["models/sciddicaT.cu", "models/sciddicaT_adjoint.cu", "models/sciddicaT_batch.cu", "models/sciara.cu",
-                 "models/sciara_batch.cu", "models/life.cu",
+                 "models/sciara_batch.cu", "models/mbusu.cu", "models/life.cu",
                  "models/probes.cu"]
 
 

@@ -179,6 +179,28 @@ def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt
     return outs
 
 
+MBUSU_SHAPE = (130, 160, 30)  # slices, rows, cols
+MBUSU_FIELDS = ("teta", "moist_cont", "psi", "k", "h", "dqdh", "convergence", "moist_diff")
+
+
+def mbusu(steps, *, kind="serial"):
+    """Run the mbusu subsurface-flow program (oracle_mbusu.c) for `steps`
+    steps (0: until its stop condition at 10 days).  Returns a dict of the
+    eight substates, each (slices, rows, cols), plus steps, delta_t and
+    delta_t_cum."""
+    n = MBUSU_SHAPE[0] * MBUSU_SHAPE[1] * MBUSU_SHAPE[2]
+    state = np.empty(8 * n)
+    tail = np.zeros(3)
+    f = _fn(kind, "mbusu")
+    f.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int
+    if f(int(steps), state.ctypes.data, tail.ctypes.data):
+        raise RuntimeError("oracle mbusu failed")
+    out = {name: state[q * n:(q + 1) * n].reshape(MBUSU_SHAPE).copy() for q, name in enumerate(MBUSU_FIELDS)}
+    out["steps"], out["delta_t"], out["delta_t_cum"] = int(tail[0]), float(tail[1]), float(tail[2])
+    return out
+
+
 def unsafe2d(v0, b0, w0, steps, *, nbhd=NB_MOORE, toroidal=True, kind="serial"):
     """The unsafe-operation probe (oracle_models.c): returns v, b, w, u, x."""
     v0 = np.ascontiguousarray(v0, dtype=np.int32)
