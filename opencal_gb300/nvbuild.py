@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-cudart", "shared",
                  "-I" + INCLUDE, "-I" + CSRC, "-diag-suppress", "550,177"]
 # model kernels restate reference arithmetic operation by operation: no FMA contraction
-MODEL_FLAGS = ["--fmad=false"]
+MODEL_FLAGS = ["--fmad=false", "-Xcompiler=-ffp-contract=off"]  # no contraction on the device or host side
 
 CORE_SOURCES = ["cal_core.cu", "cal2D.cu", "cal3D.cu", "cal2DRun.cu", "cal3DRun.cu", "calIO.cu", "calReduction.cu", "cal_noalloc.cu"]
 MODEL_SOURCES = ["models/sciddicaT.cu", "models/sciddicaT_adjoint.cu", "models/sciddicaT_batch.cu", "models/sciara.cu",
