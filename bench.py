@@ -442,6 +442,7 @@ def calibration_section(args):
 
 
 SCIARA_BYTES_PER_CELL_UPDATE = 65  # Sz, Slt, St r/w (48) + Mb r (1) + Msl r/w (16)
+SCIARA_CPU_SAMPLE_STEPS = 4
 
 
 def sciara_arm(args):
@@ -476,6 +477,19 @@ def sciara_arm(args):
         lava = sb.lava_cells()
         loss, grads, lg_ms = sb.loss_grad(target)
     del target
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        z, v, rt, et = scs[0]
+        t0 = time.perf_counter()
+        oracle.sciara(z, v, rt, et, SCIARA_CPU_SAMPLE_STEPS, kind="omp", want_cells=False)
+        dt = time.perf_counter() - t0
+        cpu = {"value": z.size * SCIARA_CPU_SAMPLE_STEPS / dt, "unit": "cell-updates/s", "cores": cores,
+               "kind": "port", "sample": f"the first {SCIARA_CPU_SAMPLE_STEPS} steps of scenario 0 "
+                                         f"({args.size}^2, every cell), OpenMP on all host cores"}
     fw_ms = float(np.median(fw))
     cells = sb.cells
     peak, peak_kind = _peaks()
@@ -500,7 +514,57 @@ def sciara_arm(args):
                              "basis": f"{SCIARA_BYTES_PER_CELL_UPDATE} B per cell-update of the dense grids; the "
                                       "split step touches only the lava cells and their tiles, so this exceeds "
                                       "the HBM peak by the work that sparsity skips"},
-        "clocks": clk, "gpu_launches_per_step": 3,
+        "clocks": clk, "cpu_baseline": cpu, "gpu_launches_per_step": 3,
+    }
+    print(json.dumps(line), flush=True)
+
+
+MBUSU_CELLS = 130 * 160 * 30
+MBUSU_CPU_SAMPLE_STEPS = 20
+
+
+def mbusu_arm(args):
+    """mbusu, the reference's 3D subsurface-flow example (160 x 30 x 130
+    cells, von Neumann 3D, toroidal, 8 real substates, float time step from
+    a global minimum), through the 3D C API: one bench step = the whole run
+    to its stop condition (10 days of simulated time, 8662 steps) as one
+    device-driven loop.  Metric: cell-updates/s.  The CPU baseline is the
+    OpenMP oracle on the first 20 steps.  One JSON line."""
+    import opencal_gb300 as cal
+    import oracle
+    cal.build()
+    cap = args.max_steps  # 0: until the stop condition
+    for _ in range(args.warmup):
+        cal.mbusu(cap, mode=2)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    runs = [cal.mbusu(cap, mode=2, timing=True) for _ in range(args.steps)]
+    clk = clocks.stop()
+    ms = float(np.median([r["ms"] for r in runs]))
+    steps = runs[0]["steps"]
+    value = MBUSU_CELLS * steps / (ms * 1e-3)
+    cpu = None
+    if not args.no_cpu_baseline:
+        oracle.build()
+        cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        t0 = time.perf_counter()
+        oracle.mbusu(MBUSU_CPU_SAMPLE_STEPS, kind="omp")
+        dt = time.perf_counter() - t0
+        cpu = {"value": MBUSU_CELLS * MBUSU_CPU_SAMPLE_STEPS / dt, "unit": "cell-updates/s", "cores": cores,
+               "kind": "port", "sample": f"the first {MBUSU_CPU_SAMPLE_STEPS} steps (initialisation included), "
+                                         "OpenMP on all host cores"}
+    line = {
+        "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "the program's own initial state",
+        "config": {"workload": "mbusu 160x30x130 (3D von Neumann, toroidal), 8 real substates, "
+                               + ("until 10 days" if not cap else f"first {cap} steps")
+                               + f" ({steps} steps), one device-driven loop (EP, min-reduction steering, device stop)",
+                   "l2": "no flush: the 40 MB of state is L2-resident by design"},
+        "run_ms": [r["ms"] for r in runs], "steps_per_run": steps, "delta_t_cum": runs[0]["delta_t_cum"],
+        "bound": "FP64 pipe: eight pow calls per cell-update",
+        "clocks": clk, "cpu_baseline": cpu, "gpu_launches_per_step": 5,
     }
     print(json.dumps(line), flush=True)
 
@@ -565,13 +629,18 @@ def main():
     ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble"],
                     help="untimed fixed sequence for ncu captures")
     ap.add_argument("--ncu-steps", type=int, default=1002)
-    ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara"],
-                    help="sciddicaT: the headline line; sciara: the SCIARA-fv2 scenario measurement")
+    ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara", "mbusu"],
+                    help="sciddicaT: the headline line; sciara: the SCIARA-fv2 scenario measurement; "
+                         "mbusu: the 3D subsurface-flow program")
     ap.add_argument("--scenarios", type=int, default=64)
+    ap.add_argument("--max-steps", type=int, default=0,
+                    help="mbusu: stop after this many steps (0: at its stop condition); for short profiles")
     ap.add_argument("--size", type=int, default=4096)
     args = ap.parse_args()
     if args.workload == "sciara":
         sciara_arm(args)
+    elif args.workload == "mbusu":
+        mbusu_arm(args)
     elif args.ncu_case:
         ncu_case(args)
     elif args.impl == "reference":

@@ -99,7 +99,15 @@ struct Dev {
     int nvents;
     const int* vent_cell;  /* packed cell index of each vent */
     const int* vent_first; /* B + 1: vents of instance b are [vent_first[b], vent_first[b + 1]) */
-    const double* emit;    /* nvents x nphases: rate / Pac * Pclock, the thickness a vent adds per step */
+    /* vent cells: the vents of one scenario at one cell form a group, led
+     * by its first vent; per group and phase the vent whose emission takes
+     * effect (the last with a positive one, -1: none) and its thickness */
+    int ngroups;
+    const int* g_cell;    /* packed cell */
+    const int* g_member;  /* g_mfirst[g]..g_mfirst[g+1]: the group's vents, leader first */
+    const int* g_mfirst;
+    const int* g_eff;     /* ngroups x nphases */
+    const double* g_emit; /* ngroups x nphases */
     int nphases;
     unsigned emission_time;
     Phys ph;
@@ -164,42 +172,26 @@ __global__ void __launch_bounds__(T) k_collect(const __grid_constant__ Dev d, un
     if (blockIdx.x == 0) {
         if (threadIdx.x == 0)
             d.counts[13] = 0;
-        for (int b = threadIdx.x; b < d.B; b += blockDim.x) {
-            const int v0 = d.vent_first[b], v1 = d.vent_first[b + 1];
-            for (int v = v0; v < v1; v++) {
-                const int c = d.vent_cell[v];
-                /* the process reads the current thickness: every vent of a
-                 * cell adds to the value before this step's emission */
-                bool first = true;
-                for (int w = v0; w < v; w++)
-                    if (d.vent_cell[w] == c) {
-                        first = false; /* handled with the first vent of this cell */
-                        break;
-                    }
-                if (!first) {
-                    if (vtape)
-                        vtape[3 * v + 2] = -2.0;
-                    continue;
-                }
-                const double orig = d.Slt[c];
-                const double orig_t = d.St[c];
-                int eff = -1;
-                for (int w = v; w < v1; w++) {
-                    if (d.vent_cell[w] != c)
-                        continue;
-                    const double emitted = phase >= (unsigned)d.nphases ? 0.0 : d.emit[(size_t)w * d.nphases + phase];
-                    if (emitted > 0) {
-                        d.Slt[c] = orig + emitted;
-                        d.St[c] = d.ph.PTvent;
-                        eff = w;
-                    }
-                }
-                if (vtape) {
-                    vtape[3 * v] = orig;
-                    vtape[3 * v + 1] = orig_t;
-                    vtape[3 * v + 2] = (double)eff;
-                }
-                if (eff >= 0 && !(orig > 0))
+        for (int g = threadIdx.x; g < d.ngroups; g += blockDim.x) {
+            const int c = d.g_cell[g];
+            const int m0 = d.g_mfirst[g], m1 = d.g_mfirst[g + 1];
+            const int eff = phase < (unsigned)d.nphases ? d.g_eff[(size_t)g * d.nphases + phase] : -1;
+            /* the process reads the current thickness: the cell's vents add
+             * to the value before this step's emission, the last positive
+             * one wins */
+            const double orig = d.Slt[c];
+            if (vtape) {
+                const int lead = d.g_member[m0];
+                vtape[3 * lead] = orig;
+                vtape[3 * lead + 1] = d.St[c];
+                vtape[3 * lead + 2] = (double)eff;
+                for (int m = m0 + 1; m < m1; m++)
+                    vtape[3 * d.g_member[m] + 2] = -2.0; /* handled with the cell's first vent */
+            }
+            if (eff >= 0) {
+                d.Slt[c] = orig + d.g_emit[(size_t)g * d.nphases + phase];
+                d.St[c] = d.ph.PTvent;
+                if (!(orig > 0))
                     append(d.list, d.counts + 0, d.capacity, d.counts + 8, c);
             }
         }
@@ -1048,6 +1040,41 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
         for (int b = 0; b < B; b++)
             vfirst[b + 1] += vfirst[b];
     }
+    /* vent cells (groups) with, per phase, the vent that takes effect */
+    std::vector<int> g_cell, g_member, g_mfirst(1, 0), g_eff;
+    std::vector<double> g_emit;
+    {
+        const double Pac = params[12] * params[12], Pclock = params[0];
+        for (int b = 0; b < B; b++)
+            for (int v = vfirst[b]; v < vfirst[b + 1]; v++) {
+                bool lead = true;
+                for (int w = vfirst[b]; w < v; w++)
+                    if (vcell[w] == vcell[v])
+                        lead = false;
+                if (!lead)
+                    continue;
+                g_cell.push_back(vcell[v]);
+                for (int w = v; w < vfirst[b + 1]; w++)
+                    if (vcell[w] == vcell[v])
+                        g_member.push_back(w);
+                g_mfirst.push_back((int)g_member.size());
+                for (int p = 0; p < nphases; p++) {
+                    int eff = -1;
+                    double e = 0.0;
+                    for (int m = g_mfirst[g_mfirst.size() - 2]; m < g_mfirst.back(); m++) {
+                        /* updateVentsEmission's thickness, rate / Pac * Pclock */
+                        const double em = vrates[(size_t)g_member[m] * nphases + p] / Pac * Pclock;
+                        if (em > 0) {
+                            eff = g_member[m];
+                            e = em;
+                        }
+                    }
+                    g_eff.push_back(eff);
+                    g_emit.push_back(e);
+                }
+            }
+    }
+    const int ngroups = (int)g_cell.size();
     sci2::Dev& d = bt->d;
     memset(&d, 0, sizeof(d));
     d.B = B;
@@ -1095,7 +1122,11 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
               sci2::dalloc(*bt, &d.tlist, sizeof(int) * (size_t)tiles) &&
               sci2::dalloc(*bt, (int**)&d.vent_cell, sizeof(int) * std::max(1, nvents)) &&
               sci2::dalloc(*bt, (int**)&d.vent_first, sizeof(int) * (B + 1)) &&
-              sci2::dalloc(*bt, (double**)&d.emit, sizeof(double) * std::max<size_t>(1, vrates.size())) &&
+              sci2::dalloc(*bt, (int**)&d.g_cell, sizeof(int) * std::max(1, ngroups)) &&
+              sci2::dalloc(*bt, (int**)&d.g_member, sizeof(int) * std::max(1, nvents)) &&
+              sci2::dalloc(*bt, (int**)&d.g_mfirst, sizeof(int) * (ngroups + 1)) &&
+              sci2::dalloc(*bt, (int**)&d.g_eff, sizeof(int) * std::max<size_t>(1, g_eff.size())) &&
+              sci2::dalloc(*bt, (double**)&d.g_emit, sizeof(double) * std::max<size_t>(1, g_emit.size())) &&
               sci2::dalloc(*bt, &bt->Sz0, nb) && sci2::dalloc(*bt, &bt->Slt0, nb) && sci2::dalloc(*bt, &bt->St0, nb);
     if (!ok) {
         fprintf(stderr, "opencal-gb300: cal_sciara_batch_create: out of device memory\n");
@@ -1104,16 +1135,16 @@ extern "C" void* cal_sciara_batch_create(int B, const int* dims, const double* z
     }
     cudaMemcpy((void*)d.inst, bt->inst.data(), sizeof(sci2::Inst) * B, cudaMemcpyHostToDevice);
     cudaMemcpy((void*)d.offs, bt->offs.data(), sizeof(long long) * (B + 1), cudaMemcpyHostToDevice);
+    d.ngroups = ngroups;
+    cudaMemcpy((void*)d.g_mfirst, g_mfirst.data(), sizeof(int) * (ngroups + 1), cudaMemcpyHostToDevice);
     if (nvents) {
         cudaMemcpy((void*)d.vent_cell, vcell.data(), sizeof(int) * nvents, cudaMemcpyHostToDevice);
-    {
-        /* updateVentsEmission's emitted thickness, rate / Pac * Pclock, in
-         * the same IEEE operations on the host */
-        std::vector<double> emit(vrates.size());
-        for (size_t k = 0; k < vrates.size(); k++)
-            emit[k] = vrates[k] / d.ph.Pac * d.ph.Pclock;
-        cudaMemcpy((void*)d.emit, emit.data(), sizeof(double) * emit.size(), cudaMemcpyHostToDevice);
-    }
+        cudaMemcpy((void*)d.g_cell, g_cell.data(), sizeof(int) * ngroups, cudaMemcpyHostToDevice);
+        cudaMemcpy((void*)d.g_member, g_member.data(), sizeof(int) * g_member.size(), cudaMemcpyHostToDevice);
+        if (!g_eff.empty()) {
+            cudaMemcpy((void*)d.g_eff, g_eff.data(), sizeof(int) * g_eff.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy((void*)d.g_emit, g_emit.data(), sizeof(double) * g_emit.size(), cudaMemcpyHostToDevice);
+        }
     }
     cudaMemcpy((void*)d.vent_first, vfirst.data(), sizeof(int) * (B + 1), cudaMemcpyHostToDevice);
     cudaMemset(d.Sz, 0, nb);
