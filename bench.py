@@ -534,11 +534,12 @@ def mbusu_arm(args):
     import oracle
     cal.build()
     cap = args.max_steps  # 0: until the stop condition
+    mode = args.mbusu_mode
     for _ in range(args.warmup):
-        cal.mbusu(cap, mode=2)
+        cal.mbusu(cap, mode=mode)
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
-    runs = [cal.mbusu(cap, mode=2, timing=True) for _ in range(args.steps)]
+    runs = [cal.mbusu(cap, mode=mode, timing=True) for _ in range(args.steps)]
     clk = clocks.stop()
     ms = float(np.median([r["ms"] for r in runs]))
     steps = runs[0]["steps"]
@@ -560,7 +561,10 @@ def mbusu_arm(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "the program's own initial state",
         "config": {"workload": "mbusu 160x30x130 (3D von Neumann, toroidal), 8 real substates, "
                                + ("until 10 days" if not cap else f"first {cap} steps")
-                               + f" ({steps} steps), one device-driven loop (EP, min-reduction steering, device stop)",
+                               + f" ({steps} steps), "
+                               + ("one device-driven loop" if mode == 2 else "a recorded step replayed" if mode == 1
+                                  else "a launch sequence per step")
+                               + " (EP, min-reduction steering, device stop)",
                    "l2": "no flush: the 40 MB of state is L2-resident by design"},
         "run_ms": [r["ms"] for r in runs], "steps_per_run": steps, "delta_t_cum": runs[0]["delta_t_cum"],
         "bound": "FP64 pipe: eight pow calls per cell-update",
@@ -635,6 +639,9 @@ def main():
     ap.add_argument("--scenarios", type=int, default=64)
     ap.add_argument("--max-steps", type=int, default=0,
                     help="mbusu: stop after this many steps (0: at its stop condition); for short profiles")
+    ap.add_argument("--mbusu-mode", type=int, default=2, choices=[0, 1, 2],
+                    help="mbusu: 0 launches per step, 1 recorded step replayed, 2 device-driven loop "
+                         "(ncu cannot profile the kernels of 2's conditional graph)")
     ap.add_argument("--size", type=int, default=4096)
     args = ap.parse_args()
     if args.workload == "sciara":
