@@ -118,6 +118,14 @@ void calMarkHostDirty3D(struct CALModel3D* ca3D);
 void calFinish3D(struct CALModel3D* ca3D);
 void* calGetStream3D(struct CALModel3D* ca3D);
 int calGetActiveCellCount3D(struct CALModel3D* ca3D);
+/* host array (rows*columns*slices, the buffer layout) -> both layers on the
+ * device, and the current layer -> host array (see cal2D.h) */
+void calCopySubstateFromHost3Db(struct CALModel3D* ca3D, struct CALSubstate3Db* Q, const CALbyte* data);
+void calCopySubstateFromHost3Di(struct CALModel3D* ca3D, struct CALSubstate3Di* Q, const CALint* data);
+void calCopySubstateFromHost3Dr(struct CALModel3D* ca3D, struct CALSubstate3Dr* Q, const CALreal* data);
+void calCopySubstateToHost3Db(struct CALModel3D* ca3D, struct CALSubstate3Db* Q, CALbyte* data);
+void calCopySubstateToHost3Di(struct CALModel3D* ca3D, struct CALSubstate3Di* Q, CALint* data);
+void calCopySubstateToHost3Dr(struct CALModel3D* ca3D, struct CALSubstate3Dr* Q, CALreal* data);
 
 struct CALDevModel3D;
 typedef int (*CALLaunchFunc3D)(const struct CALDevModel3D* m, int grid_x, int grid_y, void* stream);

@@ -388,6 +388,15 @@ extern "C" void calUpdateActiveCells2D(struct CALModel2D* ca)
             return nullptr;                                                                             \
         return g.sub[TC][s].layer[layer ? 1 : 0].dev;  /* layer 2: next, to be overwritten whole */     \
     }                                                                                                   \
+    extern "C" void calCopySubstateFromHost2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q,      \
+                                                  const T* data)                                           \
+    {                                                                                                      \
+        G(ca).load_from_host(TC, slot_of(ca, TC, Q), data);                                                \
+    }                                                                                                      \
+    extern "C" void calCopySubstateToHost2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, T* data) \
+    {                                                                                                      \
+        G(ca).store_to_host(TC, slot_of(ca, TC, Q), data);                                                 \
+    }                                                                                                      \
     extern "C" void calSyncSubstate2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q)             \
     {                                                                                                   \
         G(ca).to_host(TC, slot_of(ca, TC, Q), 0);                                                       \

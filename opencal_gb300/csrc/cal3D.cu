@@ -327,6 +327,15 @@ extern "C" void calUpdateActiveCells3D(struct CALModel3D* ca) { G(ca).compact();
             return;                                                                                     \
         std::vector<std::pair<int, int>> one(1, std::make_pair(TC, slot_of(ca, TC, Q)));                \
         g.copy_next_to_current(one, false, true);                                                       \
+    }                                                                                                   \
+    extern "C" void calCopySubstateFromHost3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q,     \
+                                                  const T* data)                                        \
+    {                                                                                                   \
+        G(ca).load_from_host(TC, slot_of(ca, TC, Q), data);                                             \
+    }                                                                                                   \
+    extern "C" void calCopySubstateToHost3D##S(struct CALModel3D* ca, struct CALSubstate3D##S* Q, T* data) \
+    {                                                                                                   \
+        G(ca).store_to_host(TC, slot_of(ca, TC, Q), data);                                              \
     }
 
 CAL_SUBSTATE_OPS_3D(b, CALbyte, 0)

@@ -482,6 +482,60 @@ bool CalGrid::flags_to_host()
     return true;
 }
 
+/* the caller's array (rows*cols[*slices] elements) becomes both layers of
+ * a substate on the device: one host-to-device copy into the current
+ * layer, one device copy into the next; the host mirrors become stale.
+ * From pinned host memory the copy is asynchronous on the model's stream. */
+bool CalGrid::load_from_host(int type, int slot, const void* src)
+{
+    Sub& q = sub[type][slot];
+    if (!q.used) {
+        set_error(CAL_ERROR_INVALID_ARGUMENT, "copy from host: not a substate of this model");
+        return false;
+    }
+    if (capturing) {
+        set_error(CAL_ERROR_NOT_CAPTURABLE, "host copy during graph capture");
+        return false;
+    }
+    const size_t bytes = (size_t)ncells * q.elem;
+    if (!cuda_ok(cudaMemcpyAsync(q.layer[0].dev, src, bytes, cudaMemcpyHostToDevice, stream), "copy from host"))
+        return false;
+    q.layer[0].dev_valid = true;
+    q.layer[0].host_valid = false;
+    if (!q.single) {
+        if (!cuda_ok(cudaMemcpyAsync(q.layer[1].dev, q.layer[0].dev, bytes, cudaMemcpyDeviceToDevice, stream),
+                     "copy current to next"))
+            return false;
+        q.layer[1].dev_valid = true;
+        q.layer[1].host_valid = false;
+        q.next_stale = false;
+    }
+    q.forced_dirty = false;
+    return true;
+}
+
+/* the current layer into the caller's array (from the host mirror when it
+ * is up to date, else straight from the device); synchronises */
+bool CalGrid::store_to_host(int type, int slot, void* dst)
+{
+    Sub& q = sub[type][slot];
+    if (!q.used) {
+        set_error(CAL_ERROR_INVALID_ARGUMENT, "copy to host: not a substate of this model");
+        return false;
+    }
+    if (capturing) {
+        set_error(CAL_ERROR_NOT_CAPTURABLE, "host copy during graph capture");
+        return false;
+    }
+    const size_t bytes = (size_t)ncells * q.elem;
+    if (q.layer[0].host_valid) {
+        memcpy(dst, q.host[0], bytes);
+        return true;
+    }
+    return cuda_ok(cudaMemcpyAsync(dst, q.layer[0].dev, bytes, cudaMemcpyDeviceToHost, stream), "copy to host") &&
+           cuda_ok(cudaStreamSynchronize(stream), "sync");
+}
+
 void CalGrid::host_wrote(int type, int slot, int layer)
 {
     Sub& q = sub[type][slot];

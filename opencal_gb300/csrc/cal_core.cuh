@@ -105,6 +105,8 @@ struct CalGrid {
     /* coherence */
     bool to_device_all();                      /* every layer of every substate + flags */
     bool to_host(int type, int slot, int layer);
+    bool load_from_host(int type, int slot, const void* src); /* caller's array -> both layers */
+    bool store_to_host(int type, int slot, void* dst);        /* current layer -> caller's array */
     bool flags_to_host();
     void host_wrote(int type, int slot, int layer);
     void device_wrote_all();                   /* after a user process */

@@ -217,6 +217,10 @@ static void mbusu_init_host(struct CALModel3D* ca)
     }
     cudaMemcpyToSymbol(mb_soil_dev, mb_soils_host, sizeof(mb_soils_host));
     const long long rc = (long long)ca->rows * ca->columns;
+    const size_t n = (size_t)rc * ca->slices;
+    double* buf = (double*)malloc(8 * n * sizeof(double)); /* teta, moist, psi, k, h, dqdh, mdiff, convergence */
+    if (!buf)
+        return;
     for (int k = 0; k < ca->slices; k++)
         for (int i = 0; i < ca->rows; i++)
             for (int j = 0; j < ca->columns; j++) {
@@ -225,14 +229,15 @@ static void mbusu_init_host(struct CALModel3D* ca)
                 const double h = -734 + quota;
                 const double psi = h - quota;
                 const MbusuPedo p = mb_pedo(mb_soils_host[mb_soil_index(i, kinv)], psi);
-                const long long c = k * rc + (long long)i * ca->columns + j;
-                const double v[7] = {p.teta, p.moist, psi, p.k, h, p.dqdh_inv, p.mdiff};
-                struct CALSubstate3Dr* q[7] = {MQ.teta, MQ.moist_cont, MQ.psi, MQ.k, MQ.h, MQ.dqdh, MQ.moist_diff};
-                for (int s = 0; s < 7; s++)
-                    q[s]->current[c] = q[s]->next[c] = v[s];
-                MQ.convergence->current[c] = MQ.convergence->next[c] = 0.0;
+                const size_t c = (size_t)(k * rc + (long long)i * ca->columns + j);
+                const double v[8] = {p.teta, p.moist, psi, p.k, h, p.dqdh_inv, p.mdiff, 0.0};
+                for (int s = 0; s < 8; s++)
+                    buf[s * n + c] = v[s];
             }
-    calMarkHostDirty3D(ca);
+    struct CALSubstate3Dr* q[8] = {MQ.teta, MQ.moist_cont, MQ.psi, MQ.k, MQ.h, MQ.dqdh, MQ.moist_diff, MQ.convergence};
+    for (int s = 0; s < 8; s++)
+        calCopySubstateFromHost3Dr(ca, q[s], buf + s * n); /* pageable: copied before the call returns */
+    free(buf);
 }
 
 /* Run mbusu: steps 0 = until the stop condition (10 days), > 0 = at most

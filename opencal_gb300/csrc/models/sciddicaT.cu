@@ -129,24 +129,30 @@ CAL_DEVICE_STOP_CONDITION_2D(sciddicaT_device_stop)(struct CALModel2D* sciddicaT
 }
 
 /* host callbacks (sciddicaT.c:104-140) */
+/* the body of the program's initialisation loop (sciddicaT_simulation_init,
+ * sciddicaT.c:104-131) at one cell: the source's depth is removed from the
+ * altitude, and with active cells on the source cells become active.  The
+ * reference runs it as a host loop over calGet2Dr / calSet2Dr; here it is
+ * a device process applied once, so the run needs no host pass over the
+ * grid (same arithmetic, same active list after the update). */
+CAL_ELEMENTARY_PROCESS_2D(sciddicaT_init_cell)(struct CALModel2D* sciddicaT, int i, int j)
+{
+    const CALreal h = calGet2Dr(sciddicaT, Q.h, i, j);
+    if (h > 0.0) {
+        const CALreal z = calGet2Dr(sciddicaT, Q.z, i, j);
+        calSet2Dr(sciddicaT, Q.z, i, j, z - h);
+        if (P.active)
+            calAddActiveCell2D(sciddicaT, i, j);
+    }
+}
+
 static void sciddicaT_simulation_init(struct CALModel2D* sciddicaT)
 {
-    CALreal z, h;
-    CALint i, j;
     calInitSubstate2Dr(sciddicaT, Q.f[0], 0);
     calInitSubstate2Dr(sciddicaT, Q.f[1], 0);
     calInitSubstate2Dr(sciddicaT, Q.f[2], 0);
     calInitSubstate2Dr(sciddicaT, Q.f[3], 0);
-    for (i = 0; i < sciddicaT->rows; i++)
-        for (j = 0; j < sciddicaT->columns; j++) {
-            h = calGet2Dr(sciddicaT, Q.h, i, j);
-            if (h > 0.0) {
-                z = calGet2Dr(sciddicaT, Q.z, i, j);
-                calSet2Dr(sciddicaT, Q.z, i, j, z - h);
-                if (P.active)
-                    calAddActiveCell2D(sciddicaT, i, j);
-            }
-        }
+    calApplyElementaryProcess2D(sciddicaT, sciddicaT_init_cell);
 }
 
 static void sciddicaT_steering_plain(struct CALModel2D* sciddicaT)
@@ -1437,24 +1443,24 @@ extern "C" int cal_sciddicaT_persist_failed(void* handle)
     return sdt2::persist_failed((cudaStream_t)calGetStream2D(((SdtSession*)handle)->ca));
 }
 
-/* host-buffer round trip through the API: load z and h into the host
- * mirrors (uploaded by the next device operation), run the program's init
- * and `steps` steps (graph: as for cal_sciddicaT_steps), read h back */
+/* host-buffer round trip through the API: z and h from the caller's arrays
+ * into the model (calCopySubstateFromHost2Dr), the program's init and
+ * `steps` steps (graph: as for cal_sciddicaT_steps), h back into the
+ * caller's array (calCopySubstateToHost2Dr) */
 extern "C" int cal_sciddicaT_host_run(void* handle, const double* z_host, const double* h_host, int steps, int graph,
                                       double* h_out)
 {
     SdtSession* s = (SdtSession*)handle;
-    memcpy(Q.z->current, z_host, s->bytes);
-    memcpy(Q.z->next, z_host, s->bytes);
-    memcpy(Q.h->current, h_host, s->bytes);
-    memcpy(Q.h->next, h_host, s->bytes);
-    calMarkHostDirty2D(s->ca);
+    /* the inputs go straight from the caller's arrays to the device (both
+     * layers, as the program's file loader leaves them); the outflows are
+     * reset by the program's init */
+    calCopySubstateFromHost2Dr(s->ca, Q.z, z_host);
+    calCopySubstateFromHost2Dr(s->ca, Q.h, h_host);
     sciddicaT_step_invalidate();
     calRunInitSimulation2D(s->run); /* the program's init: z -= h at the source, f = 0 */
     cal_sciddicaT_steps(handle, steps, graph);
     sciddicaT_sparse_resolve(s->ca);
-    calSyncSubstate2Dr(s->ca, Q.h);
-    memcpy(h_out, Q.h->current, s->bytes);
+    calCopySubstateToHost2Dr(s->ca, Q.h, h_out);
     return calGetLastError();
 }
 
