@@ -573,6 +573,120 @@ def mbusu_arm(args):
     print(json.dumps(line), flush=True)
 
 
+ADJ_SIZE, ADJ_STEPS, ADJ_SEED = 1024, 2000, 3
+ADJ_CPU_SAMPLE_STEPS = 100
+
+
+def adjoint_arm(args):
+    """SCIDDICA-T single-grid adjoint: 1024^2, T = 2000 steps, L = sum (h_T -
+    h_target)^2 with the target from the run at p_r = 0.42, p_eps = 0.0015,
+    gradient with respect to p_r, p_eps and h0 at p_r = 0.5, p_eps = 0.001 by
+    the hand-written adjoint (forward with sqrt(T) checkpoints + reverse
+    sweep, csrc/models/sciddicaT_adjoint.cu) through torch.autograd.  One
+    bench step = one gradient evaluation; metric cell-updates/s of the
+    forward (rows x cols x T per evaluation).  Compared with central finite
+    differences for (p_r, p_eps) on the GPU (4 forward runs) and with the
+    OpenMP oracle's forward, extrapolated to the same 4 runs."""
+    import torch
+    import opencal_gb300 as cal
+    from opencal_gb300 import adjoint as A
+    from opencal_gb300 import workloads as W
+    cal.build()
+    z, h0 = W.sciddicaT_inputs(ADJ_SIZE, ADJ_SIZE, seed=ADJ_SEED)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    zt = torch.from_numpy(z).to(dev)
+    ht = torch.from_numpy(h0).to(dev)
+    with torch.no_grad():
+        target = A.rollout(zt, ht, 0.42, 0.0015, ADJ_STEPS)
+
+    def grad_eval():
+        pr = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+        pe = torch.tensor(0.001, dtype=torch.float64, device=dev, requires_grad=True)
+        h = ht.clone().requires_grad_(True)
+        loss = ((A.rollout(zt, h, pr, pe, ADJ_STEPS) - target) ** 2).sum()
+        loss.backward()
+        return float(loss.detach()), float(pr.grad), float(pe.grad)
+
+    def loss_at(pr, pe):
+        with torch.no_grad():
+            return float(((A.rollout(zt, ht, pr, pe, ADJ_STEPS) - target) ** 2).sum())
+
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        grad_eval()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        loss, gr, ge = grad_eval()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    adj_ms = float(np.median(times))
+    # central finite differences for (p_r, p_eps): four forward runs
+    d_r, d_e = 1e-6 * 0.5, 1e-6 * 0.001
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fd_r = (loss_at(0.5 + d_r, 0.001) - loss_at(0.5 - d_r, 0.001)) / (2 * d_r)
+    fd_e = (loss_at(0.5, 0.001 + d_e) - loss_at(0.5, 0.001 - d_e)) / (2 * d_e)
+    e1.record(stream)
+    e1.synchronize()
+    fd_ms = e0.elapsed_time(e1)
+    # the same loss and gradients by the ensemble engine with one instance:
+    # tile work-lists, so dry regions cost nothing (csrc/models/sciddicaT_batch.cu)
+    from opencal_gb300.ensemble import Ensemble
+    ens = Ensemble([(ADJ_SIZE, ADJ_SIZE)], [(0.5, 0.001)], [z], [h0], ADJ_STEPS, device=dev)
+    tgt = ens.pack([target.cpu().numpy()])
+    for _ in range(max(1, args.warmup)):
+        ens.loss_grad(tgt, want_h0_grad=True)
+    sparse = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        s_loss, s_grad, _ = ens.loss_grad(tgt, want_h0_grad=True)
+        torch.cuda.synchronize(dev)
+        sparse.append(1e3 * (time.perf_counter() - t0))
+    ens.close()
+    sparse_ms = float(np.median(sparse))
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        t0 = time.perf_counter()
+        oracle.sciddicaT(z, h0, ADJ_CPU_SAMPLE_STEPS, toroidal=False, ac=False, p_r=0.5, p_eps=0.001, kind="omp",
+                         want_cells=False)
+        dt = time.perf_counter() - t0
+        cpu = {"value": ADJ_SIZE * ADJ_SIZE * ADJ_CPU_SAMPLE_STEPS / dt, "unit": "cell-updates/s", "cores": cores,
+               "kind": "port", "sample": f"{ADJ_CPU_SAMPLE_STEPS} forward steps of the {ADJ_SIZE}^2 grid, OpenMP on "
+                                         "all host cores",
+               "fd_gradient_s_extrapolated": 4 * dt * ADJ_STEPS / ADJ_CPU_SAMPLE_STEPS}
+    cells = ADJ_SIZE * ADJ_SIZE * ADJ_STEPS
+    line = {
+        "metric": "cell_updates_per_s", "value": cells / (adj_ms * 1e-3), "unit": "cell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": adj_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded DEM + source, seed 3)",
+        "config": {"workload": f"SCIDDICA-T adjoint {ADJ_SIZE}^2 FP64, VN, flat, plain, T = {ADJ_STEPS}: one "
+                               "gradient evaluation (forward with sqrt(T) checkpoints + reverse sweep) w.r.t. "
+                               "p_r, p_eps and h0",
+                   "l2": "no flush: 8 MiB grids"},
+        "gradient_ms": adj_ms, "gradient_runs_ms": times,
+        "fd_gradient_ms": fd_ms, "adjoint_vs_fd_speedup": fd_ms / adj_ms,
+        "sparse_engine": {"what": "the same loss and gradients (p_r, p_eps, h0) by the ensemble engine with one "
+                                  "instance (tile work-lists; host-timed, synchronised)",
+                          "gradient_ms": sparse_ms, "runs_ms": sparse, "loss": float(s_loss[0]),
+                          "grad_rel_diff_vs_dense": [abs(s_grad[0, 0] - gr) / max(abs(gr), 1e-300),
+                                                     abs(s_grad[0, 1] - ge) / max(abs(ge), 1e-300)]},
+        "gradient": {"loss": loss, "dL_dpr": gr, "dL_dpeps": ge, "fd_dL_dpr": fd_r, "fd_dL_dpeps": fd_e,
+                     "rel_diff": [abs(gr - fd_r) / max(abs(fd_r), 1e-300), abs(ge - fd_e) / max(abs(fd_e), 1e-300)]},
+        "clocks": clk, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def ncu_case_ensemble(args):
     """A fixed, untimed ensemble sequence for ncu captures: the first 32
     instances of the calibration ensemble, one forward of --ncu-steps steps
@@ -633,9 +747,9 @@ def main():
     ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble"],
                     help="untimed fixed sequence for ncu captures")
     ap.add_argument("--ncu-steps", type=int, default=1002)
-    ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara", "mbusu"],
+    ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara", "mbusu", "adjoint"],
                     help="sciddicaT: the headline line; sciara: the SCIARA-fv2 scenario measurement; "
-                         "mbusu: the 3D subsurface-flow program")
+                         "mbusu: the 3D subsurface-flow program; adjoint: the SCIDDICA-T gradient at 1024^2, T = 2000")
     ap.add_argument("--scenarios", type=int, default=64)
     ap.add_argument("--max-steps", type=int, default=0,
                     help="mbusu: stop after this many steps (0: at its stop condition); for short profiles")
@@ -648,6 +762,8 @@ def main():
         sciara_arm(args)
     elif args.workload == "mbusu":
         mbusu_arm(args)
+    elif args.workload == "adjoint":
+        adjoint_arm(args)
     elif args.ncu_case:
         ncu_case(args)
     elif args.impl == "reference":
