@@ -687,6 +687,62 @@ def adjoint_arm(args):
     print(json.dumps(line), flush=True)
 
 
+LIFE_SIZE, LIFE_STEPS, LIFE_CPU_SAMPLE_STEPS = 1024, 1000, 100
+
+
+def life_arm(args):
+    """Game of Life B3/S23, 1024^2 toroidal Moore, alive ~ Bernoulli(0.3)
+    (seed 1), 1000 generations: the reference program (one device process
+    per generation through the C API, byte substate), one fused launch per
+    generation, and temporal blocking (k generations per launch in shared
+    memory) for k = 4, 8, 16; all must give the same bits.  One bench step
+    = one 1000-generation run of each; value = the fastest form's
+    cell-updates/s; 2 B per cell-update by the metric's formula (the 1 MiB
+    state is L2-resident, so this is not an HBM figure)."""
+    import opencal_gb300 as cal
+    from opencal_gb300 import workloads as W
+    cal.build()
+    s0 = W.life_state(LIFE_SIZE, LIFE_SIZE, p=0.3, seed=1)
+    forms = [("processes", cal.MODE_PROCESSES, 1), ("fused", cal.MODE_FUSED, 1)] + \
+            [(f"blocked{k}", cal.MODE_FUSED_BLOCKED, k) for k in (4, 8, 16)]
+    results, outs = {}, {}
+    for name, mode, k in forms:
+        for _ in range(args.warmup):
+            cal.life2d(s0, LIFE_STEPS, mode=mode, block=k)
+        ms = []
+        for _ in range(args.steps):
+            out, t = cal.life2d(s0, LIFE_STEPS, mode=mode, block=k, timing=True)
+            ms.append(t)
+        results[name] = float(np.median(ms))
+        outs[name] = out
+    same = all(o.tobytes() == outs["processes"].tobytes() for o in outs.values())
+    best = min(results, key=results.get)
+    cells = LIFE_SIZE * LIFE_SIZE * LIFE_STEPS
+    value = cells / (results[best] * 1e-3)
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        t0 = time.perf_counter()
+        oracle.life2d(s0, LIFE_CPU_SAMPLE_STEPS, kind="omp")
+        dt = time.perf_counter() - t0
+        cpu = {"value": LIFE_SIZE * LIFE_SIZE * LIFE_CPU_SAMPLE_STEPS / dt, "unit": "cell-updates/s",
+               "cores": cores, "kind": "port",
+               "sample": f"{LIFE_CPU_SAMPLE_STEPS} generations, OpenMP on all host cores"}
+    line = {
+        "metric": "cell_updates_per_s", "value": value, "unit": "cell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": results[best], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (Bernoulli(0.3), seed 1)",
+        "config": {"workload": f"Life B3/S23 {LIFE_SIZE}^2 toroidal Moore, {LIFE_STEPS} generations",
+                   "l2": "no flush: the 1 MiB state is L2-resident by design"},
+        "forms_ms": results, "best": best, "identical_results": same,
+        "dense_equivalent_gbs": 2 * value / 1e9, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def ncu_case_ensemble(args):
     """A fixed, untimed ensemble sequence for ncu captures: the first 32
     instances of the calibration ensemble, one forward of --ncu-steps steps
@@ -747,9 +803,10 @@ def main():
     ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble"],
                     help="untimed fixed sequence for ncu captures")
     ap.add_argument("--ncu-steps", type=int, default=1002)
-    ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara", "mbusu", "adjoint"],
+    ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara", "mbusu", "adjoint", "life"],
                     help="sciddicaT: the headline line; sciara: the SCIARA-fv2 scenario measurement; "
-                         "mbusu: the 3D subsurface-flow program; adjoint: the SCIDDICA-T gradient at 1024^2, T = 2000")
+                         "mbusu: the 3D subsurface-flow program; adjoint: the SCIDDICA-T gradient at 1024^2, T = 2000; "
+                         "life: Game of Life 1024^2")
     ap.add_argument("--scenarios", type=int, default=64)
     ap.add_argument("--max-steps", type=int, default=0,
                     help="mbusu: stop after this many steps (0: at its stop condition); for short profiles")
@@ -764,6 +821,8 @@ def main():
         mbusu_arm(args)
     elif args.workload == "adjoint":
         adjoint_arm(args)
+    elif args.workload == "life":
+        life_arm(args)
     elif args.ncu_case:
         ncu_case(args)
     elif args.impl == "reference":
