@@ -7,13 +7,16 @@ on).  Metric: cell-updates per second (rows * cols * CA steps / time).
          snapshot, not timed), the 4000 CA steps of each run timed with CUDA
          events on the model's stream; L2 is flushed (256 MiB write) before
          every run
-  e2e    the same run through the C API with host buffers: the inputs are
-         copied from pinned host memory into the model (calMarkHostDirty2D ->
-         upload), the steps run, h is read back (calSyncSubstate2Dr); host
-         timer around each run
-  roofline  the fused step kernel: 24 algorithmic bytes per cell-update
-         (z read + h read + h write, FP64) / its average launch duration,
-         measured with CUDA events around single launches
+  e2e    the same run through the C API with host buffers: z and h are
+         copied from pinned host memory into the model
+         (calCopySubstateFromHost2Dr), the program's init and the steps run,
+         h is copied back (calCopySubstateToHost2Dr); host timer around each
+         run
+  roofline  the step (K1 + K2 of the split step): 24 algorithmic bytes per
+         cell-update (z read + h read + h write, FP64) / the mean step time
+         of the timed runs (CUDA events around each 4000-step run), i.e.
+         value x 24 B; the two kernels are also timed one launch at a time
+         over 400 steps from step 1000 (at_step_1000)
   cpu_baseline  the CPU port of the reference (oracle/, OpenMP build, all
          host cores) on a bounded sample of the same workload
 
@@ -264,8 +267,8 @@ def gpu_arm(args):
     units = ROWS * COLS * CA_STEPS * args.steps * world
     value = units / dev_s
 
-    # kernel-level roofline: the step's two kernels timed with events around
-    # every launch, over 400 steps from the mid-run state (step 1000)
+    # the step's two kernels timed with events around every launch, over 400
+    # steps from the mid-run state (step 1000)
     m.cal_sciddicaT_reset(sess)
     m.cal_sciddicaT_steps(sess, 1000, 0)
     h1000 = np.empty_like(h)
@@ -284,12 +287,14 @@ def gpu_arm(args):
     elif STEP_KERNEL == "single":
         kernel_desc = "SCIDDICA-T dense fused step sdt::fused_step (every tile every step)"
     if args.loop == "persistent":
-        # one launch runs all 4000 steps: its per-step time is the run's
-        kavg_ms = float(np.mean(run_ms)) / CA_STEPS
         kernel_desc = ("SCIDDICA-T split step, all 4000 steps in one cooperative launch of sdt2::k_persist "
                        "(K1 and K2 phases separated by grid barriers)")
     peak, peak_kind = _peaks()
-    achieved = ROWS * COLS * BYTES_PER_CELL_UPDATE / (kavg_ms * 1e-3) / 1e9
+    # the metric's formula: cell-updates/s of the timed runs x 24 B; per step,
+    # the runs' event time / 4000 (launch gaps included)
+    step_ms = float(np.mean(run_ms)) / CA_STEPS
+    achieved = ROWS * COLS * BYTES_PER_CELL_UPDATE / (step_ms * 1e-3) / 1e9
+    achieved_1000 = ROWS * COLS * BYTES_PER_CELL_UPDATE / (kavg_ms * 1e-3) / 1e9
 
     # end to end through the C API with host buffers
     pin_z = torch.from_numpy(z).pin_memory()
@@ -345,10 +350,15 @@ def gpu_arm(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "kernel": kernel_desc,
-                     "basis": "achieved = 24 B x rows x cols per step (dense algorithmic bytes) / mean event "
-                              "time of one step's kernels; traffic = ncu DRAM bytes of one step at step ~1000 "
-                              "(fields stay in L2)",
-                     "kernel_avg_ms": kavg_ms,
+                     "basis": "achieved = 24 B x rows x cols per step (dense algorithmic bytes) / mean step "
+                              "time of the timed runs (CUDA events on the model's stream around each 4000-step "
+                              "run, / 4000), i.e. value x 24 B; traffic = ncu DRAM bytes of one step at step "
+                              "~1000 (fields stay in L2)",
+                     "step_avg_ms": step_ms,
+                     "at_step_1000": {"k1_ms": k1_ms, "k2_ms": k2_ms, "achieved": achieved_1000,
+                                      "frac": achieved_1000 / peak,
+                                      "how": "events around each of the two kernels, 400 eager steps from "
+                                             "step 1000"},
                      "wet_cells_at_step_1000": wet,
                      "bytes_per_step": ROWS * COLS * BYTES_PER_CELL_UPDATE},
         "finite": bool(np.isfinite(hh).all()),
@@ -695,7 +705,9 @@ def life_arm(args):
     (seed 1), 1000 generations: the reference program (one device process
     per generation through the C API, byte substate), one fused launch per
     generation, and temporal blocking (k generations per launch in shared
-    memory) for k = 4, 8, 16; all must give the same bits.  One bench step
+    memory) for k = 4, 8, and the bit-sliced form (32 cells per word, a
+    carry-save adder tree per word) for k = 8, 16, 32; all must give the
+    same bits.  One bench step
     = one 1000-generation run of each; value = the fastest form's
     cell-updates/s; 2 B per cell-update by the metric's formula (the 1 MiB
     state is L2-resident, so this is not an HBM figure)."""
@@ -704,7 +716,8 @@ def life_arm(args):
     cal.build()
     s0 = W.life_state(LIFE_SIZE, LIFE_SIZE, p=0.3, seed=1)
     forms = [("processes", cal.MODE_PROCESSES, 1), ("fused", cal.MODE_FUSED, 1)] + \
-            [(f"blocked{k}", cal.MODE_FUSED_BLOCKED, k) for k in (4, 8, 16)]
+            [(f"blocked{k}", cal.MODE_FUSED_BLOCKED, k) for k in (4, 8)] + \
+            [(f"bits{k}", cal.MODE_BITS, k) for k in (8, 16, 32)]
     results, outs = {}, {}
     for name, mode, k in forms:
         for _ in range(args.warmup):

@@ -24,6 +24,7 @@ MODELS_LIB = os.path.join(LIB_DIR, "libopencal_models.so")
 
 NB_CUSTOM, NB_VN, NB_MOORE, NB_HEX, NB_HEX_ALT = 0, 1, 2, 3, 4
 MODE_PROCESSES, MODE_FUSED, MODE_FUSED_BLOCKED = 0, 1, 2
+MODE_BITS = 3  # Life only: bit-sliced fused launches (32 cells per word)
 
 _core = None
 _models = None

@@ -210,7 +210,8 @@ struct State {
     int* zlist[2] = {nullptr, nullptr};
     int* counts = nullptr;       /* [0..1] wet list lengths, [2..3] dried list lengths,
                                     [4] list parity, [5] K2 block ticket, [6] step epoch,
-                                    [7] flagged tiles */
+                                    [7] flagged tiles; [12], [14] the persistent
+                                    kernel's barrier counter and error flag */
     int* tflag = nullptr;        /* per K2 tile: epoch of the step that flagged it */
     int* tlist = nullptr;        /* flagged tiles of the current step */
     long long n = 0;
@@ -260,6 +261,7 @@ static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
 }
 
 constexpr int K1_THREADS = 64; /* small blocks: the wet list spreads over every SM */
+constexpr int NCOUNTS = 16;
 constexpr int K2_BLOCKS = 152 * 4;
 
 /* Loads of data that other blocks write while the kernel runs: in the
@@ -285,15 +287,28 @@ static __device__ __forceinline__ void flag_tile(int* tflag, int* tlist, int* tc
         tlist[atomicAdd(tcount, 1)] = t;
 }
 
+/* flag tile t for the lanes where `want` holds, once per distinct tile among
+ * the lanes converged here: consecutive wet cells of the list mostly share
+ * a tile, so the warp's leader for each tile does the (idempotent) flag
+ * and the others skip its load and atomic */
+template <bool CO>
+static __device__ __forceinline__ void flag_tile_warp(bool want, int t, int* tflag, int* tlist, int* tcount,
+                                                      int epoch)
+{
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, want ? t : -1);
+    if (want && (threadIdx.x & 31) == __ffs(peers) - 1)
+        flag_tile<CO>(tflag, tlist, tcount, t, epoch);
+}
+
 /* K1's work: the outflows of every listed wet cell (threads tid, tid +
  * nthreads, ...) and the clearing of the dried cells' outflows */
 template <bool CO>
-static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int epoch, int* tcount, int tid,
-                                               int nthreads)
+static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int epoch, int nw, int nz, int* tcount,
+                                               int tid, int nthreads)
 {
     const int* list = par ? p.list1 : p.list0;
     const int* zlist = par ? p.zlist1 : p.zlist0;
-    const int nw = ldm<CO>(p.counts + par);
     for (int k = tid; k < nw; k += nthreads) {
         const int c = ldm<CO>(list + k);
         const int i = c / p.cols, j = c - i * p.cols;
@@ -323,19 +338,23 @@ static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int e
         double f[4];
         sdt::outflows(ldh<CO>(p.h + c), __ldg(p.z + c), u[0], u[1], u[2], u[3], p.eps, p.r, f);
         bool any = false;
+        const int own = tile_of(i, j, p.tiles_x);
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             p.f[q * p.n + c] = f[q];
             if (__double_as_longlong(f[q]) != 0) {
                 any = true;
-                if (in[q]) /* the receiver reads it */
-                    flag_tile<CO>(p.tflag, p.tlist, tcount, tile_of(ni[q], nj[q], p.tiles_x), epoch);
+                /* the receiver reads it; a receiver in this cell's own tile
+                 * is covered by the flag of the own tile below */
+                if (in[q]) {
+                    const int t = tile_of(ni[q], nj[q], p.tiles_x);
+                    if (t != own)
+                        flag_tile<CO>(p.tflag, p.tlist, tcount, t, epoch);
+                }
             }
         }
-        if (any)
-            flag_tile<CO>(p.tflag, p.tlist, tcount, tile_of(i, j, p.tiles_x), epoch);
+        flag_tile_warp<CO>(any, own, p.tflag, p.tlist, tcount, epoch);
     }
-    const int nz = ldm<CO>(p.counts + 2 + par);
     for (int k = tid; k < nz; k += nthreads) {
         const int c = ldm<CO>(zlist + k);
 #pragma unroll
@@ -350,7 +369,8 @@ __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant_
     const int epoch = p.counts[6];
     if (blockIdx.x == 0 && threadIdx.x < 2)
         p.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists K2 will append to */
-    k1_work<false>(p, par, epoch, p.counts + 7, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+    k1_work<false>(p, par, epoch, p.counts[par], p.counts[2 + par], p.counts + 7, blockIdx.x * blockDim.x + threadIdx.x,
+                   gridDim.x * blockDim.x);
 }
 
 /* append the lanes whose predicate holds to list/count (warp-aggregated) */
@@ -549,48 +569,81 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
 /* ---- persistent form: every step of a run in one cooperative launch ----
  * The two phases of each step (K1's and K2's work) are separated by a grid
  * barrier.  counts[7 + (s & 1)] counts the flagged tiles of step s (one
- * step's count is cleared while the other is in use); counts[12..13] are the
- * barrier's arrival count and generation, counts[14] the error flag. */
+ * step's count is cleared while the other is in use); counts[12] is the
+ * barrier's arrival counter (zeroed before the launch), counts[14] the
+ * error flag.  Only one thread per block touches the shared words: it
+ * arrives, waits, and reads the two counts the next phase needs into shared
+ * memory, so that no L2 line is read by every thread of the grid. */
 constexpr unsigned BARRIER_SPIN_LIMIT = 1u << 22;
 
-/* Grid barrier for a cooperative launch (all blocks resident).  Every wait
- * is bounded: after BARRIER_SPIN_LIMIT polls the error flag is set and the
- * block goes on; callers stop working once the flag is set.  Returns false
- * when it is. */
-static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblocks)
+static __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p)
 {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+/* Grid barrier for a cooperative launch (all blocks resident).  Round r
+ * (1, 2, ...) is complete when the monotonic arrival counter counts[12]
+ * reaches r * nblocks.  Every wait is bounded: after BARRIER_SPIN_LIMIT
+ * polls the error flag is set and the block returns false, and so does
+ * every block that finds the flag set.  After the wait, thread 0 reads *r0
+ * and *r1 into out[0..1] for the whole block. */
+static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblocks, unsigned& round, const int* r0,
+                                                    const int* r1, int* out)
+{
+    __shared__ int s_ok;
     __syncthreads();
+    round++;
     if (threadIdx.x == 0) {
         unsigned* arrived = reinterpret_cast<unsigned*>(counts + 12);
-        unsigned* generation = reinterpret_cast<unsigned*>(counts + 13);
-        const unsigned g = __ldcg(generation);
+        const unsigned target = round * nblocks;
+        int ok = 1;
         __threadfence();
-        if (atomicAdd(arrived, 1u) == nblocks - 1) {
-            atomicExch(arrived, 0u);
-            __threadfence();
-            atomicAdd(generation, 1u);
-        } else {
-            unsigned polls = 0;
-            while (__ldcg(generation) == g) {
-                if (++polls > BARRIER_SPIN_LIMIT) {
-                    atomicExch(counts + 14, 1);
-                    break;
-                }
-                __nanosleep(64);
+        atomicAdd(arrived, 1u);
+        unsigned polls = 0;
+        while ((int)(ld_acquire_gpu(arrived) - target) < 0) {
+            if (++polls > BARRIER_SPIN_LIMIT) {
+                atomicExch(counts + 14, 1);
+                ok = 0;
+                break;
             }
+            __nanosleep(32);
         }
         __threadfence();
+        if (ok && __ldcg(counts + 14) != 0)
+            ok = 0;
+        out[0] = __ldcg(r0);
+        out[1] = __ldcg(r1);
+        s_ok = ok;
     }
     __syncthreads();
-    return __ldcg(counts + 14) == 0;
+    return s_ok != 0;
 }
 
 __global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ K1Params a,
                                                      const __grid_constant__ K2Params b, int nsteps)
 {
-    int par = __ldcg(a.counts + 4);
-    int epoch = __ldcg(a.counts + 6);
+    __shared__ int s_cnt[2];
+    __shared__ int s_state[2];
+    if (threadIdx.x == 0) {
+        s_state[0] = __ldcg(a.counts + 4);
+        s_state[1] = __ldcg(a.counts + 6);
+    }
+    __syncthreads();
+    int par = s_state[0];
+    int epoch = s_state[1];
+    if (threadIdx.x == 0) {
+        s_cnt[0] = __ldcg(a.counts + par);
+        s_cnt[1] = __ldcg(a.counts + 2 + par);
+    }
+    __syncthreads();
     const unsigned nb = gridDim.x;
+    unsigned round = 0;
+    /* K1's list entries in chunks of 32 (one per warp), consecutive chunks
+     * on consecutive blocks, so that the wet cells' FP64 work spreads over
+     * every SM whatever their number */
+    const int tid = ((threadIdx.x >> 5) * (int)nb + blockIdx.x) * 32 + (threadIdx.x & 31);
     for (int s = 0; s < nsteps; s++) {
         int* tcount = a.counts + 7 + (s & 1);
         if (blockIdx.x == 0 && threadIdx.x < 3) {
@@ -599,14 +652,16 @@ __global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ 
             else
                 a.counts[7 + ((s + 1) & 1)] = 0; /* next step's tile count (read last in step s - 1) */
         }
-        k1_work<true>(a, par, epoch, tcount, blockIdx.x * THREADS + threadIdx.x, nb * THREADS);
-        if (!grid_barrier(a.counts, nb))
+        k1_work<true>(a, par, epoch, s_cnt[0], s_cnt[1], tcount, tid, nb * THREADS);
+        /* then: the flagged tiles of this step and the current wet count */
+        if (!grid_barrier(a.counts, nb, round, tcount, a.counts + par, s_cnt))
             return;
-        k2_work<true>(b, par, epoch, __ldcg(tcount), __ldcg(a.counts + par), blockIdx.x, nb);
-        if (!grid_barrier(a.counts, nb))
-            return;
+        k2_work<true>(b, par, epoch, s_cnt[0], s_cnt[1], blockIdx.x, nb);
         par = 1 - par;
         epoch++;
+        /* then: the next step's wet and dried counts */
+        if (!grid_barrier(a.counts, nb, round, a.counts + par, a.counts + 2 + par, s_cnt))
+            return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         /* the state the per-step kernels expect */
@@ -664,7 +719,7 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         s.tiles_x = (ca->columns + TW - 1) / TW;
         s.tiles_y = (ca->rows + TH - 1) / TH;
         bool ok = cudaMalloc(&s.f, 4 * n * sizeof(double)) == cudaSuccess &&
-                  cudaMalloc(&s.counts, 16 * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&s.counts, NCOUNTS * sizeof(int)) == cudaSuccess &&
                   cudaMalloc(&s.tflag, sizeof(int) * s.tiles_x * s.tiles_y) == cudaSuccess &&
                   cudaMalloc(&s.tlist, sizeof(int) * s.tiles_x * s.tiles_y) == cudaSuccess;
         for (int k = 0; k < 2 && ok; k++)
@@ -676,7 +731,7 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         }
     }
     cudaMemsetAsync(s.f, 0, 4 * n * sizeof(double), st);
-    cudaMemsetAsync(s.counts, 0, 16 * sizeof(int), st); /* parity 0, ticket 0, no flagged tile */
+    cudaMemsetAsync(s.counts, 0, NCOUNTS * sizeof(int), st); /* parity 0, tickets 0, no flagged tile */
     cudaMemsetAsync(s.tflag, 0, sizeof(int) * s.tiles_x * s.tiles_y, st);
     int blocks = (int)((n + THREADS - 1) / THREADS);
     if (blocks > 152 * 16)

@@ -124,12 +124,36 @@ def test_sciddicaT_shipped_golden_processes_ac(cal):
 # ---------------------------------------------------------------- Life
 
 @pytest.mark.parametrize("tor", [0, 1])
-@pytest.mark.parametrize("mode,as_int", [(0, 0), (0, 1), (1, 0), (2, 0)])
+@pytest.mark.parametrize("mode,as_int", [(0, 0), (0, 1), (1, 0), (2, 0), (3, 0)])
 def test_life_bit_exact(cal, orc, tor, mode, as_int):
     s = W.life_state(131, 97, seed=3)
     ref = orc.life2d(s, 37, toroidal=tor, as_int=as_int)
     got = cal.life2d(s, 37, toroidal=tor, as_int=as_int, mode=mode, block=8)
     assert_same(got, ref, "life")
+
+
+@pytest.mark.parametrize("tor", [0, 1])
+@pytest.mark.parametrize("rows,cols,steps,block", [(131, 97, 71, 32), (20, 20, 45, 32), (300, 257, 63, 16),
+                                                   (5, 33, 7, 4), (1, 1, 3, 2), (200, 256, 77, 32),
+                                                   (40, 64, 45, 32), (70, 32, 33, 16), (3, 160, 9, 8)])
+def test_life_bits_shapes(cal, orc, tor, rows, cols, steps, block):
+    """Bit-sliced form: grids narrower or shorter than a tile and its halo
+    (toroidal wrap inside one tile), widths off the 32-cell word (cell-by-cell
+    loads) and on it (16-byte loads), every launch depth 32 / 16 / 8 / 4 /
+    2 / 1 in the remainders."""
+    s = W.life_state(rows, cols, seed=rows + cols)
+    ref = orc.life2d(s, steps, toroidal=tor)
+    got = cal.life2d(s, steps, toroidal=tor, mode=cal.MODE_BITS, block=block)
+    assert_same(got, ref, "life bits")
+
+
+def test_life_bits_rejects_other_states(cal):
+    """The bit-sliced form holds states 0 and 1 only; a byte state of 2 is
+    reported as an invalid argument instead of being read as alive."""
+    s = W.life_state(64, 64, seed=9)
+    s[10, 10] = 2
+    with pytest.raises(cal.CALError):
+        cal.life2d(s, 4, mode=cal.MODE_BITS, block=4)
 
 
 # ---------------------------------------------------------------- probes
