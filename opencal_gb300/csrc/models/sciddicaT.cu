@@ -209,9 +209,10 @@ struct State {
     int* list[2] = {nullptr, nullptr};
     int* zlist[2] = {nullptr, nullptr};
     int* counts = nullptr;       /* [0..1] wet list lengths, [2..3] dried list lengths,
-                                    [4] list parity, [5] K2 block ticket, [6] step epoch,
-                                    [7] flagged tiles; [12], [14] the persistent
-                                    kernel's barrier counter and error flag */
+                                    [4] list parity, [6] step epoch, [7..8] flagged
+                                    tiles; [C_TICKET] K2 block ticket; [C_ARRIVED],
+                                    [C_ERROR] the persistent kernel's barrier
+                                    counter and error flag */
     int* tflag = nullptr;        /* per K2 tile: epoch of the step that flagged it */
     int* tlist = nullptr;        /* flagged tiles of the current step */
     long long n = 0;
@@ -261,22 +262,48 @@ static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
 }
 
 constexpr int K1_THREADS = 64; /* small blocks: the wet list spreads over every SM */
-constexpr int NCOUNTS = 16;
+/* control words, each group on its own 128-byte line: the K2 ticket and the
+ * persistent kernel's barrier counter are hit by every block and polled,
+ * and must not share a line with the list and tile counters */
+constexpr int NCOUNTS = 128;
+constexpr int C_TICKET = 32, C_ARRIVED = 64, C_ERROR = 96;
 constexpr int K2_BLOCKS = 152 * 4;
+static int g_k1_blocks = 152 * 32, g_k2_blocks = K2_BLOCKS; /* launch grids of K1 and K2 (tunable) */
 
-/* Loads of data that other blocks write while the kernel runs: in the
- * persistent kernel (CO = true) they go to L2 (ld.global.cg) so that no
- * stale L1 line from an earlier step is read; the per-step kernels use the
- * ordinary paths. */
+/* Loads of data that other blocks write while the kernel runs.  In the
+ * persistent kernel (CO = true) they are weak ld.global (L1-cacheable)
+ * loads written out in PTX, so that the compiler cannot turn them into
+ * non-coherent loads through the const __restrict__ parameters: the grid
+ * barrier between the phases (a gpu-scope fence and acquire by one thread,
+ * then bar.sync) orders them after every write of the previous phase.  The
+ * per-step kernels use the ordinary paths (a kernel boundary orders them). */
+static __device__ __forceinline__ int ld_weak(const int* p)
+{
+    int v;
+    asm volatile("ld.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+static __device__ __forceinline__ double ld_weak(const double* p)
+{
+    double v;
+    asm volatile("ld.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
+}
+static __device__ __forceinline__ double2 ld_weak(const double2* p)
+{
+    double2 v;
+    asm volatile("ld.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
+    return v;
+}
 template <bool CO, typename T>
 static __device__ __forceinline__ T ldm(const T* p)
 {
-    return CO ? __ldcg(p) : *p;
+    return CO ? ld_weak(p) : *p;
 }
 template <bool CO>
 static __device__ __forceinline__ double ldh(const double* p)
 {
-    return CO ? __ldcg(p) : __ldg(p);
+    return CO ? ld_weak(p) : __ldg(p);
 }
 
 /* flag tile t for this step's K2 and append it to the work-list once */
@@ -557,9 +584,9 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
          * one to finish advances them for the next step (no block waits for
          * another) */
         __threadfence();
-        if (atomicAdd(reinterpret_cast<unsigned*>(p.counts + 5), 1u) == gridDim.x - 1) {
+        if (atomicAdd(reinterpret_cast<unsigned*>(p.counts + C_TICKET), 1u) == gridDim.x - 1) {
             p.counts[4] = 1 - par;
-            p.counts[5] = 0;
+            p.counts[C_TICKET] = 0;
             p.counts[6] = epoch + 1;
             p.counts[7] = 0;
         }
@@ -569,9 +596,9 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
 /* ---- persistent form: every step of a run in one cooperative launch ----
  * The two phases of each step (K1's and K2's work) are separated by a grid
  * barrier.  counts[7 + (s & 1)] counts the flagged tiles of step s (one
- * step's count is cleared while the other is in use); counts[12] is the
- * barrier's arrival counter (zeroed before the launch), counts[14] the
- * error flag.  Only one thread per block touches the shared words: it
+ * step's count is cleared while the other is in use); counts[C_ARRIVED] is
+ * the barrier's arrival counter (zeroed before the launch), counts[C_ERROR]
+ * the error flag.  Only one thread per block touches the shared words: it
  * arrives, waits, and reads the two counts the next phase needs into shared
  * memory, so that no L2 line is read by every thread of the grid. */
 constexpr unsigned BARRIER_SPIN_LIMIT = 1u << 22;
@@ -584,7 +611,7 @@ static __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p)
 }
 
 /* Grid barrier for a cooperative launch (all blocks resident).  Round r
- * (1, 2, ...) is complete when the monotonic arrival counter counts[12]
+ * (1, 2, ...) is complete when the monotonic arrival counter counts[C_ARRIVED]
  * reaches r * nblocks.  Every wait is bounded: after BARRIER_SPIN_LIMIT
  * polls the error flag is set and the block returns false, and so does
  * every block that finds the flag set.  After the wait, thread 0 reads *r0
@@ -596,7 +623,7 @@ static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblock
     __syncthreads();
     round++;
     if (threadIdx.x == 0) {
-        unsigned* arrived = reinterpret_cast<unsigned*>(counts + 12);
+        unsigned* arrived = reinterpret_cast<unsigned*>(counts + C_ARRIVED);
         const unsigned target = round * nblocks;
         int ok = 1;
         __threadfence();
@@ -604,14 +631,14 @@ static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblock
         unsigned polls = 0;
         while ((int)(ld_acquire_gpu(arrived) - target) < 0) {
             if (++polls > BARRIER_SPIN_LIMIT) {
-                atomicExch(counts + 14, 1);
+                atomicExch(counts + C_ERROR, 1);
                 ok = 0;
                 break;
             }
             __nanosleep(32);
         }
         __threadfence();
-        if (ok && __ldcg(counts + 14) != 0)
+        if (ok && __ldcg(counts + C_ERROR) != 0)
             ok = 0;
         out[0] = __ldcg(r0);
         out[1] = __ldcg(r1);
@@ -666,7 +693,7 @@ __global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ 
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         /* the state the per-step kernels expect */
         a.counts[4] = par;
-        a.counts[5] = 0;
+        a.counts[C_TICKET] = 0;
         a.counts[6] = epoch;
         a.counts[7] = 0;
         a.counts[8] = 0;
@@ -782,10 +809,10 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     b.eps_bits = eps_bits;
     if (ev)
         cudaEventRecord(ev[0], st);
-    k1_outflows<<<152 * 32, K1_THREADS, 0, st>>>(a);
+    k1_outflows<<<g_k1_blocks, K1_THREADS, 0, st>>>(a);
     if (ev)
         cudaEventRecord(ev[1], st);
-    k2_update<<<K2_BLOCKS, THREADS, 0, st>>>(b);
+    k2_update<<<g_k2_blocks, THREADS, 0, st>>>(b);
     if (ev)
         cudaEventRecord(ev[2], st);
     return cudaGetLastError() == cudaSuccess;
@@ -793,7 +820,7 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
 
 /* `nsteps` steps in one cooperative launch of k_persist (one resident grid:
  * SMs x resident blocks per SM); false when the launch is refused or a
- * CUDA error is pending.  A barrier that gave up sets counts[14], which
+ * CUDA error is pending.  A barrier that gave up sets counts[C_ERROR], which
  * persist_failed() reports. */
 static bool persist(struct CALModel2D* ca, const double* z, double* h, double eps, double r, long long eps_bits,
                     int nsteps, cudaStream_t st)
@@ -833,7 +860,8 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
     b.h = h;
     b.f = s.f;
     b.eps_bits = eps_bits;
-    cudaMemsetAsync(s.counts + 12, 0, 3 * sizeof(int), st); /* barrier words and error flag */
+    cudaMemsetAsync(s.counts + C_ARRIVED, 0, sizeof(int), st); /* barrier counter */
+    cudaMemsetAsync(s.counts + C_ERROR, 0, sizeof(int), st);   /* error flag */
     void* args[] = {&a, &b, &nsteps};
     return cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(THREADS), args, 0, st) ==
            cudaSuccess;
@@ -846,7 +874,7 @@ static int persist_failed(cudaStream_t st)
     if (!g_state.counts)
         return 0;
     cudaStreamSynchronize(st);
-    cudaMemcpy(&flag, g_state.counts + 14, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&flag, g_state.counts + C_ERROR, sizeof(int), cudaMemcpyDeviceToHost);
     return flag;
 }
 
@@ -1485,6 +1513,20 @@ extern "C" int cal_sciddicaT_set_params(void* handle, double p_r, double p_eps)
     SdtSession* s = (SdtSession*)handle;
     P.r = p_r;
     P.epsilon = p_eps;
+    calRunSetGraph2D(s->run, CAL_FALSE);
+    return calGetLastError();
+}
+
+/* launch grids of the split step's two kernels (64-thread K1 blocks,
+ * 256-thread K2 blocks; 0 restores the default 4864 / 608); a recorded
+ * step, which bakes them into its launches, is dropped */
+extern "C" int cal_sciddicaT_set_split_grid(void* handle, int k1_blocks, int k2_blocks)
+{
+    SdtSession* s = (SdtSession*)handle;
+    if (k1_blocks < 0 || k2_blocks < 0)
+        return CAL_ERROR_INVALID_ARGUMENT;
+    sdt2::g_k1_blocks = k1_blocks ? k1_blocks : 152 * 32;
+    sdt2::g_k2_blocks = k2_blocks ? k2_blocks : sdt2::K2_BLOCKS;
     calRunSetGraph2D(s->run, CAL_FALSE);
     return calGetLastError();
 }
