@@ -50,6 +50,10 @@ int cal_sciddicaT_set_params(void* session, double p_r, double p_eps);
  * (0 = the defaults 4864 / 608) */
 int cal_sciddicaT_set_split_grid(void* session, int k1_blocks, int k2_blocks);
 void* cal_sciddicaT_stream(void* session); /* cudaStream_t of the model */
+/* the dense step's TMA-staged form (flat grids, rows a multiple of 16 bytes;
+ * OPENCAL_SDT_TMA=0 keeps plain loads): launches queued so far and tiles
+ * whose copies timed out (synchronises the device) */
+int cal_sciddicaT_tma_stats(long long* launches, int* timeouts);
 int cal_sciddicaT_host_run(void* session, const double* z_host, const double* h_host, int steps, int graph,
                            double* h_out);
 int cal_sciddicaT_kernel_times(void* session, int n, float* ms_outflows, float* ms_update);

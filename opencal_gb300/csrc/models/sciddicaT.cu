@@ -1531,6 +1531,22 @@ extern "C" int cal_sciddicaT_set_split_grid(void* handle, int k1_blocks, int k2_
     return calGetLastError();
 }
 
+/* the dense step's TMA form: launches queued by this library's SCIDDICA-T
+ * programs so far, and tiles whose copies did not complete in time
+ * (synchronises the device) */
+extern "C" int cal_sciddicaT_tma_stats(long long* launches, int* timeouts)
+{
+    if (launches)
+        *launches = sdt::g_tma_launches;
+    if (timeouts) {
+        *timeouts = 0;
+        if (cudaDeviceSynchronize() != cudaSuccess ||
+            cudaMemcpyFromSymbol(timeouts, sdt::g_tma_timeouts, sizeof(int)) != cudaSuccess)
+            return CAL_ERROR_CUDA;
+    }
+    return CAL_SUCCESS;
+}
+
 extern "C" void* cal_sciddicaT_stream(void* handle) { return calGetStream2D(((SdtSession*)handle)->ca); }
 
 /* 1 when a barrier of the last persistent run gave up (the run stopped

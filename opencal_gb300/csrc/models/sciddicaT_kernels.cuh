@@ -10,6 +10,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "cal_tma.cuh"
 #include "exact_div.cuh"
 
 namespace sdt {
@@ -126,7 +127,7 @@ static __device__ __forceinline__ void warp_append_shared(bool pred, int value, 
  * the block-uniform result has bit 0 set when a cell of the tile was wet
  * before the step and bit 1 when one is wet after it (0 without TRACK). */
 template <int TW, int TH, bool TRACK = false>
-__device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, double* smem)
+__device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, double* smem, bool staged = false)
 {
     using T = Tile<TW, TH>;
     double* sz = smem;                      /* [R2H][R2W] */
@@ -143,7 +144,17 @@ __device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, doubl
      * is even, so every pair starts 16-byte aligned).  Edge tiles: flat ->
      * 0 outside, toroidal -> wrapped. */
     int wet_seen = 0, wet_in = 0, wet_out = 0;
-    if (interior) {
+    if (staged) {
+        /* z and h are in shared memory already (TMA, zero outside a flat
+         * grid): only the wet flags */
+        for (int t = threadIdx.x; t < T::R2H * T::R2W; t += THREADS) {
+            const int a = t / T::R2W, b = t - a * T::R2W;
+            const int w = is_wet(sh[t], p.eps_bits);
+            wet_seen |= w;
+            if (TRACK && a >= 2 && a < TH + 2 && b >= 2 && b < TW + 2 && i0 - 2 + a < p.rows && j0 - 2 + b < p.cols)
+                wet_in |= w;
+        }
+    } else if (interior) {
         constexpr int PW = T::R2W / 2;
         for (int t = threadIdx.x; t < PW * T::R2H; t += THREADS) {
             const int a = t / PW, b = 2 * (t - a * PW);
@@ -275,9 +286,96 @@ __global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Pa
     fused_tile<TW, TH>(p, blockIdx.y * TH, blockIdx.x * TW, smem);
 }
 
+/* The dense step with z and h staged by TMA: thread 0 arms an mbarrier with
+ * the two boxes' bytes and issues one cp.async.bulk.tensor.2d load per
+ * field (box R2W x R2H at (j0 - 2, i0 - 2); j0 - 2 is even, so x * 8 bytes
+ * is a multiple of 16); cells outside the array arrive as +0, which is the
+ * flat boundary's rule, so every tile of a flat grid takes this path.  The
+ * wait is bounded: a block whose copies do not complete counts itself in
+ * *timeouts, waits once more (bounded) for the copies in flight and leaves
+ * its tile unwritten. */
+constexpr uint32_t TMA_WAIT_LIMIT = 1u << 22;
+
+template <int TW, int TH>
+__global__ void __launch_bounds__(THREADS) fused_step_tma(const __grid_constant__ Params p,
+                                                          const __grid_constant__ CUtensorMap tz,
+                                                          const __grid_constant__ CUtensorMap th, int* timeouts)
+{
+    using T = Tile<TW, TH>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t bar;
+    double* smem = reinterpret_cast<double*>(smem_raw + ((128u - (caltma::smem_u32(smem_raw) & 127u)) & 127u));
+    const int i0 = blockIdx.y * TH, j0 = blockIdx.x * TW;
+    if (threadIdx.x == 0) {
+        caltma::bar_init(&bar);
+        caltma::bar_expect(&bar, 2u * T::R2W * T::R2H * (uint32_t)sizeof(double));
+        caltma::load_2d(smem, &tz, j0 - 2, i0 - 2, &bar);
+        caltma::load_2d(smem + T::R2W * T::R2H, &th, j0 - 2, i0 - 2, &bar);
+    }
+    __syncthreads(); /* the barrier is initialised before anyone waits on it */
+    const bool done = caltma::bar_wait(&bar, 0, TMA_WAIT_LIMIT);
+    if (!__syncthreads_and(done)) {
+        if (threadIdx.x == 0) {
+            atomicAdd(timeouts, 1);
+            caltma::bar_wait(&bar, 0, TMA_WAIT_LIMIT);
+        }
+        __syncthreads();
+        return;
+    }
+    fused_tile<TW, TH>(p, i0, j0, smem, true);
+}
+
+/* TMA launches queued and blocks whose copies timed out, per translation
+ * unit that launches the dense step */
+static long long g_tma_launches = 0;
+static __device__ int g_tma_timeouts;
+
+static int* tma_timeouts_ptr()
+{
+    static int* ptr = nullptr;
+    if (!ptr && cudaGetSymbolAddress((void**)&ptr, g_tma_timeouts) != cudaSuccess)
+        ptr = nullptr;
+    return ptr;
+}
+
+/* OPENCAL_SDT_TMA=0 keeps the plain loads (for comparison) */
+static bool tma_enabled()
+{
+    const char* e = getenv("OPENCAL_SDT_TMA");
+    return !(e && !strcmp(e, "0"));
+}
+
+/* queues the TMA form of the dense step; false (nothing queued) for a
+ * toroidal grid or a layout TMA cannot address */
+template <int TW, int TH>
+static bool launch_tma(const Params& p, cudaStream_t s)
+{
+    using T = Tile<TW, TH>;
+    if (p.toroidal || !tma_enabled())
+        return false;
+    int* timeouts = tma_timeouts_ptr();
+    CUtensorMap tz, th;
+    if (!timeouts ||
+        !caltma::encode_2d(&tz, p.z, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, p.rows, p.cols, T::R2W, T::R2H) ||
+        !caltma::encode_2d(&th, p.h, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, p.rows, p.cols, T::R2W, T::R2H))
+        return false;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(fused_step_tma<TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)T::smem_bytes + 128);
+        attr_set = true;
+    }
+    dim3 grid((p.cols + TW - 1) / TW, (p.rows + TH - 1) / TH);
+    fused_step_tma<TW, TH><<<grid, THREADS, T::smem_bytes + 128, s>>>(p, tz, th, timeouts);
+    g_tma_launches++;
+    return true;
+}
+
 template <int TW, int TH>
 static void launch(const Params& p, cudaStream_t s)
 {
+    if (launch_tma<TW, TH>(p, s))
+        return;
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(fused_step<TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,

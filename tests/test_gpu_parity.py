@@ -7,6 +7,7 @@ restate the reference's arithmetic operation by operation, so the test
 demands equality of the bits and reports the largest relative difference if
 it ever fails.
 """
+import ctypes as C
 import hashlib
 import json
 import os
@@ -311,6 +312,34 @@ def test_sciddicaT_other_step_kernels_bit_exact(cal, orc, monkeypatch, kernel, r
     ref = orc.sciddicaT(z, h, steps, toroidal=tor, ac=False)
     got = cal.sciddicaT(z, h, steps, toroidal=tor, ac=False, mode=cal.MODE_FUSED)
     assert_same(got[1], ref[1], f"h ({kernel})")
+
+
+def _tma_stats(cal):
+    lib = cal.models()
+    n, t = C.c_longlong(0), C.c_int(0)
+    assert lib.cal_sciddicaT_tma_stats(C.byref(n), C.byref(t)) == 0
+    return n.value, t.value
+
+
+@pytest.mark.parametrize("rows,cols,seed,steps", [(160, 144, 11, 40), (203, 250, 13, 60), (66, 64, 3, 30),
+                                                  (97, 32, 5, 25)])
+def test_sciddicaT_dense_tma_bit_exact(cal, orc, monkeypatch, rows, cols, seed, steps):
+    """The dense step with z and h staged in shared memory by TMA (flat
+    grids whose rows are a multiple of 16 bytes; the zero fill outside the
+    array is the flat boundary's rule): identical to the oracle and to the
+    plain-load form, one TMA launch per step, no copy timed out."""
+    monkeypatch.setenv("OPENCAL_SDT_KERNEL", "single")
+    z, h = W.sciddicaT_inputs(rows, cols, seed=seed)
+    ref = orc.sciddicaT(z, h, steps, toroidal=False, ac=False)
+    n0, t0 = _tma_stats(cal)
+    got = cal.sciddicaT(z, h, steps, toroidal=False, ac=False, mode=cal.MODE_FUSED)
+    n1, t1 = _tma_stats(cal)
+    assert n1 - n0 >= steps and t1 == t0 == 0
+    assert_same(got[1], ref[1], "h (dense step, TMA)")
+    monkeypatch.setenv("OPENCAL_SDT_TMA", "0")
+    plain = cal.sciddicaT(z, h, steps, toroidal=False, ac=False, mode=cal.MODE_FUSED)
+    assert _tma_stats(cal)[0] == n1
+    assert_same(plain[1], got[1], "h (dense step, plain loads)")
 
 
 @pytest.mark.parametrize("graph", [0, 1, 2])
