@@ -218,13 +218,25 @@ struct State {
     long long n = 0;
     int tiles_x = 0, tiles_y = 0;
     bool primed = false;
+    /* the device's list parity and epoch as of the next eager step, when
+     * hknown: kept by step() and dropped whenever launches the host does not
+     * see may have run (a recorded step replayed, the persistent kernel, any
+     * entry point's start) */
+    int hpar = 0, hepoch = 1;
+    bool hknown = false;
 };
 
 /* The lists alternate between two buffers; which one a step reads is the
- * parity word counts[4], flipped by the last K2 block of the step, which
- * also advances the epoch counts[6] and empties the tile list counts[7].
- * Keeping them in device memory makes every step's launches identical, so a
- * step can be recorded once as a CUDA graph and replayed. */
+ * list parity, and tiles are flagged with the step's epoch; the step's
+ * flagged tiles are counted in counts[7 + parity] (K1 empties the other one
+ * for the next step).  Two ways to know parity and epoch:
+ *  - device words counts[4] and counts[6], flipped and advanced by the last
+ *    K2 block of the step (a ticket): every step's launches are identical,
+ *    so a step can be recorded once as a CUDA graph and replayed;
+ *  - hpar >= 0: the host passes them (eager launches; the host tracks them
+ *    from the device words it read once), so that no block reads them
+ *    first and K2 ends without the fence and ticket atomic; block 0 of K2
+ *    still writes the device words for a later recorded step. */
 struct K1Params {
     const double* __restrict__ z;
     const double* __restrict__ h;
@@ -239,6 +251,7 @@ struct K1Params {
     int rows, cols, toroidal, tiles_x;
     long long n;
     double eps, r;
+    int hpar, hepoch; /* host-known parity and epoch; hpar < 0: read the device words */
 };
 
 struct K2Params {
@@ -254,6 +267,7 @@ struct K2Params {
     int rows, cols, toroidal, tiles_x;
     long long n;
     long long eps_bits;
+    int hpar, hepoch;
 };
 
 static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
@@ -392,12 +406,17 @@ static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int e
 
 __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant__ K1Params p)
 {
-    const int par = p.counts[4];
-    const int epoch = p.counts[6];
-    if (blockIdx.x == 0 && threadIdx.x < 2)
-        p.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists K2 will append to */
-    k1_work<false>(p, par, epoch, p.counts[par], p.counts[2 + par], p.counts + 7, blockIdx.x * blockDim.x + threadIdx.x,
-                   gridDim.x * blockDim.x);
+    const bool host = p.hpar >= 0;
+    const int par = host ? p.hpar : p.counts[4];
+    const int epoch = host ? p.hepoch : p.counts[6];
+    if (blockIdx.x == 0 && threadIdx.x < 3) {
+        if (threadIdx.x < 2)
+            p.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists K2 will append to */
+        else
+            p.counts[7 + (1 - par)] = 0; /* next step's tile count (read last by the previous K2) */
+    }
+    k1_work<false>(p, par, epoch, p.counts[par], p.counts[2 + par], p.counts + 7 + par,
+                   blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 /* append the lanes whose predicate holds to list/count (warp-aggregated) */
@@ -576,10 +595,17 @@ static __device__ __forceinline__ void k2_work(const K2Params& p, int par, int e
 
 __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2Params p)
 {
-    const int par = p.counts[4];
-    const int epoch = p.counts[6];
-    k2_work<false>(p, par, epoch, p.counts[7], p.counts[par], blockIdx.x, gridDim.x);
-    if (threadIdx.x == 0) {
+    const bool host = p.hpar >= 0;
+    const int par = host ? p.hpar : p.counts[4];
+    const int epoch = host ? p.hepoch : p.counts[6];
+    k2_work<false>(p, par, epoch, p.counts[7 + par], p.counts[par], blockIdx.x, gridDim.x);
+    if (host) {
+        /* nobody reads the device words during this launch */
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            p.counts[4] = 1 - par;
+            p.counts[6] = epoch + 1;
+        }
+    } else if (threadIdx.x == 0) {
         /* every block read parity, epoch and counts at its start; the last
          * one to finish advances them for the next step (no block waits for
          * another) */
@@ -588,14 +614,13 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
             p.counts[4] = 1 - par;
             p.counts[C_TICKET] = 0;
             p.counts[6] = epoch + 1;
-            p.counts[7] = 0;
         }
     }
 }
 
 /* ---- persistent form: every step of a run in one cooperative launch ----
  * The two phases of each step (K1's and K2's work) are separated by a grid
- * barrier.  counts[7 + (s & 1)] counts the flagged tiles of step s (one
+ * barrier.  counts[7 + parity] counts the flagged tiles of the step (one
  * step's count is cleared while the other is in use); counts[C_ARRIVED] is
  * the barrier's arrival counter (zeroed before the launch), counts[C_ERROR]
  * the error flag.  Only one thread per block touches the shared words: it
@@ -672,12 +697,12 @@ __global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ 
      * every SM whatever their number */
     const int tid = ((threadIdx.x >> 5) * (int)nb + blockIdx.x) * 32 + (threadIdx.x & 31);
     for (int s = 0; s < nsteps; s++) {
-        int* tcount = a.counts + 7 + (s & 1);
+        int* tcount = a.counts + 7 + par;
         if (blockIdx.x == 0 && threadIdx.x < 3) {
             if (threadIdx.x < 2)
                 a.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists phase B appends to */
             else
-                a.counts[7 + ((s + 1) & 1)] = 0; /* next step's tile count (read last in step s - 1) */
+                a.counts[7 + (1 - par)] = 0; /* next step's tile count (read last in step s - 1) */
         }
         k1_work<true>(a, par, epoch, s_cnt[0], s_cnt[1], tcount, tid, nb * THREADS);
         /* then: the flagged tiles of this step and the current wet count */
@@ -765,6 +790,9 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         blocks = 152 * 16;
     k_prime<<<blocks, THREADS, 0, st>>>(h, n, eps_bits, s.list[0], s.counts + 0);
     s.primed = true;
+    s.hpar = 0; /* what k_prime leaves: parity 0, epoch 1 */
+    s.hepoch = 1;
+    s.hknown = true;
     return cudaGetLastError() == cudaSuccess;
 }
 
@@ -807,6 +835,32 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     b.tiles_x = s.tiles_x;
     b.n = s.n;
     b.eps_bits = eps_bits;
+    /* eager launches carry parity and epoch; a step being recorded reads the
+     * device words (its replays must not depend on the host) */
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess)
+        cs = cudaStreamCaptureStatusActive;
+    a.hpar = b.hpar = -1;
+    a.hepoch = b.hepoch = 0;
+    if (cs == cudaStreamCaptureStatusNone) {
+        if (!s.hknown) {
+            int w[8];
+            if (cudaMemcpyAsync(w, s.counts, sizeof(w), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+                cudaStreamSynchronize(st) == cudaSuccess) {
+                s.hpar = w[4];
+                s.hepoch = w[6];
+                s.hknown = true;
+            }
+        }
+        if (s.hknown) {
+            a.hpar = b.hpar = s.hpar;
+            a.hepoch = b.hepoch = s.hepoch;
+            s.hpar = 1 - s.hpar;
+            s.hepoch++;
+        }
+    } else {
+        s.hknown = false;
+    }
     if (ev)
         cudaEventRecord(ev[0], st);
     k1_outflows<<<g_k1_blocks, K1_THREADS, 0, st>>>(a);
@@ -826,6 +880,7 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
                     int nsteps, cudaStream_t st)
 {
     State& s = g_state;
+    s.hknown = false; /* the kernel advances parity and epoch on the device */
     static int grid = 0;
     if (!grid) {
         int per_sm = 0, dev = 0, sms = 0;
@@ -860,6 +915,8 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
     b.h = h;
     b.f = s.f;
     b.eps_bits = eps_bits;
+    a.hpar = b.hpar = -1;
+    a.hepoch = b.hepoch = 0;
     cudaMemsetAsync(s.counts + C_ARRIVED, 0, sizeof(int), st); /* barrier counter */
     cudaMemsetAsync(s.counts + C_ERROR, 0, sizeof(int), st);   /* error flag */
     void* args[] = {&a, &b, &nsteps};
@@ -1286,6 +1343,7 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
                                  const double* z0, const double* h0, double* z_out, double* h_out, long* n_active,
                                  int* cells_out, int mode, int graph, double* ms)
 {
+    sdt2::g_state.hknown = false; /* launches this library did not see may have run since */
     calClearError();
     if (mode == SDT_MODE_FUSED && ac)
         return CAL_ERROR_INVALID_ARGUMENT;
@@ -1458,6 +1516,7 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
 /* back to the state right after init (device to device; queued) */
 extern "C" int cal_sciddicaT_reset(void* handle)
 {
+    sdt2::g_state.hknown = false; /* launches this library did not see may have run since */
     SdtSession* s = (SdtSession*)handle;
     sciddicaT_step_invalidate();
     cudaStream_t st = (cudaStream_t)calGetStream2D(s->ca);
@@ -1478,6 +1537,7 @@ extern "C" int cal_sciddicaT_reset(void* handle)
 /* queue `steps` steps; graph != 0 replays a recorded step */
 extern "C" int cal_sciddicaT_steps(void* handle, int steps, int graph)
 {
+    sdt2::g_state.hknown = false; /* launches this library did not see may have run since */
     SdtSession* s = (SdtSession*)handle;
     if (graph == 4) {
         /* every step in one cooperative launch (split step, plain mode) */
@@ -1563,6 +1623,7 @@ extern "C" int cal_sciddicaT_persist_failed(void* handle)
 extern "C" int cal_sciddicaT_host_run(void* handle, const double* z_host, const double* h_host, int steps, int graph,
                                       double* h_out)
 {
+    sdt2::g_state.hknown = false; /* launches this library did not see may have run since */
     SdtSession* s = (SdtSession*)handle;
     /* the inputs go straight from the caller's arrays to the device (both
      * layers, as the program's file loader leaves them); the outflows are
@@ -1582,6 +1643,7 @@ extern "C" int cal_sciddicaT_host_run(void* handle, const double* z_host, const 
  * single fused kernel -> ms_a[k] = the kernel, ms_b[k] = 0 */
 extern "C" int cal_sciddicaT_kernel_times(void* handle, int n, float* ms_a, float* ms_b)
 {
+    sdt2::g_state.hknown = false; /* launches this library did not see may have run since */
     SdtSession* s = (SdtSession*)handle;
     cudaStream_t st = (cudaStream_t)calGetStream2D(s->ca);
     cudaEvent_t* ev = (cudaEvent_t*)malloc(sizeof(cudaEvent_t) * 3 * n);
