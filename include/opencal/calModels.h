@@ -45,9 +45,9 @@ int cal_sciddicaT_steps(void* session, int steps, int graph);
 /* 1 when a grid barrier of the last persistent run gave up (synchronises) */
 int cal_sciddicaT_persist_failed(void* session);
 int cal_sciddicaT_set_params(void* session, double p_r, double p_eps);
-/* launch grids of the split step's kernels: k1_blocks 64-thread blocks of
- * the outflow kernel, k2_blocks 256-thread blocks of the update kernel
- * (0 = the defaults 4864 / 608) */
+/* launch grids of the split step's kernels: k1_blocks and k2_blocks
+ * 256-thread blocks of the outflow and the update kernel (0 = the defaults
+ * 608 / 608) */
 int cal_sciddicaT_set_split_grid(void* session, int k1_blocks, int k2_blocks);
 void* cal_sciddicaT_stream(void* session); /* cudaStream_t of the model */
 /* the dense step's TMA-staged form (flat grids, rows a multiple of 16 bytes;

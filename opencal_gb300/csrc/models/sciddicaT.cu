@@ -275,14 +275,19 @@ static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
     return (i / TH) * tiles_x + (j / TW);
 }
 
-constexpr int K1_THREADS = 64; /* small blocks: the wet list spreads over every SM */
+/* K1: 608 blocks of 256 threads.  Launch cost grows with the number of
+ * blocks (measured on GB300: 4864 blocks of 64 threads cost ~2 us per
+ * launch more than 608 blocks), so the wet cells' spread over every SM comes
+ * from the mapping instead: chunks of 32 list entries go to consecutive
+ * blocks (k1_outflows) */
+constexpr int K1_THREADS = 256;
 /* control words, each group on its own 128-byte line: the K2 ticket and the
  * persistent kernel's barrier counter are hit by every block and polled,
  * and must not share a line with the list and tile counters */
 constexpr int NCOUNTS = 128;
 constexpr int C_TICKET = 32, C_ARRIVED = 64, C_ERROR = 96;
 constexpr int K2_BLOCKS = 152 * 4;
-static int g_k1_blocks = 152 * 32, g_k2_blocks = K2_BLOCKS; /* launch grids of K1 and K2 (tunable) */
+static int g_k1_blocks = 152 * 4, g_k2_blocks = K2_BLOCKS; /* launch grids of K1 and K2 (tunable) */
 
 /* Loads of data that other blocks write while the kernel runs.  In the
  * persistent kernel (CO = true) they are weak ld.global (L1-cacheable)
@@ -415,8 +420,11 @@ __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant_
         else
             p.counts[7 + (1 - par)] = 0; /* next step's tile count (read last by the previous K2) */
     }
-    k1_work<false>(p, par, epoch, p.counts[par], p.counts[2 + par], p.counts + 7 + par,
-                   blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+    /* list entries in chunks of 32 (one per warp); consecutive chunks on
+     * consecutive blocks, which the hardware places on different SMs */
+    const int tid = ((threadIdx.x >> 5) * (int)gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);
+    k1_work<false>(p, par, epoch, p.counts[par], p.counts[2 + par], p.counts + 7 + par, tid,
+                   gridDim.x * blockDim.x);
 }
 
 /* append the lanes whose predicate holds to list/count (warp-aggregated) */
@@ -1577,15 +1585,15 @@ extern "C" int cal_sciddicaT_set_params(void* handle, double p_r, double p_eps)
     return calGetLastError();
 }
 
-/* launch grids of the split step's two kernels (64-thread K1 blocks,
- * 256-thread K2 blocks; 0 restores the default 4864 / 608); a recorded
+/* launch grids of the split step's two kernels (256-thread blocks; 0
+ * restores the default 608 / 608); a recorded
  * step, which bakes them into its launches, is dropped */
 extern "C" int cal_sciddicaT_set_split_grid(void* handle, int k1_blocks, int k2_blocks)
 {
     SdtSession* s = (SdtSession*)handle;
     if (k1_blocks < 0 || k2_blocks < 0)
         return CAL_ERROR_INVALID_ARGUMENT;
-    sdt2::g_k1_blocks = k1_blocks ? k1_blocks : 152 * 32;
+    sdt2::g_k1_blocks = k1_blocks ? k1_blocks : 152 * 4;
     sdt2::g_k2_blocks = k2_blocks ? k2_blocks : sdt2::K2_BLOCKS;
     calRunSetGraph2D(s->run, CAL_FALSE);
     return calGetLastError();
