@@ -365,11 +365,68 @@ def gpu_arm(args):
         "consistent": consistent,
         "clocks": clk,
     }
+    if not args.no_ac:
+        line["active_cells_on"] = active_cells_section(m, cal, z, h, hh)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(z, h)
     if not args.no_calibration:
         line["calibration"] = calibration_section(args)
     print(json.dumps(line), flush=True)
+
+
+def active_cells_section(m, cal, z, h, h_plain):
+    """The same workload with active cells on, 4000 steps per run, eager and
+    device-driven loops, in two forms: the reference program (its three
+    device processes over the device-compacted active-cell list, an update
+    after each, the steering resetting the active cells' outflows; model
+    created with CAL_OPT_ACTIVE_CELLS) and the active-cells split step (two
+    kernels per step, epoch marks for the active set).  The two must give
+    identical bits; agreement with the plain run's final h (the modes differ
+    by rounding where the reference keeps stale outflows at cells removed
+    exactly at the threshold) and mass are reported."""
+    import torch
+    forms, outs = {}, {}
+    for form, mode in (("processes", cal.MODE_PROCESSES), ("split", cal.MODE_FUSED)):
+        sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 1, P_R, P_EPS, z.ctypes.data, h.ctypes.data, mode)
+        if not sess:
+            return {"error": f"cal_sciddicaT_open ({form}) failed: " + cal.core().calGetErrorString().decode()}
+        stream = torch.cuda.ExternalStream(m.cal_sciddicaT_stream(sess))
+        for name, loop in (("eager", 0), ("device", 2)):
+            ms = []
+            for it in range(3):
+                m.cal_sciddicaT_reset(sess)
+                with torch.cuda.stream(stream):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    rc = m.cal_sciddicaT_steps(sess, CA_STEPS, loop)
+                    e1.record(stream)
+                e1.synchronize()
+                if rc:
+                    m.cal_sciddicaT_close(sess)
+                    return {"error": f"cal_sciddicaT_steps ({form}, {name}) failed: {rc}"}
+                if it:
+                    ms.append(e0.elapsed_time(e1))
+            forms[f"{form}_{name}"] = float(np.mean(ms))
+        hac = np.empty_like(h)
+        m.cal_sciddicaT_read(sess, hac.ctypes.data)
+        outs[form] = hac
+        m.cal_sciddicaT_close(sess)
+    best = min(forms, key=forms.get)
+    hac = outs["split"]
+    scale = np.maximum(np.abs(h_plain), 1e-300)
+    rel = np.abs(hac - h_plain) / scale
+    wet = np.abs(h_plain) > P_EPS
+    return {
+        "workload": f"SCIDDICA-T {ROWS}x{COLS} FP64, flat, active cells on, {CA_STEPS} CA steps",
+        "ms_per_run": forms, "best": best,
+        "value": ROWS * COLS * CA_STEPS / (forms[best] * 1e-3), "unit": "cell-updates/s",
+        "identical_forms": bool(outs["split"].tobytes() == outs["processes"].tobytes()),
+        "wet_cells_at_end": int(np.count_nonzero(hac > P_EPS)),
+        "max_rel_diff_vs_plain_wet_cells": float(rel[wet].max()) if wet.any() else 0.0,
+        "max_abs_diff_vs_plain": float(np.abs(hac - h_plain).max()),
+        "mass_rel_diff_vs_plain": float(abs(hac.sum() - h_plain.sum()) / max(abs(h_plain.sum()), 1e-300)),
+    }
 
 
 ENS_INSTANCES = 256
@@ -811,6 +868,7 @@ def main():
     ap.add_argument("--impl", default="opencal", choices=["opencal", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--loop", default="eager", choices=sorted(LOOPS))
+    ap.add_argument("--no-ac", action="store_true", help="skip the active-cells-on run of the workload")
     ap.add_argument("--no-calibration", action="store_true", help="skip the batched-calibration section")
     ap.add_argument("--calib-iters", type=int, default=12)
     ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble"],

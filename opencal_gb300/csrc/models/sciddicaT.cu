@@ -37,6 +37,12 @@
 #include "opencal/cal2D.h"
 #include "opencal/cal2DRun.h"
 
+#include <string>
+
+namespace cal {
+void set_error(CALError code, const std::string& msg); /* the library's error state (calGetLastError) */
+}
+
 #define NUMBER_OF_OUTFLOWS 4
 
 /* ======================= 1. the reference program ======================= */
@@ -945,6 +951,304 @@ static int persist_failed(cudaStream_t st)
 
 } // namespace sdt2
 
+/* ======================= 2c. the split step with active cells ===========
+ * OpenCAL's active-cells program (flows, width update and removal of dry
+ * cells, an update after each, then the steering:
+ * OpenCAL/examples/cal_sciddicaT-activecells-glut/source/sciddicaT.c:20-146)
+ * as two kernels per step, with the same result bit for bit:
+ *  - after a step's steering every active cell has zero outflows and
+ *    h > epsilon (the removal took the others out); after the
+ *    initialisation every cell with h > 0 is active and all outflows are 0.
+ *    So the next flows process overwrites all four outflows of every active
+ *    cell that is wet and leaves the dry ones (after the initialisation
+ *    only) at 0: the steering never needs to run;
+ *  - a removed cell keeps its outflows (the steering zeroes active cells
+ *    only), and the width update of its neighbours, and its own if it is
+ *    activated again, read those stale values: one outflow array that keeps
+ *    them reproduces that;
+ *  - the active set is an epoch mark per cell: a cell is active in the step
+ *    whose epoch its mark holds.
+ *   K1 (flows): over the active list; a wet cell computes its outflows and
+ *      activates every neighbour whose flow was not eliminated (the mark set
+ *      by an atomic exchange; a newly marked cell is appended after the
+ *      list, so that K1 does not process it).
+ *   K2 (width update and removal): over the extended list; h receives the
+ *      four inflow-minus-outflow terms in the reference's order (an absent
+ *      neighbour of a flat grid gives 0), then cells with h > epsilon are
+ *      marked for the next step and appended to the next list; the others
+ *      drop out.
+ * The list order is not the reference's row-major rebuild; no value depends
+ * on it, and the active set is returned in row-major order. */
+namespace sdtac {
+
+constexpr int THREADS = 256, BLOCKS = 152 * 4;
+/* counts[0..1] list lengths by parity, [4] parity, [6] epoch, [8] cells
+ * activated by this step's K1, [32] K2 block ticket (own line) */
+constexpr int NCOUNTS = 64, C_PAR = 4, C_EPOCH = 6, C_EXT = 8, C_TICKET = 32;
+
+struct State {
+    struct CALModel2D* ca = nullptr;
+    double* f = nullptr; /* 4 * n outflows, SoA */
+    int* mark = nullptr; /* epoch of the step in which the cell is (or was last) active */
+    int* list[2] = {nullptr, nullptr};
+    int* counts = nullptr;
+    long long n = 0;
+    bool primed = false;
+};
+static State g_state;
+
+struct Params {
+    const double* __restrict__ z;
+    double* h;
+    double* f;
+    int* mark;
+    int* list0;
+    int* list1;
+    int* counts;
+    int rows, cols, toroidal;
+    long long n;
+    double eps, r;
+    long long eps_bits;
+};
+
+/* neighbour q (von Neumann order: north, west, east, south) of (i, j);
+ * false outside a flat grid */
+static __device__ __forceinline__ bool nbr(const Params& p, int i, int j, int q, int& a, int& b)
+{
+    a = q == 0 ? i - 1 : (q == 3 ? i + 1 : i);
+    b = q == 1 ? j - 1 : (q == 2 ? j + 1 : j);
+    if (p.toroidal) {
+        a = a < 0 ? a + p.rows : (a >= p.rows ? a - p.rows : a);
+        b = b < 0 ? b + p.cols : (b >= p.cols ? b - p.cols : b);
+        return true;
+    }
+    return (unsigned)a < (unsigned)p.rows && (unsigned)b < (unsigned)p.cols;
+}
+
+/* chunks of 32 list entries, one per warp, on consecutive blocks: the
+ * warp's first chunk and the stride between its chunks */
+static __device__ __forceinline__ int first_chunk()
+{
+    return (threadIdx.x >> 5) * (int)gridDim.x + blockIdx.x;
+}
+static __device__ __forceinline__ int chunk_stride()
+{
+    return (int)gridDim.x * (THREADS / 32);
+}
+
+__global__ void __launch_bounds__(THREADS) k1_flows(const __grid_constant__ Params p)
+{
+    const int par = p.counts[C_PAR], epoch = p.counts[C_EPOCH];
+    const int na = p.counts[par];
+    int* list = par ? p.list1 : p.list0;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        p.counts[1 - par] = 0; /* the list K2 appends to */
+    const int lane = threadIdx.x & 31;
+    for (int g = first_chunk(); g * 32 < na; g += chunk_stride()) {
+        const int k = g * 32 + lane;
+        if (k >= na)
+            continue;
+        const int c = list[k];
+        const double hc = p.h[c];
+        if (!sdt::is_wet(hc, p.eps_bits)) /* the reference returns at h <= epsilon */
+            continue;
+        const int i = c / p.cols, j = c - i * p.cols;
+        double u[4];
+        int nc[4];
+        bool in[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int a, b;
+            in[q] = nbr(p, i, j, q, a, b);
+            nc[q] = a * p.cols + b;
+            u[q] = in[q] ? __ldg(p.z + nc[q]) + p.h[nc[q]] : 0.0 + 0.0;
+        }
+        double f[4];
+        unsigned elim;
+        sdt::outflows(hc, __ldg(p.z + c), u[0], u[1], u[2], u[3], p.eps, p.r, f, &elim);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            p.f[q * p.n + c] = f[q];
+            /* calAddActiveCellX2D for every neighbour whose flow is kept */
+            if (!(elim & (2u << q)) && in[q] && p.mark[nc[q]] != epoch &&
+                atomicExch(p.mark + nc[q], epoch) != epoch)
+                list[na + atomicAdd(p.counts + C_EXT, 1)] = nc[q];
+        }
+    }
+}
+
+/* append the lanes whose predicate holds (warp-aggregated; every lane of
+ * the warp calls it) */
+static __device__ __forceinline__ void warp_append(bool pred, int value, int* list, int* count)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0)
+        return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0)
+        base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (pred)
+        list[base + __popc(mask & ((1u << lane) - 1u))] = value;
+}
+
+__global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ Params p)
+{
+    const int par = p.counts[C_PAR], epoch = p.counts[C_EPOCH];
+    const int n2 = p.counts[par] + p.counts[C_EXT];
+    const int* list = par ? p.list1 : p.list0;
+    int* next = par ? p.list0 : p.list1;
+    int* ncount = p.counts + (1 - par);
+    const int lane = threadIdx.x & 31;
+    for (int g = first_chunk(); g * 32 < n2; g += chunk_stride()) {
+        const int k = g * 32 + lane;
+        bool keep = false;
+        int c = 0;
+        if (k < n2) {
+            c = list[k];
+            const int i = c / p.cols, j = c - i * p.cols;
+            double hn = p.h[c];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                /* inflow from neighbour n = q + 1 is its outflow f[3 - q] */
+                int a, b;
+                const double fin = nbr(p, i, j, q, a, b) ? p.f[(3 - q) * p.n + (long long)a * p.cols + b] : 0.0;
+                hn += fin - p.f[q * p.n + c];
+            }
+            p.h[c] = hn;
+            keep = sdt::is_wet(hn, p.eps_bits); /* the removal: h <= epsilon drops out */
+            if (keep)
+                p.mark[c] = epoch + 1;
+        }
+        warp_append(keep, c, next, ncount);
+    }
+    if (threadIdx.x == 0) {
+        /* the last block to finish advances parity and epoch */
+        __threadfence();
+        if (atomicAdd(reinterpret_cast<unsigned*>(p.counts + C_TICKET), 1u) == gridDim.x - 1) {
+            p.counts[C_PAR] = 1 - par;
+            p.counts[C_EPOCH] = epoch + 1;
+            p.counts[C_EXT] = 0;
+            p.counts[C_TICKET] = 0;
+        }
+    }
+}
+
+/* the initialisation's active set: every cell with h > 0 (epoch 1) */
+__global__ void __launch_bounds__(THREADS) k_prime(const double* __restrict__ h, long long n, int* mark, int* list,
+                                                   int* counts)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        counts[C_EPOCH] = 1;
+    const long long stride = (long long)gridDim.x * THREADS;
+    for (long long base = (long long)blockIdx.x * THREADS; base < n; base += stride) {
+        const long long c = base + threadIdx.x;
+        const bool act = c < n && h[c] > 0.0;
+        if (c < n)
+            mark[c] = act ? 1 : 0;
+        warp_append(act, (int)c, list, counts + 0);
+    }
+}
+
+static void release()
+{
+    State& s = g_state;
+    cudaFree(s.f);
+    cudaFree(s.mark);
+    cudaFree(s.list[0]);
+    cudaFree(s.list[1]);
+    cudaFree(s.counts);
+    s = State();
+}
+
+/* (re)allocate for `ca` and take the initialisation's state from h */
+static bool prime(struct CALModel2D* ca, const double* h, cudaStream_t st)
+{
+    State& s = g_state;
+    const long long n = (long long)ca->rows * ca->columns;
+    if (s.ca != ca || s.n != n) {
+        release();
+        s.ca = ca;
+        s.n = n;
+        bool ok = n <= 0x7fffffffLL && cudaMalloc(&s.f, 4 * n * sizeof(double)) == cudaSuccess &&
+                  cudaMalloc(&s.mark, n * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&s.list[0], n * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&s.list[1], n * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&s.counts, NCOUNTS * sizeof(int)) == cudaSuccess;
+        if (!ok) {
+            release();
+            return false;
+        }
+    }
+    cudaMemsetAsync(s.f, 0, 4 * n * sizeof(double), st);
+    cudaMemsetAsync(s.counts, 0, NCOUNTS * sizeof(int), st);
+    long long blocks = (n + THREADS - 1) / THREADS;
+    if (blocks > 152 * 16)
+        blocks = 152 * 16;
+    k_prime<<<(int)blocks, THREADS, 0, st>>>(h, n, s.mark, s.list[0], s.counts);
+    s.primed = cudaGetLastError() == cudaSuccess;
+    return s.primed;
+}
+
+/* one step: K1 then K2 on the model's stream */
+static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, double r, long long eps_bits,
+                 cudaStream_t st)
+{
+    State& s = g_state;
+    Params p;
+    p.z = z;
+    p.h = h;
+    p.f = s.f;
+    p.mark = s.mark;
+    p.list0 = s.list[0];
+    p.list1 = s.list[1];
+    p.counts = s.counts;
+    p.rows = ca->rows;
+    p.cols = ca->columns;
+    p.toroidal = ca->T == CAL_SPACE_TOROIDAL;
+    p.n = s.n;
+    p.eps = eps;
+    p.r = r;
+    p.eps_bits = eps_bits;
+    k1_flows<<<BLOCKS, THREADS, 0, st>>>(p);
+    k2_update<<<BLOCKS, THREADS, 0, st>>>(p);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+/* the active cells in row-major order (cells[2k], cells[2k + 1] = i, j;
+ * cells may be null) and their number; synchronises */
+static long read_active(int rows, int cols, int* cells, cudaStream_t st)
+{
+    State& s = g_state;
+    if (!s.primed)
+        return 0;
+    int c[NCOUNTS];
+    int* mark = (int*)malloc(sizeof(int) * (size_t)s.n);
+    if (!mark)
+        return 0;
+    if (cudaMemcpyAsync(c, s.counts, sizeof(c), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(mark, s.mark, sizeof(int) * (size_t)s.n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        free(mark);
+        return 0;
+    }
+    long m = 0;
+    for (long long k = 0; k < s.n; k++)
+        if (mark[k] == c[C_EPOCH]) {
+            if (cells) {
+                cells[2 * m] = (int)(k / cols);
+                cells[2 * m + 1] = (int)(k % cols);
+            }
+            m++;
+        }
+    free(mark);
+    (void)rows;
+    return m;
+}
+
+} // namespace sdtac
+
 /* ======================= 2c. the sparse fused step ======================
  * One launch per step.  A tile (32 x 16 cells) can only change in a step if
  * it holds a wet cell or borders one, so the step works on the tiles of
@@ -1256,6 +1560,10 @@ static void sciddicaT_split_transition_timed(struct CALModel2D* ca, cudaEvent_t*
         sciddicaT_split_prepare_now(ca);
         h = (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0);
     }
+    if (!sdt2::g_state.primed) {
+        cal::set_error(CAL_ERROR_OUT_OF_MEMORY, "SCIDDICA-T split step: buffers not allocated");
+        return;
+    }
     sdt2::step(ca, z, h, P.epsilon, P.r, eps_bits, st, ev);
     calMarkCurrentWritten2Dr(ca, Q.h);
 }
@@ -1266,6 +1574,34 @@ static void sciddicaT_step_invalidate()
 {
     sdt2::g_state.primed = false;
     sdt3::g_state.primed = false;
+    sdtac::g_state.primed = false;
+}
+
+/* the fused step of a run with active cells is the active-cells split step */
+static bool g_fused_ac = false;
+
+/* prime the active-cells split step from the initialised state (its
+ * active set: every cell with h > 0) unless it is primed for `ca` */
+static void sciddicaT_ac_prepare_now(struct CALModel2D* ca)
+{
+    if (sdtac::g_state.ca == ca && sdtac::g_state.primed)
+        return;
+    sdtac::prime(ca, (const double*)calGetDeviceBuffer2Dr(ca, Q.h, 0), (cudaStream_t)calGetStream2D(ca));
+}
+
+static void sciddicaT_ac_transition(struct CALModel2D* ca)
+{
+    sciddicaT_ac_prepare_now(ca);
+    if (!sdtac::g_state.primed) {
+        cal::set_error(CAL_ERROR_OUT_OF_MEMORY, "SCIDDICA-T active-cells split step: buffers not allocated");
+        return;
+    }
+    long long eps_bits;
+    memcpy(&eps_bits, &P.epsilon, sizeof(double));
+    const double* z = (const double*)calGetDeviceBuffer2Dr(ca, Q.z, 0);
+    double* h = (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0);
+    sdtac::step(ca, z, h, P.epsilon, P.r, eps_bits, (cudaStream_t)calGetStream2D(ca));
+    calMarkCurrentWritten2Dr(ca, Q.h);
 }
 
 /* prime the split step now (eagerly), handing h over from the sparse step
@@ -1288,6 +1624,10 @@ static void sciddicaT_split_prepare_now(struct CALModel2D* ca)
  * priming out of a step that is being recorded as a graph */
 static void sciddicaT_step_prepare(struct CALModel2D* ca)
 {
+    if (g_fused_ac) {
+        sciddicaT_ac_prepare_now(ca);
+        return;
+    }
     const SdtKernel k = sdt_kernel();
     if (k == SDT_SPLIT) {
         sciddicaT_split_prepare_now(ca);
@@ -1301,6 +1641,10 @@ static void sciddicaT_step_prepare(struct CALModel2D* ca)
 /* host side of the fused step: queue the kernel, then exchange the h layers */
 static void sciddicaT_fused_transition(struct CALModel2D* ca)
 {
+    if (g_fused_ac) {
+        sciddicaT_ac_transition(ca);
+        return;
+    }
     if (sdt_kernel() == SDT_SPARSE) {
         sciddicaT_sparse_transition(ca);
         return;
@@ -1344,7 +1688,8 @@ extern "C" int cal_sciddicaT_device_loop_fallbacks(void) { return g_fallbacks; }
 /* Runs SCIDDICA-T for `steps` steps on (z0, h0) and returns the final z, h
  * and active list -- the same contract as the oracle's orc_sciddicaT.
  * mode 0 runs the reference program (device processes); mode 1 the fused
- * step (plain mode only).  graph != 0 replays the step as a CUDA graph.
+ * step (plain mode: the split step; with active cells: the active-cells
+ * split step).  graph != 0 replays the step as a CUDA graph.
  * *ms receives the device time of the step loop (CUDA events).  Returns 0
  * on success, else the CALError code. */
 extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int steps, double p_r, double p_eps,
@@ -1353,18 +1698,22 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
 {
     sdt2::g_state.hknown = false; /* launches this library did not see may have run since */
     calClearError();
-    if (mode == SDT_MODE_FUSED && ac)
-        return CAL_ERROR_INVALID_ARGUMENT;
+    /* with active cells, the fused mode keeps its own active set (epoch
+     * marks) on a model without the active-cells option */
+    const bool fused_ac = mode == SDT_MODE_FUSED && ac;
     sciddicaT_step_invalidate();
+    g_fused_ac = fused_ac;
     struct CALModel2D* ca = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D,
                                        toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT,
-                                       ac ? CAL_OPT_ACTIVE_CELLS : CAL_NO_OPT);
-    if (!ca)
+                                       (ac && !fused_ac) ? CAL_OPT_ACTIVE_CELLS : CAL_NO_OPT);
+    if (!ca) {
+        g_fused_ac = false;
         return calGetLastError();
+    }
     struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
     P.epsilon = p_eps;
     P.r = p_r;
-    P.active = ac;
+    P.active = ac && !fused_ac;
     if (mode == SDT_MODE_PROCESSES) {
         calAddElementaryProcess2D(ca, sciddicaT_flows_computation);
         calAddElementaryProcess2D(ca, sciddicaT_width_update);
@@ -1433,12 +1782,20 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
         memcpy(z_out, Q.z->current, bytes);
     if (h_out)
         memcpy(h_out, Q.h->current, bytes);
-    if (n_active)
-        *n_active = ac ? ca->A.size_current : 0;
-    if (cells_out && ac)
-        memcpy(cells_out, ca->A.cells, sizeof(int) * 2 * (size_t)ca->A.size_current);
+    if (fused_ac) {
+        const long m = sdtac::read_active(rows, cols, cells_out, s);
+        if (n_active)
+            *n_active = m;
+    } else {
+        if (n_active)
+            *n_active = ac ? ca->A.size_current : 0;
+        if (cells_out && ac)
+            memcpy(cells_out, ca->A.cells, sizeof(int) * 2 * (size_t)ca->A.size_current);
+    }
     int err = calGetLastError();
     sdt2::release();
+    sdtac::release();
+    g_fused_ac = false;
     calRunFinalize2D(run);
     calFinalize2D(ca);
     return err;
@@ -1454,6 +1811,7 @@ struct SdtSession {
     struct CALModel2D* ca;
     struct CALRun2D* run;
     int mode, ac;
+    int fused_ac; /* active cells in fused mode: the active-cells split step */
     size_t bytes;
     double* snap[6][2]; /* device copies of z, h, f0..f3 (both layers) after init */
     CALbyte* snap_flags;
@@ -1465,23 +1823,24 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
                                     const double* z0, const double* h0, int mode)
 {
     calClearError();
-    if (mode == SDT_MODE_FUSED && ac)
-        return nullptr;
     sciddicaT_step_invalidate();
     SdtSession* s = (SdtSession*)calloc(1, sizeof(SdtSession));
     s->mode = mode;
     s->ac = ac;
+    s->fused_ac = mode == SDT_MODE_FUSED && ac;
+    g_fused_ac = s->fused_ac;
     s->bytes = sizeof(double) * (size_t)rows * cols;
     s->ca = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D, toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT,
-                       ac ? CAL_OPT_ACTIVE_CELLS : CAL_NO_OPT);
+                       (ac && !s->fused_ac) ? CAL_OPT_ACTIVE_CELLS : CAL_NO_OPT);
     if (!s->ca) {
+        g_fused_ac = false;
         free(s);
         return nullptr;
     }
     s->run = calRunDef2D(s->ca, 1, CAL_RUN_LOOP, CAL_UPDATE_IMPLICIT);
     P.epsilon = p_eps;
     P.r = p_r;
-    P.active = ac;
+    P.active = ac && !s->fused_ac;
     if (mode == SDT_MODE_PROCESSES) {
         calAddElementaryProcess2D(s->ca, sciddicaT_flows_computation);
         calAddElementaryProcess2D(s->ca, sciddicaT_width_update);
@@ -1509,7 +1868,7 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
             cudaMemcpyAsync(s->snap[k][l], calGetDeviceBuffer2Dr(s->ca, sdt_sub(k), l), s->bytes,
                             cudaMemcpyDeviceToDevice, st);
         }
-    if (ac) {
+    if (ac && !s->fused_ac) {
         CALbyte* flags;
         calGetDeviceActiveCells2D(s->ca, &flags, nullptr, nullptr);
         cudaMalloc(&s->snap_flags, (size_t)rows * cols);
@@ -1532,7 +1891,7 @@ extern "C" int cal_sciddicaT_reset(void* handle)
         for (int l = 0; l < 2; l++)
             cudaMemcpyAsync(calGetDeviceBuffer2Dr(s->ca, sdt_sub(k), l == 0 ? 0 : 2), s->snap[k][l], s->bytes,
                             cudaMemcpyDeviceToDevice, st);
-    if (s->ac) {
+    if (s->ac && !s->fused_ac) {
         CALbyte* flags;
         calGetDeviceActiveCells2D(s->ca, &flags, nullptr, nullptr);
         cudaMemcpyAsync(flags, s->snap_flags, (size_t)s->ca->rows * s->ca->columns, cudaMemcpyDeviceToDevice, st);
@@ -1549,9 +1908,11 @@ extern "C" int cal_sciddicaT_steps(void* handle, int steps, int graph)
     SdtSession* s = (SdtSession*)handle;
     if (graph == 4) {
         /* every step in one cooperative launch (split step, plain mode) */
-        if (s->mode != SDT_MODE_FUSED)
+        if (s->mode != SDT_MODE_FUSED || s->fused_ac)
             return CAL_ERROR_INVALID_ARGUMENT;
         sciddicaT_split_prepare_now(s->ca);
+        if (!sdt2::g_state.primed)
+            return CAL_ERROR_OUT_OF_MEMORY;
         long long eps_bits;
         memcpy(&eps_bits, &P.epsilon, sizeof(double));
         const double* z = (const double*)calGetDeviceBuffer2Dr(s->ca, Q.z, 0);
@@ -1712,6 +2073,8 @@ extern "C" void cal_sciddicaT_close(void* handle)
             cudaFree(s->snap[k][l]);
     cudaFree(s->snap_flags);
     sdt2::release();
+    sdtac::release();
+    g_fused_ac = false;
     calRunFinalize2D(s->run);
     calFinalize2D(s->ca);
     free(s);

@@ -47,7 +47,8 @@ static __device__ __forceinline__ bool is_wet(double h, long long eps_bits)
  * remaining cells and the comparisons are done on the integer pipe with
  * bit-identical results (exact_div.cuh). */
 static __device__ __forceinline__ void outflows(double hc, double zc, const double u1, const double u2,
-                                                const double u3, const double u4, double eps, double r, double f[4])
+                                                const double u3, const double u4, double eps, double r, double f[4],
+                                                unsigned* elim_out = nullptr)
 {
     double u[5];
     const double m = hc - eps;
@@ -81,6 +82,8 @@ static __device__ __forceinline__ void outflows(double hc, double zc, const doub
 #pragma unroll
     for (int n = 1; n < 5; n++)
         f[n - 1] = (elim & (1u << n)) ? 0.0 : (average - u[n]) * r;
+    if (elim_out)
+        *elim_out = elim; /* bit n: neighbour n (1..4) eliminated; bit 0: the cell itself */
 }
 
 static __device__ __forceinline__ int wrapi(int x, int n)

@@ -122,6 +122,35 @@ def test_sciddicaT_shipped_golden_processes_ac(cal):
     assert len(cells) > 0
 
 
+@pytest.mark.parametrize("rows,cols,seed,steps,tor", SDT_CASES)
+@pytest.mark.parametrize("graph", [0, 1, 2])
+def test_sciddicaT_active_cells_split_bit_exact(cal, orc, rows, cols, seed, steps, tor, graph):
+    """The fused mode with active cells runs the active-cells split step (two
+    kernels per step, epoch marks for the active set, the outflows of removed
+    cells kept as the reference keeps them): the oracle's active-cells run
+    bit for bit, h, z and the active set, eager, replayed and device-driven."""
+    z, h = W.sciddicaT_inputs(rows, cols, seed=seed)
+    ref = orc.sciddicaT(z, h, steps, toroidal=tor, ac=True)
+    got = cal.sciddicaT(z, h, steps, toroidal=tor, ac=True, mode=cal.MODE_FUSED, graph=graph)
+    assert_same(got[0], ref[0], "z")
+    assert_same(got[1], ref[1], "h")
+    assert len(ref[2]) > 0
+    assert np.array_equal(got[2], ref[2]), "active cells"
+
+
+def test_sciddicaT_shipped_golden_active_cells_split(cal):
+    """The reference's active-cells example on its shipped data, 4000 steps,
+    through the active-cells split step: the same printed result as the
+    device-process run."""
+    g = np.load(os.path.join(GOLDEN, "sciddicaT_610x496.npz"))
+    _, h, cells = cal.sciddicaT(g["z"], g["h0"], 4000, toroidal=True, ac=True, mode=cal.MODE_FUSED)
+    printed = np.array([[float("%.9f" % v) for v in row] for row in h])
+    assert np.array_equal(printed, g["h_ac_ref_run"])
+    _, hp, cp = cal.sciddicaT(g["z"], g["h0"], 4000, toroidal=True, ac=True, mode=cal.MODE_PROCESSES)
+    assert_same(h, hp, "h (split vs processes)")
+    assert np.array_equal(cells, cp), "active cells (split vs processes)"
+
+
 # ---------------------------------------------------------------- Life
 
 @pytest.mark.parametrize("tor", [0, 1])
