@@ -23,7 +23,9 @@ extern "C" {
 
 /* mode: 0 = the reference program (device elementary processes registered
  * with calAddElementaryProcess2D, steering, calRun2D); 1 = the same program
- * with the split step as its global transition (plain only).  graph: 0 =
+ * with the split step as its global transition (with ac: the active-cells
+ * split step, which keeps its own active set and returns it in row-major
+ * order, the reference's order).  graph: 0 =
  * launch sequence per step, 1 = recorded step replayed, 2 = device-driven
  * loop bounded by the final step, 3 = device loop ended by a device stop
  * condition.  n_active / cells_out: the active cells after the run (ac). */
