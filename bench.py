@@ -328,9 +328,10 @@ def gpu_arm(args):
 
     if rank != 0:
         return
-    # DRAM bytes of one step (K1 + K2) from the committed ncu capture
+    # DRAM bytes of one step from the committed ncu capture of the timed form
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"sciddicaT_{STEP_KERNEL}_step_2048.json")
+    tname = "persist" if args.loop == "persistent" else STEP_KERNEL
+    tpath = os.path.join(ROOT, "profiles", f"sciddicaT_{tname}_step_2048.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             traffic = json.load(f).get("dram_bytes_per_step")
@@ -352,8 +353,8 @@ def gpu_arm(args):
                      "kernel": kernel_desc,
                      "basis": "achieved = 24 B x rows x cols per step (dense algorithmic bytes) / mean step "
                               "time of the timed runs (CUDA events on the model's stream around each 4000-step "
-                              "run, / 4000), i.e. value x 24 B; traffic = ncu DRAM bytes of one step at step "
-                              "~1000 (fields stay in L2)",
+                              "run, / 4000), i.e. value x 24 B; traffic = ncu DRAM bytes per step of the timed "
+                              "form around step 1000 (fields stay in L2)",
                      "step_avg_ms": step_ms,
                      "at_step_1000": {"k1_ms": k1_ms, "k2_ms": k2_ms, "achieved": achieved_1000,
                                       "frac": achieved_1000 / peak,
@@ -867,7 +868,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="opencal", choices=["opencal", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--loop", default="eager", choices=sorted(LOOPS))
+    ap.add_argument("--loop", default="persistent", choices=sorted(LOOPS))
     ap.add_argument("--no-ac", action="store_true", help="skip the active-cells-on run of the workload")
     ap.add_argument("--no-calibration", action="store_true", help="skip the batched-calibration section")
     ap.add_argument("--calib-iters", type=int, default=12)

@@ -290,45 +290,39 @@ constexpr int K1_THREADS = 256;
 /* control words, each group on its own 128-byte line: the K2 ticket and the
  * persistent kernel's barrier counter are hit by every block and polled,
  * and must not share a line with the list and tile counters */
-constexpr int NCOUNTS = 128;
+constexpr int NCOUNTS = 512;
 constexpr int C_TICKET = 32, C_ARRIVED = 64, C_ERROR = 96;
+/* the persistent kernel's placement census: a flag (own line) and blocks
+ * per SM, for SM ids below MAX_SM */
+constexpr int C_PLACE_BAD = 128, C_SMRANK = 256, MAX_SM = 256;
 constexpr int K2_BLOCKS = 152 * 4;
 static int g_k1_blocks = 152 * 4, g_k2_blocks = K2_BLOCKS; /* launch grids of K1 and K2 (tunable) */
 
 /* Loads of data that other blocks write while the kernel runs.  In the
- * persistent kernel (CO = true) they are weak ld.global (L1-cacheable)
- * loads written out in PTX, so that the compiler cannot turn them into
- * non-coherent loads through the const __restrict__ parameters: the grid
- * barrier between the phases (a gpu-scope fence and acquire by one thread,
- * then bar.sync) orders them after every write of the previous phase.  The
- * per-step kernels use the ordinary paths (a kernel boundary orders them). */
-static __device__ __forceinline__ int ld_weak(const int* p)
+ * persistent kernel (CO = true) they are plain coherent loads through a
+ * pointer passed through a register move, so that the compiler can neither
+ * turn them into non-coherent loads (the parameters are const __restrict__)
+ * nor is kept from batching them (inline-asm loads with a memory clobber,
+ * __ldcg included, are issued one after another); the grid barrier between
+ * the phases (a gpu-scope fence and acquire by one thread, then bar.sync)
+ * orders them after every write of the previous phase.  The per-step
+ * kernels use the ordinary paths (a kernel boundary orders them). */
+template <typename T>
+static __device__ __forceinline__ const T* launder(const T* p)
 {
-    int v;
-    asm volatile("ld.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-static __device__ __forceinline__ double ld_weak(const double* p)
-{
-    double v;
-    asm volatile("ld.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
-    return v;
-}
-static __device__ __forceinline__ double2 ld_weak(const double2* p)
-{
-    double2 v;
-    asm volatile("ld.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
-    return v;
+    const T* q;
+    asm("mov.b64 %0, %1;" : "=l"(q) : "l"(p));
+    return q;
 }
 template <bool CO, typename T>
 static __device__ __forceinline__ T ldm(const T* p)
 {
-    return CO ? ld_weak(p) : *p;
+    return CO ? *launder(p) : *p;
 }
 template <bool CO>
 static __device__ __forceinline__ double ldh(const double* p)
 {
-    return CO ? ld_weak(p) : __ldg(p);
+    return CO ? *launder(p) : __ldg(p);
 }
 
 /* flag tile t for this step's K2 and append it to the work-list once */
@@ -688,10 +682,37 @@ static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblock
 }
 
 __global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ K1Params a,
-                                                     const __grid_constant__ K2Params b, int nsteps)
+                                                     const __grid_constant__ K2Params b, int nsteps, int nsm)
 {
     __shared__ int s_cnt[2];
     __shared__ int s_state[2];
+    __shared__ int s_v;
+    const unsigned nb = gridDim.x;
+    unsigned round = 0;
+    /* K2's tile items go to blocks in the order v = (rank of the block on its
+     * SM) * SMs + SM, so that they spread over the SMs first: a cooperative
+     * launch places its first blocks several to an SM, and K2's few tiles
+     * would otherwise share their FP64 pipes.  v is a permutation of the
+     * blocks when every block finds its SM id below nsm and its rank below
+     * nb / nsm (nb distinct pairs in nb places); if one does not, every
+     * block keeps its launch index. */
+    if (threadIdx.x == 0) {
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        int v = -1;
+        if (nsm > 0 && smid < (unsigned)nsm && smid < (unsigned)MAX_SM && nb % (unsigned)nsm == 0) {
+            const int rank = atomicAdd(a.counts + C_SMRANK + smid, 1);
+            if (rank < (int)(nb / (unsigned)nsm))
+                v = rank * nsm + (int)smid;
+        }
+        if (v < 0)
+            atomicExch(a.counts + C_PLACE_BAD, 1);
+        s_v = v;
+    }
+    if (!grid_barrier(a.counts, nb, round, a.counts + C_PLACE_BAD, a.counts + C_PLACE_BAD, s_cnt))
+        return;
+    const int vb = s_cnt[0] ? (int)blockIdx.x : s_v;
+    __syncthreads(); /* s_cnt is reused below */
     if (threadIdx.x == 0) {
         s_state[0] = __ldcg(a.counts + 4);
         s_state[1] = __ldcg(a.counts + 6);
@@ -704,12 +725,10 @@ __global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ 
         s_cnt[1] = __ldcg(a.counts + 2 + par);
     }
     __syncthreads();
-    const unsigned nb = gridDim.x;
-    unsigned round = 0;
     /* K1's list entries in chunks of 32 (one per warp), consecutive chunks
-     * on consecutive blocks, so that the wet cells' FP64 work spreads over
-     * every SM whatever their number */
-    const int tid = ((threadIdx.x >> 5) * (int)nb + blockIdx.x) * 32 + (threadIdx.x & 31);
+     * on consecutive blocks in the order v, so that the wet cells' FP64 work
+     * spreads over every SM whatever their number */
+    const int tid = ((threadIdx.x >> 5) * (int)nb + vb) * 32 + (threadIdx.x & 31);
     for (int s = 0; s < nsteps; s++) {
         int* tcount = a.counts + 7 + par;
         if (blockIdx.x == 0 && threadIdx.x < 3) {
@@ -722,7 +741,7 @@ __global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ 
         /* then: the flagged tiles of this step and the current wet count */
         if (!grid_barrier(a.counts, nb, round, tcount, a.counts + par, s_cnt))
             return;
-        k2_work<true>(b, par, epoch, s_cnt[0], s_cnt[1], blockIdx.x, nb);
+        k2_work<true>(b, par, epoch, s_cnt[0], s_cnt[1], vb, nb);
         par = 1 - par;
         epoch++;
         /* then: the next step's wet and dried counts */
@@ -895,13 +914,14 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
 {
     State& s = g_state;
     s.hknown = false; /* the kernel advances parity and epoch on the device */
-    static int grid = 0;
+    static int grid = 0, sms_of_device = 0;
     if (!grid) {
         int per_sm = 0, dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persist, THREADS, 0);
         grid = sms * per_sm;
+        sms_of_device = sms;
         if (grid <= 0)
             return false;
     }
@@ -933,7 +953,9 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
     a.hepoch = b.hepoch = 0;
     cudaMemsetAsync(s.counts + C_ARRIVED, 0, sizeof(int), st); /* barrier counter */
     cudaMemsetAsync(s.counts + C_ERROR, 0, sizeof(int), st);   /* error flag */
-    void* args[] = {&a, &b, &nsteps};
+    cudaMemsetAsync(s.counts + C_PLACE_BAD, 0, (NCOUNTS - C_PLACE_BAD) * sizeof(int), st); /* placement census */
+    int nsm = sms_of_device;
+    void* args[] = {&a, &b, &nsteps, &nsm};
     return cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(THREADS), args, 0, st) ==
            cudaSuccess;
 }
