@@ -381,8 +381,8 @@ def active_cells_section(m, cal, z, h, h_plain):
     device processes over the device-compacted active-cell list, an update
     after each, the steering resetting the active cells' outflows; model
     created with CAL_OPT_ACTIVE_CELLS) and the active-cells split step (two
-    kernels per step, epoch marks for the active set).  The two must give
-    identical bits; agreement with the plain run's final h (the modes differ
+    kernels per step, epoch marks for the active set; also every step in
+    one cooperative launch).  The two must give identical bits; agreement with the plain run's final h (the modes differ
     by rounding where the reference keeps stale outflows at cells removed
     exactly at the threshold) and mass are reported."""
     import torch
@@ -392,7 +392,8 @@ def active_cells_section(m, cal, z, h, h_plain):
         if not sess:
             return {"error": f"cal_sciddicaT_open ({form}) failed: " + cal.core().calGetErrorString().decode()}
         stream = torch.cuda.ExternalStream(m.cal_sciddicaT_stream(sess))
-        for name, loop in (("eager", 0), ("device", 2)):
+        loops = (("eager", 0), ("device", 2)) + ((("persistent", 4),) if form == "split" else ())
+        for name, loop in loops:
             ms = []
             for it in range(3):
                 m.cal_sciddicaT_reset(sess)
@@ -403,7 +404,7 @@ def active_cells_section(m, cal, z, h, h_plain):
                     rc = m.cal_sciddicaT_steps(sess, CA_STEPS, loop)
                     e1.record(stream)
                 e1.synchronize()
-                if rc:
+                if rc or (loop == 4 and m.cal_sciddicaT_persist_failed(sess)):
                     m.cal_sciddicaT_close(sess)
                     return {"error": f"cal_sciddicaT_steps ({form}, {name}) failed: {rc}"}
                 if it:

@@ -681,38 +681,47 @@ static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblock
     return s_ok != 0;
 }
 
-__global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ K1Params a,
-                                                     const __grid_constant__ K2Params b, int nsteps, int nsm)
+/* The order in which a persistent kernel deals work to its blocks:
+ * v = (rank of the block on its SM) * SMs + SM, so that consecutive work
+ * items go to different SMs first (a cooperative launch places its first
+ * blocks several to an SM).  v is a permutation of the blocks when every
+ * block finds its SM id below nsm and its rank below nb / nsm (nb distinct
+ * pairs in nb places); if one does not, every block keeps its launch index.
+ * Needs counts[C_PLACE_BAD] and counts[C_SMRANK ...] zeroed before the
+ * launch; one grid barrier.  Returns -1 when that barrier gave up. */
+static __device__ int placement_order(int* counts, unsigned nb, int nsm, unsigned& round, int* s_tmp)
 {
-    __shared__ int s_cnt[2];
-    __shared__ int s_state[2];
     __shared__ int s_v;
-    const unsigned nb = gridDim.x;
-    unsigned round = 0;
-    /* K2's tile items go to blocks in the order v = (rank of the block on its
-     * SM) * SMs + SM, so that they spread over the SMs first: a cooperative
-     * launch places its first blocks several to an SM, and K2's few tiles
-     * would otherwise share their FP64 pipes.  v is a permutation of the
-     * blocks when every block finds its SM id below nsm and its rank below
-     * nb / nsm (nb distinct pairs in nb places); if one does not, every
-     * block keeps its launch index. */
     if (threadIdx.x == 0) {
         unsigned smid;
         asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
         int v = -1;
         if (nsm > 0 && smid < (unsigned)nsm && smid < (unsigned)MAX_SM && nb % (unsigned)nsm == 0) {
-            const int rank = atomicAdd(a.counts + C_SMRANK + smid, 1);
+            const int rank = atomicAdd(counts + C_SMRANK + smid, 1);
             if (rank < (int)(nb / (unsigned)nsm))
                 v = rank * nsm + (int)smid;
         }
         if (v < 0)
-            atomicExch(a.counts + C_PLACE_BAD, 1);
+            atomicExch(counts + C_PLACE_BAD, 1);
         s_v = v;
     }
-    if (!grid_barrier(a.counts, nb, round, a.counts + C_PLACE_BAD, a.counts + C_PLACE_BAD, s_cnt))
+    if (!grid_barrier(counts, nb, round, counts + C_PLACE_BAD, counts + C_PLACE_BAD, s_tmp))
+        return -1;
+    const int vb = s_tmp[0] ? (int)blockIdx.x : s_v;
+    __syncthreads(); /* s_tmp is free again */
+    return vb;
+}
+
+__global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ K1Params a,
+                                                     const __grid_constant__ K2Params b, int nsteps, int nsm)
+{
+    __shared__ int s_cnt[2];
+    __shared__ int s_state[2];
+    const unsigned nb = gridDim.x;
+    unsigned round = 0;
+    const int vb = placement_order(a.counts, nb, nsm, round, s_cnt);
+    if (vb < 0)
         return;
-    const int vb = s_cnt[0] ? (int)blockIdx.x : s_v;
-    __syncthreads(); /* s_cnt is reused below */
     if (threadIdx.x == 0) {
         s_state[0] = __ldcg(a.counts + 4);
         s_state[1] = __ldcg(a.counts + 6);
@@ -1004,9 +1013,10 @@ static int persist_failed(cudaStream_t st)
 namespace sdtac {
 
 constexpr int THREADS = 256, BLOCKS = 152 * 4;
-/* counts[0..1] list lengths by parity, [4] parity, [6] epoch, [8] cells
- * activated by this step's K1, [32] K2 block ticket (own line) */
-constexpr int NCOUNTS = 64, C_PAR = 4, C_EPOCH = 6, C_EXT = 8, C_TICKET = 32;
+/* counts[0..1] list lengths by parity, [4] parity, [6] epoch, [8 + parity]
+ * cells activated by the step's flows, [32] K2 block ticket (own line); the
+ * persistent kernel's barrier and placement words at sdt2's offsets */
+constexpr int NCOUNTS = sdt2::NCOUNTS, C_PAR = 4, C_EPOCH = 6, C_EXT = 8, C_TICKET = sdt2::C_TICKET;
 
 struct State {
     struct CALModel2D* ca = nullptr;
@@ -1047,26 +1057,29 @@ static __device__ __forceinline__ bool nbr(const Params& p, int i, int j, int q,
     return (unsigned)a < (unsigned)p.rows && (unsigned)b < (unsigned)p.cols;
 }
 
-/* chunks of 32 list entries, one per warp, on consecutive blocks: the
- * warp's first chunk and the stride between its chunks */
-static __device__ __forceinline__ int first_chunk()
+/* append the lanes whose predicate holds (warp-aggregated; every lane of
+ * the warp calls it) */
+static __device__ __forceinline__ void warp_append(bool pred, int value, int* list, int* count)
 {
-    return (threadIdx.x >> 5) * (int)gridDim.x + blockIdx.x;
-}
-static __device__ __forceinline__ int chunk_stride()
-{
-    return (int)gridDim.x * (THREADS / 32);
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0)
+        return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0)
+        base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (pred)
+        list[base + __popc(mask & ((1u << lane) - 1u))] = value;
 }
 
-__global__ void __launch_bounds__(THREADS) k1_flows(const __grid_constant__ Params p)
+/* The flows process over the na entries of the active list, in chunks of
+ * 32 entries (one per warp): chunks g0, g0 + gs, ... */
+static __device__ __forceinline__ void flows_work(const Params& p, int par, int epoch, int na, int g0, int gs)
 {
-    const int par = p.counts[C_PAR], epoch = p.counts[C_EPOCH];
-    const int na = p.counts[par];
     int* list = par ? p.list1 : p.list0;
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        p.counts[1 - par] = 0; /* the list K2 appends to */
     const int lane = threadIdx.x & 31;
-    for (int g = first_chunk(); g * 32 < na; g += chunk_stride()) {
+    for (int g = g0; g * 32 < na; g += gs) {
         const int k = g * 32 + lane;
         if (k >= na)
             continue;
@@ -1094,36 +1107,20 @@ __global__ void __launch_bounds__(THREADS) k1_flows(const __grid_constant__ Para
             /* calAddActiveCellX2D for every neighbour whose flow is kept */
             if (!(elim & (2u << q)) && in[q] && p.mark[nc[q]] != epoch &&
                 atomicExch(p.mark + nc[q], epoch) != epoch)
-                list[na + atomicAdd(p.counts + C_EXT, 1)] = nc[q];
+                list[na + atomicAdd(p.counts + C_EXT + par, 1)] = nc[q];
         }
     }
 }
 
-/* append the lanes whose predicate holds (warp-aggregated; every lane of
- * the warp calls it) */
-static __device__ __forceinline__ void warp_append(bool pred, int value, int* list, int* count)
+/* The width update and the removal over the n2 entries of the extended
+ * list (chunks g0, g0 + gs, ...); survivors go to the next list */
+static __device__ __forceinline__ void update_work(const Params& p, int par, int epoch, int n2, int g0, int gs)
 {
-    const unsigned mask = __ballot_sync(0xffffffffu, pred);
-    if (mask == 0)
-        return;
-    const int lane = threadIdx.x & 31;
-    int base = 0;
-    if (lane == 0)
-        base = atomicAdd(count, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (pred)
-        list[base + __popc(mask & ((1u << lane) - 1u))] = value;
-}
-
-__global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ Params p)
-{
-    const int par = p.counts[C_PAR], epoch = p.counts[C_EPOCH];
-    const int n2 = p.counts[par] + p.counts[C_EXT];
     const int* list = par ? p.list1 : p.list0;
     int* next = par ? p.list0 : p.list1;
     int* ncount = p.counts + (1 - par);
     const int lane = threadIdx.x & 31;
-    for (int g = first_chunk(); g * 32 < n2; g += chunk_stride()) {
+    for (int g = g0; g * 32 < n2; g += gs) {
         const int k = g * 32 + lane;
         bool keep = false;
         int c = 0;
@@ -1145,15 +1142,88 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ Par
         }
         warp_append(keep, c, next, ncount);
     }
+}
+
+/* chunks of 32 list entries on consecutive blocks: the warp's first chunk
+ * and the stride between its chunks */
+static __device__ __forceinline__ int first_chunk(int block, int nblocks)
+{
+    return (threadIdx.x >> 5) * nblocks + block;
+}
+
+__global__ void __launch_bounds__(THREADS) k1_flows(const __grid_constant__ Params p)
+{
+    const int par = p.counts[C_PAR], epoch = p.counts[C_EPOCH];
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        p.counts[1 - par] = 0; /* the list K2 appends to */
+    flows_work(p, par, epoch, p.counts[par], first_chunk(blockIdx.x, gridDim.x), gridDim.x * (THREADS / 32));
+}
+
+__global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ Params p)
+{
+    const int par = p.counts[C_PAR], epoch = p.counts[C_EPOCH];
+    update_work(p, par, epoch, p.counts[par] + p.counts[C_EXT + par], first_chunk(blockIdx.x, gridDim.x),
+                gridDim.x * (THREADS / 32));
     if (threadIdx.x == 0) {
         /* the last block to finish advances parity and epoch */
         __threadfence();
         if (atomicAdd(reinterpret_cast<unsigned*>(p.counts + C_TICKET), 1u) == gridDim.x - 1) {
             p.counts[C_PAR] = 1 - par;
             p.counts[C_EPOCH] = epoch + 1;
-            p.counts[C_EXT] = 0;
+            p.counts[C_EXT + par] = 0;
             p.counts[C_TICKET] = 0;
         }
+    }
+}
+
+/* every step of a run in one cooperative launch: the flows phase, a grid
+ * barrier, the update phase, a grid barrier; work dealt in the placement
+ * order (sdt2::placement_order) */
+__global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ Params p, int nsteps, int nsm)
+{
+    __shared__ int s_cnt[2];
+    const unsigned nb = gridDim.x;
+    unsigned round = 0;
+    const int vb = sdt2::placement_order(p.counts, nb, nsm, round, s_cnt);
+    if (vb < 0)
+        return;
+    if (threadIdx.x == 0) {
+        s_cnt[0] = __ldcg(p.counts + C_PAR);
+        s_cnt[1] = __ldcg(p.counts + C_EPOCH);
+    }
+    __syncthreads();
+    int par = s_cnt[0], epoch = s_cnt[1];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        s_cnt[0] = __ldcg(p.counts + par);
+    __syncthreads();
+    int na = s_cnt[0];
+    const int g0 = first_chunk(vb, (int)nb), gs = (int)nb * (THREADS / 32);
+    for (int s = 0; s < nsteps; s++) {
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            p.counts[1 - par] = 0; /* the list the update phase appends to */
+        flows_work(p, par, epoch, na, g0, gs);
+        /* then: the extended list's length */
+        if (!sdt2::grid_barrier(p.counts, nb, round, p.counts + par, p.counts + C_EXT + par, s_cnt))
+            return;
+        const int n2 = s_cnt[0] + s_cnt[1];
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            p.counts[C_EXT + (1 - par)] = 0; /* next step's (read last by the previous step) */
+        update_work(p, par, epoch, n2, g0, gs);
+        par = 1 - par;
+        epoch++;
+        /* then: the next list's length */
+        if (!sdt2::grid_barrier(p.counts, nb, round, p.counts + par, p.counts + par, s_cnt))
+            return;
+        na = s_cnt[0];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        /* the state the per-step kernels expect */
+        p.counts[C_PAR] = par;
+        p.counts[C_EPOCH] = epoch;
+        p.counts[C_EXT] = 0;
+        p.counts[C_EXT + 1] = 0;
+        p.counts[C_TICKET] = 0;
     }
 }
 
@@ -1213,9 +1283,7 @@ static bool prime(struct CALModel2D* ca, const double* h, cudaStream_t st)
     return s.primed;
 }
 
-/* one step: K1 then K2 on the model's stream */
-static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, double r, long long eps_bits,
-                 cudaStream_t st)
+static Params params(struct CALModel2D* ca, const double* z, double* h, double eps, double r, long long eps_bits)
 {
     State& s = g_state;
     Params p;
@@ -1233,9 +1301,56 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     p.eps = eps;
     p.r = r;
     p.eps_bits = eps_bits;
+    return p;
+}
+
+/* one step: K1 then K2 on the model's stream */
+static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, double r, long long eps_bits,
+                 cudaStream_t st)
+{
+    const Params p = params(ca, z, h, eps, r, eps_bits);
     k1_flows<<<BLOCKS, THREADS, 0, st>>>(p);
     k2_update<<<BLOCKS, THREADS, 0, st>>>(p);
     return cudaGetLastError() == cudaSuccess;
+}
+
+/* `nsteps` steps in one cooperative launch of k_persist (SMs x resident
+ * blocks per SM); false when the launch is refused or a CUDA error is
+ * pending.  A barrier that gave up sets the error word persist_failed()
+ * reports. */
+static bool persist(struct CALModel2D* ca, const double* z, double* h, double eps, double r, long long eps_bits,
+                    int nsteps, cudaStream_t st)
+{
+    State& s = g_state;
+    static int grid = 0, nsm = 0;
+    if (!grid) {
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persist, THREADS, 0);
+        grid = sms * per_sm;
+        nsm = sms;
+        if (grid <= 0)
+            return false;
+    }
+    Params p = params(ca, z, h, eps, r, eps_bits);
+    cudaMemsetAsync(s.counts + sdt2::C_ARRIVED, 0, sizeof(int), st);
+    cudaMemsetAsync(s.counts + sdt2::C_ERROR, 0, sizeof(int), st);
+    cudaMemsetAsync(s.counts + sdt2::C_PLACE_BAD, 0, (NCOUNTS - sdt2::C_PLACE_BAD) * sizeof(int), st);
+    void* args[] = {&p, &nsteps, &nsm};
+    return cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(THREADS), args, 0, st) ==
+           cudaSuccess;
+}
+
+/* did the last persistent run give up at a barrier?  (synchronises) */
+static int persist_failed(cudaStream_t st)
+{
+    int flag = 0;
+    if (!g_state.counts)
+        return 0;
+    cudaStreamSynchronize(st);
+    cudaMemcpy(&flag, g_state.counts + sdt2::C_ERROR, sizeof(int), cudaMemcpyDeviceToHost);
+    return flag;
 }
 
 /* the active cells in row-major order (cells[2k], cells[2k + 1] = i, j;
@@ -1928,9 +2043,23 @@ extern "C" int cal_sciddicaT_steps(void* handle, int steps, int graph)
 {
     sdt2::g_state.hknown = false; /* launches this library did not see may have run since */
     SdtSession* s = (SdtSession*)handle;
+    if (graph == 4 && s->fused_ac) {
+        /* every step in one cooperative launch of the active-cells split step */
+        sciddicaT_ac_prepare_now(s->ca);
+        if (!sdtac::g_state.primed)
+            return CAL_ERROR_OUT_OF_MEMORY;
+        long long eps_bits;
+        memcpy(&eps_bits, &P.epsilon, sizeof(double));
+        const double* z = (const double*)calGetDeviceBuffer2Dr(s->ca, Q.z, 0);
+        double* h = (double*)calGetDeviceBuffer2Dr(s->ca, Q.h, 0);
+        if (!sdtac::persist(s->ca, z, h, P.epsilon, P.r, eps_bits, steps, (cudaStream_t)calGetStream2D(s->ca)))
+            return CAL_ERROR_CUDA;
+        calMarkCurrentWritten2Dr(s->ca, Q.h);
+        return calGetLastError();
+    }
     if (graph == 4) {
         /* every step in one cooperative launch (split step, plain mode) */
-        if (s->mode != SDT_MODE_FUSED || s->fused_ac)
+        if (s->mode != SDT_MODE_FUSED)
             return CAL_ERROR_INVALID_ARGUMENT;
         sciddicaT_split_prepare_now(s->ca);
         if (!sdt2::g_state.primed)
@@ -2004,7 +2133,9 @@ extern "C" void* cal_sciddicaT_stream(void* handle) { return calGetStream2D(((Sd
  * early and the state is not that of the requested step); synchronises */
 extern "C" int cal_sciddicaT_persist_failed(void* handle)
 {
-    return sdt2::persist_failed((cudaStream_t)calGetStream2D(((SdtSession*)handle)->ca));
+    SdtSession* s = (SdtSession*)handle;
+    cudaStream_t st = (cudaStream_t)calGetStream2D(s->ca);
+    return s->fused_ac ? sdtac::persist_failed(st) : sdt2::persist_failed(st);
 }
 
 /* host-buffer round trip through the API: z and h from the caller's arrays

@@ -307,6 +307,37 @@ def test_persistent_split_step_bit_exact(cal, orc, rows, cols, tor):
         lib.cal_sciddicaT_close(sess)
 
 
+@pytest.mark.parametrize("rows,cols,tor", [(256, 256, 0), (203, 177, 0), (160, 144, 1)])
+def test_persistent_active_cells_split_bit_exact(cal, orc, rows, cols, tor):
+    """The active-cells split step with all steps in one cooperative launch
+    == the oracle's active-cells run, alone and interleaved with per-step
+    launches, recorded-step replays and device-driven loops of the same
+    session."""
+    import ctypes as C
+
+    from opencal_gb300 import ensemble as E
+    lib = E._lib()
+    z, h = W.sciddicaT_inputs(rows, cols, seed=19)
+    ref = orc.sciddicaT(z, h, 150, toroidal=tor, ac=True)[1]
+    ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    sess = lib.cal_sciddicaT_open(rows, cols, int(tor), 1, 0.5, 0.001, ptr(z), ptr(h), cal.MODE_FUSED)
+    assert sess
+    try:
+        out = np.empty_like(h)
+        assert lib.cal_sciddicaT_steps(sess, 150, 4) == 0
+        assert lib.cal_sciddicaT_persist_failed(sess) == 0
+        assert lib.cal_sciddicaT_read(sess, ptr(out)) == 0
+        assert_same(out, ref, "h persistent, active cells")
+        lib.cal_sciddicaT_reset(sess)
+        for n, mode in ((40, 0), (30, 4), (20, 1), (25, 4), (35, 2)):
+            assert lib.cal_sciddicaT_steps(sess, n, mode) == 0
+        assert lib.cal_sciddicaT_persist_failed(sess) == 0
+        assert lib.cal_sciddicaT_read(sess, ptr(out)) == 0
+        assert_same(out, ref, "h interleaved, active cells")
+    finally:
+        lib.cal_sciddicaT_close(sess)
+
+
 def test_host_round_trip_after_device_work(cal, orc):
     """Host arrays written in full after device work, marked with
     calMarkHostDirty2D, win over the stale device copies: a session that
