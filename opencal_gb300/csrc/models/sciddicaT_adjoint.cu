@@ -30,6 +30,14 @@
  * at a time from its checkpoint (bit-identical forward) and runs the
  * adjoint through it in reverse.
  *
+ * Sparsity: the forward step (32 x 16 tiles) reports per tile whether a
+ * cell of it is wet before and after the step; during the recompute those
+ * flags are kept for every state of the segment.  The adjoint of a step
+ * then visits only the tiles holding a wet cell (coefficients) and those
+ * tiles and their edge neighbours (gather), updating lambda in place: in
+ * every other cell g, gz and w are 0, so lambda and lambda_z are unchanged
+ * there, bit for bit as the dense sweep leaves them.
+ *
  * Reductions of the parameter gradients use per-block partials folded in a
  * fixed order (deterministic).
  */
@@ -44,6 +52,7 @@ namespace sdtadj {
 
 constexpr int T = 256;      /* threads per block */
 constexpr int PBLOCKS = 1024; /* partials of the parameter gradients */
+constexpr int TW = 32, TH = 16; /* forward tiles, also the adjoint's unit of work */
 
 struct Work {
     int rows = 0, cols = 0, steps = 0, toroidal = 0, K = 0, nseg = 0;
@@ -58,6 +67,9 @@ struct Work {
     double* g = nullptr;       /* g_c */
     double* gz = nullptr;      /* [0 in A_c] g_c */
     double* w = nullptr;       /* 4 * n: w_{c,m} */
+    unsigned char* flags = nullptr; /* (K + 1) x tiles: the forward's tile_wet of each step of the segment */
+    unsigned char* all_wet = nullptr; /* tiles: 3 (every tile visited) */
+    int tiles_x = 0, tiles_y = 0;
     double* partial = nullptr; /* 2 * PBLOCKS */
     double* result = nullptr;  /* 2 */
 };
@@ -140,58 +152,78 @@ static __device__ __forceinline__ void eliminate(double hc, double zc, const dou
     *avg_out = average;
 }
 
-/* per cell: coefficients g, gz, w and partials of dL/dr, dL/deps */
-__global__ void __launch_bounds__(T) k_coeffs(Geo geo, const double* __restrict__ z, const double* __restrict__ h,
-                                              const double* __restrict__ lam, double r, double eps,
-                                              long long eps_bits, double* __restrict__ g, double* __restrict__ gz,
-                                              double* __restrict__ w, double* __restrict__ partial)
+/* per cell of the visited tiles: coefficients g, gz, w and partials of
+ * dL/dr, dL/deps; then lambda_t and lambda_z by a gather (no atomics) */
+static __device__ __forceinline__ int tile_of(int i, int j, int tiles_x)
+{
+    return (i / TH) * tiles_x + (j / TW);
+}
+
+/* k_coeffs_tiles: the tiles whose flag has `mask` set (a wet cell in h_t):
+ * block b takes tiles b, b + gridDim.x, ...; every cell of a visited tile
+ * is written (0 at dry cells) */
+__global__ void __launch_bounds__(T) k_coeffs_tiles(Geo geo, const double* __restrict__ z,
+                                                    const double* __restrict__ h, const double* __restrict__ lam,
+                                                    double r, double eps, long long eps_bits,
+                                                    double* __restrict__ g, double* __restrict__ gz,
+                                                    double* __restrict__ w, double* __restrict__ partial,
+                                                    const unsigned char* __restrict__ flags, int mask,
+                                                    int tiles_x, int ntiles)
 {
     __shared__ double sr[T / 32], se[T / 32];
     double pr = 0.0, pe = 0.0;
-    for (long long c = blockIdx.x * (long long)T + threadIdx.x; c < geo.n; c += (long long)gridDim.x * T) {
-        const int i = (int)(c / geo.cols), j = (int)(c - (long long)i * geo.cols);
-        const double hc = h[c];
-        double gc = 0.0, gzc = 0.0, wc[4] = {0.0, 0.0, 0.0, 0.0};
-        if (sdt::is_wet(hc, eps_bits)) {
-            double u14[4], lnb[4];
-            bool in[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                long long cn;
-                in[q] = nb(geo, i, j, q + 1, &cn);
-                u14[q] = in[q] ? z[cn] + h[cn] : 0.0 + 0.0;
-                lnb[q] = in[q] ? lam[cn] : 0.0;
-            }
-            unsigned a_set;
-            int k;
-            double avg, u[5];
-            eliminate(hc, z[c], u14, eps, &a_set, &k, &avg, u);
-            if (k > 0) {
-                const double lc = lam[c];
-                double S = 0.0, lf[4];
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        if (!(flags[t] & mask))
+            continue;
+        const int ty = t / tiles_x, tx = t - ty * tiles_x;
+        for (int k = threadIdx.x; k < TW * TH; k += T) {
+            const int i = ty * TH + k / TW, j = tx * TW + k % TW;
+            if (i >= geo.rows || j >= geo.cols)
+                continue;
+            const long long c = (long long)i * geo.cols + j;
+            const double hc = h[c];
+            double gc = 0.0, gzc = 0.0, wc[4] = {0.0, 0.0, 0.0, 0.0};
+            if (sdt::is_wet(hc, eps_bits)) {
+                double u14[4], lnb[4];
+                bool in[4];
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    lf[q] = 0.0;
-                    if (a_set & (1u << (q + 1))) {
-                        lf[q] = lnb[q] - lc;
-                        S += lf[q];
-                        pr += lf[q] * (avg - u[q + 1]);
-                    }
+                    long long cn;
+                    in[q] = nb(geo, i, j, q + 1, &cn);
+                    u14[q] = in[q] ? z[cn] + h[cn] : 0.0 + 0.0;
+                    lnb[q] = in[q] ? lam[cn] : 0.0;
                 }
-                gc = (r / k) * S;
-                gzc = (a_set & 1u) ? gc : 0.0;
-                pe += S * r * ((a_set & 1u) ? 0.0 : -1.0) / k;
+                unsigned a_set;
+                int kk;
+                double avg, u[5];
+                eliminate(hc, z[c], u14, eps, &a_set, &kk, &avg, u);
+                if (kk > 0) {
+                    const double lc = lam[c];
+                    double S = 0.0, lf[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (a_set & (1u << (q + 1)))
-                        wc[q] = gc - r * lf[q];
+                    for (int q = 0; q < 4; q++) {
+                        lf[q] = 0.0;
+                        if (a_set & (1u << (q + 1))) {
+                            lf[q] = lnb[q] - lc;
+                            S += lf[q];
+                            pr += lf[q] * (avg - u[q + 1]);
+                        }
+                    }
+                    gc = cal_div_small(r, kk) * S; /* = (r / kk) * S: exact division by 1..5 on the integer pipe */
+                    gzc = (a_set & 1u) ? gc : 0.0;
+                    pe += cal_div_small(S * r * ((a_set & 1u) ? 0.0 : -1.0), kk);
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (a_set & (1u << (q + 1)))
+                            wc[q] = gc - r * lf[q];
+                }
             }
-        }
-        g[c] = gc;
-        gz[c] = gzc;
+            g[c] = gc;
+            gz[c] = gzc;
 #pragma unroll
-        for (int q = 0; q < 4; q++)
-            w[q * geo.n + c] = wc[q];
+            for (int q = 0; q < 4; q++)
+                w[q * geo.n + c] = wc[q];
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         pr += __shfl_down_sync(0xffffffffu, pr, o);
@@ -213,27 +245,61 @@ __global__ void __launch_bounds__(T) k_coeffs(Geo geo, const double* __restrict_
     }
 }
 
-/* lambda_t and lambda_z from the coefficients (gather: no atomics) */
-__global__ void __launch_bounds__(T) k_gather(Geo geo, const double* __restrict__ lam_next,
-                                              const double* __restrict__ g, const double* __restrict__ gz,
-                                              const double* __restrict__ w, double* __restrict__ lam_out,
-                                              double* __restrict__ lamz)
+/* is tile (ty, tx) flagged?  Outside a flat grid: no */
+static __device__ __forceinline__ bool tile_flag(const Geo& geo, const unsigned char* flags, int mask, int ty,
+                                                 int tx, int tiles_x, int tiles_y)
 {
-    for (long long c = blockIdx.x * (long long)T + threadIdx.x; c < geo.n; c += (long long)gridDim.x * T) {
-        const int i = (int)(c / geo.cols), j = (int)(c - (long long)i * geo.cols);
-        double from_nb = 0.0;
-        long long cn;
-        /* x is neighbour opp(d) of its neighbour d: north<->south (1<->4), west<->east (2<->3) */
-        if (nb(geo, i, j, 1, &cn))
-            from_nb += w[3 * geo.n + cn]; /* north cell's w towards its south (m = 4) */
-        if (nb(geo, i, j, 2, &cn))
-            from_nb += w[2 * geo.n + cn]; /* west cell's w towards its east (m = 3) */
-        if (nb(geo, i, j, 3, &cn))
-            from_nb += w[1 * geo.n + cn]; /* east cell's w towards its west (m = 2) */
-        if (nb(geo, i, j, 4, &cn))
-            from_nb += w[cn];             /* south cell's w towards its north (m = 1) */
-        lam_out[c] = lam_next[c] + g[c] + from_nb;
-        lamz[c] += gz[c] + from_nb;
+    if (geo.toroidal) {
+        ty = ty < 0 ? ty + tiles_y : (ty >= tiles_y ? ty - tiles_y : ty);
+        tx = tx < 0 ? tx + tiles_x : (tx >= tiles_x ? tx - tiles_x : tx);
+    } else if ((unsigned)ty >= (unsigned)tiles_y || (unsigned)tx >= (unsigned)tiles_x) {
+        return false;
+    }
+    return (flags[ty * tiles_x + tx] & mask) != 0;
+}
+
+/* k_gather_tiles: in place, on the tiles that are flagged or have a flagged edge
+ * neighbour; coefficients of unflagged tiles read as 0 (the dense sweep
+ * wrote 0 there) */
+__global__ void __launch_bounds__(T) k_gather_tiles(Geo geo, double* __restrict__ lam,
+                                                    const double* __restrict__ g, const double* __restrict__ gz,
+                                                    const double* __restrict__ w, double* __restrict__ lamz,
+                                                    const unsigned char* __restrict__ flags, int mask, int tiles_x,
+                                                    int tiles_y)
+{
+    const int ntiles = tiles_x * tiles_y;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int ty = t / tiles_x, tx = t - ty * tiles_x;
+        const bool own = (flags[t] & mask) != 0;
+        if (!own && !tile_flag(geo, flags, mask, ty - 1, tx, tiles_x, tiles_y) &&
+            !tile_flag(geo, flags, mask, ty + 1, tx, tiles_x, tiles_y) &&
+            !tile_flag(geo, flags, mask, ty, tx - 1, tiles_x, tiles_y) &&
+            !tile_flag(geo, flags, mask, ty, tx + 1, tiles_x, tiles_y))
+            continue;
+        for (int k = threadIdx.x; k < TW * TH; k += T) {
+            const int i = ty * TH + k / TW, j = tx * TW + k % TW;
+            if (i >= geo.rows || j >= geo.cols)
+                continue;
+            const long long c = (long long)i * geo.cols + j;
+            double from_nb = 0.0;
+            long long cn;
+            /* x is neighbour opp(d) of its neighbour d: north<->south (1<->4), west<->east (2<->3) */
+            if (nb(geo, i, j, 1, &cn))
+                from_nb += (flags[tile_of((int)(cn / geo.cols), (int)(cn % geo.cols), tiles_x)] & mask)
+                               ? w[3 * geo.n + cn] : 0.0;
+            if (nb(geo, i, j, 2, &cn))
+                from_nb += (flags[tile_of((int)(cn / geo.cols), (int)(cn % geo.cols), tiles_x)] & mask)
+                               ? w[2 * geo.n + cn] : 0.0;
+            if (nb(geo, i, j, 3, &cn))
+                from_nb += (flags[tile_of((int)(cn / geo.cols), (int)(cn % geo.cols), tiles_x)] & mask)
+                               ? w[1 * geo.n + cn] : 0.0;
+            if (nb(geo, i, j, 4, &cn))
+                from_nb += (flags[tile_of((int)(cn / geo.cols), (int)(cn % geo.cols), tiles_x)] & mask)
+                               ? w[cn] : 0.0;
+            const double gc = own ? g[c] : 0.0, gzc = own ? gz[c] : 0.0;
+            lam[c] = lam[c] + gc + from_nb;
+            lamz[c] += gzc + from_nb;
+        }
     }
 }
 
@@ -260,8 +326,10 @@ static int grid_for(long long n)
     return (int)(b > 152 * 8 ? 152 * 8 : (b < 1 ? 1 : b));
 }
 
-/* one forward step from `h` into `h_next` (the fused kernel, bit-exact) */
-static void fwd_step(const Work& W, const double* h, double* h_next, cudaStream_t st)
+/* one forward step from `h` into `h_next` (the fused kernel, bit-exact);
+ * tile_wet: optional per-tile wet flags before / after the step */
+static void fwd_step(const Work& W, const double* h, double* h_next, cudaStream_t st,
+                     unsigned char* tile_wet = nullptr)
 {
     sdt::Params p;
     p.z = W.z;
@@ -273,7 +341,8 @@ static void fwd_step(const Work& W, const double* h, double* h_next, cudaStream_
     p.eps = W.eps;
     p.r = W.r;
     memcpy(&p.eps_bits, &W.eps, sizeof(double));
-    sdt::launch<64, 32>(p, st);
+    p.tile_wet = tile_wet;
+    sdt::launch<TW, TH>(p, st);
 }
 
 } // namespace sdtadj
@@ -302,6 +371,11 @@ extern "C" void* cal_sdt_adj_create(int rows, int cols, int steps, int toroidal)
               cudaMalloc(&W->gz, b) == cudaSuccess && cudaMalloc(&W->w, 4 * b) == cudaSuccess &&
               cudaMalloc(&W->partial, 2 * sdtadj::PBLOCKS * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&W->result, 2 * sizeof(double)) == cudaSuccess;
+    W->tiles_x = (cols + sdtadj::TW - 1) / sdtadj::TW;
+    W->tiles_y = (rows + sdtadj::TH - 1) / sdtadj::TH;
+    const size_t nt = (size_t)W->tiles_x * W->tiles_y;
+    ok = ok && cudaMalloc(&W->flags, nt * (size_t)(W->K + 1)) == cudaSuccess &&
+         cudaMalloc(&W->all_wet, nt) == cudaSuccess && cudaMemset(W->all_wet, 3, nt) == cudaSuccess;
     if (!ok) {
         fprintf(stderr, "opencal-gb300: cal_sdt_adj_create: out of device memory\n");
         return nullptr;
@@ -326,6 +400,8 @@ extern "C" void cal_sdt_adj_destroy(void* handle)
     cudaFree(W->w);
     cudaFree(W->partial);
     cudaFree(W->result);
+    cudaFree(W->flags);
+    cudaFree(W->all_wet);
     delete W;
 }
 
@@ -371,25 +447,55 @@ extern "C" int cal_sdt_adj_backward(void* handle, const double* gT, double* g_h0
     cudaMemcpyAsync(W->lam[0], gT, b, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(W->lamz, 0, b, st);
     cudaMemsetAsync(W->partial, 0, 2 * sdtadj::PBLOCKS * sizeof(double), st);
-    int cur = 0;
-    const int grid = sdtadj::grid_for(W->n) > sdtadj::PBLOCKS ? sdtadj::PBLOCKS : sdtadj::grid_for(W->n);
+    const int ntiles = W->tiles_x * W->tiles_y;
+    /* one resident wave of each kernel (blocks stride over the tiles): the
+     * dry tiles cost a flag test, not a block launch */
+    static int wave_c = 0, wave_g = 0;
+    if (!wave_c) {
+        int dev = 0, sms = 0, pc = 0, pg = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pc, sdtadj::k_coeffs_tiles, sdtadj::T, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pg, sdtadj::k_gather_tiles, sdtadj::T, 0);
+        wave_c = sms * (pc > 0 ? pc : 1);
+        wave_g = sms * (pg > 0 ? pg : 1);
+    }
+    int cgrid = ntiles < wave_c ? ntiles : wave_c;
+    if (cgrid > sdtadj::PBLOCKS)
+        cgrid = sdtadj::PBLOCKS;
+    const int ggrid = ntiles < wave_g ? ntiles : wave_g;
     for (int s = W->nseg - 1; s >= 0; s--) {
         const int t0 = s * W->K;
         const int t1 = (t0 + W->K < W->steps) ? t0 + W->K : W->steps; /* states t0..t1-1 feed steps */
-        /* recompute the states of the segment from its checkpoint */
+        /* recompute the states of the segment from its checkpoint, keeping
+         * each step's tile flags (bit 0: wet before, bit 1: wet after) */
         cudaMemcpyAsync(W->seg, W->ckpt + s * W->n, b, cudaMemcpyDeviceToDevice, st);
         for (int t = t0; t < t1 - 1; t++)
-            sdtadj::fwd_step(*W, W->seg + (t - t0) * W->n, W->seg + (t - t0 + 1) * W->n, st);
-        /* reverse through the segment */
+            sdtadj::fwd_step(*W, W->seg + (t - t0) * W->n, W->seg + (t - t0 + 1) * W->n, st,
+                             W->flags + (size_t)(t - t0) * ntiles);
+        /* reverse through the segment: state t's wet tiles are bit 0 of the
+         * step from t, or bit 1 of the step into it for the last state */
         for (int t = t1 - 1; t >= t0; t--) {
             const double* ht = W->seg + (t - t0) * W->n;
-            sdtadj::k_coeffs<<<grid, sdtadj::T, 0, st>>>(geo, W->z, ht, W->lam[cur], W->r, W->eps, eps_bits, W->g,
-                                                         W->gz, W->w, W->partial);
-            sdtadj::k_gather<<<sdtadj::grid_for(W->n), sdtadj::T, 0, st>>>(geo, W->lam[cur], W->g, W->gz, W->w,
-                                                                            W->lam[1 - cur], W->lamz);
-            cur = 1 - cur;
+            const unsigned char* fl;
+            int mask;
+            if (t < t1 - 1) {
+                fl = W->flags + (size_t)(t - t0) * ntiles;
+                mask = 1;
+            } else if (t > t0) {
+                fl = W->flags + (size_t)(t - 1 - t0) * ntiles;
+                mask = 2;
+            } else {
+                fl = W->all_wet; /* a one-state segment: no step reported on it */
+                mask = 1;
+            }
+            sdtadj::k_coeffs_tiles<<<cgrid, sdtadj::T, 0, st>>>(geo, W->z, ht, W->lam[0], W->r, W->eps, eps_bits, W->g,
+                                                               W->gz, W->w, W->partial, fl, mask, W->tiles_x, ntiles);
+            sdtadj::k_gather_tiles<<<ggrid, sdtadj::T, 0, st>>>(geo, W->lam[0], W->g, W->gz, W->w, W->lamz, fl, mask,
+                                                               W->tiles_x, W->tiles_y);
         }
     }
+    const int cur = 0;
     sdtadj::k_final_grad<<<sdtadj::grid_for(W->n), sdtadj::T, 0, st>>>(W->h0, W->lam[cur], W->lamz, g_h0, W->n);
     sdtadj::k_fold_partials<<<1, 32, 0, st>>>(W->partial, W->result);
     double res[2] = {0.0, 0.0};

@@ -411,9 +411,9 @@ __global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, con
                         pr += lf[d] * (avg - u[d + 1]);
                     }
                 }
-                gc = (I.r / kk) * S;
+                gc = cal_div_small(I.r, kk) * S; /* = (I.r / kk) * S: exact division by 1..5 on the integer pipe */
                 gzc = (a_set & 1u) ? gc : 0.0;
-                pe += S * I.r * ((a_set & 1u) ? 0.0 : -1.0) / kk;
+                pe += cal_div_small(S * I.r * ((a_set & 1u) ? 0.0 : -1.0), kk);
 #pragma unroll
                 for (int d = 0; d < 4; d++)
                     if (a_set & (1u << (d + 1)))

@@ -29,6 +29,9 @@ struct Params {
     int toroidal;
     double eps, r;
     long long eps_bits;
+    /* dense step only, optional: per tile (row-major over the launch grid)
+     * bit 0 = a cell of the tile is wet before the step, bit 1 = after */
+    unsigned char* tile_wet = nullptr;
 };
 
 /* h > eps as the reference evaluates `!(h <= eps)`, on the bit pattern:
@@ -277,8 +280,13 @@ __device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, doubl
         if (TRACK)
             wet_out |= is_wet(hn, p.eps_bits);
     }
-    if (TRACK)
-        return __syncthreads_or(wet_in | (wet_out << 1));
+    if (TRACK) {
+        /* __syncthreads_or returns non-zero, not the OR of the values: one
+         * barrier per bit */
+        const int before = __syncthreads_or(wet_in) ? 1 : 0;
+        const int after = __syncthreads_or(wet_out) ? 2 : 0;
+        return before | after;
+    }
     return 0;
 }
 
@@ -286,7 +294,13 @@ template <int TW, int TH>
 __global__ void __launch_bounds__(THREADS) fused_step(const __grid_constant__ Params p)
 {
     extern __shared__ __align__(16) double smem[];
-    fused_tile<TW, TH>(p, blockIdx.y * TH, blockIdx.x * TW, smem);
+    if (p.tile_wet) {
+        const int wet = fused_tile<TW, TH, true>(p, blockIdx.y * TH, blockIdx.x * TW, smem);
+        if (threadIdx.x == 0)
+            p.tile_wet[blockIdx.y * gridDim.x + blockIdx.x] = (unsigned char)wet;
+    } else {
+        fused_tile<TW, TH>(p, blockIdx.y * TH, blockIdx.x * TW, smem);
+    }
 }
 
 /* The dense step with z and h staged by TMA: thread 0 arms an mbarrier with
@@ -325,7 +339,13 @@ __global__ void __launch_bounds__(THREADS) fused_step_tma(const __grid_constant_
         __syncthreads();
         return;
     }
-    fused_tile<TW, TH>(p, i0, j0, smem, true);
+    if (p.tile_wet) {
+        const int wet = fused_tile<TW, TH, true>(p, i0, j0, smem, true);
+        if (threadIdx.x == 0)
+            p.tile_wet[blockIdx.y * gridDim.x + blockIdx.x] = (unsigned char)wet;
+    } else {
+        fused_tile<TW, TH>(p, i0, j0, smem, true);
+    }
 }
 
 /* TMA launches queued and blocks whose copies timed out, per translation
