@@ -30,7 +30,7 @@
  * at a time from its checkpoint (bit-identical forward) and runs the
  * adjoint through it in reverse.
  *
- * Sparsity: the forward step (32 x 16 tiles) reports per tile whether a
+ * Sparsity: the forward step (16 x 8 tiles) reports per tile whether a
  * cell of it is wet before and after the step; during the recompute those
  * flags are kept for every state of the segment.  The adjoint of a step
  * then visits only the tiles holding a wet cell (coefficients) and those
@@ -52,7 +52,7 @@ namespace sdtadj {
 
 constexpr int T = 256;      /* threads per block */
 constexpr int PBLOCKS = 1024; /* partials of the parameter gradients */
-constexpr int TW = 32, TH = 16; /* forward tiles, also the adjoint's unit of work */
+constexpr int TW = 16, TH = 8; /* forward tiles, also the adjoint's unit of work */
 
 struct Work {
     int rows = 0, cols = 0, steps = 0, toroidal = 0, K = 0, nseg = 0;
