@@ -204,10 +204,19 @@ static void sciddicaT_steering_ac(struct CALModel2D* sciddicaT)
  * order does not matter: each cell's result depends only on its
  * neighbourhood.  A priming kernel canonicalises -0 to +0 in h (the first
  * reference step adds 0.0 to every cell) and builds the first wet list. */
+/* the split step's update tile (compile-time; measured on the 2048 x 2048
+ * bench run, persistent loop: 32 x 16 73.0 ms, 64 x 8 74.4, 64 x 16 76.5,
+ * 32 x 8 78.7 per 4000 steps, identical bits) */
+#ifndef SDT2_TW
+#define SDT2_TW 32
+#endif
+#ifndef SDT2_TH
+#define SDT2_TH 16
+#endif
 namespace sdt2 {
 
 constexpr int THREADS = 256;
-constexpr int TW = 64, TH = 16; /* K2 tile: 16 rows x 64 columns, 4 cells per thread */
+constexpr int TW = SDT2_TW, TH = SDT2_TH; /* K2 tile: TH rows x TW columns, 4 cells per thread */
 
 struct State {
     struct CALModel2D* ca = nullptr;
@@ -494,14 +503,16 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
                                                int* zcount)
 {
     const int ty = tile / p.tiles_x, tx = tile - ty * p.tiles_x;
-    const int r = threadIdx.x / (TW / 4);       /* 0..15 */
-    const int j4 = (threadIdx.x % (TW / 4)) * 4; /* 0, 4, ..., 60 */
+    static_assert((TW / 4) * TH <= THREADS && TW % 4 == 0, "one group of 4 cells per thread at most");
+    const int r = threadIdx.x / (TW / 4);       /* the tile's row; r >= TH: no cells */
+    const int j4 = (threadIdx.x % (TW / 4)) * 4; /* 0, 4, ..., TW - 4 */
+    const bool has = r < TH;
     const int i = ty * TH + r;
     const int jb = tx * TW + j4;
     const long long c0 = (long long)i * p.cols + jb;
     double hv[4] = {0.0, 0.0, 0.0, 0.0};
     bool cell[4];
-    const bool full = i < p.rows && jb + 3 < p.cols && (p.cols & 1) == 0;
+    const bool full = has && i < p.rows && jb + 3 < p.cols && (p.cols & 1) == 0;
     if (full) {
         /* c0 is a multiple of 2 (jb and cols even): two 16-byte loads */
         const double2 a = ldm<CO>(reinterpret_cast<const double2*>(p.h + c0));
@@ -516,7 +527,7 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
     } else {
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            cell[q] = i < p.rows && jb + q < p.cols;
+            cell[q] = has && i < p.rows && jb + q < p.cols;
             if (cell[q])
                 hv[q] = ldm<CO>(p.h + c0 + q);
         }
