@@ -338,6 +338,31 @@ def test_persistent_active_cells_split_bit_exact(cal, orc, rows, cols, tor):
         lib.cal_sciddicaT_close(sess)
 
 
+@pytest.mark.parametrize("k1,k2", [(0, 0), (152, 304), (1216, 76), (1, 1)])
+def test_split_step_grids_bit_exact(cal, orc, k1, k2):
+    """cal_sciddicaT_set_split_grid: any launch grid of the split step's two
+    kernels (down to one block each) gives the oracle's bits."""
+    import ctypes as C
+
+    from opencal_gb300 import ensemble as E
+    lib = E._lib()
+    lib.cal_sciddicaT_set_split_grid.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    z, h = W.sciddicaT_inputs(203, 250, seed=23)
+    ref = orc.sciddicaT(z, h, 90, toroidal=False, ac=False)[1]
+    ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    sess = lib.cal_sciddicaT_open(203, 250, 0, 0, 0.5, 0.001, ptr(z), ptr(h), cal.MODE_FUSED)
+    assert sess
+    try:
+        assert lib.cal_sciddicaT_set_split_grid(sess, k1, k2) == 0
+        out = np.empty_like(h)
+        assert lib.cal_sciddicaT_steps(sess, 90, 0) == 0
+        assert lib.cal_sciddicaT_read(sess, ptr(out)) == 0
+        assert_same(out, ref, f"h, grids {k1} / {k2}")
+    finally:
+        lib.cal_sciddicaT_set_split_grid(sess, 0, 0)
+        lib.cal_sciddicaT_close(sess)
+
+
 def test_host_round_trip_after_device_work(cal, orc):
     """Host arrays written in full after device work, marked with
     calMarkHostDirty2D, win over the stale device copies: a session that
