@@ -136,14 +136,20 @@ class ClockSampler:
 
 
 def dist_setup(n_gpus):
+    """Rank, world size, local rank and the process group of a torchrun
+    launch (one process per GPU, NCCL; gloo on a host without a GPU, which
+    the multi-process tests use); (0, 1, 0, None) for a single process."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
         return rank, world, local, dist
     return 0, 1, 0, None
 
@@ -154,10 +160,12 @@ def barrier(dist):
 
 
 def max_over_ranks(dist, x: float) -> float:
+    """The largest x of all ranks (the job's time is its slowest rank's)."""
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
