@@ -723,7 +723,10 @@ static __device__ int placement_order(int* counts, unsigned nb, int nsm, unsigne
     return vb;
 }
 
-__global__ void __launch_bounds__(THREADS, 4) k_persist(const __grid_constant__ K1Params a,
+#ifndef SDT2_PERSIST_MINB
+#define SDT2_PERSIST_MINB 4 /* resident blocks per SM (5 measured slower: 78.4 against 72.8 ms per run) */
+#endif
+__global__ void __launch_bounds__(THREADS, SDT2_PERSIST_MINB) k_persist(const __grid_constant__ K1Params a,
                                                      const __grid_constant__ K2Params b, int nsteps, int nsm)
 {
     __shared__ int s_cnt[2];
@@ -940,6 +943,10 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persist, THREADS, 0);
+#ifdef SDT2_PERSIST_PER_SM /* compile-time cap (2 or 3 per SM measured slower than 4) */
+        if (per_sm > SDT2_PERSIST_PER_SM)
+            per_sm = SDT2_PERSIST_PER_SM;
+#endif
         grid = sms * per_sm;
         sms_of_device = sms;
         if (grid <= 0)
