@@ -82,7 +82,7 @@ long long cal_sdt_batch_cells(void* ensemble, long long* offsets /* B + 1, or NU
 void* cal_sdt_batch_stream(void* ensemble);
 int cal_sdt_batch_shape(void* ensemble);
 int cal_sdt_batch_set_shape(void* ensemble, int shape /* 0: 32x16, 1: 64x16, 2: 64x32 */);
-int cal_sdt_batch_autotune(void* ensemble, int probe_steps, float* ms /* 3 */);
+int cal_sdt_batch_autotune(void* ensemble, int probe_steps, float* ms /* 5: 32x16, 64x16, 64x32, 16x8, 32x8 */);
 int cal_sdt_batch_set_params(void* ensemble, const double* params);
 int cal_sdt_batch_forward(void* ensemble, double* hT /* device, or NULL */);
 int cal_sdt_batch_active_tiles(void* ensemble, int* counts /* steps + 1 */);

@@ -70,7 +70,8 @@ struct Inst {
 struct Shape {
     int tw, th;
 };
-static const Shape kShapes[3] = {{32, 16}, {64, 16}, {64, 32}};
+constexpr int NSHAPES = 5;
+static const Shape kShapes[NSHAPES] = {{32, 16}, {64, 16}, {64, 32}, {16, 8}, {32, 8}};
 
 struct Batch {
     int B = 0, steps = 0, K = 0, nseg = 0, shape = 1;
@@ -541,6 +542,8 @@ static void launch_adjoint(Batch& bt, int t, const double* h)
     switch ((batch).shape) {                                   \
     case 0: fn<32, 16>(__VA_ARGS__); break;                    \
     case 1: fn<64, 16>(__VA_ARGS__); break;                    \
+    case 3: fn<16, 8>(__VA_ARGS__); break;                     \
+    case 4: fn<32, 8>(__VA_ARGS__); break;                     \
     default: fn<64, 32>(__VA_ARGS__); break;                   \
     }
 
@@ -773,8 +776,12 @@ extern "C" int cal_sdt_batch_loss_grad(void* handle, const double* target, doubl
 
 /* Pick the fastest tile shape for this ensemble: a forward of `probe_steps`
  * steps per candidate (0: 32x16, 1: 64x16, 2: 64x32), timed with CUDA
- * events after one untimed probe.  Writes the milliseconds to ms[3] and
- * returns the chosen shape, or -1 on a CUDA error. */
+ * events after one untimed probe.  Writes the milliseconds to ms[0..2]
+ * (ms[3..4] = 0) and returns the chosen shape, or -1 on a CUDA error.  The
+ * smaller shapes 3 (16x8) and 4 (32x8) are not candidates: on the 256
+ * instance calibration ensemble 16x8 wins a 100-step forward probe (9.5
+ * against 10.4 ms) but loses the forward + adjoint iteration (1.084 against
+ * 0.963 s); cal_sdt_batch_set_shape selects them. */
 extern "C" int cal_sdt_batch_autotune(void* handle, int probe_steps, float* ms)
 {
     Batch* bt = (Batch*)handle;
@@ -785,6 +792,9 @@ extern "C" int cal_sdt_batch_autotune(void* handle, int probe_steps, float* ms)
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    for (int s = 0; s < sdtb::NSHAPES; s++)
+        if (ms)
+            ms[s] = 0.f;
     for (int s = 0; s < 3; s++) {
         bt->shape = s;
         if (!sdtb::tiles_for(*bt)) {
@@ -815,11 +825,12 @@ extern "C" int cal_sdt_batch_autotune(void* handle, int probe_steps, float* ms)
     return cudaGetLastError() == cudaSuccess ? best : -1;
 }
 
-/* set the tile shape (0: 32x16, 1: 64x16, 2: 64x32); 0 on success */
+/* set the tile shape (0: 32x16, 1: 64x16, 2: 64x32, 3: 16x8, 4: 32x8); 0 on
+ * success */
 extern "C" int cal_sdt_batch_set_shape(void* handle, int shape)
 {
     Batch* bt = (Batch*)handle;
-    if (shape < 0 || shape > 2)
+    if (shape < 0 || shape >= sdtb::NSHAPES)
         return 1;
     bt->shape = shape;
     return sdtb::tiles_for(*bt) ? 0 : 2;

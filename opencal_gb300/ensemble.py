@@ -27,7 +27,7 @@ import torch
 
 from . import CALError, models as _models
 
-SHAPES = ("32x16", "64x16", "64x32")
+SHAPES = ("32x16", "64x16", "64x32", "16x8", "32x8")
 _bound = False
 _pd = C.POINTER(C.c_double)
 _pi = C.POINTER(C.c_int)
@@ -170,7 +170,7 @@ class Ensemble:
     def autotune(self, probe_steps: int = 50):
         """Time each tile shape on a forward probe; keep the fastest.
         Returns (shape name, {shape: ms})."""
-        ms = (C.c_float * 3)()
+        ms = (C.c_float * len(SHAPES))()
         best = self._lib.cal_sdt_batch_autotune(self.handle, int(probe_steps), ms)
         if best < 0:
             raise CALError("cal_sdt_batch_autotune failed")
@@ -288,8 +288,11 @@ class FDSession:
     keeps its substates in globals, as the reference's does: one session is
     open at a time."""
 
-    def __init__(self, z, h, p_r, p_eps, steps, target: np.ndarray):
+    def __init__(self, z, h, p_r, p_eps, steps, target: np.ndarray, loop: int = 1):
+        """loop: 1 = the recorded step replayed (the drop-in's run loop), 4 =
+        every step in one cooperative launch (the fastest single-grid loop)"""
         self._lib = _lib()
+        self.loop = int(loop)
         z = np.ascontiguousarray(z, np.float64)
         h = np.ascontiguousarray(h, np.float64)
         self.rows, self.cols = z.shape
@@ -305,7 +308,8 @@ class FDSession:
         lib = self._lib
         lib.cal_sciddicaT_set_params(self.handle, float(p_r), float(p_eps))
         lib.cal_sciddicaT_reset(self.handle)
-        lib.cal_sciddicaT_steps(self.handle, self.steps, 1)
+        if lib.cal_sciddicaT_steps(self.handle, self.steps, self.loop):
+            raise CALError("cal_sciddicaT_steps failed")
         if lib.cal_sciddicaT_read(self.handle, _ptr(self.out, C.c_double)):
             raise CALError("cal_sciddicaT_read failed")
         d = self.out - self.target

@@ -44,7 +44,7 @@ def test_forward_bit_exact(env):
         assert g.tobytes() == r.tobytes(), f"instance {b} {DIMS[b]}"
 
 
-@pytest.mark.parametrize("shape", ["32x16", "64x16", "64x32"])
+@pytest.mark.parametrize("shape", ["32x16", "64x16", "64x32", "16x8", "32x8"])
 def test_every_tile_shape_bit_exact(env, shape):
     torch, oracle, E, params, zs, hs = env
     ens = E.Ensemble(DIMS, params, zs, hs, 25)
