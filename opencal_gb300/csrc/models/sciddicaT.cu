@@ -503,30 +503,36 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
                                                int* zcount)
 {
     const int ty = tile / p.tiles_x, tx = tile - ty * p.tiles_x;
-    static_assert((TW / 4) * TH <= THREADS && TW % 4 == 0, "one group of 4 cells per thread at most");
-    const int r = threadIdx.x / (TW / 4);       /* the tile's row; r >= TH: no cells */
-    const int j4 = (threadIdx.x % (TW / 4)) * 4; /* 0, 4, ..., TW - 4 */
+    /* CPT consecutive cells of a row per thread: 4 when the tile has 4
+     * cells per thread or more, else 2 (32 x 16: every thread busy, half the
+     * serial FP64 chain per thread) */
+    constexpr int CPT = (TW * TH >= 4 * THREADS) ? 4 : 2;
+    static_assert((TW / CPT) * TH <= THREADS && TW % CPT == 0, "one group of CPT cells per thread at most");
+    const int r = threadIdx.x / (TW / CPT);         /* the tile's row; r >= TH: no cells */
+    const int j4 = (threadIdx.x % (TW / CPT)) * CPT; /* 0, CPT, ..., TW - CPT */
     const bool has = r < TH;
     const int i = ty * TH + r;
     const int jb = tx * TW + j4;
     const long long c0 = (long long)i * p.cols + jb;
     double hv[4] = {0.0, 0.0, 0.0, 0.0};
-    bool cell[4];
-    const bool full = has && i < p.rows && jb + 3 < p.cols && (p.cols & 1) == 0;
+    bool cell[4] = {false, false, false, false};
+    const bool full = has && i < p.rows && jb + CPT - 1 < p.cols && (p.cols & 1) == 0;
     if (full) {
-        /* c0 is a multiple of 2 (jb and cols even): two 16-byte loads */
+        /* c0 is a multiple of 2 (jb and cols even): 16-byte loads */
         const double2 a = ldm<CO>(reinterpret_cast<const double2*>(p.h + c0));
-        const double2 b = ldm<CO>(reinterpret_cast<const double2*>(p.h + c0 + 2));
         hv[0] = a.x;
         hv[1] = a.y;
-        hv[2] = b.x;
-        hv[3] = b.y;
+        if (CPT == 4) {
+            const double2 b = ldm<CO>(reinterpret_cast<const double2*>(p.h + c0 + 2));
+            hv[2] = b.x;
+            hv[3] = b.y;
+        }
 #pragma unroll
-        for (int q = 0; q < 4; q++)
+        for (int q = 0; q < CPT; q++)
             cell[q] = true;
     } else {
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < CPT; q++) {
             cell[q] = has && i < p.rows && jb + q < p.cols;
             if (cell[q])
                 hv[q] = ldm<CO>(p.h + c0 + q);
