@@ -205,10 +205,13 @@ static void sciddicaT_steering_ac(struct CALModel2D* sciddicaT)
  * neighbourhood.  A priming kernel canonicalises -0 to +0 in h (the first
  * reference step adds 0.0 to every cell) and builds the first wet list. */
 /* the split step's update tile (compile-time; measured on the 2048 x 2048
- * bench run, persistent loop: 32 x 16 73.0 ms, 64 x 8 74.4, 64 x 16 76.5,
- * 32 x 8 78.7 per 4000 steps, identical bits) */
+ * bench run, ms per 4000 steps, persistent / eager loop, identical bits):
+ * 16 x 16 (one cell per thread) 66.7 / 76.7, 16 x 32 66.6 / 80.2, 32 x 16
+ * (two per thread) 69.5 / 81.6, 8 x 16 69.9 / 80.6, 32 x 8 70.0 / 100.3,
+ * 64 x 8 70.8 / 81.4, 16 x 8 71.4 / 81.0; with four cells per thread,
+ * 32 x 16 73.0, 64 x 16 76.5 */
 #ifndef SDT2_TW
-#define SDT2_TW 32
+#define SDT2_TW 16
 #endif
 #ifndef SDT2_TH
 #define SDT2_TH 16
@@ -504,9 +507,9 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
 {
     const int ty = tile / p.tiles_x, tx = tile - ty * p.tiles_x;
     /* CPT consecutive cells of a row per thread: 4 when the tile has 4
-     * cells per thread or more, else 2 (32 x 16: every thread busy, half the
-     * serial FP64 chain per thread) */
-    constexpr int CPT = (TW * TH >= 4 * THREADS) ? 4 : 2;
+     * cells per thread or more, else 2 or 1 (32 x 16: 2, every thread busy,
+     * half the serial FP64 chain per thread) */
+    constexpr int CPT = (TW * TH >= 4 * THREADS) ? 4 : ((TW * TH >= 2 * THREADS) ? 2 : 1);
     static_assert((TW / CPT) * TH <= THREADS && TW % CPT == 0, "one group of CPT cells per thread at most");
     const int r = threadIdx.x / (TW / CPT);         /* the tile's row; r >= TH: no cells */
     const int j4 = (threadIdx.x % (TW / CPT)) * CPT; /* 0, CPT, ..., TW - CPT */
@@ -516,7 +519,7 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
     const long long c0 = (long long)i * p.cols + jb;
     double hv[4] = {0.0, 0.0, 0.0, 0.0};
     bool cell[4] = {false, false, false, false};
-    const bool full = has && i < p.rows && jb + CPT - 1 < p.cols && (p.cols & 1) == 0;
+    const bool full = CPT > 1 && has && i < p.rows && jb + CPT - 1 < p.cols && (p.cols & 1) == 0;
     if (full) {
         /* c0 is a multiple of 2 (jb and cols even): 16-byte loads */
         const double2 a = ldm<CO>(reinterpret_cast<const double2*>(p.h + c0));
