@@ -413,7 +413,10 @@ static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int e
         }
         flag_tile_warp<CO>(any, own, p.tflag, p.tlist, tcount, epoch);
     }
-    for (int k = tid; k < nz; k += nthreads) {
+    /* the dried cells from the other end of the thread range: threads
+     * nthreads - 1, nthreads - 2, ... (a bijection, each entry once), so that
+     * this work lands on threads the wet list leaves idle */
+    for (int k = nthreads - 1 - tid; k < nz; k += nthreads) {
         const int c = ldm<CO>(zlist + k);
 #pragma unroll
         for (int q = 0; q < 4; q++)
