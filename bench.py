@@ -851,11 +851,13 @@ def ncu_case_ensemble(args):
 
 
 def ncu_case(args):
-    """A fixed, untimed sequence for ncu captures: open the 2048^2 session,
-    run --ncu-steps fused steps from the initial state, report the wet
-    fraction.  No torch, no extra allocations."""
+    """A fixed, untimed sequence for ncu captures: open the 2048^2 session
+    (activecells: with active cells on), run --ncu-steps fused steps from the
+    initial state, report the wet fraction.  No torch, no extra
+    allocations."""
     if args.ncu_case == "ensemble":
         return ncu_case_ensemble(args)
+    ac = 1 if args.ncu_case == "activecells" else 0
     import opencal_gb300 as cal
     from opencal_gb300 import workloads as W
     cal.build()
@@ -867,7 +869,7 @@ def ncu_case(args):
     m.cal_sciddicaT_read.argtypes = [C.c_void_p, C.c_void_p]
     m.cal_sciddicaT_close.argtypes = [C.c_void_p]
     z, h = W.sciddicaT_inputs(ROWS, COLS, seed=SEED)
-    sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_FUSED)
+    sess = m.cal_sciddicaT_open(ROWS, COLS, 0, ac, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_FUSED)
     done = 0
     for target in sorted(set([args.ncu_steps] + [s for s in (500, 1000, 2000, 3000, 4000) if s < args.ncu_steps])):
         m.cal_sciddicaT_steps(sess, target - done, LOOPS[args.loop])
@@ -890,7 +892,7 @@ def main():
     ap.add_argument("--no-ac", action="store_true", help="skip the active-cells-on run of the workload")
     ap.add_argument("--no-calibration", action="store_true", help="skip the batched-calibration section")
     ap.add_argument("--calib-iters", type=int, default=12)
-    ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble"],
+    ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble", "activecells"],
                     help="untimed fixed sequence for ncu captures")
     ap.add_argument("--ncu-steps", type=int, default=1002)
     ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara", "mbusu", "adjoint", "life"],
