@@ -51,7 +51,12 @@ CA_STEPS = 4000
 SEED = 2
 P_R, P_EPS = 0.5, 0.001
 BYTES_PER_CELL_UPDATE = 24  # z read + h read + h write (FP64)
+# FP64 operations of one wet cell-update (SURVEY scope table: 5 + up to 5
+# minimisation iterations x (<= 5 adds + 1 division) + 8 of the update; an
+# upper estimate of the reference's own operation count per wet cell)
+FP64_OPS_PER_WET_CELL = 70
 REF_SAMPLE_STEPS = 64
+SERIAL_SAMPLE_STEPS = 8  # the 1-core serial comparator's sample (CA steps of the full grid)
 # how the 4000 steps are issued: a launch sequence per step, a recorded step
 # replayed as a CUDA graph, or one device-driven graph launch for the loop
 # or every step in one cooperative launch of the persistent split-step kernel
@@ -206,14 +211,24 @@ def reference_arm(args):
 
 
 def cpu_baseline_sample(z, h):
+    """The oracle on the host: OpenMP build on every core (the reported
+    baseline) and the serial build on one core (the serial reference's
+    semantics, OpenCAL-OMP/source/cal2DRun.c:125-139 without OpenMP)."""
     import oracle
     oracle.build()
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
     oracle.sciddicaT(z, h, REF_SAMPLE_STEPS, toroidal=False, ac=False, kind="omp", want_cells=False)
     dt = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    oracle.sciddicaT(z, h, SERIAL_SAMPLE_STEPS, toroidal=False, ac=False, kind="serial", want_cells=False)
+    ds = time.perf_counter() - t0
     return {"value": ROWS * COLS * REF_SAMPLE_STEPS / dt, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-            "sample": f"{REF_SAMPLE_STEPS} CA steps of the {ROWS}x{COLS} grid, OpenMP on all host cores"}
+            "sample": f"{REF_SAMPLE_STEPS} CA steps of the {ROWS}x{COLS} grid, OpenMP on all host cores",
+            "serial": {"value": ROWS * COLS * SERIAL_SAMPLE_STEPS / ds, "unit": "cell-updates/s", "cores": 1,
+                       "kind": "port",
+                       "sample": f"{SERIAL_SAMPLE_STEPS} CA steps of the {ROWS}x{COLS} grid, serial build, one "
+                                 "core"}}
 
 
 def gpu_arm(args):
@@ -234,8 +249,9 @@ def gpu_arm(args):
     m.cal_sciddicaT_host_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
     m.cal_sciddicaT_persist_failed.argtypes = [C.c_void_p]
     m.cal_sciddicaT_read.argtypes = [C.c_void_p, C.c_void_p]
+    m.cal_sciddicaT_trace.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    m.cal_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_float)]
 
-    cudart = C.CDLL("libcudart.so", mode=C.RTLD_GLOBAL) if False else None  # noqa: F841
     import torch  # device memory for the L2 flush buffer and events
     torch.cuda.set_device(local)
     z, h = W.sciddicaT_inputs(ROWS, COLS, seed=SEED)
@@ -331,8 +347,48 @@ def gpu_arm(args):
     m.cal_sciddicaT_steps(sess, CA_STEPS, 0)
     he = np.empty_like(h)
     m.cal_sciddicaT_read(sess, he.ctypes.data)
+    # the boundary trace (not timed): one split step at a time with a trace
+    # kernel after each -- the first step at which the two-cell edge band is
+    # wet, the mass leaving through the flat boundary per step, the wet cells
+    # of every step
+    m.cal_sciddicaT_reset(sess)
+    outflux = np.zeros(CA_STEPS)
+    wet_steps = np.zeros(CA_STEPS, np.int32)
+    edge = C.c_int(-1)
+    trace_rc = m.cal_sciddicaT_trace(sess, CA_STEPS, outflux.ctypes.data, wet_steps.ctypes.data, C.byref(edge))
+    ht = np.empty_like(h)
+    m.cal_sciddicaT_read(sess, ht.ctypes.data)
     m.cal_sciddicaT_close(sess)
-    consistent = bool(hh.tobytes() == he.tobytes() == out.numpy().tobytes()) and not barrier_failed
+    consistent = (bool(hh.tobytes() == he.tobytes() == out.numpy().tobytes() == ht.tobytes()) and not barrier_failed
+                  and trace_rc == 0)
+    import math
+    mass0 = math.fsum(h.ravel())
+    mass_t = math.fsum(hh.ravel())
+    out_total = math.fsum(outflux)
+    boundary = {
+        "edge_reached_step": int(edge.value),
+        "mass0": mass0, "mass_final": mass_t, "mass_out_through_boundary": out_total,
+        "mass_balance_rel": (mass0 - out_total - mass_t) / mass0,
+        "how": "split step one launch pair at a time with a trace kernel after each (not timed): first step "
+               "after which a cell of the two-cell edge band holds h != 0; the outflows of border cells towards "
+               "absent neighbours summed per step; balance = (M0 - outflux - M_T) / M0 with exactly rounded sums",
+    }
+    wet_total = int(wet_steps.astype(np.int64).sum())
+    parity = None
+    gpath = os.path.join(ROOT, "tests", "golden", "sciddicaT_2048.json")
+    if os.path.exists(gpath):
+        import hashlib
+        with open(gpath) as f:
+            gold = json.load(f)
+        parity = {"oracle_h_sha256_equal": hashlib.sha256(hh.tobytes()).hexdigest() == gold["plain"]["h_sha256"],
+                  "oracle_edge_step_equal": int(edge.value) == gold["plain"]["edge_step"],
+                  "fixture": "tests/golden/sciddicaT_2048.json (oracle, OpenMP build, same inputs)"}
+    # measured FP64 throughput (DADD and DFMA instructions per second)
+    fp64 = {}
+    for name, op in (("dadd", 1), ("dfma", 0)):
+        rate, tms = C.c_double(0.0), C.c_float(0.0)
+        if m.cal_fp64_peak(op, C.byref(rate), C.byref(tms)) == 0:
+            fp64[name] = rate.value
 
     if rank != 0:
         return
@@ -372,8 +428,21 @@ def gpu_arm(args):
                      "bytes_per_step": ROWS * COLS * BYTES_PER_CELL_UPDATE},
         "finite": bool(np.isfinite(hh).all()),
         "consistent": consistent,
+        "parity_vs_oracle": parity,
+        "boundary": boundary,
+        "wet_cell_updates_per_s": wet_total * args.steps * world / dev_s,
         "clocks": clk,
     }
+    if fp64.get("dadd"):
+        run_s = float(np.mean(run_ms)) * 1e-3
+        ach = wet_total * FP64_OPS_PER_WET_CELL / run_s / 1e9
+        line["roofline"]["fp64"] = {
+            "achieved": ach, "peak": fp64["dadd"] / 1e9, "unit": "GFLOP/s", "frac": ach / (fp64["dadd"] / 1e9),
+            "peak_dfma_gflops": 2 * fp64.get("dfma", 0.0) / 1e9,
+            "basis": f"wet cell-updates of the run ({wet_total}, from the trace) x {FP64_OPS_PER_WET_CELL} FP64 "
+                     "operations (adds, multiplies, divisions as one each) / mean run time; peak = DADD "
+                     "instructions per second measured live (cal_fp64_peak: independent chains on every SM, CUDA "
+                     "events; the kernel's FP64 work is adds and multiplies, no FMA)"}
     if not args.no_ac:
         line["active_cells_on"] = active_cells_section(m, cal, z, h, hh)
     if not args.no_cpu_baseline:

@@ -203,14 +203,17 @@ int calGetActiveCellCount2D(struct CALModel2D* ca2D);
  * No counterpart in the reference.  It computes what calUpdateActiveCells2D
  * computes -- the cells whose flag is set, in row-major order, their linear
  * indices and their number -- from caller-owned device buffers: `flags`
- * (rows*columns bytes), `cells` and `linear` (room for every cell), `count`
- * (one int), queued on `stream` (a cudaStream_t, NULL for the default
- * stream).  It allocates nothing: its scratch is a fixed array in device
- * memory owned by the library, so grids are limited to
- * CAL_NOALLOC_MAX_CELLS cells (larger ones return CAL_ERROR_LIMIT), calls
- * whose kernels overlap on the GPU race on that array, and the first call
- * on each device (which looks the array up) should come before any stream
- * capture.  Returns a CALError code. */
+ * (rows*columns bytes, any alignment), `cells` and `linear` (room for every
+ * cell) and `count` (one int), all three 4-byte aligned (otherwise
+ * CAL_ERROR_INVALID_ARGUMENT and nothing is launched), queued on `stream`
+ * (a cudaStream_t, NULL for the default stream).  It allocates nothing: its
+ * scratch is a fixed array in device memory owned by the library, so grids
+ * are limited to CAL_NOALLOC_MAX_CELLS cells (larger ones return
+ * CAL_ERROR_LIMIT), calls whose kernels overlap on the GPU race on that
+ * array, and the first call on each device (which looks the array up)
+ * should come before any stream capture; the address it looks up is kept,
+ * so a cudaDeviceReset after that first call is not supported.  Returns a
+ * CALError code. */
 #define CAL_NOALLOC_MAX_CELLS 268435456
 int calCompactActiveCellsNoAlloc2D(const CALbyte* flags, int rows, int columns, struct CALCell2D* cells,
                                    int* linear, int* count, void* stream);

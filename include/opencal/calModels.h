@@ -28,7 +28,7 @@ extern "C" {
  * order, the reference's order).  graph: 0 =
  * launch sequence per step, 1 = recorded step replayed, 2 = device-driven
  * loop bounded by the final step, 3 = device loop ended by a device stop
- * condition.  n_active / cells_out: the active cells after the run (ac). */
+ * condition, 4 = every step in one cooperative launch (mode 1 only).  n_active / cells_out: the active cells after the run (ac). */
 int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int steps, double p_r, double p_eps, const double* z0,
                       const double* h0, double* z_out, double* h_out, long* n_active, int* cells_out, int mode,
                       int graph, double* ms);
@@ -60,6 +60,12 @@ int cal_sciddicaT_host_run(void* session, const double* z_host, const double* h_
                            double* h_out);
 int cal_sciddicaT_kernel_times(void* session, int n, float* ms_outflows, float* ms_update);
 int cal_sciddicaT_wet_count(void* session);
+/* `steps` plain split steps from the current state with a trace after each
+ * (flat grids of at least 5 x 5 cells): outflux[t] = mass that left the grid
+ * in step t + 1 (border cells' outflows towards absent neighbours), wet[t] =
+ * wet cells processed in it, *edge_step = first step after which a cell of
+ * the two-cell edge band holds h != 0, or -1.  Host arrays. */
+int cal_sciddicaT_trace(void* session, int steps, double* outflux, int* wet, int* edge_step);
 int cal_sciddicaT_read(void* session, double* h_out);
 void cal_sciddicaT_close(void* session);
 
@@ -133,20 +139,16 @@ int cal_life2d_run(int rows, int cols, int toroidal, int as_int, int steps, cons
 int cal_life3d_run(int rows, int cols, int slices, int nbhd, int toroidal, int steps, int r1, int r2, int r3, int r4,
                    const unsigned char* s0, unsigned char* s_out, int graph);
 
-/* ---- engine probes used by the parity tests ---- */
-int cal_nbprobe2d_run(int rows, int cols, int nbhd, int toroidal, int steps, const double* v0, double* v_out,
-                      int graph);
-int cal_acprobe_run(int dim, int rows, int cols, int slices, int nbhd, int toroidal, int steps, double thr,
-                    const double* v0, double* v_out, long* n_active, int* cells_out, int graph);
-int cal_reduce2d_run(int type, int rows, int cols, const void* data, int op, double* out);
-int cal_unsafe2d_run(int rows, int cols, int nbhd, int toroidal, int steps, const int* v0, const signed char* b0,
-                     const double* w0, int* v_out, signed char* b_out, double* w_out, double* u_out, double* x_out,
-                     int graph);
 /* SCIDDICA-T in the reference's unsafe form
  * (OpenCAL/examples/cal_sciddicaT-unsafe/source/sciddicaT.c) */
 int cal_sciddicaT_unsafe_run(int rows, int cols, int toroidal, int steps, double p_r, double p_eps, const double* z0,
                              const double* h0, double* z_out, double* h_out, int graph);
-long cal_test_exact_div(const double* x, const int* c, const double* y, long long n);
+
+/* ---- measurement aid ----
+ * FP64 instructions per second of op 0 (DFMA), 1 (DADD) or 2 (DMUL) on the
+ * current GPU (independent dependency chains on every SM, CUDA events);
+ * *ms: duration of the timed launch */
+int cal_fp64_peak(int op, double* instr_per_s, float* ms);
 
 #ifdef __cplusplus
 }

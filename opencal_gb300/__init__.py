@@ -67,10 +67,8 @@ def models() -> C.CDLL:
         m.cal_sciddicaT_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                         _dp, _dp, _dp, _dp, _pl, C.c_void_p, C.c_int, C.c_int, _pd]
         m.cal_life2d_run.argtypes = [C.c_int] * 5 + [_u8, _u8, C.c_int, C.c_int, C.c_int, _pd]
-        m.cal_nbprobe2d_run.argtypes = [C.c_int] * 5 + [_dp, _dp, C.c_int]
-        m.cal_acprobe_run.argtypes = [C.c_int] * 7 + [C.c_double, _dp, _dp, _pl, C.c_void_p, C.c_int]
         m.cal_life3d_run.argtypes = [C.c_int] * 10 + [_u8, _u8, C.c_int]
-        for f in ("cal_sciddicaT_run", "cal_life2d_run", "cal_nbprobe2d_run", "cal_acprobe_run", "cal_life3d_run"):
+        for f in ("cal_sciddicaT_run", "cal_life2d_run", "cal_life3d_run"):
             getattr(m, f).restype = C.c_int
         _models = m
     return _models
@@ -121,31 +119,6 @@ def life2d(s0, steps, *, toroidal=True, as_int=False, mode=MODE_FUSED_BLOCKED, b
     return (out, ms.value) if timing else out
 
 
-def nbprobe2d(v0, steps, *, nbhd=NB_HEX, toroidal=True, graph=False):
-    v0 = np.ascontiguousarray(v0, dtype=np.float64)
-    rows, cols = v0.shape
-    out = np.empty_like(v0)
-    _check(models().cal_nbprobe2d_run(rows, cols, int(nbhd), int(toroidal), int(steps), v0, out, int(graph)),
-           "cal_nbprobe2d_run")
-    return out
-
-
-def acprobe(v0, steps, *, nbhd=NB_MOORE, toroidal=True, thr=0.5, graph=False):
-    v0 = np.ascontiguousarray(v0, dtype=np.float64)
-    dim = v0.ndim
-    if dim == 2:
-        rows, cols = v0.shape
-        slices = 1
-    else:
-        slices, rows, cols = v0.shape
-    out = np.empty_like(v0)
-    n = C.c_long(0)
-    cells = np.zeros((v0.size, dim), dtype=np.int32)
-    _check(models().cal_acprobe_run(dim, rows, cols, slices, int(nbhd), int(toroidal), int(steps), thr, v0, out,
-                                    C.byref(n), cells.ctypes.data, int(graph)), "cal_acprobe_run")
-    return out, cells[: n.value].copy()
-
-
 def life3d(s0, steps, *, nbhd=2, toroidal=True, rule=(5, 7, 6, 6), graph=False):
     s0 = np.ascontiguousarray(s0, dtype=np.uint8)
     slices, rows, cols = s0.shape
@@ -192,24 +165,6 @@ def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt
     if timing:
         outs["ms"] = ms.value
     return outs
-
-
-def unsafe2d(v0, b0, w0, steps, *, nbhd=NB_MOORE, toroidal=True, graph=False):
-    """The unsafe-operation probe on the GPU (csrc/models/probes.cu); same
-    contract as oracle.unsafe2d."""
-    v0 = np.ascontiguousarray(v0, dtype=np.int32)
-    b0 = np.ascontiguousarray(b0, dtype=np.int8)
-    w0 = np.ascontiguousarray(w0, dtype=np.float64)
-    rows, cols = v0.shape
-    v, b, w = np.empty_like(v0), np.empty_like(b0), np.empty_like(w0)
-    u, x = np.empty_like(w0), np.empty_like(w0)
-    f = models().cal_unsafe2d_run
-    f.restype = C.c_int
-    f.argtypes = [C.c_int] * 5 + [C.c_void_p] * 8 + [C.c_int]
-    _check(f(rows, cols, int(nbhd), int(toroidal), int(steps), v0.ctypes.data, b0.ctypes.data, w0.ctypes.data,
-             v.ctypes.data, b.ctypes.data, w.ctypes.data, u.ctypes.data, x.ctypes.data, int(bool(graph))),
-           "cal_unsafe2d_run")
-    return v, b, w, u, x
 
 
 def sciddicaT_unsafe(z0, h0, steps, *, toroidal=True, p_r=0.5, p_eps=0.001, graph=False):

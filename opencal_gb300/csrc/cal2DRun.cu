@@ -316,9 +316,22 @@ static int run_device_steps(struct CALRun2D* sim, int first, int last)
     if (!sim->stopCondition && device_loop(sim, stop, have_steps)) {
         gr->device_loop_used = 1;
     } else {
-        /* one step at a time; the device condition still decides */
-        for (;;) {
+        /* one step at a time; the device condition decides, and the host
+         * counts the steps too, so that the loop ends even when a failed
+         * launch leaves the device's decision stale: at most last - first + 1
+         * steps (CAL_DEVICE_LOOP_MAX_STEP with CAL_RUN_LOOP), and at the
+         * first error of a step's launches */
+        const long long host_limit =
+            last == CAL_RUN_LOOP ? (long long)CAL_DEVICE_LOOP_MAX_STEP : (long long)last - first + 1;
+        for (long long taken = 0;; taken++) {
+            if (taken >= host_limit) {
+                cal::set_error(CAL_ERROR_INVALID_ARGUMENT, "device-driven run: host step count reached its limit");
+                break;
+            }
+            calClearError();
             step_work(sim);
+            if (calGetLastError() != CAL_SUCCESS || !cal::cuda_ok(cudaGetLastError(), "step launches"))
+                break;
             CALDevModel2D d;
             if (!cal_internal_desc2D(sim->ca2D, &d))
                 break;

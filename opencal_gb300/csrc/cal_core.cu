@@ -128,16 +128,30 @@ __global__ void k_update(const __grid_constant__ UpdateParams p)
 }
 
 /* ---- active-cell compaction -------------------------------------------
- * Two passes over the flags, in the reference's list order:
+ * The list order is the reference's:
  *   2D: memory order (row-major);
  *   3D: i, then j, then k, while memory is slice-major (k*rows*cols + ...).
- * Pass 1 counts set flags per block; pass 2 gives each block its offset
- * (sum of the counts before it), scans within the block and writes the
- * cells in order.  Each thread owns a contiguous run of kPerThread
- * positions, so thread order is list order.  block_counts is scratch
- * (n_blocks ints); the last block writes the total. */
-static const int kPerThread = 16;
-static const int kChunk = kThreads * kPerThread; /* positions per block */
+ * Positions v = 0 .. n-1 of that order are cut into chunks of kChunk per
+ * block and kWarpSpan per warp; a warp takes kRounds rounds of 32
+ * consecutive positions, one per lane, and sees each round's flags as one
+ * __ballot_sync word.
+ *   Pass 1 (k_compact_count): every warp counts its set flags (__popc of the
+ *   ballots), the block sums its warps and stores its count; the last block
+ *   to finish (a ticket) turns the counts into exclusive offsets in place (a
+ *   block-wide prefix scan), writes the total to *count and puts the ticket
+ *   back to 0 for the next call.
+ *   Pass 2 (k_compact_scatter): every block reads its offset, scans its
+ *   warps' counts, and each warp writes its cells round by round: a lane's
+ *   slot is the running offset plus the set lanes below it in the round's
+ *   ballot, so the list comes out in order with coalesced stores.
+ * Scratch (compact_scratch_ints): kScratchHead ints holding the ticket on a
+ * 128-byte line of its own, then one int per block.  Flags are read one
+ * byte per lane, so the flags pointer needs no alignment; cells, lin and
+ * count need 4-byte alignment. */
+static const int kRounds = 16;
+static const int kWarpSpan = 32 * kRounds;                 /* 512 positions per warp */
+static const int kChunk = (kThreads / 32) * kWarpSpan;     /* 4096 positions per block */
+static const int kScratchHead = 32;                        /* ticket line */
 
 struct CompactGeom {
     int dim, rows, cols, slices;
@@ -153,116 +167,117 @@ static __device__ __forceinline__ long long order_to_mem(const CompactGeom& g, l
     return k * (long long)g.rows * g.cols + ij;
 }
 
-static __device__ __forceinline__ int count_run(const unsigned char* flags, const CompactGeom& g, long long start)
+static __device__ __forceinline__ bool flag_at(const unsigned char* __restrict__ flags, const CompactGeom& g,
+                                               long long v)
 {
-    int c = 0;
-    if (g.dim == 2 && start + kPerThread <= g.n) {
-        const uint4 w = *(const uint4*)(flags + start); /* start is a multiple of 16 */
-        const unsigned ws[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            /* one bit per non-zero byte */
-            const unsigned x = ws[q];
-            const unsigned nz = ((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x;
-            c += __popc(nz & 0x80808080u);
-        }
-        return c;
-    }
-    for (int q = 0; q < kPerThread; q++) {
-        const long long v = start + q;
-        if (v < g.n && flags[order_to_mem(g, v)])
-            c++;
-    }
-    return c;
+    return v < g.n && flags[order_to_mem(g, v)] != 0;
 }
 
-__global__ void k_compact_count(const unsigned char* flags, CompactGeom g, int* block_counts)
+/* exclusive prefix sums of a[0..n) in place by one block; the total goes to
+ * *total.  Each thread owns a contiguous segment, so the result is in order. */
+static __device__ void block_exclusive_scan(int* a, int n, int* total)
 {
-    __shared__ int warp_sums[kThreads / 32];
-    const long long start = ((long long)blockIdx.x * kThreads + threadIdx.x) * kPerThread;
-    int c = start < g.n ? count_run(flags, g, start) : 0;
-    for (int o = 16; o > 0; o >>= 1)
-        c += __shfl_down_sync(0xffffffffu, c, o);
-    if ((threadIdx.x & 31) == 0)
-        warp_sums[threadIdx.x >> 5] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int s = 0;
-        for (int w = 0; w < kThreads / 32; w++)
-            s += warp_sums[w];
-        block_counts[blockIdx.x] = s;
-    }
-}
-
-__global__ void k_compact_scatter(const unsigned char* flags, CompactGeom g, const int* block_counts,
-                                  int* cells, int* lin, int* count)
-{
-    __shared__ int warp_sums[kThreads / 32];
-    __shared__ int s_offset;
-    /* offset of this block = sum of the counts of the blocks before it */
-    int part = 0;
-    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x)
-        part += block_counts[b];
-    for (int o = 16; o > 0; o >>= 1)
-        part += __shfl_down_sync(0xffffffffu, part, o);
-    if ((threadIdx.x & 31) == 0)
-        warp_sums[threadIdx.x >> 5] = part;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int s = 0;
-        for (int w = 0; w < kThreads / 32; w++)
-            s += warp_sums[w];
-        s_offset = s;
-    }
-    __syncthreads();
-
-    const long long start = ((long long)blockIdx.x * kThreads + threadIdx.x) * kPerThread;
-    const int mine = start < g.n ? count_run(flags, g, start) : 0;
-    /* exclusive scan of `mine` across the block */
+    __shared__ int s_warp[kThreads / 32];
+    const int per = (n + kThreads - 1) / kThreads;
+    const int lo = threadIdx.x * per;
+    const int hi = min(lo + per, n);
+    int sum = 0;
+    for (int b = lo; b < hi; b++)
+        sum += __ldcg(a + b);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int incl = mine;
+    int incl = sum;
     for (int o = 1; o < 32; o <<= 1) {
         const int y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o)
             incl += y;
     }
-    __syncthreads();
     if (lane == 31)
-        warp_sums[warp] = incl;
+        s_warp[warp] = incl;
     __syncthreads();
-    int warp_base = 0;
+    int run = incl - sum;
     for (int w = 0; w < warp; w++)
-        warp_base += warp_sums[w];
-    int pos = s_offset + warp_base + incl - mine;
-    if (mine > 0) {
-        for (int q = 0; q < kPerThread; q++) {
-            const long long v = start + q;
-            if (v >= g.n)
-                break;
-            const long long mem = order_to_mem(g, v);
-            if (flags[mem]) {
-                int i, j, k = 0;
-                if (g.dim == 2) {
-                    i = (int)(v / g.cols);
-                    j = (int)(v % g.cols);
-                    cells[2 * pos] = i;
-                    cells[2 * pos + 1] = j;
-                } else {
-                    k = (int)(v % g.slices);
-                    const long long ij = v / g.slices;
-                    i = (int)(ij / g.cols);
-                    j = (int)(ij % g.cols);
-                    cells[3 * pos] = i;
-                    cells[3 * pos + 1] = j;
-                    cells[3 * pos + 2] = k;
-                }
-                lin[pos] = (int)mem;
-                pos++;
-            }
-        }
+        run += s_warp[w];
+    for (int b = lo; b < hi; b++) {
+        const int c = __ldcg(a + b);
+        a[b] = run;
+        run += c;
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1)
-        *count = pos; /* the last thread ends at the running total */
+    if (threadIdx.x == kThreads - 1)
+        *total = run;
+}
+
+__global__ void __launch_bounds__(kThreads) k_compact_count(const unsigned char* __restrict__ flags, CompactGeom g,
+                                                              int* scratch, int* count)
+{
+    __shared__ int s_warp[kThreads / 32];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long base = (long long)blockIdx.x * kChunk + (long long)warp * kWarpSpan + lane;
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < kRounds; q++)
+        c += __popc(__ballot_sync(0xffffffffu, flag_at(flags, g, base + 32 * q)));
+    if (lane == 0)
+        s_warp[warp] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int w = 0; w < kThreads / 32; w++)
+            s += s_warp[w];
+        scratch[kScratchHead + blockIdx.x] = s;
+        __threadfence(); /* the count is visible before the ticket is taken */
+        s_last = atomicAdd(reinterpret_cast<unsigned*>(scratch), 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last)
+        return;
+    __threadfence();
+    block_exclusive_scan(scratch + kScratchHead, gridDim.x, count);
+    if (threadIdx.x == 0)
+        scratch[0] = 0; /* every ticket of this call has been taken */
+}
+
+__global__ void __launch_bounds__(kThreads) k_compact_scatter(const unsigned char* __restrict__ flags, CompactGeom g,
+                                                                const int* __restrict__ scratch, int* cells, int* lin)
+{
+    __shared__ int s_warp[kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long base = (long long)blockIdx.x * kChunk + (long long)warp * kWarpSpan;
+    unsigned m[kRounds];
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < kRounds; q++) {
+        m[q] = __ballot_sync(0xffffffffu, flag_at(flags, g, base + 32 * q + lane));
+        c += __popc(m[q]);
+    }
+    if (lane == 0)
+        s_warp[warp] = c;
+    __syncthreads();
+    int pos = scratch[kScratchHead + blockIdx.x];
+    for (int w = 0; w < warp; w++)
+        pos += s_warp[w];
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int q = 0; q < kRounds; q++) {
+        if ((m[q] >> lane) & 1u) {
+            const long long v = base + 32 * q + lane;
+            const int slot = pos + __popc(m[q] & below);
+            const long long mem = order_to_mem(g, v);
+            if (g.dim == 2) {
+                const unsigned i = (unsigned)v / (unsigned)g.cols;
+                cells[2 * slot] = (int)i;
+                cells[2 * slot + 1] = (int)((unsigned)v - i * (unsigned)g.cols);
+            } else {
+                const unsigned ij = (unsigned)v / (unsigned)g.slices;
+                const unsigned i = ij / (unsigned)g.cols;
+                cells[3 * slot] = (int)i;
+                cells[3 * slot + 1] = (int)(ij - i * (unsigned)g.cols);
+                cells[3 * slot + 2] = (int)((unsigned)v - ij * (unsigned)g.slices);
+            }
+            lin[slot] = (int)mem;
+        }
+        pos += __popc(m[q]);
+    }
 }
 
 int compact_blocks_needed(long long ncells)
@@ -270,8 +285,13 @@ int compact_blocks_needed(long long ncells)
     return (int)((ncells + kChunk - 1) / kChunk);
 }
 
+long long compact_scratch_ints(long long ncells)
+{
+    return kScratchHead + (long long)compact_blocks_needed(ncells);
+}
+
 cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int cols, int slices, int* cells, int* lin,
-                          int* count, int* block_counts, int n_blocks, cudaStream_t stream)
+                          int* count, int* scratch, long long scratch_ints, cudaStream_t stream)
 {
     CompactGeom g;
     g.dim = dim;
@@ -279,11 +299,11 @@ cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int col
     g.cols = cols;
     g.slices = dim == 3 ? slices : 1;
     g.n = (long long)rows * cols * g.slices;
-    if (n_blocks < compact_blocks_needed(g.n))
+    if (g.n <= 0 || g.n > 0x7fffffffLL || scratch_ints < compact_scratch_ints(g.n))
         return cudaErrorInvalidValue;
     const int nb = compact_blocks_needed(g.n);
-    k_compact_count<<<nb, kThreads, 0, stream>>>(flags, g, block_counts);
-    k_compact_scatter<<<nb, kThreads, 0, stream>>>(flags, g, block_counts, cells, lin, count);
+    k_compact_count<<<nb, kThreads, 0, stream>>>(flags, g, scratch, count);
+    k_compact_scatter<<<nb, kThreads, 0, stream>>>(flags, g, scratch, cells, lin);
     return cudaGetLastError();
 }
 
@@ -333,11 +353,13 @@ bool CalGrid::init(int dim_, int rows_, int cols_, int slices_, int toroidal_, i
         !cuda_ok(cudaMalloc(&d_reduce_result, 64), "cudaMalloc reduction result"))
         return false;
     if (active) {
-        n_blocks = compact_blocks_needed(ncells);
+        scratch_ints = compact_scratch_ints(ncells);
         if (!cuda_ok(cudaMalloc(&d_flags, (size_t)ncells), "cudaMalloc flags") ||
             !cuda_ok(cudaMalloc(&d_cells, (size_t)ncells * dim * sizeof(int)), "cudaMalloc cells") ||
             !cuda_ok(cudaMalloc(&d_lin, (size_t)ncells * sizeof(int)), "cudaMalloc lin") ||
-            !cuda_ok(cudaMalloc(&d_block_counts, (size_t)n_blocks * sizeof(int)), "cudaMalloc scratch") ||
+            !cuda_ok(cudaMalloc(&d_block_counts, (size_t)scratch_ints * sizeof(int)), "cudaMalloc scratch") ||
+            !cuda_ok(cudaMemsetAsync(d_block_counts, 0, (size_t)scratch_ints * sizeof(int), stream),
+                     "memset scratch") ||
             !cuda_ok(cudaMemsetAsync(d_flags, 0, (size_t)ncells, stream), "memset flags"))
             return false;
         if (!cuda_ok(cudaMallocHost(&h_flags, (size_t)ncells), "cudaMallocHost flags"))
@@ -650,7 +672,7 @@ bool CalGrid::compact()
     if (!to_device_all())
         return false;
     return cuda_ok(compact_flags(d_flags, dim, rows, cols, slices, d_cells, d_lin, d_count, d_block_counts,
-                                 n_blocks, stream),
+                                 scratch_ints, stream),
                    "active-cell compaction");
 }
 

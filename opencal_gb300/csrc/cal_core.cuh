@@ -80,8 +80,8 @@ struct CalGrid {
     int* d_cells = nullptr;  /* dim ints per cell, reference order */
     int* d_lin = nullptr;    /* linear index per listed cell */
     int* d_count = nullptr;
-    int* d_block_counts = nullptr;
-    int n_blocks = 0;
+    int* d_block_counts = nullptr; /* compaction scratch: ticket line + per-block counts */
+    long long scratch_ints = 0;
     bool flags_host_valid = true, flags_dev_valid = true;
     unsigned char* h_flags = nullptr; /* host mirror (pinned) */
 
@@ -130,9 +130,12 @@ struct CalGrid {
     void restore(const GridState* st);
 };
 
-/* compaction of byte flags into the reference-ordered active list */
+/* compaction of byte flags into the reference-ordered active list; scratch
+ * holds compact_scratch_ints(cells) ints, the first of which (the ticket)
+ * must be 0 before the first call: every call leaves it at 0 */
 cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int cols, int slices, int* cells, int* lin,
-                          int* count, int* block_counts, int n_blocks, cudaStream_t stream);
+                          int* count, int* scratch, long long scratch_ints, cudaStream_t stream);
 int compact_blocks_needed(long long ncells);
+long long compact_scratch_ints(long long ncells);
 
 } // namespace cal

@@ -43,6 +43,15 @@ namespace cal {
 void set_error(CALError code, const std::string& msg); /* the library's error state (calGetLastError) */
 }
 
+/* false (and the library's error state set) when a CUDA call failed */
+static bool cal_cuda(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess)
+        return true;
+    cal::set_error(CAL_ERROR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
 #define NUMBER_OF_OUTFLOWS 4
 
 /* ======================= 1. the reference program ======================= */
@@ -999,6 +1008,64 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
            cudaSuccess;
 }
 
+/* Trace of one step of a plain run on a flat grid, launched after K2 (one
+ * block): the mass that left the grid in step t (the step's outflows of
+ * border cells towards absent neighbours: f[0] north of row 0, f[3] south of
+ * the last row, f[1] west of column 0, f[2] east of the last column; K2 does
+ * not change f), the step's wet-cell count (K2 has advanced the parity word,
+ * so the step's list is the other one), and whether a cell of the two-cell
+ * edge band holds h != 0 after the step (atomicMin of t + 1 into *edge).
+ * Needs rows, cols >= 5. */
+__global__ void __launch_bounds__(THREADS) k_trace(const double* __restrict__ f, const double* __restrict__ h,
+                                                  const int* __restrict__ counts, int rows, int cols, long long n,
+                                                  int t, double* outflux, int* wet, int* edge)
+{
+    __shared__ double s_part[THREADS / 32];
+    __shared__ int s_any;
+    if (threadIdx.x == 0)
+        s_any = 0;
+    double s = 0.0;
+    for (int j = threadIdx.x; j < cols; j += THREADS)
+        s += f[j];
+    for (int j = threadIdx.x; j < cols; j += THREADS)
+        s += f[3 * n + (long long)(rows - 1) * cols + j];
+    for (int i = threadIdx.x; i < rows; i += THREADS)
+        s += f[n + (long long)i * cols];
+    for (int i = threadIdx.x; i < rows; i += THREADS)
+        s += f[2 * n + (long long)i * cols + cols - 1];
+    for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0)
+        s_part[threadIdx.x >> 5] = s;
+    bool any = false;
+    const int ring = 4 * cols + 4 * (rows - 4);
+    for (int k = threadIdx.x; k < ring; k += THREADS) {
+        int i, j;
+        if (k < 4 * cols) {
+            const int r = k / cols; /* rows 0, 1, rows - 2, rows - 1 */
+            i = r < 2 ? r : rows - 4 + r;
+            j = k - r * cols;
+        } else {
+            const int q = k - 4 * cols, c = q & 3; /* columns 0, 1, cols - 2, cols - 1 */
+            i = 2 + q / 4;
+            j = c < 2 ? c : cols - 4 + c;
+        }
+        any |= h[(long long)i * cols + j] != 0.0;
+    }
+    if (any)
+        s_any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < THREADS / 32; w++)
+            tot += s_part[w];
+        outflux[t] = tot;
+        wet[t] = counts[1 - counts[4]];
+        if (s_any)
+            atomicMin(edge, t + 1);
+    }
+}
+
 /* did the last persistent run give up at a barrier?  (synchronises) */
 static int persist_failed(cudaStream_t st)
 {
@@ -1852,6 +1919,34 @@ static int g_fallbacks = 0;
 static void cal_note_fallback() { g_fallbacks++; }
 extern "C" int cal_sciddicaT_device_loop_fallbacks(void) { return g_fallbacks; }
 
+/* every one of `steps` steps in one cooperative launch: the persistent
+ * split step (plain) or the persistent active-cells split step; the state
+ * must be initialised.  Returns a CALError code (CAL_ERROR_CUDA also when a
+ * grid barrier gave up, which synchronises). */
+static int sciddicaT_persist_steps(struct CALModel2D* ca, int steps, bool fused_ac)
+{
+    long long eps_bits;
+    memcpy(&eps_bits, &P.epsilon, sizeof(double));
+    cudaStream_t st = (cudaStream_t)calGetStream2D(ca);
+    if (fused_ac) {
+        sciddicaT_ac_prepare_now(ca);
+        if (!sdtac::g_state.primed)
+            return CAL_ERROR_OUT_OF_MEMORY;
+    } else {
+        sciddicaT_split_prepare_now(ca);
+        if (!sdt2::g_state.primed)
+            return CAL_ERROR_OUT_OF_MEMORY;
+    }
+    const double* z = (const double*)calGetDeviceBuffer2Dr(ca, Q.z, 0);
+    double* h = (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0);
+    const bool ok = fused_ac ? sdtac::persist(ca, z, h, P.epsilon, P.r, eps_bits, steps, st)
+                             : sdt2::persist(ca, z, h, P.epsilon, P.r, eps_bits, steps, st);
+    if (!ok)
+        return CAL_ERROR_CUDA;
+    calMarkCurrentWritten2Dr(ca, Q.h);
+    return calGetLastError();
+}
+
 /* Runs SCIDDICA-T for `steps` steps on (z0, h0) and returns the final z, h
  * and active list -- the same contract as the oracle's orc_sciddicaT.
  * mode 0 runs the reference program (device processes); mode 1 the fused
@@ -1927,6 +2022,11 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
         P.steps = steps;
         calRunAddDeviceStopConditionFunc2D(run, sciddicaT_device_stop);
         calRunDeviceSteps2D(run, run->initial_step, CAL_RUN_LOOP);
+    } else if (graph == 4 && mode == SDT_MODE_FUSED) {
+        /* every step in one cooperative launch (the persistent split step) */
+        if (steps > 0 && sciddicaT_persist_steps(ca, steps, fused_ac) == CAL_SUCCESS &&
+            (fused_ac ? sdtac::persist_failed(s) : sdt2::persist_failed(s)) != 0)
+            cal::set_error(CAL_ERROR_CUDA, "SCIDDICA-T persistent step: a grid barrier gave up");
     } else {
         for (run->step = run->initial_step; run->step <= run->final_step; run->step++)
             if (!calRunCAStep2D(run))
@@ -2073,35 +2173,10 @@ extern "C" int cal_sciddicaT_steps(void* handle, int steps, int graph)
 {
     sdt2::g_state.hknown = false; /* launches this library did not see may have run since */
     SdtSession* s = (SdtSession*)handle;
-    if (graph == 4 && s->fused_ac) {
-        /* every step in one cooperative launch of the active-cells split step */
-        sciddicaT_ac_prepare_now(s->ca);
-        if (!sdtac::g_state.primed)
-            return CAL_ERROR_OUT_OF_MEMORY;
-        long long eps_bits;
-        memcpy(&eps_bits, &P.epsilon, sizeof(double));
-        const double* z = (const double*)calGetDeviceBuffer2Dr(s->ca, Q.z, 0);
-        double* h = (double*)calGetDeviceBuffer2Dr(s->ca, Q.h, 0);
-        if (!sdtac::persist(s->ca, z, h, P.epsilon, P.r, eps_bits, steps, (cudaStream_t)calGetStream2D(s->ca)))
-            return CAL_ERROR_CUDA;
-        calMarkCurrentWritten2Dr(s->ca, Q.h);
-        return calGetLastError();
-    }
     if (graph == 4) {
-        /* every step in one cooperative launch (split step, plain mode) */
         if (s->mode != SDT_MODE_FUSED)
             return CAL_ERROR_INVALID_ARGUMENT;
-        sciddicaT_split_prepare_now(s->ca);
-        if (!sdt2::g_state.primed)
-            return CAL_ERROR_OUT_OF_MEMORY;
-        long long eps_bits;
-        memcpy(&eps_bits, &P.epsilon, sizeof(double));
-        const double* z = (const double*)calGetDeviceBuffer2Dr(s->ca, Q.z, 0);
-        double* h = (double*)calGetDeviceBuffer2Dr(s->ca, Q.h, 0);
-        if (!sdt2::persist(s->ca, z, h, P.epsilon, P.r, eps_bits, steps, (cudaStream_t)calGetStream2D(s->ca)))
-            return CAL_ERROR_CUDA;
-        calMarkCurrentWritten2Dr(s->ca, Q.h);
-        return calGetLastError();
+        return sciddicaT_persist_steps(s->ca, steps, s->fused_ac);
     }
     if (s->mode == SDT_MODE_FUSED)
         sciddicaT_step_prepare(s->ca);
@@ -2242,6 +2317,59 @@ extern "C" int cal_sciddicaT_read(void* handle, double* h_out)
     sciddicaT_sparse_resolve(s->ca);
     calSyncSubstate2Dr(s->ca, Q.h);
     memcpy(h_out, Q.h->current, s->bytes);
+    return calGetLastError();
+}
+
+/* `steps` plain steps from the current state, one split step (K1, K2) at a
+ * time, each followed by sdt2::k_trace: outflux[t] = mass that left the grid
+ * in step t + 1, wet[t] = wet cells processed in it, *edge_step = first step
+ * after which the two-cell edge band holds h != 0 (-1: none).  Host arrays;
+ * flat grids of at least 5 x 5 cells, plain split-step sessions only.  A
+ * measurement aid, not a timed path (two extra launches per step). */
+extern "C" int cal_sciddicaT_trace(void* handle, int steps, double* outflux, int* wet, int* edge_step)
+{
+    sdt2::g_state.hknown = false;
+    SdtSession* s = (SdtSession*)handle;
+    struct CALModel2D* ca = s ? s->ca : nullptr;
+    if (!s || s->mode != SDT_MODE_FUSED || s->fused_ac || steps < 0 || !outflux || !wet || !edge_step ||
+        ca->T == CAL_SPACE_TOROIDAL || ca->rows < 5 || ca->columns < 5) {
+        cal::set_error(CAL_ERROR_INVALID_ARGUMENT, "cal_sciddicaT_trace: plain split-step session on a flat grid");
+        return CAL_ERROR_INVALID_ARGUMENT;
+    }
+    cudaStream_t st = (cudaStream_t)calGetStream2D(ca);
+    sciddicaT_split_prepare_now(ca);
+    if (!sdt2::g_state.primed)
+        return CAL_ERROR_OUT_OF_MEMORY;
+    double* d_out = nullptr;
+    int* d_wet = nullptr;
+    if (!cal_cuda(cudaMalloc(&d_out, sizeof(double) * (steps + 1)), "cudaMalloc trace") ||
+        !cal_cuda(cudaMalloc(&d_wet, sizeof(int) * (steps + 2)), "cudaMalloc trace")) {
+        cudaFree(d_out);
+        return CAL_ERROR_CUDA;
+    }
+    int* d_edge = d_wet + steps + 1;
+    const int never = 0x7fffffff;
+    cudaMemcpyAsync(d_edge, &never, sizeof(int), cudaMemcpyHostToDevice, st);
+    long long eps_bits;
+    memcpy(&eps_bits, &P.epsilon, sizeof(double));
+    const double* z = (const double*)calGetDeviceBuffer2Dr(ca, Q.z, 0);
+    double* h = (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0);
+    for (int t = 0; t < steps; t++) {
+        if (!sdt2::step(ca, z, h, P.epsilon, P.r, eps_bits, st, nullptr))
+            break;
+        sdt2::k_trace<<<1, sdt2::THREADS, 0, st>>>(sdt2::g_state.f, h, sdt2::g_state.counts, ca->rows, ca->columns,
+                                                   sdt2::g_state.n, t, d_out, d_wet, d_edge);
+    }
+    calMarkCurrentWritten2Dr(ca, Q.h);
+    int edge = never;
+    if (cal_cuda(cudaGetLastError(), "trace launches") &&
+        cal_cuda(cudaMemcpyAsync(outflux, d_out, sizeof(double) * steps, cudaMemcpyDeviceToHost, st), "trace") &&
+        cal_cuda(cudaMemcpyAsync(wet, d_wet, sizeof(int) * steps, cudaMemcpyDeviceToHost, st), "trace") &&
+        cal_cuda(cudaMemcpyAsync(&edge, d_edge, sizeof(int), cudaMemcpyDeviceToHost, st), "trace"))
+        cal_cuda(cudaStreamSynchronize(st), "trace");
+    *edge_step = edge == never ? -1 : edge;
+    cudaFree(d_out);
+    cudaFree(d_wet);
     return calGetLastError();
 }
 

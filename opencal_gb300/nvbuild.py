@@ -2,8 +2,9 @@
 
   opencal_gb300/lib/libopencal_gb300.so  the C-ABI library (include/opencal/*.h)
   opencal_gb300/lib/libopencal_models.so the models shipped with it (SCIDDICA-T,
-                                         Life, probe rules) and their driver
-                                         entry points, linked against the former
+                                         SCIARA-fv2, mbusu, Life 2D/3D) and their
+                                         driver entry points, linked against the
+                                         former
 
 Compiles translation units in parallel and skips those whose object is newer
 than the source and every header.  No cmake.
@@ -33,9 +34,9 @@ COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-cuda
 MODEL_FLAGS = ["--fmad=false", "-Xcompiler=-ffp-contract=off"]  # no contraction on the device or host side
 
 CORE_SOURCES = ["cal_core.cu", "cal2D.cu", "cal3D.cu", "cal2DRun.cu", "cal3DRun.cu", "calIO.cu", "calReduction.cu", "cal_noalloc.cu"]
-MODEL_SOURCES = ["models/sciddicaT.cu", "models/sciddicaT_adjoint.cu", "models/sciddicaT_batch.cu", "models/sciara.cu",
-                 "models/sciara_batch.cu", "models/mbusu.cu", "models/life.cu",
-                 "models/probes.cu"]
+MODEL_SOURCES = ["models/sciddicaT.cu", "models/sciddicaT_adjoint.cu", "models/sciddicaT_batch.cu",
+                 "models/sciddicaT_unsafe.cu", "models/sciara.cu", "models/sciara_batch.cu", "models/mbusu.cu",
+                 "models/life.cu", "models/life3d.cu", "models/fp64_peak.cu"]
 
 
 def nvcc() -> str:

@@ -20,7 +20,9 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = os.environ.get("OPENCAL_REFERENCE", "/root/reference")
+# the reference source tree, for the reference build that pins the oracle:
+# given by the OPENCAL_REFERENCE environment variable (no default)
+REF_TREE = os.environ.get("OPENCAL_REFERENCE")
 
 _LIBS: dict[str, C.CDLL] = {}
 
@@ -32,11 +34,13 @@ _i32 = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _pl = C.POINTER(C.c_long)
 
 
-def build(ref: bool = False) -> None:
-    """Compile the oracle (and, when asked and available, the reference)."""
+def build(ref: bool = False, ref_tree: str | None = None) -> None:
+    """Compile the oracle and, when asked and the reference tree is given
+    (argument or OPENCAL_REFERENCE) and present, the reference build."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref and os.path.isdir(os.path.join(REF_TREE, "OpenCAL-OMP", "source")):
-        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={REF_TREE}"], check=True)
+    tree = ref_tree or REF_TREE
+    if ref and tree and os.path.isdir(os.path.join(tree, "OpenCAL-OMP", "source")):
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={tree}"], check=True)
 
 
 def ref_available() -> bool:
@@ -60,6 +64,12 @@ def _bind(lib: C.CDLL, prefix: str) -> C.CDLL:
     f.restype = C.c_int
     f = getattr(lib, prefix + "life3d")
     f.argtypes = [C.c_int] * 10 + [_u8, _u8]
+    f.restype = C.c_int
+    f = getattr(lib, prefix + "nbprobe2d_custom")
+    f.argtypes = [C.c_int] * 5 + [C.c_void_p, _dp, _dp]
+    f.restype = C.c_int
+    f = getattr(lib, prefix + "reduce2d")
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_double)]
     f.restype = C.c_int
     return lib
 
@@ -98,6 +108,27 @@ def sciddicaT(z0, h0, steps, *, toroidal=False, ac=False, p_r=0.5, p_eps=0.001, 
     return z, h, (cells[: n.value].copy() if (ac and want_cells) else np.zeros((0, 2), np.int32))
 
 
+def sciddicaT_trace(z0, h0, steps, *, p_r=0.5, p_eps=0.001, kind="serial"):
+    """Plain SCIDDICA-T on a flat grid with its boundary trace: returns
+    (z, h, outflux, edge_step): outflux[s - 1] is the mass that left the grid
+    in step s (outflows of border cells towards absent neighbours), edge_step
+    the first step after which a cell of the two-cell edge band is wet (-1:
+    never).  Serial or OpenMP build only."""
+    z0 = np.ascontiguousarray(z0, dtype=np.float64)
+    h0 = np.ascontiguousarray(h0, dtype=np.float64)
+    rows, cols = z0.shape
+    z, h = np.empty_like(z0), np.empty_like(h0)
+    out = np.zeros(max(int(steps), 1))
+    edge = C.c_int(-1)
+    f = _fn(kind, "sciddicaT_trace")
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double] + [C.c_void_p] * 5 + [C.POINTER(C.c_int)]
+    f.restype = C.c_int
+    if f(rows, cols, int(steps), p_r, p_eps, z0.ctypes.data, h0.ctypes.data, z.ctypes.data, h.ctypes.data,
+         out.ctypes.data, C.byref(edge)):
+        raise RuntimeError("oracle sciddicaT_trace failed")
+    return z, h, out[: int(steps)], edge.value
+
+
 def life2d(s0, steps, *, toroidal=True, as_int=False, kind="serial"):
     s0 = np.ascontiguousarray(s0, dtype=np.uint8)
     out = np.empty_like(s0)
@@ -114,6 +145,31 @@ def nbprobe2d(v0, steps, *, nbhd=NB_HEX, toroidal=True, kind="serial"):
     if _fn(kind, "nbprobe2d")(rows, cols, int(nbhd), int(toroidal), int(steps), v0, out):
         raise RuntimeError("oracle nbprobe2d failed")
     return out
+
+
+def nbprobe2d_custom(v0, steps, offsets, *, toroidal=True, kind="serial"):
+    """The probe rule on a custom neighbourhood: `offsets` (di, dj) appended
+    in order, as calAddNeighbor2D does."""
+    v0 = np.ascontiguousarray(v0, dtype=np.float64)
+    offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int32).reshape(-1))
+    out = np.empty_like(v0)
+    rows, cols = v0.shape
+    if _fn(kind, "nbprobe2d_custom")(rows, cols, int(toroidal), int(steps), len(offs) // 2, offs.ctypes.data, v0,
+                                     out):
+        raise RuntimeError("oracle nbprobe2d_custom failed")
+    return out
+
+
+def reduce2d(kind_of_data: int, data, op: int, *, kind="serial") -> float:
+    """calReductionOperation2D{b,i,r} over `data` (kind_of_data: 0 byte, 1
+    int, 2 real; op: the REDUCTION_OPERATION value).  The serial oracle folds
+    every cell; the reference build folds elements 0 .. rows-1 only."""
+    data = np.ascontiguousarray(data)
+    rows, cols = data.shape
+    out = C.c_double(0.0)
+    if _fn(kind, "reduce2d")(int(kind_of_data), rows, cols, data.ctypes.data, int(op), C.byref(out)):
+        raise RuntimeError("oracle reduce2d failed")
+    return out.value
 
 
 def acprobe(v0, steps, *, nbhd=NB_MOORE, toroidal=True, thr=0.5, kind="serial"):

@@ -541,3 +541,62 @@ void orc_add_nextx(orc_ca* m, orc_sub* q, int i, int j, int k, int n, double v)
     if (orc_neighbor(m, i, j, k, n, &a, &b, &c))
         orc_add_next(m, q, a, b, c, v);
 }
+
+/* ======================= reductions ===================================== */
+/* calReductionOperation2Db/i/r (OpenCAL-OMP/source/cal2DReduction.c:18-500,
+ * serial path): start from element 0 of the current layer and fold every
+ * other element in index order, in the substate's own type (CALbyte and
+ * CALint wrap; the binary operations on reals go through CALint,
+ * cal2DReduction.c:437-455).  One deliberate difference: the reference sets
+ * the last thread's end index to `model->rows` instead of rows * columns
+ * (cal2DReduction.c:45-47), so its serial build folds only elements
+ * 0 .. rows-1; here every cell is folded.  Both agree on grids with one
+ * column.  kind: 0 byte, 1 int, 2 real; the result is returned as a double. */
+#define ORC_FOLD(T, ACC, X, OP)                                                          \
+    switch (OP) {                                                                        \
+    case 1: if (ACC < X) ACC = X; break;                                                 \
+    case 2: if (ACC > X) ACC = X; break;                                                 \
+    case 3: ACC += X; break;                                                             \
+    case 4: ACC *= X; break;                                                             \
+    case 5: ACC = (T)(ACC && X); break;                                                  \
+    case 6: ACC = (T)((CALINT_T)ACC & (CALINT_T)X); break;                               \
+    case 7: ACC = (T)(ACC || X); break;                                                  \
+    case 8: ACC = (T)((CALINT_T)ACC | (CALINT_T)X); break;                               \
+    case 9: ACC = (T)(!!ACC != !!X); break;                                              \
+    case 10: ACC = (T)((CALINT_T)ACC ^ (CALINT_T)X); break;                              \
+    default: break;                                                                      \
+    }
+#define CALINT_T int
+
+int orc_reduce2d(int kind, int rows, int cols, const void* data, int op, double* out)
+{
+    long n = (long)rows * cols, i;
+    if (n <= 0 || op < 1 || op > 10)
+        return 1;
+    if (kind == 0) {
+        const char* v = (const char*)data;
+        char acc = v[0];
+        for (i = 1; i < n; i++) {
+            char x = v[i];
+            ORC_FOLD(char, acc, x, op)
+        }
+        *out = (double)acc;
+    } else if (kind == 1) {
+        const int* v = (const int*)data;
+        int acc = v[0];
+        for (i = 1; i < n; i++) {
+            int x = v[i];
+            ORC_FOLD(int, acc, x, op)
+        }
+        *out = (double)acc;
+    } else {
+        const double* v = (const double*)data;
+        double acc = v[0];
+        for (i = 1; i < n; i++) {
+            double x = v[i];
+            ORC_FOLD(double, acc, x, op)
+        }
+        *out = acc;
+    }
+    return 0;
+}

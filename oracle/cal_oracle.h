@@ -151,4 +151,14 @@ void orc_run_all(orc_run* r);
 #ifdef __cplusplus
 }
 #endif
+/* a reduction of cal2DReduction.h over rows x cols values (kind: 0 byte,
+ * 1 int, 2 real) */
+int orc_reduce2d(int kind, int rows, int cols, const void* data, int op, double* out);
+
+/* plain SCIDDICA-T on a flat grid with the mass leaving the grid per step
+ * (outflux[steps]) and the first step after which the two-cell edge band
+ * holds h != 0 (edge_step, -1 if never) */
+int orc_sciddicaT_trace(int rows, int cols, int steps, double p_r, double p_eps, const double* z0, const double* h0,
+                        double* z_out, double* h_out, double* outflux, int* edge_step);
+
 #endif

@@ -121,6 +121,49 @@ static void sdt_steer_ac(orc_ca* m)
         orc_init_sub_next(m, sdt.f[q], 0.0);
 }
 
+/* Trace of a plain run on a flat grid, for the mass balance: after each
+ * step (at the steering, when f holds the step's outflows) the outflows of
+ * border cells towards absent neighbours -- the mass that leaves the grid --
+ * are summed into outflux[step - 1], and the first step after which a cell
+ * of the two-cell edge band holds h != 0 is recorded. */
+static struct {
+    double* outflux;
+    int* edge_step;
+    int step;
+} trc;
+
+static void sdt_steer_trace(orc_ca* m)
+{
+    const int R = m->rows, C = m->cols;
+    double s = 0.0;
+    int i, j;
+    trc.step++;
+    /* von Neumann: f[0] north, f[1] west, f[2] east, f[3] south */
+    for (j = 0; j < C; j++)
+        s += orc_get(m, sdt.f[0], 0, j, 0);
+    for (j = 0; j < C; j++)
+        s += orc_get(m, sdt.f[3], R - 1, j, 0);
+    for (i = 0; i < R; i++)
+        s += orc_get(m, sdt.f[1], i, 0, 0);
+    for (i = 0; i < R; i++)
+        s += orc_get(m, sdt.f[2], i, C - 1, 0);
+    trc.outflux[trc.step - 1] = s;
+    if (*trc.edge_step < 0) {
+        for (i = 0; i < R && *trc.edge_step < 0; i++)
+            for (j = 0; j < C; j++) {
+                if (i >= 2 && i < R - 2 && j == 2) {
+                    j = C - 3; /* skip the interior of the row */
+                    continue;
+                }
+                if (orc_get(m, sdt.h, i, j, 0) != 0.0) {
+                    *trc.edge_step = trc.step;
+                    break;
+                }
+            }
+    }
+    sdt_steer_plain(m);
+}
+
 static void export_active(const orc_ca* m, long* n_active, int* cells_out)
 {
     if (n_active)
@@ -174,6 +217,53 @@ int orc_sciddicaT(int rows, int cols, int toroidal, int ac, int steps, double p_
     orc_free(m);
     return err;
 }
+
+/* plain SCIDDICA-T on a flat grid with the trace above: outflux[steps]
+ * (mass leaving per step) and edge_step (-1 when the band stays dry) */
+int orc_sciddicaT_trace(int rows, int cols, int steps, double p_r, double p_eps, const double* z0, const double* h0,
+                        double* z_out, double* h_out, double* outflux, int* edge_step)
+{
+    orc_run run;
+    int q, err;
+    orc_ca* m = orc_def2d(rows, cols, ORC_NB_VN, 0, 0);
+    if (!m || rows < 5 || cols < 5)
+        return 1;
+    memset(&sdt, 0, sizeof(sdt));
+    sdt.r = p_r;
+    sdt.eps = p_eps;
+    orc_add_ep2(m, sdt_flows);
+    orc_add_ep2(m, sdt_width);
+    sdt.z = orc_add_sub(m, ORC_R);
+    sdt.h = orc_add_sub(m, ORC_R);
+    for (q = 0; q < 4; q++)
+        sdt.f[q] = orc_add_sub(m, ORC_R);
+    orc_load(m, sdt.z, z0);
+    orc_load(m, sdt.h, h0);
+    trc.outflux = outflux;
+    trc.edge_step = edge_step;
+    trc.step = 0;
+    *edge_step = -1;
+
+    memset(&run, 0, sizeof(run));
+    run.m = m;
+    run.initial = 1;
+    run.final_ = steps;
+    run.implicit = 1;
+    run.init = sdt_init;
+    run.steering = sdt_steer_trace;
+    if (steps > 0)
+        orc_run_all(&run);
+    else
+        orc_run_init(&run);
+    if (z_out)
+        orc_store(m, sdt.z, z_out);
+    if (h_out)
+        orc_store(m, sdt.h, h_out);
+    err = m->error;
+    orc_free(m);
+    return err;
+}
+
 
 /* ======================= Life 2D (B3/S23) ============================= */
 
@@ -243,6 +333,35 @@ int orc_nbprobe2d(int rows, int cols, int nbhd, int toroidal, int steps, const d
     orc_ca* m = orc_def2d(rows, cols, nbhd, toroidal, 0);
     if (!m)
         return 1;
+    orc_add_ep2(m, hex_rule);
+    hex_q = orc_add_sub(m, ORC_R);
+    orc_load(m, hex_q, v0);
+    memset(&run, 0, sizeof(run));
+    run.m = m;
+    run.initial = 1;
+    run.final_ = steps;
+    run.implicit = 1;
+    if (steps > 0)
+        orc_run_all(&run);
+    orc_store(m, hex_q, v_out);
+    orc_free(m);
+    return 0;
+}
+
+/* the same rule on a custom neighbourhood: the model is defined with
+ * CAL_CUSTOM_NEIGHBORHOOD_2D (no entries) and the offsets (di, dj) are
+ * appended in order, as calAddNeighbor2D does (OpenCAL-OMP/source/
+ * cal2D.c:444-466); entry 0 is the caller's first offset */
+int orc_nbprobe2d_custom(int rows, int cols, int toroidal, int steps, int nx, const int* offs, const double* v0,
+                         double* v_out)
+{
+    orc_run run;
+    int n;
+    orc_ca* m = orc_def2d(rows, cols, ORC_NB_CUSTOM, toroidal, 0);
+    if (!m || nx > ORC_MAX_X)
+        return 1;
+    for (n = 0; n < nx; n++)
+        orc_add_neighbor(m, offs[2 * n], offs[2 * n + 1], 0);
     orc_add_ep2(m, hex_rule);
     hex_q = orc_add_sub(m, ORC_R);
     orc_load(m, hex_q, v0);

@@ -273,6 +273,29 @@ int ref_nbprobe2d(int rows, int cols, int nbhd, int toroidal, int steps, const d
     return 0;
 }
 
+/* the rule on a custom neighbourhood built with calAddNeighbor2D */
+int ref_nbprobe2d_custom(int rows, int cols, int toroidal, int steps, int nx, const int* offs, const double* v0,
+                         double* v_out)
+{
+    struct CALModel2D* m = calCADef2D(rows, cols, CAL_CUSTOM_NEIGHBORHOOD_2D,
+                                      toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    struct CALRun2D* run = calRunDef2D(m, 1, steps, CAL_UPDATE_IMPLICIT);
+    size_t bytes = sizeof(double) * (size_t)rows * cols;
+    int n;
+    for (n = 0; n < nx; n++)
+        calAddNeighbor2D(m, offs[2 * n], offs[2 * n + 1]);
+    calAddElementaryProcess2D(m, hex_rule);
+    HQ = calAddSubstate2Dr(m);
+    memcpy(HQ->current, v0, bytes);
+    memcpy(HQ->next, v0, bytes);
+    if (steps > 0)
+        calRun2D(run);
+    memcpy(v_out, HQ->current, bytes);
+    calRunFinalize2D(run);
+    finalize2d(m);
+    return 0;
+}
+
 /* ======================= active-cell spread probe ===================== */
 
 static struct {
@@ -618,6 +641,34 @@ int ref_sciddicaT_unsafe(int rows, int cols, int toroidal, int steps, double p_r
     memcpy(z_out, SUR.z->current, bytes);
     memcpy(h_out, SUR.h->current, bytes);
     calRunFinalize2D(run);
+    finalize2d(m);
+    return 0;
+}
+
+/* ======================= reductions ===================================== */
+/* the reference's own calReductionOperation2Db/i/r on a model holding
+ * `data` (kind: 0 byte, 1 int, 2 real); its serial build folds elements
+ * 0 .. rows-1 only (cal2DReduction.c:45-47), so callers compare it with the
+ * oracle on grids of one column */
+#include <cal2DReduction.h>
+
+int ref_reduce2d(int kind, int rows, int cols, const void* data, int op, double* out)
+{
+    struct CALModel2D* m = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D, CAL_SPACE_TOROIDAL, CAL_NO_OPT);
+    size_t n = (size_t)rows * cols;
+    if (kind == 0) {
+        struct CALSubstate2Db* q = calAddSubstate2Db(m);
+        memcpy(q->current, data, n);
+        *out = (double)calReductionOperation2Db(m, q, (enum REDUCTION_OPERATION)op);
+    } else if (kind == 1) {
+        struct CALSubstate2Di* q = calAddSubstate2Di(m);
+        memcpy(q->current, data, n * sizeof(int));
+        *out = (double)calReductionOperation2Di(m, q, (enum REDUCTION_OPERATION)op);
+    } else {
+        struct CALSubstate2Dr* q = calAddSubstate2Dr(m);
+        memcpy(q->current, data, n * sizeof(double));
+        *out = calReductionOperation2Dr(m, q, (enum REDUCTION_OPERATION)op);
+    }
     finalize2d(m);
     return 0;
 }

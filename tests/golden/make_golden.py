@@ -1,7 +1,7 @@
 """Regenerate the committed golden fixtures from the REFERENCE itself.
 
-Needs the reference source tree (default /root/reference, override with
-OPENCAL_REFERENCE); nothing that runs on the GPU machine calls this script.
+Needs the reference source tree, named by the OPENCAL_REFERENCE environment
+variable; nothing that runs on the GPU machine calls this script.
 
 1. Compiles the reference library and its two SCIDDICA-T examples from their
    own sources (oracle/ref/Makefile), runs them on the examples' shipped
@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 from opencal_gb300 import workloads as W  # noqa: E402
 
-REF = os.environ.get("OPENCAL_REFERENCE", "/root/reference")
+REF = os.environ.get("OPENCAL_REFERENCE") or ""  # required when run as a script (checked in main)
 PLAIN_DATA = os.path.join(REF, "OpenCAL-OMP/examples/calomp_sciddicaT/data")
 AC_DATA = os.path.join(REF, "OpenCAL/examples/cal_sciddicaT-activecells-glut/data")
 

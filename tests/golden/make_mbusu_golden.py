@@ -1,7 +1,7 @@
 """Regenerate the mbusu golden fixtures from the REFERENCE itself.
 
-Needs the reference source tree (default /root/reference, override with
-OPENCAL_REFERENCE); nothing that runs on the GPU machine calls this script.
+Needs the reference source tree, named by the OPENCAL_REFERENCE environment
+variable; nothing that runs on the GPU machine calls this script.
 
 Compiles the reference's mbusu example (OpenCAL/examples/cal_mbusu-glut/
 source/mbusu.c, unmodified) against the serially built reference library
@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
 
-REF = os.environ.get("OPENCAL_REFERENCE", "/root/reference")
+REF = os.environ.get("OPENCAL_REFERENCE") or ""  # required when run as a script (checked in main)
 SHIPPED = os.path.join(REF, "OpenCAL", "examples", "cal_mbusu-glut")
 N = 130 * 160 * 30
 
@@ -54,6 +54,8 @@ def hashes(raw: np.ndarray) -> np.ndarray:
 
 
 def main() -> None:
+    if not REF or not os.path.isdir(os.path.join(REF, "OpenCAL-OMP")):
+        sys.exit("set OPENCAL_REFERENCE to the OpenCAL source tree")
     ap = argparse.ArgumentParser()
     ap.add_argument("--reuse", help="state file of a finished full reference run (skips the 35-minute run)")
     ap.add_argument("--reuse-ris", help="ris10g.txt written by that run")

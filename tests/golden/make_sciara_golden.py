@@ -1,7 +1,7 @@
 """Regenerate the SCIARA-fv2 golden fixtures from the REFERENCE itself.
 
-Needs the reference source tree (default /root/reference, override with
-OPENCAL_REFERENCE); nothing that runs on the GPU machine calls this script.
+Needs the reference source tree, named by the OPENCAL_REFERENCE environment
+variable; nothing that runs on the GPU machine calls this script.
 
 Compiles the reference's SCIARA-fv2 example (OpenCAL-OMP/examples/
 calomp_sciara-fv2, its own sources, unmodified) against the serially built
@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 from opencal_gb300 import workloads as W  # noqa: E402
 
-REF = os.environ.get("OPENCAL_REFERENCE", "/root/reference")
+REF = os.environ.get("OPENCAL_REFERENCE") or ""  # required when run as a script (checked in main)
 CFG_KEYS = ["Pclock", "PTsol", "PTvent", "Pr(Tsol)", "Pr(Tvent)", "Phc(Tsol)", "Phc(Tvent)", "Pcool", "Prho",
             "Pepsilon", "Psigma", "Pcv"]
 
@@ -84,6 +84,8 @@ def write_case(prefix: str, z, vents, rates, emission_time, params):
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "OpenCAL-OMP")):
+        sys.exit("set OPENCAL_REFERENCE to the OpenCAL source tree")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={REF}", "all", "sciara"],
                    check=True)
     oracle.build()

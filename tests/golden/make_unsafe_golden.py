@@ -5,8 +5,8 @@ compiled serially into oracle/_ref/libref.so by oracle/ref/Makefile) on the
 unsafe-operation probe (every neighbourhood, toroidal) and on SCIDDICA-T in
 the unsafe form of OpenCAL/examples/cal_sciddicaT-unsafe, checks that the
 oracle restatement reproduces them bit for bit, and writes unsafe_cases.npz.
-Needs the reference source tree (default /root/reference, override with
-OPENCAL_REFERENCE).
+Needs the reference source tree, named by the OPENCAL_REFERENCE environment
+variable.
 
 Run:  python tests/golden/make_unsafe_golden.py
 """
@@ -36,6 +36,8 @@ def probe_inputs(rows, cols, seed):
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "OpenCAL-OMP")):
+        sys.exit("set OPENCAL_REFERENCE to the OpenCAL source tree")
     oracle.build(ref=True)
     out = {}
     for nb in (1, 2, 3, 4):

@@ -1,22 +1,23 @@
 /*
- * probes.cu -- small rules that exercise the engine's semantics, written as
- * device elementary processes through the public API.  Each entry point has
- * the same contract as the oracle's function of the same suffix
+ * probes.cu -- TEST INFRASTRUCTURE: small rules that exercise the engine's
+ * semantics through the public C API, built into a test-only library
+ * (tests/native/build/libopencal_probes.so, linked against
+ * libopencal_gb300.so) and never shipped with the product.  Each entry
+ * point has the same contract as the oracle's function of the same suffix
  * (oracle/oracle_models.c), so the parity tests compare them directly.
  *
  *   nbprobe2d  v' = v/4 + sum_n v_n * n/64 on any 2D neighbourhood (exercises
  *              the neighbour tables, including the hexagonal odd-column /
- *              odd-row shift of OpenCAL-OMP/source/cal2D.c:859-870)
+ *              odd-row shift of OpenCAL-OMP/source/cal2D.c:859-870, and
+ *              custom neighbourhoods built with calAddNeighbor2D,
+ *              OpenCAL-OMP/source/cal2D.c:444-466)
  *   acprobe    three processes with SCIDDICA-T's active-cell structure,
  *              2D or 3D (add on outflow, update, remove, steering on next)
- *   life3d     OpenCAL/examples/cal_life3D-glut/source/life3D.cpp:70-83
  *   unsafe2d   every unsafe operation (cal2DUnsafe.h): integer spreads with
  *              calAddNext / calAddNextX, and single-writer neighbour stores
  *              with calSetX / calGetNextX / calSetCurrentX / calInitX
- *   sciddicaT_unsafe  OpenCAL/examples/cal_sciddicaT-unsafe/source/
- *              sciddicaT.c:35-107: outflows moved at once into next(h) of
- *              the cell and the receiver (calAddNext / calAddNextX on the
- *              GPU: the reference's get-then-set under a lock)
+ *   reduce2d   the device reductions of cal2DReduction.h on a given array
+ *   exact_div  device check of models/exact_div.cuh against IEEE division
  */
 #include <string.h>
 
@@ -41,7 +42,6 @@ static int finish3d(struct CALModel3D* ca, struct CALRun3D* run)
     calFinalize3D(ca);
     return err;
 }
-
 /* ======================= neighbourhood probe ============================ */
 
 __managed__ struct CALSubstate2Dr* nbQ;
@@ -62,6 +62,33 @@ extern "C" int cal_nbprobe2d_run(int rows, int cols, int nbhd, int toroidal, int
                                        toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
     if (!ca)
         return calGetLastError();
+    struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
+    calAddElementaryProcess2D(ca, nbprobe_rule);
+    nbQ = calAddSubstate2Dr(ca);
+    const size_t bytes = sizeof(double) * (size_t)rows * cols;
+    memcpy(nbQ->current, v0, bytes);
+    memcpy(nbQ->next, v0, bytes);
+    calMarkHostDirty2D(ca);
+    calRunSetGraph2D(run, graph ? CAL_TRUE : CAL_FALSE);
+    if (steps > 0)
+        calRun2D(run);
+    calSync2D(ca);
+    memcpy(v_out, nbQ->current, bytes);
+    return finish2d(ca, run);
+}
+
+/* the same rule on a custom neighbourhood: CAL_CUSTOM_NEIGHBORHOOD_2D, then
+ * the offsets (di, dj) appended with calAddNeighbor2D */
+extern "C" int cal_nbprobe2d_custom_run(int rows, int cols, int toroidal, int steps, int nx, const int* offs,
+                                        const double* v0, double* v_out, int graph)
+{
+    calClearError();
+    struct CALModel2D* ca = calCADef2D(rows, cols, CAL_CUSTOM_NEIGHBORHOOD_2D,
+                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    if (!ca)
+        return calGetLastError();
+    for (int n = 0; n < nx; n++)
+        calAddNeighbor2D(ca, offs[2 * n], offs[2 * n + 1]);
     struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
     calAddElementaryProcess2D(ca, nbprobe_rule);
     nbQ = calAddSubstate2Dr(ca);
@@ -224,53 +251,6 @@ extern "C" int cal_acprobe_run(int dim, int rows, int cols, int slices, int nbhd
         *n_active = ca->A.size_current;
     if (cells_out && ca->A.size_current > 0)
         memcpy(cells_out, ca->A.cells, sizeof(int) * 3 * (size_t)ca->A.size_current);
-    return finish3d(ca, run);
-}
-
-/* ======================= Life 3D ======================================== */
-
-__managed__ struct CALSubstate3Db* L3;
-__managed__ int L3rule[4];
-
-CAL_ELEMENTARY_PROCESS_3D(life3d_rule)(struct CALModel3D* ca, int i, int j, int k)
-{
-    int sum = 0, n;
-    CALbyte alive = calGet3Db(ca, L3, i, j, k);
-    CALbyte nextState = alive;
-    for (n = 0; n < ca->sizeof_X; n++)
-        sum += calGetX3Db(ca, L3, i, j, k, n);
-    if (alive && (sum < L3rule[0] || sum > L3rule[1]))
-        nextState = 0;
-    else if (!alive && (sum >= L3rule[2] && sum <= L3rule[3]))
-        nextState = 1;
-    calSet3Db(ca, L3, i, j, k, nextState);
-}
-
-extern "C" int cal_life3d_run(int rows, int cols, int slices, int nbhd, int toroidal, int steps, int r1, int r2,
-                              int r3, int r4, const unsigned char* s0, unsigned char* s_out, int graph)
-{
-    calClearError();
-    struct CALModel3D* ca = calCADef3D(rows, cols, slices, (enum CALNeighborhood3D)nbhd,
-                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
-    if (!ca)
-        return calGetLastError();
-    struct CALRun3D* run = calRunDef3D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
-    L3rule[0] = r1;
-    L3rule[1] = r2;
-    L3rule[2] = r3;
-    L3rule[3] = r4;
-    calAddElementaryProcess3D(ca, life3d_rule);
-    L3 = calAddSubstate3Db(ca);
-    const long long n = (long long)rows * cols * slices;
-    for (long long c = 0; c < n; c++)
-        L3->current[c] = L3->next[c] = (CALbyte)s0[c];
-    calMarkHostDirty3D(ca);
-    calRunSetGraph3D(run, graph ? CAL_TRUE : CAL_FALSE);
-    if (steps > 0)
-        calRun3D(run);
-    calSync3D(ca);
-    for (long long c = 0; c < n; c++)
-        s_out[c] = (unsigned char)L3->current[c];
     return finish3d(ca, run);
 }
 
@@ -447,89 +427,3 @@ extern "C" int cal_unsafe2d_run(int rows, int cols, int nbhd, int toroidal, int 
     return finish2d(ca, run);
 }
 
-/* ======================= SCIDDICA-T, unsafe form ======================== */
-
-struct SdtuQ {
-    struct CALSubstate2Dr* z;
-    struct CALSubstate2Dr* h;
-    double r, eps;
-};
-__managed__ struct SdtuQ SU;
-
-CAL_ELEMENTARY_PROCESS_2D(sciddicaT_unsafe_transition)(struct CALModel2D* ca, int i, int j)
-{
-    bool out[5] = {false, false, false, false, false};
-    double u[5];
-    const double m = calGet2Dr(ca, SU.h, i, j) - SU.eps;
-    u[0] = calGet2Dr(ca, SU.z, i, j) + SU.eps;
-    for (int n = 1; n < ca->sizeof_X; n++)
-        u[n] = calGetX2Dr(ca, SU.z, i, j, n) + calGetX2Dr(ca, SU.h, i, j, n);
-    double avg;
-    bool again;
-    do {
-        again = false;
-        avg = m;
-        int count = 0;
-        for (int n = 0; n < ca->sizeof_X; n++)
-            if (!out[n]) {
-                avg += u[n];
-                count++;
-            }
-        if (count != 0)
-            avg /= count;
-        for (int n = 0; n < ca->sizeof_X; n++)
-            if (avg <= u[n] && !out[n]) {
-                out[n] = true;
-                again = true;
-            }
-    } while (again);
-    for (int n = 1; n < ca->sizeof_X; n++)
-        if (!out[n]) {
-            const double f = (avg - u[n]) * SU.r;
-            calAddNext2Dr(ca, SU.h, i, j, -f);
-            calAddNextX2Dr(ca, SU.h, i, j, n, f);
-        }
-}
-
-static void sciddicaT_unsafe_init(struct CALModel2D* ca)
-{
-    for (int i = 0; i < ca->rows; i++)
-        for (int j = 0; j < ca->columns; j++) {
-            const double h = calGet2Dr(ca, SU.h, i, j);
-            if (h > 0.0)
-                calSetCurrent2Dr(ca, SU.z, i, j, calGet2Dr(ca, SU.z, i, j) - h);
-        }
-}
-
-extern "C" int cal_sciddicaT_unsafe_run(int rows, int cols, int toroidal, int steps, double p_r, double p_eps,
-                                        const double* z0, const double* h0, double* z_out, double* h_out, int graph)
-{
-    calClearError();
-    struct CALModel2D* ca = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D,
-                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
-    if (!ca)
-        return calGetLastError();
-    calSetUnsafe2D(ca);
-    struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
-    calAddElementaryProcess2D(ca, sciddicaT_unsafe_transition);
-    SU.z = calAddSubstate2Dr(ca);
-    SU.h = calAddSubstate2Dr(ca);
-    SU.r = p_r;
-    SU.eps = p_eps;
-    const size_t bytes = sizeof(double) * (size_t)rows * cols;
-    memcpy(SU.z->current, z0, bytes);
-    memcpy(SU.z->next, z0, bytes);
-    memcpy(SU.h->current, h0, bytes);
-    memcpy(SU.h->next, h0, bytes);
-    calMarkHostDirty2D(ca);
-    calRunAddInitFunc2D(run, sciddicaT_unsafe_init);
-    calRunSetGraph2D(run, graph ? CAL_TRUE : CAL_FALSE);
-    if (steps > 0)
-        calRun2D(run);
-    else
-        calRunInitSimulation2D(run);
-    calSync2D(ca);
-    memcpy(z_out, SU.z->current, bytes);
-    memcpy(h_out, SU.h->current, bytes);
-    return finish2d(ca, run);
-}

@@ -33,6 +33,14 @@ def cal():
 
 
 @pytest.fixture(scope="module")
+def probes():
+    """The test-only probe library (tests/native/probes.cu)."""
+    import probes as P
+    P.lib()
+    return P
+
+
+@pytest.fixture(scope="module")
 def orc():
     import oracle
     oracle.build()
@@ -190,16 +198,36 @@ def test_life_bits_rejects_other_states(cal):
 
 @pytest.mark.parametrize("nbhd", [1, 2, 3, 4])
 @pytest.mark.parametrize("tor", [0, 1])
-def test_neighbourhoods_bit_exact(cal, orc, nbhd, tor):
+def test_neighbourhoods_bit_exact(probes, orc, nbhd, tor):
     v = W.random_field((41, 37), seed=9)
-    assert_same(cal.nbprobe2d(v, 6, nbhd=nbhd, toroidal=tor), orc.nbprobe2d(v, 6, nbhd=nbhd, toroidal=tor), "v")
+    assert_same(probes.nbprobe2d(v, 6, nbhd=nbhd, toroidal=tor), orc.nbprobe2d(v, 6, nbhd=nbhd, toroidal=tor), "v")
+
+
+CUSTOM_NEIGHBOURHOODS = [
+    [(0, 0), (-1, 0), (0, 2), (2, -1), (1, 1)],
+    [(0, 0), (-2, -2), (-2, 2), (2, -2), (2, 2), (0, -3), (3, 0)],
+    [(1, 0), (0, 0), (0, -1)],
+]
+
+
+@pytest.mark.parametrize("idx", range(len(CUSTOM_NEIGHBOURHOODS)))
+@pytest.mark.parametrize("tor", [0, 1])
+@pytest.mark.parametrize("graph", [False, True])
+def test_custom_neighbourhood_bit_exact(probes, orc, idx, tor, graph):
+    """calAddNeighbor2D (OpenCAL-OMP/source/cal2D.c:444-466) on a custom
+    model: offsets up to three cells away, and a table whose entry 0 is not
+    the cell itself; flat grids read 0 outside (the oracle's rule)."""
+    v = W.random_field((45, 38), seed=20 + idx)
+    offs = CUSTOM_NEIGHBOURHOODS[idx]
+    assert_same(probes.nbprobe2d_custom(v, 6, offs, toroidal=tor, graph=graph),
+                orc.nbprobe2d_custom(v, 6, offs, toroidal=tor), "v")
 
 
 @pytest.mark.parametrize("nbhd", [1, 2, 3, 4])
 @pytest.mark.parametrize("tor", [0, 1])
-def test_active_cells_2d_bit_exact(cal, orc, nbhd, tor):
+def test_active_cells_2d_bit_exact(probes, orc, nbhd, tor):
     v = W.sparse_blobs((64, 52), seed=4, margin=8)
-    a = cal.acprobe(v, 25, nbhd=nbhd, toroidal=tor)
+    a = probes.acprobe(v, 25, nbhd=nbhd, toroidal=tor)
     b = orc.acprobe(v, 25, nbhd=nbhd, toroidal=tor)
     assert_same(a[0], b[0], "v")
     assert_same(a[1], b[1], "active cells")
@@ -207,9 +235,9 @@ def test_active_cells_2d_bit_exact(cal, orc, nbhd, tor):
 
 @pytest.mark.parametrize("nbhd", [1, 2])
 @pytest.mark.parametrize("tor", [0, 1])
-def test_active_cells_3d_bit_exact(cal, orc, nbhd, tor):
+def test_active_cells_3d_bit_exact(probes, orc, nbhd, tor):
     v = W.sparse_blobs((14, 18, 20), seed=6, radius=2.5, margin=4)
-    a = cal.acprobe(v, 8, nbhd=nbhd, toroidal=tor)
+    a = probes.acprobe(v, 8, nbhd=nbhd, toroidal=tor)
     b = orc.acprobe(v, 8, nbhd=nbhd, toroidal=tor)
     assert_same(a[0], b[0], "v")
     assert_same(a[1], b[1], "active cells")
@@ -230,7 +258,7 @@ def _fixture_cases():
 
 
 @pytest.mark.parametrize("idx", range(len(_fixture_cases())))
-def test_gpu_matches_reference_fixtures(cal, idx):
+def test_gpu_matches_reference_fixtures(cal, probes, idx):
     meta = _fixture_cases()[idx]
     fx = np.load(os.path.join(GOLDEN, "synthetic_cases.npz"))
     kind, kw = meta["kind"], meta["kw"]
@@ -249,9 +277,9 @@ def test_gpu_matches_reference_fixtures(cal, idx):
         out = {"s": cal.life2d(x, kw["steps"], toroidal=kw["toroidal"], as_int=kw["as_int"],
                                mode=0 if kw["as_int"] else cal.MODE_FUSED_BLOCKED)}
     elif kind == "nb":
-        out = {"v": cal.nbprobe2d(x, kw["steps"], nbhd=kw["nbhd"], toroidal=kw["toroidal"])}
+        out = {"v": probes.nbprobe2d(x, kw["steps"], nbhd=kw["nbhd"], toroidal=kw["toroidal"])}
     elif kind in ("acp2", "acp3"):
-        v, cells = cal.acprobe(x, kw["steps"], nbhd=kw["nbhd"], toroidal=kw["toroidal"])
+        v, cells = probes.acprobe(x, kw["steps"], nbhd=kw["nbhd"], toroidal=kw["toroidal"])
         out = {"v": v, "cells": cells}
     else:
         out = {"s": cal.life3d(x, kw["steps"], toroidal=kw["toroidal"])}

@@ -89,13 +89,10 @@ def test_oracle_serial_equals_openmp(oracle_lib):
         assert bits_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("OPENCAL_REFERENCE", "/root/reference"),
-                                                   "OpenCAL-OMP")), reason="reference tree absent")
 @pytest.mark.parametrize("seed", [31, 32])
-def test_oracle_vs_live_reference(oracle_lib, seed):
-    import oracle
+def test_oracle_vs_live_reference(reference_oracle, seed):
+    oracle = reference_oracle
     from opencal_gb300 import workloads as W
-    oracle.build(ref=True)
     z, h = W.sciddicaT_inputs(200, 176, seed=seed)
     for tor in (0, 1):
         for ac in (0, 1):
@@ -109,6 +106,58 @@ def test_oracle_vs_live_reference(oracle_lib, seed):
     v = W.random_field((30, 26), seed=seed)
     for nb in (1, 2, 3, 4):
         assert bits_equal(oracle.nbprobe2d(v, 4, nbhd=nb), oracle.nbprobe2d(v, 4, nbhd=nb, kind="ref"))
+
+
+CUSTOM_NEIGHBOURHOODS = [
+    [(0, 0), (-1, 0), (0, 2), (2, -1), (1, 1)],
+    [(0, 0), (-2, -2), (-2, 2), (2, -2), (2, 2), (0, -3), (3, 0)],
+    [(1, 0), (0, 0), (0, -1)],  # the cell itself need not come first
+]
+
+
+@pytest.mark.parametrize("idx", range(len(CUSTOM_NEIGHBOURHOODS)))
+def test_oracle_custom_neighbourhood_vs_live_reference(reference_oracle, idx):
+    """calAddNeighbor2D on a CAL_CUSTOM_NEIGHBORHOOD_2D model (OpenCAL-OMP/
+    source/cal2D.c:444-466), toroidal (the reference's flat reads outside the
+    grid are unchecked)."""
+    oracle = reference_oracle
+    from opencal_gb300 import workloads as W
+    v = W.random_field((23, 29), seed=40 + idx)
+    offs = CUSTOM_NEIGHBOURHOODS[idx]
+    a = oracle.nbprobe2d_custom(v, 5, offs, toroidal=True)
+    b = oracle.nbprobe2d_custom(v, 5, offs, toroidal=True, kind="ref")
+    assert bits_equal(a, b)
+
+
+def _reduction_data(kind, op, rows, cols, seed):
+    from opencal_gb300.workloads import uniform_array
+    u = uniform_array(seed, (rows, cols))
+    if kind == 0:
+        d = (u * 7).astype(np.int8) + 1
+        if op == 4:
+            d = np.where(u < 0.5, 1, 3).astype(np.int8)
+    elif kind == 1:
+        d = (u * 1000 - 300).astype(np.int32)
+        if op == 4:
+            d = np.where(u < 0.5, 1, 3).astype(np.int32)
+    else:
+        d = u * 10.0 - 2.0
+        if op == 4:
+            d = 1.0 + (u - 0.5) * 1e-3
+    return np.ascontiguousarray(d)
+
+
+@pytest.mark.parametrize("op", range(1, 11))
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_oracle_reduction_vs_live_reference(reference_oracle, kind, op):
+    """The reference's serial calReductionOperation2D* folds elements
+    0 .. rows-1 (cal2DReduction.c:45-47); on a one-column grid that is every
+    cell, and the oracle (which folds every cell) must give its bits."""
+    oracle = reference_oracle
+    d = _reduction_data(kind, op, 173, 1, 300 + op + 10 * kind)
+    a = oracle.reduce2d(kind, d, op)
+    b = oracle.reduce2d(kind, d, op, kind="ref")
+    assert bits_equal(np.float64(a), np.float64(b)), (a, b)
 
 
 def _sciara_cases():

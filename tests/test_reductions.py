@@ -1,7 +1,15 @@
-"""Device reductions (cal2DReduction.h) against a direct fold of the same
-values: exact for byte/int and for min/max, logical and binary operations;
-real sums and products within 1e-12 relative (fixed tree order)."""
-import ctypes as C
+"""Device reductions (cal2DReduction.h) against the oracle's fold
+(oracle/cal_oracle.c, orc_reduce2d: the serial calReductionOperation2D* of
+OpenCAL-OMP/source/cal2DReduction.c over every cell, pinned to the reference
+itself on one-column grids in tests/test_oracle_pins.py) and against a
+direct fold of the same values: exact for byte/int and for min/max, logical
+and binary operations; real sums and products within 1e-12 relative (the
+device folds in a fixed tree order, the oracle in index order).
+
+Which semantics: the reference's serial build folds elements 0 .. rows-1
+only (the last thread's end index is `rows`, cal2DReduction.c:45-47) and its
+OpenMP build drops the last thread's share the same way; this library folds
+every cell, as the oracle does."""
 import operator
 from functools import reduce
 
@@ -42,10 +50,12 @@ def fold(values, op, kind):
 @pytest.fixture(scope="module")
 def lib():
     import opencal_gb300 as cal
+    import oracle
+    import probes
     cal.build()
-    m = cal.models()
-    m.cal_reduce2d_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_double)]
-    return m
+    oracle.build()
+    probes.lib()
+    return probes, oracle
 
 
 @pytest.mark.parametrize("op", list(OPS))
@@ -66,13 +76,15 @@ def test_reduction(lib, kind, op):
         data = np.ascontiguousarray(u * 10.0 - 2.0)
         if op == 4:
             data[:] = 1.0 + (u - 0.5) * 1e-3
-    out = C.c_double(0)
-    assert lib.cal_reduce2d_run(kind, rows, cols, data.ctypes.data, op, C.byref(out)) == 0
+    probes, oracle = lib
+    got = probes.reduce2d(kind, data, op)
     want = fold(data, op, kind)
+    orc = oracle.reduce2d(kind, data, op)
     if kind == 2 and OPS[op] in ("sum", "prod"):
-        assert abs(out.value - want) <= 1e-12 * abs(want)
+        assert abs(got - want) <= 1e-12 * abs(want)
+        assert abs(got - orc) <= 1e-12 * abs(orc)
     elif kind == 0 and OPS[op] in ("sum", "prod"):
         # CALbyte is char: its signedness is the platform's, compare modulo 256
-        assert int(out.value) % 256 == want % 256
+        assert int(got) % 256 == want % 256 == int(orc) % 256
     else:
-        assert out.value == want, (OPS[op], out.value, want)
+        assert got == want == orc, (OPS[op], got, want, orc)

@@ -13,7 +13,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 CAL_MOORE, CAL_TOROIDAL, CAL_OPT_ACTIVE_CELLS = 2, 1, 1
-CAL_ERROR_LIMIT = 5
+CAL_ERROR_INVALID_ARGUMENT, CAL_ERROR_LIMIT = 1, 5
 
 
 class CALActiveCells2D(C.Structure):
@@ -63,22 +63,38 @@ def _reference_list(L, ca):
     return np.ctypeslib.as_array(ca.contents.A.cells, shape=(n * 2,)).reshape(n, 2).copy()
 
 
-def _no_alloc_list(L, ca, rows, cols):
+def _no_alloc_list(L, ca, rows, cols, stream=None, flag_offset=0):
+    """The no-allocation entry point on the model's flags (copied to an
+    address `flag_offset` bytes past an allocation when that is non-zero),
+    on the model's stream or on a caller's torch stream."""
     import torch
     flags = C.c_void_p()
     L.calGetDeviceActiveCells2D(ca, C.byref(flags), None, None)
+    L.calFinish2D(ca)
+    flag_ptr = flags.value
+    if flag_offset:
+        shifted = torch.zeros(rows * cols + flag_offset, dtype=torch.uint8, device="cuda")
+        src = torch.as_tensor(_DeviceArray(flags.value, (rows * cols,), "|u1"), device="cuda")
+        shifted[flag_offset:].copy_(src)
+        flag_ptr = shifted.data_ptr() + flag_offset
     cells = torch.full((rows * cols, 2), -1, dtype=torch.int32, device="cuda")
     linear = torch.full((rows * cols,), -1, dtype=torch.int32, device="cuda")
     count = torch.full((1,), -1, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
-    rc = L.calCompactActiveCellsNoAlloc2D(flags, rows, cols, cells.data_ptr(), linear.data_ptr(), count.data_ptr(),
-                                          L.calGetStream2D(ca))
+    st = stream.cuda_stream if stream is not None else L.calGetStream2D(ca)
+    rc = L.calCompactActiveCellsNoAlloc2D(flag_ptr, rows, cols, cells.data_ptr(), linear.data_ptr(),
+                                          count.data_ptr(), st)
     assert rc == 0
+    if stream is not None:
+        stream.synchronize()
     L.calFinish2D(ca)
     n = int(count.cpu()[0])
     got = cells[:n].cpu().numpy()
     lin = linear[:n].cpu().numpy()
     assert np.array_equal(lin, got[:, 0] * cols + got[:, 1])
+    if n < rows * cols:
+        # nothing written past the list
+        assert (cells[n:].cpu().numpy() == -1).all() and (linear[n:].cpu().numpy() == -1).all()
     return got
 
 
@@ -122,5 +138,50 @@ def test_no_alloc_rejects_grids_beyond_its_limit(lib):
         L.calGetDeviceActiveCells2D(ca, C.byref(flags), C.byref(cells), C.byref(count))
         rc = L.calCompactActiveCellsNoAlloc2D(flags, 20000, 20000, cells, cells, count, None)
         assert rc == CAL_ERROR_LIMIT
+    finally:
+        L.calFinalize2D(ca)
+
+
+def test_no_alloc_empty_set_caller_stream_and_unaligned_flags(lib):
+    """An empty flag set gives count 0 and writes nothing; the call runs on a
+    stream the caller created; flags at an odd address give the same list."""
+    import torch
+    L = lib
+    rows, cols = 301, 255
+    ca = L.calCADef2D(rows, cols, CAL_MOORE, CAL_TOROIDAL, CAL_OPT_ACTIVE_CELLS)
+    assert ca
+    try:
+        assert len(_reference_list(L, ca)) == 0
+        assert len(_no_alloc_list(L, ca, rows, cols)) == 0
+        for i, j in _random_cells(rows, cols, 0.07, 8):
+            L.calAddActiveCell2D(ca, int(i), int(j))
+        ref = _reference_list(L, ca)
+        assert len(ref) > 0
+        stream = torch.cuda.Stream()
+        assert np.array_equal(_no_alloc_list(L, ca, rows, cols, stream=stream), ref)
+        for off in (1, 3, 8):
+            assert np.array_equal(_no_alloc_list(L, ca, rows, cols, flag_offset=off), ref)
+    finally:
+        L.calFinalize2D(ca)
+
+
+def test_no_alloc_rejects_misaligned_outputs(lib):
+    """cells, linear and count must be 4-byte aligned: an offset pointer is
+    refused with CAL_ERROR_INVALID_ARGUMENT before anything is launched."""
+    import torch
+    L = lib
+    rows, cols = 64, 64
+    ca = L.calCADef2D(rows, cols, CAL_MOORE, CAL_TOROIDAL, CAL_OPT_ACTIVE_CELLS)
+    try:
+        flags = C.c_void_p()
+        L.calGetDeviceActiveCells2D(ca, C.byref(flags), None, None)
+        buf = torch.zeros(4 * rows * cols + 64, dtype=torch.int32, device="cuda")
+        base = buf.data_ptr()
+        cells, linear, count = base, base + 8 * rows * cols, base + 12 * rows * cols
+        for bad in ((cells + 2, linear, count), (cells, linear + 1, count), (cells, linear, count + 3)):
+            rc = L.calCompactActiveCellsNoAlloc2D(flags, rows, cols, bad[0], bad[1], bad[2], None)
+            assert rc == CAL_ERROR_INVALID_ARGUMENT
+        torch.cuda.synchronize()
+        assert int(buf.abs().sum().item()) == 0  # nothing was written
     finally:
         L.calFinalize2D(ca)
