@@ -445,11 +445,56 @@ def gpu_arm(args):
                      "events; the kernel's FP64 work is adds and multiplies, no FMA)"}
     if not args.no_ac:
         line["active_cells_on"] = active_cells_section(m, cal, z, h, hh)
+    if not args.no_processes:
+        line["processes_plain"] = processes_plain_section(m, cal, z, h, hh)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(z, h)
     if not args.no_calibration:
         line["calibration"] = calibration_section(args)
     print(json.dumps(line), flush=True)
+
+
+def processes_plain_section(m, cal, z, h, h_plain):
+    """The same plain workload through the generic engine: the reference
+    program's two elementary processes (device processes registered with
+    calAddElementaryProcess2D) and its steering, run by calRunCAStep2D
+    (eager: a launch sequence per step; graph: the recorded step replayed) or
+    calRunDeviceSteps2D (one device-driven graph launch for the loop).  The
+    engine updates and fills only the tiles a process changed (change
+    tracking).  Must give the split step's bits."""
+    import torch
+    sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_PROCESSES)
+    if not sess:
+        return {"error": "cal_sciddicaT_open (processes) failed: " + cal.core().calGetErrorString().decode()}
+    stream = torch.cuda.ExternalStream(m.cal_sciddicaT_stream(sess))
+    forms, same = {}, True
+    for name, loop in (("eager", 0), ("graph", 1), ("device", 2)):
+        ms = []
+        for it in range(3):
+            m.cal_sciddicaT_reset(sess)
+            with torch.cuda.stream(stream):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                rc = m.cal_sciddicaT_steps(sess, CA_STEPS, loop)
+                e1.record(stream)
+            e1.synchronize()
+            if rc:
+                m.cal_sciddicaT_close(sess)
+                return {"error": f"cal_sciddicaT_steps (processes, {name}) failed: {rc}"}
+            if it:
+                ms.append(e0.elapsed_time(e1))
+        hp = np.empty_like(h)
+        m.cal_sciddicaT_read(sess, hp.ctypes.data)
+        same = same and hp.tobytes() == h_plain.tobytes()
+        forms[name] = float(np.mean(ms))
+    m.cal_sciddicaT_close(sess)
+    best = min(forms, key=forms.get)
+    return {"workload": f"SCIDDICA-T {ROWS}x{COLS} FP64, flat, plain, {CA_STEPS} CA steps, the reference "
+                        "program's device processes + steering through the run loop",
+            "ms_per_run": forms, "best": best,
+            "value": ROWS * COLS * CA_STEPS / (forms[best] * 1e-3), "unit": "cell-updates/s",
+            "identical_to_split_step": bool(same)}
 
 
 def active_cells_section(m, cal, z, h, h_plain):
@@ -959,6 +1004,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--loop", default="persistent", choices=sorted(LOOPS))
     ap.add_argument("--no-ac", action="store_true", help="skip the active-cells-on run of the workload")
+    ap.add_argument("--no-processes", action="store_true", help="skip the generic-engine (device processes) figure")
     ap.add_argument("--no-calibration", action="store_true", help="skip the batched-calibration section")
     ap.add_argument("--calib-iters", type=int, default=12)
     ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble", "activecells"],

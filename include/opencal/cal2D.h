@@ -146,16 +146,17 @@ void calFinalize2D(struct CALModel2D* ca2D);                                    
 /* Bring every host mirror up to date with the device: substate layers,
  * A.flags, A.cells, A.size_current.  Synchronises the model's stream. */
 void calSync2D(struct CALModel2D* ca2D);
-/* A caller's array (rows*columns elements, the buffer layout) becomes
- * both layers of a substate on the device -- what calLoadSubstate2D* does
- * with a file -- without passing through the host mirrors; the mirrors
- * become stale.  From pinned host memory the copy runs asynchronously on
- * the model's stream: keep the array unchanged until the next
- * synchronising call. */
+/* A caller's array (rows*columns elements, the buffer layout; host or
+ * device memory) becomes both layers of a substate on the device -- what
+ * calLoadSubstate2D* does with a file -- without passing through the host
+ * mirrors; the mirrors become stale.  From pinned host memory or device
+ * memory the copy runs asynchronously on the model's stream: keep the array
+ * unchanged until the next synchronising call. */
 void calCopySubstateFromHost2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, const CALbyte* data);
 void calCopySubstateFromHost2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, const CALint* data);
 void calCopySubstateFromHost2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, const CALreal* data);
-/* The current layer of a substate into a caller's array (synchronises). */
+/* The current layer of a substate into a caller's array (host or device
+ * memory; synchronises). */
 void calCopySubstateToHost2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q, CALbyte* data);
 void calCopySubstateToHost2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q, CALint* data);
 void calCopySubstateToHost2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q, CALreal* data);

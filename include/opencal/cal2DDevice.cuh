@@ -56,13 +56,41 @@ struct CALDevModel2D {
     int nx;
     int xi[CAL_MAX_NEIGHBORS];
     int xj[CAL_MAX_NEIGHBORS];
+    /* change tracking (models without active cells): the grid is cut into
+     * CAL_TILE_W x CAL_TILE_H tiles; a process that stores into next a value
+     * whose bits differ from current sets the tile's bit in chg (one bitmap
+     * of tile_words words per substate slot, index type * CAL_MAX_SUBSTATES
+     * + slot), so that the update copies only those tiles; writes the tile
+     * bitmaps cannot follow (unsafe operations) set the substate's bit in
+     * untracked[type] and the update copies all of it */
+    int track;
+    int tiles_x, tiles_y, tile_words;
+    unsigned int* chg;
+    unsigned int* untracked;
 };
+
 
 #if defined(__CUDACC__)
 
 /* per-block record of which substates a process wrote (plain byte stores:
  * every writer stores 1, so concurrent writers cannot lose an update) */
 static __shared__ unsigned char cal_written2D[3 * CAL_MAX_SUBSTATES];
+/* per warp: substates whose next layer this warp changed in the current
+ * tile (flushed into the chg bitmaps after each tile row), and per block:
+ * substates written by unsafe operations */
+static __shared__ unsigned char cal_chg2D[CAL_EP_THREADS / 32][3 * CAL_MAX_SUBSTATES];
+static __shared__ unsigned char cal_untracked2D[3 * CAL_MAX_SUBSTATES];
+
+template <typename T>
+static __device__ __forceinline__ bool cal_same_bits(T a, T b)
+{
+    return a == b;
+}
+template <>
+__device__ __forceinline__ bool cal_same_bits<double>(double a, double b)
+{
+    return __double_as_longlong(a) == __double_as_longlong(b);
+}
 
 static __device__ __forceinline__ const struct CALDevModel2D* cal_dm2D(const struct CALModel2D* ca)
 {
@@ -111,13 +139,24 @@ static __device__ __forceinline__ T cal_getx2D(const struct CALModel2D* ca, int 
     return static_cast<const T*>(m->cur[t][cal_slot2D(m, t, q)])[cal_lin2D(m, a, b)];
 }
 
+/* the tile of a tracked process changed substate (t, s): flagged for the
+ * calling warp (a process writes only its own cell, which lies in the
+ * block's current tile) */
+static __device__ __forceinline__ void cal_mark_chg2D(int t, int s)
+{
+    cal_chg2D[threadIdx.x >> 5][t * CAL_MAX_SUBSTATES + s] = 1;
+}
+
 template <typename T>
 static __device__ __forceinline__ void cal_set2D(const struct CALModel2D* ca, int t, const void* q, int i, int j, T v)
 {
     const struct CALDevModel2D* m = cal_dm2D(ca);
     int s = cal_slot2D(m, t, q);
-    static_cast<T*>(m->nxt[t][s])[cal_lin2D(m, i, j)] = v;
+    const long long c = cal_lin2D(m, i, j);
+    static_cast<T*>(m->nxt[t][s])[c] = v;
     cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
+    if (m->track && !cal_same_bits(static_cast<const T*>(m->cur[t][s])[c], v))
+        cal_mark_chg2D(t, s);
 }
 
 template <typename T>
@@ -128,6 +167,8 @@ static __device__ __forceinline__ void cal_setcur2D(const struct CALModel2D* ca,
     static_cast<T*>(m->cur[t][s])[cal_lin2D(m, i, j)] = v;
     /* the next update copies next over it, as in the reference */
     cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
+    if (m->track)
+        cal_mark_chg2D(t, s);
 }
 
 template <typename T>
@@ -140,6 +181,8 @@ static __device__ __forceinline__ void cal_init2D(const struct CALModel2D* ca, i
     if (m->nxt[t][s])
         static_cast<T*>(m->nxt[t][s])[c] = v;
     cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
+    if (m->track)
+        cal_mark_chg2D(t, s); /* the tile no longer holds the substate's uniform value */
 }
 
 static __device__ __forceinline__ void cal_addactive2D(const struct CALModel2D* ca, int i, int j)
@@ -180,31 +223,57 @@ static __device__ __forceinline__ int calGetActiveCellCountDevice2D(const struct
 
 /* One elementary process over every cell, or over the active list when the
  * optimisation is on and the list is non-empty (cal2D.c:717-734).  The grid
- * is sized by the host to a few waves of the GPU; both loops are grid-stride.
- * At the end each block publishes which substates it wrote. */
+ * is sized by the host to a few waves of the GPU; both loops are
+ * grid-stride.  Without the list the blocks take CAL_TILE_W x CAL_TILE_H
+ * tiles (one cell per thread, a warp per tile row); with change tracking
+ * each warp then adds its tile to the chg bitmap of every substate whose
+ * next layer it changed.  At the end each block publishes which substates
+ * it wrote (and which it wrote by unsafe operations). */
 template <void (*EP)(struct CALModel2D*, int, int)>
 __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_constant__ struct CALDevModel2D m)
 {
-    for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x) {
         cal_written2D[t] = 0;
+        cal_untracked2D[t] = 0;
+    }
+    for (int t = lane; t < 3 * CAL_MAX_SUBSTATES; t += 32)
+        cal_chg2D[warp][t] = 0;
     __syncthreads();
     struct CALModel2D* ca = const_cast<struct CALModel2D*>(&m.model);
     const int listed = m.use_list ? *m.count : 0;
+    const int nblocks = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
     if (listed > 0) {
-        const int stride = gridDim.x * gridDim.y * blockDim.x;
-        for (int n = (blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; n < listed; n += stride) {
+        const int stride = nblocks * blockDim.x;
+        for (int n = bid * blockDim.x + threadIdx.x; n < listed; n += stride) {
             const struct CALCell2D c = m.cells[n];
             EP(ca, c.i, c.j);
         }
     } else {
-        for (int i = blockIdx.y; i < m.rows; i += gridDim.y)
-            for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m.cols; j += gridDim.x * blockDim.x)
+        const int ntiles = m.tiles_x * m.tiles_y;
+        for (int tile = bid; tile < ntiles; tile += nblocks) {
+            const int ty = tile / m.tiles_x;
+            const int i = ty * CAL_TILE_H + warp, j = (tile - ty * m.tiles_x) * CAL_TILE_W + lane;
+            if (i < m.rows && j < m.cols)
                 EP(ca, i, j);
+            if (m.track) {
+                __syncwarp();
+                for (int t = lane; t < 3 * CAL_MAX_SUBSTATES; t += 32)
+                    if (cal_chg2D[warp][t]) {
+                        cal_chg2D[warp][t] = 0;
+                        atomicOr(&m.chg[(long long)t * m.tile_words + (tile >> 5)], 1u << (tile & 31));
+                    }
+                __syncwarp();
+            }
+        }
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x)
+    for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x) {
         if (cal_written2D[t])
             atomicOr(&m.dirty[t / CAL_MAX_SUBSTATES], 1u << (t % CAL_MAX_SUBSTATES));
+        if (cal_untracked2D[t] && m.untracked)
+            atomicOr(&m.untracked[t / CAL_MAX_SUBSTATES], 1u << (t % CAL_MAX_SUBSTATES));
+    }
 }
 
 template <void (*EP)(struct CALModel2D*, int, int)>

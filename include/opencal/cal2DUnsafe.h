@@ -110,6 +110,7 @@ static __device__ __forceinline__ void cal_storex2D(const struct CALModel2D* ca,
     if (WHICH != 1)
         static_cast<T*>(m->cur[t][s])[c] = v;
     cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
+    cal_untracked2D[t * CAL_MAX_SUBSTATES + s] = 1; /* another cell's tile: the update copies the whole substate */
 }
 
 template <typename T>
@@ -119,6 +120,7 @@ static __device__ __forceinline__ void cal_addnext2D(const struct CALModel2D* ca
     const int s = cal_slot2D(m, t, q);
     cal_atomic_add(static_cast<T*>(m->nxt[t][s]) + cal_lin2D(m, i, j), v);
     cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
+    cal_untracked2D[t * CAL_MAX_SUBSTATES + s] = 1; /* other threads add into the same cell */
 }
 
 template <typename T>
@@ -132,6 +134,7 @@ static __device__ __forceinline__ void cal_addnextx2D(const struct CALModel2D* c
     const int s = cal_slot2D(m, t, q);
     cal_atomic_add(static_cast<T*>(m->nxt[t][s]) + cal_lin2D(m, a, b), v);
     cal_written2D[t * CAL_MAX_SUBSTATES + s] = 1;
+    cal_untracked2D[t * CAL_MAX_SUBSTATES + s] = 1; /* another cell's tile */
 }
 
 #ifndef CAL_BUILDING_LIBRARY

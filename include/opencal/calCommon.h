@@ -81,6 +81,12 @@ struct CALSubstate3Di { CALint* current; CALint* next; CAL_SUBSTATE_RESERVED; };
 struct CALSubstate3Dr { CALreal* current; CALreal* next; CAL_SUBSTATE_RESERVED; };
 
 /* calCommon.h:193: final_step value that turns the run into a loop */
+/* Tiles of the 2D process kernels (library internals, shared by the device
+ * header and the engine): CAL_TILE_W columns (one warp per tile row) by
+ * CAL_TILE_H rows, one cell per thread of a 256-thread block. */
+#define CAL_TILE_W 32
+#define CAL_TILE_H 8
+
 #define CAL_RUN_LOOP 0
 
 /* calCommon.h:201-213 */

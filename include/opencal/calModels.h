@@ -32,6 +32,11 @@ extern "C" {
 int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int steps, double p_r, double p_eps, const double* z0,
                       const double* h0, double* z_out, double* h_out, long* n_active, int* cells_out, int mode,
                       int graph, double* ms);
+/* the reference example's main() as written: z and h loaded from text files
+ * (calLoadSubstate2Dr), the run (calRun2D; graph 1 replays the recorded
+ * step), h saved with calSaveSubstate2Dr to output_path */
+int cal_sciddicaT_run_files(int rows, int cols, int toroidal, int steps, double p_r, double p_eps,
+                            const char* dem_path, const char* source_path, const char* output_path, int graph);
 /* how many device-loop runs fell back to a launch sequence per step */
 int cal_sciddicaT_device_loop_fallbacks(void);
 
@@ -104,6 +109,26 @@ int cal_sciara_run(int rows, int cols, int ac, int max_steps, const double* para
                    unsigned emission_time, int nphases, const double* rates, const double* z0, const double* slt0,
                    const double* st0, double* z_out, double* slt_out, double* st_out, double* msl_out,
                    int* steps_done, long* n_active, int* cells_out, int graph, double* ms);
+
+/* form of the transcendental parts for the following cal_sciara_run calls:
+ * 0 (default) identities suited to the FP64 pipe (exp10, the shear test
+ * without atan / cos, T*T*T, cbrt); 1 pow, atan and cos written as the
+ * reference writes them (Sciara.cpp:18-21, 61, 85, 147-150) */
+int cal_sciara_set_math(int form);
+
+/* The reference example's input files (OpenCAL-OMP/examples/calomp_sciara-fv2/
+ * source/io.cpp:357-404): `path` names the .cfg (or the prefix to which
+ * "_000000000000.cfg" is appended); Morphology.stt, Vents.stt and
+ * EmissionRate.txt beside it are required, Thickness / Temperature /
+ * SolidifiedLavaThickness.stt optional.  cal_sciara_read_sizes gives the
+ * sizes to allocate; cal_sciara_read fills params (the 12 .cfg parameters
+ * and Pc, cal_sciara_run's order), z, vent_xy (x, y per vent in the
+ * reference's order), rates (nvents x nphases, shorter lists padded with 0)
+ * and the emission time, and the optional grids where present[k] is set.
+ * Returns CAL_ERROR_IO when a file is missing or malformed. */
+int cal_sciara_read_sizes(const char* path, int* rows, int* cols, int* nvents, int* nphases);
+int cal_sciara_read(const char* path, double* params, double* z, int* vent_xy, double* rates,
+                    unsigned* emission_time, double* slt, double* st, double* msl, int* present);
 
 /* SCIARA-fv2 scenarios by the split step (vents, flows of the lava cells,
  * update of the flagged tiles); one scenario or many in the same launches.

@@ -129,11 +129,13 @@ def life3d(s0, steps, *, nbhd=2, toroidal=True, rule=(5, 7, 6, 6), graph=False):
 
 
 def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt0=None, st0=None, graph=False,
-           timing=False):
+           timing=False, libm=False):
     """SCIARA-fv2 on the GPU (csrc/models/sciara.cu): the reference program's
     elementary processes as device processes behind the C API.  Same
     arguments and result as oracle.sciara (dict z, slt, st, msl, steps,
-    cells), plus the device milliseconds of the step loop with timing=True."""
+    cells), plus the device milliseconds of the step loop with timing=True.
+    libm=True evaluates pow / atan / cos as the reference writes them
+    instead of the identity forms."""
     from .workloads import SCIARA_PARAMS
     z0 = np.ascontiguousarray(z0, dtype=np.float64)
     rows, cols = z0.shape
@@ -147,6 +149,8 @@ def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt
     ms = C.c_double(0.0)
     cells = np.zeros((rows * cols if ac else 1, 2), dtype=np.int32)
     m = models()
+    m.cal_sciara_set_math.argtypes = [C.c_int]
+    _check(m.cal_sciara_set_math(1 if libm else 0), "cal_sciara_set_math")
     f = m.cal_sciara_run
     f.restype = C.c_int
     f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_uint, C.c_int, C.c_void_p,
@@ -165,6 +169,37 @@ def sciara(z0, vents, rates, emission_time, steps, *, ac=False, params=None, slt
     if timing:
         outs["ms"] = ms.value
     return outs
+
+
+def sciara_read(path):
+    """A SCIARA-fv2 configuration in the reference example's files (.cfg,
+    Morphology.stt, Vents.stt, EmissionRate.txt, optional Thickness /
+    Temperature / SolidifiedLavaThickness.stt) as
+    dict(params, z, vents, rates, emission_time, slt0, st0, msl0), ready for
+    ``sciara``."""
+    m = models()
+    rows, cols, nv, nph = (C.c_int() for _ in range(4))
+    f = m.cal_sciara_read_sizes
+    f.restype = C.c_int
+    f.argtypes = [C.c_char_p] + [C.POINTER(C.c_int)] * 4
+    _check(f(str(path).encode(), C.byref(rows), C.byref(cols), C.byref(nv), C.byref(nph)), "cal_sciara_read_sizes")
+    params = np.zeros(13)
+    z = np.zeros((rows.value, cols.value))
+    vent_xy = np.zeros((max(nv.value, 1), 2), dtype=np.int32)
+    rates = np.zeros((max(nv.value, 1), max(nph.value, 1)))
+    grids = [np.zeros_like(z) for _ in range(3)]
+    present = (C.c_int * 3)()
+    et = C.c_uint(0)
+    g = m.cal_sciara_read
+    g.restype = C.c_int
+    g.argtypes = [C.c_char_p] + [C.c_void_p] * 4 + [C.POINTER(C.c_uint)] + [C.c_void_p] * 4
+    _check(g(str(path).encode(), params.ctypes.data, z.ctypes.data, vent_xy.ctypes.data, rates.ctypes.data,
+             C.byref(et), grids[0].ctypes.data, grids[1].ctypes.data, grids[2].ctypes.data, present),
+           "cal_sciara_read")
+    return {"params": params, "z": z, "vents": [tuple(v) for v in vent_xy[: nv.value]],
+            "rates": rates[: nv.value, : nph.value].tolist(), "emission_time": et.value,
+            "slt0": grids[0] if present[0] else None, "st0": grids[1] if present[1] else None,
+            "msl0": grids[2] if present[2] else None}
 
 
 def sciddicaT_unsafe(z0, h0, steps, *, toroidal=True, p_r=0.5, p_eps=0.001, graph=False):

@@ -157,6 +157,14 @@ static bool build_desc(struct CALModel2D* ca, CALDevModel2D* d)
         d->xi[n] = ca->X[n].i;
         d->xj[n] = ca->X[n].j;
     }
+    /* process tiles (every launch) and change tracking (models without
+     * active cells) */
+    d->tiles_x = (ca->columns + CAL_TILE_W - 1) / CAL_TILE_W;
+    d->tiles_y = (ca->rows + CAL_TILE_H - 1) / CAL_TILE_H;
+    d->track = g.tracking ? 1 : 0;
+    d->tile_words = g.tile_words;
+    d->chg = g.d_chg;
+    d->untracked = g.d_untracked;
     return true;
 }
 
@@ -362,9 +370,7 @@ extern "C" void calUpdateActiveCells2D(struct CALModel2D* ca)
 #define CAL_SUBSTATE_OPS_2D(S, T, TC)                                                                   \
     extern "C" void calInitSubstate2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, T value)    \
     {                                                                                                   \
-        int s = slot_of(ca, TC, Q);                                                                     \
-        if (G(ca).fill(TC, s, 0, &value, true))                                                         \
-            G(ca).fill(TC, s, 1, &value, true);                                                         \
+        G(ca).fill_both(TC, slot_of(ca, TC, Q), &value);                                                \
     }                                                                                                   \
     extern "C" void calInitSubstateNext2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q, T value) \
     {                                                                                                   \
@@ -386,6 +392,7 @@ extern "C" void calUpdateActiveCells2D(struct CALModel2D* ca)
             return nullptr;                                                                             \
         if (layer == 1 && !g.repair_stale(TC, s))                                                       \
             return nullptr;                                                                             \
+        g.untrack(TC, s); /* the caller may write it: no change tracking from now on */                \
         return g.sub[TC][s].layer[layer ? 1 : 0].dev;  /* layer 2: next, to be overwritten whole */     \
     }                                                                                                   \
     extern "C" void calCopySubstateFromHost2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q,      \
@@ -404,6 +411,7 @@ extern "C" void calUpdateActiveCells2D(struct CALModel2D* ca)
     extern "C" void calMarkCurrentWritten2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q)       \
     {                                                                                                   \
         G(ca).sub[TC][slot_of(ca, TC, Q)].layer[0].host_valid = false;                                  \
+        G(ca).untrack(TC, slot_of(ca, TC, Q));                                                          \
     }                                                                                                   \
     extern "C" void calSwapSubstate2D##S(struct CALModel2D* ca, struct CALSubstate2D##S* Q)             \
     {                                                                                                   \
@@ -562,7 +570,11 @@ extern "C" void calMarkHostDirty2D(struct CALModel2D* ca)
 
 extern "C" void calMarkDeviceWritten2D(struct CALModel2D* ca)
 {
-    G(ca).device_wrote_all();
+    CalGrid& g = G(ca);
+    g.device_wrote_all();
+    for (int t = 0; t < CAL_NTYPES; t++)
+        for (int s = 0; s < g.nslot[t]; s++)
+            g.untrack(t, s); /* written outside the library: no change tracking from now on */
 }
 
 extern "C" void calFinish2D(struct CALModel2D* ca)

@@ -26,6 +26,7 @@ struct CALGpuRun2D {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long replays = 0;
+    long rec_epoch = 0; /* the grid's invalidation epoch when the step was recorded */
     CALStopLaunchFunc2D dev_stop = nullptr; /* device stop condition */
     int* d_flag = nullptr;                  /* its decision, for the step-by-step fallback */
     int device_loop_used = 0;
@@ -155,6 +156,7 @@ static bool capture_step(struct CALRun2D* sim)
     }
     gr->graph = graph;
     gr->exec = exec;
+    gr->rec_epoch = g.inval_epoch;
     return cal::cuda_ok(cudaGraphLaunch(exec, g.stream), "graph launch");
 }
 
@@ -164,6 +166,16 @@ extern "C" CALbyte calRunCAStep2D(struct CALRun2D* sim)
     cal::CalGrid& g = G(sim->ca2D);
     bool done = false;
     if (gr && gr->graph_enabled && !gr->graph_failed) {
+        if (gr->exec && gr->rec_epoch != g.inval_epoch) {
+            /* host-side events since the recording (host writes, copies into
+             * a substate, handed-out device pointers) invalidated what it
+             * assumed: record the step again */
+            cudaGraphExecDestroy(gr->exec);
+            gr->exec = nullptr;
+            if (gr->graph)
+                cudaGraphDestroy(gr->graph);
+            gr->graph = nullptr;
+        }
         if (gr->exec) {
             done = cal::cuda_ok(cudaGraphLaunch(gr->exec, g.stream), "graph launch");
             if (done) {

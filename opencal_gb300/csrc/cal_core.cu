@@ -127,6 +127,127 @@ __global__ void k_update(const __grid_constant__ UpdateParams p)
     }
 }
 
+/* ---- change tracking: tile-sparse update and fill ----------------------
+ * A tile is CAL_TILE_W x CAL_TILE_H cells (the process kernels' tiles);
+ * tile index = tile row * tiles_x + tile column; one bit per tile. */
+struct TileGeom {
+    int rows, cols, tiles_x, tile_words, ntiles;
+};
+
+/* the cells of `tile`, one per thread of a 256-thread block */
+static __device__ __forceinline__ bool tile_cell(const TileGeom& g, int tile, long long* c)
+{
+    const int ty = tile / g.tiles_x;
+    const int i = ty * CAL_TILE_H + (int)(threadIdx.x >> 5);
+    const int j = (tile - ty * g.tiles_x) * CAL_TILE_W + (int)(threadIdx.x & 31);
+    *c = (long long)i * g.cols + j;
+    return i < g.rows && j < g.cols;
+}
+
+template <typename T>
+static __device__ __forceinline__ void copy_tile(const TileGeom& g, int tile, const void* src, void* dst)
+{
+    long long c;
+    if (tile_cell(g, tile, &c))
+        static_cast<T*>(dst)[c] = static_cast<const T*>(src)[c];
+}
+
+struct TileUpdateParams {
+    const void* src[CAL_UPDATE_MAX];
+    void* dst[CAL_UPDATE_MAX];
+    unsigned char elem[CAL_UPDATE_MAX];
+    unsigned char type[CAL_UPDATE_MAX];
+    unsigned char slot[CAL_UPDATE_MAX];
+    int n_entries;
+    TileGeom g;
+    const unsigned* dirty;
+    unsigned forced[CAL_NTYPES];
+    int use_dirty;
+    unsigned* chg;
+    unsigned* dev;
+    unsigned* untracked; /* [3] per type, [3] the ticket */
+};
+
+/* next -> current of the tracked substates, tile by tile: the tiles whose
+ * chg bit is set (every tile of a substate written by unsafe operations);
+ * the copied tiles' bits move from chg to dev.  Work items are (entry,
+ * bitmap word), grid-stride; the last block to finish clears the unsafe
+ * marks (a ticket, reset by that block). */
+__global__ void __launch_bounds__(kThreads) k_update_tiles(const __grid_constant__ TileUpdateParams p)
+{
+    __shared__ unsigned s_bits;
+    __shared__ int s_last;
+    const int items = p.n_entries * p.g.tile_words;
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int e = item / p.g.tile_words, w = item - e * p.g.tile_words;
+        const int t = p.type[e], sl = p.slot[e];
+        if (p.use_dirty && !(((p.dirty[t] | p.forced[t]) >> sl) & 1u))
+            continue;
+        const long long row = (long long)(t * CAL_MAX_SUBSTATES_CORE + sl) * p.g.tile_words;
+        if (threadIdx.x == 0) {
+            unsigned b = p.chg[row + w];
+            if ((p.untracked[t] >> sl) & 1u) {
+                const int left = p.g.ntiles - w * 32;
+                b = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
+            }
+            s_bits = b;
+        }
+        __syncthreads();
+        unsigned bits = s_bits;
+        while (bits) {
+            const int tile = w * 32 + __ffs(bits) - 1;
+            bits &= bits - 1;
+            switch (p.elem[e]) {
+            case 8: copy_tile<unsigned long long>(p.g, tile, p.src[e], p.dst[e]); break;
+            case 4: copy_tile<unsigned>(p.g, tile, p.src[e], p.dst[e]); break;
+            default: copy_tile<unsigned char>(p.g, tile, p.src[e], p.dst[e]); break;
+            }
+        }
+        if (threadIdx.x == 0 && s_bits) {
+            p.chg[row + w] = 0;
+            p.dev[row + w] |= s_bits;
+        }
+        __syncthreads(); /* s_bits is reused */
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(p.untracked + 3, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x < 4)
+        p.untracked[threadIdx.x] = 0; /* the unsafe marks (read by every block) and the ticket */
+}
+
+/* both layers of one substate to `value` on the tiles of dev | chg, whose
+ * bits are then cleared (the layers are equal and uniform again) */
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_fill_tiles(TileGeom g, T* l0, T* l1, T value, unsigned* chg,
+                                                          unsigned* dev)
+{
+    __shared__ unsigned s_bits;
+    for (int w = blockIdx.x; w < g.tile_words; w += gridDim.x) {
+        if (threadIdx.x == 0)
+            s_bits = chg[w] | dev[w];
+        __syncthreads();
+        unsigned bits = s_bits;
+        while (bits) {
+            const int tile = w * 32 + __ffs(bits) - 1;
+            bits &= bits - 1;
+            long long c;
+            if (tile_cell(g, tile, &c)) {
+                l0[c] = value;
+                if (l1)
+                    l1[c] = value;
+            }
+        }
+        if (threadIdx.x == 0 && s_bits) {
+            chg[w] = 0;
+            dev[w] = 0;
+        }
+        __syncthreads();
+    }
+}
+
 /* ---- active-cell compaction -------------------------------------------
  * The list order is the reference's:
  *   2D: memory order (row-major);
@@ -352,6 +473,22 @@ bool CalGrid::init(int dim_, int rows_, int cols_, int slices_, int toroidal_, i
     if (!cuda_ok(cudaMalloc(&d_reduce_partial, 512 * sizeof(double) + 64), "cudaMalloc reduction") ||
         !cuda_ok(cudaMalloc(&d_reduce_result, 64), "cudaMalloc reduction result"))
         return false;
+    /* change tracking for 2D models without active cells (every substate
+     * starts zero in both layers: equal and uniform) */
+    tracking = dim == 2 && !active;
+    if (tracking) {
+        tiles_x = (cols + CAL_TILE_W - 1) / CAL_TILE_W;
+        tiles_y = (rows + CAL_TILE_H - 1) / CAL_TILE_H;
+        tile_words = (int)(((long long)tiles_x * tiles_y + 31) / 32);
+        const size_t bm = (size_t)CAL_NTYPES * CAL_MAX_SUBSTATES_CORE * tile_words * sizeof(unsigned);
+        if (!cuda_ok(cudaMalloc(&d_chg, bm), "cudaMalloc change bitmaps") ||
+            !cuda_ok(cudaMalloc(&d_dev, bm), "cudaMalloc change bitmaps") ||
+            !cuda_ok(cudaMalloc(&d_untracked, 4 * sizeof(unsigned)), "cudaMalloc change bitmaps") ||
+            !cuda_ok(cudaMemsetAsync(d_chg, 0, bm, stream), "memset change bitmaps") ||
+            !cuda_ok(cudaMemsetAsync(d_dev, 0, bm, stream), "memset change bitmaps") ||
+            !cuda_ok(cudaMemsetAsync(d_untracked, 0, 4 * sizeof(unsigned), stream), "memset change bitmaps"))
+            return false;
+    }
     if (active) {
         scratch_ints = compact_scratch_ints(ncells);
         if (!cuda_ok(cudaMalloc(&d_flags, (size_t)ncells), "cudaMalloc flags") ||
@@ -392,6 +529,9 @@ void CalGrid::destroy()
     cudaFree(d_count);
     cudaFree(d_block_counts);
     cudaFree(d_dirty);
+    cudaFree(d_chg);
+    cudaFree(d_dev);
+    cudaFree(d_untracked);
     cudaFree(d_step);
     cudaFree(d_reduce_partial);
     cudaFree(d_reduce_result);
@@ -520,7 +660,8 @@ bool CalGrid::load_from_host(int type, int slot, const void* src)
         return false;
     }
     const size_t bytes = (size_t)ncells * q.elem;
-    if (!cuda_ok(cudaMemcpyAsync(q.layer[0].dev, src, bytes, cudaMemcpyHostToDevice, stream), "copy from host"))
+    /* cudaMemcpyDefault: the caller's array may be in host or device memory */
+    if (!cuda_ok(cudaMemcpyAsync(q.layer[0].dev, src, bytes, cudaMemcpyDefault, stream), "copy from host"))
         return false;
     q.layer[0].dev_valid = true;
     q.layer[0].host_valid = false;
@@ -533,6 +674,15 @@ bool CalGrid::load_from_host(int type, int slot, const void* src)
         q.next_stale = false;
     }
     q.forced_dirty = false;
+    q.uval_valid = false;
+    inval_epoch++;
+    if (tracking && !q.single) {
+        /* both layers are equal: no tile differs */
+        const size_t row = (size_t)(type * CAL_MAX_SUBSTATES_CORE + slot) * tile_words;
+        if (!cuda_ok(cudaMemsetAsync(d_chg + row, 0, tile_words * sizeof(unsigned), stream), "clear change bits"))
+            return false;
+        q.track = true;
+    }
     return true;
 }
 
@@ -550,11 +700,9 @@ bool CalGrid::store_to_host(int type, int slot, void* dst)
         return false;
     }
     const size_t bytes = (size_t)ncells * q.elem;
-    if (q.layer[0].host_valid) {
-        memcpy(dst, q.host[0], bytes);
-        return true;
-    }
-    return cuda_ok(cudaMemcpyAsync(dst, q.layer[0].dev, bytes, cudaMemcpyDeviceToHost, stream), "copy to host") &&
+    /* cudaMemcpyDefault: the caller's array may be in host or device memory */
+    const void* from = q.layer[0].host_valid ? q.host[0] : q.layer[0].dev;
+    return cuda_ok(cudaMemcpyAsync(dst, from, bytes, cudaMemcpyDefault, stream), "copy to host") &&
            cuda_ok(cudaStreamSynchronize(stream), "sync");
 }
 
@@ -562,7 +710,18 @@ void CalGrid::host_wrote(int type, int slot, int layer)
 {
     Sub& q = sub[type][slot];
     q.layer[layer].dev_valid = false;
-    q.forced_dirty = true;
+    q.forced_dirty = true; /* the next update copies the whole substate, after which tracking resumes */
+    q.track = false;
+    q.uval_valid = false;
+    inval_epoch++;
+}
+
+void CalGrid::untrack(int type, int slot)
+{
+    if (sub[type][slot].trackable) {
+        sub[type][slot].trackable = false;
+        inval_epoch++;
+    }
 }
 
 void CalGrid::device_wrote_all()
@@ -623,38 +782,153 @@ bool CalGrid::fill(int type, int slot, int layer, const void* value, bool at_act
         return false;
     q.layer[layer].host_valid = false;
     q.forced_dirty = true;
+    q.track = false; /* one layer only: the layers differ; the next update copies the whole substate */
+    q.uval_valid = false;
+    if (tracking)
+        inval_epoch++;
+    return true;
+}
+
+/* calInitSubstate*: both layers.  With change tracking the layers stay
+ * equal (no update copy is needed afterwards), and when the substate
+ * already holds this value outside the tiles of its dev and chg bitmaps,
+ * only those tiles are filled. */
+bool CalGrid::fill_both(int type, int slot, const void* value)
+{
+    Sub& q = sub[type][slot];
+    if (!tracking || !q.trackable || q.single || !q.used) {
+        if (!fill(type, slot, 0, value, true))
+            return false;
+        return fill(type, slot, 1, value, true);
+    }
+    if (!repair_stale(type, slot) || !to_device_all())
+        return false;
+    unsigned long long v = 0;
+    memcpy(&v, value, q.elem);
+    const size_t row = (size_t)(type * CAL_MAX_SUBSTATES_CORE + slot) * tile_words;
+    void* l0 = q.layer[0].dev;
+    void* l1 = q.layer[1].dev;
+    if (q.track && q.uval_valid && q.uval == v) {
+        TileGeom tg;
+        tg.rows = rows;
+        tg.cols = cols;
+        tg.tiles_x = tiles_x;
+        tg.tile_words = tile_words;
+        tg.ntiles = tiles_x * tiles_y;
+        const int g = tile_words < 152 * 8 ? tile_words : 152 * 8;
+        switch (type) {
+        case 0: k_fill_tiles<CALbyte><<<g, kThreads, 0, stream>>>(tg, (CALbyte*)l0, (CALbyte*)l1, *(const CALbyte*)value, d_chg + row, d_dev + row); break;
+        case 1: k_fill_tiles<CALint><<<g, kThreads, 0, stream>>>(tg, (CALint*)l0, (CALint*)l1, *(const CALint*)value, d_chg + row, d_dev + row); break;
+        default: k_fill_tiles<CALreal><<<g, kThreads, 0, stream>>>(tg, (CALreal*)l0, (CALreal*)l1, *(const CALreal*)value, d_chg + row, d_dev + row); break;
+        }
+        if (!cuda_ok(cudaGetLastError(), "tile fill kernel"))
+            return false;
+    } else {
+        const int g = grid_for(ncells);
+        for (int l = 0; l < 2; l++) {
+            void* buf = q.layer[l].dev;
+            switch (type) {
+            case 0: k_fill<CALbyte><<<g, kThreads, 0, stream>>>((CALbyte*)buf, *(const CALbyte*)value, ncells, d_lin, d_count, 0); break;
+            case 1: k_fill<CALint><<<g, kThreads, 0, stream>>>((CALint*)buf, *(const CALint*)value, ncells, d_lin, d_count, 0); break;
+            default: k_fill<CALreal><<<g, kThreads, 0, stream>>>((CALreal*)buf, *(const CALreal*)value, ncells, d_lin, d_count, 0); break;
+            }
+        }
+        if (!cuda_ok(cudaGetLastError(), "fill kernel") ||
+            !cuda_ok(cudaMemsetAsync(d_chg + row, 0, tile_words * sizeof(unsigned), stream), "clear change bits") ||
+            !cuda_ok(cudaMemsetAsync(d_dev + row, 0, tile_words * sizeof(unsigned), stream), "clear change bits"))
+            return false;
+        q.uval = v;
+        q.uval_valid = true;
+        q.track = true;
+    }
+    /* the layers are equal: whatever a process wrote into next before is gone */
+    q.layer[0].host_valid = false;
+    q.layer[1].host_valid = false;
+    q.forced_dirty = false;
     return true;
 }
 
 bool CalGrid::copy_next_to_current(const std::vector<std::pair<int, int>>& which, bool use_dirty, bool at_active)
 {
+    /* tracked substates go tile by tile (k_update_tiles), the others whole
+     * (k_update); a substate whose bitmap was not exact becomes tracked again
+     * once its whole copy is queued */
     UpdateParams p;
     memset(&p, 0, sizeof(p));
+    TileUpdateParams tp;
+    memset(&tp, 0, sizeof(tp));
+    std::vector<std::pair<int, int>> retrack;
     for (size_t w = 0; w < which.size(); w++) {
-        Sub& q = sub[which[w].first][which[w].second];
+        const int t = which[w].first, sl = which[w].second;
+        Sub& q = sub[t][sl];
         if (!q.used || q.single || q.next_stale)
             continue;
+        const bool tiles = tracking && q.trackable && q.track;
+        if (tiles) {
+            const int e = tp.n_entries++;
+            tp.src[e] = q.layer[1].dev;
+            tp.dst[e] = q.layer[0].dev;
+            tp.elem[e] = (unsigned char)q.elem;
+            tp.type[e] = (unsigned char)t;
+            tp.slot[e] = (unsigned char)sl;
+            if (q.forced_dirty)
+                tp.forced[t] |= 1u << sl;
+            continue;
+        }
         const int e = p.n_entries++;
         p.src[e] = q.layer[1].dev;
         p.dst[e] = q.layer[0].dev;
         p.elem[e] = (unsigned char)q.elem;
-        p.type[e] = (unsigned char)which[w].first;
-        p.slot[e] = (unsigned char)which[w].second;
+        p.type[e] = (unsigned char)t;
+        p.slot[e] = (unsigned char)sl;
         if (q.forced_dirty)
-            p.forced[which[w].first] |= 1u << which[w].second;
+            p.forced[t] |= 1u << sl;
+        if (tracking && q.trackable)
+            retrack.push_back(which[w]);
     }
-    if (p.n_entries == 0)
-        return true;
-    p.ncells = ncells;
-    p.dirty = d_dirty;
-    p.use_dirty = use_dirty ? 1 : 0;
-    p.at_active = (at_active && active) ? 1 : 0;
-    p.lin = d_lin;
-    p.count = d_count;
-    const long long work = p.at_active ? ncells : (ncells * 8) / 16;
-    k_update<<<grid_for(work), kThreads, 0, stream>>>(p);
-    if (!cuda_ok(cudaGetLastError(), "update kernel"))
-        return false;
+    if (p.n_entries > 0) {
+        p.ncells = ncells;
+        p.dirty = d_dirty;
+        p.use_dirty = use_dirty ? 1 : 0;
+        p.at_active = (at_active && active) ? 1 : 0;
+        p.lin = d_lin;
+        p.count = d_count;
+        const long long work = p.at_active ? ncells : (ncells * 8) / 16;
+        k_update<<<grid_for(work), kThreads, 0, stream>>>(p);
+        if (!cuda_ok(cudaGetLastError(), "update kernel"))
+            return false;
+        for (size_t r = 0; r < retrack.size(); r++) {
+            /* copied whole only if written or forced: a substate that lost
+             * its tracking was forced (host write, one-layer fill), so the
+             * layers are equal after this copy */
+            Sub& q = sub[retrack[r].first][retrack[r].second];
+            if (!q.forced_dirty && use_dirty)
+                continue;
+            const size_t row = (size_t)(retrack[r].first * CAL_MAX_SUBSTATES_CORE + retrack[r].second) * tile_words;
+            if (!cuda_ok(cudaMemsetAsync(d_chg + row, 0, tile_words * sizeof(unsigned), stream),
+                         "clear change bits"))
+                return false;
+            q.track = true;
+            q.uval_valid = false;
+        }
+    }
+    if (tp.n_entries > 0) {
+        tp.g.rows = rows;
+        tp.g.cols = cols;
+        tp.g.tiles_x = tiles_x;
+        tp.g.tile_words = tile_words;
+        tp.g.ntiles = tiles_x * tiles_y;
+        tp.dirty = d_dirty;
+        tp.use_dirty = use_dirty ? 1 : 0;
+        tp.chg = d_chg;
+        tp.dev = d_dev;
+        tp.untracked = d_untracked;
+        const long long items = (long long)tp.n_entries * tile_words;
+        const int g = (int)(items < 152 * 8 ? items : 152 * 8);
+        k_update_tiles<<<g, kThreads, 0, stream>>>(tp);
+        if (!cuda_ok(cudaGetLastError(), "tile update kernel"))
+            return false;
+    }
     for (size_t w = 0; w < which.size(); w++) {
         Sub& q = sub[which[w].first][which[w].second];
         if (!q.used || q.single || q.next_stale)
@@ -718,6 +992,10 @@ bool CalGrid::swap(int type, int slot)
     q.layer[0].host_valid = false;
     q.layer[1].host_valid = false;
     q.next_stale = true;
+    if (q.trackable) {
+        q.trackable = false; /* the layers were written outside the tracked path */
+        inval_epoch++;
+    }
     swaps++;
     return true;
 }

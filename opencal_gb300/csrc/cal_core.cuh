@@ -52,6 +52,17 @@ struct Sub {
     void* host[2] = {nullptr, nullptr};
     bool next_stale = false; /* after a pointer swap next holds old data */
     bool forced_dirty = false;
+    /* change tracking (2D models without active cells, CalGrid::tracking):
+     *  trackable  false for good once a device pointer of the substate was
+     *             handed out or its layers were swapped (writes the library
+     *             does not see)
+     *  track      the chg bitmap is exact: next == current outside its tiles
+     *  uval_valid both layers hold `uval` (bit pattern) outside the tiles of
+     *             the dev and chg bitmaps */
+    bool trackable = true;
+    bool track = true;
+    bool uval_valid = true;
+    unsigned long long uval = 0;
 };
 
 /* host-side bookkeeping that a step may change; restored when a graph
@@ -86,6 +97,22 @@ struct CalGrid {
     unsigned char* h_flags = nullptr; /* host mirror (pinned) */
 
     unsigned* d_dirty = nullptr; /* [3] written-substate bits */
+    /* change tracking: CAL_TILE_W x CAL_TILE_H tiles (include/opencal/
+     * cal2DDevice.cuh), one bitmap of tile_words words per substate slot
+     * (index type * CAL_MAX_SUBSTATES_CORE + slot) in d_chg (next may differ
+     * from current) and d_dev (the layers may differ from the substate's
+     * uniform value); d_untracked: [3] substates written by unsafe
+     * operations since the last update, [3] the update kernel's ticket */
+    bool tracking = false;
+    /* bumped by every host-side event that invalidates tracked state (host
+     * writes, one-layer fills, copies into both layers, handed-out device
+     * pointers, swaps): a step recorded as a graph before such an event
+     * holds decisions that no longer apply and is recorded again */
+    long inval_epoch = 0;
+    int tiles_x = 0, tiles_y = 0, tile_words = 0;
+    unsigned* d_chg = nullptr;
+    unsigned* d_dev = nullptr;
+    unsigned* d_untracked = nullptr;
     int* d_step = nullptr;       /* step counter of a device-driven run */
     void* d_reduce_partial = nullptr; /* reduction scratch (per-block partials) */
     void* d_reduce_result = nullptr;  /* reduction result read back by the host */
@@ -115,6 +142,8 @@ struct CalGrid {
 
     /* device operations */
     bool fill(int type, int slot, int layer, const void* value, bool at_active);
+    bool fill_both(int type, int slot, const void* value); /* calInitSubstate: both layers, all (or active) cells */
+    void untrack(int type, int slot);                    /* device pointer handed out: no tracking from now on */
     bool copy_next_to_current(const std::vector<std::pair<int, int>>& which, bool use_dirty, bool at_active);
     bool update_all();                         /* calUpdate: compaction + copies */
     bool compact();                            /* calUpdateActiveCells */

@@ -57,6 +57,7 @@ struct SciaraParams {
     double effusion_duration;
     unsigned emission_time;
     int nvents, nphases, active;
+    int libm; /* 1: pow / atan / cos as the reference calls them (sciara_math.cuh), 0: the identity forms */
     int vent_x[SCI_MAX_VENTS], vent_y[SCI_MAX_VENTS];
     double rates[SCI_MAX_VENTS * SCI_MAX_PHASES];
 };
@@ -99,8 +100,8 @@ static __device__ void sci_outflows_min(struct CALModel2D* model, int i, int j, 
     double z[9], h[9], H[9], dz[9];
     const double t = calGet2Dr(model, SQ.St, i, j);
     const double w = SP.Pc;
-    const double Pr = sci_power_law(SP.a, SP.b, t);
-    const double hc = sci_power_law(SP.c, SP.d, t);
+    const double Pr = SP.libm ? sci_power_law_libm(SP.a, SP.b, t) : sci_power_law(SP.a, SP.b, t);
+    const double hc = SP.libm ? sci_power_law_libm(SP.c, SP.d, t) : sci_power_law(SP.c, SP.d, t);
     const double sz0 = calGet2Dr(model, SQ.Sz, i, j);
     for (int k = 0; k < 9; k++) {
         h[k] = calGetX2Dr(model, SQ.Slt, i, j, k);
@@ -141,7 +142,8 @@ static __device__ void sci_outflows_min(struct CALModel2D* model, int i, int j, 
             }
     } while (loop);
     for (int k = 1; k < 9; k++)
-        if (in_set[k] && sci_shear_exceeded(h[0], hc, dz[k], w))
+        if (in_set[k] && (SP.libm ? sci_shear_exceeded_libm(h[0], hc, dz[k], w)
+                                  : sci_shear_exceeded(h[0], hc, dz[k], w)))
             f[k] = Pr * (avg - H[k]);
 }
 
@@ -195,7 +197,10 @@ CAL_ELEMENTARY_PROCESS_2D(sciara_update_temperature)(struct CALModel2D* model, i
         if (h != 0) {
             const double nT = T;
             double aus;
-            st = sci_cool(nT, h, SP.Pepsilon, SP.Psigma, SP.Pclock, SP.Pcool, SP.Prho, SP.Pcv, SP.Pac, &aus);
+            st = SP.libm ? sci_cool_libm(nT, h, SP.Pepsilon, SP.Psigma, SP.Pclock, SP.Pcool, SP.Prho, SP.Pcv,
+                                         SP.Pac, &aus)
+                         : sci_cool(nT, h, SP.Pepsilon, SP.Psigma, SP.Pclock, SP.Pcool, SP.Prho, SP.Pcv, SP.Pac,
+                                    &aus);
             calSet2Dr(model, SQ.St, i, j, st);
         }
         if (st <= SP.PTsol && sh > 0) {
@@ -318,6 +323,18 @@ static void sciara_init(struct CALModel2D* model)
  * Pr(Tsol), Pr(Tvent), Phc(Tsol), Phc(Tvent), Pcool, Prho, Pepsilon, Psigma,
  * Pcv, Pc.  vents: (x, y) pairs; rates: nvents x nphases m^3/s.  max_steps 0
  * runs until the emission ends.  graph != 0 replays a recorded step. */
+/* 0: the identity forms of sciara_math.cuh (default); 1: pow / atan / cos
+ * as the reference writes them (CUDA's functions); applies to the following
+ * cal_sciara_run calls */
+static int g_sci_libm = 0;
+extern "C" int cal_sciara_set_math(int form)
+{
+    if (form != 0 && form != 1)
+        return CAL_ERROR_INVALID_ARGUMENT;
+    g_sci_libm = form;
+    return CAL_SUCCESS;
+}
+
 extern "C" int cal_sciara_run(int rows, int cols, int ac, int max_steps, const double* params, int nvents,
                               const int* vent_xy, unsigned emission_time, int nphases, const double* rates,
                               const double* z0, const double* slt0, const double* st0, double* z_out,
@@ -347,6 +364,7 @@ extern "C" int cal_sciara_run(int rows, int cols, int ac, int max_steps, const d
     SP.nvents = nvents;
     SP.nphases = nphases;
     SP.active = ac;
+    SP.libm = g_sci_libm;
     for (int k = 0; k < nvents; k++) {
         SP.vent_x[k] = vent_xy[2 * k];
         SP.vent_y[k] = vent_xy[2 * k + 1];

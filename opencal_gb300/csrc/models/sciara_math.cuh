@@ -46,4 +46,28 @@ static __device__ __forceinline__ double sci_cool(double T, double h, double eps
     return T / cbrt(*aus);
 }
 
+/* The same three quantities written as the reference writes them, with
+ * CUDA's pow, atan and cos in place of the C library's (the
+ * device-process program selects them with cal_sciara_set_math(1)): the
+ * difference from the C library is then CUDA's own rounding of those
+ * functions alone. */
+static __device__ __forceinline__ double sci_power_law_libm(double k1, double k2, double T)
+{
+    const double log_value = k1 + k2 * T;
+    return pow(10.0, log_value);
+}
+
+static __device__ __forceinline__ bool sci_shear_exceeded_libm(double h0, double hc, double dz, double w)
+{
+    const double theta = atan(dz / w);
+    return h0 > hc * cos(theta);
+}
+
+static __device__ __forceinline__ double sci_cool_libm(double T, double h, double eps, double sigma, double clock,
+                                                       double cool, double rho, double cv, double ac, double* aus)
+{
+    *aus = 1.0 + (3 * pow(T, 3.0) * eps * sigma * clock * cool) / (rho * cv * h * ac);
+    return T / pow(*aus, 1.0 / 3.0);
+}
+
 #endif

@@ -35,6 +35,7 @@
 
 #include "exact_div.cuh"
 #include "opencal/cal2D.h"
+#include "opencal/cal2DIO.h"
 #include "opencal/cal2DRun.h"
 
 #include <string>
@@ -1914,6 +1915,53 @@ static void sciddicaT_simulation_init_fused(struct CALModel2D* sciddicaT)
 
 enum { SDT_MODE_PROCESSES = 0, SDT_MODE_FUSED = 1 };
 
+/* The reference example's main() as it stands (OpenCAL-OMP/examples/
+ * calomp_sciddicaT/source/sciddicaT.c:140-180): the model, its two device
+ * processes and six substates, z and h loaded from text files with
+ * calLoadSubstate2Dr, the run (init, steering, IMPLICIT updates) with
+ * calRun2D, and h saved with calSaveSubstate2Dr.  graph: 1 replays the
+ * recorded step.  Returns a CALError code (CAL_ERROR_IO when a file cannot
+ * be read or written). */
+extern "C" int cal_sciddicaT_run_files(int rows, int cols, int toroidal, int steps, double p_r, double p_eps,
+                                       const char* dem_path, const char* source_path, const char* output_path,
+                                       int graph)
+{
+    sdt2::g_state.hknown = false;
+    calClearError();
+    sciddicaT_step_invalidate();
+    g_fused_ac = false;
+    struct CALModel2D* ca = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D,
+                                       toroidal ? CAL_SPACE_TOROIDAL : CAL_SPACE_FLAT, CAL_NO_OPT);
+    if (!ca)
+        return calGetLastError();
+    struct CALRun2D* run = calRunDef2D(ca, 1, steps, CAL_UPDATE_IMPLICIT);
+    P.epsilon = p_eps;
+    P.r = p_r;
+    P.active = 0;
+    calAddElementaryProcess2D(ca, sciddicaT_flows_computation);
+    calAddElementaryProcess2D(ca, sciddicaT_width_update);
+    Q.z = calAddSubstate2Dr(ca);
+    Q.h = calAddSubstate2Dr(ca);
+    for (int q = 0; q < NUMBER_OF_OUTFLOWS; q++)
+        Q.f[q] = calAddSubstate2Dr(ca);
+    int err = CAL_SUCCESS;
+    if (!calLoadSubstate2Dr(ca, Q.z, (char*)dem_path) || !calLoadSubstate2Dr(ca, Q.h, (char*)source_path)) {
+        err = CAL_ERROR_IO;
+    } else {
+        calRunAddInitFunc2D(run, sciddicaT_simulation_init);
+        calRunAddSteeringFunc2D(run, sciddicaT_steering_plain);
+        calRunSetGraph2D(run, graph ? CAL_TRUE : CAL_FALSE);
+        calRun2D(run);
+        if (!calSaveSubstate2Dr(ca, Q.h, (char*)output_path) && calGetLastError() == CAL_SUCCESS)
+            err = CAL_ERROR_IO;
+    }
+    if (err == CAL_SUCCESS)
+        err = calGetLastError();
+    calRunFinalize2D(run);
+    calFinalize2D(ca);
+    return err;
+}
+
 /* how many device-loop runs had to fall back to a launch sequence per step */
 static int g_fallbacks = 0;
 static void cal_note_fallback() { g_fallbacks++; }
@@ -2132,6 +2180,13 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
     for (int k = 0; k < 6; k++)
         for (int l = 0; l < 2; l++) {
             cudaMalloc(&s->snap[k][l], s->bytes);
+            if (mode == SDT_MODE_PROCESSES) {
+                /* through the API, so that the substates keep their change
+                 * tracking (after the init's update both layers are equal) */
+                if (l == 0)
+                    calCopySubstateToHost2Dr(s->ca, sdt_sub(k), (double*)s->snap[k][0]);
+                continue;
+            }
             cudaMemcpyAsync(s->snap[k][l], calGetDeviceBuffer2Dr(s->ca, sdt_sub(k), l), s->bytes,
                             cudaMemcpyDeviceToDevice, st);
         }
@@ -2154,17 +2209,23 @@ extern "C" int cal_sciddicaT_reset(void* handle)
     SdtSession* s = (SdtSession*)handle;
     sciddicaT_step_invalidate();
     cudaStream_t st = (cudaStream_t)calGetStream2D(s->ca);
-    for (int k = 0; k < 6; k++)
-        for (int l = 0; l < 2; l++)
-            cudaMemcpyAsync(calGetDeviceBuffer2Dr(s->ca, sdt_sub(k), l == 0 ? 0 : 2), s->snap[k][l], s->bytes,
-                            cudaMemcpyDeviceToDevice, st);
+    if (s->mode == SDT_MODE_PROCESSES) {
+        for (int k = 0; k < 6; k++)
+            calCopySubstateFromHost2Dr(s->ca, sdt_sub(k), (const double*)s->snap[k][0]);
+    } else {
+        for (int k = 0; k < 6; k++)
+            for (int l = 0; l < 2; l++)
+                cudaMemcpyAsync(calGetDeviceBuffer2Dr(s->ca, sdt_sub(k), l == 0 ? 0 : 2), s->snap[k][l], s->bytes,
+                                cudaMemcpyDeviceToDevice, st);
+    }
     if (s->ac && !s->fused_ac) {
         CALbyte* flags;
         calGetDeviceActiveCells2D(s->ca, &flags, nullptr, nullptr);
         cudaMemcpyAsync(flags, s->snap_flags, (size_t)s->ca->rows * s->ca->columns, cudaMemcpyDeviceToDevice, st);
         calUpdateActiveCells2D(s->ca);
     }
-    calMarkDeviceWritten2D(s->ca);
+    if (s->mode != SDT_MODE_PROCESSES)
+        calMarkDeviceWritten2D(s->ca);
     return calGetLastError();
 }
 

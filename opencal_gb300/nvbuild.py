@@ -35,7 +35,7 @@ MODEL_FLAGS = ["--fmad=false", "-Xcompiler=-ffp-contract=off"]  # no contraction
 
 CORE_SOURCES = ["cal_core.cu", "cal2D.cu", "cal3D.cu", "cal2DRun.cu", "cal3DRun.cu", "calIO.cu", "calReduction.cu", "cal_noalloc.cu"]
 MODEL_SOURCES = ["models/sciddicaT.cu", "models/sciddicaT_adjoint.cu", "models/sciddicaT_batch.cu",
-                 "models/sciddicaT_unsafe.cu", "models/sciara.cu", "models/sciara_batch.cu", "models/mbusu.cu",
+                 "models/sciddicaT_unsafe.cu", "models/sciara.cu", "models/sciara_batch.cu", "models/sciara_io.cu", "models/mbusu.cu",
                  "models/life.cu", "models/life3d.cu", "models/fp64_peak.cu"]
 
 

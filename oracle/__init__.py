@@ -129,6 +129,34 @@ def sciddicaT_trace(z0, h0, steps, *, p_r=0.5, p_eps=0.001, kind="serial"):
     return z, h, out[: int(steps)], edge.value
 
 
+_KINDS = {np.dtype(np.int8): 0, np.dtype(np.uint8): 0, np.dtype(np.int32): 1, np.dtype(np.float64): 2}
+
+
+def save_text(data, path, *, kind="serial"):
+    """A 2D (rows, cols) or 3D (slices, rows, cols) array of int8/uint8,
+    int32 or float64 written in the reference's substate text format."""
+    data = np.ascontiguousarray(data)
+    dim = data.ndim
+    slices, rows, cols = (1,) + data.shape if dim == 2 else data.shape
+    f = _fn(kind, "save_text")
+    f.argtypes = [C.c_int] * 5 + [C.c_void_p, C.c_char_p]
+    if f(dim, _KINDS[data.dtype], rows, cols, slices, data.ctypes.data, str(path).encode()):
+        raise RuntimeError("save_text failed")
+
+
+def load_text(shape, dtype, path, *, kind="serial"):
+    """The reference's substate text format read into an array of `shape`
+    ((rows, cols) or (slices, rows, cols)) and `dtype`."""
+    out = np.zeros(shape, dtype=dtype)
+    dim = len(shape)
+    slices, rows, cols = (1,) + tuple(shape) if dim == 2 else tuple(shape)
+    f = _fn(kind, "load_text")
+    f.argtypes = [C.c_int] * 5 + [C.c_void_p, C.c_char_p]
+    if f(dim, _KINDS[np.dtype(dtype)], rows, cols, slices, out.ctypes.data, str(path).encode()):
+        raise RuntimeError("load_text failed")
+    return out
+
+
 def life2d(s0, steps, *, toroidal=True, as_int=False, kind="serial"):
     s0 = np.ascontiguousarray(s0, dtype=np.uint8)
     out = np.empty_like(s0)

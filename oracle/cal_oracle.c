@@ -5,6 +5,7 @@
  */
 #include "cal_oracle.h"
 
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -598,5 +599,66 @@ int orc_reduce2d(int kind, int rows, int cols, const void* data, int op, double*
         }
         *out = acc;
     }
+    return 0;
+}
+
+/* ======================= substate text files ============================ */
+/* calfSaveMatrix2D* / calfSaveMatrix3D* (OpenCAL-OMP/source/
+ * cal2DBufferIO.c:105-147, cal3DBufferIO.c:110-160): each value printed with
+ * "%d " (byte, int) or "%.9f " (2D real) / "%f " (3D real) into a string
+ * that is then written followed by one more space; a newline after every
+ * row; in 3D slice by slice, with an empty line after every slice.
+ * calfLoadMatrix* (cal2DBufferIO.c:17-45): whitespace-separated tokens,
+ * atoi / atof, in the same order.  kind: 0 byte, 1 int, 2 real. */
+int orc_save_text(int dim, int kind, int rows, int cols, int slices, const void* data, const char* path)
+{
+    char str[256];
+    int i, j, k;
+    FILE* f = fopen(path, "w");
+    if (!f)
+        return 1;
+    if (dim == 2)
+        slices = 1;
+    for (k = 0; k < slices; k++) {
+        for (i = 0; i < rows; i++) {
+            for (j = 0; j < cols; j++) {
+                long c = ((long)k * rows + i) * cols + j;
+                if (kind == 0)
+                    sprintf(str, "%d ", ((const char*)data)[c]);
+                else if (kind == 1)
+                    sprintf(str, "%d ", ((const int*)data)[c]);
+                else
+                    sprintf(str, dim == 2 ? "%.9f " : "%f ", ((const double*)data)[c]);
+                fprintf(f, "%s ", str);
+            }
+            fprintf(f, "\n");
+        }
+        if (dim == 3)
+            fprintf(f, "\n");
+    }
+    fclose(f);
+    return 0;
+}
+
+int orc_load_text(int dim, int kind, int rows, int cols, int slices, void* data, const char* path)
+{
+    char str[256];
+    long c, n = (long)rows * cols * (dim == 3 ? slices : 1);
+    FILE* f = fopen(path, "r");
+    if (!f)
+        return 1;
+    for (c = 0; c < n; c++) {
+        if (fscanf(f, "%255s", str) != 1) {
+            fclose(f);
+            return 2;
+        }
+        if (kind == 0)
+            ((char*)data)[c] = (char)atoi(str);
+        else if (kind == 1)
+            ((int*)data)[c] = atoi(str);
+        else
+            ((double*)data)[c] = atof(str);
+    }
+    fclose(f);
     return 0;
 }

@@ -161,4 +161,9 @@ int orc_reduce2d(int kind, int rows, int cols, const void* data, int op, double*
 int orc_sciddicaT_trace(int rows, int cols, int steps, double p_r, double p_eps, const double* z0, const double* h0,
                         double* z_out, double* h_out, double* outflux, int* edge_step);
 
+/* substate text files in the reference's format (dim 2 or 3; kind: 0 byte,
+ * 1 int, 2 real; 3D data slice-major) */
+int orc_save_text(int dim, int kind, int rows, int cols, int slices, const void* data, const char* path);
+int orc_load_text(int dim, int kind, int rows, int cols, int slices, void* data, const char* path);
+
 #endif

@@ -672,3 +672,91 @@ int ref_reduce2d(int kind, int rows, int cols, const void* data, int op, double*
     finalize2d(m);
     return 0;
 }
+
+/* ======================= substate text files ============================ */
+/* the reference's own calSaveSubstate2D* / 3D* and calLoadSubstate2D* / 3D*
+ * on a model holding `data` (kind: 0 byte, 1 int, 2 real; 3D slice-major) */
+#include <cal2DIO.h>
+#include <cal3DIO.h>
+
+int ref_save_text(int dim, int kind, int rows, int cols, int slices, const void* data, const char* path)
+{
+    size_t n = (size_t)rows * cols * (dim == 3 ? slices : 1);
+    CALbyte ok;
+    if (dim == 2) {
+        struct CALModel2D* m = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D, CAL_SPACE_TOROIDAL, CAL_NO_OPT);
+        if (kind == 0) {
+            struct CALSubstate2Db* q = calAddSubstate2Db(m);
+            memcpy(q->current, data, n);
+            ok = calSaveSubstate2Db(m, q, (char*)path);
+        } else if (kind == 1) {
+            struct CALSubstate2Di* q = calAddSubstate2Di(m);
+            memcpy(q->current, data, n * sizeof(int));
+            ok = calSaveSubstate2Di(m, q, (char*)path);
+        } else {
+            struct CALSubstate2Dr* q = calAddSubstate2Dr(m);
+            memcpy(q->current, data, n * sizeof(double));
+            ok = calSaveSubstate2Dr(m, q, (char*)path);
+        }
+        finalize2d(m);
+    } else {
+        struct CALModel3D* m = calCADef3D(rows, cols, slices, CAL_VON_NEUMANN_NEIGHBORHOOD_3D, CAL_SPACE_TOROIDAL,
+                                          CAL_NO_OPT);
+        if (kind == 0) {
+            struct CALSubstate3Db* q = calAddSubstate3Db(m);
+            memcpy(q->current, data, n);
+            ok = calSaveSubstate3Db(m, q, (char*)path);
+        } else if (kind == 1) {
+            struct CALSubstate3Di* q = calAddSubstate3Di(m);
+            memcpy(q->current, data, n * sizeof(int));
+            ok = calSaveSubstate3Di(m, q, (char*)path);
+        } else {
+            struct CALSubstate3Dr* q = calAddSubstate3Dr(m);
+            memcpy(q->current, data, n * sizeof(double));
+            ok = calSaveSubstate3Dr(m, q, (char*)path);
+        }
+        calFinalize3D(m);
+    }
+    return ok ? 0 : 1;
+}
+
+int ref_load_text(int dim, int kind, int rows, int cols, int slices, void* data, const char* path)
+{
+    size_t n = (size_t)rows * cols * (dim == 3 ? slices : 1);
+    CALbyte ok;
+    if (dim == 2) {
+        struct CALModel2D* m = calCADef2D(rows, cols, CAL_VON_NEUMANN_NEIGHBORHOOD_2D, CAL_SPACE_TOROIDAL, CAL_NO_OPT);
+        if (kind == 0) {
+            struct CALSubstate2Db* q = calAddSubstate2Db(m);
+            ok = calLoadSubstate2Db(m, q, (char*)path);
+            memcpy(data, q->current, n);
+        } else if (kind == 1) {
+            struct CALSubstate2Di* q = calAddSubstate2Di(m);
+            ok = calLoadSubstate2Di(m, q, (char*)path);
+            memcpy(data, q->current, n * sizeof(int));
+        } else {
+            struct CALSubstate2Dr* q = calAddSubstate2Dr(m);
+            ok = calLoadSubstate2Dr(m, q, (char*)path);
+            memcpy(data, q->current, n * sizeof(double));
+        }
+        finalize2d(m);
+    } else {
+        struct CALModel3D* m = calCADef3D(rows, cols, slices, CAL_VON_NEUMANN_NEIGHBORHOOD_3D, CAL_SPACE_TOROIDAL,
+                                          CAL_NO_OPT);
+        if (kind == 0) {
+            struct CALSubstate3Db* q = calAddSubstate3Db(m);
+            ok = calLoadSubstate3Db(m, q, (char*)path);
+            memcpy(data, q->current, n);
+        } else if (kind == 1) {
+            struct CALSubstate3Di* q = calAddSubstate3Di(m);
+            ok = calLoadSubstate3Di(m, q, (char*)path);
+            memcpy(data, q->current, n * sizeof(int));
+        } else {
+            struct CALSubstate3Dr* q = calAddSubstate3Dr(m);
+            ok = calLoadSubstate3Dr(m, q, (char*)path);
+            memcpy(data, q->current, n * sizeof(double));
+        }
+        calFinalize3D(m);
+    }
+    return ok ? 0 : 1;
+}

@@ -427,3 +427,76 @@ extern "C" int cal_unsafe2d_run(int rows, int cols, int nbhd, int toroidal, int 
     return finish2d(ca, run);
 }
 
+/* ======================= substate text files ============================ */
+#include "opencal/cal2DIO.h"
+#include "opencal/cal3DIO.h"
+
+/* a model on the GPU loads a substate (kind: 0 byte, 1 int, 2 real) from
+ * in_path with calLoadSubstate2D / 3D (b, i, r), pushes it through an update
+ * on the device, saves it with calSaveSubstate2D / 3D to out_path and copies
+ * the current layer into data_out */
+extern "C" int cal_io_roundtrip(int dim, int kind, int rows, int cols, int slices, const char* in_path,
+                                const char* out_path, void* data_out)
+{
+    calClearError();
+    const size_t n = (size_t)rows * cols * (dim == 3 ? slices : 1);
+    int ok = 1;
+    if (dim == 2) {
+        struct CALModel2D* ca = calCADef2D(rows, cols, CAL_MOORE_NEIGHBORHOOD_2D, CAL_SPACE_TOROIDAL, CAL_NO_OPT);
+        if (!ca)
+            return calGetLastError();
+        if (kind == 0) {
+            struct CALSubstate2Db* q = calAddSubstate2Db(ca);
+            ok = calLoadSubstate2Db(ca, q, (char*)in_path);
+            calUpdate2D(ca);
+            ok = ok && calSaveSubstate2Db(ca, q, (char*)out_path);
+            calSync2D(ca);
+            memcpy(data_out, q->current, n);
+        } else if (kind == 1) {
+            struct CALSubstate2Di* q = calAddSubstate2Di(ca);
+            ok = calLoadSubstate2Di(ca, q, (char*)in_path);
+            calUpdate2D(ca);
+            ok = ok && calSaveSubstate2Di(ca, q, (char*)out_path);
+            calSync2D(ca);
+            memcpy(data_out, q->current, n * sizeof(int));
+        } else {
+            struct CALSubstate2Dr* q = calAddSubstate2Dr(ca);
+            ok = calLoadSubstate2Dr(ca, q, (char*)in_path);
+            calUpdate2D(ca);
+            ok = ok && calSaveSubstate2Dr(ca, q, (char*)out_path);
+            calSync2D(ca);
+            memcpy(data_out, q->current, n * sizeof(double));
+        }
+        const int err = calGetLastError();
+        calFinalize2D(ca);
+        return err ? err : (ok ? 0 : CAL_ERROR_IO);
+    }
+    struct CALModel3D* ca = calCADef3D(rows, cols, slices, CAL_MOORE_NEIGHBORHOOD_3D, CAL_SPACE_TOROIDAL, CAL_NO_OPT);
+    if (!ca)
+        return calGetLastError();
+    if (kind == 0) {
+        struct CALSubstate3Db* q = calAddSubstate3Db(ca);
+        ok = calLoadSubstate3Db(ca, q, (char*)in_path);
+        calUpdate3D(ca);
+        ok = ok && calSaveSubstate3Db(ca, q, (char*)out_path);
+        calSync3D(ca);
+        memcpy(data_out, q->current, n);
+    } else if (kind == 1) {
+        struct CALSubstate3Di* q = calAddSubstate3Di(ca);
+        ok = calLoadSubstate3Di(ca, q, (char*)in_path);
+        calUpdate3D(ca);
+        ok = ok && calSaveSubstate3Di(ca, q, (char*)out_path);
+        calSync3D(ca);
+        memcpy(data_out, q->current, n * sizeof(int));
+    } else {
+        struct CALSubstate3Dr* q = calAddSubstate3Dr(ca);
+        ok = calLoadSubstate3Dr(ca, q, (char*)in_path);
+        calUpdate3D(ca);
+        ok = ok && calSaveSubstate3Dr(ca, q, (char*)out_path);
+        calSync3D(ca);
+        memcpy(data_out, q->current, n * sizeof(double));
+    }
+    const int err = calGetLastError();
+    calFinalize3D(ca);
+    return err ? err : (ok ? 0 : CAL_ERROR_IO);
+}

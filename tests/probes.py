@@ -122,3 +122,19 @@ def exact_div_mismatches(x, c, y) -> int:
     f.restype = C.c_long
     f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong]
     return f(x.ctypes.data, c.ctypes.data, y.ctypes.data, len(x))
+
+
+def io_roundtrip(data, in_path, out_path):
+    """calLoadSubstate* from in_path into a GPU model, an update, then
+    calSaveSubstate* to out_path; returns the model's current layer."""
+    data = np.ascontiguousarray(data)
+    dim = data.ndim
+    slices, rows, cols = (1,) + data.shape if dim == 2 else data.shape
+    kind = {1: 0, 4: 1, 8: 2}[data.dtype.itemsize]
+    out = np.zeros_like(data)
+    f = lib().cal_io_roundtrip
+    f.restype = C.c_int
+    f.argtypes = [C.c_int] * 5 + [C.c_char_p, C.c_char_p, C.c_void_p]
+    _check(f(dim, kind, rows, cols, slices, str(in_path).encode(), str(out_path).encode(), out.ctypes.data),
+           "cal_io_roundtrip")
+    return out

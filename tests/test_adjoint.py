@@ -90,3 +90,45 @@ def test_gradients_vs_oracle_finite_differences(setup):
     assert abs(L - L_cpu(P_R)) <= 1e-12 * L
     fd_r = _fd(L_cpu, P_R, 1e-7)
     assert abs(gr - fd_r) <= 1e-5 * abs(fd_r), (gr, fd_r)
+
+
+def test_config_size_gradients_vs_gpu_finite_differences():
+    """The calibration configuration itself: 1024 x 1024, T = 2000 steps,
+    DEM and source from seed 3, target from a forward run at p_r = 0.42,
+    p_eps = 0.0015, gradient at (0.5, 0.001) with sqrt(T) checkpoints.  The
+    forward gives the split step's bits (the oracle-pinned plain step); the
+    gradients agree with central differences of the GPU forward to 1e-4
+    relative (the differences' own truncation and rounding at this size)."""
+    import torch
+
+    import opencal_gb300 as cal
+    cal.build()
+    rows = cols = 1024
+    steps = 2000
+    z, h = W.sciddicaT_inputs(rows, cols, seed=3)
+    dev = torch.device("cuda")
+    zt = torch.from_numpy(z).to(dev)
+    with torch.no_grad():
+        tgt = cal.adjoint.rollout(zt, torch.from_numpy(h).to(dev), 0.42, 0.0015, steps)
+    _, ref, _ = cal.sciddicaT(z, h, steps, toroidal=False, p_r=0.42, p_eps=0.0015, mode=cal.MODE_FUSED)
+    assert tgt.cpu().numpy().tobytes() == ref.tobytes()
+    h0 = torch.from_numpy(h).to(dev).requires_grad_(True)
+    pr = torch.tensor(P_R, dtype=torch.float64, device=dev, requires_grad=True)
+    pe = torch.tensor(P_EPS, dtype=torch.float64, device=dev, requires_grad=True)
+    L = ((cal.adjoint.rollout(zt, h0, pr, pe, steps) - tgt) ** 2).sum()
+    L.backward()
+
+    def L_gpu(p_r=P_R, p_eps=P_EPS, hh=h):
+        with torch.no_grad():
+            hT = cal.adjoint.rollout(zt, torch.from_numpy(hh).to(dev), p_r, p_eps, steps)
+            return float(((hT - tgt) ** 2).sum())
+
+    fd_r = _fd(lambda x: L_gpu(p_r=x), P_R, 1e-7)
+    fd_e = _fd(lambda x: L_gpu(p_eps=x), P_EPS, 1e-10)
+    assert float(pr.grad) != 0 and abs(float(pr.grad) - fd_r) <= 1e-4 * abs(fd_r), (float(pr.grad), fd_r)
+    assert float(pe.grad) != 0 and abs(float(pe.grad) - fd_e) <= 1e-4 * abs(fd_e), (float(pe.grad), fd_e)
+    rng = np.random.default_rng(7)
+    v = np.where(h > 0.05, rng.standard_normal(h.shape), 0.0)
+    fd_v = _fd(lambda s: L_gpu(hh=h + s * v), 0.0, 1e-8)
+    an_v = float((h0.grad.cpu().numpy() * v).sum())
+    assert abs(an_v - fd_v) <= 1e-4 * abs(fd_v), (an_v, fd_v)

@@ -202,3 +202,27 @@ def test_oracle_sciddicaT_unsafe_matches_reference_fixture(oracle_lib):
     fx = np.load(os.path.join(GOLDEN, "unsafe_cases.npz"))
     z, h = oracle_lib.sciddicaT_unsafe(fx["sdtu_z0"], fx["sdtu_h0"], 50, toroidal=True)
     assert z.tobytes() == fx["sdtu_z"].tobytes() and h.tobytes() == fx["sdtu_h"].tobytes()
+
+
+def _io_arrays():
+    from opencal_gb300 import workloads as W
+    u2, u3 = W.uniform_array(61, (17, 23)), W.uniform_array(62, (5, 9, 11))
+    return [
+        (u2 * 120 - 60).astype(np.int8), (u2 * 2e6 - 1e6).astype(np.int32), (u2 - 0.5) * 3e3,
+        (u3 * 120 - 60).astype(np.int8), (u3 * 2e6 - 1e6).astype(np.int32), (u3 - 0.5) * 3e3,
+    ]
+
+
+@pytest.mark.parametrize("idx", range(6))
+def test_oracle_text_files_vs_live_reference(reference_oracle, tmp_path, idx):
+    """Substate text files: the oracle's writer gives the reference's bytes
+    (calSaveSubstate2D* "%.9f " / 3D "%f " / "%d " plus a space, newline per
+    row, empty line per slice), and both readers give the same values."""
+    oracle = reference_oracle
+    a = _io_arrays()[idx]
+    oracle.save_text(a, tmp_path / "o.txt")
+    oracle.save_text(a, tmp_path / "r.txt", kind="ref")
+    assert (tmp_path / "o.txt").read_bytes() == (tmp_path / "r.txt").read_bytes()
+    x = oracle.load_text(a.shape, a.dtype, tmp_path / "r.txt")
+    y = oracle.load_text(a.shape, a.dtype, tmp_path / "r.txt", kind="ref")
+    assert x.tobytes() == y.tobytes()

@@ -92,3 +92,56 @@ def test_gpu_matches_oracle_longer_run(cal):
     assert out["steps"] == ref["steps"]
     for k in ("slt", "st", "z", "msl"):
         _close(out[k], ref[k], k)
+
+
+def _write_2006_files(tmp_path):
+    fx = np.load(os.path.join(GOLDEN, "sciara_2006.npz"))
+    names = {"file_000000000000_cfg": "2006_000000000000.cfg", "file_Morphology_stt": "2006_000000000000_Morphology.stt",
+             "file_Vents_stt": "2006_000000000000_Vents.stt",
+             "file_EmissionRate_txt": "2006_000000000000_EmissionRate.txt"}
+    for key, name in names.items():
+        (tmp_path / name).write_bytes(fx[key].tobytes())
+    return fx, str(tmp_path / "2006")
+
+
+@pytest.mark.parametrize("ac", [0, 1])
+def test_reference_2006_inputs_through_the_reader(cal, tmp_path, ac):
+    """The reference's own 2006 Etna configuration files, read by
+    cal_sciara_read (the example's .cfg / GIS .stt / emission-rate readers
+    restated), run on the GPU for the fixture's step count: the reference
+    program's final fields on the same files to the tolerance above."""
+    fx, prefix = _write_2006_files(tmp_path)
+    c = cal.sciara_read(prefix)
+    steps = int(fx["steps"][0])
+    out = cal.sciara(c["z"], c["vents"], c["rates"], c["emission_time"], steps, ac=bool(ac), params=c["params"])
+    p = f"ac{ac}_"
+    assert out["steps"] == int(fx[p + "steps"][0])
+    _close(out["slt"], fx[p + "slt"], "slt")
+    _close(out["st"], fx[p + "st"], "st")
+    _close(out["msl"], fx[p + "msl"], "msl")
+    _close(out["z"], c["z"] + fx[p + "dz"], "z")
+    assert (fx[p + "slt"] > 0).sum() > 100  # the flow is under way
+
+
+def test_transcendental_forms_against_oracle(cal):
+    """Both forms of the transcendental parts against the oracle (glibc's
+    pow / atan / cos) on one run, sampled after 1, 10, 100 and every step:
+    the largest relative difference per cell of Slt, St, Sz and Msl (cells
+    above 1e-9 of the field's maximum), printed for the record and bounded
+    by the tolerance above.  The libm form (CUDA's pow / atan / cos as the
+    reference writes them) isolates the functions' own rounding; the
+    identity forms add the rewritten expressions' rounding."""
+    import oracle
+    from opencal_gb300 import workloads as W
+    oracle.build()
+    z, vents, rates = W.sciara_inputs(128, 160, seed=13)
+    report = {}
+    for steps in (1, 10, 100, 0):
+        ref = oracle.sciara(z, vents, rates, 1200, steps, ac=False)
+        for libm in (False, True):
+            out = cal.sciara(z, vents, rates, 1200, steps, ac=False, libm=libm)
+            assert out["steps"] == ref["steps"]
+            worst = max(_close(out[k], ref[k], k) for k in ("slt", "st", "z", "msl"))
+            report[(ref["steps"], "libm" if libm else "identities")] = worst
+    for key in sorted(report):
+        print(f"SCIARA forms: after {key[0]} steps, {key[1]}: max relative difference {report[key]:.3e}")
