@@ -39,6 +39,7 @@
 #include "opencal/cal2DRun.h"
 
 #include <string>
+#include <vector>
 
 namespace cal {
 void set_error(CALError code, const std::string& msg); /* the library's error state (calGetLastError) */
@@ -234,13 +235,13 @@ constexpr int TW = SDT2_TW, TH = SDT2_TH; /* K2 tile: TH rows x TW columns, 4 ce
 struct State {
     struct CALModel2D* ca = nullptr;
     double* f = nullptr;         /* 4 * n outflows, SoA */
-    int* list[2] = {nullptr, nullptr};
-    int* zlist[2] = {nullptr, nullptr};
-    int* counts = nullptr;       /* [0..1] wet list lengths, [2..3] dried list lengths,
-                                    [4] list parity, [6] step epoch, [7..8] flagged
-                                    tiles; [C_TICKET] K2 block ticket; [C_ARRIVED],
-                                    [C_ERROR] the persistent kernel's barrier
-                                    counter and error flag */
+    double* zh = nullptr;        /* z + h per cell (u of a neighbour), kept where K2 writes h */
+    double* zeps = nullptr;      /* z + epsilon per cell (u[0] of the cell), from the priming */
+    int* list[2] = {nullptr, nullptr}; /* a step's cells: c for a wet cell, ~c for one that dried */
+    int* counts = nullptr;       /* [4] list parity, [6] step epoch; [C_TICKET] K2 block
+                                    ticket; [C_ARRIVED], [C_ERROR] the persistent kernel's
+                                    placement barrier counter and error flag */
+    unsigned long long* ctl = nullptr; /* 64-bit counters, one per 128-byte line (W_*) */
     int* tflag = nullptr;        /* per K2 tile: epoch of the step that flagged it */
     int* tlist = nullptr;        /* flagged tiles of the current step */
     long long n = 0;
@@ -256,8 +257,8 @@ struct State {
 
 /* The lists alternate between two buffers; which one a step reads is the
  * list parity, and tiles are flagged with the step's epoch; the step's
- * flagged tiles are counted in counts[7 + parity] (K1 empties the other one
- * for the next step).  Two ways to know parity and epoch:
+ * flagged tiles are counted in ctl[W_TILES + 16 * parity] (K1 empties the
+ * other one for the next step).  Two ways to know parity and epoch:
  *  - device words counts[4] and counts[6], flipped and advanced by the last
  *    K2 block of the step (a ticket): every step's launches are identical,
  *    so a step can be recorded once as a CUDA graph and replayed;
@@ -268,12 +269,13 @@ struct State {
 struct K1Params {
     const double* __restrict__ z;
     const double* __restrict__ h;
+    const double* __restrict__ zh;   /* z + h (written by K2) */
+    const double* __restrict__ zeps; /* z + eps */
     double* __restrict__ f;
     int* list0;
     int* list1;
-    int* zlist0;
-    int* zlist1;
     int* counts;
+    unsigned long long* ctl;
     int* tflag;
     int* tlist;
     int rows, cols, toroidal, tiles_x;
@@ -284,12 +286,13 @@ struct K1Params {
 
 struct K2Params {
     double* __restrict__ h;
+    double* __restrict__ zh;
+    const double* __restrict__ z;
     const double* __restrict__ f;
     int* list0;
     int* list1;
-    int* zlist0;
-    int* zlist1;
     int* counts;
+    unsigned long long* ctl;
     const int* tflag;
     const int* tlist;
     int rows, cols, toroidal, tiles_x;
@@ -317,6 +320,20 @@ constexpr int C_TICKET = 32, C_ARRIVED = 64, C_ERROR = 96;
 /* the persistent kernel's placement census: a flag (own line) and blocks
  * per SM, for SM ids below MAX_SM */
 constexpr int C_PLACE_BAD = 128, C_SMRANK = 256, MAX_SM = 256;
+/* 64-bit counters (State::ctl), each on a 128-byte line of its own; the low
+ * 32 bits count appended items, the high 32 bits a barrier's arrivals:
+ *   W_TILES + 16 * parity   tiles flagged in a step (per-step launches)
+ *   W_LIST + 16 * parity    entries of a step's list (per-step launches)
+ *   W_PT + 16 * (s % 3)     step s of a persistent run: flagged tiles, then
+ *                           the arrivals at the barrier that ends its K1 phase
+ *   W_PL + 16 * (s % 3)     step s of a persistent run: entries of the next
+ *                           list, then the arrivals at the barrier that ends
+ *                           its K2 phase
+ * so that the poll that releases a barrier returns the count the next phase
+ * needs.  A persistent word is reused three steps later; block 0 clears it
+ * one step before its use, when every block has finished polling it. */
+constexpr int W_TILES = 0, W_LIST = 32, W_PT = 64, W_PL = 112, NCTL = 160;
+static __host__ __device__ __forceinline__ int low32(unsigned long long v) { return (int)(unsigned)(v & 0xffffffffull); }
 constexpr int K2_BLOCKS = 152 * 4;
 static int g_k1_blocks = 152 * 4, g_k2_blocks = K2_BLOCKS; /* launch grids of K1 and K2 (tunable) */
 
@@ -349,10 +366,10 @@ static __device__ __forceinline__ double ldh(const double* p)
 
 /* flag tile t for this step's K2 and append it to the work-list once */
 template <bool CO>
-static __device__ __forceinline__ void flag_tile(int* tflag, int* tlist, int* tcount, int t, int epoch)
+static __device__ __forceinline__ void flag_tile(int* tflag, int* tlist, unsigned long long* tcount, int t, int epoch)
 {
     if (ldm<CO>(tflag + t) != epoch && atomicExch(tflag + t, epoch) != epoch)
-        tlist[atomicAdd(tcount, 1)] = t;
+        tlist[low32(atomicAdd(tcount, 1ull))] = t;
 }
 
 /* flag tile t for the lanes where `want` holds, once per distinct tile among
@@ -360,8 +377,8 @@ static __device__ __forceinline__ void flag_tile(int* tflag, int* tlist, int* tc
  * a tile, so the warp's leader for each tile does the (idempotent) flag
  * and the others skip its load and atomic */
 template <bool CO>
-static __device__ __forceinline__ void flag_tile_warp(bool want, int t, int* tflag, int* tlist, int* tcount,
-                                                      int epoch)
+static __device__ __forceinline__ void flag_tile_warp(bool want, int t, int* tflag, int* tlist,
+                                                      unsigned long long* tcount, int epoch)
 {
     const unsigned act = __activemask();
     const unsigned peers = __match_any_sync(act, want ? t : -1);
@@ -369,16 +386,24 @@ static __device__ __forceinline__ void flag_tile_warp(bool want, int t, int* tfl
         flag_tile<CO>(tflag, tlist, tcount, t, epoch);
 }
 
-/* K1's work: the outflows of every listed wet cell (threads tid, tid +
- * nthreads, ...) and the clearing of the dried cells' outflows */
+/* K1's work on the step's list (threads tid, tid + nthreads, ...): the
+ * outflows of every wet cell (entry c >= 0) and the clearing of the outflows
+ * of every cell that dried in the previous step (entry ~c) */
 template <bool CO>
-static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int epoch, int nw, int nz, int* tcount,
-                                               int tid, int nthreads)
+static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int epoch, int nlist,
+                                               unsigned long long* tcount, int tid, int nthreads)
 {
     const int* list = par ? p.list1 : p.list0;
-    const int* zlist = par ? p.zlist1 : p.zlist0;
-    for (int k = tid; k < nw; k += nthreads) {
-        const int c = ldm<CO>(list + k);
+    for (int k = tid; k < nlist; k += nthreads) {
+        const int e = ldm<CO>(list + k);
+        if (e < 0) {
+            const long long c = ~e;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                p.f[q * p.n + c] = 0.0;
+            continue;
+        }
+        const int c = e;
         const int i = c / p.cols, j = c - i * p.cols;
         /* neighbours in von Neumann order n = 1..4: north, west, east, south */
         int ni[4] = {i - 1, i, i, i + 1}, nj[4] = {j, j - 1, j + 1, j};
@@ -397,14 +422,15 @@ static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int e
             ni[q] = a;
             nj[q] = b;
             if (in[q]) {
-                const long long cn = (long long)a * p.cols + b;
-                u[q] = __ldg(p.z + cn) + ldh<CO>(p.h + cn);
+                /* z + h of the neighbour, as K2 (or the priming) computed it
+                 * from the same operands */
+                u[q] = ldh<CO>(p.zh + (long long)a * p.cols + b);
             } else {
                 u[q] = 0.0 + 0.0; /* an absent neighbour reads z = 0, h = 0 */
             }
         }
         double f[4];
-        sdt::outflows(ldh<CO>(p.h + c), __ldg(p.z + c), u[0], u[1], u[2], u[3], p.eps, p.r, f);
+        sdt::outflows_u0(ldh<CO>(p.h + c), __ldg(p.zeps + c), u[0], u[1], u[2], u[3], p.eps, p.r, f);
         bool any = false;
         const int own = tile_of(i, j, p.tiles_x);
 #pragma unroll
@@ -423,15 +449,6 @@ static __device__ __forceinline__ void k1_work(const K1Params& p, int par, int e
         }
         flag_tile_warp<CO>(any, own, p.tflag, p.tlist, tcount, epoch);
     }
-    /* the dried cells from the other end of the thread range: threads
-     * nthreads - 1, nthreads - 2, ... (a bijection, each entry once), so that
-     * this work lands on threads the wet list leaves idle */
-    for (int k = nthreads - 1 - tid; k < nz; k += nthreads) {
-        const int c = ldm<CO>(zlist + k);
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            p.f[q * p.n + c] = 0.0;
-    }
 }
 
 __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant__ K1Params p)
@@ -439,21 +456,28 @@ __global__ void __launch_bounds__(K1_THREADS) k1_outflows(const __grid_constant_
     const bool host = p.hpar >= 0;
     const int par = host ? p.hpar : p.counts[4];
     const int epoch = host ? p.hepoch : p.counts[6];
-    if (blockIdx.x == 0 && threadIdx.x < 3) {
-        if (threadIdx.x < 2)
-            p.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists K2 will append to */
+    if (blockIdx.x == 0 && threadIdx.x < 2) {
+        if (threadIdx.x == 0)
+            p.ctl[W_LIST + 16 * (1 - par)] = 0; /* the list K2 will append to */
         else
-            p.counts[7 + (1 - par)] = 0; /* next step's tile count (read last by the previous K2) */
+            p.ctl[W_TILES + 16 * (1 - par)] = 0; /* next step's tile count (read last by the previous K2) */
     }
     /* list entries in chunks of 32 (one per warp); consecutive chunks on
      * consecutive blocks, which the hardware places on different SMs */
     const int tid = ((threadIdx.x >> 5) * (int)gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);
-    k1_work<false>(p, par, epoch, p.counts[par], p.counts[2 + par], p.counts + 7 + par, tid,
+    k1_work<false>(p, par, epoch, low32(p.ctl[W_LIST + 16 * par]), p.ctl + W_TILES + 16 * par, tid,
                    gridDim.x * blockDim.x);
 }
 
-/* append the lanes whose predicate holds to list/count (warp-aggregated) */
-static __device__ __forceinline__ void warp_append(bool pred, int value, int* list, int* count)
+/* append the lanes whose predicate holds to list/count (warp-aggregated);
+ * a 64-bit counter counts in its low 32 bits */
+static __device__ __forceinline__ int count_add(int* count, int v) { return atomicAdd(count, v); }
+static __device__ __forceinline__ int count_add(unsigned long long* count, int v)
+{
+    return low32(atomicAdd(count, (unsigned long long)v));
+}
+template <typename C>
+static __device__ __forceinline__ void warp_append(bool pred, int value, int* list, C* count)
 {
     const unsigned mask = __ballot_sync(0xffffffffu, pred);
     if (mask == 0)
@@ -461,16 +485,17 @@ static __device__ __forceinline__ void warp_append(bool pred, int value, int* li
     const int lane = threadIdx.x & 31;
     int base = 0;
     if (lane == 0)
-        base = atomicAdd(count, __popc(mask));
+        base = count_add(count, __popc(mask));
     base = __shfl_sync(0xffffffffu, base, 0);
     if (pred)
         list[base + __popc(mask & ((1u << lane) - 1u))] = value;
 }
 
-/* Block-wide append of up to 4 items per thread to two lists, one atomicAdd
- * per list per block.  want[q] / dried[q]: item q goes to list / zlist. */
+/* Block-wide append of up to 4 items per thread to the next list, one
+ * atomicAdd per block: item q as value[q] when want[q] (a wet cell) and as
+ * ~value[q] when dried[q] (a cell whose outflows K1 must clear). */
 static __device__ __forceinline__ void block_append4(const bool want[4], const bool dried[4], const int value[4],
-                                                     int* list, int* count, int* zlist, int* zcount)
+                                                     int* list, unsigned long long* count)
 {
     __shared__ int s_warp[2][THREADS / 32];
     __shared__ int s_base[2];
@@ -490,11 +515,15 @@ static __device__ __forceinline__ void block_append4(const bool want[4], const b
         s_warp[1][warp] = nd;
     }
     __syncthreads();
-    if (threadIdx.x < 2) {
-        int tot = 0;
-        for (int w = 0; w < THREADS / 32; w++)
-            tot += s_warp[threadIdx.x][w];
-        s_base[threadIdx.x] = tot ? atomicAdd(threadIdx.x == 0 ? count : zcount, tot) : 0;
+    if (threadIdx.x == 0) {
+        int tw = 0, td = 0;
+        for (int w = 0; w < THREADS / 32; w++) {
+            tw += s_warp[0][w];
+            td += s_warp[1][w];
+        }
+        const int base = (tw + td) ? count_add(count, tw + td) : 0;
+        s_base[0] = base;      /* wet entries first, */
+        s_base[1] = base + tw; /* then the dried ones */
     }
     __syncthreads();
     int bw = s_base[0], bd = s_base[1];
@@ -507,7 +536,7 @@ static __device__ __forceinline__ void block_append4(const bool want[4], const b
         if (want[q])
             list[bw + __popc(mw[q] & below)] = value[q];
         if (dried[q])
-            zlist[bd + __popc(md[q] & below)] = value[q];
+            list[bd + __popc(md[q] & below)] = ~value[q];
         bw += __popc(mw[q]);
         bd += __popc(md[q]);
     }
@@ -515,8 +544,7 @@ static __device__ __forceinline__ void block_append4(const bool want[4], const b
 
 /* one flagged tile: h += inflows - outflows in place, then the wet test */
 template <bool CO>
-static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int* list, int* count, int* zlist,
-                                               int* zcount)
+static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int* list, unsigned long long* count)
 {
     const int ty = tile / p.tiles_x, tx = tile - ty * p.tiles_x;
     /* CPT consecutive cells of a row per thread: 4 when the tile has 4
@@ -593,6 +621,7 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
                 x += in4 - o3;
                 hn = x;
                 p.h[c] = x;
+                p.zh[c] = __ldg(p.z + c) + x; /* the u K1 will read next step */
             }
         }
         const bool wb = cell[q] && sdt::is_wet(hv[q], p.eps_bits);
@@ -600,34 +629,33 @@ static __device__ __forceinline__ void k2_tile(const K2Params& p, int tile, int*
         dried[q] = wb && !want[q];
         value[q] = (int)c;
     }
-    block_append4(want, dried, value, list, count, zlist, zcount);
+    block_append4(want, dried, value, list, count);
 }
 
 /* K2's work for blocks block, block + nblocks, ...: the flagged tiles, then
  * the current wet list in chunks of THREADS entries (carrying over the wet
  * cells of unflagged tiles, whose h did not change) */
 template <bool CO>
-static __device__ __forceinline__ void k2_work(const K2Params& p, int par, int epoch, int ntiles, int nwet, int block,
-                                               int nblocks)
+static __device__ __forceinline__ void k2_work(const K2Params& p, int par, int epoch, int ntiles, int nlist,
+                                               unsigned long long* count, int block, int nblocks)
 {
     const int* cur = par ? p.list1 : p.list0;
-    int* list = par ? p.list0 : p.list1; /* next step's lists */
-    int* zlist = par ? p.zlist0 : p.zlist1;
-    int* count = p.counts + (1 - par);
-    int* zcount = p.counts + 2 + (1 - par);
-    const int items = ntiles + (nwet + THREADS - 1) / THREADS;
+    int* list = par ? p.list0 : p.list1; /* next step's list */
+    const int items = ntiles + (nlist + THREADS - 1) / THREADS;
     for (int item = block; item < items; item += nblocks) {
         if (item < ntiles) {
-            k2_tile<CO>(p, ldm<CO>(p.tlist + item), list, count, zlist, zcount);
+            k2_tile<CO>(p, ldm<CO>(p.tlist + item), list, count);
             __syncthreads(); /* block_append4's shared words are reused */
         } else {
             const int k = (item - ntiles) * THREADS + threadIdx.x;
             bool carry = false;
             int c = 0;
-            if (k < nwet) {
+            if (k < nlist) {
                 c = ldm<CO>(cur + k);
-                const int i = c / p.cols, j = c - i * p.cols;
-                carry = ldm<CO>(p.tflag + tile_of(i, j, p.tiles_x)) != epoch;
+                if (c >= 0) { /* a dried entry's outflows were cleared this step */
+                    const int i = c / p.cols, j = c - i * p.cols;
+                    carry = ldm<CO>(p.tflag + tile_of(i, j, p.tiles_x)) != epoch;
+                }
             }
             warp_append(carry, c, list, count);
         }
@@ -639,7 +667,8 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
     const bool host = p.hpar >= 0;
     const int par = host ? p.hpar : p.counts[4];
     const int epoch = host ? p.hepoch : p.counts[6];
-    k2_work<false>(p, par, epoch, p.counts[7 + par], p.counts[par], blockIdx.x, gridDim.x);
+    k2_work<false>(p, par, epoch, low32(p.ctl[W_TILES + 16 * par]), low32(p.ctl[W_LIST + 16 * par]),
+                   p.ctl + W_LIST + 16 * (1 - par), blockIdx.x, gridDim.x);
     if (host) {
         /* nobody reads the device words during this launch */
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -661,12 +690,13 @@ __global__ void __launch_bounds__(THREADS) k2_update(const __grid_constant__ K2P
 
 /* ---- persistent form: every step of a run in one cooperative launch ----
  * The two phases of each step (K1's and K2's work) are separated by a grid
- * barrier.  counts[7 + parity] counts the flagged tiles of the step (one
- * step's count is cleared while the other is in use); counts[C_ARRIVED] is
- * the barrier's arrival counter (zeroed before the launch), counts[C_ERROR]
- * the error flag.  Only one thread per block touches the shared words: it
- * arrives, waits, and reads the two counts the next phase needs into shared
- * memory, so that no L2 line is read by every thread of the grid. */
+ * barrier on the 64-bit word that counts what the phase appended (packed
+ * barrier below), so that the poll that ends the wait also returns the count
+ * the next phase needs.  counts[C_ARRIVED] is the arrival counter of the
+ * one-off barrier of the placement census (zeroed before the launch),
+ * counts[C_ERROR] the error flag.  Only one thread per block touches the
+ * shared words: it arrives, waits, and hands the count to its block through
+ * shared memory, so that no L2 line is read by every thread of the grid. */
 constexpr unsigned BARRIER_SPIN_LIMIT = 1u << 22;
 
 static __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p)
@@ -745,6 +775,48 @@ static __device__ int placement_order(int* counts, unsigned nb, int nsm, unsigne
     return vb;
 }
 
+static __device__ __forceinline__ unsigned long long ld_acquire_gpu_u64(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+/* Grid barrier on a counter word (W_PT / W_PL): every block adds one
+ * arrival to its high 32 bits after the phase's appends, which went to its
+ * low 32 bits; the barrier is complete when the arrivals reach nblocks, and
+ * the value that shows it carries the phase's final count (the appends of
+ * every block precede that block's arrival in the word's order), which
+ * thread 0 hands to the block in *out.  Bounded like grid_barrier: after
+ * BARRIER_SPIN_LIMIT polls the error flag is set and false returned; a
+ * block that gave up stops arriving, so the others give up at their next
+ * barrier. */
+static __device__ __forceinline__ bool packed_barrier(unsigned long long* word, unsigned nblocks, int* counts, int* out)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        atomicAdd(word, 1ull << 32);
+        unsigned polls = 0;
+        unsigned long long v;
+        while ((unsigned)((v = ld_acquire_gpu_u64(word)) >> 32) < nblocks) {
+            if (++polls > BARRIER_SPIN_LIMIT) {
+                atomicExch(counts + C_ERROR, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+        *out = low32(v);
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
 #ifndef SDT2_PERSIST_MINB
 #define SDT2_PERSIST_MINB 4 /* resident blocks per SM (5 measured slower: 78.4 against 72.8 ms per run) */
 #endif
@@ -752,7 +824,7 @@ __global__ void __launch_bounds__(THREADS, SDT2_PERSIST_MINB) k_persist(const __
                                                      const __grid_constant__ K2Params b, int nsteps, int nsm)
 {
     __shared__ int s_cnt[2];
-    __shared__ int s_state[2];
+    __shared__ int s_state[3];
     const unsigned nb = gridDim.x;
     unsigned round = 0;
     const int vb = placement_order(a.counts, nb, nsm, round, s_cnt);
@@ -761,60 +833,68 @@ __global__ void __launch_bounds__(THREADS, SDT2_PERSIST_MINB) k_persist(const __
     if (threadIdx.x == 0) {
         s_state[0] = __ldcg(a.counts + 4);
         s_state[1] = __ldcg(a.counts + 6);
+        s_state[2] = low32(__ldcg(a.ctl + W_LIST + 16 * s_state[0]));
     }
     __syncthreads();
     int par = s_state[0];
     int epoch = s_state[1];
-    if (threadIdx.x == 0) {
-        s_cnt[0] = __ldcg(a.counts + par);
-        s_cnt[1] = __ldcg(a.counts + 2 + par);
-    }
-    __syncthreads();
+    int nlist = s_state[2]; /* entries of the current step's list */
     /* K1's list entries in chunks of 32 (one per warp), consecutive chunks
      * on consecutive blocks in the order v, so that the wet cells' FP64 work
      * spreads over every SM whatever their number */
     const int tid = ((threadIdx.x >> 5) * (int)nb + vb) * 32 + (threadIdx.x & 31);
     for (int s = 0; s < nsteps; s++) {
-        int* tcount = a.counts + 7 + par;
-        if (blockIdx.x == 0 && threadIdx.x < 3) {
-            if (threadIdx.x < 2)
-                a.counts[(1 - par) + 2 * threadIdx.x] = 0; /* the lists phase B appends to */
-            else
-                a.counts[7 + (1 - par)] = 0; /* next step's tile count (read last in step s - 1) */
+        const int w = 16 * (s % 3);
+        unsigned long long* tword = a.ctl + W_PT + w;
+        unsigned long long* lword = a.ctl + W_PL + w;
+        if (blockIdx.x == 0 && threadIdx.x < 2) {
+            /* the words of step s + 1, last polled in step s - 2 */
+            const int wn = 16 * ((s + 1) % 3);
+            a.ctl[(threadIdx.x ? W_PL : W_PT) + wn] = 0;
         }
-        k1_work<true>(a, par, epoch, s_cnt[0], s_cnt[1], tcount, tid, nb * THREADS);
-        /* then: the flagged tiles of this step and the current wet count */
-        if (!grid_barrier(a.counts, nb, round, tcount, a.counts + par, s_cnt))
+        k1_work<true>(a, par, epoch, nlist, tword, tid, nb * THREADS);
+        /* then: the flagged tiles of this step */
+        if (!packed_barrier(tword, nb, a.counts, s_cnt))
             return;
-        k2_work<true>(b, par, epoch, s_cnt[0], s_cnt[1], vb, nb);
+        k2_work<true>(b, par, epoch, s_cnt[0], nlist, lword, vb, nb);
         par = 1 - par;
         epoch++;
-        /* then: the next step's wet and dried counts */
-        if (!grid_barrier(a.counts, nb, round, a.counts + par, a.counts + 2 + par, s_cnt))
+        /* then: the entries of the next step's list */
+        if (!packed_barrier(lword, nb, a.counts, s_cnt + 1))
             return;
+        nlist = s_cnt[1];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         /* the state the per-step kernels expect */
         a.counts[4] = par;
         a.counts[C_TICKET] = 0;
         a.counts[6] = epoch;
-        a.counts[7] = 0;
-        a.counts[8] = 0;
+        a.ctl[W_LIST + 16 * par] = (unsigned long long)(unsigned)nlist;
+        a.ctl[W_TILES] = 0;
+        a.ctl[W_TILES + 16] = 0;
     }
 }
 
-/* -0 -> +0 in h and the first wet list (counts[parity] must be 0) */
-__global__ void __launch_bounds__(THREADS) k_prime(double* h, long long n, long long eps_bits, int* list, int* count)
+/* -0 -> +0 in h, z + h and z + eps of every cell, and the first wet list
+ * (its counter must be 0) */
+__global__ void __launch_bounds__(THREADS) k_prime(double* h, const double* __restrict__ z, double* zh, double* zeps,
+                                                  double eps, long long n, long long eps_bits, int* list,
+                                                  unsigned long long* count, int* counts)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0)
-        count[6] = 1; /* first epoch (tile stamps start at 0) */
+        counts[6] = 1; /* first epoch (tile stamps start at 0) */
     for (long long c0 = (long long)blockIdx.x * blockDim.x; c0 < n; c0 += (long long)gridDim.x * blockDim.x) {
         const long long c = c0 + threadIdx.x;
         bool wet = false;
         if (c < n) {
-            const double hv = h[c];
-            if (__double_as_longlong(hv) == (long long)0x8000000000000000ULL)
+            double hv = h[c];
+            if (__double_as_longlong(hv) == (long long)0x8000000000000000ULL) {
+                hv = 0.0;
                 h[c] = 0.0;
+            }
+            const double zv = z[c];
+            zh[c] = zv + hv;
+            zeps[c] = zv + eps;
             wet = sdt::is_wet(hv, eps_bits);
         }
         warp_append(wet, (int)c, list, count);
@@ -827,18 +907,19 @@ static void release()
 {
     State& s = g_state;
     cudaFree(s.f);
-    for (int k = 0; k < 2; k++) {
+    cudaFree(s.zh);
+    cudaFree(s.zeps);
+    for (int k = 0; k < 2; k++)
         cudaFree(s.list[k]);
-        cudaFree(s.zlist[k]);
-    }
     cudaFree(s.counts);
+    cudaFree(s.ctl);
     cudaFree(s.tflag);
     cudaFree(s.tlist);
     s = State();
 }
 
-/* (re)allocate for `ca` and prime from the current h */
-static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStream_t st)
+/* (re)allocate for `ca` and prime from the current h and z */
+static bool prime(struct CALModel2D* ca, double* h, const double* z, double eps, long long eps_bits, cudaStream_t st)
 {
     State& s = g_state;
     const long long n = (long long)ca->rows * ca->columns;
@@ -849,24 +930,27 @@ static bool prime(struct CALModel2D* ca, double* h, long long eps_bits, cudaStre
         s.tiles_x = (ca->columns + TW - 1) / TW;
         s.tiles_y = (ca->rows + TH - 1) / TH;
         bool ok = cudaMalloc(&s.f, 4 * n * sizeof(double)) == cudaSuccess &&
+                  cudaMalloc(&s.zh, n * sizeof(double)) == cudaSuccess &&
+                  cudaMalloc(&s.zeps, n * sizeof(double)) == cudaSuccess &&
                   cudaMalloc(&s.counts, NCOUNTS * sizeof(int)) == cudaSuccess &&
+                  cudaMalloc(&s.ctl, NCTL * sizeof(unsigned long long)) == cudaSuccess &&
                   cudaMalloc(&s.tflag, sizeof(int) * s.tiles_x * s.tiles_y) == cudaSuccess &&
                   cudaMalloc(&s.tlist, sizeof(int) * s.tiles_x * s.tiles_y) == cudaSuccess;
         for (int k = 0; k < 2 && ok; k++)
-            ok = cudaMalloc(&s.list[k], n * sizeof(int)) == cudaSuccess &&
-                 cudaMalloc(&s.zlist[k], n * sizeof(int)) == cudaSuccess;
+            ok = cudaMalloc(&s.list[k], n * sizeof(int)) == cudaSuccess;
         if (!ok) {
             release();
             return false;
         }
     }
     cudaMemsetAsync(s.f, 0, 4 * n * sizeof(double), st);
-    cudaMemsetAsync(s.counts, 0, NCOUNTS * sizeof(int), st); /* parity 0, tickets 0, no flagged tile */
+    cudaMemsetAsync(s.counts, 0, NCOUNTS * sizeof(int), st); /* parity 0, tickets 0 */
+    cudaMemsetAsync(s.ctl, 0, NCTL * sizeof(unsigned long long), st); /* empty lists, no flagged tile */
     cudaMemsetAsync(s.tflag, 0, sizeof(int) * s.tiles_x * s.tiles_y, st);
     int blocks = (int)((n + THREADS - 1) / THREADS);
     if (blocks > 152 * 16)
         blocks = 152 * 16;
-    k_prime<<<blocks, THREADS, 0, st>>>(h, n, eps_bits, s.list[0], s.counts + 0);
+    k_prime<<<blocks, THREADS, 0, st>>>(h, z, s.zh, s.zeps, eps, n, eps_bits, s.list[0], s.ctl + W_LIST, s.counts);
     s.primed = true;
     s.hpar = 0; /* what k_prime leaves: parity 0, epoch 1 */
     s.hepoch = 1;
@@ -882,12 +966,13 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     K1Params a;
     a.z = z;
     a.h = h;
+    a.zh = s.zh;
+    a.zeps = s.zeps;
     a.f = s.f;
     a.list0 = s.list[0];
     a.list1 = s.list[1];
-    a.zlist0 = s.zlist[0];
-    a.zlist1 = s.zlist[1];
     a.counts = s.counts;
+    a.ctl = s.ctl;
     a.tflag = s.tflag;
     a.tlist = s.tlist;
     a.rows = ca->rows;
@@ -899,12 +984,13 @@ static bool step(struct CALModel2D* ca, const double* z, double* h, double eps, 
     a.r = r;
     K2Params b;
     b.h = h;
+    b.zh = s.zh;
+    b.z = z;
     b.f = s.f;
     b.list0 = s.list[0];
     b.list1 = s.list[1];
-    b.zlist0 = s.zlist[0];
-    b.zlist1 = s.zlist[1];
     b.counts = s.counts;
+    b.ctl = s.ctl;
     b.tflag = s.tflag;
     b.tlist = s.tlist;
     b.rows = ca->rows;
@@ -978,12 +1064,13 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
     K2Params b;
     a.z = z;
     a.h = h;
+    a.zh = s.zh;
+    a.zeps = s.zeps;
     a.f = s.f;
     a.list0 = b.list0 = s.list[0];
     a.list1 = b.list1 = s.list[1];
-    a.zlist0 = b.zlist0 = s.zlist[0];
-    a.zlist1 = b.zlist1 = s.zlist[1];
     a.counts = b.counts = s.counts;
+    a.ctl = b.ctl = s.ctl;
     a.tflag = s.tflag;
     b.tflag = s.tflag;
     a.tlist = s.tlist;
@@ -996,13 +1083,16 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
     a.eps = eps;
     a.r = r;
     b.h = h;
+    b.zh = s.zh;
+    b.z = z;
     b.f = s.f;
     b.eps_bits = eps_bits;
     a.hpar = b.hpar = -1;
     a.hepoch = b.hepoch = 0;
-    cudaMemsetAsync(s.counts + C_ARRIVED, 0, sizeof(int), st); /* barrier counter */
+    cudaMemsetAsync(s.counts + C_ARRIVED, 0, sizeof(int), st); /* placement barrier counter */
     cudaMemsetAsync(s.counts + C_ERROR, 0, sizeof(int), st);   /* error flag */
     cudaMemsetAsync(s.counts + C_PLACE_BAD, 0, (NCOUNTS - C_PLACE_BAD) * sizeof(int), st); /* placement census */
+    cudaMemsetAsync(s.ctl + W_PT, 0, (NCTL - W_PT) * sizeof(unsigned long long), st); /* the steps' counters */
     int nsm = sms_of_device;
     void* args[] = {&a, &b, &nsteps, &nsm};
     return cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(THREADS), args, 0, st) ==
@@ -1013,18 +1103,33 @@ static bool persist(struct CALModel2D* ca, const double* z, double* h, double ep
  * block): the mass that left the grid in step t (the step's outflows of
  * border cells towards absent neighbours: f[0] north of row 0, f[3] south of
  * the last row, f[1] west of column 0, f[2] east of the last column; K2 does
- * not change f), the step's wet-cell count (K2 has advanced the parity word,
- * so the step's list is the other one), and whether a cell of the two-cell
- * edge band holds h != 0 after the step (atomicMin of t + 1 into *edge).
- * Needs rows, cols >= 5. */
+ * not change f), the step's wet-cell count (the entries c >= 0 of its list;
+ * K2 has advanced the parity word, so the step's list is the other one),
+ * and whether a cell of the two-cell edge band holds h != 0 after the step
+ * (atomicMin of t + 1 into *edge).  Needs rows, cols >= 5. */
 __global__ void __launch_bounds__(THREADS) k_trace(const double* __restrict__ f, const double* __restrict__ h,
-                                                  const int* __restrict__ counts, int rows, int cols, long long n,
-                                                  int t, double* outflux, int* wet, int* edge)
+                                                  const int* __restrict__ counts,
+                                                  const unsigned long long* __restrict__ ctl, const int* list0,
+                                                  const int* list1, int rows, int cols, long long n, int t,
+                                                  double* outflux, int* wet, int* edge)
 {
     __shared__ double s_part[THREADS / 32];
     __shared__ int s_any;
-    if (threadIdx.x == 0)
+    __shared__ int s_wet;
+    if (threadIdx.x == 0) {
         s_any = 0;
+        s_wet = 0;
+    }
+    __syncthreads();
+    {
+        const int par = 1 - counts[4];
+        const int* list = par ? list1 : list0;
+        const int nlist = low32(ctl[W_LIST + 16 * par]);
+        int mine = 0;
+        for (int k = threadIdx.x; k < nlist; k += THREADS)
+            mine += list[k] >= 0;
+        atomicAdd(&s_wet, mine);
+    }
     double s = 0.0;
     for (int j = threadIdx.x; j < cols; j += THREADS)
         s += f[j];
@@ -1061,7 +1166,7 @@ __global__ void __launch_bounds__(THREADS) k_trace(const double* __restrict__ f,
         for (int w = 0; w < THREADS / 32; w++)
             tot += s_part[w];
         outflux[t] = tot;
-        wet[t] = counts[1 - counts[4]];
+        wet[t] = s_wet;
         if (s_any)
             atomicMin(edge, t + 1);
     }
@@ -1852,7 +1957,8 @@ static void sciddicaT_split_prepare_now(struct CALModel2D* ca)
         return;
     long long eps_bits;
     memcpy(&eps_bits, &P.epsilon, sizeof(double));
-    sdt2::prime(ca, (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0), eps_bits, (cudaStream_t)calGetStream2D(ca));
+    sdt2::prime(ca, (double*)calGetDeviceBuffer2Dr(ca, Q.h, 0), (const double*)calGetDeviceBuffer2Dr(ca, Q.z, 0),
+                P.epsilon, eps_bits, (cudaStream_t)calGetStream2D(ca));
 }
 
 /* prime the selected plain-mode step now if its next step would: keeps the
@@ -2363,13 +2469,22 @@ extern "C" int cal_sciddicaT_kernel_times(void* handle, int n, float* ms_a, floa
 extern "C" int cal_sciddicaT_wet_count(void* handle)
 {
     SdtSession* s = (SdtSession*)handle;
-    int c[6] = {-1, -1, -1, -1, 0, 0};
-    if (sdt2::g_state.counts) {
-        /* the model's stream does not synchronise with the legacy stream */
-        cudaStreamSynchronize((cudaStream_t)calGetStream2D(s->ca));
-        cudaMemcpy(c, sdt2::g_state.counts, sizeof(c), cudaMemcpyDeviceToHost);
-    }
-    return c[c[4] & 1];
+    if (!sdt2::g_state.counts)
+        return -1;
+    /* the model's stream does not synchronise with the legacy stream */
+    cudaStreamSynchronize((cudaStream_t)calGetStream2D(s->ca));
+    int c[6] = {0, 0, 0, 0, 0, 0};
+    cudaMemcpy(c, sdt2::g_state.counts, sizeof(c), cudaMemcpyDeviceToHost);
+    const int par = c[4] & 1;
+    unsigned long long w = 0;
+    cudaMemcpy(&w, sdt2::g_state.ctl + sdt2::W_LIST + 16 * par, sizeof(w), cudaMemcpyDeviceToHost);
+    std::vector<int> list(sdt2::low32(w));
+    if (!list.empty())
+        cudaMemcpy(list.data(), sdt2::g_state.list[par], list.size() * sizeof(int), cudaMemcpyDeviceToHost);
+    int wet = 0;
+    for (int e : list)
+        wet += e >= 0;
+    return wet;
 }
 
 extern "C" int cal_sciddicaT_read(void* handle, double* h_out)
@@ -2418,8 +2533,9 @@ extern "C" int cal_sciddicaT_trace(void* handle, int steps, double* outflux, int
     for (int t = 0; t < steps; t++) {
         if (!sdt2::step(ca, z, h, P.epsilon, P.r, eps_bits, st, nullptr))
             break;
-        sdt2::k_trace<<<1, sdt2::THREADS, 0, st>>>(sdt2::g_state.f, h, sdt2::g_state.counts, ca->rows, ca->columns,
-                                                   sdt2::g_state.n, t, d_out, d_wet, d_edge);
+        sdt2::k_trace<<<1, sdt2::THREADS, 0, st>>>(sdt2::g_state.f, h, sdt2::g_state.counts, sdt2::g_state.ctl,
+                                                   sdt2::g_state.list[0], sdt2::g_state.list[1], ca->rows,
+                                                   ca->columns, sdt2::g_state.n, t, d_out, d_wet, d_edge);
     }
     calMarkCurrentWritten2Dr(ca, Q.h);
     int edge = never;

@@ -49,13 +49,26 @@ static __device__ __forceinline__ bool is_wet(double h, long long eps_bits)
  * the same additions in the same order; the division by the number of
  * remaining cells and the comparisons are done on the integer pipe with
  * bit-identical results (exact_div.cuh). */
+static __device__ __forceinline__ void outflows_u0(double hc, double u0, const double u1, const double u2,
+                                                   const double u3, const double u4, double eps, double r,
+                                                   double f[4], unsigned* elim_out = nullptr);
+
 static __device__ __forceinline__ void outflows(double hc, double zc, const double u1, const double u2,
                                                 const double u3, const double u4, double eps, double r, double f[4],
                                                 unsigned* elim_out = nullptr)
 {
+    outflows_u0(hc, zc + eps, u1, u2, u3, u4, eps, r, f, elim_out);
+}
+
+/* the same with u[0] = z + eps of the cell given (a caller that keeps it
+ * per cell saves the addition) */
+static __device__ __forceinline__ void outflows_u0(double hc, double u0, const double u1, const double u2,
+                                                   const double u3, const double u4, double eps, double r,
+                                                   double f[4], unsigned* elim_out)
+{
     double u[5];
     const double m = hc - eps;
-    u[0] = zc + eps;
+    u[0] = u0;
     u[1] = u1;
     u[2] = u2;
     u[3] = u3;
