@@ -2013,6 +2013,11 @@ static void sciddicaT_fused_transition(struct CALModel2D* ca)
 static void sciddicaT_simulation_init_fused(struct CALModel2D* sciddicaT)
 {
     sciddicaT_simulation_init(sciddicaT);
+    /* the init's z -= h is in the next layer until the run's update; the
+     * split step's priming reads z (z + h, z + epsilon per cell), so the
+     * update runs here (the run's own update after the init then finds
+     * nothing written and copies nothing) */
+    calUpdate2D(sciddicaT);
     sciddicaT_step_invalidate();
     sciddicaT_step_prepare(sciddicaT);
 }
