@@ -92,9 +92,28 @@ __device__ __forceinline__ bool cal_same_bits<double>(double a, double b)
     return __double_as_longlong(a) == __double_as_longlong(b);
 }
 
+/* The model a device process receives is a copy of the descriptor's public
+ * part made by the kernel (cal_model_view2D): its `gpu` field points at the
+ * launch descriptor, where the accessors find the buffers. */
 static __device__ __forceinline__ const struct CALDevModel2D* cal_dm2D(const struct CALModel2D* ca)
 {
-    return reinterpret_cast<const struct CALDevModel2D*>(ca);
+    return reinterpret_cast<const struct CALDevModel2D*>(ca->gpu);
+}
+
+/* The kernel-local model handed to user code.  NX > 0: the launch is for a
+ * model whose neighbourhood has NX cells, and the copy says so as a
+ * compile-time constant, so that a process's loops over ca->sizeof_X have a
+ * fixed count and arrays indexed by the neighbour (u[n], eliminated[n], ...)
+ * live in registers instead of local memory.  The copy is only read; once
+ * the process is inlined its fields are the descriptor's, in registers. */
+template <int NX>
+static __device__ __forceinline__ struct CALModel2D cal_model_view2D(const struct CALDevModel2D& m)
+{
+    struct CALModel2D v = m.model;
+    if (NX > 0)
+        v.sizeof_X = NX;
+    v.gpu = reinterpret_cast<struct CALGpuModel2D*>(const_cast<struct CALDevModel2D*>(&m));
+    return v;
 }
 
 static __device__ __forceinline__ int cal_slot2D(const struct CALDevModel2D* m, int t, const void* q)
@@ -229,7 +248,7 @@ static __device__ __forceinline__ int calGetActiveCellCountDevice2D(const struct
  * each warp then adds its tile to the chg bitmap of every substate whose
  * next layer it changed.  At the end each block publishes which substates
  * it wrote (and which it wrote by unsafe operations). */
-template <void (*EP)(struct CALModel2D*, int, int)>
+template <void (*EP)(struct CALModel2D*, int, int), int NX>
 __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_constant__ struct CALDevModel2D m)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -240,7 +259,8 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     for (int t = lane; t < 3 * CAL_MAX_SUBSTATES; t += 32)
         cal_chg2D[warp][t] = 0;
     __syncthreads();
-    struct CALModel2D* ca = const_cast<struct CALModel2D*>(&m.model);
+    struct CALModel2D view = cal_model_view2D<NX>(m);
+    struct CALModel2D* ca = &view;
     const int listed = m.use_list ? *m.count : 0;
     const int nblocks = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
     if (listed > 0) {
@@ -276,10 +296,19 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     }
 }
 
+/* one kernel per common neighbourhood size (von Neumann 5, hexagonal 7,
+ * Moore 9) and a generic one for the others */
 template <void (*EP)(struct CALModel2D*, int, int)>
 static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* stream)
 {
-    cal_ep2D_kernel<EP><<<dim3(gx, gy), CAL_EP_THREADS, 0, (cudaStream_t)stream>>>(*m);
+    const dim3 grid(gx, gy);
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (m->model.sizeof_X) {
+    case 5: cal_ep2D_kernel<EP, 5><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+    case 7: cal_ep2D_kernel<EP, 7><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+    case 9: cal_ep2D_kernel<EP, 9><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+    default: cal_ep2D_kernel<EP, 0><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+    }
     return (int)cudaGetLastError();
 }
 
@@ -298,8 +327,8 @@ template <CALbyte (*STOP)(struct CALModel2D*)>
 __global__ void cal_stop2D_kernel(const __grid_constant__ struct CALDevModel2D m, cudaGraphConditionalHandle h,
                                   int use_handle, int final_step, int* flag)
 {
-    struct CALModel2D* ca = const_cast<struct CALModel2D*>(&m.model);
-    const bool stop = STOP(ca) != 0;
+    struct CALModel2D view = cal_model_view2D<0>(m);
+    const bool stop = STOP(&view) != 0;
     int again = 0;
     if (!stop) {
         const int next = *m.step + 1;

@@ -42,9 +42,23 @@ struct CALDevModel3D {
 
 static __shared__ unsigned char cal_written3D[3 * CAL_MAX_SUBSTATES];
 
+/* A device process receives a kernel-local copy of the model's public part
+ * (cal_model_view3D) whose `gpu` field points at the launch descriptor. */
 static __device__ __forceinline__ const struct CALDevModel3D* cal_dm3D(const struct CALModel3D* ca)
 {
-    return reinterpret_cast<const struct CALDevModel3D*>(ca);
+    return reinterpret_cast<const struct CALDevModel3D*>(ca->gpu);
+}
+
+/* NX > 0: the neighbourhood's size as a compile-time constant (fixed-count
+ * loops over ca->sizeof_X, per-neighbour arrays in registers) */
+template <int NX>
+static __device__ __forceinline__ struct CALModel3D cal_model_view3D(const struct CALDevModel3D& m)
+{
+    struct CALModel3D v = m.model;
+    if (NX > 0)
+        v.sizeof_X = NX;
+    v.gpu = reinterpret_cast<struct CALGpuModel3D*>(const_cast<struct CALDevModel3D*>(&m));
+    return v;
 }
 
 static __device__ __forceinline__ int cal_slot3D(const struct CALDevModel3D* m, int t, const void* q)
@@ -162,8 +176,8 @@ template <CALbyte (*STOP)(struct CALModel3D*)>
 __global__ void cal_stop3D_kernel(const __grid_constant__ struct CALDevModel3D m, cudaGraphConditionalHandle h,
                                   int use_handle, int final_step, int* flag)
 {
-    struct CALModel3D* ca = const_cast<struct CALModel3D*>(&m.model);
-    const bool stop = STOP(ca) != 0;
+    struct CALModel3D view = cal_model_view3D<0>(m);
+    const bool stop = STOP(&view) != 0;
     int again = 0;
     if (!stop) {
         const int next = *m.step + 1;
@@ -202,13 +216,14 @@ static int cal_launch_stop3D(const struct CALDevModel3D* m, unsigned long long h
 
 /* one elementary process over every cell (lines of j for each (k, i)) or
  * over the active list when it is non-empty (cal3D.c:658-674) */
-template <void (*EP)(struct CALModel3D*, int, int, int)>
+template <void (*EP)(struct CALModel3D*, int, int, int), int NX>
 __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep3D_kernel(const __grid_constant__ struct CALDevModel3D m)
 {
     for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x)
         cal_written3D[t] = 0;
     __syncthreads();
-    struct CALModel3D* ca = const_cast<struct CALModel3D*>(&m.model);
+    struct CALModel3D view = cal_model_view3D<NX>(m);
+    struct CALModel3D* ca = &view;
     const int listed = m.use_list ? *m.count : 0;
     if (listed > 0) {
         const int stride = gridDim.x * gridDim.y * blockDim.x;
@@ -230,10 +245,18 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep3D_kernel(const __grid_c
             atomicOr(&m.dirty[t / CAL_MAX_SUBSTATES], 1u << (t % CAL_MAX_SUBSTATES));
 }
 
+/* one kernel per common neighbourhood size (von Neumann 7, Moore 27) and
+ * a generic one for the others */
 template <void (*EP)(struct CALModel3D*, int, int, int)>
 static int cal_launch_ep3D(const struct CALDevModel3D* m, int gx, int gy, void* stream)
 {
-    cal_ep3D_kernel<EP><<<dim3(gx, gy), CAL_EP_THREADS, 0, (cudaStream_t)stream>>>(*m);
+    const dim3 grid(gx, gy);
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (m->model.sizeof_X) {
+    case 7: cal_ep3D_kernel<EP, 7><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+    case 27: cal_ep3D_kernel<EP, 27><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+    default: cal_ep3D_kernel<EP, 0><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+    }
     return (int)cudaGetLastError();
 }
 

@@ -24,6 +24,10 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # solidified thickness after the whole run (cells above 1e-9 of the field's
 # maximum); the transcendental parts differ in the last bits
 RTOL = 1e-10
+# the reference's 2006 Etna inputs over the fixture's whole run (1000 steps
+# of a real flow field): the last-bit differences of the transcendental
+# parts accumulate further there
+RTOL_2006 = 1e-9
 
 
 @pytest.fixture(scope="module")
@@ -41,12 +45,12 @@ def _case(fx, idx):
         int(fx[p + "steps"][0])
 
 
-def _close(got, ref, name):
+def _close(got, ref, name, rtol=RTOL):
     scale = max(np.abs(ref).max(), 1e-300)
     mask = (np.abs(ref) > 1e-9 * scale) | (np.abs(got) > 1e-9 * scale)
     rel = np.abs(got - ref)[mask] / np.maximum(np.abs(ref)[mask], 1e-300)
     worst = float(rel.max()) if rel.size else 0.0
-    assert worst <= RTOL, f"{name}: max relative difference {worst:.3e}"
+    assert worst <= rtol, f"{name}: max relative difference {worst:.3e}"
     return worst
 
 
@@ -104,22 +108,27 @@ def _write_2006_files(tmp_path):
     return fx, str(tmp_path / "2006")
 
 
+@pytest.mark.parametrize("libm", [False, True])
 @pytest.mark.parametrize("ac", [0, 1])
-def test_reference_2006_inputs_through_the_reader(cal, tmp_path, ac):
+def test_reference_2006_inputs_through_the_reader(cal, tmp_path, ac, libm):
     """The reference's own 2006 Etna configuration files, read by
     cal_sciara_read (the example's .cfg / GIS .stt / emission-rate readers
-    restated), run on the GPU for the fixture's step count: the reference
-    program's final fields on the same files to the tolerance above."""
+    restated), run on the GPU for the fixture's step count, in both forms of
+    the transcendental parts: the reference program's final fields on the
+    same files to RTOL_2006 (the worst relative difference is printed)."""
     fx, prefix = _write_2006_files(tmp_path)
     c = cal.sciara_read(prefix)
     steps = int(fx["steps"][0])
-    out = cal.sciara(c["z"], c["vents"], c["rates"], c["emission_time"], steps, ac=bool(ac), params=c["params"])
+    out = cal.sciara(c["z"], c["vents"], c["rates"], c["emission_time"], steps, ac=bool(ac), params=c["params"],
+                     libm=libm)
     p = f"ac{ac}_"
     assert out["steps"] == int(fx[p + "steps"][0])
-    _close(out["slt"], fx[p + "slt"], "slt")
-    _close(out["st"], fx[p + "st"], "st")
-    _close(out["msl"], fx[p + "msl"], "msl")
-    _close(out["z"], c["z"] + fx[p + "dz"], "z")
+    worst = max(_close(out["slt"], fx[p + "slt"], "slt", RTOL_2006),
+                _close(out["st"], fx[p + "st"], "st", RTOL_2006),
+                _close(out["msl"], fx[p + "msl"], "msl", RTOL_2006),
+                _close(out["z"], c["z"] + fx[p + "dz"], "z", RTOL_2006))
+    print(f"SCIARA 2006 inputs, active cells {ac}, {'libm' if libm else 'identity'} forms, {steps} steps: "
+          f"max relative difference {worst:.3e}")
     assert (fx[p + "slt"] > 0).sum() > 100  # the flow is under way
 
 
