@@ -289,8 +289,12 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     }
     __syncthreads();
     for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x) {
-        if (cal_written2D[t])
-            atomicOr(&m.dirty[t / CAL_MAX_SUBSTATES], 1u << (t % CAL_MAX_SUBSTATES));
+        /* every block of a dense launch writes the same bits: the atomic only
+         * where the bit is not already set, so that the blocks do not queue
+         * on one word */
+        const unsigned bit = 1u << (t % CAL_MAX_SUBSTATES);
+        if (cal_written2D[t] && !(*(volatile const unsigned*)&m.dirty[t / CAL_MAX_SUBSTATES] & bit))
+            atomicOr(&m.dirty[t / CAL_MAX_SUBSTATES], bit);
         if (cal_untracked2D[t] && m.untracked)
             atomicOr(&m.untracked[t / CAL_MAX_SUBSTATES], 1u << (t % CAL_MAX_SUBSTATES));
     }

@@ -240,9 +240,13 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep3D_kernel(const __grid_c
         }
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x)
-        if (cal_written3D[t])
-            atomicOr(&m.dirty[t / CAL_MAX_SUBSTATES], 1u << (t % CAL_MAX_SUBSTATES));
+    for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x) {
+        /* the atomic only where the bit is not already set (every block of a
+         * dense launch writes the same bits) */
+        const unsigned bit = 1u << (t % CAL_MAX_SUBSTATES);
+        if (cal_written3D[t] && !(*(volatile const unsigned*)&m.dirty[t / CAL_MAX_SUBSTATES] & bit))
+            atomicOr(&m.dirty[t / CAL_MAX_SUBSTATES], bit);
+    }
 }
 
 /* one kernel per common neighbourhood size (von Neumann 7, Moore 27) and

@@ -358,8 +358,35 @@ __global__ void __launch_bounds__(kThreads) k_compact_count(const unsigned char*
         scratch[0] = 0; /* every ticket of this call has been taken */
 }
 
-__global__ void __launch_bounds__(kThreads) k_compact_scatter(const unsigned char* __restrict__ flags, CompactGeom g,
-                                                                const int* __restrict__ scratch, int* cells, int* lin)
+/* next -> current at the listed cells, fused into the scatter pass of the
+ * compaction that lists them (CalGrid::update_all with active cells): the
+ * substates to copy, and the list's length (an empty list copies every
+ * cell, calUpdateSubstate2D* in cal2D.c) */
+struct ActiveCopy {
+    const void* src[CAL_UPDATE_MAX];
+    void* dst[CAL_UPDATE_MAX];
+    unsigned char elem[CAL_UPDATE_MAX];
+    int n;
+    const int* count;
+};
+
+static __device__ __forceinline__ void copy_cell(const ActiveCopy& u, long long o)
+{
+    for (int e = 0; e < u.n; e++) {
+        const int es = u.elem[e];
+        if (es == 8)
+            ((unsigned long long*)u.dst[e])[o] = ((const unsigned long long*)u.src[e])[o];
+        else if (es == 4)
+            ((unsigned*)u.dst[e])[o] = ((const unsigned*)u.src[e])[o];
+        else
+            ((unsigned char*)u.dst[e])[o] = ((const unsigned char*)u.src[e])[o];
+    }
+}
+
+template <bool UPD>
+static __device__ __forceinline__ void compact_scatter(const unsigned char* __restrict__ flags, const CompactGeom& g,
+                                                       const int* __restrict__ scratch, int* cells, int* lin,
+                                                       const ActiveCopy* u)
 {
     __shared__ int s_warp[kThreads / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -396,9 +423,33 @@ __global__ void __launch_bounds__(kThreads) k_compact_scatter(const unsigned cha
                 cells[3 * slot + 2] = (int)((unsigned)v - ij * (unsigned)g.slices);
             }
             lin[slot] = (int)mem;
+            if (UPD)
+                copy_cell(*u, mem);
         }
         pos += __popc(m[q]);
     }
+}
+
+__global__ void __launch_bounds__(kThreads) k_compact_scatter(const unsigned char* __restrict__ flags, CompactGeom g,
+                                                                const int* __restrict__ scratch, int* cells, int* lin)
+{
+    compact_scatter<false>(flags, g, scratch, cells, lin, nullptr);
+}
+
+__global__ void __launch_bounds__(kThreads) k_compact_scatter_update(const unsigned char* __restrict__ flags,
+                                                                       CompactGeom g, const int* __restrict__ scratch,
+                                                                       int* cells, int* lin,
+                                                                       const __grid_constant__ ActiveCopy u)
+{
+    if (*u.count > 0) {
+        compact_scatter<true>(flags, g, scratch, cells, lin, &u);
+        return;
+    }
+    /* no active cell: every cell of this block's range (linear memory) */
+    const long long lo = (long long)blockIdx.x * kChunk;
+    const long long hi = lo + kChunk < g.n ? lo + kChunk : g.n;
+    for (long long c = lo + threadIdx.x; c < hi; c += kThreads)
+        copy_cell(u, c);
 }
 
 int compact_blocks_needed(long long ncells)
@@ -425,6 +476,26 @@ cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int col
     const int nb = compact_blocks_needed(g.n);
     k_compact_count<<<nb, kThreads, 0, stream>>>(flags, g, scratch, count);
     k_compact_scatter<<<nb, kThreads, 0, stream>>>(flags, g, scratch, cells, lin);
+    return cudaGetLastError();
+}
+
+/* the compaction, then next -> current of the listed substates at the new
+ * list's cells (every cell when the list is empty) in its scatter pass */
+static cudaError_t compact_and_copy(const unsigned char* flags, int dim, int rows, int cols, int slices, int* cells,
+                                    int* lin, int* count, int* scratch, long long scratch_ints, const ActiveCopy& u,
+                                    cudaStream_t stream)
+{
+    CompactGeom g;
+    g.dim = dim;
+    g.rows = rows;
+    g.cols = cols;
+    g.slices = dim == 3 ? slices : 1;
+    g.n = (long long)rows * cols * g.slices;
+    if (g.n <= 0 || g.n > 0x7fffffffLL || scratch_ints < compact_scratch_ints(g.n))
+        return cudaErrorInvalidValue;
+    const int nb = compact_blocks_needed(g.n);
+    k_compact_count<<<nb, kThreads, 0, stream>>>(flags, g, scratch, count);
+    k_compact_scatter_update<<<nb, kThreads, 0, stream>>>(flags, g, scratch, cells, lin, u);
     return cudaGetLastError();
 }
 
@@ -959,8 +1030,38 @@ bool CalGrid::update_all()
 {
     if (!to_device_all())
         return false;
-    if (active && !compact())
-        return false;
+    if (active) {
+        /* calUpdateActiveCells2D, then every registered substate's next ->
+         * current at the new list's cells: one compaction whose scatter
+         * pass does the copy */
+        ActiveCopy u;
+        memset(&u, 0, sizeof(u));
+        for (int t = 0; t < CAL_NTYPES; t++)
+            for (int sl = 0; sl < nslot[t]; sl++) {
+                Sub& q = sub[t][sl];
+                if (!q.used || q.single || q.next_stale)
+                    continue;
+                u.src[u.n] = q.layer[1].dev;
+                u.dst[u.n] = q.layer[0].dev;
+                u.elem[u.n] = (unsigned char)q.elem;
+                u.n++;
+            }
+        u.count = d_count;
+        if (!cuda_ok(compact_and_copy(d_flags, dim, rows, cols, slices, d_cells, d_lin, d_count, d_block_counts,
+                                      scratch_ints, u, stream),
+                     "active-cell compaction and update"))
+            return false;
+        for (int t = 0; t < CAL_NTYPES; t++)
+            for (int sl = 0; sl < nslot[t]; sl++) {
+                Sub& q = sub[t][sl];
+                if (!q.used || q.single || q.next_stale)
+                    continue;
+                q.layer[0].host_valid = false;
+                q.forced_dirty = false;
+            }
+        written_since_update = false;
+        return clear_dirty();
+    }
     std::vector<std::pair<int, int>> all;
     for (int t = 0; t < CAL_NTYPES; t++)
         for (int s = 0; s < nslot[t]; s++)
