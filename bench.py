@@ -461,40 +461,50 @@ def processes_plain_section(m, cal, z, h, h_plain):
     (eager: a launch sequence per step; graph: the recorded step replayed) or
     calRunDeviceSteps2D (one device-driven graph launch for the loop).  The
     engine updates and fills only the tiles a process changed (change
-    tracking).  Must give the split step's bits."""
+    tracking).  Twice: as the reference program stands, and with both
+    processes declared pure (calSetElementaryProcessPure2D), which lets the
+    process kernels skip the tiles whose neighbourhood did not change since
+    they last changed nothing there.  Every form must give the split step's
+    bits."""
     import torch
-    sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_PROCESSES)
-    if not sess:
-        return {"error": "cal_sciddicaT_open (processes) failed: " + cal.core().calGetErrorString().decode()}
-    stream = torch.cuda.ExternalStream(m.cal_sciddicaT_stream(sess))
-    forms, same = {}, True
-    for name, loop in (("eager", 0), ("graph", 1), ("device", 2)):
-        ms = []
-        for it in range(3):
-            m.cal_sciddicaT_reset(sess)
-            with torch.cuda.stream(stream):
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                rc = m.cal_sciddicaT_steps(sess, CA_STEPS, loop)
-                e1.record(stream)
-            e1.synchronize()
-            if rc:
-                m.cal_sciddicaT_close(sess)
-                return {"error": f"cal_sciddicaT_steps (processes, {name}) failed: {rc}"}
-            if it:
-                ms.append(e0.elapsed_time(e1))
-        hp = np.empty_like(h)
-        m.cal_sciddicaT_read(sess, hp.ctypes.data)
-        same = same and hp.tobytes() == h_plain.tobytes()
-        forms[name] = float(np.mean(ms))
-    m.cal_sciddicaT_close(sess)
-    best = min(forms, key=forms.get)
-    return {"workload": f"SCIDDICA-T {ROWS}x{COLS} FP64, flat, plain, {CA_STEPS} CA steps, the reference "
-                        "program's device processes + steering through the run loop",
-            "ms_per_run": forms, "best": best,
-            "value": ROWS * COLS * CA_STEPS / (forms[best] * 1e-3), "unit": "cell-updates/s",
-            "identical_to_split_step": bool(same)}
+    m.cal_sciddicaT_set_pure.argtypes = [C.c_int]
+    out = {}
+    for label, pure in (("as_written", 0), ("declared_pure", 1)):
+        m.cal_sciddicaT_set_pure(pure)
+        sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_PROCESSES)
+        m.cal_sciddicaT_set_pure(0)
+        if not sess:
+            return {"error": "cal_sciddicaT_open (processes) failed: " + cal.core().calGetErrorString().decode()}
+        stream = torch.cuda.ExternalStream(m.cal_sciddicaT_stream(sess))
+        forms, same = {}, True
+        for name, loop in (("eager", 0), ("graph", 1), ("device", 2)):
+            ms = []
+            for it in range(3):
+                m.cal_sciddicaT_reset(sess)
+                with torch.cuda.stream(stream):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    rc = m.cal_sciddicaT_steps(sess, CA_STEPS, loop)
+                    e1.record(stream)
+                e1.synchronize()
+                if rc:
+                    m.cal_sciddicaT_close(sess)
+                    return {"error": f"cal_sciddicaT_steps (processes, {label}, {name}) failed: {rc}"}
+                if it:
+                    ms.append(e0.elapsed_time(e1))
+            hp = np.empty_like(h)
+            m.cal_sciddicaT_read(sess, hp.ctypes.data)
+            same = same and hp.tobytes() == h_plain.tobytes()
+            forms[name] = float(np.mean(ms))
+        m.cal_sciddicaT_close(sess)
+        best = min(forms, key=forms.get)
+        out[label] = {"ms_per_run": forms, "best": best,
+                      "value": ROWS * COLS * CA_STEPS / (forms[best] * 1e-3), "unit": "cell-updates/s",
+                      "identical_to_split_step": bool(same)}
+    out["workload"] = (f"SCIDDICA-T {ROWS}x{COLS} FP64, flat, plain, {CA_STEPS} CA steps, the reference program's "
+                       "device processes + steering through the run loop")
+    return out
 
 
 def active_cells_section(m, cal, z, h, h_plain):

@@ -219,6 +219,23 @@ int calGetActiveCellCount2D(struct CALModel2D* ca2D);
 int calCompactActiveCellsNoAlloc2D(const CALbyte* flags, int rows, int columns, struct CALCell2D* cells,
                                    int* linear, int* count, void* stream);
 
+/* Declares that an elementary process added with calAddElementaryProcess2D
+ * is a pure function of the current values of the model's substates over
+ * its cell's neighbourhood and of values that do not change during the run
+ * (no step number, no parameters changed by steering, no randomness).  Then,
+ * in a model without active cells whose substates the library alone writes
+ * (no unsafe operations, no device pointers handed out, no swaps), the
+ * process kernel of calGlobalTransitionFunction2D skips every 32 x 8 tile
+ * where the process changed nothing the last time it ran and where no
+ * substate has changed since in that tile or the eight around it: it would
+ * change nothing again.  The results are those of the dense run.  The
+ * neighbourhood must reach at most 8 rows and 32 columns; every tile is run
+ * again after calRunInitSimulation2D and after any write the library cannot
+ * follow tile by tile.  `pure` 0 withdraws the declaration.  No counterpart
+ * in the reference (a performance declaration; the reference runs every
+ * cell).  Returns a CALError code. */
+int calSetElementaryProcessPure2D(struct CALModel2D* ca2D, CALCallbackFunc2D elementary_process, CALbyte pure);
+
 /* Registration of device elementary processes (used by
  * CAL_ELEMENTARY_PROCESS_2D; not called directly). */
 struct CALDevModel2D;

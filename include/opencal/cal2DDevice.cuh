@@ -67,6 +67,12 @@ struct CALDevModel2D {
     int tiles_x, tiles_y, tile_words;
     unsigned int* chg;
     unsigned int* untracked;
+    /* tile skipping of a process declared pure (calSetElementaryProcessPure2D),
+     * NULL otherwise: one bit per tile, set where the process must run (its
+     * neighbourhood changed since it last changed nothing there); the kernel
+     * skips the other tiles and clears the bit of every tile where it
+     * changed nothing */
+    unsigned int* run;
 };
 
 
@@ -272,18 +278,25 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     } else {
         const int ntiles = m.tiles_x * m.tiles_y;
         for (int tile = bid; tile < ntiles; tile += nblocks) {
+            const unsigned tbit = 1u << (tile & 31);
+            if (m.run && !(m.run[tile >> 5] & tbit))
+                continue; /* unchanged neighbourhood, no-op last time (block-uniform) */
             const int ty = tile / m.tiles_x;
             const int i = ty * CAL_TILE_H + warp, j = (tile - ty * m.tiles_x) * CAL_TILE_W + lane;
             if (i < m.rows && j < m.cols)
                 EP(ca, i, j);
             if (m.track) {
+                bool changed = false;
                 __syncwarp();
                 for (int t = lane; t < 3 * CAL_MAX_SUBSTATES; t += 32)
                     if (cal_chg2D[warp][t]) {
                         cal_chg2D[warp][t] = 0;
-                        atomicOr(&m.chg[(long long)t * m.tile_words + (tile >> 5)], 1u << (tile & 31));
+                        changed = true;
+                        atomicOr(&m.chg[(long long)t * m.tile_words + (tile >> 5)], tbit);
                     }
                 __syncwarp();
+                if (m.run && !__syncthreads_or(changed) && threadIdx.x == 0)
+                    atomicAnd(&m.run[tile >> 5], ~tbit);
             }
         }
     }

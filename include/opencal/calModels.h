@@ -52,6 +52,11 @@ int cal_sciddicaT_steps(void* session, int steps, int graph);
 /* 1 when a grid barrier of the last persistent run gave up (synchronises) */
 int cal_sciddicaT_persist_failed(void* session);
 int cal_sciddicaT_set_params(void* session, double p_r, double p_eps);
+/* 1: models created afterwards (cal_sciddicaT_run, cal_sciddicaT_open,
+ * processes mode) declare the two plain processes pure
+ * (calSetElementaryProcessPure2D), so that the engine skips quiet tiles;
+ * 0 (default): the reference program as it stands */
+int cal_sciddicaT_set_pure(int on);
 /* launch grids of the split step's kernels: k1_blocks and k2_blocks
  * 256-thread blocks of the outflow and the update kernel (0 = the defaults
  * 608 / 608) */

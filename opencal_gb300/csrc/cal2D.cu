@@ -16,6 +16,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+
 #include "cal_model_internal.cuh"
 #include "opencal/cal2DUnsafe.h"
 
@@ -424,7 +426,8 @@ CAL_SUBSTATE_OPS_2D(r, CALreal, 2)
 
 /* ======================= transition ===================================== */
 
-static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch)
+/* run: the process's must-run bitmap when its tiles may be skipped */
+static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned* run = nullptr)
 {
     CalGrid& g = G(ca);
     if (!g.repair_all_stale() || !g.to_device_all())
@@ -432,6 +435,7 @@ static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch)
     CALDevModel2D d;
     if (!build_desc(ca, &d))
         return;
+    d.run = run;
     int gx, gy;
     g.launch_grid(&gx, &gy);
     int rc = launch(&d, gx, gy, (void*)g.stream);
@@ -457,12 +461,87 @@ extern "C" void calUpdate2D(struct CALModel2D* ca)
     G(ca).update_all();
 }
 
+/* Whether the pure processes' tiles may be skipped now: change tracking on
+ * (no active cells), no unsafe operations, every substate written by the
+ * library alone, and a neighbourhood that reaches only the eight tiles
+ * around a cell's tile (at most CAL_TILE_H rows and CAL_TILE_W columns; on
+ * toroidal grids whose last tile row / column is partial, at most its
+ * height / width, so that the wrap stays within the next tile). */
+static bool skipping_allowed(struct CALModel2D* ca)
+{
+    CalGrid& g = G(ca);
+    if (!g.tracking || !g.d_run || ca->is_safe == CAL_UNSAFE_ACTIVE)
+        return false;
+    for (int t = 0; t < CAL_NTYPES; t++)
+        for (int s = 0; s < g.nslot[t]; s++)
+            if (g.sub[t][s].used && !g.sub[t][s].single && !g.sub[t][s].trackable)
+                return false;
+    int ri = 0, rj = 0;
+    const int len = table_len(ca);
+    for (int n = 0; n < len; n++) {
+        ri = std::max(ri, std::abs(ca->X[n].i));
+        rj = std::max(rj, std::abs(ca->X[n].j));
+    }
+    if (ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_2D || ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_ALT_2D) {
+        ri = std::max(ri, 1);
+        rj = std::max(rj, 1);
+    }
+    if (ri > CAL_TILE_H || rj > CAL_TILE_W)
+        return false;
+    if (ca->T == CAL_SPACE_TOROIDAL) {
+        const int pr = ca->rows % CAL_TILE_H, pc = ca->columns % CAL_TILE_W;
+        if ((pr && ri > pr) || (pc && rj > pc))
+            return false;
+    }
+    return true;
+}
+
+/* Bring the skipping state up to date: whether the pure processes' tiles
+ * may be skipped, and if the bitmaps were not kept meanwhile (skipping just
+ * became possible, or an event the tiles cannot follow happened), every
+ * tile runs again.  Returns whether tiles may be skipped. */
+bool cal_prepare_skipping2D(struct CALModel2D* ca)
+{
+    CalGrid& g = G(ca);
+    bool any_pure = false;
+    for (int b = 0; b < ca->num_of_elementary_processes; b++)
+        any_pure = any_pure || ca->gpu->pure[b];
+    const bool skip = any_pure && skipping_allowed(ca);
+    const int nrun = skip ? ca->num_of_elementary_processes : 0;
+    if (nrun != g.nrun || (skip && g.run_epoch != g.inval_epoch)) {
+        g.nrun = nrun;
+        if (nrun && !g.arm_runs())
+            return false;
+    }
+    return skip;
+}
+
 extern "C" void calGlobalTransitionFunction2D(struct CALModel2D* ca)
 {
+    CalGrid& g = G(ca);
+    const bool skip = cal_prepare_skipping2D(ca);
     for (int b = 0; b < ca->num_of_elementary_processes; b++) {
-        apply_launch(ca, ca->gpu->launch[b]);
+        unsigned* run = (skip && ca->gpu->pure[b]) ? g.d_run + (size_t)b * g.tile_words : nullptr;
+        apply_launch(ca, ca->gpu->launch[b], run);
         calUpdate2D(ca);
     }
+}
+
+extern "C" int calSetElementaryProcessPure2D(struct CALModel2D* ca, CALCallbackFunc2D ep, CALbyte pure)
+{
+    if (!ca || !ca->gpu) {
+        cal::set_error(CAL_ERROR_INVALID_ARGUMENT, "calSetElementaryProcessPure2D: no model");
+        return CAL_ERROR_INVALID_ARGUMENT;
+    }
+    for (int b = 0; b < ca->num_of_elementary_processes; b++)
+        if (ca->elementary_processes[b] == ep) {
+            ca->gpu->pure[b] = pure != 0;
+            G(ca).nrun = -1; /* re-armed before the next transition */
+            return CAL_SUCCESS;
+        }
+    cal::set_error(CAL_ERROR_INVALID_ARGUMENT,
+                   "calSetElementaryProcessPure2D: not a process added with calAddElementaryProcess2D");
+    return CAL_ERROR_INVALID_ARGUMENT;
 }
 
 /* ======================= host cell accessors ============================ */

@@ -33,6 +33,7 @@ struct CALGpuRun2D {
 };
 
 bool cal_internal_desc2D(struct CALModel2D* ca, CALDevModel2D* d);
+bool cal_prepare_skipping2D(struct CALModel2D* ca);
 
 /* ======================= device stop conditions ========================= */
 
@@ -92,6 +93,11 @@ extern "C" void calRunInitSimulation2D(struct CALRun2D* sim)
         if (sim->UPDATE_MODE == CAL_UPDATE_IMPLICIT)
             calUpdate2D(sim->ca2D);
     }
+    /* a new run: pure processes run on every tile again (their parameters
+     * may have changed between runs); done here, after the init, so that a
+     * first step recorded as a graph does not record the re-arming */
+    G(sim->ca2D).nrun = -1;
+    cal_prepare_skipping2D(sim->ca2D);
 }
 
 /* the device work of one step (cal2DRun.c:88-105 without the stop test) */
@@ -119,6 +125,7 @@ static bool capture_step(struct CALRun2D* sim)
     cal::CalGrid& g = G(sim->ca2D);
     if (!g.repair_all_stale() || !g.to_device_all())
         return false;
+    cal_prepare_skipping2D(sim->ca2D); /* any re-arming before the recording, not in it */
     const int transfers0 = g.transfers;
     const long swaps0 = g.swaps;
     cal::GridState* before = new cal::GridState;
@@ -270,6 +277,7 @@ static bool device_loop(struct CALRun2D* sim, CALStopLaunchFunc2D stop, int have
         return false;
     }
     cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cal_prepare_skipping2D(sim->ca2D); /* any re-arming before the recording, not in it */
     cal::GridState* before = new cal::GridState;
     g.save(before);
     const int transfers0 = g.transfers;

@@ -106,13 +106,13 @@ __global__ void k_update(const __grid_constant__ UpdateParams p)
         const int es = p.elem[e];
         if (listed > 0) {
             for (long long c = t0; c < listed; c += stride) {
-                const long long o = (long long)p.lin[c];
+                const long long o = (long long)__ldg(p.lin + c);
                 if (es == 8)
-                    ((unsigned long long*)p.dst[e])[o] = ((const unsigned long long*)p.src[e])[o];
+                    ((unsigned long long*)p.dst[e])[o] = __ldg((const unsigned long long*)p.src[e] + o);
                 else if (es == 4)
-                    ((unsigned*)p.dst[e])[o] = ((const unsigned*)p.src[e])[o];
+                    ((unsigned*)p.dst[e])[o] = __ldg((const unsigned*)p.src[e] + o);
                 else
-                    ((unsigned char*)p.dst[e])[o] = ((const unsigned char*)p.src[e])[o];
+                    ((unsigned char*)p.dst[e])[o] = __ldg((const unsigned char*)p.src[e] + o);
             }
         } else {
             const long long bytes = p.ncells * es;
@@ -132,7 +132,31 @@ __global__ void k_update(const __grid_constant__ UpdateParams p)
  * tile index = tile row * tiles_x + tile column; one bit per tile. */
 struct TileGeom {
     int rows, cols, tiles_x, tile_words, ntiles;
+    int toroidal;
+    unsigned* run; /* must-run bitmaps of the processes (NULL: no skipping) */
+    int nrun;
 };
+
+/* tile `tile`'s current layer changed: every process must run again on it
+ * and on the eight tiles around it (wrapping on toroidal grids); thread k <
+ * 9 of the caller takes neighbour k */
+static __device__ __forceinline__ void mark_run(const TileGeom& g, int tile, int k)
+{
+    if (!g.run || k >= 9)
+        return;
+    const int tiles_y = g.ntiles / g.tiles_x;
+    const int ty = tile / g.tiles_x, tx = tile - ty * g.tiles_x;
+    int y = ty + k / 3 - 1, x = tx + k % 3 - 1;
+    if (g.toroidal) {
+        y = y < 0 ? y + tiles_y : (y >= tiles_y ? y - tiles_y : y);
+        x = x < 0 ? x + g.tiles_x : (x >= g.tiles_x ? x - g.tiles_x : x);
+    } else if (y < 0 || y >= tiles_y || x < 0 || x >= g.tiles_x) {
+        return;
+    }
+    const int t = y * g.tiles_x + x;
+    for (int p = 0; p < g.nrun; p++)
+        atomicOr(&g.run[(long long)p * g.tile_words + (t >> 5)], 1u << (t & 31));
+}
 
 /* the cells of `tile`, one per thread of a 256-thread block */
 static __device__ __forceinline__ bool tile_cell(const TileGeom& g, int tile, long long* c)
@@ -202,6 +226,7 @@ __global__ void __launch_bounds__(kThreads) k_update_tiles(const __grid_constant
             case 4: copy_tile<unsigned>(p.g, tile, p.src[e], p.dst[e]); break;
             default: copy_tile<unsigned char>(p.g, tile, p.src[e], p.dst[e]); break;
             }
+            mark_run(p.g, tile, threadIdx.x);
         }
         if (threadIdx.x == 0 && s_bits) {
             p.chg[row + w] = 0;
@@ -239,6 +264,7 @@ __global__ void __launch_bounds__(kThreads) k_fill_tiles(TileGeom g, T* l0, T* l
                 if (l1)
                     l1[c] = value;
             }
+            mark_run(g, tile, threadIdx.x);
         }
         if (threadIdx.x == 0 && s_bits) {
             chg[w] = 0;
@@ -370,17 +396,18 @@ struct ActiveCopy {
     const int* count;
 };
 
-static __device__ __forceinline__ void copy_cell(const ActiveCopy& u, long long o)
+/* next -> current of substate e at cell o; next is not written during the
+ * kernel, so it is read through the non-coherent path and the loads of
+ * successive calls can be in flight together */
+static __device__ __forceinline__ void copy_elem(const ActiveCopy& u, int e, long long o)
 {
-    for (int e = 0; e < u.n; e++) {
-        const int es = u.elem[e];
-        if (es == 8)
-            ((unsigned long long*)u.dst[e])[o] = ((const unsigned long long*)u.src[e])[o];
-        else if (es == 4)
-            ((unsigned*)u.dst[e])[o] = ((const unsigned*)u.src[e])[o];
-        else
-            ((unsigned char*)u.dst[e])[o] = ((const unsigned char*)u.src[e])[o];
-    }
+    const int es = u.elem[e];
+    if (es == 8)
+        ((unsigned long long*)u.dst[e])[o] = __ldg((const unsigned long long*)u.src[e] + o);
+    else if (es == 4)
+        ((unsigned*)u.dst[e])[o] = __ldg((const unsigned*)u.src[e] + o);
+    else
+        ((unsigned char*)u.dst[e])[o] = __ldg((const unsigned char*)u.src[e] + o);
 }
 
 template <bool UPD>
@@ -423,10 +450,22 @@ static __device__ __forceinline__ void compact_scatter(const unsigned char* __re
                 cells[3 * slot + 2] = (int)((unsigned)v - ij * (unsigned)g.slices);
             }
             lin[slot] = (int)mem;
-            if (UPD)
-                copy_cell(*u, mem);
         }
         pos += __popc(m[q]);
+    }
+    if (UPD) {
+        /* the block's listed cells, slots [first, pos of the last warp),
+         * one per thread, substate by substate */
+        __shared__ int s_range[2];
+        if (threadIdx.x == kThreads - 1) {
+            s_range[0] = scratch[kScratchHead + blockIdx.x];
+            s_range[1] = pos; /* the last warp's end: the block's end */
+        }
+        __syncthreads(); /* this block's lin[] entries are visible to it */
+        const int first = s_range[0], last = s_range[1];
+        for (int e = 0; e < u->n; e++)
+            for (int k = first + threadIdx.x; k < last; k += kThreads)
+                copy_elem(*u, e, lin[k]);
     }
 }
 
@@ -448,8 +487,9 @@ __global__ void __launch_bounds__(kThreads) k_compact_scatter_update(const unsig
     /* no active cell: every cell of this block's range (linear memory) */
     const long long lo = (long long)blockIdx.x * kChunk;
     const long long hi = lo + kChunk < g.n ? lo + kChunk : g.n;
-    for (long long c = lo + threadIdx.x; c < hi; c += kThreads)
-        copy_cell(u, c);
+    for (int e = 0; e < u.n; e++)
+        for (long long c = lo + threadIdx.x; c < hi; c += kThreads)
+            copy_elem(u, e, c);
 }
 
 int compact_blocks_needed(long long ncells)
@@ -557,7 +597,10 @@ bool CalGrid::init(int dim_, int rows_, int cols_, int slices_, int toroidal_, i
             !cuda_ok(cudaMalloc(&d_untracked, 4 * sizeof(unsigned)), "cudaMalloc change bitmaps") ||
             !cuda_ok(cudaMemsetAsync(d_chg, 0, bm, stream), "memset change bitmaps") ||
             !cuda_ok(cudaMemsetAsync(d_dev, 0, bm, stream), "memset change bitmaps") ||
-            !cuda_ok(cudaMemsetAsync(d_untracked, 0, 4 * sizeof(unsigned), stream), "memset change bitmaps"))
+            !cuda_ok(cudaMemsetAsync(d_untracked, 0, 4 * sizeof(unsigned), stream), "memset change bitmaps") ||
+            !cuda_ok(cudaMalloc(&d_run, (size_t)CAL_MAX_PROCESSES_CORE * tile_words * sizeof(unsigned)),
+                     "cudaMalloc skipping bitmaps") ||
+            !arm_runs())
             return false;
     }
     if (active) {
@@ -603,6 +646,7 @@ void CalGrid::destroy()
     cudaFree(d_chg);
     cudaFree(d_dev);
     cudaFree(d_untracked);
+    cudaFree(d_run);
     cudaFree(d_step);
     cudaFree(d_reduce_partial);
     cudaFree(d_reduce_result);
@@ -849,7 +893,7 @@ bool CalGrid::fill(int type, int slot, int layer, const void* value, bool at_act
     case 1: k_fill<CALint><<<g, kThreads, 0, stream>>>((CALint*)buf, *(const CALint*)value, ncells, d_lin, d_count, use); break;
     default: k_fill<CALreal><<<g, kThreads, 0, stream>>>((CALreal*)buf, *(const CALreal*)value, ncells, d_lin, d_count, use); break;
     }
-    if (!cuda_ok(cudaGetLastError(), "fill kernel"))
+    if (!cuda_ok(cudaGetLastError(), "fill kernel") || !arm_runs())
         return false;
     q.layer[layer].host_valid = false;
     q.forced_dirty = true;
@@ -886,6 +930,9 @@ bool CalGrid::fill_both(int type, int slot, const void* value)
         tg.tiles_x = tiles_x;
         tg.tile_words = tile_words;
         tg.ntiles = tiles_x * tiles_y;
+        tg.toroidal = toroidal;
+        tg.run = nrun > 0 ? d_run : nullptr;
+        tg.nrun = nrun;
         const int g = tile_words < 152 * 8 ? tile_words : 152 * 8;
         switch (type) {
         case 0: k_fill_tiles<CALbyte><<<g, kThreads, 0, stream>>>(tg, (CALbyte*)l0, (CALbyte*)l1, *(const CALbyte*)value, d_chg + row, d_dev + row); break;
@@ -904,7 +951,7 @@ bool CalGrid::fill_both(int type, int slot, const void* value)
             default: k_fill<CALreal><<<g, kThreads, 0, stream>>>((CALreal*)buf, *(const CALreal*)value, ncells, d_lin, d_count, 0); break;
             }
         }
-        if (!cuda_ok(cudaGetLastError(), "fill kernel") ||
+        if (!cuda_ok(cudaGetLastError(), "fill kernel") || !arm_runs() ||
             !cuda_ok(cudaMemsetAsync(d_chg + row, 0, tile_words * sizeof(unsigned), stream), "clear change bits") ||
             !cuda_ok(cudaMemsetAsync(d_dev + row, 0, tile_words * sizeof(unsigned), stream), "clear change bits"))
             return false;
@@ -968,6 +1015,8 @@ bool CalGrid::copy_next_to_current(const std::vector<std::pair<int, int>>& which
         k_update<<<grid_for(work), kThreads, 0, stream>>>(p);
         if (!cuda_ok(cudaGetLastError(), "update kernel"))
             return false;
+        if (!arm_runs()) /* whole copies: no tile-by-tile record of what changed */
+            return false;
         for (size_t r = 0; r < retrack.size(); r++) {
             /* copied whole only if written or forced: a substate that lost
              * its tracking was forced (host write, one-layer fill), so the
@@ -989,6 +1038,9 @@ bool CalGrid::copy_next_to_current(const std::vector<std::pair<int, int>>& which
         tp.g.tiles_x = tiles_x;
         tp.g.tile_words = tile_words;
         tp.g.ntiles = tiles_x * tiles_y;
+        tp.g.toroidal = toroidal;
+        tp.g.run = nrun > 0 ? d_run : nullptr;
+        tp.g.nrun = nrun;
         tp.dirty = d_dirty;
         tp.use_dirty = use_dirty ? 1 : 0;
         tp.chg = d_chg;
@@ -1019,6 +1071,15 @@ bool CalGrid::compact()
     return cuda_ok(compact_flags(d_flags, dim, rows, cols, slices, d_cells, d_lin, d_count, d_block_counts,
                                  scratch_ints, stream),
                    "active-cell compaction");
+}
+
+bool CalGrid::arm_runs()
+{
+    run_epoch = inval_epoch;
+    if (!d_run)
+        return true;
+    return cuda_ok(cudaMemsetAsync(d_run, 0xff, (size_t)CAL_MAX_PROCESSES_CORE * tile_words * sizeof(unsigned), stream),
+                   "arm tile skipping");
 }
 
 bool CalGrid::clear_dirty()

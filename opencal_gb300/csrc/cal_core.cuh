@@ -30,6 +30,7 @@
 
 #define CAL_MAX_SUBSTATES_CORE 32
 #define CAL_NTYPES 3
+#define CAL_MAX_PROCESSES_CORE 32 /* CAL_MAX_ELEMENTARY_PROCESSES of cal2D.h */
 
 namespace cal {
 
@@ -113,6 +114,14 @@ struct CalGrid {
     unsigned* d_chg = nullptr;
     unsigned* d_dev = nullptr;
     unsigned* d_untracked = nullptr;
+    /* tile skipping of pure processes: one must-run bitmap (tile_words
+     * words) per process slot; the update and fill kernels set the bits of
+     * the 3 x 3 tiles around every tile whose current layer they change, in
+     * the first nrun bitmaps; run_epoch: inval_epoch when every bit was last
+     * set (-1: never) */
+    unsigned* d_run = nullptr;
+    int nrun = 0;
+    long run_epoch = -1;
     int* d_step = nullptr;       /* step counter of a device-driven run */
     void* d_reduce_partial = nullptr; /* reduction scratch (per-block partials) */
     void* d_reduce_result = nullptr;  /* reduction result read back by the host */
@@ -148,6 +157,7 @@ struct CalGrid {
     bool update_all();                         /* calUpdate: compaction + copies */
     bool compact();                            /* calUpdateActiveCells */
     bool clear_dirty();
+    bool arm_runs();                           /* every tile must run again, for every process */
     bool swap(int type, int slot);
     bool sync();
     long long lin(int i, int j, int k) const

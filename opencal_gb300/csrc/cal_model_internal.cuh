@@ -13,6 +13,7 @@ struct CALGpuModel2D {
     struct CALCell2D* d_X = nullptr; /* device copy of the neighbourhood table */
     int d_X_len = 0;                 /* entries uploaded; -1 forces an upload */
     CALLaunchFunc2D launch[CAL_MAX_ELEMENTARY_PROCESSES];
+    bool pure[CAL_MAX_ELEMENTARY_PROCESSES] = {}; /* calSetElementaryProcessPure2D */
 };
 
 struct CALGpuModel3D {

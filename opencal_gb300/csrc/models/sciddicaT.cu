@@ -2024,6 +2024,27 @@ static void sciddicaT_simulation_init_fused(struct CALModel2D* sciddicaT)
 
 /* ======================= driver entry points ============================ */
 
+/* The two processes of the plain program read only z, h and the outflows
+ * over the von Neumann neighbourhood and the run's constant parameters:
+ * pure in the sense of calSetElementaryProcessPure2D.  Declared when
+ * cal_sciddicaT_set_pure(1) was called (off by default: the reference
+ * program as it stands). */
+static int g_sdt_pure = 0;
+
+static void sciddicaT_declare_pure(struct CALModel2D* ca)
+{
+    if (!g_sdt_pure)
+        return;
+    calSetElementaryProcessPure2D(ca, sciddicaT_flows_computation, CAL_TRUE);
+    calSetElementaryProcessPure2D(ca, sciddicaT_width_update, CAL_TRUE);
+}
+
+extern "C" int cal_sciddicaT_set_pure(int on)
+{
+    g_sdt_pure = on != 0;
+    return 0;
+}
+
 enum { SDT_MODE_PROCESSES = 0, SDT_MODE_FUSED = 1 };
 
 /* The reference example's main() as it stands (OpenCAL-OMP/examples/
@@ -2140,6 +2161,7 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
         calAddElementaryProcess2D(ca, sciddicaT_width_update);
         if (ac)
             calAddElementaryProcess2D(ca, sciddicaT_remove_inactive_cells);
+        sciddicaT_declare_pure(ca);
     }
     Q.z = calAddSubstate2Dr(ca);
     Q.h = calAddSubstate2Dr(ca);
@@ -2270,6 +2292,7 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
     if (mode == SDT_MODE_PROCESSES) {
         calAddElementaryProcess2D(s->ca, sciddicaT_flows_computation);
         calAddElementaryProcess2D(s->ca, sciddicaT_width_update);
+        sciddicaT_declare_pure(s->ca);
         if (ac)
             calAddElementaryProcess2D(s->ca, sciddicaT_remove_inactive_cells);
         calRunAddSteeringFunc2D(s->run, ac ? sciddicaT_steering_ac : sciddicaT_steering_plain);

@@ -86,6 +86,7 @@ def capi() -> C.CDLL:
         "calCADef2D": ([i, i, i, i, i], vp),
         "calFinalize2D": ([vp], None),
         "calAddElementaryProcess2D": ([vp, vp], vp),
+        "calSetElementaryProcessPure2D": ([vp, vp, C.c_byte], i),
         "calApplyElementaryProcess2D": ([vp, vp], None),
         "calUpdate2D": ([vp], None),
         "calAddActiveCell2D": ([vp, i, i], None),
@@ -330,6 +331,13 @@ class Model2D:
         """calAddElementaryProcess2D with a process of a built program."""
         self._c.calAddElementaryProcess2D(self, process)
         _raise_on_error("calAddElementaryProcess2D")
+
+    def set_pure(self, process: int, pure: bool = True) -> None:
+        """calSetElementaryProcessPure2D: the process is a pure function of
+        its neighbourhood and of values constant during the run, so the
+        engine may skip tiles where it would change nothing."""
+        if self._c.calSetElementaryProcessPure2D(self, process, 1 if pure else 0):
+            _raise_on_error("calSetElementaryProcessPure2D")
 
     def apply(self, process: int) -> None:
         """calApplyElementaryProcess2D: one process over the grid now (then

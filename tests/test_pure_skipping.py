@@ -1,0 +1,137 @@
+"""Tile skipping of processes declared pure (calSetElementaryProcessPure2D):
+the process kernel skips the 32 x 8 tiles where the process changed nothing
+the last time and whose 3 x 3 tile neighbourhood has not changed since.  The
+results must be the dense run's bits: checked here against the oracle on
+SCIDDICA-T (the reference program with both processes declared pure, flat
+and toroidal grids, per-step launches, recorded-step replay and the
+device-driven loop, including the reference's shipped 610 x 496 golden) and
+on Life defined from Python, and for a custom neighbourhood that reaches
+further than one tile (skipping refused, still exact).
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture
+def pure_sdt():
+    import opencal_gb300 as cal
+    cal.build()
+    m = cal.models()
+    m.cal_sciddicaT_set_pure(1)
+    yield cal
+    m.cal_sciddicaT_set_pure(0)
+
+
+@pytest.mark.parametrize("rows,cols,seed,steps,tor", [(160, 144, 11, 60, 0), (203, 177, 13, 90, 1),
+                                                      (256, 256, 5, 150, 0)])
+@pytest.mark.parametrize("graph", [0, 1, 2])
+def test_sciddicaT_pure_processes_bit_exact(pure_sdt, rows, cols, seed, steps, tor, graph):
+    import oracle
+    from opencal_gb300 import workloads as W
+    cal = pure_sdt
+    oracle.build()
+    z, h = W.sciddicaT_inputs(rows, cols, seed=seed)
+    ref = oracle.sciddicaT(z, h, steps, toroidal=bool(tor), ac=False)
+    got = cal.sciddicaT(z, h, steps, toroidal=bool(tor), ac=False, mode=cal.MODE_PROCESSES, graph=graph)
+    assert got[1].tobytes() == ref[1].tobytes()
+    assert got[0].tobytes() == ref[0].tobytes()
+
+
+def test_sciddicaT_pure_processes_shipped_golden(pure_sdt):
+    cal = pure_sdt
+    g = np.load(os.path.join(GOLDEN, "sciddicaT_610x496.npz"))
+    meta = json.load(open(os.path.join(GOLDEN, "manifest.json")))["sciddicaT_610x496"]
+    _, h, _ = cal.sciddicaT(g["z"], g["h0"], 4000, toroidal=True, ac=False, mode=cal.MODE_PROCESSES, graph=1)
+    text = "".join("".join("%.9f  " % v for v in row) + "\n" for row in h).encode()
+    assert hashlib.sha256(text).hexdigest() == meta["plain_text_sha256"]
+
+
+LIFE_BODY = """
+    int sum = 0;
+    for (int n = 1; n < ca->sizeof_X; n++)
+        sum += calGetX2Db(ca, Q.alive, i, j, n);
+    const CALbyte a = calGet2Db(ca, Q.alive, i, j);
+    calSet2Db(ca, Q.alive, i, j, (sum == 3 || (a == 1 && sum == 2)) ? 1 : 0);
+"""
+
+
+@pytest.mark.parametrize("shape,tor,graph", [((96, 80), True, False), ((130, 70), False, True),
+                                            ((72, 256), True, True)])
+def test_life_pure_from_python(shape, tor, graph):
+    """Life on a sparse field (most tiles dead and skipped after their first
+    generation) declared pure from Python."""
+    import oracle
+    import opencal_gb300 as cal
+    from opencal_gb300 import program as P
+    cal.build()
+    oracle.build()
+    rng = np.random.default_rng(3)
+    s0 = np.zeros(shape, np.uint8)
+    s0[10:30, 12:40] = rng.random((20, 28)) < 0.35  # one live patch
+    lib = P.Program("pylife_pure").substates(alive="b").process("pylife_pure_rule", LIFE_BODY).build()
+    model = P.Model2D(shape[0], shape[1], P.CAL_MOORE_NEIGHBORHOOD_2D,
+                      P.CAL_SPACE_TOROIDAL if tor else P.CAL_SPACE_FLAT)
+    alive = model.add_substate("b")
+    lib.bind(alive=alive)
+    rule = lib.process("pylife_pure_rule")
+    model.add_process(rule)
+    model.set_pure(rule)
+    model.load(alive, s0.astype(np.int8))
+    run = P.Run2D(model, 1, 60, graph=graph)
+    try:
+        run.run()
+        got = model.read(alive).astype(np.uint8)
+    finally:
+        run.close()
+        model.close()
+    assert np.array_equal(got, oracle.life2d(s0, 60, toroidal=tor))
+
+
+def test_far_reaching_custom_neighbourhood_is_not_skipped():
+    """A custom neighbourhood 12 rows tall reaches past the adjacent tile:
+    the declaration is accepted but tiles are not skipped, and the run
+    matches a dense run of the same program."""
+    import opencal_gb300 as cal
+    from opencal_gb300 import program as P
+    cal.build()
+    body = """
+        CALint s = calGet2Di(ca, Q.v, i, j);
+        for (int n = 1; n < ca->sizeof_X; n++) s += calGetX2Di(ca, Q.v, i, j, n);
+        calSet2Di(ca, Q.v, i, j, s % 7);
+    """
+    lib = P.Program("pyfar").substates(v="i").process("pyfar_rule", body).build()
+    capi = P.capi()
+    import ctypes as C
+    capi.calAddNeighbor2D.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    capi.calAddNeighbor2D.restype = C.c_void_p
+    out = []
+    for pure in (False, True):
+        model = P.Model2D(64, 96, P.CAL_CUSTOM_NEIGHBORHOOD_2D, P.CAL_SPACE_FLAT)
+        for di, dj in ((0, 0), (-12, 0), (12, 0), (0, 1)):
+            capi.calAddNeighbor2D(model, di, dj)
+        v = model.add_substate("i")
+        lib.bind(v=v)
+        rule = lib.process("pyfar_rule")
+        model.add_process(rule)
+        if pure:
+            model.set_pure(rule)
+        v0 = np.zeros((64, 96), np.int32)
+        v0[30:34, 40:44] = 1
+        model.load(v, v0)
+        run = P.Run2D(model, 1, 15)
+        try:
+            run.run()
+            out.append(model.read(v))
+        finally:
+            run.close()
+            model.close()
+    assert out[0].tobytes() == out[1].tobytes()
+    assert out[0].any()
