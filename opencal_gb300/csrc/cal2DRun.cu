@@ -27,6 +27,12 @@ struct CALGpuRun2D {
     cudaGraphExec_t exec = nullptr;
     long replays = 0;
     long rec_epoch = 0; /* the grid's invalidation epoch when the step was recorded */
+    /* the grid's invalidation epoch after the last step run launch by launch:
+     * a step is recorded only once one step has run that way since the last
+     * invalidation, because the first step after one takes one-off host
+     * decisions (a substate filled whole before its fills go tile by tile,
+     * the skipping bitmaps re-armed) that a replay would repeat every step */
+    long eager_epoch = -1;
     CALStopLaunchFunc2D dev_stop = nullptr; /* device stop condition */
     int* d_flag = nullptr;                  /* its decision, for the step-by-step fallback */
     int device_loop_used = 0;
@@ -189,12 +195,15 @@ extern "C" CALbyte calRunCAStep2D(struct CALRun2D* sim)
                 gr->replays++;
                 g.device_wrote_all();
             }
-        } else {
+        } else if (gr->eager_epoch == g.inval_epoch) {
             done = capture_step(sim);
         }
     }
-    if (!done)
+    if (!done) {
         step_work(sim);
+        if (gr)
+            gr->eager_epoch = g.inval_epoch;
+    }
     if (sim->stopCondition && sim->stopCondition(sim->ca2D))
         return CAL_FALSE;
     return CAL_TRUE;
@@ -333,7 +342,26 @@ static int run_device_steps(struct CALRun2D* sim, int first, int last)
     g.sync();
     const int saved_final = sim->final_step;
     sim->final_step = last;
-    if (!sim->stopCondition && device_loop(sim, stop, have_steps)) {
+    bool settled = gr->eager_epoch == g.inval_epoch;
+    bool more = true;
+    if (!sim->stopCondition && !settled) {
+        /* one step launch by launch before the loop is recorded (see
+         * CALGpuRun2D::eager_epoch), with the device's decision */
+        calClearError();
+        step_work(sim);
+        gr->eager_epoch = g.inval_epoch;
+        CALDevModel2D d;
+        int again = 0;
+        more = calGetLastError() == CAL_SUCCESS && cal::cuda_ok(cudaGetLastError(), "step launches") &&
+               cal_internal_desc2D(sim->ca2D, &d) && stop(&d, 0ULL, 0, last, gr->d_flag, (void*)g.stream) == 0 &&
+               cal::cuda_ok(cudaMemcpyAsync(&again, gr->d_flag, sizeof(int), cudaMemcpyDeviceToHost, g.stream),
+                            "read stop flag") &&
+               g.sync() && again;
+        settled = true;
+    }
+    if (!more) {
+        /* the run ended with that step (or it failed: the error is set) */
+    } else if (!sim->stopCondition && device_loop(sim, stop, have_steps)) {
         gr->device_loop_used = 1;
     } else {
         /* one step at a time; the device condition decides, and the host
