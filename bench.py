@@ -604,6 +604,13 @@ def calibration_section(args):
         loss, grad = ens.loss_grad(tgt)
         t_b.append(time.perf_counter() - t0)
     batched_s = float(np.median(t_b))
+    g_launches0, g_nodes = ens.graph_stats()
+    # the same evaluation launch by launch (tape layout on the host), once
+    ens.set_graph(False)
+    t0 = time.perf_counter()
+    ens.loss_grad(tgt)
+    batched_eager_s = time.perf_counter() - t0
+    ens.set_graph(True)
 
     # the plain drop-in per instance with central differences (five runs):
     # its run loop (the recorded step replayed), and the fastest single-grid
@@ -679,9 +686,13 @@ def calibration_section(args):
             "fd_sample_recovered": fd_traj["recovered"],
             "batched_sample_recovered": batched_on_sample,
         },
-        # forward: init + one step kernel per step, loss kernel; backward per
-        # step: recomputed step, tape restore, coefficients, gather
-        "gpu_launches_per_batched_iter": 5 * ENS_STEPS + 2,
+        # one launch of the recorded evaluation; its nodes: forward (init +
+        # one step kernel per step, checkpoint copies), loss, tape layout;
+        # backward per step: recomputed step, tape restore, coefficients,
+        # gather; the result copies
+        "gpu_launches_per_batched_iter": 1,
+        "graph_nodes_per_batched_iter": g_nodes,
+        "batched_iter_s_launch_by_launch": batched_eager_s,
     }
 
 

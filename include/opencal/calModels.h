@@ -104,6 +104,12 @@ int cal_sdt_batch_forward(void* ensemble, double* hT /* device, or NULL */);
 int cal_sdt_batch_active_tiles(void* ensemble, int* counts /* steps + 1 */);
 int cal_sdt_batch_loss_grad(void* ensemble, const double* target /* device */, double* loss /* B */,
                             double* grad /* 2B */, double* dL_dh0 /* device, or NULL */);
+/* 1 (default): cal_sdt_batch_loss_grad is one launch of a recorded CUDA graph
+ * (forward, loss, tape layout computed on the device, reverse sweep, results
+ * to pinned host memory) for rollouts of up to 1024 steps; 0: launch by
+ * launch with the tape layout computed on the host */
+int cal_sdt_batch_set_graph(void* ensemble, int on);
+int cal_sdt_batch_graph_stats(void* ensemble, long long* launches, long long* nodes);
 
 /* ---- SCIARA-fv2 (OpenCAL-OMP/examples/calomp_sciara-fv2/source/Sciara.cpp) ----
  * params: Pclock, PTsol, PTvent, Pr(Tsol), Pr(Tvent), Phc(Tsol), Phc(Tvent),

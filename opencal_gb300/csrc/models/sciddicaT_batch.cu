@@ -95,14 +95,38 @@ struct Batch {
     double* grad = nullptr; /* 2B: dL/dr[0..B), dL/deps[B..2B) */
     double* loss = nullptr; /* B */
     cudaStream_t st = nullptr;
+    /* the loss + gradient evaluation recorded once as a CUDA graph and
+     * replayed every call: tape offsets computed on the device (toff: the
+     * offset of each step's tiles within its segment's tape, need: the
+     * largest segment), results copied into pinned host memory (h_out: B
+     * losses, 2B gradients, then `need`); valid for the target, dL/dh0
+     * buffer, tile shape and tape it was recorded with */
+    long long* toff = nullptr;  /* steps + 1 offsets, then need */
+    double* h_out = nullptr;    /* pinned: 3B doubles + one long long */
+    cudaGraphExec_t gexec = nullptr;
+    const double* g_target = nullptr;
+    const double* g_gh0 = nullptr;
+    const double* g_tape = nullptr;
+    int g_shape = -1;
+    long long graph_launches = 0;
+    long long graph_nodes = 0;  /* kernel and copy nodes of the recorded evaluation */
+    bool use_graph = true;
 };
 
 static int tile_cells(const Batch& bt) { return kShapes[bt.shape].tw * kShapes[bt.shape].th; }
 
 /* re-tile every instance for the current shape */
+static void drop_graph(Batch& bt)
+{
+    if (bt.gexec)
+        cudaGraphExecDestroy(bt.gexec);
+    bt.gexec = nullptr;
+}
+
 static bool tiles_for(Batch& bt)
 {
     const int tw = kShapes[bt.shape].tw, th = kShapes[bt.shape].th;
+    drop_graph(bt); /* the work-list buffers are reallocated */
     std::vector<int> tinst;
     for (int b = 0; b < bt.B; b++) {
         Inst& I = bt.inst[b];
@@ -174,11 +198,22 @@ __global__ void __launch_bounds__(sdt::THREADS) k_step(const Inst* __restrict__ 
                                                        const double* __restrict__ z, const double* __restrict__ h,
                                                        double* __restrict__ hn, const int* __restrict__ list,
                                                        const int* __restrict__ count, int* list_next, int* count_next,
-                                                       int* stamps, int stamp, double* __restrict__ tape)
+                                                       int* stamps, int stamp, double* __restrict__ tape,
+                                                       const long long* __restrict__ toff, long long tape_cap)
 {
     extern __shared__ __align__(16) double smem[];
     using TL = sdt::Tile<TW, TH>;
     const int n = *count;
+    if (tape && toff) {
+        /* the step's tiles at the device-computed offset; a segment that
+         * does not fit is not taped (the host sees `need` and runs again
+         * with a larger tape) */
+        const long long off = *toff;
+        if (off + (long long)n * (TW * TH) > tape_cap)
+            tape = nullptr;
+        else
+            tape += off;
+    }
     for (int k = blockIdx.x; k < n; k += gridDim.x) {
         const int t = list[k];
         const Inst I = inst[tile_inst[t]];
@@ -209,9 +244,16 @@ template <int TW, int TH>
 __global__ void __launch_bounds__(sdt::THREADS) k_restore(const Inst* __restrict__ inst,
                                                           const int* __restrict__ tile_inst,
                                                           const int* __restrict__ list, const int* __restrict__ count,
-                                                          const double* __restrict__ tape, double* __restrict__ h)
+                                                          const double* __restrict__ tape, double* __restrict__ h,
+                                                          const long long* __restrict__ toff, long long tape_cap)
 {
     const int n = *count;
+    if (toff) {
+        const long long off = *toff;
+        if (off + (long long)n * (TW * TH) > tape_cap)
+            return; /* not taped (see k_step): this evaluation is discarded */
+        tape += off;
+    }
     for (int k = blockIdx.x; k < n; k += gridDim.x) {
         const int t = list[k];
         const Inst I = inst[tile_inst[t]];
@@ -487,6 +529,39 @@ __global__ void k_final_grad(const double* __restrict__ h0, const double* __rest
         g_h0[c] = lam[c] - (h0[c] > 0.0 ? lamz[c] : 0.0);
 }
 
+/* Tape layout on the device: one warp per segment of K <= 32 steps scans
+ * the segment's work-list sizes (counts[t] tiles of tc cells each) into the
+ * offsets toff[t]; toff[steps] = the largest segment's total (the tape
+ * size this evaluation needs). */
+__global__ void k_tape_offsets(const int* __restrict__ counts, int steps, int K, int tc, long long* toff)
+{
+    __shared__ long long s_need;
+    if (threadIdx.x == 0)
+        s_need = 0;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nseg = (steps + K - 1) / K;
+    for (int sg = warp; sg < nseg; sg += blockDim.x >> 5) {
+        const int t = sg * K + lane;
+        const bool in = lane < K && t < steps;
+        const long long v = in ? (long long)counts[t] * tc : 0;
+        long long incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += y;
+        }
+        if (in)
+            toff[t] = incl - v;
+        const long long total = __shfl_sync(0xffffffffu, incl, 31);
+        if (lane == 0)
+            atomicMax((unsigned long long*)&s_need, (unsigned long long)total);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        toff[steps] = s_need;
+}
+
 static int dense_grid(long long n)
 {
     long long b = (n + T - 1) / T;
@@ -513,19 +588,21 @@ static int step_grid()
 
 /* step t: list L_t -> (mark ? L_{t+1}) */
 template <int TW, int TH>
-static void launch_step(Batch& bt, int t, const double* h, double* hn, bool mark, double* tape)
+static void launch_step(Batch& bt, int t, const double* h, double* hn, bool mark, double* tape,
+                        const long long* toff = nullptr)
 {
     const size_t nt = (size_t)bt.ntiles;
     k_step<TW, TH><<<step_grid<TW, TH>(), sdt::THREADS, sdt::Tile<TW, TH>::smem_bytes, bt.st>>>(
         bt.d_inst, bt.d_tile_inst, bt.z, h, hn, bt.lists + nt * t, bt.counts + t,
-        mark ? bt.lists + nt * (t + 1) : nullptr, bt.counts + t + 1, bt.stamps, t + 2, tape);
+        mark ? bt.lists + nt * (t + 1) : nullptr, bt.counts + t + 1, bt.stamps, t + 2, tape, toff,
+        (long long)bt.tape_cap);
 }
 
 template <int TW, int TH>
-static void launch_restore(Batch& bt, int t, const double* tape, double* h)
+static void launch_restore(Batch& bt, int t, const double* tape, double* h, const long long* toff = nullptr)
 {
     k_restore<TW, TH><<<152 * 8, sdt::THREADS, 0, bt.st>>>(bt.d_inst, bt.d_tile_inst, bt.lists + (size_t)bt.ntiles * t,
-                                                            bt.counts + t, tape, h);
+                                                            bt.counts + t, tape, h, toff, (long long)bt.tape_cap);
 }
 
 template <int TW, int TH>
@@ -568,6 +645,10 @@ static void destroy(Batch* bt)
 {
     if (bt->st)
         cudaStreamSynchronize(bt->st);
+    drop_graph(*bt);
+    cudaFree(bt->toff);
+    if (bt->h_out)
+        cudaFreeHost(bt->h_out);
     void* ptrs[] = {bt->d_inst, bt->d_offs, bt->d_tile_inst, bt->stamps, bt->lists, bt->counts, bt->z_dem,
                     bt->z,      bt->h0,     bt->hbuf[0],      bt->hbuf[1], bt->ckpt, bt->tape,   bt->lam,
                     bt->lamz,   bt->g,      bt->gz,           bt->w,      bt->grad,  bt->loss};
@@ -701,6 +782,113 @@ extern "C" int cal_sdt_batch_active_tiles(void* handle, int* out)
     return (int)cudaMemcpy(out, bt->counts, sizeof(int) * (bt->steps + 1), cudaMemcpyDeviceToHost);
 }
 
+namespace sdtb {
+
+/* The whole loss + gradient evaluation queued on the ensemble's stream with
+ * the tape layout computed on the device (k_tape_offsets): forward with
+ * checkpoints, loss, layout, the reverse sweep segment by segment, dL/dh0,
+ * and the losses, gradients and the tape size needed copied into the
+ * pinned h_out.  Nothing in it waits for the host, so it can be recorded. */
+static void queue_loss_grad(Batch& bt, const double* target, double* g_h0)
+{
+    const size_t nb = (size_t)bt.N * sizeof(double);
+    cudaStream_t st = bt.st;
+    forward(bt, bt.steps, true);
+    cudaMemsetAsync(bt.loss, 0, bt.B * sizeof(double), st);
+    cudaMemsetAsync(bt.grad, 0, 2 * bt.B * sizeof(double), st);
+    k_loss<<<dense_grid(bt.N), T, sizeof(long long) * (bt.B + 1), st>>>(bt.d_inst, bt.d_offs, bt.B, bt.N,
+                                                                         bt.hbuf[bt.steps & 1], target, bt.lam,
+                                                                         bt.lamz, bt.loss);
+    k_tape_offsets<<<1, 1024, 0, st>>>(bt.counts, bt.steps, bt.K, tile_cells(bt), bt.toff);
+    for (int s = bt.nseg - 1; s >= 0; s--) {
+        const int t0 = s * bt.K, t1 = std::min(t0 + bt.K, bt.steps);
+        if (t1 <= t0)
+            continue;
+        cudaMemcpyAsync(bt.hbuf[0], bt.ckpt + (size_t)s * bt.N, nb, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(bt.hbuf[1], bt.ckpt + (size_t)s * bt.N, nb, cudaMemcpyDeviceToDevice, st);
+        for (int t = t0; t < t1; t++)
+            SDTB_DISPATCH(bt, launch_step, bt, t, bt.hbuf[(t - t0) & 1], bt.hbuf[(t - t0 + 1) & 1], false, bt.tape,
+                          bt.toff + t);
+        double* X = bt.hbuf[(t1 - t0) & 1];
+        for (int t = t1 - 1; t >= t0; t--) {
+            SDTB_DISPATCH(bt, launch_restore, bt, t, bt.tape, X, bt.toff + t);
+            SDTB_DISPATCH(bt, launch_adjoint, bt, t, X);
+        }
+    }
+    if (g_h0)
+        k_final_grad<<<dense_grid(bt.N), T, 0, st>>>(bt.h0, bt.lam, bt.lamz, g_h0, bt.N);
+    cudaMemcpyAsync(bt.h_out, bt.loss, bt.B * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(bt.h_out + bt.B, bt.grad, 2 * bt.B * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(bt.h_out + 3 * bt.B, bt.toff + bt.steps, sizeof(long long), cudaMemcpyDeviceToHost, st);
+}
+
+/* one evaluation as one launch of the recorded graph (recorded again when
+ * the target, the dL/dh0 buffer, the tile shape or the tape changed); when
+ * the tape was too small for a segment the evaluation is discarded, the
+ * tape grown to the size the device reported (plus a quarter) and the
+ * evaluation run again.  0 on success. */
+static int loss_grad_graph(Batch& bt, const double* target, double* loss_out, double* grad_out, double* g_h0)
+{
+    cudaStream_t st = bt.st;
+    if (!bt.toff && cudaMalloc(&bt.toff, sizeof(long long) * (bt.steps + 1)) != cudaSuccess)
+        return (int)cudaErrorMemoryAllocation;
+    if (!bt.h_out && cudaMallocHost(&bt.h_out, sizeof(double) * (3 * bt.B + 1)) != cudaSuccess)
+        return (int)cudaErrorMemoryAllocation;
+    for (int attempt = 0; attempt < 3; attempt++) {
+        if (!bt.gexec || bt.g_target != target || bt.g_gh0 != g_h0 || bt.g_shape != bt.shape ||
+            bt.g_tape != bt.tape) {
+            drop_graph(bt);
+            cudaGraph_t graph = nullptr;
+            if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                return (int)cudaGetLastError();
+            queue_loss_grad(bt, target, g_h0);
+            cudaError_t e = cudaStreamEndCapture(st, &graph);
+            if (e != cudaSuccess || !graph) {
+                (void)cudaGetLastError();
+                return (int)(e != cudaSuccess ? e : cudaErrorUnknown);
+            }
+            e = cudaGraphInstantiate(&bt.gexec, graph, 0);
+            size_t nodes = 0;
+            cudaGraphGetNodes(graph, nullptr, &nodes);
+            bt.graph_nodes = (long long)nodes;
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess)
+                return (int)e;
+            bt.g_target = target;
+            bt.g_gh0 = g_h0;
+            bt.g_shape = bt.shape;
+            bt.g_tape = bt.tape;
+        }
+        if (cudaGraphLaunch(bt.gexec, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
+            return (int)cudaGetLastError();
+        bt.graph_launches++;
+        long long need = 0;
+        memcpy(&need, bt.h_out + 3 * bt.B, sizeof(need));
+        if (need <= (long long)bt.tape_cap) {
+            if (loss_out)
+                memcpy(loss_out, bt.h_out, bt.B * sizeof(double));
+            if (grad_out)
+                for (int b = 0; b < bt.B; b++) {
+                    grad_out[2 * b] = bt.h_out[bt.B + b];
+                    grad_out[2 * b + 1] = bt.h_out[2 * bt.B + b];
+                }
+            return 0;
+        }
+        cudaFree(bt.tape);
+        bt.tape = nullptr;
+        bt.tape_cap = 0;
+        const size_t cap = (size_t)(need + need / 4);
+        if (cudaMalloc(&bt.tape, cap * sizeof(double)) != cudaSuccess) {
+            fprintf(stderr, "opencal-gb300: cal_sdt_batch_loss_grad: out of device memory for the tape\n");
+            return (int)cudaErrorMemoryAllocation;
+        }
+        bt.tape_cap = cap;
+    }
+    return (int)cudaErrorUnknown;
+}
+
+} // namespace sdtb
+
 /* Loss L_b = sum over instance b of (h_T - target)^2 and its gradients:
  * forward with checkpoints, then the adjoint.  target: device array in the
  * padded layout.  loss_out[B], grad_out[2B] (dL/dp_r, dL/dp_eps of each
@@ -710,6 +898,10 @@ extern "C" int cal_sdt_batch_loss_grad(void* handle, const double* target, doubl
                                        double* g_h0)
 {
     Batch* bt = (Batch*)handle;
+    /* segments of at most 32 steps (one warp each in k_tape_offsets):
+     * rollouts of up to 1024 steps run as one recorded graph */
+    if (bt->use_graph && bt->K <= 32 && bt->steps > 0)
+        return sdtb::loss_grad_graph(*bt, target, loss_out, grad_out, g_h0);
     const size_t nb = (size_t)bt->N * sizeof(double);
     const int tc = sdtb::tile_cells(*bt);
     cudaStream_t st = bt->st;
@@ -834,4 +1026,26 @@ extern "C" int cal_sdt_batch_set_shape(void* handle, int shape)
         return 1;
     bt->shape = shape;
     return sdtb::tiles_for(*bt) ? 0 : 2;
+}
+
+/* 1 (default): cal_sdt_batch_loss_grad runs as one launch of a recorded
+ * graph (rollouts of up to 1024 steps); 0: launch by launch with the tape
+ * layout computed on the host */
+extern "C" int cal_sdt_batch_set_graph(void* handle, int on)
+{
+    Batch* bt = (Batch*)handle;
+    bt->use_graph = on != 0;
+    return 0;
+}
+
+/* graph launches made by cal_sdt_batch_loss_grad so far and the nodes of
+ * the recorded evaluation (kernels and copies) */
+extern "C" int cal_sdt_batch_graph_stats(void* handle, long long* launches, long long* nodes)
+{
+    Batch* bt = (Batch*)handle;
+    if (launches)
+        *launches = bt->graph_launches;
+    if (nodes)
+        *nodes = bt->graph_nodes;
+    return 0;
 }

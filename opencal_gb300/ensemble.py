@@ -50,6 +50,8 @@ def _lib():
         m.cal_sdt_batch_forward.argtypes = [C.c_void_p, C.c_void_p]
         m.cal_sdt_batch_active_tiles.argtypes = [C.c_void_p, _pi]
         m.cal_sdt_batch_loss_grad.argtypes = [C.c_void_p, C.c_void_p, _pd, _pd, C.c_void_p]
+        m.cal_sdt_batch_set_graph.argtypes = [C.c_void_p, C.c_int]
+        m.cal_sdt_batch_graph_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
         m.cal_sdt_batch_autotune.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
         m.cal_sdt_batch_set_shape.argtypes = [C.c_void_p, C.c_int]
         m.cal_sciddicaT_open.restype = C.c_void_p
@@ -161,6 +163,16 @@ class Ensemble:
             raise CALError(f"cal_sdt_batch_loss_grad failed ({rc})")
         grad = grad.reshape(self.B, 2)
         return (loss, grad, gh0) if want_h0_grad else (loss, grad)
+
+    def set_graph(self, on: bool) -> None:
+        """loss_grad as one launch of a recorded graph (default) or launch by launch."""
+        self._lib.cal_sdt_batch_set_graph(self.handle, 1 if on else 0)
+
+    def graph_stats(self) -> tuple[int, int]:
+        """(graph launches made by loss_grad so far, nodes of the recorded evaluation)"""
+        a, b = C.c_longlong(0), C.c_longlong(0)
+        self._lib.cal_sdt_batch_graph_stats(self.handle, C.byref(a), C.byref(b))
+        return a.value, b.value
 
     def active_tiles(self) -> np.ndarray:
         out = np.zeros(self.steps + 1, dtype=np.int32)

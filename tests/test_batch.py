@@ -110,6 +110,30 @@ def test_gradients_match_single_model_adjoint(env):
         np.testing.assert_allclose(gh0[b], h0.grad.cpu().numpy(), rtol=1e-9, atol=1e-12)
 
 
+def test_recorded_evaluation_equals_launch_by_launch(env):
+    """loss_grad as one graph launch (tape layout on the device) against the
+    launch-by-launch evaluation: losses and gradients equal up to the
+    summation order of their atomics; a second call replays the same graph."""
+    torch, oracle, E, params, zs, hs = env
+    true = [(p[0] * 0.9, p[1] * 1.2) for p in params]
+    tgts = _refs(oracle, true, zs, hs, STEPS)
+    ens = E.Ensemble(DIMS, params, zs, hs, STEPS)
+    tgt = ens.pack(tgts)
+    ens.set_graph(False)
+    l0, g0, h0 = ens.loss_grad(tgt, want_h0_grad=True)
+    ens.set_graph(True)
+    l1, g1, h1 = ens.loss_grad(tgt, want_h0_grad=True)
+    launches, nodes = ens.graph_stats()
+    assert launches >= 1 and nodes > 4 * STEPS
+    l2, g2, _ = ens.loss_grad(tgt, want_h0_grad=True)
+    assert ens.graph_stats()[0] == launches + 1  # replayed: one launch, tape already large enough
+    np.testing.assert_allclose(l1, l0, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(l2, l0, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(g1, g0, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(g2, g0, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(h1.cpu().numpy(), h0.cpu().numpy(), rtol=1e-9, atol=1e-12)
+
+
 def test_fd_arm_agrees_with_adjoint(env):
     """central FD of the plain drop-in (the comparison arm) against the
     ensemble adjoint on one instance, at a point where no decision flips"""
