@@ -195,7 +195,11 @@ void calSwapSubstate2Db(struct CALModel2D* ca2D, struct CALSubstate2Db* Q);
 void calSwapSubstate2Di(struct CALModel2D* ca2D, struct CALSubstate2Di* Q);
 void calSwapSubstate2Dr(struct CALModel2D* ca2D, struct CALSubstate2Dr* Q);
 /* Device pointers of the active-cell state: flags (rows*columns bytes), the
- * compacted list and its length (an int in device memory). */
+ * compacted list and its length (an int in device memory).  Flags written
+ * through the pointer are taken into account by the next
+ * calUpdateActiveCells2D, or by the next update after calMarkDeviceWritten2D
+ * (the updates that follow a process otherwise keep the list when no process
+ * changed a flag). */
 void calGetDeviceActiveCells2D(struct CALModel2D* ca2D, CALbyte** flags, struct CALCell2D** cells, int** count);
 /* Number of active cells, read from the device (synchronises). */
 int calGetActiveCellCount2D(struct CALModel2D* ca2D);

@@ -45,6 +45,7 @@ struct CALDevModel2D {
     void* cur[3][CAL_MAX_SUBSTATES];
     void* nxt[3][CAL_MAX_SUBSTATES];
     unsigned int* dirty;         /* [3] bitmasks: substates whose next layer was written */
+    unsigned int* flags_dirty;   /* set when a process changed an active-cell flag (NULL: not kept) */
     int* step;                   /* current step of a device-driven run (calRunDevice2D) */
     CALbyte* flags;              /* active-cell flags, NULL without the optimisation */
     struct CALCell2D* cells;     /* compacted active list */
@@ -86,6 +87,8 @@ static __shared__ unsigned char cal_written2D[3 * CAL_MAX_SUBSTATES];
  * substates written by unsafe operations */
 static __shared__ unsigned char cal_chg2D[CAL_EP_THREADS / 32][3 * CAL_MAX_SUBSTATES];
 static __shared__ unsigned char cal_untracked2D[3 * CAL_MAX_SUBSTATES];
+/* per block: a process changed an active-cell flag */
+static __shared__ unsigned char cal_flagchg2D;
 
 template <typename T>
 static __device__ __forceinline__ bool cal_same_bits(T a, T b)
@@ -210,11 +213,23 @@ static __device__ __forceinline__ void cal_init2D(const struct CALModel2D* ca, i
         cal_mark_chg2D(t, s); /* the tile no longer holds the substate's uniform value */
 }
 
+/* flag writes: only a changed flag is stored, and the block notes it (the
+ * compaction after the process keeps the list when no block did) */
+static __device__ __forceinline__ void cal_setflag2D(const struct CALDevModel2D* m, long long c, CALbyte v)
+{
+    if (!m->flags) /* a model without active cells: nothing to record */
+        return;
+    if (m->flags[c] != v) {
+        m->flags[c] = v;
+        cal_flagchg2D = 1;
+    }
+}
+
 static __device__ __forceinline__ void cal_addactive2D(const struct CALModel2D* ca, int i, int j)
 {
     const struct CALDevModel2D* m = cal_dm2D(ca);
     if ((unsigned)i < (unsigned)m->rows && (unsigned)j < (unsigned)m->cols)
-        m->flags[cal_lin2D(m, i, j)] = 1;
+        cal_setflag2D(m, cal_lin2D(m, i, j), 1);
 }
 
 static __device__ __forceinline__ void cal_addactivex2D(const struct CALModel2D* ca, int i, int j, int n)
@@ -222,13 +237,13 @@ static __device__ __forceinline__ void cal_addactivex2D(const struct CALModel2D*
     const struct CALDevModel2D* m = cal_dm2D(ca);
     int a, b;
     if (cal_nbr2D(m, i, j, n, a, b))
-        m->flags[cal_lin2D(m, a, b)] = 1;
+        cal_setflag2D(m, cal_lin2D(m, a, b), 1);
 }
 
 static __device__ __forceinline__ void cal_removeactive2D(const struct CALModel2D* ca, int i, int j)
 {
     const struct CALDevModel2D* m = cal_dm2D(ca);
-    m->flags[cal_lin2D(m, i, j)] = 0;
+    cal_setflag2D(m, cal_lin2D(m, i, j), 0);
 }
 
 /* the step number a device-driven run is executing (calRunDevice2D); the
@@ -264,6 +279,8 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     }
     for (int t = lane; t < 3 * CAL_MAX_SUBSTATES; t += 32)
         cal_chg2D[warp][t] = 0;
+    if (threadIdx.x == 0)
+        cal_flagchg2D = 0;
     __syncthreads();
     struct CALModel2D view = cal_model_view2D<NX>(m);
     struct CALModel2D* ca = &view;
@@ -311,6 +328,8 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         if (cal_untracked2D[t] && m.untracked)
             atomicOr(&m.untracked[t / CAL_MAX_SUBSTATES], 1u << (t % CAL_MAX_SUBSTATES));
     }
+    if (threadIdx.x == 0 && cal_flagchg2D && m.flags_dirty)
+        *m.flags_dirty = 1;
 }
 
 /* one kernel per common neighbourhood size (von Neumann 5, hexagonal 7,
@@ -345,7 +364,10 @@ __global__ void cal_stop2D_kernel(const __grid_constant__ struct CALDevModel2D m
                                   int use_handle, int final_step, int* flag)
 {
     struct CALModel2D view = cal_model_view2D<0>(m);
+    cal_flagchg2D = 0;
     const bool stop = STOP(&view) != 0;
+    if (cal_flagchg2D && m.flags_dirty)
+        *m.flags_dirty = 1;
     int again = 0;
     if (!stop) {
         const int next = *m.step + 1;

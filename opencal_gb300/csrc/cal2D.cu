@@ -145,6 +145,7 @@ static bool build_desc(struct CALModel2D* ca, CALDevModel2D* d)
         }
     }
     d->dirty = g.d_dirty;
+    d->flags_dirty = g.flags_dirty_word();
     d->step = g.d_step;
     d->flags = (CALbyte*)g.d_flags;
     d->cells = (struct CALCell2D*)g.d_cells;
@@ -438,6 +439,13 @@ static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned
     d.run = run;
     int gx, gy;
     g.launch_grid(&gx, &gy);
+    if (g.active) {
+        /* the active list, one cell per thread: 608 blocks of 256 threads
+         * (four resident per SM) cover 155K cells a pass, and fewer blocks
+         * launch faster than the dense grid */
+        gx = 1;
+        gy = 152 * 4;
+    }
     int rc = launch(&d, gx, gy, (void*)g.stream);
     if (rc != 0) {
         cal::cuda_ok((cudaError_t)rc, "elementary process launch");
@@ -651,6 +659,7 @@ extern "C" void calMarkDeviceWritten2D(struct CALModel2D* ca)
 {
     CalGrid& g = G(ca);
     g.device_wrote_all();
+    g.mark_flags_changed(); /* the active flags may have been written too */
     for (int t = 0; t < CAL_NTYPES; t++)
         for (int s = 0; s < g.nslot[t]; s++)
             g.untrack(t, s); /* written outside the library: no change tracking from now on */

@@ -303,6 +303,12 @@ static const int kScratchHead = 32;                        /* ticket line */
 struct CompactGeom {
     int dim, rows, cols, slices;
     long long n;
+    /* non-NULL: a word that the process kernels set when they changed a
+     * flag; while it is 0 the list of the previous compaction (still in
+     * cells, lin, count and the block offsets in scratch) is the answer and
+     * both passes keep it.  The count pass's last block records its decision
+     * in scratch[1] for the scatter pass and clears the word. */
+    unsigned* dirty;
 };
 
 static __device__ __forceinline__ long long order_to_mem(const CompactGeom& g, long long v)
@@ -357,21 +363,29 @@ __global__ void __launch_bounds__(kThreads) k_compact_count(const unsigned char*
                                                               int* scratch, int* count)
 {
     __shared__ int s_warp[kThreads / 32];
-    __shared__ int s_last;
+    __shared__ int s_last, s_go;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long base = (long long)blockIdx.x * kChunk + (long long)warp * kWarpSpan + lane;
-    int c = 0;
-#pragma unroll
-    for (int q = 0; q < kRounds; q++)
-        c += __popc(__ballot_sync(0xffffffffu, flag_at(flags, g, base + 32 * q)));
-    if (lane == 0)
-        s_warp[warp] = c;
+    if (threadIdx.x == 0)
+        s_go = g.dirty ? (*(volatile const unsigned*)g.dirty != 0) : 1; /* the same for every block */
     __syncthreads();
+    const int go = s_go;
+    if (go) {
+        const long long base = (long long)blockIdx.x * kChunk + (long long)warp * kWarpSpan + lane;
+        int c = 0;
+#pragma unroll
+        for (int q = 0; q < kRounds; q++)
+            c += __popc(__ballot_sync(0xffffffffu, flag_at(flags, g, base + 32 * q)));
+        if (lane == 0)
+            s_warp[warp] = c;
+        __syncthreads();
+    }
     if (threadIdx.x == 0) {
-        int s = 0;
-        for (int w = 0; w < kThreads / 32; w++)
-            s += s_warp[w];
-        scratch[kScratchHead + blockIdx.x] = s;
+        if (go) {
+            int s = 0;
+            for (int w = 0; w < kThreads / 32; w++)
+                s += s_warp[w];
+            scratch[kScratchHead + blockIdx.x] = s;
+        }
         __threadfence(); /* the count is visible before the ticket is taken */
         s_last = atomicAdd(reinterpret_cast<unsigned*>(scratch), 1u) == gridDim.x - 1;
     }
@@ -379,9 +393,14 @@ __global__ void __launch_bounds__(kThreads) k_compact_count(const unsigned char*
     if (!s_last)
         return;
     __threadfence();
-    block_exclusive_scan(scratch + kScratchHead, gridDim.x, count);
-    if (threadIdx.x == 0)
-        scratch[0] = 0; /* every ticket of this call has been taken */
+    if (go)
+        block_exclusive_scan(scratch + kScratchHead, gridDim.x, count);
+    if (threadIdx.x == 0) {
+        scratch[1] = go;      /* the scatter pass's decision */
+        if (g.dirty)
+            *g.dirty = 0;     /* every block has read it */
+        scratch[0] = 0;       /* every ticket of this call has been taken */
+    }
 }
 
 /* next -> current at the listed cells, fused into the scatter pass of the
@@ -472,7 +491,8 @@ static __device__ __forceinline__ void compact_scatter(const unsigned char* __re
 __global__ void __launch_bounds__(kThreads) k_compact_scatter(const unsigned char* __restrict__ flags, CompactGeom g,
                                                                 const int* __restrict__ scratch, int* cells, int* lin)
 {
-    compact_scatter<false>(flags, g, scratch, cells, lin, nullptr);
+    if (scratch[1])
+        compact_scatter<false>(flags, g, scratch, cells, lin, nullptr);
 }
 
 __global__ void __launch_bounds__(kThreads) k_compact_scatter_update(const unsigned char* __restrict__ flags,
@@ -480,8 +500,18 @@ __global__ void __launch_bounds__(kThreads) k_compact_scatter_update(const unsig
                                                                        int* cells, int* lin,
                                                                        const __grid_constant__ ActiveCopy u)
 {
-    if (*u.count > 0) {
+    const int listed = *u.count;
+    if (listed > 0 && scratch[1]) {
         compact_scatter<true>(flags, g, scratch, cells, lin, &u);
+        return;
+    }
+    if (listed > 0) {
+        /* the flags did not change: the previous list, this block's slots */
+        const int first = scratch[kScratchHead + blockIdx.x];
+        const int last = blockIdx.x + 1 < gridDim.x ? scratch[kScratchHead + blockIdx.x + 1] : listed;
+        for (int e = 0; e < u.n; e++)
+            for (int k = first + threadIdx.x; k < last; k += kThreads)
+                copy_elem(u, e, lin[k]);
         return;
     }
     /* no active cell: every cell of this block's range (linear memory) */
@@ -503,9 +533,10 @@ long long compact_scratch_ints(long long ncells)
 }
 
 cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int cols, int slices, int* cells, int* lin,
-                          int* count, int* scratch, long long scratch_ints, cudaStream_t stream)
+                          int* count, int* scratch, long long scratch_ints, cudaStream_t stream, unsigned* dirty)
 {
     CompactGeom g;
+    g.dirty = dirty;
     g.dim = dim;
     g.rows = rows;
     g.cols = cols;
@@ -523,9 +554,10 @@ cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int col
  * list's cells (every cell when the list is empty) in its scatter pass */
 static cudaError_t compact_and_copy(const unsigned char* flags, int dim, int rows, int cols, int slices, int* cells,
                                     int* lin, int* count, int* scratch, long long scratch_ints, const ActiveCopy& u,
-                                    cudaStream_t stream)
+                                    cudaStream_t stream, unsigned* dirty)
 {
     CompactGeom g;
+    g.dirty = dirty;
     g.dim = dim;
     g.rows = rows;
     g.cols = cols;
@@ -613,6 +645,9 @@ bool CalGrid::init(int dim_, int rows_, int cols_, int slices_, int toroidal_, i
                      "memset scratch") ||
             !cuda_ok(cudaMemsetAsync(d_flags, 0, (size_t)ncells, stream), "memset flags"))
             return false;
+        if (dim == 2 && (!cuda_ok(cudaMalloc(&d_flags_dirty, sizeof(unsigned)), "cudaMalloc flags word") ||
+                         !cuda_ok(cudaMemsetAsync(d_flags_dirty, 0xff, sizeof(unsigned), stream), "set flags word")))
+            return false;
         if (!cuda_ok(cudaMallocHost(&h_flags, (size_t)ncells), "cudaMallocHost flags"))
             return false;
         memset(h_flags, 0, (size_t)ncells);
@@ -638,6 +673,7 @@ void CalGrid::destroy()
         pool[t] = nullptr;
     }
     cudaFree(d_flags);
+    cudaFree(d_flags_dirty);
     cudaFree(d_cells);
     cudaFree(d_lin);
     cudaFree(d_count);
@@ -716,6 +752,9 @@ bool CalGrid::to_device_all()
         }
         if (!cuda_ok(cudaMemcpyAsync(d_flags, h_flags, (size_t)ncells, cudaMemcpyHostToDevice, stream),
                      "upload flags"))
+            return false;
+        if (d_flags_dirty &&
+            !cuda_ok(cudaMemsetAsync(d_flags_dirty, 0xff, sizeof(unsigned), stream), "set flags word"))
             return false;
         flags_dev_valid = true;
         transfers++;
@@ -1062,14 +1101,22 @@ bool CalGrid::copy_next_to_current(const std::vector<std::pair<int, int>>& which
     return true;
 }
 
+bool CalGrid::mark_flags_changed()
+{
+    return !d_flags_dirty ||
+           cuda_ok(cudaMemsetAsync(d_flags_dirty, 0xff, sizeof(unsigned), stream), "set flags word");
+}
+
+/* calUpdateActiveCells2D: always a full compaction (flags may have been
+ * written through the device pointer) */
 bool CalGrid::compact()
 {
     if (!active)
         return true;
-    if (!to_device_all())
+    if (!to_device_all() || !mark_flags_changed())
         return false;
     return cuda_ok(compact_flags(d_flags, dim, rows, cols, slices, d_cells, d_lin, d_count, d_block_counts,
-                                 scratch_ints, stream),
+                                 scratch_ints, stream, flags_dirty_word()),
                    "active-cell compaction");
 }
 
@@ -1109,7 +1156,7 @@ bool CalGrid::update_all()
             }
         u.count = d_count;
         if (!cuda_ok(compact_and_copy(d_flags, dim, rows, cols, slices, d_cells, d_lin, d_count, d_block_counts,
-                                      scratch_ints, u, stream),
+                                      scratch_ints, u, stream, flags_dirty_word()),
                      "active-cell compaction and update"))
             return false;
         for (int t = 0; t < CAL_NTYPES; t++)

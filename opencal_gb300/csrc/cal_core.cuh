@@ -96,6 +96,14 @@ struct CalGrid {
     long long scratch_ints = 0;
     bool flags_host_valid = true, flags_dev_valid = true;
     unsigned char* h_flags = nullptr; /* host mirror (pinned) */
+    /* 2D: a device word the process kernels set when they change a flag, so
+     * that a compaction after a process that changed none keeps the list
+     * (cal_core.cu, CompactGeom::dirty); flags written through the handed-out
+     * device pointer are seen by the next explicit compaction
+     * (calUpdateActiveCells2D) or after calMarkDeviceWritten2D, which set it */
+    unsigned* d_flags_dirty = nullptr;
+    unsigned* flags_dirty_word() const { return d_flags_dirty; }
+    bool mark_flags_changed();
 
     unsigned* d_dirty = nullptr; /* [3] written-substate bits */
     /* change tracking: CAL_TILE_W x CAL_TILE_H tiles (include/opencal/
@@ -173,7 +181,8 @@ struct CalGrid {
  * holds compact_scratch_ints(cells) ints, the first of which (the ticket)
  * must be 0 before the first call: every call leaves it at 0 */
 cudaError_t compact_flags(const unsigned char* flags, int dim, int rows, int cols, int slices, int* cells, int* lin,
-                          int* count, int* scratch, long long scratch_ints, cudaStream_t stream);
+                          int* count, int* scratch, long long scratch_ints, cudaStream_t stream,
+                          unsigned* dirty = nullptr);
 int compact_blocks_needed(long long ncells);
 long long compact_scratch_ints(long long ncells);
 

@@ -6,7 +6,10 @@ SCIDDICA-T (the reference program with both processes declared pure, flat
 and toroidal grids, per-step launches, recorded-step replay and the
 device-driven loop, including the reference's shipped 610 x 496 golden) and
 on Life defined from Python, and for a custom neighbourhood that reaches
-further than one tile (skipping refused, still exact).
+further than one tile (skipping refused, still exact).  Also the active-cell
+counterpart: the compaction after a process that changed no flag keeps the
+list (a session reset that rewrites the flags through their device pointer
+must still be seen).
 """
 import hashlib
 import json
@@ -135,3 +138,37 @@ def test_far_reaching_custom_neighbourhood_is_not_skipped():
             model.close()
     assert out[0].tobytes() == out[1].tobytes()
     assert out[0].any()
+
+
+def test_active_cells_session_reset_and_rerun():
+    """The active-cells program through a session: run, reset (the flags
+    restored through their device pointer, then calUpdateActiveCells2D),
+    run again.  The compactions after processes that changed no flag keep
+    the list; both runs must give the oracle's h and active set."""
+    import ctypes as C
+    import oracle
+    import opencal_gb300 as cal
+    from opencal_gb300 import workloads as W
+    cal.build()
+    oracle.build()
+    z, h = W.sciddicaT_inputs(160, 144, seed=11)
+    steps = 50
+    ref = oracle.sciddicaT(z, h, steps, toroidal=False, ac=True)
+    m = cal.models()
+    m.cal_sciddicaT_open.restype = C.c_void_p
+    m.cal_sciddicaT_open.argtypes = [C.c_int] * 4 + [C.c_double] * 2 + [C.c_void_p] * 2 + [C.c_int]
+    for fn in ("cal_sciddicaT_reset", "cal_sciddicaT_close"):
+        getattr(m, fn).argtypes = [C.c_void_p]
+    m.cal_sciddicaT_steps.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    m.cal_sciddicaT_read.argtypes = [C.c_void_p, C.c_void_p]
+    sess = m.cal_sciddicaT_open(160, 144, 0, 1, 0.5, 0.001, z.ctypes.data, h.ctypes.data, cal.MODE_PROCESSES)
+    assert sess
+    try:
+        for loop in (0, 1, 2):
+            assert m.cal_sciddicaT_reset(sess) == 0
+            assert m.cal_sciddicaT_steps(sess, steps, loop) == 0
+            out = np.empty_like(h)
+            assert m.cal_sciddicaT_read(sess, out.ctypes.data) == 0
+            assert out.tobytes() == ref[1].tobytes(), loop
+    finally:
+        m.cal_sciddicaT_close(sess)
