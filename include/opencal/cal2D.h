@@ -49,6 +49,7 @@ enum CALNeighborhood2D {
 #define CAL_MAX_SUBSTATES 32          /* per type, double- and single-layer together */
 #define CAL_MAX_NEIGHBORS 64          /* entries of the neighbourhood table */
 #define CAL_MAX_ELEMENTARY_PROCESSES 32
+#define CAL_MAX_STAGED 8              /* substates a process may declare it reads (staged by TMA) */
 
 /* cal2D.h:44-50.  flags/cells are host mirrors refreshed by calSync2D. */
 struct CALActiveCells2D {
@@ -239,6 +240,22 @@ int calCompactActiveCellsNoAlloc2D(const CALbyte* flags, int rows, int columns, 
  * in the reference (a performance declaration; the reference runs every
  * cell).  Returns a CALError code. */
 int calSetElementaryProcessPure2D(struct CALModel2D* ca2D, CALCallbackFunc2D elementary_process, CALbyte pure);
+
+/* Declares the substates (up to CAL_MAX_STAGED handles of any type) whose
+ * current layer an elementary process reads with calGet / calGetX, and that
+ * it does not write in their current layer.  Then, in a model without
+ * active cells, the process kernel stages those substates' 32 x 8 tile plus
+ * the neighbourhood's halo into shared memory with one TMA tensor copy per
+ * substate and tile (cp.async.bulk.tensor, zero fill outside a flat grid;
+ * in a toroidal grid the tiles along the border read global memory), and
+ * calGet / calGetX read them there.  Substates whose rows are not a
+ * multiple of 16 bytes, or neighbourhoods reaching further than 8 rows or
+ * (for 8-, 4-, 1-byte cells) 2, 4, 16 columns, keep global reads.  The
+ * results are those of global reads.  count 0 withdraws the declaration.
+ * No counterpart in the reference (a performance declaration).  Returns a
+ * CALError code. */
+int calSetElementaryProcessReads2D(struct CALModel2D* ca2D, CALCallbackFunc2D elementary_process,
+                                   const void* const* substates, int count);
 
 /* Registration of device elementary processes (used by
  * CAL_ELEMENTARY_PROCESS_2D; not called directly). */

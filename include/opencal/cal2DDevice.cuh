@@ -29,6 +29,7 @@
 #ifndef cal2DDevice_cuh
 #define cal2DDevice_cuh
 
+#include <cuda.h> /* CUtensorMap */
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -37,6 +38,9 @@
 #define CAL_TYPE_R 2
 #define CAL_HANDLE_SHIFT 5 /* log2(sizeof(struct CALSubstate2Dr)) */
 #define CAL_EP_THREADS 256
+#ifndef CAL_MAX_STAGED
+#define CAL_MAX_STAGED 8 /* substates a process may declare it reads (calSetElementaryProcessReads2D) */
+#endif
 
 /* Launch descriptor of one elementary-process kernel. */
 struct CALDevModel2D {
@@ -74,6 +78,24 @@ struct CALDevModel2D {
      * skips the other tiles and clears the bit of every tile where it
      * changed nothing */
     unsigned int* run;
+    /* TMA staging of the substates a process declared it reads
+     * (calSetElementaryProcessReads2D); nstage == 0: none.  On every tile
+     * that the process runs on (in toroidal grids only tiles off the grid's
+     * border), box k -- (CAL_TILE_W + 2 * hx) x (CAL_TILE_H + 2 * stage_r)
+     * elements from (j0 - hx, i0 - stage_r), hx = 16 / element size, so
+     * that the box starts on a 16-byte boundary -- is loaded into the
+     * dynamic shared memory at stage_off[k] bytes by one
+     * cp.async.bulk.tensor.2d through stage_map[k] (zero fill outside the
+     * grid: the flat boundary's "absent neighbours read 0"), and the
+     * accessors read the staged substates there.  stage_of[type][slot] = k
+     * or -1; stage_tx: the bytes the boxes bring (the mbarrier's
+     * transaction count); stage_bytes: the dynamic shared memory. */
+    int nstage, stage_r, stage_tx, stage_bytes;
+    int stage_off[CAL_MAX_STAGED];
+    int stage_hx[CAL_MAX_STAGED]; /* 16 / element size: 16, 4, 2 (x stays 16-byte aligned) */
+    signed char stage_of[3][CAL_MAX_SUBSTATES];
+    int* stage_err; /* set when a box did not arrive in time (the tile then reads global memory) */
+    CUtensorMap stage_map[CAL_MAX_STAGED];
 };
 
 
@@ -89,6 +111,50 @@ static __shared__ unsigned char cal_chg2D[CAL_EP_THREADS / 32][3 * CAL_MAX_SUBST
 static __shared__ unsigned char cal_untracked2D[3 * CAL_MAX_SUBSTATES];
 /* per block: a process changed an active-cell flag */
 static __shared__ unsigned char cal_flagchg2D;
+/* per block: the current tile is staged, its origin, the staging barrier */
+static __shared__ int cal_stage_on2D, cal_stage_i02D, cal_stage_j02D;
+static __shared__ __align__(8) unsigned long long cal_stage_bar2D;
+extern __shared__ __align__(128) unsigned char cal_stage_mem2D[];
+
+/* ---- TMA: mbarrier with a transaction count, tiled 2D loads, bounded wait */
+static __device__ __forceinline__ uint32_t cal_smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+static __device__ __forceinline__ void cal_bar_init(unsigned long long* bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cal_smem_u32(bar)) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+static __device__ __forceinline__ void cal_bar_expect(unsigned long long* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(cal_smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+static __device__ __forceinline__ void cal_tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                                       unsigned long long* bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(cal_smem_u32(dst)),
+                 "l"(map), "r"(x), "r"(y), "r"(cal_smem_u32(bar))
+                 : "memory");
+}
+static __device__ __forceinline__ bool cal_bar_wait(unsigned long long* bar, uint32_t parity, uint32_t limit)
+{
+    for (uint32_t k = 0; k < limit; k++) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(cal_smem_u32(bar)), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+#define CAL_STAGE_WAIT_LIMIT (1u << 20)
 
 template <typename T>
 static __device__ __forceinline__ bool cal_same_bits(T a, T b)
@@ -150,21 +216,48 @@ static __device__ __forceinline__ bool cal_nbr2D(const struct CALDevModel2D* m, 
     return (unsigned)ni < (unsigned)m->rows && (unsigned)nj < (unsigned)m->cols;
 }
 
+/* the staged copy of substate (t, slot) at (a, b), when the current tile is
+ * staged and the substate is one of the declared reads; NULL otherwise */
+template <typename T>
+static __device__ __forceinline__ const T* cal_staged2D(const struct CALDevModel2D* m, int t, int s, int a, int b)
+{
+    if (!m->nstage || !cal_stage_on2D)
+        return nullptr;
+    const int k = m->stage_of[t][s];
+    if (k < 0)
+        return nullptr;
+    constexpr int hx = 16 / (int)sizeof(T);
+    constexpr int bw = CAL_TILE_W + 2 * hx;
+    const T* box = reinterpret_cast<const T*>(cal_stage_mem2D + m->stage_off[k]);
+    return box + (a - cal_stage_i02D + m->stage_r) * bw + (b - cal_stage_j02D + hx);
+}
+
 template <typename T>
 static __device__ __forceinline__ T cal_get2D(const struct CALModel2D* ca, int t, const void* q, int i, int j)
 {
     const struct CALDevModel2D* m = cal_dm2D(ca);
-    return static_cast<const T*>(m->cur[t][cal_slot2D(m, t, q)])[cal_lin2D(m, i, j)];
+    const int s = cal_slot2D(m, t, q);
+    if (const T* p = cal_staged2D<T>(m, t, s, i, j))
+        return *p;
+    return static_cast<const T*>(m->cur[t][s])[cal_lin2D(m, i, j)];
 }
 
 template <typename T>
 static __device__ __forceinline__ T cal_getx2D(const struct CALModel2D* ca, int t, const void* q, int i, int j, int n)
 {
     const struct CALDevModel2D* m = cal_dm2D(ca);
+    const int s = cal_slot2D(m, t, q);
+    if (m->nstage && cal_stage_on2D) {
+        /* a staged tile lies inside a toroidal grid or the box's zero fill
+         * is the flat boundary: the neighbour is read without wrapping */
+        const int nn = ((m->hex == 1 && (j & 1)) || (m->hex == 2 && (i & 1))) ? n + CAL_HEXAGONAL_SHIFT : n;
+        if (const T* p = cal_staged2D<T>(m, t, s, i + m->xi[nn], j + m->xj[nn]))
+            return *p;
+    }
     int a, b;
     if (!cal_nbr2D(m, i, j, n, a, b))
         return (T)0;
-    return static_cast<const T*>(m->cur[t][cal_slot2D(m, t, q)])[cal_lin2D(m, a, b)];
+    return static_cast<const T*>(m->cur[t][s])[cal_lin2D(m, a, b)];
 }
 
 /* the tile of a tracked process changed substate (t, s): flagged for the
@@ -279,10 +372,16 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     }
     for (int t = lane; t < 3 * CAL_MAX_SUBSTATES; t += 32)
         cal_chg2D[warp][t] = 0;
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         cal_flagchg2D = 0;
+        cal_stage_on2D = 0;
+        if (m.nstage)
+            cal_bar_init(&cal_stage_bar2D);
+    }
     __syncthreads();
     struct CALModel2D view = cal_model_view2D<NX>(m);
+    int nstage = m.nstage;  /* 0 after a box failed to arrive: global reads for the rest */
+    uint32_t phase = 0;
     struct CALModel2D* ca = &view;
     const int listed = m.use_list ? *m.count : 0;
     const int nblocks = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
@@ -298,10 +397,39 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
             const unsigned tbit = 1u << (tile & 31);
             if (m.run && !(m.run[tile >> 5] & tbit))
                 continue; /* unchanged neighbourhood, no-op last time (block-uniform) */
-            const int ty = tile / m.tiles_x;
-            const int i = ty * CAL_TILE_H + warp, j = (tile - ty * m.tiles_x) * CAL_TILE_W + lane;
+            const int ty = tile / m.tiles_x, tx = tile - ty * m.tiles_x;
+            const int i = ty * CAL_TILE_H + warp, j = tx * CAL_TILE_W + lane;
+            if (nstage) {
+                /* toroidal grids: only tiles whose boxes need no wrap */
+                const bool stage = !m.toroidal || (ty > 0 && tx > 0 && ty < m.tiles_y - 1 && tx < m.tiles_x - 1);
+                if (stage && threadIdx.x == 0) {
+                    cal_stage_i02D = ty * CAL_TILE_H;
+                    cal_stage_j02D = tx * CAL_TILE_W;
+                    cal_bar_expect(&cal_stage_bar2D, (uint32_t)m.stage_tx);
+                    for (int k = 0; k < nstage; k++)
+                        cal_tma_load_2d(cal_stage_mem2D + m.stage_off[k], &m.stage_map[k],
+                                        tx * CAL_TILE_W - m.stage_hx[k], ty * CAL_TILE_H - m.stage_r,
+                                        &cal_stage_bar2D);
+                }
+                bool arrived = true;
+                if (stage) {
+                    arrived = cal_bar_wait(&cal_stage_bar2D, phase, CAL_STAGE_WAIT_LIMIT);
+                    phase ^= 1u;
+                }
+                if (threadIdx.x == 0)
+                    cal_stage_on2D = stage && arrived;
+                if (!__syncthreads_and(arrived)) {
+                    /* a box did not arrive: record it; this tile and the
+                     * rest read global memory */
+                    if (threadIdx.x == 0 && m.stage_err)
+                        atomicExch(m.stage_err, 1);
+                    nstage = 0;
+                }
+            }
             if (i < m.rows && j < m.cols)
                 EP(ca, i, j);
+            if (nstage)
+                __syncthreads(); /* every staged read done before the next tile's boxes land */
             if (m.track) {
                 bool changed = false;
                 __syncwarp();
@@ -339,11 +467,12 @@ static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* 
 {
     const dim3 grid(gx, gy);
     cudaStream_t st = (cudaStream_t)stream;
+    const size_t smem = m->nstage ? (size_t)m->stage_bytes : 0;
     switch (m->model.sizeof_X) {
-    case 5: cal_ep2D_kernel<EP, 5><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
-    case 7: cal_ep2D_kernel<EP, 7><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
-    case 9: cal_ep2D_kernel<EP, 9><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
-    default: cal_ep2D_kernel<EP, 0><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+    case 5: cal_ep2D_kernel<EP, 5><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+    case 7: cal_ep2D_kernel<EP, 7><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+    case 9: cal_ep2D_kernel<EP, 9><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+    default: cal_ep2D_kernel<EP, 0><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
     }
     return (int)cudaGetLastError();
 }

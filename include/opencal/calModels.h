@@ -57,6 +57,11 @@ int cal_sciddicaT_set_params(void* session, double p_r, double p_eps);
  * (calSetElementaryProcessPure2D), so that the engine skips quiet tiles;
  * 0 (default): the reference program as it stands */
 int cal_sciddicaT_set_pure(int on);
+/* 1: models created afterwards (processes mode) declare what the two plain
+ * processes read (calSetElementaryProcessReads2D: z and h; h and the four
+ * outflows), so that their kernels stage those substates by TMA; 0
+ * (default): global reads */
+int cal_sciddicaT_set_staged(int on);
 /* launch grids of the split step's kernels: k1_blocks and k2_blocks
  * 256-thread blocks of the outflow and the update kernel (0 = the defaults
  * 608 / 608) */

@@ -19,6 +19,7 @@
 #include <algorithm>
 
 #include "cal_model_internal.cuh"
+#include "cal_tma.cuh"
 #include "opencal/cal2DUnsafe.h"
 
 using cal::CalGrid;
@@ -427,8 +428,59 @@ CAL_SUBSTATE_OPS_2D(r, CALreal, 2)
 
 /* ======================= transition ===================================== */
 
-/* run: the process's must-run bitmap when its tiles may be skipped */
-static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned* run = nullptr)
+/* TMA staging of process b's declared reads into the descriptor: one
+ * tensor map per substate over its current layer; nothing staged (global
+ * reads, same results) when the model keeps an active list, a substate's
+ * rows are not a multiple of 16 bytes, the neighbourhood reaches further
+ * than the box's halo, or the boxes would not fit in 48 KB */
+static void stage_reads(struct CALModel2D* ca, int b, CALDevModel2D* d)
+{
+    CalGrid& g = G(ca);
+    const int n = ca->gpu->nreads[b];
+    if (n <= 0 || g.active || g.dim != 2)
+        return;
+    int ri = 0, rj = 0;
+    const int len = table_len(ca);
+    for (int k = 0; k < len; k++) {
+        ri = std::max(ri, std::abs(ca->X[k].i));
+        rj = std::max(rj, std::abs(ca->X[k].j));
+    }
+    if (ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_2D || ca->X_id == CAL_HEXAGONAL_NEIGHBORHOOD_ALT_2D) {
+        ri = std::max(ri, 1);
+        rj = std::max(rj, 1);
+    }
+    if (ri > CAL_TILE_H)
+        return;
+    static const CUtensorMapDataType kType[3] = {CU_TENSOR_MAP_DATA_TYPE_UINT8, CU_TENSOR_MAP_DATA_TYPE_INT32,
+                                                 CU_TENSOR_MAP_DATA_TYPE_FLOAT64};
+    int off = 0, tx = 0;
+    for (int k = 0; k < n; k++) {
+        const int t = ca->gpu->read_t[b][k], s = ca->gpu->read_s[b][k];
+        const cal::Sub& q = g.sub[t][s];
+        const int es = (int)q.elem, hx = 16 / es;
+        if (!q.used || rj > hx)
+            return;
+        const int bw = CAL_TILE_W + 2 * hx, bh = CAL_TILE_H + 2 * ri;
+        if (!caltma::encode_2d(&d->stage_map[k], q.layer[0].dev, kType[t], es, ca->rows, ca->columns, bw, bh))
+            return;
+        d->stage_off[k] = off;
+        d->stage_hx[k] = hx;
+        d->stage_of[t][s] = (signed char)k;
+        off += (bw * bh * es + 127) & ~127;
+        tx += bw * bh * es;
+    }
+    if (off > 48 * 1024 || !ca->gpu->d_stage_err)
+        return;
+    d->nstage = n;
+    d->stage_r = ri;
+    d->stage_tx = tx;
+    d->stage_bytes = off;
+    d->stage_err = ca->gpu->d_stage_err;
+}
+
+/* run: the process's must-run bitmap when its tiles may be skipped; b: the
+ * process's index (its declared reads are staged), -1 for none */
+static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned* run = nullptr, int b = -1)
 {
     CalGrid& g = G(ca);
     if (!g.repair_all_stale() || !g.to_device_all())
@@ -437,6 +489,15 @@ static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned
     if (!build_desc(ca, &d))
         return;
     d.run = run;
+    for (int t = 0; t < 3; t++)
+        for (int s = 0; s < CAL_MAX_SUBSTATES; s++)
+            d.stage_of[t][s] = -1;
+    if (b >= 0)
+        stage_reads(ca, b, &d);
+    if (!d.nstage)
+        for (int t = 0; t < 3; t++)
+            for (int s = 0; s < CAL_MAX_SUBSTATES; s++)
+                d.stage_of[t][s] = -1;
     int gx, gy;
     g.launch_grid(&gx, &gy);
     if (g.active) {
@@ -530,9 +591,62 @@ extern "C" void calGlobalTransitionFunction2D(struct CALModel2D* ca)
     const bool skip = cal_prepare_skipping2D(ca);
     for (int b = 0; b < ca->num_of_elementary_processes; b++) {
         unsigned* run = (skip && ca->gpu->pure[b]) ? g.d_run + (size_t)b * g.tile_words : nullptr;
-        apply_launch(ca, ca->gpu->launch[b], run);
+        apply_launch(ca, ca->gpu->launch[b], run, b);
         calUpdate2D(ca);
     }
+}
+
+extern "C" int calSetElementaryProcessReads2D(struct CALModel2D* ca, CALCallbackFunc2D ep, const void* const* substates,
+                                              int count)
+{
+    if (!ca || !ca->gpu || count < 0 || count > CAL_MAX_STAGED || (count > 0 && !substates)) {
+        cal::set_error(CAL_ERROR_INVALID_ARGUMENT, "calSetElementaryProcessReads2D: bad arguments");
+        return CAL_ERROR_INVALID_ARGUMENT;
+    }
+    CalGrid& g = G(ca);
+    int b = -1;
+    for (int k = 0; k < ca->num_of_elementary_processes; k++)
+        if (ca->elementary_processes[k] == ep)
+            b = k;
+    if (b < 0) {
+        cal::set_error(CAL_ERROR_INVALID_ARGUMENT,
+                       "calSetElementaryProcessReads2D: not a process added with calAddElementaryProcess2D");
+        return CAL_ERROR_INVALID_ARGUMENT;
+    }
+    int ts[CAL_MAX_STAGED], ss[CAL_MAX_STAGED];
+    for (int k = 0; k < count; k++) {
+        /* a handle's type is the pool it lies in, its slot its 32-byte record */
+        ts[k] = -1;
+        for (int t = 0; t < CAL_NTYPES && ts[k] < 0; t++) {
+            const uintptr_t h = (uintptr_t)substates[k], p0 = (uintptr_t)g.pool[t];
+            if (h >= p0 && h < p0 + 32u * CAL_MAX_SUBSTATES_CORE && ((h - p0) & 31u) == 0 &&
+                (int)((h - p0) >> 5) < g.nslot[t] && g.sub[t][(h - p0) >> 5].used) {
+                ts[k] = t;
+                ss[k] = (int)((h - p0) >> 5);
+            }
+        }
+        if (ts[k] < 0 || g.sub[ts[k]][ss[k]].single) {
+            cal::set_error(CAL_ERROR_INVALID_ARGUMENT,
+                           "calSetElementaryProcessReads2D: not a (two-layer) substate of this model");
+            return CAL_ERROR_INVALID_ARGUMENT;
+        }
+        for (int j = 0; j < k; j++)
+            if (ts[j] == ts[k] && ss[j] == ss[k]) {
+                cal::set_error(CAL_ERROR_INVALID_ARGUMENT, "calSetElementaryProcessReads2D: substate listed twice");
+                return CAL_ERROR_INVALID_ARGUMENT;
+            }
+    }
+    if (count > 0 && !ca->gpu->d_stage_err &&
+        (!cal::cuda_ok(cudaMalloc(&ca->gpu->d_stage_err, sizeof(int)), "cudaMalloc staging flag") ||
+         !cal::cuda_ok(cudaMemset(ca->gpu->d_stage_err, 0, sizeof(int)), "memset staging flag")))
+        return CAL_ERROR_CUDA;
+    ca->gpu->nreads[b] = count;
+    for (int k = 0; k < count; k++) {
+        ca->gpu->read_t[b][k] = ts[k];
+        ca->gpu->read_s[b][k] = ss[k];
+    }
+    g.inval_epoch++; /* a recorded step holds the old launch */
+    return CAL_SUCCESS;
 }
 
 extern "C" int calSetElementaryProcessPure2D(struct CALModel2D* ca, CALCallbackFunc2D ep, CALbyte pure)
@@ -704,6 +818,8 @@ extern "C" void calFinalize2D(struct CALModel2D* ca)
         ca->gpu->g.destroy();
         if (ca->gpu->d_X)
             cudaFree(ca->gpu->d_X);
+        if (ca->gpu->d_stage_err)
+            cudaFree(ca->gpu->d_stage_err);
         delete ca->gpu;
     }
     free(ca->A.cells);

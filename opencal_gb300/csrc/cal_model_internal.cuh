@@ -14,6 +14,12 @@ struct CALGpuModel2D {
     int d_X_len = 0;                 /* entries uploaded; -1 forces an upload */
     CALLaunchFunc2D launch[CAL_MAX_ELEMENTARY_PROCESSES];
     bool pure[CAL_MAX_ELEMENTARY_PROCESSES] = {}; /* calSetElementaryProcessPure2D */
+    /* calSetElementaryProcessReads2D: the substates (type, slot) each
+     * process reads, staged into shared memory by TMA */
+    int nreads[CAL_MAX_ELEMENTARY_PROCESSES] = {};
+    int read_t[CAL_MAX_ELEMENTARY_PROCESSES][CAL_MAX_STAGED] = {};
+    int read_s[CAL_MAX_ELEMENTARY_PROCESSES][CAL_MAX_STAGED] = {};
+    int* d_stage_err = nullptr; /* a staged box that did not arrive in time */
 };
 
 struct CALGpuModel3D {

@@ -2030,18 +2030,36 @@ static void sciddicaT_simulation_init_fused(struct CALModel2D* sciddicaT)
  * cal_sciddicaT_set_pure(1) was called (off by default: the reference
  * program as it stands). */
 static int g_sdt_pure = 0;
+static int g_sdt_staged = 0;
 
+/* the declarations cal_sciddicaT_set_pure / _set_staged asked for; called
+ * once the processes and the substates exist */
 static void sciddicaT_declare_pure(struct CALModel2D* ca)
 {
-    if (!g_sdt_pure)
-        return;
-    calSetElementaryProcessPure2D(ca, sciddicaT_flows_computation, CAL_TRUE);
-    calSetElementaryProcessPure2D(ca, sciddicaT_width_update, CAL_TRUE);
+    if (g_sdt_pure) {
+        calSetElementaryProcessPure2D(ca, sciddicaT_flows_computation, CAL_TRUE);
+        calSetElementaryProcessPure2D(ca, sciddicaT_width_update, CAL_TRUE);
+    }
+    if (g_sdt_staged) {
+        const void* flows_reads[2] = {Q.z, Q.h};
+        const void* width_reads[5] = {Q.h, Q.f[0], Q.f[1], Q.f[2], Q.f[3]};
+        calSetElementaryProcessReads2D(ca, sciddicaT_flows_computation, flows_reads, 2);
+        calSetElementaryProcessReads2D(ca, sciddicaT_width_update, width_reads, 5);
+    }
 }
 
 extern "C" int cal_sciddicaT_set_pure(int on)
 {
     g_sdt_pure = on != 0;
+    return 0;
+}
+
+/* 1: models created afterwards (processes mode) declare what the two plain
+ * processes read (calSetElementaryProcessReads2D), so that the process
+ * kernels stage z, h and the outflows by TMA; 0 (default): global reads */
+extern "C" int cal_sciddicaT_set_staged(int on)
+{
+    g_sdt_staged = on != 0;
     return 0;
 }
 
@@ -2161,12 +2179,13 @@ extern "C" int cal_sciddicaT_run(int rows, int cols, int toroidal, int ac, int s
         calAddElementaryProcess2D(ca, sciddicaT_width_update);
         if (ac)
             calAddElementaryProcess2D(ca, sciddicaT_remove_inactive_cells);
-        sciddicaT_declare_pure(ca);
     }
     Q.z = calAddSubstate2Dr(ca);
     Q.h = calAddSubstate2Dr(ca);
     for (int q = 0; q < NUMBER_OF_OUTFLOWS; q++)
         Q.f[q] = calAddSubstate2Dr(ca);
+    if (mode == SDT_MODE_PROCESSES)
+        sciddicaT_declare_pure(ca);
     if (calGetLastError() != CAL_SUCCESS) {
         int e = calGetLastError();
         calRunFinalize2D(run);
@@ -2292,7 +2311,6 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
     if (mode == SDT_MODE_PROCESSES) {
         calAddElementaryProcess2D(s->ca, sciddicaT_flows_computation);
         calAddElementaryProcess2D(s->ca, sciddicaT_width_update);
-        sciddicaT_declare_pure(s->ca);
         if (ac)
             calAddElementaryProcess2D(s->ca, sciddicaT_remove_inactive_cells);
         calRunAddSteeringFunc2D(s->run, ac ? sciddicaT_steering_ac : sciddicaT_steering_plain);
@@ -2303,6 +2321,8 @@ extern "C" void* cal_sciddicaT_open(int rows, int cols, int toroidal, int ac, do
     Q.h = calAddSubstate2Dr(s->ca);
     for (int q = 0; q < NUMBER_OF_OUTFLOWS; q++)
         Q.f[q] = calAddSubstate2Dr(s->ca);
+    if (mode == SDT_MODE_PROCESSES)
+        sciddicaT_declare_pure(s->ca);
     memcpy(Q.z->current, z0, s->bytes);
     memcpy(Q.z->next, z0, s->bytes);
     memcpy(Q.h->current, h0, s->bytes);

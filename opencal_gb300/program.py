@@ -87,6 +87,7 @@ def capi() -> C.CDLL:
         "calFinalize2D": ([vp], None),
         "calAddElementaryProcess2D": ([vp, vp], vp),
         "calSetElementaryProcessPure2D": ([vp, vp, C.c_byte], i),
+        "calSetElementaryProcessReads2D": ([vp, vp, vp, i], i),
         "calApplyElementaryProcess2D": ([vp, vp], None),
         "calUpdate2D": ([vp], None),
         "calAddActiveCell2D": ([vp, i, i], None),
@@ -338,6 +339,15 @@ class Model2D:
         engine may skip tiles where it would change nothing."""
         if self._c.calSetElementaryProcessPure2D(self, process, 1 if pure else 0):
             _raise_on_error("calSetElementaryProcessPure2D")
+
+    def set_reads(self, process: int, substates) -> None:
+        """calSetElementaryProcessReads2D: the substates the process reads
+        (current layer, calGet / calGetX), staged into shared memory by TMA
+        tile by tile."""
+        subs = list(substates)
+        arr = (C.c_void_p * max(len(subs), 1))(*[h.ptr for h in subs])
+        if self._c.calSetElementaryProcessReads2D(self, process, arr, len(subs)):
+            _raise_on_error("calSetElementaryProcessReads2D")
 
     def apply(self, process: int) -> None:
         """calApplyElementaryProcess2D: one process over the grid now (then

@@ -1,4 +1,7 @@
-"""Tile skipping of processes declared pure (calSetElementaryProcessPure2D):
+"""Performance declarations of elementary processes, which must not change
+any result.
+
+Tile skipping of processes declared pure (calSetElementaryProcessPure2D):
 the process kernel skips the 32 x 8 tiles where the process changed nothing
 the last time and whose 3 x 3 tile neighbourhood has not changed since.  The
 results must be the dense run's bits: checked here against the oracle on
@@ -10,6 +13,13 @@ further than one tile (skipping refused, still exact).  Also the active-cell
 counterpart: the compaction after a process that changed no flag keeps the
 list (a session reset that rewrites the flags through their device pointer
 must still be seen).
+
+TMA staging of the substates a process declared it reads
+(calSetElementaryProcessReads2D): SCIDDICA-T (doubles, von Neumann, flat and
+toroidal: border tiles of toroidal grids read global memory), Life (bytes,
+Moore, boxes 64 cells wide), an integer rule on a hexagonal neighbourhood,
+each against the oracle or the same program without the declaration; rows
+that are not a multiple of 16 bytes keep global reads.
 """
 import hashlib
 import json
@@ -23,14 +33,17 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-@pytest.fixture
-def pure_sdt():
+@pytest.fixture(params=[(1, 0), (0, 1), (1, 1)], ids=["pure", "staged", "pure+staged"])
+def pure_sdt(request):
     import opencal_gb300 as cal
     cal.build()
     m = cal.models()
-    m.cal_sciddicaT_set_pure(1)
+    pure, staged = request.param
+    m.cal_sciddicaT_set_pure(pure)
+    m.cal_sciddicaT_set_staged(staged)
     yield cal
     m.cal_sciddicaT_set_pure(0)
+    m.cal_sciddicaT_set_staged(0)
 
 
 @pytest.mark.parametrize("rows,cols,seed,steps,tor", [(160, 144, 11, 60, 0), (203, 177, 13, 90, 1),
@@ -66,11 +79,13 @@ LIFE_BODY = """
 """
 
 
+@pytest.mark.parametrize("staged", [False, True])
 @pytest.mark.parametrize("shape,tor,graph", [((96, 80), True, False), ((130, 70), False, True),
-                                            ((72, 256), True, True)])
-def test_life_pure_from_python(shape, tor, graph):
+                                            ((72, 256), True, True), ((64, 96), False, False)])
+def test_life_pure_from_python(shape, tor, graph, staged):
     """Life on a sparse field (most tiles dead and skipped after their first
-    generation) declared pure from Python."""
+    generation) declared pure from Python, with and without its substate
+    staged (byte rows of 80, 256, 96 cells are staged, 70 are not)."""
     import oracle
     import opencal_gb300 as cal
     from opencal_gb300 import program as P
@@ -87,6 +102,8 @@ def test_life_pure_from_python(shape, tor, graph):
     rule = lib.process("pylife_pure_rule")
     model.add_process(rule)
     model.set_pure(rule)
+    if staged:
+        model.set_reads(rule, [alive])
     model.load(alive, s0.astype(np.int8))
     run = P.Run2D(model, 1, 60, graph=graph)
     try:
@@ -172,3 +189,39 @@ def test_active_cells_session_reset_and_rerun():
             assert out.tobytes() == ref[1].tobytes(), loop
     finally:
         m.cal_sciddicaT_close(sess)
+
+
+def test_staged_hexagonal_integer_rule_equals_global_reads():
+    """An integer rule over the hexagonal neighbourhood (both layouts), with
+    and without its substate staged: the same bits, flat and toroidal."""
+    from opencal_gb300 import program as P
+    import opencal_gb300 as cal
+    cal.build()
+    body = """
+        CALint s = 3 * calGet2Di(ca, Q.v, i, j);
+        for (int n = 1; n < ca->sizeof_X; n++) s += n * calGetX2Di(ca, Q.v, i, j, n);
+        calSet2Di(ca, Q.v, i, j, s % 1009);
+    """
+    lib = P.Program("pyhexint").substates(v="i").process("pyhexint_rule", body).build()
+    rng = np.random.default_rng(9)
+    v0 = rng.integers(0, 1009, size=(72, 96)).astype(np.int32)
+    for nb in (P.CAL_HEXAGONAL_NEIGHBORHOOD_2D, P.CAL_HEXAGONAL_NEIGHBORHOOD_ALT_2D):
+        for space in (P.CAL_SPACE_FLAT, P.CAL_SPACE_TOROIDAL):
+            out = []
+            for staged in (False, True):
+                model = P.Model2D(72, 96, nb, space)
+                v = model.add_substate("i")
+                lib.bind(v=v)
+                rule = lib.process("pyhexint_rule")
+                model.add_process(rule)
+                if staged:
+                    model.set_reads(rule, [v])
+                model.load(v, v0)
+                run = P.Run2D(model, 1, 12)
+                try:
+                    run.run()
+                    out.append(model.read(v))
+                finally:
+                    run.close()
+                    model.close()
+            assert out[0].tobytes() == out[1].tobytes(), (nb, space)
