@@ -112,7 +112,7 @@ static __shared__ unsigned char cal_untracked2D[3 * CAL_MAX_SUBSTATES];
 /* per block: a process changed an active-cell flag */
 static __shared__ unsigned char cal_flagchg2D;
 /* per block: the current tile is staged, its origin, the staging barrier */
-static __shared__ int cal_stage_on2D, cal_stage_i02D, cal_stage_j02D;
+static __shared__ int cal_stage_on2D, cal_stage_i02D, cal_stage_j02D, cal_stage_pad2D;
 static __shared__ __align__(8) unsigned long long cal_stage_bar2D;
 extern __shared__ __align__(128) unsigned char cal_stage_mem2D[];
 
@@ -228,7 +228,7 @@ static __device__ __forceinline__ const T* cal_staged2D(const struct CALDevModel
         return nullptr;
     constexpr int hx = 16 / (int)sizeof(T);
     constexpr int bw = CAL_TILE_W + 2 * hx;
-    const T* box = reinterpret_cast<const T*>(cal_stage_mem2D + m->stage_off[k]);
+    const T* box = reinterpret_cast<const T*>(cal_stage_mem2D + cal_stage_pad2D + m->stage_off[k]);
     return box + (a - cal_stage_i02D + m->stage_r) * bw + (b - cal_stage_j02D + hx);
 }
 
@@ -375,6 +375,9 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     if (threadIdx.x == 0) {
         cal_flagchg2D = 0;
         cal_stage_on2D = 0;
+        /* the boxes start on a 128-byte boundary of the shared window (the
+         * launch adds 128 bytes for this) */
+        cal_stage_pad2D = (int)((128u - (cal_smem_u32(cal_stage_mem2D) & 127u)) & 127u);
         if (m.nstage)
             cal_bar_init(&cal_stage_bar2D);
     }
@@ -405,9 +408,13 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                 if (stage && threadIdx.x == 0) {
                     cal_stage_i02D = ty * CAL_TILE_H;
                     cal_stage_j02D = tx * CAL_TILE_W;
+                    /* the previous tile's reads of the boxes (generic proxy,
+                     * ordered by the block barrier) before the copies
+                     * (async proxy) overwrite them */
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     cal_bar_expect(&cal_stage_bar2D, (uint32_t)m.stage_tx);
                     for (int k = 0; k < nstage; k++)
-                        cal_tma_load_2d(cal_stage_mem2D + m.stage_off[k], &m.stage_map[k],
+                        cal_tma_load_2d(cal_stage_mem2D + cal_stage_pad2D + m.stage_off[k], &m.stage_map[k],
                                         tx * CAL_TILE_W - m.stage_hx[k], ty * CAL_TILE_H - m.stage_r,
                                         &cal_stage_bar2D);
                 }
@@ -419,10 +426,15 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                 if (threadIdx.x == 0)
                     cal_stage_on2D = stage && arrived;
                 if (!__syncthreads_and(arrived)) {
-                    /* a box did not arrive: record it; this tile and the
-                     * rest read global memory */
-                    if (threadIdx.x == 0 && m.stage_err)
-                        atomicExch(m.stage_err, 1);
+                    /* a box did not arrive: record it, wait (bounded) for the
+                     * copies still in flight into this block's shared
+                     * memory, and read global memory from here on */
+                    if (threadIdx.x == 0) {
+                        if (m.stage_err)
+                            atomicExch(m.stage_err, 1);
+                        cal_bar_wait(&cal_stage_bar2D, phase ^ 1u, CAL_STAGE_WAIT_LIMIT);
+                    }
+                    __syncthreads();
                     nstage = 0;
                 }
             }
@@ -467,7 +479,7 @@ static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* 
 {
     const dim3 grid(gx, gy);
     cudaStream_t st = (cudaStream_t)stream;
-    const size_t smem = m->nstage ? (size_t)m->stage_bytes : 0;
+    const size_t smem = m->nstage ? (size_t)m->stage_bytes + 128 : 0; /* + alignment of the boxes */
     switch (m->model.sizeof_X) {
     case 5: cal_ep2D_kernel<EP, 5><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
     case 7: cal_ep2D_kernel<EP, 7><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
