@@ -228,8 +228,12 @@ static __device__ __forceinline__ const T* cal_staged2D(const struct CALDevModel
         return nullptr;
     constexpr int hx = 16 / (int)sizeof(T);
     constexpr int bw = CAL_TILE_W + 2 * hx;
+    const int y = a - cal_stage_i02D + m->stage_r, x = b - cal_stage_j02D + hx;
+    /* a cell outside the box (calGet at other coordinates) reads global memory */
+    if ((unsigned)y >= (unsigned)(CAL_TILE_H + 2 * m->stage_r) || (unsigned)x >= (unsigned)bw)
+        return nullptr;
     const T* box = reinterpret_cast<const T*>(cal_stage_mem2D + cal_stage_pad2D + m->stage_off[k]);
-    return box + (a - cal_stage_i02D + m->stage_r) * bw + (b - cal_stage_j02D + hx);
+    return box + y * bw + x;
 }
 
 template <typename T>
