@@ -90,7 +90,7 @@ struct CALDevModel2D {
      * accessors read the staged substates there.  stage_of[type][slot] = k
      * or -1; stage_tx: the bytes the boxes bring (the mbarrier's
      * transaction count); stage_bytes: the dynamic shared memory. */
-    int nstage, stage_r, stage_tx, stage_bytes;
+    int nstage, stage_r, stage_tx, stage_bytes, stage_hxmax;
     int stage_off[CAL_MAX_STAGED];
     int stage_hx[CAL_MAX_STAGED]; /* 16 / element size: 16, 4, 2 (x stays 16-byte aligned) */
     signed char stage_of[3][CAL_MAX_SUBSTATES];
@@ -407,8 +407,11 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
             const int ty = tile / m.tiles_x, tx = tile - ty * m.tiles_x;
             const int i = ty * CAL_TILE_H + warp, j = tx * CAL_TILE_W + lane;
             if (nstage) {
-                /* toroidal grids: only tiles whose boxes need no wrap */
-                const bool stage = !m.toroidal || (ty > 0 && tx > 0 && ty < m.tiles_y - 1 && tx < m.tiles_x - 1);
+                /* toroidal grids: only tiles whose boxes lie inside the grid
+                 * (no neighbour read needs a wrap) */
+                const int i0 = ty * CAL_TILE_H, j0 = tx * CAL_TILE_W;
+                const bool stage = !m.toroidal || (i0 - m.stage_r >= 0 && i0 + CAL_TILE_H + m.stage_r <= m.rows &&
+                                                   j0 - m.stage_hxmax >= 0 && j0 + CAL_TILE_W + m.stage_hxmax <= m.cols);
                 if (stage && threadIdx.x == 0) {
                     cal_stage_i02D = ty * CAL_TILE_H;
                     cal_stage_j02D = tx * CAL_TILE_W;

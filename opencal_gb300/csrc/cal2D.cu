@@ -473,6 +473,9 @@ static void stage_reads(struct CALModel2D* ca, int b, CALDevModel2D* d)
         return;
     d->nstage = n;
     d->stage_r = ri;
+    d->stage_hxmax = 0;
+    for (int k = 0; k < n; k++)
+        d->stage_hxmax = std::max(d->stage_hxmax, d->stage_hx[k]);
     d->stage_tx = tx;
     d->stage_bytes = off;
     d->stage_err = ca->gpu->d_stage_err;
