@@ -461,18 +461,23 @@ def processes_plain_section(m, cal, z, h, h_plain):
     (eager: a launch sequence per step; graph: the recorded step replayed) or
     calRunDeviceSteps2D (one device-driven graph launch for the loop).  The
     engine updates and fills only the tiles a process changed (change
-    tracking).  Twice: as the reference program stands, and with both
+    tracking).  Three times: as the reference program stands; with both
     processes declared pure (calSetElementaryProcessPure2D), which lets the
     process kernels skip the tiles whose neighbourhood did not change since
-    they last changed nothing there.  Every form must give the split step's
-    bits."""
+    they last changed nothing there; and with their reads declared too
+    (calSetElementaryProcessReads2D), which stages z, h and the outflows into
+    shared memory by TMA tile by tile.  Every form must give the split
+    step's bits."""
     import torch
     m.cal_sciddicaT_set_pure.argtypes = [C.c_int]
+    m.cal_sciddicaT_set_staged.argtypes = [C.c_int]
     out = {}
-    for label, pure in (("as_written", 0), ("declared_pure", 1)):
+    for label, pure, staged in (("as_written", 0, 0), ("declared_pure", 1, 0), ("declared_pure_and_reads", 1, 1)):
         m.cal_sciddicaT_set_pure(pure)
+        m.cal_sciddicaT_set_staged(staged)
         sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_PROCESSES)
         m.cal_sciddicaT_set_pure(0)
+        m.cal_sciddicaT_set_staged(0)
         if not sess:
             return {"error": "cal_sciddicaT_open (processes) failed: " + cal.core().calGetErrorString().decode()}
         stream = torch.cuda.ExternalStream(m.cal_sciddicaT_stream(sess))
