@@ -112,8 +112,8 @@ static __shared__ unsigned char cal_untracked2D[3 * CAL_MAX_SUBSTATES];
 /* per block: a process changed an active-cell flag */
 static __shared__ unsigned char cal_flagchg2D;
 /* per block: the current tile is staged, its origin, the staging barrier */
-static __shared__ int cal_stage_on2D, cal_stage_i02D, cal_stage_j02D, cal_stage_pad2D;
-static __shared__ __align__(8) unsigned long long cal_stage_bar2D;
+static __shared__ int cal_stage_on2D, cal_stage_i02D, cal_stage_j02D, cal_stage_pad2D, cal_stage_buf2D;
+static __shared__ __align__(8) unsigned long long cal_stage_bar2D[2];
 extern __shared__ __align__(128) unsigned char cal_stage_mem2D[];
 
 /* ---- TMA: mbarrier with a transaction count, tiled 2D loads, bounded wait */
@@ -232,7 +232,7 @@ static __device__ __forceinline__ const T* cal_staged2D(const struct CALDevModel
     /* a cell outside the box (calGet at other coordinates) reads global memory */
     if ((unsigned)y >= (unsigned)(CAL_TILE_H + 2 * m->stage_r) || (unsigned)x >= (unsigned)bw)
         return nullptr;
-    const T* box = reinterpret_cast<const T*>(cal_stage_mem2D + cal_stage_pad2D + m->stage_off[k]);
+    const T* box = reinterpret_cast<const T*>(cal_stage_mem2D + cal_stage_pad2D + cal_stage_buf2D + m->stage_off[k]);
     return box + y * bw + x;
 }
 
@@ -382,13 +382,15 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         /* the boxes start on a 128-byte boundary of the shared window (the
          * launch adds 128 bytes for this) */
         cal_stage_pad2D = (int)((128u - (cal_smem_u32(cal_stage_mem2D) & 127u)) & 127u);
-        if (m.nstage)
-            cal_bar_init(&cal_stage_bar2D);
+        cal_stage_buf2D = 0;
+        if (m.nstage) {
+            cal_bar_init(&cal_stage_bar2D[0]);
+            cal_bar_init(&cal_stage_bar2D[1]);
+        }
     }
     __syncthreads();
     struct CALModel2D view = cal_model_view2D<NX>(m);
     int nstage = m.nstage;  /* 0 after a box failed to arrive: global reads for the rest */
-    uint32_t phase = 0;
     struct CALModel2D* ca = &view;
     const int listed = m.use_list ? *m.count : 0;
     const int nblocks = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
@@ -400,46 +402,80 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         }
     } else {
         const int ntiles = m.tiles_x * m.tiles_y;
-        for (int tile = bid; tile < ntiles; tile += nblocks) {
+        /* the block's tiles: bid, bid + nblocks, ...; with tile skipping only
+         * those whose bit is set (a bit is cleared only by the block that
+         * owns the tile, after processing it, so every thread finds the same
+         * next tile).  With staging, the next tile's boxes are loaded into the
+         * other of two buffers while the current tile computes. */
+        auto next_tile = [&](int from) {
+            int t = from;
+            while (t < ntiles && m.run && !(m.run[t >> 5] & (1u << (t & 31))))
+                t += nblocks;
+            return t;
+        };
+        auto staged_tile = [&](int t) {
+            /* toroidal grids: only tiles whose boxes lie inside the grid (no
+             * neighbour read needs a wrap); flat grids: every tile */
+            const int ty = t / m.tiles_x;
+            const int i0 = ty * CAL_TILE_H, j0 = (t - ty * m.tiles_x) * CAL_TILE_W;
+            return !m.toroidal || (i0 - m.stage_r >= 0 && i0 + CAL_TILE_H + m.stage_r <= m.rows &&
+                                   j0 - m.stage_hxmax >= 0 && j0 + CAL_TILE_W + m.stage_hxmax <= m.cols);
+        };
+        /* thread 0: the boxes of tile t into buffer b */
+        auto issue = [&](int t, int b) {
+            const int ty = t / m.tiles_x, tx = t - ty * m.tiles_x;
+            /* earlier reads of the buffer (generic proxy, ordered by the
+             * block barrier) before the copies (async proxy) overwrite it */
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            cal_bar_expect(&cal_stage_bar2D[b], (uint32_t)m.stage_tx);
+            for (int k = 0; k < nstage; k++)
+                cal_tma_load_2d(cal_stage_mem2D + cal_stage_pad2D + b * m.stage_bytes + m.stage_off[k],
+                                &m.stage_map[k], tx * CAL_TILE_W - m.stage_hx[k], ty * CAL_TILE_H - m.stage_r,
+                                &cal_stage_bar2D[b]);
+        };
+        uint32_t phases = 0; /* bit b: parity of buffer b's next phase */
+        bool pending[2] = {false, false};
+        int buf = 0;
+        int tile = next_tile(bid);
+        if (nstage && tile < ntiles && staged_tile(tile)) {
+            if (threadIdx.x == 0)
+                issue(tile, 0);
+            pending[0] = true;
+        }
+        while (tile < ntiles) {
             const unsigned tbit = 1u << (tile & 31);
-            if (m.run && !(m.run[tile >> 5] & tbit))
-                continue; /* unchanged neighbourhood, no-op last time (block-uniform) */
+            const int nxt = next_tile(tile + nblocks);
             const int ty = tile / m.tiles_x, tx = tile - ty * m.tiles_x;
             const int i = ty * CAL_TILE_H + warp, j = tx * CAL_TILE_W + lane;
             if (nstage) {
-                /* toroidal grids: only tiles whose boxes lie inside the grid
-                 * (no neighbour read needs a wrap) */
-                const int i0 = ty * CAL_TILE_H, j0 = tx * CAL_TILE_W;
-                const bool stage = !m.toroidal || (i0 - m.stage_r >= 0 && i0 + CAL_TILE_H + m.stage_r <= m.rows &&
-                                                   j0 - m.stage_hxmax >= 0 && j0 + CAL_TILE_W + m.stage_hxmax <= m.cols);
-                if (stage && threadIdx.x == 0) {
-                    cal_stage_i02D = ty * CAL_TILE_H;
-                    cal_stage_j02D = tx * CAL_TILE_W;
-                    /* the previous tile's reads of the boxes (generic proxy,
-                     * ordered by the block barrier) before the copies
-                     * (async proxy) overwrite them */
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    cal_bar_expect(&cal_stage_bar2D, (uint32_t)m.stage_tx);
-                    for (int k = 0; k < nstage; k++)
-                        cal_tma_load_2d(cal_stage_mem2D + cal_stage_pad2D + m.stage_off[k], &m.stage_map[k],
-                                        tx * CAL_TILE_W - m.stage_hx[k], ty * CAL_TILE_H - m.stage_r,
-                                        &cal_stage_bar2D);
+                if (nxt < ntiles && staged_tile(nxt)) { /* prefetch */
+                    if (threadIdx.x == 0)
+                        issue(nxt, buf ^ 1);
+                    pending[buf ^ 1] = true;
                 }
                 bool arrived = true;
-                if (stage) {
-                    arrived = cal_bar_wait(&cal_stage_bar2D, phase, CAL_STAGE_WAIT_LIMIT);
-                    phase ^= 1u;
+                if (pending[buf]) {
+                    arrived = cal_bar_wait(&cal_stage_bar2D[buf], (phases >> buf) & 1u, CAL_STAGE_WAIT_LIMIT);
+                    phases ^= 1u << buf;
+                    pending[buf] = false;
                 }
-                if (threadIdx.x == 0)
-                    cal_stage_on2D = stage && arrived;
+                if (threadIdx.x == 0) {
+                    cal_stage_on2D = staged_tile(tile) && arrived;
+                    cal_stage_i02D = ty * CAL_TILE_H;
+                    cal_stage_j02D = tx * CAL_TILE_W;
+                    cal_stage_buf2D = buf * m.stage_bytes;
+                }
                 if (!__syncthreads_and(arrived)) {
                     /* a box did not arrive: record it, wait (bounded) for the
-                     * copies still in flight into this block's shared
-                     * memory, and read global memory from here on */
+                     * copies still in flight into this block's shared memory,
+                     * and read global memory from here on */
                     if (threadIdx.x == 0) {
                         if (m.stage_err)
                             atomicExch(m.stage_err, 1);
-                        cal_bar_wait(&cal_stage_bar2D, phase ^ 1u, CAL_STAGE_WAIT_LIMIT);
+                        cal_bar_wait(&cal_stage_bar2D[buf], ((phases >> buf) & 1u) ^ 1u, CAL_STAGE_WAIT_LIMIT);
+                        if (pending[buf ^ 1])
+                            cal_bar_wait(&cal_stage_bar2D[buf ^ 1], (phases >> (buf ^ 1)) & 1u, CAL_STAGE_WAIT_LIMIT);
+                        cal_stage_on2D = 0;
                     }
                     __syncthreads();
                     nstage = 0;
@@ -448,7 +484,7 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
             if (i < m.rows && j < m.cols)
                 EP(ca, i, j);
             if (nstage)
-                __syncthreads(); /* every staged read done before the next tile's boxes land */
+                __syncthreads(); /* every read of this buffer done before it is refilled */
             if (m.track) {
                 bool changed = false;
                 __syncwarp();
@@ -462,6 +498,8 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                 if (m.run && !__syncthreads_or(changed) && threadIdx.x == 0)
                     atomicAnd(&m.run[tile >> 5], ~tbit);
             }
+            tile = nxt;
+            buf ^= 1;
         }
     }
     __syncthreads();
@@ -486,7 +524,8 @@ static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* 
 {
     const dim3 grid(gx, gy);
     cudaStream_t st = (cudaStream_t)stream;
-    const size_t smem = m->nstage ? (size_t)m->stage_bytes + 128 : 0; /* + alignment of the boxes */
+    /* two buffers of boxes, + alignment */
+    const size_t smem = m->nstage ? 2 * (size_t)m->stage_bytes + 128 : 0;
     switch (m->model.sizeof_X) {
     case 5: cal_ep2D_kernel<EP, 5><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
     case 7: cal_ep2D_kernel<EP, 7><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;

@@ -469,7 +469,7 @@ static void stage_reads(struct CALModel2D* ca, int b, CALDevModel2D* d)
         off += (bw * bh * es + 127) & ~127;
         tx += bw * bh * es;
     }
-    if (off + 128 > 48 * 1024 || !ca->gpu->d_stage_err)
+    if (2 * off + 128 > 48 * 1024 || !ca->gpu->d_stage_err) /* two buffers in 48 KB */
         return;
     d->nstage = n;
     d->stage_r = ri;
