@@ -433,14 +433,14 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                                 &m.stage_map[k], tx * CAL_TILE_W - m.stage_hx[k], ty * CAL_TILE_H - m.stage_r,
                                 &cal_stage_bar2D[b]);
         };
-        uint32_t phases = 0; /* bit b: parity of buffer b's next phase */
-        bool pending[2] = {false, false};
+        uint32_t phases = 0;  /* bit b: parity of buffer b's next phase */
+        uint32_t pending = 0; /* bit b: copies issued into buffer b and not yet waited for */
         int buf = 0;
         int tile = next_tile(bid);
         if (nstage && tile < ntiles && staged_tile(tile)) {
             if (threadIdx.x == 0)
                 issue(tile, 0);
-            pending[0] = true;
+            pending = 1u;
         }
         while (tile < ntiles) {
             const unsigned tbit = 1u << (tile & 31);
@@ -451,13 +451,13 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                 if (nxt < ntiles && staged_tile(nxt)) { /* prefetch */
                     if (threadIdx.x == 0)
                         issue(nxt, buf ^ 1);
-                    pending[buf ^ 1] = true;
+                    pending |= 1u << (buf ^ 1);
                 }
                 bool arrived = true;
-                if (pending[buf]) {
+                if ((pending >> buf) & 1u) {
                     arrived = cal_bar_wait(&cal_stage_bar2D[buf], (phases >> buf) & 1u, CAL_STAGE_WAIT_LIMIT);
                     phases ^= 1u << buf;
-                    pending[buf] = false;
+                    pending &= ~(1u << buf);
                 }
                 if (threadIdx.x == 0) {
                     cal_stage_on2D = staged_tile(tile) && arrived;
@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                         if (m.stage_err)
                             atomicExch(m.stage_err, 1);
                         cal_bar_wait(&cal_stage_bar2D[buf], ((phases >> buf) & 1u) ^ 1u, CAL_STAGE_WAIT_LIMIT);
-                        if (pending[buf ^ 1])
+                        if ((pending >> (buf ^ 1)) & 1u)
                             cal_bar_wait(&cal_stage_bar2D[buf ^ 1], (phases >> (buf ^ 1)) & 1u, CAL_STAGE_WAIT_LIMIT);
                         cal_stage_on2D = 0;
                     }
