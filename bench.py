@@ -965,11 +965,17 @@ def life_arm(args):
     from opencal_gb300 import workloads as W
     cal.build()
     s0 = W.life_state(LIFE_SIZE, LIFE_SIZE, p=0.3, seed=1)
-    forms = [("processes", cal.MODE_PROCESSES, 1), ("fused", cal.MODE_FUSED, 1)] + \
+    forms = [("processes", cal.MODE_PROCESSES, 1), ("processes_reads_declared", cal.MODE_PROCESSES, 1),
+             ("processes_pure", cal.MODE_PROCESSES, 1), ("processes_pure_reads_declared", cal.MODE_PROCESSES, 1),
+             ("fused", cal.MODE_FUSED, 1)] + \
             [(f"blocked{k}", cal.MODE_FUSED_BLOCKED, k) for k in (4, 8)] + \
             [(f"bits{k}", cal.MODE_BITS, k) for k in (8, 16, 32)]
+    decl = {"processes_reads_declared": 2, "processes_pure": 1, "processes_pure_reads_declared": 3}
+    m = cal.models()
+    m.cal_life2d_set_declarations.argtypes = [C.c_int]
     results, outs = {}, {}
     for name, mode, k in forms:
+        m.cal_life2d_set_declarations(decl.get(name, 0))
         for _ in range(args.warmup):
             cal.life2d(s0, LIFE_STEPS, mode=mode, block=k)
         ms = []
@@ -978,6 +984,7 @@ def life_arm(args):
             ms.append(t)
         results[name] = float(np.median(ms))
         outs[name] = out
+    m.cal_life2d_set_declarations(0)
     same = all(o.tobytes() == outs["processes"].tobytes() for o in outs.values())
     best = min(results, key=results.get)
     cells = LIFE_SIZE * LIFE_SIZE * LIFE_STEPS

@@ -177,6 +177,10 @@ int cal_mbusu_run(int steps, int mode, double* state, double* tail, double* ms);
 /* ---- Game of Life (OpenCAL-OMP/examples/calomp_life) and the 3D rule ---- */
 int cal_life2d_run(int rows, int cols, int toroidal, int as_int, int steps, const unsigned char* s0,
                    unsigned char* s_out, int mode, int block, int graph, double* ms);
+/* declarations for the reference program's process in runs started
+ * afterwards: bit 0 pure, bit 1 reads its state substate (staged by TMA);
+ * 0: the program as it stands */
+int cal_life2d_set_declarations(int flags);
 int cal_life3d_run(int rows, int cols, int slices, int nbhd, int toroidal, int steps, int r1, int r2, int r3, int r4,
                    const unsigned char* s0, unsigned char* s_out, int graph);
 

@@ -353,6 +353,19 @@ static void life_fused_transition(struct CALModel2D* ca)
     life_fused_generations(ca, 1);
 }
 
+/* Declarations for the reference program's process (mode 0), for runs
+ * started afterwards: bit 0 declares it pure (calSetElementaryProcessPure2D:
+ * tiles whose neighbourhood did not change are skipped), bit 1 declares
+ * that it reads the state substate (calSetElementaryProcessReads2D: staged
+ * by TMA tile by tile).  0 (default): the program as it stands. */
+static int g_life_decl = 0;
+
+extern "C" int cal_life2d_set_declarations(int flags)
+{
+    g_life_decl = flags & 3;
+    return 0;
+}
+
 /* Runs Life for `steps` generations; state in/out as 0/1 bytes.
  * mode 0: the reference program (device process, byte or int substate);
  * mode 1: fused launches of one generation each (byte substate);
@@ -375,13 +388,26 @@ extern "C" int cal_life2d_run(int rows, int cols, int toroidal, int as_int, int 
     if (as_int) {
         lifeQi = calAddSubstate2Di(ca);
         calAddElementaryProcess2D(ca, lifeTransitionFunctionI);
+        if (g_life_decl & 1)
+            calSetElementaryProcessPure2D(ca, lifeTransitionFunctionI, CAL_TRUE);
+        if (g_life_decl & 2) {
+            const void* reads[1] = {lifeQi};
+            calSetElementaryProcessReads2D(ca, lifeTransitionFunctionI, reads, 1);
+        }
         for (long long c = 0; c < n; c++)
             lifeQi->current[c] = lifeQi->next[c] = s0[c];
     } else {
         lifeQb = calAddSubstate2Db(ca);
-        if (mode == 0)
+        if (mode == 0) {
             calAddElementaryProcess2D(ca, lifeTransitionFunctionB);
-        else if (mode == 1)
+            if (g_life_decl & 1)
+                calSetElementaryProcessPure2D(ca, lifeTransitionFunctionB, CAL_TRUE);
+            if (g_life_decl & 2) {
+                const void* reads[1] = {lifeQb};
+                calSetElementaryProcessReads2D(ca, lifeTransitionFunctionB, reads, 1);
+            }
+        }
+        if (mode == 1)
             calRunAddGlobalTransitionFunc2D(run, life_fused_transition);
         for (long long c = 0; c < n; c++)
             lifeQb->current[c] = lifeQb->next[c] = (CALbyte)s0[c];

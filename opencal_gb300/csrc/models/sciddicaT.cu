@@ -657,7 +657,13 @@ static __device__ __forceinline__ void k2_work(const K2Params& p, int par, int e
                     carry = ldm<CO>(p.tflag + tile_of(i, j, p.tiles_x)) != epoch;
                 }
             }
-            warp_append(carry, c, list, count);
+            /* one atomic on the step's counter per block, not per warp:
+             * every block of the phase appends to that one word */
+            const bool want[4] = {carry, false, false, false};
+            const bool none[4] = {false, false, false, false};
+            const int value[4] = {c, 0, 0, 0};
+            block_append4(want, none, value, list, count);
+            __syncthreads(); /* block_append4's shared words are reused */
         }
     }
 }

@@ -225,3 +225,23 @@ def test_staged_hexagonal_integer_rule_equals_global_reads():
                     run.close()
                     model.close()
             assert out[0].tobytes() == out[1].tobytes(), (nb, space)
+
+
+@pytest.mark.parametrize("flags", [1, 2, 3])
+@pytest.mark.parametrize("shape,tor", [((96, 80), True), ((128, 256), False), ((100, 72), True)])
+def test_life_program_declarations(flags, shape, tor):
+    """The reference Life program (calModels.h) with its process declared
+    pure (1), its reads declared (2) or both (3): the oracle's bits."""
+    import oracle
+    import opencal_gb300 as cal
+    from opencal_gb300 import workloads as W
+    cal.build()
+    oracle.build()
+    m = cal.models()
+    s0 = W.life_state(shape[0], shape[1], p=0.3, seed=5)
+    m.cal_life2d_set_declarations(flags)
+    try:
+        got = cal.life2d(s0, 40, toroidal=tor, mode=cal.MODE_PROCESSES)
+    finally:
+        m.cal_life2d_set_declarations(0)
+    assert np.array_equal(got, oracle.life2d(s0, 40, toroidal=tor))
