@@ -172,7 +172,11 @@ __device__ __forceinline__ bool cal_same_bits<double>(double a, double b)
  * launch descriptor, where the accessors find the buffers. */
 static __device__ __forceinline__ const struct CALDevModel2D* cal_dm2D(const struct CALModel2D* ca)
 {
+#ifdef CAL_EXPERIMENT_NO_VIEW
+    return reinterpret_cast<const struct CALDevModel2D*>(ca);
+#else
     return reinterpret_cast<const struct CALDevModel2D*>(ca->gpu);
+#endif
 }
 
 /* The kernel-local model handed to user code.  NX > 0: the launch is for a
@@ -221,6 +225,9 @@ static __device__ __forceinline__ bool cal_nbr2D(const struct CALDevModel2D* m, 
 template <typename T>
 static __device__ __forceinline__ const T* cal_staged2D(const struct CALDevModel2D* m, int t, int s, int a, int b)
 {
+#ifdef CAL_EXPERIMENT_NO_STAGE
+    return nullptr;
+#endif
     if (!m->nstage || !cal_stage_on2D)
         return nullptr;
     const int k = m->stage_of[t][s];
@@ -251,6 +258,7 @@ static __device__ __forceinline__ T cal_getx2D(const struct CALModel2D* ca, int 
 {
     const struct CALDevModel2D* m = cal_dm2D(ca);
     const int s = cal_slot2D(m, t, q);
+#ifndef CAL_EXPERIMENT_NO_STAGE
     if (m->nstage && cal_stage_on2D) {
         /* a staged tile lies inside a toroidal grid or the box's zero fill
          * is the flat boundary: the neighbour is read without wrapping */
@@ -258,6 +266,7 @@ static __device__ __forceinline__ T cal_getx2D(const struct CALModel2D* ca, int 
         if (const T* p = cal_staged2D<T>(m, t, s, i + m->xi[nn], j + m->xj[nn]))
             return *p;
     }
+#endif
     int a, b;
     if (!cal_nbr2D(m, i, j, n, a, b))
         return (T)0;
@@ -389,9 +398,13 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         }
     }
     __syncthreads();
+#ifdef CAL_EXPERIMENT_NO_VIEW
+    struct CALModel2D* ca = const_cast<struct CALModel2D*>(&m.model);
+#else
     struct CALModel2D view = cal_model_view2D<NX>(m);
-    int nstage = m.nstage;  /* 0 after a box failed to arrive: global reads for the rest */
     struct CALModel2D* ca = &view;
+#endif
+    int nstage = m.nstage;  /* 0 after a box failed to arrive: global reads for the rest */
     const int listed = m.use_list ? *m.count : 0;
     const int nblocks = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
     if (listed > 0) {
@@ -402,6 +415,33 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         }
     } else {
         const int ntiles = m.tiles_x * m.tiles_y;
+#ifdef CAL_EXPERIMENT_OLD_LOOP
+        for (int tile = bid; tile < ntiles; tile += nblocks) {
+            const unsigned tbit = 1u << (tile & 31);
+            if (m.run && !(m.run[tile >> 5] & tbit))
+                continue;
+            const int ty = tile / m.tiles_x;
+            const int i = ty * CAL_TILE_H + warp, j = (tile - ty * m.tiles_x) * CAL_TILE_W + lane;
+            if (i < m.rows && j < m.cols)
+                EP(ca, i, j);
+            if (m.track) {
+                bool changed = false;
+                __syncwarp();
+                for (int t = lane; t < 3 * CAL_MAX_SUBSTATES; t += 32)
+                    if (cal_chg2D[warp][t]) {
+                        cal_chg2D[warp][t] = 0;
+                        changed = true;
+                        atomicOr(&m.chg[(long long)t * m.tile_words + (tile >> 5)], tbit);
+                    }
+                __syncwarp();
+                if (m.run && !__syncthreads_or(changed) && threadIdx.x == 0)
+                    atomicAnd(&m.run[tile >> 5], ~tbit);
+            }
+        }
+        if (false) {
+#else
+        {
+#endif
         /* the block's tiles: bid, bid + nblocks, ...; with tile skipping only
          * those whose bit is set (a bit is cleared only by the block that
          * owns the tile, after processing it, so every thread finds the same
@@ -500,6 +540,7 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
             }
             tile = nxt;
             buf ^= 1;
+        }
         }
     }
     __syncthreads();

@@ -219,13 +219,13 @@ class Program:
             out.append(f"CAL_DEVICE_STOP_CONDITION_2D({n})(struct CALModel2D* ca)\n{{\n{body}\n}}")
         return "\n".join(out) + "\n"
 
-    def build(self, *, exact: bool = True, verbose: bool = False) -> "ProgramLib":
+    def build(self, *, exact: bool = True, verbose: bool = False, extra_flags=()) -> "ProgramLib":
         """Compile (or reuse the cached build of) the program for sm_103a and
         load it.  exact: no FMA contraction (--fmad=false), so that FP64
         arithmetic follows the source operation by operation, as the
         reference's C compiler evaluates it."""
         src = self.source()
-        flags = nvbuild.COMMON + (nvbuild.MODEL_FLAGS if exact else [])
+        flags = nvbuild.COMMON + (nvbuild.MODEL_FLAGS if exact else []) + list(extra_flags)
         key = hashlib.sha256((src + "\0" + " ".join(flags)).encode()).hexdigest()[:16]
         os.makedirs(PROGRAM_DIR, exist_ok=True)
         base = os.path.join(PROGRAM_DIR, f"{self.name}_{key}")
