@@ -172,11 +172,7 @@ __device__ __forceinline__ bool cal_same_bits<double>(double a, double b)
  * launch descriptor, where the accessors find the buffers. */
 static __device__ __forceinline__ const struct CALDevModel2D* cal_dm2D(const struct CALModel2D* ca)
 {
-#ifdef CAL_EXPERIMENT_NO_VIEW
-    return reinterpret_cast<const struct CALDevModel2D*>(ca);
-#else
     return reinterpret_cast<const struct CALDevModel2D*>(ca->gpu);
-#endif
 }
 
 /* The kernel-local model handed to user code.  NX > 0: the launch is for a
@@ -225,9 +221,6 @@ static __device__ __forceinline__ bool cal_nbr2D(const struct CALDevModel2D* m, 
 template <typename T>
 static __device__ __forceinline__ const T* cal_staged2D(const struct CALDevModel2D* m, int t, int s, int a, int b)
 {
-#ifdef CAL_EXPERIMENT_NO_STAGE
-    return nullptr;
-#endif
     if (!m->nstage || !cal_stage_on2D)
         return nullptr;
     const int k = m->stage_of[t][s];
@@ -258,7 +251,6 @@ static __device__ __forceinline__ T cal_getx2D(const struct CALModel2D* ca, int 
 {
     const struct CALDevModel2D* m = cal_dm2D(ca);
     const int s = cal_slot2D(m, t, q);
-#ifndef CAL_EXPERIMENT_NO_STAGE
     if (m->nstage && cal_stage_on2D) {
         /* a staged tile lies inside a toroidal grid or the box's zero fill
          * is the flat boundary: the neighbour is read without wrapping */
@@ -266,7 +258,6 @@ static __device__ __forceinline__ T cal_getx2D(const struct CALModel2D* ca, int 
         if (const T* p = cal_staged2D<T>(m, t, s, i + m->xi[nn], j + m->xj[nn]))
             return *p;
     }
-#endif
     int a, b;
     if (!cal_nbr2D(m, i, j, n, a, b))
         return (T)0;
@@ -375,7 +366,7 @@ static __device__ __forceinline__ int calGetActiveCellCountDevice2D(const struct
  * each warp then adds its tile to the chg bitmap of every substate whose
  * next layer it changed.  At the end each block publishes which substates
  * it wrote (and which it wrote by unsafe operations). */
-template <void (*EP)(struct CALModel2D*, int, int), int NX>
+template <void (*EP)(struct CALModel2D*, int, int), int NX, bool STAGED>
 __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_constant__ struct CALDevModel2D m)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -392,19 +383,15 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
          * launch adds 128 bytes for this) */
         cal_stage_pad2D = (int)((128u - (cal_smem_u32(cal_stage_mem2D) & 127u)) & 127u);
         cal_stage_buf2D = 0;
-        if (m.nstage) {
+        if (STAGED && m.nstage) {
             cal_bar_init(&cal_stage_bar2D[0]);
             cal_bar_init(&cal_stage_bar2D[1]);
         }
     }
     __syncthreads();
-#ifdef CAL_EXPERIMENT_NO_VIEW
-    struct CALModel2D* ca = const_cast<struct CALModel2D*>(&m.model);
-#else
     struct CALModel2D view = cal_model_view2D<NX>(m);
     struct CALModel2D* ca = &view;
-#endif
-    int nstage = m.nstage;  /* 0 after a box failed to arrive: global reads for the rest */
+    int nstage = STAGED ? m.nstage : 0; /* 0 after a box failed to arrive: global reads for the rest */
     const int listed = m.use_list ? *m.count : 0;
     const int nblocks = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
     if (listed > 0) {
@@ -415,7 +402,8 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         }
     } else {
         const int ntiles = m.tiles_x * m.tiles_y;
-#ifdef CAL_EXPERIMENT_OLD_LOOP
+        if (!STAGED) {
+        /* tile by tile; with tile skipping only the tiles whose bit is set */
         for (int tile = bid; tile < ntiles; tile += nblocks) {
             const unsigned tbit = 1u << (tile & 31);
             if (m.run && !(m.run[tile >> 5] & tbit))
@@ -438,11 +426,8 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                     atomicAnd(&m.run[tile >> 5], ~tbit);
             }
         }
-        if (false) {
-#else
-        {
-#endif
-        /* the block's tiles: bid, bid + nblocks, ...; with tile skipping only
+        } else {
+        /* staged: the block's tiles bid, bid + nblocks, ...; with tile skipping only
          * those whose bit is set (a bit is cleared only by the block that
          * owns the tile, after processing it, so every thread finds the same
          * next tile).  With staging, the next tile's boxes are loaded into the
@@ -559,7 +544,9 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
 }
 
 /* one kernel per common neighbourhood size (von Neumann 5, hexagonal 7,
- * Moore 9) and a generic one for the others */
+ * Moore 9) and a generic one for the others, each with and without the
+ * staging of declared reads (the staging loop costs registers and barriers
+ * that the plain loop does not pay) */
 template <void (*EP)(struct CALModel2D*, int, int)>
 static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* stream)
 {
@@ -567,11 +554,20 @@ static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* 
     cudaStream_t st = (cudaStream_t)stream;
     /* two buffers of boxes, + alignment */
     const size_t smem = m->nstage ? 2 * (size_t)m->stage_bytes + 128 : 0;
-    switch (m->model.sizeof_X) {
-    case 5: cal_ep2D_kernel<EP, 5><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
-    case 7: cal_ep2D_kernel<EP, 7><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
-    case 9: cal_ep2D_kernel<EP, 9><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
-    default: cal_ep2D_kernel<EP, 0><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+    if (m->nstage) {
+        switch (m->model.sizeof_X) {
+        case 5: cal_ep2D_kernel<EP, 5, true><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        case 7: cal_ep2D_kernel<EP, 7, true><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        case 9: cal_ep2D_kernel<EP, 9, true><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        default: cal_ep2D_kernel<EP, 0, true><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        }
+    } else {
+        switch (m->model.sizeof_X) {
+        case 5: cal_ep2D_kernel<EP, 5, false><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 7: cal_ep2D_kernel<EP, 7, false><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 9: cal_ep2D_kernel<EP, 9, false><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        default: cal_ep2D_kernel<EP, 0, false><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        }
     }
     return (int)cudaGetLastError();
 }
