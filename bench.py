@@ -1031,6 +1031,42 @@ def ncu_case_ensemble(args):
                       "loss_median": float(np.median(loss))}), flush=True)
 
 
+def ncu_case_processes(args):
+    """A fixed, untimed sequence for ncu captures of the generic engine: the
+    2048^2 session in processes mode (the reference program's device
+    processes; processes_ac: with active cells on), --ncu-warm steps, then
+    --ncu-steps steps, launch by launch (--loop eager) or device-driven
+    (--loop device); --declare: 1 pure, 2 reads staged, 3 both."""
+    import opencal_gb300 as cal
+    from opencal_gb300 import workloads as W
+    cal.build()
+    m = cal.models()
+    m.cal_sciddicaT_open.restype = C.c_void_p
+    m.cal_sciddicaT_open.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                     C.c_void_p, C.c_void_p, C.c_int]
+    m.cal_sciddicaT_steps.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    m.cal_sciddicaT_close.argtypes = [C.c_void_p]
+    m.cal_sciddicaT_set_pure.argtypes = [C.c_int]
+    m.cal_sciddicaT_set_staged.argtypes = [C.c_int]
+    ac = 1 if args.ncu_case == "processes_ac" else 0
+    z, h = W.sciddicaT_inputs(ROWS, COLS, seed=SEED)
+    m.cal_sciddicaT_set_pure(args.declare & 1)
+    m.cal_sciddicaT_set_staged((args.declare >> 1) & 1)
+    sess = m.cal_sciddicaT_open(ROWS, COLS, 0, ac, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_PROCESSES)
+    m.cal_sciddicaT_set_pure(0)
+    m.cal_sciddicaT_set_staged(0)
+    loop = {"eager": 0, "graph": 1, "device": 2}.get(args.loop, 0)
+    t0 = time.perf_counter()
+    rc = m.cal_sciddicaT_steps(sess, args.ncu_warm, loop)
+    rc |= m.cal_sciddicaT_steps(sess, args.ncu_steps, loop)
+    cal.core().calGetLastError()
+    m.cal_sciddicaT_close(sess)
+    print(json.dumps({"case": args.ncu_case, "declare": args.declare, "loop": args.loop, "rc": rc,
+                      "steps": args.ncu_warm + args.ncu_steps, "wall_s": time.perf_counter() - t0}), flush=True)
+    if rc:
+        raise SystemExit(1)
+
+
 def ncu_case(args):
     """A fixed, untimed sequence for ncu captures: open the 2048^2 session
     (activecells: with active cells on), run --ncu-steps fused steps from the
@@ -1038,6 +1074,8 @@ def ncu_case(args):
     allocations."""
     if args.ncu_case == "ensemble":
         return ncu_case_ensemble(args)
+    if args.ncu_case in ("processes", "processes_ac"):
+        return ncu_case_processes(args)
     ac = 1 if args.ncu_case == "activecells" else 0
     import opencal_gb300 as cal
     from opencal_gb300 import workloads as W
@@ -1074,9 +1112,13 @@ def main():
     ap.add_argument("--no-processes", action="store_true", help="skip the generic-engine (device processes) figure")
     ap.add_argument("--no-calibration", action="store_true", help="skip the batched-calibration section")
     ap.add_argument("--calib-iters", type=int, default=40)
-    ap.add_argument("--ncu-case", nargs="?", const="split", choices=["split", "ensemble", "activecells"],
+    ap.add_argument("--ncu-case", nargs="?", const="split",
+                    choices=["split", "ensemble", "activecells", "processes", "processes_ac"],
                     help="untimed fixed sequence for ncu captures")
     ap.add_argument("--ncu-steps", type=int, default=1002)
+    ap.add_argument("--ncu-warm", type=int, default=400, help="processes cases: steps before the captured ones")
+    ap.add_argument("--declare", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="processes cases: 1 processes declared pure, 2 reads declared, 3 both")
     ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara", "mbusu", "adjoint", "life"],
                     help="sciddicaT: the headline line; sciara: the SCIARA-fv2 scenario measurement; "
                          "mbusu: the 3D subsurface-flow program; adjoint: the SCIDDICA-T gradient at 1024^2, T = 2000; "
