@@ -70,12 +70,6 @@ struct CALDevModel2D {
      * untracked[type] and the update copies all of it */
     int track;
     int tiles_x, tiles_y, tile_words;
-    /* with tile skipping the launch is 4 blocks per SM (sms SMs), and block
-     * b takes the tiles congruent to (b % 4) * sms + b / 4 modulo the
-     * grid, so that neighbouring tiles -- which turn busy together -- go to
-     * blocks 4 apart, on different SMs whether the hardware deals blocks
-     * round-robin or four to an SM */
-    int sms;
     unsigned int* chg;
     unsigned int* untracked;
     /* tile skipping of a process declared pure (calSetElementaryProcessPure2D),
@@ -410,8 +404,7 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         const int ntiles = m.tiles_x * m.tiles_y;
         if (!STAGED) {
         /* tile by tile; with tile skipping only the tiles whose bit is set */
-        const int first = (m.run && m.sms > 0 && nblocks == 4 * m.sms) ? (bid % 4) * m.sms + bid / 4 : bid;
-        for (int tile = first; tile < ntiles; tile += nblocks) {
+        for (int tile = bid; tile < ntiles; tile += nblocks) {
             const unsigned tbit = 1u << (tile & 31);
             if (m.run && !(m.run[tile >> 5] & tbit))
                 continue;

@@ -503,21 +503,12 @@ static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned
                 d.stage_of[t][s] = -1;
     int gx, gy;
     g.launch_grid(&gx, &gy);
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-            sms = 152;
-    }
-    if (g.active || run) {
-        /* the active list, one cell per thread, or the tiles left to run
-         * after skipping: four resident blocks of 256 threads per SM (155K
-         * cells a pass on 152 SMs); fewer blocks launch faster than the
-         * dense grid, and with skipping the tiles are dealt SM-first */
+    if (g.active) {
+        /* the active list, one cell per thread: 608 blocks of 256 threads
+         * (four resident per SM) cover 155K cells a pass, and fewer blocks
+         * launch faster than the dense grid */
         gx = 1;
-        gy = 4 * sms;
-        d.sms = sms;
+        gy = 152 * 4;
     }
     int rc = launch(&d, gx, gy, (void*)g.stream);
     if (rc != 0) {
