@@ -610,12 +610,22 @@ def calibration_section(args):
         t_b.append(time.perf_counter() - t0)
     batched_s = float(np.median(t_b))
     g_launches0, g_nodes = ens.graph_stats()
-    # the same evaluation launch by launch (tape layout on the host), once
+    tape = ens.tape_info()
+    # the same evaluation launch by launch, once
     ens.set_graph(False)
     t0 = time.perf_counter()
     ens.loss_grad(tgt)
     batched_eager_s = time.perf_counter() - t0
     ens.set_graph(True)
+    # and with the sqrt(T) segments recomputed from checkpoints (the mode
+    # taken when the whole rollout's tape does not fit), once after a
+    # recording call
+    ens.set_tape("segments")
+    ens.loss_grad(tgt)
+    t0 = time.perf_counter()
+    ens.loss_grad(tgt)
+    batched_segments_s = time.perf_counter() - t0
+    ens.set_tape("auto")
 
     # the plain drop-in per instance with central differences (five runs):
     # its run loop (the recorded step replayed), and the fastest single-grid
@@ -692,12 +702,13 @@ def calibration_section(args):
             "batched_sample_recovered": batched_on_sample,
         },
         # one launch of the recorded evaluation; its nodes: forward (init +
-        # one step kernel per step, checkpoint copies), loss, tape layout;
-        # backward per step: recomputed step, tape restore, coefficients,
-        # gather; the result copies
+        # one step kernel per step, each taping its tiles), loss; backward
+        # per step: tape restore, coefficients, gather; the result copies
         "gpu_launches_per_batched_iter": 1,
         "graph_nodes_per_batched_iter": g_nodes,
         "batched_iter_s_launch_by_launch": batched_eager_s,
+        "tape": {"whole_rollout": tape["full"], "bytes": tape["need_bytes"],
+                 "batched_iter_s_sqrt_t_segments": batched_segments_s},
     }
 
 

@@ -111,10 +111,19 @@ int cal_sdt_batch_loss_grad(void* ensemble, const double* target /* device */, d
                             double* grad /* 2B */, double* dL_dh0 /* device, or NULL */);
 /* 1 (default): cal_sdt_batch_loss_grad is one launch of a recorded CUDA graph
  * (forward, loss, tape layout computed on the device, reverse sweep, results
- * to pinned host memory) for rollouts of up to 1024 steps; 0: launch by
- * launch with the tape layout computed on the host */
+ * to pinned host memory); 0: launch by launch.  Segmented tapes of more than
+ * 32 steps a segment (rollouts over 1024 steps) are laid out on the host and
+ * run launch by launch. */
 int cal_sdt_batch_set_graph(void* ensemble, int on);
 int cal_sdt_batch_graph_stats(void* ensemble, long long* launches, long long* nodes);
+/* What the adjoint's tape holds: -1 (default) the whole rollout (the
+ * backward recomputes nothing) while that tape fits in half of the free
+ * device memory, else sqrt(T) segments recomputed from checkpoints; 0 always
+ * segments; 1 always the whole rollout. */
+int cal_sdt_batch_set_tape(void* ensemble, int mode);
+/* info[0] = 1 when the last evaluation taped the whole rollout, info[1] =
+ * tape capacity (bytes), info[2] = tape bytes the last evaluation needed */
+int cal_sdt_batch_tape_info(void* ensemble, long long* info /* 3 */);
 
 /* ---- SCIARA-fv2 (OpenCAL-OMP/examples/calomp_sciara-fv2/source/Sciara.cpp) ----
  * params: Pclock, PTsol, PTvent, Pr(Tsol), Pr(Tvent), Phc(Tsol), Phc(Tvent),

@@ -27,13 +27,17 @@
  * left out of L_t was unchanged by steps t-1 and t, so both buffers hold its
  * value.  Dry tiles far from the flow cost nothing.
  *
- * Adjoint.  sqrt(T) checkpointing: h is stored every K = ceil(sqrt(T))
- * steps.  The backward recomputes one segment from its checkpoint with the
- * stored work-lists and, doing so, TAPES each processed tile's input
- * values; reversing the segment, it restores the taped tiles of step t into
- * the state (turning h_{t+1} into h_t in place: the other tiles did not
- * change) and runs the adjoint kernels on the tiles of L_t only (lambda
- * changes only within one cell of a wet cell).  The adjoint of one step is
+ * Adjoint.  The forward TAPES each processed tile's input values, step
+ * after step at offsets the steps chain on the device; the backward walks
+ * the rollout in reverse, restoring the taped tiles of step t into the
+ * state (turning h_{t+1} into h_t in place: the other tiles did not change)
+ * and running the adjoint kernels on the tiles of L_t only (lambda changes
+ * only within one cell of a wet cell).  The tape holds every tile a step
+ * processed, so it grows with the flow's area times T; when it would not
+ * fit in device memory the ensemble falls back to sqrt(T) checkpointing: h
+ * is stored every K = ceil(sqrt(T)) steps and the backward recomputes one
+ * segment at a time from its checkpoint with the stored work-lists, taping
+ * that segment only.  The adjoint of one step is
  * the single-model one (sciddicaT_adjoint.cu): elimination sets recomputed
  * bit-identically from h_t and frozen; lambda is updated in place; per-
  * instance dL/dp_r and dL/dp_eps are block-reduced per tile and added with
@@ -90,7 +94,8 @@ struct Batch {
     double* hbuf[2] = {nullptr, nullptr};
     double* ckpt = nullptr; /* nseg x N */
     double* tape = nullptr;
-    size_t tape_cap = 0;    /* doubles */
+    unsigned char* etape = nullptr; /* elimination sets, one byte per taped cell */
+    size_t tape_cap = 0;    /* cells (doubles of tape, bytes of etape) */
     double *lam = nullptr, *lamz = nullptr, *g = nullptr, *gz = nullptr, *w = nullptr;
     double* grad = nullptr; /* 2B: dL/dr[0..B), dL/deps[B..2B) */
     double* loss = nullptr; /* B */
@@ -107,13 +112,43 @@ struct Batch {
     const double* g_target = nullptr;
     const double* g_gh0 = nullptr;
     const double* g_tape = nullptr;
+    const unsigned char* g_etape = nullptr;
     int g_shape = -1;
     long long graph_launches = 0;
     long long graph_nodes = 0;  /* kernel and copy nodes of the recorded evaluation */
     bool use_graph = true;
+    /* what the tape holds: the whole rollout (run_full: the backward
+     * recomputes nothing) or one sqrt(T) segment at a time.  tape_mode -1
+     * chooses by memory: the whole rollout while its tape (plus a quarter)
+     * fits in half of the device memory free for it, else segments; 0
+     * always segments, 1 always the whole rollout */
+    int tape_mode = -1;
+    bool run_full = true;
+    bool g_full = true;
+    long long last_need = 0; /* doubles of tape the last evaluation needed */
 };
 
 static int tile_cells(const Batch& bt) { return kShapes[bt.shape].tw * kShapes[bt.shape].th; }
+
+/* a tape (and elimination tape) for `cap` cells; false when out of memory */
+static bool grow_tape(Batch& bt, size_t cap)
+{
+    cudaFree(bt.tape);
+    cudaFree(bt.etape);
+    bt.tape = nullptr;
+    bt.etape = nullptr;
+    bt.tape_cap = 0;
+    if (cudaMalloc(&bt.tape, cap * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&bt.etape, cap) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaFree(bt.tape);
+        bt.tape = nullptr;
+        bt.etape = nullptr;
+        return false;
+    }
+    bt.tape_cap = cap;
+    return true;
+}
 
 /* re-tile every instance for the current shape */
 static void drop_graph(Batch& bt)
@@ -192,27 +227,38 @@ static __device__ __forceinline__ void mark(int* stamps, int* list, int* count, 
 
 /* One ensemble step over the work-list (list, *count): h -> hn.  With a
  * next list the following step's list is built; with a tape the processed
- * tiles' input values are saved (tile k of the list at tape + k * TW * TH). */
+ * tiles' input values are saved (tile k of the list at tape + k * TW * TH)
+ * and, with an elimination tape, each wet cell's elimination set (one byte
+ * per cell at the same offsets). */
 template <int TW, int TH>
 __global__ void __launch_bounds__(sdt::THREADS) k_step(const Inst* __restrict__ inst, const int* __restrict__ tile_inst,
                                                        const double* __restrict__ z, const double* __restrict__ h,
                                                        double* __restrict__ hn, const int* __restrict__ list,
                                                        const int* __restrict__ count, int* list_next, int* count_next,
                                                        int* stamps, int stamp, double* __restrict__ tape,
-                                                       const long long* __restrict__ toff, long long tape_cap)
+                                                       unsigned char* __restrict__ etape,
+                                                       const long long* __restrict__ toff, long long* toff_next,
+                                                       long long tape_cap)
 {
     extern __shared__ __align__(16) double smem[];
     using TL = sdt::Tile<TW, TH>;
     const int n = *count;
-    if (tape && toff) {
-        /* the step's tiles at the device-computed offset; a segment that
-         * does not fit is not taped (the host sees `need` and runs again
-         * with a larger tape) */
+    if (toff) {
+        /* the step's tiles at the device-computed offset; steps that do not
+         * fit are not taped (the host sees `need` and runs again with a
+         * larger tape).  When the whole rollout is taped the step also
+         * places the next one: toff[t + 1] = toff[t] + its tiles. */
         const long long off = *toff;
-        if (off + (long long)n * (TW * TH) > tape_cap)
+        const long long end = off + (long long)n * (TW * TH);
+        if (toff_next && blockIdx.x == 0 && threadIdx.x == 0)
+            *toff_next = end;
+        if (!tape || end > tape_cap) {
             tape = nullptr;
-        else
+            etape = nullptr;
+        } else {
             tape += off;
+            etape = etape ? etape + off : nullptr;
+        }
     }
     for (int k = blockIdx.x; k < n; k += gridDim.x) {
         const int t = list[k];
@@ -220,7 +266,8 @@ __global__ void __launch_bounds__(sdt::THREADS) k_step(const Inst* __restrict__ 
         const int lt = t - I.tile0;
         const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
         const sdt::Params p = params_of(I, z, h, hn);
-        const int wet = sdt::fused_tile<TW, TH, true>(p, ty * TH, tx * TW, smem);
+        const int wet = sdt::fused_tile<TW, TH, true>(p, ty * TH, tx * TW, smem, false,
+                                                      etape ? etape + (size_t)k * (TW * TH) : nullptr);
         if (tape) {
             /* the tile's input h is still in shared memory (load region, +2 ring) */
             const double* sh = smem + TL::R2W * TL::R2H;
@@ -370,19 +417,31 @@ static __device__ __forceinline__ double block_sum(double v, double* s_red)
 /* adjoint coefficients g, gz, w of the wet cells of the listed tiles (the
  * single-model k_coeffs; k_gather reads them at wet cells only), and the
  * tiles' contributions to dL/dr, dL/deps.  The wet cells of a tile are
- * compacted first so that warps run the FP64 elimination densely. */
+ * compacted first.  The elimination sets are the forward's, read from the
+ * elimination tape (etape, at the step's offset *toff when toff is given),
+ * so the minimisation is not iterated again: the average is the one sum
+ * over the kept cells and one division, the last pass of the forward's
+ * iteration, bit for bit.  A step that was not taped (the evaluation is
+ * discarded and run again with a larger tape) is skipped. */
 template <int TW, int TH>
 __global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, const int* __restrict__ tile_inst,
                                               const int* __restrict__ list, const int* __restrict__ count, long long N,
                                               const double* __restrict__ z, const double* __restrict__ h,
                                               const double* __restrict__ lam, double* __restrict__ g,
                                               double* __restrict__ gz, double* __restrict__ w,
-                                              double* __restrict__ grad, int B)
+                                              double* __restrict__ grad, int B, const unsigned char* __restrict__ etape,
+                                              const long long* __restrict__ toff, long long tape_cap)
 {
     __shared__ double s_red[T / 32];
     __shared__ unsigned short s_wet[TW * TH];
     __shared__ int s_n;
     const int n = *count;
+    if (etape && toff) {
+        const long long off = *toff;
+        etape = off + (long long)n * (TW * TH) > tape_cap ? nullptr : etape + off;
+    }
+    if (!etape)
+        return;
     for (int k = blockIdx.x; k < n; k += gridDim.x) {
         const int t = list[k];
         const int bi = tile_inst[t];
@@ -418,28 +477,17 @@ __global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, con
                 lnb[d] = in ? lam[cn] : 0.0;
             }
             const double m = hc - I.eps;
-            unsigned elim = 0;
-            double avg;
-            bool again;
-            do {
-                again = false;
-                avg = m;
-                int cnt = 0;
+            const unsigned elim = etape[(size_t)k * (TW * TH) + q];
+            double avg = m;
+            int cnt = 0;
 #pragma unroll
-                for (int d = 0; d < 5; d++)
-                    if (!(elim & (1u << d))) {
-                        avg += u[d];
-                        cnt++;
-                    }
-                if (cnt != 0)
-                    avg = cal_div_small(avg, cnt);
-#pragma unroll
-                for (int d = 0; d < 5; d++)
-                    if (!(elim & (1u << d)) && cal_le(avg, u[d])) {
-                        elim |= 1u << d;
-                        again = true;
-                    }
-            } while (again);
+            for (int d = 0; d < 5; d++)
+                if (!(elim & (1u << d))) {
+                    avg += u[d];
+                    cnt++;
+                }
+            if (cnt != 0)
+                avg = cal_div_small(avg, cnt);
             const unsigned a_set = (~elim) & 31u;
             const int kk = __popc(a_set);
             if (kk > 0) {
@@ -588,14 +636,19 @@ static int step_grid()
 
 /* step t: list L_t -> (mark ? L_{t+1}) */
 template <int TW, int TH>
-static void launch_step(Batch& bt, int t, const double* h, double* hn, bool mark, double* tape,
-                        const long long* toff = nullptr)
+/* taped: the step's tiles go to the tape (and their elimination sets to the
+ * elimination tape) at the device offset *toff, or at host_off when toff is
+ * NULL; toff_next: where the step chains the next step's offset */
+static void launch_step(Batch& bt, int t, const double* h, double* hn, bool mark, bool taped = false,
+                        const long long* toff = nullptr, long long* toff_next = nullptr, size_t host_off = 0)
 {
     const size_t nt = (size_t)bt.ntiles;
+    double* tape = taped && bt.tape ? bt.tape + host_off : nullptr;
+    unsigned char* etape = taped && bt.etape ? bt.etape + host_off : nullptr;
     k_step<TW, TH><<<step_grid<TW, TH>(), sdt::THREADS, sdt::Tile<TW, TH>::smem_bytes, bt.st>>>(
         bt.d_inst, bt.d_tile_inst, bt.z, h, hn, bt.lists + nt * t, bt.counts + t,
-        mark ? bt.lists + nt * (t + 1) : nullptr, bt.counts + t + 1, bt.stamps, t + 2, tape, toff,
-        (long long)bt.tape_cap);
+        mark ? bt.lists + nt * (t + 1) : nullptr, bt.counts + t + 1, bt.stamps, t + 2, tape, etape, toff,
+        toff_next, (long long)bt.tape_cap);
 }
 
 template <int TW, int TH>
@@ -606,11 +659,13 @@ static void launch_restore(Batch& bt, int t, const double* tape, double* h, cons
 }
 
 template <int TW, int TH>
-static void launch_adjoint(Batch& bt, int t, const double* h)
+static void launch_adjoint(Batch& bt, int t, const double* h, const long long* toff = nullptr, size_t host_off = 0)
 {
     const int* list = bt.lists + (size_t)bt.ntiles * t;
     k_coeffs<TW, TH><<<152 * 8, T, 0, bt.st>>>(bt.d_inst, bt.d_tile_inst, list, bt.counts + t, bt.N, bt.z, h, bt.lam,
-                                                bt.g, bt.gz, bt.w, bt.grad, bt.B);
+                                                bt.g, bt.gz, bt.w, bt.grad, bt.B,
+                                                bt.etape ? bt.etape + host_off : nullptr, toff,
+                                                (long long)bt.tape_cap);
     k_gather<TW, TH><<<152 * 8, T, 0, bt.st>>>(bt.d_inst, bt.d_tile_inst, list, bt.counts + t, bt.N, h, bt.g, bt.gz,
                                                 bt.w, bt.lam, bt.lamz);
 }
@@ -624,8 +679,10 @@ static void launch_adjoint(Batch& bt, int t, const double* h)
     default: fn<64, 32>(__VA_ARGS__); break;                   \
     }
 
-/* forward over `steps` steps from h0; checkpoints every K steps when keep */
-static void forward(Batch& bt, int steps, bool keep)
+/* forward over `steps` steps from h0; checkpoints every K steps when keep;
+ * with `taped`, every step's tiles go to the tape at device-chained offsets
+ * (toff[0] = 0, toff[t + 1] = toff[t] + the tiles of step t) */
+static void forward(Batch& bt, int steps, bool keep, bool taped = false)
 {
     const size_t nb = (size_t)bt.N * sizeof(double);
     const int tw = kShapes[bt.shape].tw, th = kShapes[bt.shape].th;
@@ -634,10 +691,17 @@ static void forward(Batch& bt, int steps, bool keep)
     k_init<<<dense_grid(bt.N), T, sizeof(long long) * (bt.B + 1), bt.st>>>(bt.d_inst, bt.d_offs, bt.B, bt.N, tw, th,
                                                                            bt.z_dem, bt.h0, bt.z, bt.hbuf[0],
                                                                            bt.hbuf[1], bt.stamps, bt.lists, bt.counts);
+    if (taped)
+        cudaMemsetAsync(bt.toff, 0, sizeof(long long), bt.st);
     for (int t = 0; t < steps; t++) {
         if (keep && t % bt.K == 0)
             cudaMemcpyAsync(bt.ckpt + (size_t)(t / bt.K) * bt.N, bt.hbuf[t & 1], nb, cudaMemcpyDeviceToDevice, bt.st);
-        SDTB_DISPATCH(bt, launch_step, bt, t, bt.hbuf[t & 1], bt.hbuf[(t + 1) & 1], true, nullptr);
+        if (taped) {
+            SDTB_DISPATCH(bt, launch_step, bt, t, bt.hbuf[t & 1], bt.hbuf[(t + 1) & 1], true, true, bt.toff + t,
+                          bt.toff + t + 1);
+        } else {
+            SDTB_DISPATCH(bt, launch_step, bt, t, bt.hbuf[t & 1], bt.hbuf[(t + 1) & 1], true);
+        }
     }
 }
 
@@ -650,7 +714,7 @@ static void destroy(Batch* bt)
     if (bt->h_out)
         cudaFreeHost(bt->h_out);
     void* ptrs[] = {bt->d_inst, bt->d_offs, bt->d_tile_inst, bt->stamps, bt->lists, bt->counts, bt->z_dem,
-                    bt->z,      bt->h0,     bt->hbuf[0],      bt->hbuf[1], bt->ckpt, bt->tape,   bt->lam,
+                    bt->z,      bt->h0,     bt->hbuf[0],      bt->hbuf[1], bt->ckpt, bt->tape,   bt->etape, bt->lam,
                     bt->lamz,   bt->g,      bt->gz,           bt->w,      bt->grad,  bt->loss};
     for (void* p : ptrs)
         cudaFree(p);
@@ -793,26 +857,36 @@ static void queue_loss_grad(Batch& bt, const double* target, double* g_h0)
 {
     const size_t nb = (size_t)bt.N * sizeof(double);
     cudaStream_t st = bt.st;
-    forward(bt, bt.steps, true);
+    forward(bt, bt.steps, !bt.run_full, bt.run_full);
     cudaMemsetAsync(bt.loss, 0, bt.B * sizeof(double), st);
     cudaMemsetAsync(bt.grad, 0, 2 * bt.B * sizeof(double), st);
     k_loss<<<dense_grid(bt.N), T, sizeof(long long) * (bt.B + 1), st>>>(bt.d_inst, bt.d_offs, bt.B, bt.N,
                                                                          bt.hbuf[bt.steps & 1], target, bt.lam,
                                                                          bt.lamz, bt.loss);
-    k_tape_offsets<<<1, 1024, 0, st>>>(bt.counts, bt.steps, bt.K, tile_cells(bt), bt.toff);
-    for (int s = bt.nseg - 1; s >= 0; s--) {
+    if (bt.run_full) {
+        /* the whole rollout is on the tape: no recomputation, the state
+         * buffer holding h_T is walked back one step at a time */
+        double* X = bt.hbuf[bt.steps & 1];
+        for (int t = bt.steps - 1; t >= 0; t--) {
+            SDTB_DISPATCH(bt, launch_restore, bt, t, bt.tape, X, bt.toff + t);
+            SDTB_DISPATCH(bt, launch_adjoint, bt, t, X, bt.toff + t);
+        }
+    } else {
+        k_tape_offsets<<<1, 1024, 0, st>>>(bt.counts, bt.steps, bt.K, tile_cells(bt), bt.toff);
+    }
+    for (int s = bt.run_full ? -1 : bt.nseg - 1; s >= 0; s--) {
         const int t0 = s * bt.K, t1 = std::min(t0 + bt.K, bt.steps);
         if (t1 <= t0)
             continue;
         cudaMemcpyAsync(bt.hbuf[0], bt.ckpt + (size_t)s * bt.N, nb, cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(bt.hbuf[1], bt.ckpt + (size_t)s * bt.N, nb, cudaMemcpyDeviceToDevice, st);
         for (int t = t0; t < t1; t++)
-            SDTB_DISPATCH(bt, launch_step, bt, t, bt.hbuf[(t - t0) & 1], bt.hbuf[(t - t0 + 1) & 1], false, bt.tape,
+            SDTB_DISPATCH(bt, launch_step, bt, t, bt.hbuf[(t - t0) & 1], bt.hbuf[(t - t0 + 1) & 1], false, true,
                           bt.toff + t);
         double* X = bt.hbuf[(t1 - t0) & 1];
         for (int t = t1 - 1; t >= t0; t--) {
             SDTB_DISPATCH(bt, launch_restore, bt, t, bt.tape, X, bt.toff + t);
-            SDTB_DISPATCH(bt, launch_adjoint, bt, t, X);
+            SDTB_DISPATCH(bt, launch_adjoint, bt, t, X, bt.toff + t);
         }
     }
     if (g_h0)
@@ -822,48 +896,64 @@ static void queue_loss_grad(Batch& bt, const double* target, double* g_h0)
     cudaMemcpyAsync(bt.h_out + 3 * bt.B, bt.toff + bt.steps, sizeof(long long), cudaMemcpyDeviceToHost, st);
 }
 
-/* one evaluation as one launch of the recorded graph (recorded again when
- * the target, the dL/dh0 buffer, the tile shape or the tape changed); when
- * the tape was too small for a segment the evaluation is discarded, the
- * tape grown to the size the device reported (plus a quarter) and the
- * evaluation run again.  0 on success. */
-static int loss_grad_graph(Batch& bt, const double* target, double* loss_out, double* grad_out, double* g_h0)
+/* One evaluation queued with the tape layout computed on the device: as one
+ * launch of the recorded graph (recorded again when the target, the dL/dh0
+ * buffer, the tile shape, the tape or what it holds changed), or launch by
+ * launch.  When the tape was too small the evaluation is discarded, the tape
+ * grown to the size the device reported (plus a quarter) and the evaluation
+ * run again; in the memory-chosen mode a whole-rollout tape that would not
+ * fit switches the ensemble to segments.  0 on success; SEGMENTS_ON_HOST
+ * when segments of more than 32 steps are needed (the caller runs them with
+ * the layout computed on the host). */
+constexpr int SEGMENTS_ON_HOST = -2;
+
+static int loss_grad_device(Batch& bt, const double* target, double* loss_out, double* grad_out, double* g_h0)
 {
     cudaStream_t st = bt.st;
     if (!bt.toff && cudaMalloc(&bt.toff, sizeof(long long) * (bt.steps + 1)) != cudaSuccess)
         return (int)cudaErrorMemoryAllocation;
     if (!bt.h_out && cudaMallocHost(&bt.h_out, sizeof(double) * (3 * bt.B + 1)) != cudaSuccess)
         return (int)cudaErrorMemoryAllocation;
-    for (int attempt = 0; attempt < 3; attempt++) {
-        if (!bt.gexec || bt.g_target != target || bt.g_gh0 != g_h0 || bt.g_shape != bt.shape ||
-            bt.g_tape != bt.tape) {
-            drop_graph(bt);
-            cudaGraph_t graph = nullptr;
-            if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-                return (int)cudaGetLastError();
-            queue_loss_grad(bt, target, g_h0);
-            cudaError_t e = cudaStreamEndCapture(st, &graph);
-            if (e != cudaSuccess || !graph) {
-                (void)cudaGetLastError();
-                return (int)(e != cudaSuccess ? e : cudaErrorUnknown);
+    for (int attempt = 0; attempt < 4; attempt++) {
+        if (!bt.run_full && bt.K > 32)
+            return SEGMENTS_ON_HOST;
+        if (bt.use_graph) {
+            if (!bt.gexec || bt.g_target != target || bt.g_gh0 != g_h0 || bt.g_shape != bt.shape ||
+                bt.g_tape != bt.tape || bt.g_etape != bt.etape || bt.g_full != bt.run_full) {
+                drop_graph(bt);
+                cudaGraph_t graph = nullptr;
+                if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                    return (int)cudaGetLastError();
+                queue_loss_grad(bt, target, g_h0);
+                cudaError_t e = cudaStreamEndCapture(st, &graph);
+                if (e != cudaSuccess || !graph) {
+                    (void)cudaGetLastError();
+                    return (int)(e != cudaSuccess ? e : cudaErrorUnknown);
+                }
+                e = cudaGraphInstantiate(&bt.gexec, graph, 0);
+                size_t nodes = 0;
+                cudaGraphGetNodes(graph, nullptr, &nodes);
+                bt.graph_nodes = (long long)nodes;
+                cudaGraphDestroy(graph);
+                if (e != cudaSuccess)
+                    return (int)e;
+                bt.g_target = target;
+                bt.g_gh0 = g_h0;
+                bt.g_shape = bt.shape;
+                bt.g_tape = bt.tape;
+                bt.g_etape = bt.etape;
+                bt.g_full = bt.run_full;
             }
-            e = cudaGraphInstantiate(&bt.gexec, graph, 0);
-            size_t nodes = 0;
-            cudaGraphGetNodes(graph, nullptr, &nodes);
-            bt.graph_nodes = (long long)nodes;
-            cudaGraphDestroy(graph);
-            if (e != cudaSuccess)
-                return (int)e;
-            bt.g_target = target;
-            bt.g_gh0 = g_h0;
-            bt.g_shape = bt.shape;
-            bt.g_tape = bt.tape;
-        }
-        if (cudaGraphLaunch(bt.gexec, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
+            if (cudaGraphLaunch(bt.gexec, st) != cudaSuccess)
+                return (int)cudaGetLastError();
+            bt.graph_launches++;
+        } else
+            queue_loss_grad(bt, target, g_h0);
+        if (cudaStreamSynchronize(st) != cudaSuccess)
             return (int)cudaGetLastError();
-        bt.graph_launches++;
         long long need = 0;
         memcpy(&need, bt.h_out + 3 * bt.B, sizeof(need));
+        bt.last_need = need;
         if (need <= (long long)bt.tape_cap) {
             if (loss_out)
                 memcpy(loss_out, bt.h_out, bt.B * sizeof(double));
@@ -874,15 +964,23 @@ static int loss_grad_graph(Batch& bt, const double* target, double* loss_out, do
                 }
             return 0;
         }
-        cudaFree(bt.tape);
-        bt.tape = nullptr;
-        bt.tape_cap = 0;
         const size_t cap = (size_t)(need + need / 4);
-        if (cudaMalloc(&bt.tape, cap * sizeof(double)) != cudaSuccess) {
+        if (bt.run_full && bt.tape_mode < 0) {
+            size_t free_b = 0, total_b = 0;
+            cudaMemGetInfo(&free_b, &total_b);
+            if (cap * (sizeof(double) + 1) > (free_b + bt.tape_cap * (sizeof(double) + 1)) / 2) {
+                bt.run_full = false; /* the segments' tape is about sqrt(T) times smaller */
+                continue;
+            }
+        }
+        if (!grow_tape(bt, cap)) {
+            if (bt.run_full && bt.tape_mode < 0) {
+                bt.run_full = false;
+                continue;
+            }
             fprintf(stderr, "opencal-gb300: cal_sdt_batch_loss_grad: out of device memory for the tape\n");
             return (int)cudaErrorMemoryAllocation;
         }
-        bt.tape_cap = cap;
     }
     return (int)cudaErrorUnknown;
 }
@@ -898,10 +996,14 @@ extern "C" int cal_sdt_batch_loss_grad(void* handle, const double* target, doubl
                                        double* g_h0)
 {
     Batch* bt = (Batch*)handle;
-    /* segments of at most 32 steps (one warp each in k_tape_offsets):
-     * rollouts of up to 1024 steps run as one recorded graph */
-    if (bt->use_graph && bt->K <= 32 && bt->steps > 0)
-        return sdtb::loss_grad_graph(*bt, target, loss_out, grad_out, g_h0);
+    /* the tape layout is computed on the device for the whole rollout and
+     * for segments of at most 32 steps (one warp each in k_tape_offsets:
+     * rollouts of up to 1024 steps); longer segments are laid out here */
+    if (bt->steps > 0) {
+        const int rc = sdtb::loss_grad_device(*bt, target, loss_out, grad_out, g_h0);
+        if (rc != sdtb::SEGMENTS_ON_HOST)
+            return rc;
+    }
     const size_t nb = (size_t)bt->N * sizeof(double);
     const int tc = sdtb::tile_cells(*bt);
     cudaStream_t st = bt->st;
@@ -926,15 +1028,10 @@ extern "C" int cal_sdt_batch_loss_grad(void* handle, const double* target, doubl
         }
         need = std::max(need, acc);
     }
-    if (need > bt->tape_cap) {
-        cudaFree(bt->tape);
-        bt->tape = nullptr;
-        bt->tape_cap = 0;
-        if (cudaMalloc(&bt->tape, need * sizeof(double)) != cudaSuccess) {
-            fprintf(stderr, "opencal-gb300: cal_sdt_batch_loss_grad: out of device memory for the tape\n");
-            return (int)cudaErrorMemoryAllocation;
-        }
-        bt->tape_cap = need;
+    bt->last_need = (long long)need;
+    if (need > bt->tape_cap && !sdtb::grow_tape(*bt, need)) {
+        fprintf(stderr, "opencal-gb300: cal_sdt_batch_loss_grad: out of device memory for the tape\n");
+        return (int)cudaErrorMemoryAllocation;
     }
     for (int s = bt->nseg - 1; s >= 0; s--) {
         const int t0 = s * bt->K, t1 = std::min(t0 + bt->K, bt->steps);
@@ -944,11 +1041,11 @@ extern "C" int cal_sdt_batch_loss_grad(void* handle, const double* target, doubl
         cudaMemcpyAsync(bt->hbuf[1], bt->ckpt + (size_t)s * bt->N, nb, cudaMemcpyDeviceToDevice, st);
         for (int t = t0; t < t1; t++)
             SDTB_DISPATCH(*bt, sdtb::launch_step, *bt, t, bt->hbuf[(t - t0) & 1], bt->hbuf[(t - t0 + 1) & 1], false,
-                          bt->tape + tape_off[t]);
+                          true, nullptr, nullptr, tape_off[t]);
         double* X = bt->hbuf[(t1 - t0) & 1]; /* h_{t1} everywhere */
         for (int t = t1 - 1; t >= t0; t--) {
             SDTB_DISPATCH(*bt, sdtb::launch_restore, *bt, t, bt->tape + tape_off[t], X);
-            SDTB_DISPATCH(*bt, sdtb::launch_adjoint, *bt, t, X);
+            SDTB_DISPATCH(*bt, sdtb::launch_adjoint, *bt, t, X, nullptr, tape_off[t]);
         }
     }
     if (g_h0)
@@ -1029,12 +1126,37 @@ extern "C" int cal_sdt_batch_set_shape(void* handle, int shape)
 }
 
 /* 1 (default): cal_sdt_batch_loss_grad runs as one launch of a recorded
- * graph (rollouts of up to 1024 steps); 0: launch by launch with the tape
- * layout computed on the host */
+ * graph; 0: launch by launch */
 extern "C" int cal_sdt_batch_set_graph(void* handle, int on)
 {
     Batch* bt = (Batch*)handle;
     bt->use_graph = on != 0;
+    return 0;
+}
+
+/* What the adjoint's tape holds: -1 (default) the whole rollout while it
+ * fits in half of the free device memory, else sqrt(T) segments recomputed
+ * from checkpoints; 0 always segments; 1 always the whole rollout.  1 on a
+ * bad mode. */
+extern "C" int cal_sdt_batch_set_tape(void* handle, int mode)
+{
+    Batch* bt = (Batch*)handle;
+    if (mode < -1 || mode > 1)
+        return 1;
+    bt->tape_mode = mode;
+    bt->run_full = mode != 0;
+    return 0;
+}
+
+/* info[0] = 1 when the last evaluation taped the whole rollout (0:
+ * segments), info[1] = the tape's capacity in bytes, info[2] = the bytes of
+ * tape the last evaluation needed */
+extern "C" int cal_sdt_batch_tape_info(void* handle, long long* info)
+{
+    Batch* bt = (Batch*)handle;
+    info[0] = bt->run_full ? 1 : 0;
+    info[1] = (long long)(bt->tape_cap * (sizeof(double) + 1));
+    info[2] = bt->last_need * (long long)(sizeof(double) + 1);
     return 0;
 }
 

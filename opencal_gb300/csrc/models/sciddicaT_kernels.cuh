@@ -146,7 +146,8 @@ static __device__ __forceinline__ void warp_append_shared(bool pred, int value, 
  * the block-uniform result has bit 0 set when a cell of the tile was wet
  * before the step and bit 1 when one is wet after it (0 without TRACK). */
 template <int TW, int TH, bool TRACK = false>
-__device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, double* smem, bool staged = false)
+__device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, double* smem, bool staged = false,
+                                          unsigned char* elim_tile = nullptr)
 {
     using T = Tile<TW, TH>;
     double* sz = smem;                      /* [R2H][R2W] */
@@ -257,10 +258,15 @@ __device__ __forceinline__ int fused_tile(const Params& p, int i0, int j0, doubl
         const double u3 = sz[c + 1] + sh[c + 1];
         const double u4 = sz[c + T::R2W] + sh[c + T::R2W];
         double f[4];
-        outflows(sh[c], sz[c], u1, u2, u3, u4, p.eps, p.r, f);
+        unsigned elim;
+        outflows(sh[c], sz[c], u1, u2, u3, u4, p.eps, p.r, f, &elim);
 #pragma unroll
         for (int q = 0; q < 4; q++)
             sf[q * F + t] = f[q];
+        /* the tile's own cells' elimination sets, for an adjoint that
+         * reuses them (elim_tile: TW x TH bytes, row-major) */
+        if (elim_tile && a >= 1 && a <= TH && b >= 1 && b <= TW)
+            elim_tile[(a - 1) * TW + (b - 1)] = (unsigned char)elim;
     }
     __syncthreads();
 

@@ -52,6 +52,8 @@ def _lib():
         m.cal_sdt_batch_loss_grad.argtypes = [C.c_void_p, C.c_void_p, _pd, _pd, C.c_void_p]
         m.cal_sdt_batch_set_graph.argtypes = [C.c_void_p, C.c_int]
         m.cal_sdt_batch_graph_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        m.cal_sdt_batch_set_tape.argtypes = [C.c_void_p, C.c_int]
+        m.cal_sdt_batch_tape_info.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
         m.cal_sdt_batch_autotune.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_float)]
         m.cal_sdt_batch_set_shape.argtypes = [C.c_void_p, C.c_int]
         m.cal_sciddicaT_open.restype = C.c_void_p
@@ -167,6 +169,20 @@ class Ensemble:
     def set_graph(self, on: bool) -> None:
         """loss_grad as one launch of a recorded graph (default) or launch by launch."""
         self._lib.cal_sdt_batch_set_graph(self.handle, 1 if on else 0)
+
+    def set_tape(self, mode: str) -> None:
+        """What the adjoint's tape holds: "auto" (the whole rollout while it fits in
+        half of the free device memory, else sqrt(T) segments), "segments", "full"."""
+        code = {"auto": -1, "segments": 0, "full": 1}[mode]
+        if self._lib.cal_sdt_batch_set_tape(self.handle, code):
+            raise CALError(f"bad tape mode {mode}")
+
+    def tape_info(self) -> dict:
+        """{"full": the last evaluation taped the whole rollout, "capacity_bytes",
+        "need_bytes": tape the last evaluation needed}"""
+        info = (C.c_longlong * 3)()
+        self._lib.cal_sdt_batch_tape_info(self.handle, info)
+        return {"full": bool(info[0]), "capacity_bytes": int(info[1]), "need_bytes": int(info[2])}
 
     def graph_stats(self) -> tuple[int, int]:
         """(graph launches made by loss_grad so far, nodes of the recorded evaluation)"""

@@ -134,6 +134,54 @@ def test_recorded_evaluation_equals_launch_by_launch(env):
     np.testing.assert_allclose(h1.cpu().numpy(), h0.cpu().numpy(), rtol=1e-9, atol=1e-12)
 
 
+@pytest.mark.parametrize("graph", [True, False])
+def test_whole_rollout_tape_equals_segments(env, graph):
+    """the adjoint with the whole rollout on the tape (no recomputation)
+    against sqrt(T) segments recomputed from checkpoints: same losses, same
+    dL/dh0, gradients equal up to the summation order of their atomics"""
+    torch, oracle, E, params, zs, hs = env
+    true = [(p[0] * 0.9, p[1] * 1.2) for p in params]
+    tgts = _refs(oracle, true, zs, hs, STEPS)
+    ens = E.Ensemble(DIMS, params, zs, hs, STEPS)
+    ens.set_graph(graph)
+    tgt = ens.pack(tgts)
+    assert ens.tape_info()["full"]  # the default chooses by memory: this small ensemble fits
+    ens.set_tape("segments")
+    l0, g0, h0 = ens.loss_grad(tgt, want_h0_grad=True)
+    seg = ens.tape_info()
+    ens.set_tape("full")
+    l1, g1, h1 = ens.loss_grad(tgt, want_h0_grad=True)
+    full = ens.tape_info()
+    assert not seg["full"] and full["full"]
+    assert full["need_bytes"] > seg["need_bytes"] > 0
+    assert full["capacity_bytes"] >= full["need_bytes"]
+    np.testing.assert_allclose(l1, l0, rtol=1e-12, atol=0)  # per-block sums added by atomics
+    np.testing.assert_allclose(g1, g0, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(h1.cpu().numpy(), h0.cpu().numpy(), rtol=1e-12, atol=1e-15)
+
+
+def test_long_rollout_segments_laid_out_on_host(env):
+    """1100 steps: segments of 34 steps are laid out on the host and run
+    launch by launch; the whole-rollout tape (offsets chained on the device)
+    gives the same losses and gradients"""
+    torch, oracle, E, params, zs, hs = env
+    steps = 1100
+    dims, ps = DIMS[:2], params[:2]
+    true = [(p[0] * 0.9, p[1] * 1.2) for p in ps]
+    tgts = _refs(oracle, true, zs[:2], hs[:2], steps)
+    ens = E.Ensemble(dims, ps, zs[:2], hs[:2], steps)
+    tgt = ens.pack(tgts)
+    ens.set_tape("segments")
+    l0, g0, h0 = ens.loss_grad(tgt, want_h0_grad=True)
+    assert ens.graph_stats()[0] == 0  # not run as a graph
+    ens.set_tape("full")
+    l1, g1, h1 = ens.loss_grad(tgt, want_h0_grad=True)
+    assert ens.graph_stats()[0] >= 1
+    np.testing.assert_allclose(l1, l0, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(g1, g0, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(h1.cpu().numpy(), h0.cpu().numpy(), rtol=1e-12, atol=1e-15)
+
+
 def test_fd_arm_agrees_with_adjoint(env):
     """central FD of the plain drop-in (the comparison arm) against the
     ensemble adjoint on one instance, at a point where no decision flips"""
