@@ -712,6 +712,24 @@ static __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p)
     return v;
 }
 
+/* An arrival: an atomic add with release semantics at GPU scope.  Issued by
+ * thread 0 after the block barrier, it orders every write the block made
+ * before that barrier ahead of the arrival (the block barrier orders the
+ * other threads' writes before thread 0's release; release is cumulative),
+ * and the acquire poll of a waiting block orders its later reads after it;
+ * no separate fence.sc on either side (measured on an empty 608-block grid:
+ * 5.2-5.5 us per barrier against 5.6-5.8 us with a fence.sc before a
+ * relaxed add and after the poll). */
+static __device__ __forceinline__ void red_release_gpu(unsigned* p, unsigned v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+static __device__ __forceinline__ void red_release_gpu(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 /* Grid barrier for a cooperative launch (all blocks resident).  Round r
  * (1, 2, ...) is complete when the monotonic arrival counter counts[C_ARRIVED]
  * reaches r * nblocks.  Every wait is bounded: after BARRIER_SPIN_LIMIT
@@ -728,8 +746,7 @@ static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblock
         unsigned* arrived = reinterpret_cast<unsigned*>(counts + C_ARRIVED);
         const unsigned target = round * nblocks;
         int ok = 1;
-        __threadfence();
-        atomicAdd(arrived, 1u);
+        red_release_gpu(arrived, 1u);
         unsigned polls = 0;
         while ((int)(ld_acquire_gpu(arrived) - target) < 0) {
             if (++polls > BARRIER_SPIN_LIMIT) {
@@ -739,7 +756,6 @@ static __device__ __forceinline__ bool grid_barrier(int* counts, unsigned nblock
             }
             __nanosleep(32);
         }
-        __threadfence();
         if (ok && __ldcg(counts + C_ERROR) != 0)
             ok = 0;
         out[0] = __ldcg(r0);
@@ -803,8 +819,7 @@ static __device__ __forceinline__ bool packed_barrier(unsigned long long* word, 
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        __threadfence();
-        atomicAdd(word, 1ull << 32);
+        red_release_gpu(word, 1ull << 32);
         unsigned polls = 0;
         unsigned long long v;
         while ((unsigned)((v = ld_acquire_gpu_u64(word)) >> 32) < nblocks) {
@@ -815,7 +830,6 @@ static __device__ __forceinline__ bool packed_barrier(unsigned long long* word, 
             }
             __nanosleep(32);
         }
-        __threadfence();
         *out = low32(v);
         s_ok = ok;
     }
