@@ -366,9 +366,12 @@ static __device__ __forceinline__ int calGetActiveCellCountDevice2D(const struct
  * each warp then adds its tile to the chg bitmap of every substate whose
  * next layer it changed.  At the end each block publishes which substates
  * it wrote (and which it wrote by unsafe operations). */
-template <void (*EP)(struct CALModel2D*, int, int), int NX, bool STAGED>
+template <void (*EP)(struct CALModel2D*, int, int), int NX, int MODE>
 __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_constant__ struct CALDevModel2D m)
 {
+    /* MODE 0: tile by tile; 1: declared reads staged by TMA; 2: tile
+     * skipping, the block's run bits fetched 32 tiles at a time */
+    constexpr bool STAGED = MODE == 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x) {
         cal_written2D[t] = 0;
@@ -403,11 +406,11 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     } else {
         const int ntiles = m.tiles_x * m.tiles_y;
         if (!STAGED) {
-        /* tile by tile; with tile skipping only the tiles whose bit is set */
-        for (int tile = bid; tile < ntiles; tile += nblocks) {
+        /* one tile, one cell per thread; with change tracking each warp
+         * records which substates its row changed, and with tile skipping
+         * the tile's bit is cleared when the process changed nothing there */
+        auto run_tile = [&](int tile) {
             const unsigned tbit = 1u << (tile & 31);
-            if (m.run && !(m.run[tile >> 5] & tbit))
-                continue;
             const int ty = tile / m.tiles_x;
             const int i = ty * CAL_TILE_H + warp, j = (tile - ty * m.tiles_x) * CAL_TILE_W + lane;
             if (i < m.rows && j < m.cols)
@@ -425,6 +428,27 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                 if (m.run && !__syncthreads_or(changed) && threadIdx.x == 0)
                     atomicAnd(&m.run[tile >> 5], ~tbit);
             }
+        };
+        if (MODE == 2) {
+            /* the block's tiles bid, bid + nblocks, ..., only those whose run
+             * bit is set.  The bits of 32 of them come in one load per lane
+             * and a ballot (the same in every warp: a bit is cleared only by
+             * the block that owns the tile, after every warp has taken its
+             * ballot), so that a block with nothing to run leaves after one
+             * round trip instead of one per tile.  Its own instantiation:
+             * the loop's state costs registers the plain loop does not pay. */
+            for (int base = bid; base < ntiles; base += 32 * nblocks) {
+                const int t = base + lane * nblocks;
+                bool need = t < ntiles;
+                if (need && m.run)
+                    need = (m.run[t >> 5] >> (t & 31)) & 1u;
+                for (unsigned todo = __ballot_sync(0xffffffffu, need); todo; todo &= todo - 1)
+                    run_tile(base + (__ffs(todo) - 1) * nblocks);
+            }
+        } else {
+            for (int tile = bid; tile < ntiles; tile += nblocks)
+                if (!m.run || (m.run[tile >> 5] >> (tile & 31)) & 1u)
+                    run_tile(tile);
         }
         } else {
         /* staged: the block's tiles bid, bid + nblocks, ...; with tile skipping only
@@ -544,9 +568,9 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
 }
 
 /* one kernel per common neighbourhood size (von Neumann 5, hexagonal 7,
- * Moore 9) and a generic one for the others, each with and without the
- * staging of declared reads (the staging loop costs registers and barriers
- * that the plain loop does not pay) */
+ * Moore 9) and a generic one for the others, each plain, with the staging
+ * of declared reads, and with tile skipping (the staging and skipping loops
+ * cost registers and barriers that the plain loop does not pay) */
 template <void (*EP)(struct CALModel2D*, int, int)>
 static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* stream)
 {
@@ -556,17 +580,24 @@ static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* 
     const size_t smem = m->nstage ? 2 * (size_t)m->stage_bytes + 128 : 0;
     if (m->nstage) {
         switch (m->model.sizeof_X) {
-        case 5: cal_ep2D_kernel<EP, 5, true><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
-        case 7: cal_ep2D_kernel<EP, 7, true><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
-        case 9: cal_ep2D_kernel<EP, 9, true><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
-        default: cal_ep2D_kernel<EP, 0, true><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        case 5: cal_ep2D_kernel<EP, 5, 1><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        case 7: cal_ep2D_kernel<EP, 7, 1><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        case 9: cal_ep2D_kernel<EP, 9, 1><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        default: cal_ep2D_kernel<EP, 0, 1><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        }
+    } else if (m->run) {
+        switch (m->model.sizeof_X) {
+        case 5: cal_ep2D_kernel<EP, 5, 2><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 7: cal_ep2D_kernel<EP, 7, 2><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 9: cal_ep2D_kernel<EP, 9, 2><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        default: cal_ep2D_kernel<EP, 0, 2><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
         }
     } else {
         switch (m->model.sizeof_X) {
-        case 5: cal_ep2D_kernel<EP, 5, false><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
-        case 7: cal_ep2D_kernel<EP, 7, false><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
-        case 9: cal_ep2D_kernel<EP, 9, false><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
-        default: cal_ep2D_kernel<EP, 0, false><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 5: cal_ep2D_kernel<EP, 5, 0><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 7: cal_ep2D_kernel<EP, 7, 0><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 9: cal_ep2D_kernel<EP, 9, 0><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        default: cal_ep2D_kernel<EP, 0, 0><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
         }
     }
     return (int)cudaGetLastError();
