@@ -466,18 +466,24 @@ def processes_plain_section(m, cal, z, h, h_plain):
     process kernels skip the tiles whose neighbourhood did not change since
     they last changed nothing there; and with their reads declared too
     (calSetElementaryProcessReads2D), which stages z, h and the outflows into
-    shared memory by TMA tile by tile.  Every form must give the split
-    step's bits."""
+    shared memory by TMA tile by tile; and pure with the flows process's
+    early return on dry cells declared (calSetElementaryProcessGuard2Dr),
+    which runs it on each tile's wet cells packed into consecutive threads.
+    Every form must give the split step's bits."""
     import torch
     m.cal_sciddicaT_set_pure.argtypes = [C.c_int]
     m.cal_sciddicaT_set_staged.argtypes = [C.c_int]
+    m.cal_sciddicaT_set_guard.argtypes = [C.c_int]
     out = {}
-    for label, pure, staged in (("as_written", 0, 0), ("declared_pure", 1, 0), ("declared_pure_and_reads", 1, 1)):
+    for label, pure, staged, guard in (("as_written", 0, 0, 0), ("declared_pure", 1, 0, 0),
+                                       ("declared_pure_and_reads", 1, 1, 0), ("declared_pure_and_guard", 1, 0, 1)):
         m.cal_sciddicaT_set_pure(pure)
         m.cal_sciddicaT_set_staged(staged)
+        m.cal_sciddicaT_set_guard(guard)
         sess = m.cal_sciddicaT_open(ROWS, COLS, 0, 0, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_PROCESSES)
         m.cal_sciddicaT_set_pure(0)
         m.cal_sciddicaT_set_staged(0)
+        m.cal_sciddicaT_set_guard(0)
         if not sess:
             return {"error": "cal_sciddicaT_open (processes) failed: " + cal.core().calGetErrorString().decode()}
         stream = torch.cuda.ExternalStream(m.cal_sciddicaT_stream(sess))
@@ -1059,13 +1065,16 @@ def ncu_case_processes(args):
     m.cal_sciddicaT_close.argtypes = [C.c_void_p]
     m.cal_sciddicaT_set_pure.argtypes = [C.c_int]
     m.cal_sciddicaT_set_staged.argtypes = [C.c_int]
+    m.cal_sciddicaT_set_guard.argtypes = [C.c_int]
     ac = 1 if args.ncu_case == "processes_ac" else 0
     z, h = W.sciddicaT_inputs(ROWS, COLS, seed=SEED)
     m.cal_sciddicaT_set_pure(args.declare & 1)
     m.cal_sciddicaT_set_staged((args.declare >> 1) & 1)
+    m.cal_sciddicaT_set_guard((args.declare >> 2) & 1)
     sess = m.cal_sciddicaT_open(ROWS, COLS, 0, ac, P_R, P_EPS, z.ctypes.data, h.ctypes.data, cal.MODE_PROCESSES)
     m.cal_sciddicaT_set_pure(0)
     m.cal_sciddicaT_set_staged(0)
+    m.cal_sciddicaT_set_guard(0)
     loop = {"eager": 0, "graph": 1, "device": 2}.get(args.loop, 0)
     t0 = time.perf_counter()
     rc = m.cal_sciddicaT_steps(sess, args.ncu_warm, loop)
@@ -1128,8 +1137,8 @@ def main():
                     help="untimed fixed sequence for ncu captures")
     ap.add_argument("--ncu-steps", type=int, default=1002)
     ap.add_argument("--ncu-warm", type=int, default=400, help="processes cases: steps before the captured ones")
-    ap.add_argument("--declare", type=int, default=0, choices=[0, 1, 2, 3],
-                    help="processes cases: 1 processes declared pure, 2 reads declared, 3 both")
+    ap.add_argument("--declare", type=int, default=0, choices=range(8),
+                    help="processes cases, bits: 1 processes declared pure, 2 reads declared, 4 flows guard declared")
     ap.add_argument("--workload", default="sciddicaT", choices=["sciddicaT", "sciara", "mbusu", "adjoint", "life"],
                     help="sciddicaT: the headline line; sciara: the SCIARA-fv2 scenario measurement; "
                          "mbusu: the 3D subsurface-flow program; adjoint: the SCIDDICA-T gradient at 1024^2, T = 2000; "

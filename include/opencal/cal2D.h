@@ -257,6 +257,31 @@ int calSetElementaryProcessPure2D(struct CALModel2D* ca2D, CALCallbackFunc2D ele
 int calSetElementaryProcessReads2D(struct CALModel2D* ca2D, CALCallbackFunc2D elementary_process,
                                    const void* const* substates, int count);
 
+/* Declares that an elementary process returns at once, writing and
+ * changing nothing, on every cell where the current value v of the real
+ * substate Q satisfies `v op value`: the early return its body starts with
+ * (SCIDDICA-T's flows process: `if (calGet2Dr(ca, Q.h, i, j) <= P.epsilon)
+ * return;` is CAL_GUARD_LE, Q.h, P.epsilon).  Then, in a model without
+ * active cells, the process kernel tests the guard for the 256 cells of a
+ * tile and runs the process only on those that pass, packed into
+ * consecutive threads, so that warps are not held by cells that return at
+ * once.  The comparison is the C one (a NaN passes every guard but
+ * CAL_GUARD_NE), so the results are those of the plain run whenever the
+ * declaration is true.  Not applied to processes whose reads are staged
+ * (calSetElementaryProcessReads2D).  `value` is taken at the call: declare
+ * again after changing the parameter it stands for.  op CAL_GUARD_NONE
+ * withdraws the declaration.  No counterpart in the reference (a
+ * performance declaration).  Returns a CALError code. */
+#define CAL_GUARD_NONE 0
+#define CAL_GUARD_LE 1 /* returns where v <= value */
+#define CAL_GUARD_LT 2 /* v < value */
+#define CAL_GUARD_GE 3 /* v >= value */
+#define CAL_GUARD_GT 4 /* v > value */
+#define CAL_GUARD_EQ 5 /* v == value */
+#define CAL_GUARD_NE 6 /* v != value */
+int calSetElementaryProcessGuard2Dr(struct CALModel2D* ca2D, CALCallbackFunc2D elementary_process,
+                                    struct CALSubstate2Dr* Q, int op, CALreal value);
+
 /* Registration of device elementary processes (used by
  * CAL_ELEMENTARY_PROCESS_2D; not called directly). */
 struct CALDevModel2D;

@@ -78,6 +78,11 @@ struct CALDevModel2D {
      * skips the other tiles and clears the bit of every tile where it
      * changed nothing */
     unsigned int* run;
+    /* guard of the process (calSetElementaryProcessGuard2Dr): it returns at
+     * once where the current layer of real slot guard_slot compares true
+     * with guard_value under guard_op; 0: none */
+    int guard_op, guard_slot;
+    double guard_value;
     /* TMA staging of the substates a process declared it reads
      * (calSetElementaryProcessReads2D); nstage == 0: none.  On every tile
      * that the process runs on (in toroidal grids only tiles off the grid's
@@ -114,6 +119,10 @@ static __shared__ unsigned char cal_flagchg2D;
 /* per block: the current tile is staged, its origin, the staging barrier */
 static __shared__ int cal_stage_on2D, cal_stage_i02D, cal_stage_j02D, cal_stage_pad2D, cal_stage_buf2D;
 static __shared__ __align__(8) unsigned long long cal_stage_bar2D[2];
+/* per block: the cells of the current tile that pass the process's guard
+ * (thread index in the tile: row * 32 + column) and each warp's count */
+static __shared__ unsigned char cal_gcell2D[CAL_EP_THREADS];
+static __shared__ int cal_gcount2D[CAL_EP_THREADS / 32];
 extern __shared__ __align__(128) unsigned char cal_stage_mem2D[];
 
 /* ---- TMA: mbarrier with a transaction count, tiled 2D loads, bounded wait */
@@ -370,7 +379,9 @@ template <void (*EP)(struct CALModel2D*, int, int), int NX, int MODE>
 __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_constant__ struct CALDevModel2D m)
 {
     /* MODE 0: tile by tile; 1: declared reads staged by TMA; 2: tile
-     * skipping, the block's run bits fetched 32 tiles at a time */
+     * skipping, the block's run bits fetched 32 tiles at a time; 3: a
+     * guarded process, the tile's passing cells packed into consecutive
+     * threads (with or without tile skipping) */
     constexpr bool STAGED = MODE == 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int t = threadIdx.x; t < 3 * CAL_MAX_SUBSTATES; t += blockDim.x) {
@@ -413,8 +424,48 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
             const unsigned tbit = 1u << (tile & 31);
             const int ty = tile / m.tiles_x;
             const int i = ty * CAL_TILE_H + warp, j = (tile - ty * m.tiles_x) * CAL_TILE_W + lane;
-            if (i < m.rows && j < m.cols)
+            if (MODE == 3) {
+                /* the cells that pass the guard, in tile order, onto threads
+                 * 0, 1, ... (the counting barrier comes first: the previous
+                 * tile's list is read until every thread has taken its cell) */
+                bool pass = false;
+                if (i < m.rows && j < m.cols) {
+                    const double v = ((const double*)m.cur[CAL_TYPE_R][m.guard_slot])[(long long)i * m.cols + j];
+                    const double w = m.guard_value;
+                    switch (m.guard_op) {
+                    case 1: pass = !(v <= w); break;
+                    case 2: pass = !(v < w); break;
+                    case 3: pass = !(v >= w); break;
+                    case 4: pass = !(v > w); break;
+                    case 5: pass = !(v == w); break;
+                    case 6: pass = !(v != w); break;
+                    default: pass = true; break;
+                    }
+                }
+                /* one barrier settles a tile where no cell or every cell
+                 * passes; the others are packed */
+                const int total = __syncthreads_count(pass);
+                if (total == CAL_EP_THREADS) {
+                    EP(ca, i, j);
+                } else if (total > 0) {
+                    const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                    if (lane == 0)
+                        cal_gcount2D[warp] = __popc(bal);
+                    __syncthreads();
+                    int off = 0;
+                    for (int w = 0; w < warp; w++)
+                        off += cal_gcount2D[w];
+                    if (pass)
+                        cal_gcell2D[off + __popc(bal & ((1u << lane) - 1u))] = (unsigned char)threadIdx.x;
+                    __syncthreads();
+                    if ((int)threadIdx.x < total) {
+                        const int q = cal_gcell2D[threadIdx.x];
+                        EP(ca, ty * CAL_TILE_H + (q >> 5), (tile - ty * m.tiles_x) * CAL_TILE_W + (q & 31));
+                    }
+                }
+            } else if (i < m.rows && j < m.cols) {
                 EP(ca, i, j);
+            }
             if (m.track) {
                 bool changed = false;
                 __syncwarp();
@@ -429,7 +480,7 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                     atomicAnd(&m.run[tile >> 5], ~tbit);
             }
         };
-        if (MODE == 2) {
+        if (MODE == 2 || (MODE == 3 && m.run)) {
             /* the block's tiles bid, bid + nblocks, ..., only those whose run
              * bit is set.  The bits of 32 of them come in one load per lane
              * and a ballot (the same in every warp: a bit is cleared only by
@@ -569,8 +620,9 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
 
 /* one kernel per common neighbourhood size (von Neumann 5, hexagonal 7,
  * Moore 9) and a generic one for the others, each plain, with the staging
- * of declared reads, and with tile skipping (the staging and skipping loops
- * cost registers and barriers that the plain loop does not pay) */
+ * of declared reads, with tile skipping, and for a guarded process (the
+ * staging, skipping and packing loops cost registers and barriers that the
+ * plain loop does not pay) */
 template <void (*EP)(struct CALModel2D*, int, int)>
 static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* stream)
 {
@@ -584,6 +636,13 @@ static int cal_launch_ep2D(const struct CALDevModel2D* m, int gx, int gy, void* 
         case 7: cal_ep2D_kernel<EP, 7, 1><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
         case 9: cal_ep2D_kernel<EP, 9, 1><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
         default: cal_ep2D_kernel<EP, 0, 1><<<grid, CAL_EP_THREADS, smem, st>>>(*m); break;
+        }
+    } else if (m->guard_op) {
+        switch (m->model.sizeof_X) {
+        case 5: cal_ep2D_kernel<EP, 5, 3><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 7: cal_ep2D_kernel<EP, 7, 3><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        case 9: cal_ep2D_kernel<EP, 9, 3><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
+        default: cal_ep2D_kernel<EP, 0, 3><<<grid, CAL_EP_THREADS, 0, st>>>(*m); break;
         }
     } else if (m->run) {
         switch (m->model.sizeof_X) {

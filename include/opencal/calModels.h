@@ -62,6 +62,11 @@ int cal_sciddicaT_set_pure(int on);
  * outflows), so that their kernels stage those substates by TMA; 0
  * (default): global reads */
 int cal_sciddicaT_set_staged(int on);
+/* 1: models created afterwards (processes mode) declare the flows
+ * process's early return on cells with h <= epsilon
+ * (calSetElementaryProcessGuard2Dr), so that its kernel runs it on each
+ * tile's wet cells packed into consecutive threads; 0 (default): off */
+int cal_sciddicaT_set_guard(int on);
 /* launch grids of the split step's kernels: k1_blocks and k2_blocks
  * 256-thread blocks of the outflow and the update kernel (0 = the defaults
  * 608 / 608) */

@@ -495,8 +495,12 @@ static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned
     for (int t = 0; t < 3; t++)
         for (int s = 0; s < CAL_MAX_SUBSTATES; s++)
             d.stage_of[t][s] = -1;
-    if (b >= 0)
+    if (b >= 0) {
         stage_reads(ca, b, &d);
+        d.guard_op = ca->gpu->guard_op[b];
+        d.guard_slot = ca->gpu->guard_slot[b];
+        d.guard_value = ca->gpu->guard_value[b];
+    }
     if (!d.nstage)
         for (int t = 0; t < 3; t++)
             for (int s = 0; s < CAL_MAX_SUBSTATES; s++)
@@ -649,6 +653,40 @@ extern "C" int calSetElementaryProcessReads2D(struct CALModel2D* ca, CALCallback
         ca->gpu->read_s[b][k] = ss[k];
     }
     g.inval_epoch++; /* a recorded step holds the old launch */
+    return CAL_SUCCESS;
+}
+
+extern "C" int calSetElementaryProcessGuard2Dr(struct CALModel2D* ca, CALCallbackFunc2D ep, struct CALSubstate2Dr* Q,
+                                               int op, CALreal value)
+{
+    if (!ca || !ca->gpu || op < CAL_GUARD_NONE || op > CAL_GUARD_NE || (op != CAL_GUARD_NONE && !Q)) {
+        cal::set_error(CAL_ERROR_INVALID_ARGUMENT, "calSetElementaryProcessGuard2Dr: bad arguments");
+        return CAL_ERROR_INVALID_ARGUMENT;
+    }
+    int b = -1;
+    for (int k = 0; k < ca->num_of_elementary_processes; k++)
+        if (ca->elementary_processes[k] == ep)
+            b = k;
+    if (b < 0) {
+        cal::set_error(CAL_ERROR_INVALID_ARGUMENT,
+                       "calSetElementaryProcessGuard2Dr: not a process added with calAddElementaryProcess2D");
+        return CAL_ERROR_INVALID_ARGUMENT;
+    }
+    int slot = 0;
+    if (op != CAL_GUARD_NONE) {
+        CalGrid& g = G(ca);
+        const uintptr_t h = (uintptr_t)Q, p0 = (uintptr_t)g.pool[CAL_TYPE_R];
+        if (!(h >= p0 && h < p0 + 32u * CAL_MAX_SUBSTATES_CORE && ((h - p0) & 31u) == 0 &&
+              (int)((h - p0) >> 5) < g.nslot[CAL_TYPE_R] && g.sub[CAL_TYPE_R][(h - p0) >> 5].used)) {
+            cal::set_error(CAL_ERROR_INVALID_ARGUMENT, "calSetElementaryProcessGuard2Dr: not a real substate of this model");
+            return CAL_ERROR_INVALID_ARGUMENT;
+        }
+        slot = (int)((h - p0) >> 5);
+    }
+    ca->gpu->guard_op[b] = op;
+    ca->gpu->guard_slot[b] = slot;
+    ca->gpu->guard_value[b] = value;
+    G(ca).inval_epoch++; /* a recorded step holds the old launch */
     return CAL_SUCCESS;
 }
 

@@ -16,6 +16,10 @@ struct CALGpuModel2D {
     bool pure[CAL_MAX_ELEMENTARY_PROCESSES] = {}; /* calSetElementaryProcessPure2D */
     /* calSetElementaryProcessReads2D: the substates (type, slot) each
      * process reads, staged into shared memory by TMA */
+    /* calSetElementaryProcessGuard2Dr: CAL_GUARD_* and the real slot / value */
+    int guard_op[CAL_MAX_ELEMENTARY_PROCESSES] = {};
+    int guard_slot[CAL_MAX_ELEMENTARY_PROCESSES] = {};
+    double guard_value[CAL_MAX_ELEMENTARY_PROCESSES] = {};
     int nreads[CAL_MAX_ELEMENTARY_PROCESSES] = {};
     int read_t[CAL_MAX_ELEMENTARY_PROCESSES][CAL_MAX_STAGED] = {};
     int read_s[CAL_MAX_ELEMENTARY_PROCESSES][CAL_MAX_STAGED] = {};

@@ -2055,6 +2055,7 @@ static void sciddicaT_simulation_init_fused(struct CALModel2D* sciddicaT)
  * program as it stands). */
 static int g_sdt_pure = 0;
 static int g_sdt_staged = 0;
+static int g_sdt_guard = 0;
 
 /* the declarations cal_sciddicaT_set_pure / _set_staged asked for; called
  * once the processes and the substates exist */
@@ -2070,11 +2071,24 @@ static void sciddicaT_declare_pure(struct CALModel2D* ca)
         calSetElementaryProcessReads2D(ca, sciddicaT_flows_computation, flows_reads, 2);
         calSetElementaryProcessReads2D(ca, sciddicaT_width_update, width_reads, 5);
     }
+    /* the flows process starts with `if (h <= epsilon) return;` */
+    if (g_sdt_guard)
+        calSetElementaryProcessGuard2Dr(ca, sciddicaT_flows_computation, Q.h, CAL_GUARD_LE, P.epsilon);
 }
 
 extern "C" int cal_sciddicaT_set_pure(int on)
 {
     g_sdt_pure = on != 0;
+    return 0;
+}
+
+/* 1: models created afterwards (processes mode) declare the flows
+ * process's early return on dry cells (calSetElementaryProcessGuard2Dr), so
+ * that its kernel runs it on the wet cells of each tile packed into
+ * consecutive threads; 0 (default): every cell's thread runs it */
+extern "C" int cal_sciddicaT_set_guard(int on)
+{
+    g_sdt_guard = on != 0;
     return 0;
 }
 
@@ -2437,6 +2451,8 @@ extern "C" int cal_sciddicaT_set_params(void* handle, double p_r, double p_eps)
     SdtSession* s = (SdtSession*)handle;
     P.r = p_r;
     P.epsilon = p_eps;
+    if (s->mode == SDT_MODE_PROCESSES)
+        sciddicaT_declare_pure(s->ca); /* the guard holds epsilon's value */
     calRunSetGraph2D(s->run, CAL_FALSE);
     return calGetLastError();
 }

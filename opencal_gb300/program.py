@@ -88,6 +88,7 @@ def capi() -> C.CDLL:
         "calAddElementaryProcess2D": ([vp, vp], vp),
         "calSetElementaryProcessPure2D": ([vp, vp, C.c_byte], i),
         "calSetElementaryProcessReads2D": ([vp, vp, vp, i], i),
+        "calSetElementaryProcessGuard2Dr": ([vp, vp, vp, i, C.c_double], i),
         "calApplyElementaryProcess2D": ([vp, vp], None),
         "calUpdate2D": ([vp], None),
         "calAddActiveCell2D": ([vp, i, i], None),
@@ -348,6 +349,18 @@ class Model2D:
         arr = (C.c_void_p * max(len(subs), 1))(*[h.ptr for h in subs])
         if self._c.calSetElementaryProcessReads2D(self, process, arr, len(subs)):
             _raise_on_error("calSetElementaryProcessReads2D")
+
+    GUARD_OPS = {"<=": 1, "<": 2, ">=": 3, ">": 4, "==": 5, "!=": 6}
+
+    def set_guard(self, process: int, sub: Substate, op: str, value: float) -> None:
+        """calSetElementaryProcessGuard2Dr: the process returns at once,
+        changing nothing, where the real substate's current value v
+        satisfies ``v op value`` (op one of <=, <, >=, >, ==, !=; None
+        withdraws the declaration); the kernel then runs it on each tile's
+        other cells packed into consecutive threads."""
+        code = 0 if op is None else self.GUARD_OPS[op]
+        if self._c.calSetElementaryProcessGuard2Dr(self, process, sub, code, float(value)):
+            _raise_on_error("calSetElementaryProcessGuard2Dr")
 
     def apply(self, process: int) -> None:
         """calApplyElementaryProcess2D: one process over the grid now (then

@@ -213,11 +213,13 @@ def test_life_from_python_stop_conditions(gpu):
 
 
 @pytest.mark.gpu
-def test_sciddicaT_from_python_reproduces_shipped_golden(gpu):
+@pytest.mark.parametrize("declared", [False, True], ids=["as_written", "pure+guard"])
+def test_sciddicaT_from_python_reproduces_shipped_golden(gpu, declared):
     """The reference's SCIDDICA-T example written in Python (processes as
     bodies, init and steering as Python callbacks) on its shipped 610 x 496
     data: 4000 steps, toroidal, the final h printed %.9f is the shipped
-    golden byte for byte."""
+    golden byte for byte; also with both processes declared pure and the
+    flows process's early return (h <= epsilon) declared as its guard."""
     from opencal_gb300 import program as P
     g = np.load(os.path.join(GOLDEN, "sciddicaT_610x496.npz"))
     meta = json.load(open(os.path.join(GOLDEN, "manifest.json")))["sciddicaT_610x496"]
@@ -229,6 +231,13 @@ def test_sciddicaT_from_python_reproduces_shipped_golden(gpu):
     lib.bind(**subs)
     model.add_process(lib.process("pysdt_flows"))
     model.add_process(lib.process("pysdt_width"))
+    if declared:
+        model.set_pure(lib.process("pysdt_flows"))
+        model.set_pure(lib.process("pysdt_width"))
+        model.set_guard(lib.process("pysdt_flows"), subs["h"], "<=", meta["p_eps"])
+        with pytest.raises(P.CALError):  # not a substate handle of the model
+            model.set_guard(lib.process("pysdt_flows"), P.Substate(subs["h"].ptr + 1, "r"), "<=", 0.0)
+        P.core().calClearError()
     model.load(subs["z"], g["z"])
     model.load(subs["h"], g["h0"])
 

@@ -14,6 +14,11 @@ counterpart: the compaction after a process that changed no flag keeps the
 list (a session reset that rewrites the flags through their device pointer
 must still be seen).
 
+Guards (calSetElementaryProcessGuard2Dr): SCIDDICA-T's flows process with
+its early return on dry cells declared, alone and with the other
+declarations, against the same oracle runs and the shipped golden; a guard
+on a substate of another type is refused.
+
 TMA staging of the substates a process declared it reads
 (calSetElementaryProcessReads2D): SCIDDICA-T (doubles, von Neumann, flat and
 toroidal: border tiles of toroidal grids read global memory), Life (bytes,
@@ -33,17 +38,20 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-@pytest.fixture(params=[(1, 0), (0, 1), (1, 1)], ids=["pure", "staged", "pure+staged"])
+@pytest.fixture(params=[(1, 0, 0), (0, 1, 0), (1, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1)],
+                ids=["pure", "staged", "pure+staged", "guard", "pure+guard", "pure+staged+guard"])
 def pure_sdt(request):
     import opencal_gb300 as cal
     cal.build()
     m = cal.models()
-    pure, staged = request.param
+    pure, staged, guard = request.param
     m.cal_sciddicaT_set_pure(pure)
     m.cal_sciddicaT_set_staged(staged)
+    m.cal_sciddicaT_set_guard(guard)
     yield cal
     m.cal_sciddicaT_set_pure(0)
     m.cal_sciddicaT_set_staged(0)
+    m.cal_sciddicaT_set_guard(0)
 
 
 @pytest.mark.parametrize("rows,cols,seed,steps,tor", [(160, 144, 11, 60, 0), (203, 177, 13, 90, 1),
