@@ -78,6 +78,14 @@ struct CALDevModel2D {
      * skips the other tiles and clears the bit of every tile where it
      * changed nothing */
     unsigned int* run;
+    /* with quiet (skipping launches whose busy tiles are dealt over the
+     * blocks): run stays unchanged during the launch, every block computes
+     * the same compaction of it, block b takes busy tiles b, b + nblocks, ...
+     * (the lowest blocks, which the hardware places on different SMs, get
+     * the work), the tiles where the process changed nothing are gathered in
+     * quiet and the last block to finish (ticket) clears them from run */
+    unsigned int* quiet;
+    unsigned int* ticket;
     /* guard of the process (calSetElementaryProcessGuard2Dr): it returns at
      * once where the current layer of real slot guard_slot compares true
      * with guard_value under guard_op; 0: none */
@@ -123,6 +131,10 @@ static __shared__ __align__(8) unsigned long long cal_stage_bar2D[2];
  * (thread index in the tile: row * 32 + column) and each warp's count */
 static __shared__ unsigned char cal_gcell2D[CAL_EP_THREADS];
 static __shared__ int cal_gcount2D[CAL_EP_THREADS / 32];
+/* per block: the busy tiles dealt to it (skipping launches with quiet) */
+#define CAL_DEAL_MAX 64
+static __shared__ int cal_dtile2D[CAL_DEAL_MAX];
+static __shared__ int cal_dlast2D;
 extern __shared__ __align__(128) unsigned char cal_stage_mem2D[];
 
 /* ---- TMA: mbarrier with a transaction count, tiled 2D loads, bounded wait */
@@ -476,11 +488,60 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                         atomicOr(&m.chg[(long long)t * m.tile_words + (tile >> 5)], tbit);
                     }
                 __syncwarp();
-                if (m.run && !__syncthreads_or(changed) && threadIdx.x == 0)
-                    atomicAnd(&m.run[tile >> 5], ~tbit);
+                if (m.run && !__syncthreads_or(changed) && threadIdx.x == 0) {
+                    if (m.quiet)
+                        atomicOr(&m.quiet[tile >> 5], tbit);
+                    else
+                        atomicAnd(&m.run[tile >> 5], ~tbit);
+                }
             }
         };
-        if (MODE == 2 || (MODE == 3 && m.run)) {
+        if ((MODE == 2 || MODE == 3) && m.run && m.quiet) {
+            /* every block ranks the busy tiles (the set bits of run, in tile
+             * order: each thread counts a run of words, then a block scan)
+             * and takes ranks bid, bid + nblocks, ... (at most CAL_DEAL_MAX:
+             * the host deals only when the tiles allow it) */
+            const int W = m.tile_words;
+            const int per = (W + CAL_EP_THREADS - 1) / CAL_EP_THREADS;
+            const int w0 = (int)threadIdx.x * per, w1 = min(W, w0 + per);
+            int cnt = 0;
+            for (int w = w0; w < w1; w++)
+                cnt += __popc(m.run[w]);
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                    incl += y;
+            }
+            if (lane == 31)
+                cal_gcount2D[warp] = incl;
+            __syncthreads();
+            int pre = incl - cnt, total = 0;
+            for (int w = 0; w < CAL_EP_THREADS / 32; w++) {
+                const int v = cal_gcount2D[w];
+                pre += w < warp ? v : 0;
+                total += v;
+            }
+            if (cnt) {
+                int r = bid >= pre ? bid : bid + (pre - bid + nblocks - 1) / nblocks * nblocks;
+                int seen = pre;
+                for (int w = w0; w < w1 && r < pre + cnt; w++) {
+                    const unsigned bits = m.run[w];
+                    const int n = __popc(bits);
+                    for (; r < seen + n; r += nblocks) {
+                        unsigned b = bits;
+                        for (int k = r - seen; k > 0; k--)
+                            b &= b - 1; /* drop the lowest set bits below rank r */
+                        cal_dtile2D[(r - bid) / nblocks] = w * 32 + __ffs(b) - 1;
+                    }
+                    seen += n;
+                }
+            }
+            __syncthreads();
+            const int ntodo = total > bid ? (total - bid + nblocks - 1) / nblocks : 0;
+            for (int k = 0; k < ntodo; k++)
+                run_tile(cal_dtile2D[k]);
+        } else if (MODE == 2 || (MODE == 3 && m.run)) {
             /* the block's tiles bid, bid + nblocks, ..., only those whose run
              * bit is set.  The bits of 32 of them come in one load per lane
              * and a ballot (the same in every warp: a bit is cleared only by
@@ -616,6 +677,26 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     }
     if (threadIdx.x == 0 && cal_flagchg2D && m.flags_dirty)
         *m.flags_dirty = 1;
+    if ((MODE == 2 || MODE == 3) && m.run && m.quiet && !listed) {
+        /* the last block to finish clears the quiet tiles from run */
+        if (threadIdx.x == 0) {
+            __threadfence();
+            cal_dlast2D = atomicAdd(m.ticket, 1u) == (unsigned)(gridDim.x * gridDim.y) - 1u;
+        }
+        __syncthreads();
+        if (cal_dlast2D) {
+            __threadfence();
+            for (int w = threadIdx.x; w < m.tile_words; w += blockDim.x) {
+                const unsigned q = __ldcg(m.quiet + w);
+                if (q) {
+                    m.run[w] &= ~q;
+                    m.quiet[w] = 0;
+                }
+            }
+            if (threadIdx.x == 0)
+                *m.ticket = 0;
+        }
+    }
 }
 
 /* one kernel per common neighbourhood size (von Neumann 5, hexagonal 7,

@@ -514,6 +514,14 @@ static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned
         gx = 1;
         gy = 152 * 4;
     }
+    /* a skipping launch deals its busy tiles over the blocks when every
+     * block can rank the bitmap (at most 16 words a thread) and keep its
+     * share (at most CAL_DEAL_MAX tiles) */
+    if (run && !d.nstage && g.d_quiet && g.tile_words <= 16 * CAL_EP_THREADS &&
+        (long long)g.tiles_x * g.tiles_y <= (long long)CAL_DEAL_MAX * gx * gy) {
+        d.quiet = g.d_quiet;
+        d.ticket = g.d_ticket;
+    }
     int rc = launch(&d, gx, gy, (void*)g.stream);
     if (rc != 0) {
         cal::cuda_ok((cudaError_t)rc, "elementary process launch");

@@ -632,8 +632,12 @@ bool CalGrid::init(int dim_, int rows_, int cols_, int slices_, int toroidal_, i
             !cuda_ok(cudaMemsetAsync(d_untracked, 0, 4 * sizeof(unsigned), stream), "memset change bitmaps") ||
             !cuda_ok(cudaMalloc(&d_run, (size_t)CAL_MAX_PROCESSES_CORE * tile_words * sizeof(unsigned)),
                      "cudaMalloc skipping bitmaps") ||
+            !cuda_ok(cudaMalloc(&d_quiet, (size_t)(tile_words + 32) * sizeof(unsigned)), "cudaMalloc skipping bitmaps") ||
+            !cuda_ok(cudaMemsetAsync(d_quiet, 0, (size_t)(tile_words + 32) * sizeof(unsigned), stream),
+                     "memset skipping bitmaps") ||
             !arm_runs())
             return false;
+        d_ticket = d_quiet + tile_words + 16; /* a line of its own past the bitmap */
     }
     if (active) {
         scratch_ints = compact_scratch_ints(ncells);
@@ -683,6 +687,7 @@ void CalGrid::destroy()
     cudaFree(d_dev);
     cudaFree(d_untracked);
     cudaFree(d_run);
+    cudaFree(d_quiet);
     cudaFree(d_step);
     cudaFree(d_reduce_partial);
     cudaFree(d_reduce_result);

@@ -130,6 +130,13 @@ struct CalGrid {
     unsigned* d_run = nullptr;
     int nrun = 0;
     long run_epoch = -1;
+    /* a skipping launch that deals its busy tiles over the blocks keeps the
+     * bitmap unchanged while it runs: the tiles where the process changed
+     * nothing are gathered in d_quiet (tile_words words, zero between
+     * launches) and cleared from the bitmap by the launch's last block
+     * (d_ticket counts the finished blocks, zero between launches) */
+    unsigned* d_quiet = nullptr;
+    unsigned* d_ticket = nullptr;
     int* d_step = nullptr;       /* step counter of a device-driven run */
     void* d_reduce_partial = nullptr; /* reduction scratch (per-block partials) */
     void* d_reduce_result = nullptr;  /* reduction result read back by the host */
