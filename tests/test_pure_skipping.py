@@ -123,6 +123,39 @@ def test_life_pure_from_python(shape, tor, graph, staged):
     assert np.array_equal(got, oracle.life2d(s0, 60, toroidal=tor))
 
 
+def test_life_pure_grid_too_large_to_deal():
+    """6144 x 6400 cells: 200 x 768 tiles (4800 bitmap words, 63 tiles per
+    block of the launch) is past what a skipping launch deals over its
+    blocks (4096 words), so the blocks walk their own tiles instead; three
+    sparse patches, 12 generations, against the oracle."""
+    import oracle
+    import opencal_gb300 as cal
+    from opencal_gb300 import program as P
+    cal.build()
+    oracle.build()
+    rows, cols = 6144, 6400
+    rng = np.random.default_rng(7)
+    s0 = np.zeros((rows, cols), np.uint8)
+    for (i, j) in ((40, 60), (3000, 3100), (6100, 6350)):
+        s0[i:i + 30, j:j + 40] = rng.random((30, 40)) < 0.4
+    lib = P.Program("pylife_large").substates(alive="b").process("pylife_large_rule", LIFE_BODY).build()
+    model = P.Model2D(rows, cols, P.CAL_MOORE_NEIGHBORHOOD_2D, P.CAL_SPACE_TOROIDAL)
+    alive = model.add_substate("b")
+    lib.bind(alive=alive)
+    rule = lib.process("pylife_large_rule")
+    model.add_process(rule)
+    model.set_pure(rule)
+    model.load(alive, s0.astype(np.int8))
+    run = P.Run2D(model, 1, 12, graph=False)
+    try:
+        run.run()
+        got = model.read(alive).astype(np.uint8)
+    finally:
+        run.close()
+        model.close()
+    assert np.array_equal(got, oracle.life2d(s0, 12, toroidal=True))
+
+
 def test_far_reaching_custom_neighbourhood_is_not_skipped():
     """A custom neighbourhood 12 rows tall reaches past the adjacent tile:
     the declaration is accepted but tiles are not skipped, and the run
