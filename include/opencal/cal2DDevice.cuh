@@ -428,6 +428,52 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         }
     } else {
         const int ntiles = m.tiles_x * m.tiles_y;
+        /* skipping launches with quiet: every block ranks the busy tiles
+         * (the set bits of run, in tile order: each thread counts a run of
+         * words, then a block scan) and takes ranks bid, bid + nblocks, ...
+         * into cal_dtile2D (at most CAL_DEAL_MAX: the host deals only when
+         * the tiles allow it); -1 when the launch does not deal */
+        auto deal_tiles = [&]() -> int {
+            const int W = m.tile_words;
+            const int per = (W + CAL_EP_THREADS - 1) / CAL_EP_THREADS;
+            const int w0 = (int)threadIdx.x * per, w1 = min(W, w0 + per);
+            int cnt = 0;
+            for (int w = w0; w < w1; w++)
+                cnt += __popc(m.run[w]);
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                    incl += y;
+            }
+            if (lane == 31)
+                cal_gcount2D[warp] = incl;
+            __syncthreads();
+            int pre = incl - cnt, total = 0;
+            for (int w = 0; w < CAL_EP_THREADS / 32; w++) {
+                const int v = cal_gcount2D[w];
+                pre += w < warp ? v : 0;
+                total += v;
+            }
+            if (cnt) {
+                int r = bid >= pre ? bid : bid + (pre - bid + nblocks - 1) / nblocks * nblocks;
+                int seen = pre;
+                for (int w = w0; w < w1 && r < pre + cnt; w++) {
+                    const unsigned bits = m.run[w];
+                    const int n = __popc(bits);
+                    for (; r < seen + n; r += nblocks) {
+                        unsigned b = bits;
+                        for (int k = r - seen; k > 0; k--)
+                            b &= b - 1; /* drop the lowest set bits below rank r */
+                        cal_dtile2D[(r - bid) / nblocks] = w * 32 + __ffs(b) - 1;
+                    }
+                    seen += n;
+                }
+            }
+            __syncthreads();
+            return total > bid ? (total - bid + nblocks - 1) / nblocks : 0;
+        };
+        const int ntodo = (MODE != 0 && m.run && m.quiet) ? deal_tiles() : -1;
         if (!STAGED) {
         /* one tile, one cell per thread; with change tracking each warp
          * records which substates its row changed, and with tile skipping
@@ -496,49 +542,7 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                 }
             }
         };
-        if ((MODE == 2 || MODE == 3) && m.run && m.quiet) {
-            /* every block ranks the busy tiles (the set bits of run, in tile
-             * order: each thread counts a run of words, then a block scan)
-             * and takes ranks bid, bid + nblocks, ... (at most CAL_DEAL_MAX:
-             * the host deals only when the tiles allow it) */
-            const int W = m.tile_words;
-            const int per = (W + CAL_EP_THREADS - 1) / CAL_EP_THREADS;
-            const int w0 = (int)threadIdx.x * per, w1 = min(W, w0 + per);
-            int cnt = 0;
-            for (int w = w0; w < w1; w++)
-                cnt += __popc(m.run[w]);
-            int incl = cnt;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o)
-                    incl += y;
-            }
-            if (lane == 31)
-                cal_gcount2D[warp] = incl;
-            __syncthreads();
-            int pre = incl - cnt, total = 0;
-            for (int w = 0; w < CAL_EP_THREADS / 32; w++) {
-                const int v = cal_gcount2D[w];
-                pre += w < warp ? v : 0;
-                total += v;
-            }
-            if (cnt) {
-                int r = bid >= pre ? bid : bid + (pre - bid + nblocks - 1) / nblocks * nblocks;
-                int seen = pre;
-                for (int w = w0; w < w1 && r < pre + cnt; w++) {
-                    const unsigned bits = m.run[w];
-                    const int n = __popc(bits);
-                    for (; r < seen + n; r += nblocks) {
-                        unsigned b = bits;
-                        for (int k = r - seen; k > 0; k--)
-                            b &= b - 1; /* drop the lowest set bits below rank r */
-                        cal_dtile2D[(r - bid) / nblocks] = w * 32 + __ffs(b) - 1;
-                    }
-                    seen += n;
-                }
-            }
-            __syncthreads();
-            const int ntodo = total > bid ? (total - bid + nblocks - 1) / nblocks : 0;
+        if (ntodo >= 0) {
             for (int k = 0; k < ntodo; k++)
                 run_tile(cal_dtile2D[k]);
         } else if (MODE == 2 || (MODE == 3 && m.run)) {
@@ -563,12 +567,16 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                     run_tile(tile);
         }
         } else {
-        /* staged: the block's tiles bid, bid + nblocks, ...; with tile skipping only
-         * those whose bit is set (a bit is cleared only by the block that
-         * owns the tile, after processing it, so every thread finds the same
-         * next tile).  With staging, the next tile's boxes are loaded into the
-         * other of two buffers while the current tile computes. */
-        auto next_tile = [&](int from) {
+        /* staged: the tiles dealt to the block, or the block's tiles bid,
+         * bid + nblocks, ... (with tile skipping only those whose bit is set:
+         * a bit is cleared only by the block that owns the tile, after
+         * processing it, so every thread finds the same next tile).  With
+         * staging, the next tile's boxes are loaded into the other of two
+         * buffers while the current tile computes.  next_tile(from, k): the
+         * tile after the k-th of the block. */
+        auto next_tile = [&](int from, int k) {
+            if (ntodo >= 0)
+                return k < ntodo ? cal_dtile2D[k] : ntiles;
             int t = from;
             while (t < ntiles && m.run && !(m.run[t >> 5] & (1u << (t & 31))))
                 t += nblocks;
@@ -597,7 +605,8 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         uint32_t phases = 0;  /* bit b: parity of buffer b's next phase */
         uint32_t pending = 0; /* bit b: copies issued into buffer b and not yet waited for */
         int buf = 0;
-        int tile = next_tile(bid);
+        int nk = 0; /* the block's tiles taken so far */
+        int tile = next_tile(bid, nk++);
         if (nstage && tile < ntiles && staged_tile(tile)) {
             if (threadIdx.x == 0)
                 issue(tile, 0);
@@ -605,7 +614,7 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         }
         while (tile < ntiles) {
             const unsigned tbit = 1u << (tile & 31);
-            const int nxt = next_tile(tile + nblocks);
+            const int nxt = next_tile(tile + nblocks, nk++);
             const int ty = tile / m.tiles_x, tx = tile - ty * m.tiles_x;
             const int i = ty * CAL_TILE_H + warp, j = tx * CAL_TILE_W + lane;
             if (nstage) {
@@ -656,8 +665,12 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
                         atomicOr(&m.chg[(long long)t * m.tile_words + (tile >> 5)], tbit);
                     }
                 __syncwarp();
-                if (m.run && !__syncthreads_or(changed) && threadIdx.x == 0)
-                    atomicAnd(&m.run[tile >> 5], ~tbit);
+                if (m.run && !__syncthreads_or(changed) && threadIdx.x == 0) {
+                    if (m.quiet)
+                        atomicOr(&m.quiet[tile >> 5], tbit);
+                    else
+                        atomicAnd(&m.run[tile >> 5], ~tbit);
+                }
             }
             tile = nxt;
             buf ^= 1;
@@ -677,7 +690,7 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
     }
     if (threadIdx.x == 0 && cal_flagchg2D && m.flags_dirty)
         *m.flags_dirty = 1;
-    if ((MODE == 2 || MODE == 3) && m.run && m.quiet && !listed) {
+    if (MODE != 0 && m.run && m.quiet && !listed) {
         /* the last block to finish clears the quiet tiles from run */
         if (threadIdx.x == 0) {
             __threadfence();

@@ -517,7 +517,7 @@ static void apply_launch(struct CALModel2D* ca, CALLaunchFunc2D launch, unsigned
     /* a skipping launch deals its busy tiles over the blocks when every
      * block can rank the bitmap (at most 16 words a thread) and keep its
      * share (at most CAL_DEAL_MAX tiles) */
-    if (run && !d.nstage && g.d_quiet && g.tile_words <= 16 * CAL_EP_THREADS &&
+    if (run && g.d_quiet && g.tile_words <= 16 * CAL_EP_THREADS &&
         (long long)g.tiles_x * g.tiles_y <= (long long)CAL_DEAL_MAX * gx * gy) {
         d.quiet = g.d_quiet;
         d.ticket = g.d_ticket;
