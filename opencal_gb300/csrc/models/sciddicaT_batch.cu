@@ -399,19 +399,27 @@ static __device__ __forceinline__ bool nbr(const Inst& I, int i, int j, int n, l
 }
 
 /* block sum, result in thread 0; every thread calls it */
-static __device__ __forceinline__ double block_sum(double v, double* s_red)
+/* the block's sums of a and b, in thread 0 (warp shuffles, then thread 0
+ * over the warps in order); one barrier: s_red is next written after the
+ * barriers that open the block's next tile */
+static __device__ __forceinline__ void block_sum2(double& a, double& b, double2* s_red)
 {
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_down_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
     if ((threadIdx.x & 31) == 0)
-        s_red[threadIdx.x >> 5] = v;
+        s_red[threadIdx.x >> 5] = make_double2(a, b);
     __syncthreads();
-    double s = 0.0;
-    if (threadIdx.x == 0)
-        for (int q = 0; q < T / 32; q++)
-            s += s_red[q];
-    __syncthreads();
-    return s;
+    if (threadIdx.x == 0) {
+        double sa = 0.0, sb = 0.0;
+        for (int q = 0; q < T / 32; q++) {
+            sa += s_red[q].x;
+            sb += s_red[q].y;
+        }
+        a = sa;
+        b = sb;
+    }
 }
 
 /* adjoint coefficients g, gz, w of the wet cells of the listed tiles (the
@@ -432,7 +440,7 @@ __global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, con
                                               double* __restrict__ grad, int B, const unsigned char* __restrict__ etape,
                                               const long long* __restrict__ toff, long long tape_cap)
 {
-    __shared__ double s_red[T / 32];
+    __shared__ double2 s_red2[T / 32];
     __shared__ unsigned short s_wet[TW * TH];
     __shared__ int s_n;
     const int n = *count;
@@ -516,8 +524,8 @@ __global__ void __launch_bounds__(T) k_coeffs(const Inst* __restrict__ inst, con
             for (int d = 0; d < 4; d++)
                 w[d * N + c] = wc[d];
         }
-        const double sr = block_sum(pr, s_red);
-        const double se = block_sum(pe, s_red);
+        block_sum2(pr, pe, s_red2);
+        const double sr = pr, se = pe;
         if (threadIdx.x == 0) {
             if (sr != 0.0)
                 atomicAdd(grad + bi, sr);
