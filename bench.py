@@ -51,9 +51,9 @@ CA_STEPS = 4000
 SEED = 2
 P_R, P_EPS = 0.5, 0.001
 BYTES_PER_CELL_UPDATE = 24  # z read + h read + h write (FP64)
-# FP64 operations of one wet cell-update (SURVEY scope table: 5 + up to 5
-# minimisation iterations x (<= 5 adds + 1 division) + 8 of the update; an
-# upper estimate of the reference's own operation count per wet cell)
+# FP64 operations of one wet cell-update (5 + up to 5 minimisation
+# iterations x (<= 5 adds + 1 division) + 8 of the update; an upper
+# estimate of the reference's own operation count per wet cell)
 FP64_OPS_PER_WET_CELL = 70
 REF_SAMPLE_STEPS = 64
 SERIAL_SAMPLE_STEPS = 8  # the 1-core serial comparator's sample (CA steps of the full grid)
