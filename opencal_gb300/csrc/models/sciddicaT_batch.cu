@@ -558,22 +558,36 @@ __global__ void __launch_bounds__(T) k_gather(const Inst* __restrict__ inst, con
             const long long c = I.off + (long long)i * I.cols + j;
             double from_nb = 0.0;
             long long cn = 0;
+            bool touched = false; /* the cell or a neighbour is wet */
             /* x is neighbour opp(d) of its neighbour d: north<->south, west<->east */
-            if (nbr(I, i, j, 1, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+            if (nbr(I, i, j, 1, &cn) && sdt::is_wet(h[cn], I.eps_bits)) {
                 from_nb += w[3 * N + cn];
-            if (nbr(I, i, j, 2, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+                touched = true;
+            }
+            if (nbr(I, i, j, 2, &cn) && sdt::is_wet(h[cn], I.eps_bits)) {
                 from_nb += w[2 * N + cn];
-            if (nbr(I, i, j, 3, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+                touched = true;
+            }
+            if (nbr(I, i, j, 3, &cn) && sdt::is_wet(h[cn], I.eps_bits)) {
                 from_nb += w[1 * N + cn];
-            if (nbr(I, i, j, 4, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+                touched = true;
+            }
+            if (nbr(I, i, j, 4, &cn) && sdt::is_wet(h[cn], I.eps_bits)) {
                 from_nb += w[cn];
+                touched = true;
+            }
             double gc = 0.0, gzc = 0.0;
             if (sdt::is_wet(h[c], I.eps_bits)) {
                 gc = g[c];
                 gzc = gz[c];
+                touched = true;
             }
-            lam[c] = lam[c] + gc + from_nb;
-            lamz[c] += gzc + from_nb;
+            /* elsewhere nothing is added: lambda stays (the arrays are far
+             * larger than L2, so the skipped read and write are DRAM bytes) */
+            if (touched) {
+                lam[c] = lam[c] + gc + from_nb;
+                lamz[c] += gzc + from_nb;
+            }
         }
     }
 }
