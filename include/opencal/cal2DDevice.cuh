@@ -476,8 +476,10 @@ __global__ void __launch_bounds__(CAL_EP_THREADS) cal_ep2D_kernel(const __grid_c
         const int ntodo = (MODE != 0 && m.run && m.quiet) ? deal_tiles() : -1;
         if (!STAGED) {
         /* one tile, one cell per thread; with change tracking each warp
-         * records which substates its row changed, and with tile skipping
-         * the tile's bit is cleared when the process changed nothing there */
+         * records which substates it changed in the tile, and with tile
+         * skipping a tile where the process changed nothing has its bit
+         * cleared (or, when the launch deals its tiles, gathered in quiet for
+         * the last block to clear) */
         auto run_tile = [&](int tile) {
             const unsigned tbit = 1u << (tile & 31);
             const int ty = tile / m.tiles_x;
