@@ -398,7 +398,6 @@ static __device__ __forceinline__ bool nbr(const Inst& I, int i, int j, int n, l
     return true;
 }
 
-/* block sum, result in thread 0; every thread calls it */
 /* the block's sums of a and b, in thread 0 (warp shuffles, then thread 0
  * over the warps in order); one barrier: s_red is next written after the
  * barriers that open the block's next tile */
@@ -551,40 +550,51 @@ __global__ void __launch_bounds__(T) k_gather(const Inst* __restrict__ inst, con
         const Inst I = inst[tile_inst[t]];
         const int lt = t - I.tile0;
         const int ty = lt / I.tiles_x, tx = lt - ty * I.tiles_x;
-        for (int q0 = threadIdx.x; q0 < TW * TH; q0 += T) {
-            const int i = ty * TH + q0 / TW, j = tx * TW + q0 % TW;
-            if (i >= I.rows || j >= I.cols)
-                continue;
-            const long long c = I.off + (long long)i * I.cols + j;
-            double from_nb = 0.0;
-            long long cn = 0;
-            bool touched = false; /* the cell or a neighbour is wet */
-            /* x is neighbour opp(d) of its neighbour d: north<->south, west<->east */
-            if (nbr(I, i, j, 1, &cn) && sdt::is_wet(h[cn], I.eps_bits)) {
-                from_nb += w[3 * N + cn];
-                touched = true;
+        /* two cells a thread per pass, their loads issued together (the
+         * pass is bound by the latency of these loads); each cell's sums
+         * keep their order */
+        for (int q0 = threadIdx.x; q0 < TW * TH; q0 += 2 * T) {
+            /* first the wet flags of both cells and their neighbours (ten
+             * loads in flight), then the coefficients of the wet ones */
+            unsigned wet[2] = {0u, 0u}; /* bit d: neighbour d + 1; bit 4: the cell */
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int q = q0 + u * T;
+                const int i = ty * TH + q / TW, j = tx * TW + q % TW;
+                if (q < TW * TH && i < I.rows && j < I.cols) {
+                    long long cn = 0;
+#pragma unroll
+                    for (int d = 0; d < 4; d++)
+                        if (nbr(I, i, j, d + 1, &cn) && sdt::is_wet(h[cn], I.eps_bits))
+                            wet[u] |= 1u << d;
+                    if (sdt::is_wet(h[I.off + (long long)i * I.cols + j], I.eps_bits))
+                        wet[u] |= 16u;
+                }
             }
-            if (nbr(I, i, j, 2, &cn) && sdt::is_wet(h[cn], I.eps_bits)) {
-                from_nb += w[2 * N + cn];
-                touched = true;
-            }
-            if (nbr(I, i, j, 3, &cn) && sdt::is_wet(h[cn], I.eps_bits)) {
-                from_nb += w[1 * N + cn];
-                touched = true;
-            }
-            if (nbr(I, i, j, 4, &cn) && sdt::is_wet(h[cn], I.eps_bits)) {
-                from_nb += w[cn];
-                touched = true;
-            }
-            double gc = 0.0, gzc = 0.0;
-            if (sdt::is_wet(h[c], I.eps_bits)) {
-                gc = g[c];
-                gzc = gz[c];
-                touched = true;
-            }
-            /* elsewhere nothing is added: lambda stays (the arrays are far
-             * larger than L2, so the skipped read and write are DRAM bytes) */
-            if (touched) {
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                if (!wet[u])
+                    continue; /* nothing is added: lambda stays (the arrays are far
+                               * larger than L2, so the skipped read and write are
+                               * DRAM bytes) */
+                const int q = q0 + u * T;
+                const int i = ty * TH + q / TW, j = tx * TW + q % TW;
+                const long long c = I.off + (long long)i * I.cols + j;
+                double from_nb = 0.0;
+                long long cn = 0;
+                /* x is neighbour opp(d) of its neighbour d: north<->south,
+                 * west<->east, so neighbour d contributes w of plane 3 - d */
+#pragma unroll
+                for (int d = 0; d < 4; d++)
+                    if ((wet[u] >> d) & 1u) {
+                        nbr(I, i, j, d + 1, &cn);
+                        from_nb += w[(3 - d) * N + cn];
+                    }
+                double gc = 0.0, gzc = 0.0;
+                if (wet[u] & 16u) {
+                    gc = g[c];
+                    gzc = gz[c];
+                }
                 lam[c] = lam[c] + gc + from_nb;
                 lamz[c] += gzc + from_nb;
             }
